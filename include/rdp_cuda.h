@@ -1,0 +1,144 @@
+/*
+ * librdp_cuda -- C ABI of the GB300-native N64 RDP rendering path.
+ *
+ * This is the drop-in boundary for the reference's RDP::CommandProcessor
+ * (parallel-rdp/rdp_device.hpp:111-197).  Every entry point takes plain
+ * pointers and sizes and returns an int status (RDP_OK or an RDP_ERR_* code);
+ * no exception or C++ type crosses it.  Each function names the reference
+ * interface it replaces.
+ *
+ * Threading: a processor is used from one emulator thread at a time.  Command
+ * words are decoded synchronously by the calling thread (the reference's
+ * PARALLEL_RDP_SINGLE_THREADED_COMMAND mode, rdp_device.cpp:144-158); GPU work
+ * is asynchronous and tracked by a monotonically increasing 64-bit timeline.
+ *
+ * RDRAM ownership: the caller owns RDRAM (rdp_device.cpp:81-87).  The
+ * authoritative copy lives in device memory (HBM).  The caller's buffer is
+ * uploaded at creation and by rdp_cp_end_write_rdram(); framebuffer bytes the
+ * GPU writes are copied back into the caller's buffer before the timeline value
+ * that covers them completes (the reference's incoherent path,
+ * rdp_renderer.cpp:2523-2907, at framebuffer granularity).  Hidden RDRAM and
+ * TMEM are owned by the processor (rdp_device.cpp:120-131).
+ */
+#ifndef RDP_CUDA_H
+#define RDP_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+enum
+{
+	RDP_OK = 0,
+	RDP_ERR_UNSUPPORTED = 1, /* no usable CUDA device, or an unsupported request */
+	RDP_ERR_OOM = 2,         /* device or pinned-host allocation failed */
+	RDP_ERR_TIMEOUT = 3,     /* a bounded wait expired */
+	RDP_ERR_INVALID = 4,     /* bad argument */
+	RDP_ERR_DEVICE = 5       /* a CUDA call failed */
+};
+
+/* Validation errors reported through the callback (rdp_renderer.hpp:75-95). */
+enum
+{
+	RDP_VALIDATION_FILL_4BPP = 0,
+	RDP_VALIDATION_FILL_DEPTH_TEST = 1,
+	RDP_VALIDATION_FILL_DEPTH_WRITE = 2,
+	RDP_VALIDATION_FILL_IMAGE_READ = 3,
+	RDP_VALIDATION_COPY_32BPP = 4,
+	RDP_VALIDATION_LOAD_TILE_4BPP = 5,
+	RDP_VALIDATION_MULTILINE_TLUT = 6
+};
+
+typedef struct rdp_cp rdp_cp;
+
+typedef void (*rdp_validation_cb)(void *user, int error, const char *message);
+
+/* Mirrors the CommandProcessor constructor arguments (rdp_device.hpp:113-115). */
+typedef struct rdp_create_info
+{
+	void *rdram;              /* caller-owned RDRAM base (may be NULL: processor allocates a host mirror) */
+	size_t rdram_offset;      /* byte offset of RDRAM inside `rdram` */
+	size_t rdram_size;        /* power of two, e.g. 8 MiB */
+	size_t hidden_rdram_size; /* power of two, normally rdram_size / 2 */
+	uint32_t flags;           /* reserved, must be 0 */
+	int device;               /* CUDA device ordinal */
+} rdp_create_info;
+
+/* CommandProcessor::CommandProcessor (rdp_device.cpp:44-162). */
+int rdp_cp_create(const rdp_create_info *info, rdp_cp **out);
+/* CommandProcessor::~CommandProcessor (rdp_device.cpp:225-233). */
+void rdp_cp_destroy(rdp_cp *cp);
+/* CommandProcessor::device_is_supported (rdp_device.cpp:164-167): 1 when a CUDA device is usable. */
+int rdp_device_is_supported(int device);
+
+/* CommandProcessor::enqueue_command (rdp_device.cpp:874-897).  Accepts any
+ * number of whole or partial commands; a trailing partial command is kept until
+ * the rest of its words arrive. */
+int rdp_cp_enqueue(rdp_cp *cp, uint32_t num_words, const uint32_t *words);
+
+/* CommandProcessor::signal_timeline (rdp_device.cpp:1053-1065). */
+int rdp_cp_signal_timeline(rdp_cp *cp, uint64_t *value);
+/* CommandProcessor::wait_for_timeline (rdp_device.cpp:1067-1080), bounded by timeout_ns. */
+int rdp_cp_wait_timeline(rdp_cp *cp, uint64_t value, uint64_t timeout_ns);
+/* CommandProcessor::flush (rdp_device.cpp:1045-1051). */
+int rdp_cp_flush(rdp_cp *cp);
+/* CommandProcessor::idle (rdp_device.cpp:1039-1043). */
+int rdp_cp_idle(rdp_cp *cp);
+/* CommandProcessor::begin_frame_context (rdp_device.cpp:169-174). */
+int rdp_cp_begin_frame_context(rdp_cp *cp);
+/* CommandProcessor::set_quirks (rdp_device.cpp:961-968): the Quirks word. */
+int rdp_cp_set_quirks(rdp_cp *cp, uint32_t quirks);
+/* CommandProcessor::set_validation_interface (rdp_device.cpp:230-233). */
+int rdp_cp_set_validation_callback(rdp_cp *cp, rdp_validation_cb cb, void *user);
+
+/* CommandProcessor::begin_read_rdram / end_write_rdram / begin_read_hidden_rdram /
+ * end_write_hidden_rdram / get_rdram_size / get_hidden_rdram_size / get_tmem
+ * (rdp_device.cpp:996-1037). */
+void *rdp_cp_begin_read_rdram(rdp_cp *cp);
+int rdp_cp_end_write_rdram(rdp_cp *cp);
+void *rdp_cp_begin_read_hidden_rdram(rdp_cp *cp);
+int rdp_cp_end_write_hidden_rdram(rdp_cp *cp);
+size_t rdp_cp_get_rdram_size(rdp_cp *cp);
+size_t rdp_cp_get_hidden_rdram_size(rdp_cp *cp);
+int rdp_cp_get_tmem(rdp_cp *cp, uint16_t *out_2048_words);
+
+/* CommandProcessor::set_vi_register (rdp_device.cpp:970-975); reg is VIRegister (rdp_common.hpp:286-302). */
+int rdp_cp_set_vi_register(rdp_cp *cp, uint32_t reg, uint32_t value);
+
+/* ScanoutOptions subset (video_interface.hpp:31-81) honoured by rdp_cp_scanout_sync. */
+typedef struct rdp_scanout_options
+{
+	uint32_t persist_frame_on_invalid_input;
+	uint32_t blend_previous_frame;
+	uint32_t upscale_deinterlacing; /* must be 0 */
+	uint32_t crop_overscan_pixels;
+} rdp_scanout_options;
+
+/* CommandProcessor::scanout_sync (rdp_device.cpp:1130-1182): renders the VI
+ * output as RGBA8 into `rgba_out` (capacity in pixels given by *width x *height
+ * on entry is not required: the buffer must hold 640 x 576 pixels), returning
+ * the image size.  A width/height of 0 means no image (blank or invalid VI). */
+int rdp_cp_scanout_sync(rdp_cp *cp, const rdp_scanout_options *opts, uint32_t *rgba_out, uint32_t *width,
+                        uint32_t *height);
+
+/* Counters for benchmarking: primitives drawn, passes submitted, reference-equivalent
+ * render passes (the reference's <=256-primitive segmentation, rdp_renderer.cpp:1564-1590),
+ * fragments processed by the depth/blend, fill and copy pipes. */
+typedef struct rdp_stats
+{
+	uint64_t primitives;
+	uint64_t passes;
+	uint64_t reference_passes;
+	uint64_t fragments;
+	uint64_t tmem_uploads;
+} rdp_stats;
+int rdp_cp_get_stats(rdp_cp *cp, rdp_stats *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

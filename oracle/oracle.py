@@ -1,0 +1,106 @@
+"""ctypes binding of the CPU oracle (oracle/rdp_oracle.cpp) -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg use this
+module, as the checker.  The product library never loads it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_PATH = os.path.join(_HERE, "_build", "liboracle_rdp.so")
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _PATH
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_PATH):
+            build()
+        L = ctypes.CDLL(_PATH)
+        vp, u32 = ctypes.c_void_p, ctypes.c_uint32
+        L.oracle_create.argtypes = [u32, u32]
+        L.oracle_create.restype = vp
+        L.oracle_destroy.argtypes = [vp]
+        for n in ("oracle_write_rdram", "oracle_read_rdram", "oracle_read_hidden", "oracle_write_hidden"):
+            getattr(L, n).argtypes = [vp, vp, u32, u32]
+        L.oracle_read_tmem.argtypes = [vp, vp]
+        L.oracle_enqueue.argtypes = [vp, vp, u32]
+        L.oracle_enqueue.restype = u32
+        L.oracle_fragments.argtypes = [vp]
+        L.oracle_fragments.restype = ctypes.c_uint64
+        L.oracle_primitive_count.argtypes = [vp]
+        L.oracle_primitive_count.restype = u32
+        L.oracle_blender_lut.argtypes = [vp, vp]
+        for n in ("oracle_z_compress", "oracle_z_decompress", "oracle_dz_compress", "oracle_clamp_9bit",
+                  "oracle_clamp_z"):
+            getattr(L, n).argtypes = [ctypes.c_int]
+            getattr(L, n).restype = ctypes.c_int
+        L.oracle_perspective_divide.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+        L.oracle_noise.argtypes = [u32, u32, u32]
+        L.oracle_noise.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def lib():
+    return _load()
+
+
+class Oracle:
+    """Sequential per-pixel RDP oracle with its own RDRAM, hidden RDRAM and TMEM."""
+
+    def __init__(self, rdram_size=8 << 20, hidden_size=None):
+        if hidden_size is None:
+            hidden_size = rdram_size // 2
+        self.L = _load()
+        self.h = self.L.oracle_create(rdram_size, hidden_size)
+        if not self.h:
+            raise ValueError("bad RDRAM sizes")
+        self.rdram_size = rdram_size
+        self.hidden_size = hidden_size
+
+    def close(self):
+        if self.h:
+            self.L.oracle_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def write_rdram(self, data, offset=0):
+        d = np.ascontiguousarray(data, dtype=np.uint8)
+        self.L.oracle_write_rdram(self.h, d.ctypes.data, offset, d.size)
+
+    def rdram(self):
+        out = np.zeros(self.rdram_size, dtype=np.uint8)
+        self.L.oracle_read_rdram(self.h, out.ctypes.data, 0, out.size)
+        return out
+
+    def hidden(self):
+        out = np.zeros(self.hidden_size, dtype=np.uint8)
+        self.L.oracle_read_hidden(self.h, out.ctypes.data, 0, out.size)
+        return out
+
+    def tmem(self):
+        out = np.zeros(2048, dtype=np.uint16)
+        self.L.oracle_read_tmem(self.h, out.ctypes.data)
+        return out
+
+    def enqueue(self, words):
+        w = np.ascontiguousarray(words, dtype=np.uint32)
+        return self.L.oracle_enqueue(self.h, w.ctypes.data, w.size)
+
+    def fragments(self):
+        return self.L.oracle_fragments(self.h)
+
+    def primitive_count(self):
+        return self.L.oracle_primitive_count(self.h)

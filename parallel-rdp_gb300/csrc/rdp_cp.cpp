@@ -1,0 +1,1073 @@
+/*
+ * Host side of the GB300 RDP path: the command processor behind the C ABI
+ * (include/rdp_cuda.h), replacing RDP::CommandProcessor + RDP::Renderer
+ * (parallel-rdp/rdp_device.cpp, parallel-rdp/rdp_renderer.cpp).
+ *
+ * The host performs only the sequential part of command processing:
+ *   - splits the word stream into commands (RDP command lengths),
+ *   - keeps the state registers as raw words (state blocks) -- decoding them is
+ *     done per primitive on the GPU,
+ *   - decodes tile descriptors and plans TMEM uploads (load_tile,
+ *     rdp_renderer.cpp:3099-3486), which depend on the order of loads,
+ *   - segments the stream into passes on framebuffer changes, TMEM loads that
+ *     read pending framebuffer writes (rdp_renderer.cpp:3051-3097), SyncFull and
+ *     capacity limits, and
+ *   - owns RDRAM coherency and the timeline.
+ * One pass is one H2D copy of a packed staging buffer plus four kernel
+ * launches on the processor's stream.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+#include <stdlib.h>
+#include <algorithm>
+#include <chrono>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <utility>
+#include <vector>
+
+#include "../../include/rdp_cuda.h"
+#include "rdp_types.h"
+#include "rdp_kernels.h"
+#include "blender_divider_runs.inc"
+
+namespace {
+
+constexpr uint32_t kMaxWordsPerPass = RDP_MAX_PRIMS_PER_PASS * 44;
+constexpr uint32_t kMaxStateBlocks = RDP_MAX_PRIMS_PER_PASS;
+constexpr uint32_t kMaxTilesets = 4096;
+constexpr uint32_t kMaxTiles = RDP_MAX_TILES_X * RDP_MAX_TILES_Y;
+
+static inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
+
+static uint32_t command_length(uint32_t op)
+{
+	switch (op)
+	{
+	case 0x08: return 8;
+	case 0x09: return 12;
+	case 0x0a: return 24;
+	case 0x0b: return 28;
+	case 0x0c: return 24;
+	case 0x0d: return 28;
+	case 0x0e: return 40;
+	case 0x0f: return 44;
+	case 0x24:
+	case 0x25: return 4;
+	default: return 2;
+	}
+}
+
+static int sext(uint32_t v, int bits) { return int(v << (32 - bits)) >> (32 - bits); }
+
+// Blender divider table: floor(n / d) & 0xff except for the irregular entries stored as runs.
+static void build_blender_lut(uint8_t *lut)
+{
+	for (int d = 0; d < 16; d++)
+		for (int n = 0; n < 2048; n++)
+			lut[(d << 11) | n] = d ? uint8_t((n / d) & 0xff) : 0;
+	for (int i = 0; i < RDP_BLENDER_DIVIDER_NUM_RUNS; i++)
+	{
+		const unsigned short *r = rdp_blender_divider_runs[i];
+		for (int k = 0; k < r[2]; k++) lut[(r[0] << 11) | (r[1] + k)] = uint8_t(r[3]);
+	}
+}
+
+std::mutex g_lut_mutex;
+std::vector<int> g_lut_devices;
+
+static cudaError_t ensure_luts(int device)
+{
+	std::lock_guard<std::mutex> hold(g_lut_mutex);
+	for (int d : g_lut_devices)
+		if (d == device) return cudaSuccess;
+	static uint8_t lut[0x8000];
+	build_blender_lut(lut);
+	cudaError_t e = rdp_kernels_init_luts(lut);
+	if (e == cudaSuccess) g_lut_devices.push_back(device);
+	return e;
+}
+
+} // namespace
+
+struct rdp_cp
+{
+	// ---------------------------------------------------------------- configuration
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	uint8_t *host_rdram = nullptr;
+	bool own_host_rdram = false;
+	bool host_registered = false;
+	uint32_t rdram_size = 0, hidden_size = 0;
+	std::vector<uint8_t> hidden_mirror;
+
+	// ---------------------------------------------------------------- device memory
+	uint8_t *d_rdram = nullptr, *d_hidden = nullptr;
+	uint16_t *d_tmem = nullptr, *d_snapshots = nullptr;
+	uint32_t *d_masks = nullptr;
+	RdpPrimGeom *d_geom = nullptr;
+	RdpPrimAttr *d_attr = nullptr;
+	RdpPrimShade *d_shade = nullptr;
+	uint8_t *d_staging = nullptr;
+	unsigned long long *d_fragments = nullptr;
+	size_t staging_cap = 0;
+
+	struct Staging
+	{
+		uint8_t *h = nullptr;
+		cudaEvent_t done = nullptr;
+		bool in_flight = false;
+	} staging[2];
+	int staging_index = 0;
+
+	// ---------------------------------------------------------------- pass being recorded
+	std::vector<RdpPrimIn> prims;
+	std::vector<uint32_t> words;
+	std::vector<uint32_t> state_blocks;
+	std::vector<RdpTile> tilesets;
+	std::vector<RdpUpload> uploads;
+
+	// ---------------------------------------------------------------- register state
+	uint32_t sb[RDP_STATE_BLOCK_WORDS] = {};
+	bool sb_dirty = true;
+	RdpTile tiles[8] = {};
+	bool tiles_dirty = true;
+	struct { uint32_t addr = 0, width = 0, size = 0, fmt = 0; } tex_image;
+	struct
+	{
+		uint32_t addr = 0, width = 0, fmt = FBF_RGBA5551, depth_addr = 0;
+		uint32_t deduced_height = 0;
+		bool color_pending = false, depth_pending = false;
+	} fb;
+	uint64_t base_prim_index = 0;
+	std::vector<uint32_t> carry;
+
+	// The reference keeps pixel state in registers for a whole render pass; for I8 colour
+	// images and colour/depth aliasing the store/reload round trip is not transparent, so
+	// those passes are cut exactly where the reference cuts them: after 256 primitives
+	// (Limits::MaxPrimitives) and before the 256th TMEM upload (rdp_renderer.cpp:3484-3485).
+	uint32_t rsr_prims = 0, rsr_uploads = 0;
+	bool pass_boundaries_visible() const { return fb.fmt == FBF_I8 || fb.addr == fb.depth_addr; }
+
+	// ---------------------------------------------------------------- coherency + timeline
+	std::vector<std::pair<uint32_t, uint32_t>> dirty_ranges;
+	bool host_rdram_dirty = false;
+	uint64_t timeline_counter = 0;
+	std::deque<std::pair<uint64_t, cudaEvent_t>> pending;
+	std::vector<cudaEvent_t> free_events;
+	uint64_t completed_value = 0;
+
+	// ---------------------------------------------------------------- statistics
+	rdp_stats stats = {};
+	struct
+	{
+		uint32_t prims = 0, uploads = 0, span_jobs = 0;
+		std::vector<uint64_t> static_keys, depth_keys;
+	} ref;
+
+	uint32_t vi_regs[16] = {};
+	rdp_validation_cb validation_cb = nullptr;
+	void *validation_user = nullptr;
+	int sticky_error = RDP_OK;
+
+	// ================================================================= helpers
+	void report(int err, const char *msg)
+	{
+		if (validation_cb) validation_cb(validation_user, err, msg);
+	}
+
+	int check(cudaError_t e)
+	{
+		if (e != cudaSuccess)
+		{
+			sticky_error = RDP_ERR_DEVICE;
+			return RDP_ERR_DEVICE;
+		}
+		return RDP_OK;
+	}
+
+	uint32_t cycle_type() const { return (sb[SB_OTHER_MODES] >> 20) & 3; }
+
+	// Emulation of the reference's pass segmentation for the reference_passes counter
+	// (need_flush rdp_renderer.cpp:1564-1590 and the upload limit at 3484-3485).
+	void ref_pass_break()
+	{
+		stats.reference_passes++;
+		ref.prims = ref.uploads = ref.span_jobs = 0;
+		ref.static_keys.clear();
+		ref.depth_keys.clear();
+	}
+	void ref_note_prim(int lines)
+	{
+		uint64_t skey = (uint64_t(sb[SB_OTHER_MODES]) << 32) ^ (uint64_t(sb[SB_OTHER_MODES + 1] & 0x3f0fu) << 20) ^
+		                uint64_t(sb[SB_COMBINE]) ^ (uint64_t(sb[SB_COMBINE + 1]) << 7);
+		uint64_t dkey = (uint64_t(sb[SB_OTHER_MODES + 1]) << 8) | ((sb[SB_OTHER_MODES] >> 20) & 3);
+		if (std::find(ref.static_keys.begin(), ref.static_keys.end(), skey) == ref.static_keys.end())
+			ref.static_keys.push_back(skey);
+		if (std::find(ref.depth_keys.begin(), ref.depth_keys.end(), dkey) == ref.depth_keys.end())
+			ref.depth_keys.push_back(dkey);
+		ref.prims++;
+		if (lines > 0) ref.span_jobs += uint32_t((lines + 2 + 63) / 64);
+		if (ref.prims >= 256 || ref.static_keys.size() >= 64 || ref.depth_keys.size() >= 64 ||
+		    ref.span_jobs * 64 + 1024 > 32 * 1024)
+			ref_pass_break();
+	}
+
+	// ================================================================= creation
+	int init(const rdp_create_info *info)
+	{
+		device = info->device;
+		rdram_size = uint32_t(info->rdram_size);
+		hidden_size = uint32_t(info->hidden_rdram_size);
+		if (cudaSetDevice(device) != cudaSuccess) return RDP_ERR_UNSUPPORTED;
+		if (ensure_luts(device) != cudaSuccess) return RDP_ERR_DEVICE;
+		if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return RDP_ERR_DEVICE;
+
+		if (info->rdram)
+			host_rdram = static_cast<uint8_t *>(info->rdram) + info->rdram_offset;
+		else
+		{
+			host_rdram = static_cast<uint8_t *>(calloc(1, rdram_size));
+			if (!host_rdram) return RDP_ERR_OOM;
+			own_host_rdram = true;
+		}
+		host_registered = cudaHostRegister(host_rdram, rdram_size, cudaHostRegisterDefault) == cudaSuccess;
+		if (!host_registered) cudaGetLastError();
+		hidden_mirror.assign(hidden_size, 0x03);
+
+		staging_cap = align16(sizeof(RdpPass)) + align16(sizeof(RdpPrimIn) * RDP_MAX_PRIMS_PER_PASS) +
+		              align16(sizeof(uint32_t) * kMaxWordsPerPass) +
+		              align16(sizeof(uint32_t) * RDP_STATE_BLOCK_WORDS * kMaxStateBlocks) +
+		              align16(sizeof(RdpTile) * 8 * kMaxTilesets) +
+		              align16(sizeof(RdpUpload) * RDP_MAX_UPLOADS_PER_PASS) + 64;
+
+		if (cudaMalloc(&d_rdram, rdram_size) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_hidden, hidden_size) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_tmem, 4096) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_snapshots, size_t(RDP_MAX_UPLOADS_PER_PASS + 1) * 4096) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_masks, size_t(kMaxTiles) * RDP_MASK_WORDS_PER_TILE * 4) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_geom, sizeof(RdpPrimGeom) * RDP_MAX_PRIMS_PER_PASS) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_attr, sizeof(RdpPrimAttr) * RDP_MAX_PRIMS_PER_PASS) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_shade, sizeof(RdpPrimShade) * RDP_MAX_PRIMS_PER_PASS) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_staging, staging_cap) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_fragments, sizeof(unsigned long long)) != cudaSuccess) return RDP_ERR_OOM;
+		for (auto &s : staging)
+		{
+			if (cudaMallocHost(&s.h, staging_cap) != cudaSuccess) return RDP_ERR_OOM;
+			if (cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess) return RDP_ERR_DEVICE;
+		}
+		if (check(cudaMemsetAsync(d_masks, 0, size_t(kMaxTiles) * RDP_MASK_WORDS_PER_TILE * 4, stream))) return RDP_ERR_DEVICE;
+		if (check(cudaMemsetAsync(d_hidden, 0x03, hidden_size, stream))) return RDP_ERR_DEVICE;
+		if (check(cudaMemsetAsync(d_tmem, 0, 4096, stream))) return RDP_ERR_DEVICE;
+		if (check(cudaMemsetAsync(d_fragments, 0, sizeof(unsigned long long), stream))) return RDP_ERR_DEVICE;
+		if (check(cudaMemcpyAsync(d_rdram, host_rdram, rdram_size, cudaMemcpyHostToDevice, stream))) return RDP_ERR_DEVICE;
+		if (check(cudaStreamSynchronize(stream))) return RDP_ERR_DEVICE;
+
+		// Default register state matches a freshly constructed CommandProcessor.
+		sb[SB_QUIRKS] = 1; // native_resolution_tex_rect (rdp_device.hpp:79-83)
+		for (auto &t : tiles) t = RdpTile{};
+		prims.reserve(RDP_MAX_PRIMS_PER_PASS);
+		words.reserve(1 << 16);
+		return RDP_OK;
+	}
+
+	void destroy()
+	{
+		if (stream)
+		{
+			cudaSetDevice(device);
+			cudaStreamSynchronize(stream);
+		}
+		for (auto &p : pending) cudaEventDestroy(p.second);
+		for (auto e : free_events) cudaEventDestroy(e);
+		for (auto &s : staging)
+		{
+			if (s.h) cudaFreeHost(s.h);
+			if (s.done) cudaEventDestroy(s.done);
+		}
+		cudaFree(d_rdram);
+		cudaFree(d_hidden);
+		cudaFree(d_tmem);
+		cudaFree(d_snapshots);
+		cudaFree(d_masks);
+		cudaFree(d_geom);
+		cudaFree(d_attr);
+		cudaFree(d_shade);
+		cudaFree(d_staging);
+		cudaFree(d_fragments);
+		if (host_registered) cudaHostUnregister(host_rdram);
+		if (own_host_rdram) free(host_rdram);
+		if (stream) cudaStreamDestroy(stream);
+	}
+
+	// ================================================================= pass submission
+	uint32_t fb_bytes_per_pixel() const
+	{
+		switch (fb.fmt)
+		{
+		case FBF_I4:
+		case FBF_I8: return 1;
+		case FBF_RGBA8888: return 4;
+		default: return 2;
+		}
+	}
+
+	void add_dirty(uint32_t addr, uint32_t bytes)
+	{
+		if (!bytes) return;
+		addr &= rdram_size - 1;
+		uint32_t end = std::min<uint64_t>(uint64_t(addr) + bytes, rdram_size);
+		for (auto &r : dirty_ranges)
+		{
+			if (addr <= r.second && end >= r.first)
+			{
+				r.first = std::min(r.first, addr);
+				r.second = std::max(r.second, end);
+				return;
+			}
+		}
+		dirty_ranges.emplace_back(addr, end);
+	}
+
+	int flush()
+	{
+		if (prims.empty() && uploads.empty())
+		{
+			reset_pass();
+			return sticky_error;
+		}
+		if (host_rdram_dirty)
+		{
+			if (check(cudaMemcpyAsync(d_rdram, host_rdram, rdram_size, cudaMemcpyHostToDevice, stream))) return sticky_error;
+			host_rdram_dirty = false;
+		}
+
+		Staging &st = staging[staging_index];
+		staging_index ^= 1;
+		if (st.in_flight)
+		{
+			if (check(cudaEventSynchronize(st.done))) return sticky_error;
+			st.in_flight = false;
+		}
+
+		bool render = fb.width != 0 && fb.deduced_height != 0 && !prims.empty();
+		RdpPass pass = {};
+		pass.rdram = d_rdram;
+		pass.hidden = d_hidden;
+		pass.masks = d_masks;
+		pass.coarse = nullptr;
+		pass.tmem_snapshots = uploads.empty() ? d_tmem : d_snapshots;
+		pass.tmem_state = d_tmem;
+		pass.rdram_size = rdram_size;
+		pass.hidden_size = hidden_size;
+		pass.fb_addr = fb.addr;
+		pass.depth_addr = fb.depth_addr;
+		pass.fb_width = fb.width;
+		pass.fb_height = std::min<uint32_t>(fb.deduced_height, RDP_MAX_TILES_Y * 8);
+		pass.fb_fmt = fb.fmt;
+		pass.tiles_x = render ? (fb.width + 7) / 8 : 0;
+		pass.tiles_y = render ? (pass.fb_height + 7) / 8 : 0;
+		pass.prim_begin = 0;
+		pass.prim_count = uint32_t(prims.size());
+		pass.upload_begin = 0;
+		pass.upload_count = uint32_t(uploads.size());
+		pass.tile_item_begin = 0;
+		pass.instance = 0;
+		pass.base_prim_index = uint32_t(base_prim_index);
+
+		// Pack the staging buffer: pass | prims | words | state blocks | tilesets | uploads | tmem pass list.
+		uint8_t *h = st.h;
+		size_t off = 0;
+		auto put = [&](const void *src, size_t bytes) -> size_t {
+			size_t at = off;
+			if (bytes) memcpy(h + off, src, bytes);
+			off = align16(off + bytes);
+			return at;
+		};
+		size_t o_pass = put(&pass, sizeof(pass));
+		size_t o_prims = put(prims.data(), prims.size() * sizeof(RdpPrimIn));
+		size_t o_words = put(words.data(), words.size() * 4);
+		size_t o_sb = put(state_blocks.data(), state_blocks.size() * 4);
+		size_t o_ts = put(tilesets.data(), tilesets.size() * sizeof(RdpTile));
+		size_t o_up = put(uploads.data(), uploads.size() * sizeof(RdpUpload));
+		uint32_t zero = 0;
+		size_t o_list = put(&zero, 4);
+		if (check(cudaMemcpyAsync(d_staging, h, off, cudaMemcpyHostToDevice, stream))) return sticky_error;
+		if (check(cudaEventRecord(st.done, stream))) return sticky_error;
+		st.in_flight = true;
+
+		RdpLaunch L = {};
+		L.prims_in = reinterpret_cast<const RdpPrimIn *>(d_staging + o_prims);
+		L.num_prims = render ? uint32_t(prims.size()) : 0;
+		L.words = reinterpret_cast<const uint32_t *>(d_staging + o_words);
+		L.state_blocks = reinterpret_cast<const uint32_t *>(d_staging + o_sb);
+		L.passes = reinterpret_cast<const RdpPass *>(d_staging + o_pass);
+		L.num_passes = 1;
+		L.geom = d_geom;
+		L.attr = d_attr;
+		L.shade = d_shade;
+		L.tilesets = reinterpret_cast<const RdpTile *>(d_staging + o_ts);
+		L.tmem_pass_list = reinterpret_cast<const uint32_t *>(d_staging + o_list);
+		L.num_tmem_passes = uploads.empty() ? 0 : 1;
+		L.uploads = reinterpret_cast<const RdpUpload *>(d_staging + o_up);
+		L.num_tile_items = pass.tiles_x * pass.tiles_y;
+		L.fragments = d_fragments;
+		if (check(rdp_kernels_launch(&L, stream))) return sticky_error;
+
+		if (render)
+		{
+			add_dirty(fb.addr, fb.width * fb.deduced_height * fb_bytes_per_pixel());
+			if (fb.depth_pending) add_dirty(fb.depth_addr, fb.width * fb.deduced_height * 2);
+		}
+		stats.passes++;
+		stats.primitives += prims.size();
+		stats.tmem_uploads += uploads.size();
+		base_prim_index += prims.size();
+		reset_pass();
+		return sticky_error;
+	}
+
+	void reset_pass()
+	{
+		prims.clear();
+		words.clear();
+		state_blocks.clear();
+		tilesets.clear();
+		uploads.clear();
+		sb_dirty = true;
+		tiles_dirty = true;
+		fb.deduced_height = 0;
+		fb.color_pending = false;
+		fb.depth_pending = false;
+		rsr_prims = rsr_uploads = 0;
+	}
+
+	// A flush the reference would also perform (framebuffer change, hazard, SyncFull).
+	int hard_flush()
+	{
+		if (ref.prims || ref.uploads) ref_pass_break();
+		return flush();
+	}
+
+	// ================================================================= primitives
+	void record_prim(const uint32_t *w, uint32_t len, uint32_t op)
+	{
+		if (prims.size() >= RDP_MAX_PRIMS_PER_PASS || words.size() + len > kMaxWordsPerPass ||
+		    (sb_dirty && state_blocks.size() / RDP_STATE_BLOCK_WORDS >= kMaxStateBlocks) ||
+		    (tiles_dirty && tilesets.size() / 8 >= kMaxTilesets))
+			flush();
+
+		if (sb_dirty)
+		{
+			state_blocks.insert(state_blocks.end(), sb, sb + RDP_STATE_BLOCK_WORDS);
+			sb_dirty = false;
+		}
+		if (tiles_dirty)
+		{
+			tilesets.insert(tilesets.end(), tiles, tiles + 8);
+			tiles_dirty = false;
+		}
+		RdpPrimIn pi;
+		pi.word_offset = uint32_t(words.size());
+		pi.state_block = uint32_t(state_blocks.size() / RDP_STATE_BLOCK_WORDS - 1);
+		pi.tileset = uint32_t(tilesets.size() / 8 - 1);
+		pi.tmem_index = uint16_t(uploads.size());
+		pi.pass = 0;
+		prims.push_back(pi);
+		words.insert(words.end(), w, w + len);
+
+		// Deduced framebuffer height (rdp_renderer.cpp:1556-1562).
+		int yl, yh;
+		bool fill_copy = cycle_type() >= 2;
+		if (op >= 0x08 && op <= 0x0f)
+		{
+			yl = sext(w[0], 14);
+			yh = sext(w[1], 14);
+		}
+		else
+		{
+			yl = int(w[0] & 0xfff);
+			if (fill_copy) yl |= 3;
+			yh = int(w[1] & 0xfff);
+		}
+		int scissor_ylo = int(sb[SB_SCISSOR] & 0xfff), scissor_yhi = int(sb[SB_SCISSOR + 1] & 0xfff);
+		int max_sub = std::min(yl - 1, scissor_yhi - 1);
+		int h = std::max((max_sub >> 2) + 1, 0);
+		fb.deduced_height = std::max<uint32_t>(fb.deduced_height, uint32_t(h));
+		fb.color_pending = true;
+		if (sb[SB_OTHER_MODES + 1] & (1u << 5)) fb.depth_pending = true;
+		int min_line = std::max(yh, scissor_ylo) >> 2;
+		ref_note_prim((max_sub >> 2) - min_line + 1);
+		bool cut = ++rsr_prims >= 256 && pass_boundaries_visible();
+
+		if (validation_cb)
+		{
+			uint32_t om1 = sb[SB_OTHER_MODES + 1];
+			bool prim_depth = (om1 & (1u << 2)) != 0;
+			if (cycle_type() == 3)
+			{
+				if (fb.fmt == FBF_I4) report(RDP_VALIDATION_FILL_4BPP, "Attempted to use Fill mode on 4bpp surface.");
+				if (om1 & (1u << 4)) report(RDP_VALIDATION_FILL_DEPTH_TEST, "Attempted to use Fill mode with depth test.");
+				if (om1 & (1u << 6)) report(RDP_VALIDATION_FILL_IMAGE_READ, "Attempted to use Fill mode with image read enable.");
+				if ((om1 & (1u << 5)) && !prim_depth)
+					report(RDP_VALIDATION_FILL_DEPTH_WRITE, "Attempted to use Fill mode with depth write enabled.");
+			}
+			else if (cycle_type() == 2 && fb.fmt == FBF_RGBA8888)
+				report(RDP_VALIDATION_COPY_32BPP, "Attempted to use Copy mode on 32bpp surface.");
+		}
+		if (cut) flush();
+	}
+
+	// ================================================================= TMEM loads (rdp_renderer.cpp:3051-3486)
+	bool upload_needs_flush(uint32_t addr) const
+	{
+		if (fb.color_pending)
+		{
+			uint32_t offset = (addr - fb.addr) & (rdram_size - 1);
+			uint32_t pixels = fb.deduced_height * fb.width;
+			if (fb.fmt == FBF_RGBA5551 || fb.fmt == FBF_I8) offset >>= 1;
+			else if (fb.fmt == FBF_RGBA8888) offset >>= 2;
+			if (offset < pixels) return true;
+		}
+		if (fb.depth_pending)
+		{
+			uint32_t offset = ((addr - fb.depth_addr) & (rdram_size - 1)) >> 1;
+			if (offset < fb.deduced_height * fb.width) return true;
+		}
+		return false;
+	}
+
+	void load_tile(uint32_t tile, uint32_t slo, uint32_t tlo, uint32_t shi, uint32_t thi, int mode)
+	{
+		if (mode == 1 && (thi >> 2) > (tlo >> 2))
+			report(RDP_VALIDATION_MULTILINE_TLUT, "Attempting to load multiple lines in TLUT.");
+		if (upload_needs_flush(tex_image.addr)) hard_flush();
+		if (mode != 2)
+		{
+			if ((thi >> 2) < (tlo >> 2)) return;
+			if (!((((shi >> 2) - (slo >> 2)) + 1) & 0xfff)) return;
+		}
+		else
+		{
+			unsigned pc = ((shi - slo) + 1) & 0xfff;
+			if (!pc || pc > 2048) return;
+		}
+		if (mode == 0)
+		{
+			const RdpTile &meta = tiles[tile];
+			unsigned ppl = (((shi >> 2) - (slo >> 2)) + 1) & 0xfff;
+			unsigned qw = ((ppl << meta.size) + 15) >> 4;
+			if (meta.size > tex_image.size) qw <<= meta.size - tex_image.size;
+			else if (meta.size < tex_image.size) qw >>= tex_image.size - meta.size;
+			unsigned bpl = std::max<unsigned>(qw * 8, meta.stride);
+			unsigned max_bpl = meta.fmt == 1 ? 0x800 : 0x1000;
+			unsigned lines = ((thi >> 2) - (tlo >> 2)) + 1;
+			if (bpl * lines > max_bpl)
+			{
+				unsigned per = (max_bpl / bpl) & ~1u;
+				if (per == 0) return;
+				for (unsigned line = 0; line < lines; line += per)
+				{
+					unsigned n = std::min(lines - line, per);
+					uint32_t t_lo = tlo + (line << 2);
+					load_tile_iteration(tile, slo, t_lo, shi, t_lo + ((n - 1) << 2), mode, line * meta.stride);
+				}
+				tiles[tile].slo = slo;
+				tiles[tile].shi = shi;
+				tiles[tile].tlo = tlo;
+				tiles[tile].thi = thi;
+				tiles_dirty = true;
+				return;
+			}
+		}
+		load_tile_iteration(tile, slo, tlo, shi, thi, mode, 0);
+	}
+
+	void load_tile_iteration(uint32_t tile, uint32_t slo, uint32_t tlo, uint32_t shi, uint32_t thi, int mode,
+	                         uint32_t tmem_offset)
+	{
+		RdpTile &meta = tiles[tile];
+		meta.slo = slo;
+		meta.shi = shi;
+		meta.tlo = tlo;
+		meta.thi = thi;
+		tiles_dirty = true;
+		uint32_t isize = tex_image.size;
+		if (meta.fmt == 1 && (meta.size != 2 || isize != 2)) return;
+		if (isize == 0)
+		{
+			report(RDP_VALIDATION_LOAD_TILE_4BPP, "4-bit VRAM pointer crashes the RDP.");
+			return;
+		}
+		if (meta.size == 3 && meta.fmt != 0) return;
+		if (mode == 1 && meta.size == 3) return;
+		if (mode != 1)
+		{
+			if (isize == 3 && meta.size == 1) return;
+			if (isize == 2 && meta.size == 0) return;
+			if (isize == 3 && meta.size == 0) return;
+		}
+		RdpUpload up = {};
+		up.tmem_stride_words = int(meta.stride >> 1);
+		uint32_t ux = 0, uy = 0;
+		int upload_mode = mode;
+		if (upload_mode == 2)
+		{
+			ux = slo;
+			uy = tlo;
+			unsigned pixel_count = (shi - slo + 1) & 0xfff;
+			unsigned dt = thi;
+			unsigned max_iter = (pixel_count - 1) >> (4u - isize);
+			unsigned max_t = (max_iter * dt) >> 11;
+			if (max_t != 0)
+			{
+				unsigned maxn = ((1u << 11u) + dt - 1u) / dt;
+				unsigned minn = (1u << 11u) / dt;
+				bool uneven = maxn != minn;
+				if (uneven)
+				{
+					unsigned ov = (dt * maxn - (1u << 11)) * max_t;
+					if (ov < dt)
+					{
+						minn = maxn;
+						uneven = false;
+					}
+				}
+				up.dxt = int(dt << 5);
+				if (meta.size == 3 || meta.fmt == 1)
+				{
+					up.tmem_stride_words <<= 1;
+					if (uneven && meta.size != isize) return;
+				}
+				if (meta.size > isize)
+				{
+					unsigned sh = meta.size - isize;
+					maxn <<= sh;
+					minn <<= sh;
+					up.dxt >>= sh;
+				}
+				else if (isize > meta.size)
+					return;
+				unsigned max_ls = maxn + (unsigned(up.tmem_stride_words) >> 2);
+				unsigned min_ls = minn + (unsigned(up.tmem_stride_words) >> 2);
+				up.min_t_mod = 1.0f / float(max_ls);
+				up.max_t_mod = 1.0f / float(min_ls);
+				up.width = int(pixel_count);
+				up.height = 1;
+				up.tmem_stride_words >>= 2;
+			}
+			else
+			{
+				up.width = int(pixel_count);
+				up.height = 1;
+				up.tmem_stride_words = 0;
+				upload_mode = 0;
+			}
+		}
+		else
+		{
+			ux = slo >> 2;
+			uy = tlo >> 2;
+			up.width = int((((shi >> 2) - (slo >> 2)) + 1) & 0xfff);
+			up.height = int(((thi >> 2) - (tlo >> 2)) + 1);
+		}
+		if (!up.width) return;
+		if (isize == 1) up.vram_effective_width = (up.width + 7) & ~7;
+		else if (isize == 2) up.vram_effective_width = upload_mode == 1 ? up.width : ((up.width + 3) & ~3);
+		else if (isize == 3) up.vram_effective_width = (up.width + 1) & ~1;
+		switch (meta.size)
+		{
+		case 0: up.width = ((up.width + 15) & ~15) >> 2; break;
+		case 1: up.width = ((up.width + 7) & ~7) >> 1; break;
+		case 2:
+			up.width = (up.width + 3) & ~3;
+			if (meta.fmt == 1) up.width >>= 1;
+			break;
+		default: up.width = (up.width + 1) & ~1; break;
+		}
+		if (up.height > 1 && upload_mode == 1) return;
+		up.vram_addr = int(tex_image.addr + ((tex_image.width * uy + ux) << (isize - 1)));
+		up.vram_width = upload_mode == 2 ? up.vram_effective_width : int(tex_image.width);
+		up.vram_size = int(isize);
+		up.tmem_offset = int((meta.offset + tmem_offset) & 0xfff);
+		up.tmem_size = meta.size;
+		up.tmem_fmt = meta.fmt;
+		up.mode = upload_mode;
+		up.inv_tmem_stride_words = 1.0f / float(up.tmem_stride_words);
+		uploads.push_back(up);
+		ref.uploads++;
+		if (ref.uploads + 1 >= 256) ref_pass_break();
+		if (uploads.size() + 1 >= RDP_MAX_UPLOADS_PER_PASS || (++rsr_uploads + 1 >= 256 && pass_boundaries_visible()))
+			flush();
+	}
+
+	// ================================================================= command dispatch
+	void set_tile(const uint32_t *w)
+	{
+		RdpTile &t = tiles[(w[1] >> 24) & 7];
+		t.offset = ((w[0] >> 0) & 511) << 3;
+		t.stride = ((w[0] >> 9) & 511) << 3;
+		t.size = uint8_t((w[0] >> 19) & 3);
+		t.fmt = uint8_t((w[0] >> 21) & 7);
+		t.palette = uint8_t((w[1] >> 20) & 15);
+		t.shift_s = uint8_t((w[1] >> 0) & 15);
+		t.mask_s = uint8_t((w[1] >> 4) & 15);
+		t.shift_t = uint8_t((w[1] >> 10) & 15);
+		t.mask_t = uint8_t((w[1] >> 14) & 15);
+		t.flags = 0;
+		if (w[1] & (1u << 8)) t.flags |= TIF_MIRROR_S;
+		if (w[1] & (1u << 9)) t.flags |= TIF_CLAMP_S;
+		if (w[1] & (1u << 18)) t.flags |= TIF_MIRROR_T;
+		if (w[1] & (1u << 19)) t.flags |= TIF_CLAMP_T;
+		if (t.mask_s > 10) t.mask_s = 10;
+		else if (t.mask_s == 0) t.flags |= TIF_CLAMP_S;
+		if (t.mask_t > 10) t.mask_t = 10;
+		else if (t.mask_t == 0) t.flags |= TIF_CLAMP_T;
+		tiles_dirty = true;
+	}
+
+	void set_state(int index, const uint32_t *w)
+	{
+		if (sb[index] != w[0] || sb[index + 1] != w[1])
+		{
+			sb[index] = w[0];
+			sb[index + 1] = w[1];
+			sb_dirty = true;
+		}
+	}
+
+	void command(const uint32_t *w)
+	{
+		uint32_t op = (w[0] >> 24) & 63;
+		switch (op)
+		{
+		case 0x04: // MetaSetQuirks (rdp_device.cpp:948-952)
+			if (sb[SB_QUIRKS] != w[1]) { sb[SB_QUIRKS] = w[1]; sb_dirty = true; }
+			break;
+		case 0x08: case 0x09: case 0x0a: case 0x0b: case 0x0c: case 0x0d: case 0x0e: case 0x0f:
+		case 0x24: case 0x25: case 0x36:
+			record_prim(w, command_length(op), op);
+			break;
+		case 0x29: hard_flush(); break;
+		case 0x2a: set_state(SB_KEY_GB, w); break;
+		case 0x2b: set_state(SB_KEY_R, w); break;
+		case 0x2c: set_state(SB_CONVERT, w); break;
+		case 0x2d: set_state(SB_SCISSOR, w); break;
+		case 0x2e: set_state(SB_PRIM_DEPTH, w); break;
+		case 0x2f: set_state(SB_OTHER_MODES, w); break;
+		case 0x30: load_tile((w[1] >> 24) & 7, (w[0] >> 12) & 0xfff, w[0] & 0xfff, (w[1] >> 12) & 0xfff, w[1] & 0xfff, 1); break;
+		case 0x32:
+		{
+			RdpTile &t = tiles[(w[1] >> 24) & 7];
+			t.slo = (w[0] >> 12) & 0xfff;
+			t.shi = (w[1] >> 12) & 0xfff;
+			t.tlo = w[0] & 0xfff;
+			t.thi = w[1] & 0xfff;
+			tiles_dirty = true;
+			break;
+		}
+		case 0x33: load_tile((w[1] >> 24) & 7, (w[0] >> 12) & 0xfff, w[0] & 0xfff, (w[1] >> 12) & 0xfff, w[1] & 0xfff, 2); break;
+		case 0x34: load_tile((w[1] >> 24) & 7, (w[0] >> 12) & 0xfff, w[0] & 0xfff, (w[1] >> 12) & 0xfff, w[1] & 0xfff, 0); break;
+		case 0x35: set_tile(w); break;
+		case 0x37: set_state(SB_FILL_COLOR, w); break;
+		case 0x38: set_state(SB_FOG_COLOR, w); break;
+		case 0x39: set_state(SB_BLEND_COLOR, w); break;
+		case 0x3a: set_state(SB_PRIM_COLOR, w); break;
+		case 0x3b: set_state(SB_ENV_COLOR, w); break;
+		case 0x3c: set_state(SB_COMBINE, w); break;
+		case 0x3d:
+			tex_image.fmt = (w[0] >> 21) & 7;
+			tex_image.size = (w[0] >> 19) & 3;
+			tex_image.width = (w[0] & 0x3ff) + 1;
+			tex_image.addr = w[1] & 0xffffff;
+			break;
+		case 0x3e:
+		{
+			uint32_t a = w[1] & 0xffffff;
+			if (a != fb.depth_addr) hard_flush();
+			fb.depth_addr = a;
+			break;
+		}
+		case 0x3f:
+		{
+			uint32_t f = (w[0] >> 21) & 7, size = (w[0] >> 19) & 3;
+			uint32_t width = (w[0] & 1023) + 1, addr = w[1] & 0xffffff;
+			uint32_t fmt = size == 0 ? FBF_I4 : size == 1 ? FBF_I8 : size == 2 ? (f ? FBF_IA88 : FBF_RGBA5551) : FBF_RGBA8888;
+			if (addr != fb.addr || width != fb.width || fmt != fb.fmt) hard_flush();
+			fb.addr = addr;
+			fb.width = width;
+			fb.fmt = fmt;
+			break;
+		}
+		default:
+			break;
+		}
+	}
+
+	int enqueue(uint32_t n, const uint32_t *w)
+	{
+		uint32_t i = 0;
+		if (!carry.empty())
+		{
+			uint32_t need = command_length((carry[0] >> 24) & 63);
+			while (carry.size() < need && i < n) carry.push_back(w[i++]);
+			if (carry.size() < need) return sticky_error;
+			command(carry.data());
+			carry.clear();
+		}
+		while (i < n)
+		{
+			uint32_t len = command_length((w[i] >> 24) & 63);
+			if (i + len > n)
+			{
+				carry.assign(w + i, w + n);
+				break;
+			}
+			command(w + i);
+			i += len;
+		}
+		return sticky_error;
+	}
+
+	// ================================================================= timeline + coherency
+	cudaEvent_t get_event()
+	{
+		if (!free_events.empty())
+		{
+			cudaEvent_t e = free_events.back();
+			free_events.pop_back();
+			return e;
+		}
+		cudaEvent_t e = nullptr;
+		cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+		return e;
+	}
+
+	int copy_back()
+	{
+		for (auto &r : dirty_ranges)
+		{
+			if (host_registered)
+			{
+				if (check(cudaMemcpyAsync(host_rdram + r.first, d_rdram + r.first, r.second - r.first,
+				                          cudaMemcpyDeviceToHost, stream)))
+					return sticky_error;
+			}
+			else
+			{
+				if (check(cudaStreamSynchronize(stream))) return sticky_error;
+				if (check(cudaMemcpy(host_rdram + r.first, d_rdram + r.first, r.second - r.first,
+				                     cudaMemcpyDeviceToHost)))
+					return sticky_error;
+			}
+		}
+		dirty_ranges.clear();
+		return sticky_error;
+	}
+
+	int signal_timeline(uint64_t *value)
+	{
+		if (hard_flush() != RDP_OK) return sticky_error;
+		if (copy_back() != RDP_OK) return sticky_error;
+		cudaEvent_t e = get_event();
+		if (!e) return RDP_ERR_DEVICE;
+		if (check(cudaEventRecord(e, stream))) return sticky_error;
+		uint64_t v = ++timeline_counter;
+		pending.emplace_back(v, e);
+		if (value) *value = v;
+		return RDP_OK;
+	}
+
+	int wait_timeline(uint64_t value, uint64_t timeout_ns)
+	{
+		auto deadline = std::chrono::steady_clock::now() + std::chrono::nanoseconds(timeout_ns);
+		while (!pending.empty() && pending.front().first <= value)
+		{
+			cudaEvent_t e = pending.front().second;
+			for (;;)
+			{
+				cudaError_t q = cudaEventQuery(e);
+				if (q == cudaSuccess) break;
+				if (q != cudaErrorNotReady) return check(q);
+				if (std::chrono::steady_clock::now() >= deadline) return RDP_ERR_TIMEOUT;
+				std::this_thread::yield();
+			}
+			completed_value = pending.front().first;
+			free_events.push_back(e);
+			pending.pop_front();
+		}
+		if (value > timeline_counter) return RDP_ERR_INVALID;
+		return sticky_error;
+	}
+
+	int idle()
+	{
+		uint64_t v = 0;
+		int r = signal_timeline(&v);
+		if (r != RDP_OK) return r;
+		return wait_timeline(v, UINT64_MAX / 2);
+	}
+};
+
+// ============================================================================ C ABI
+extern "C" {
+
+int rdp_device_is_supported(int device)
+{
+	int n = 0;
+	if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+	return device >= 0 && device < n ? 1 : 0;
+}
+
+int rdp_cp_create(const rdp_create_info *info, rdp_cp **out)
+{
+	if (!info || !out) return RDP_ERR_INVALID;
+	*out = nullptr;
+	size_t rs = info->rdram_size, hs = info->hidden_rdram_size;
+	if (!rs || (rs & (rs - 1)) || !hs || (hs & (hs - 1)) || rs > (64u << 20) || info->flags != 0)
+		return RDP_ERR_INVALID;
+	if (!rdp_device_is_supported(info->device)) return RDP_ERR_UNSUPPORTED;
+	rdp_cp *cp = new (std::nothrow) rdp_cp();
+	if (!cp) return RDP_ERR_OOM;
+	int r = cp->init(info);
+	if (r != RDP_OK)
+	{
+		cp->destroy();
+		delete cp;
+		return r;
+	}
+	*out = cp;
+	return RDP_OK;
+}
+
+void rdp_cp_destroy(rdp_cp *cp)
+{
+	if (!cp) return;
+	cp->destroy();
+	delete cp;
+}
+
+int rdp_cp_enqueue(rdp_cp *cp, uint32_t num_words, const uint32_t *words)
+{
+	if (!cp || (num_words && !words)) return RDP_ERR_INVALID;
+	cudaSetDevice(cp->device);
+	return cp->enqueue(num_words, words);
+}
+
+int rdp_cp_signal_timeline(rdp_cp *cp, uint64_t *value)
+{
+	if (!cp) return RDP_ERR_INVALID;
+	cudaSetDevice(cp->device);
+	return cp->signal_timeline(value);
+}
+
+int rdp_cp_wait_timeline(rdp_cp *cp, uint64_t value, uint64_t timeout_ns)
+{
+	if (!cp) return RDP_ERR_INVALID;
+	cudaSetDevice(cp->device);
+	return cp->wait_timeline(value, timeout_ns);
+}
+
+int rdp_cp_flush(rdp_cp *cp)
+{
+	if (!cp) return RDP_ERR_INVALID;
+	cudaSetDevice(cp->device);
+	return cp->hard_flush();
+}
+
+int rdp_cp_idle(rdp_cp *cp)
+{
+	if (!cp) return RDP_ERR_INVALID;
+	cudaSetDevice(cp->device);
+	return cp->idle();
+}
+
+int rdp_cp_begin_frame_context(rdp_cp *cp)
+{
+	if (!cp) return RDP_ERR_INVALID;
+	cudaSetDevice(cp->device);
+	return cp->hard_flush();
+}
+
+int rdp_cp_set_quirks(rdp_cp *cp, uint32_t quirks)
+{
+	if (!cp) return RDP_ERR_INVALID;
+	const uint32_t w[2] = { 0x04u << 24, quirks };
+	return cp->enqueue(2, w);
+}
+
+int rdp_cp_set_validation_callback(rdp_cp *cp, rdp_validation_cb cb, void *user)
+{
+	if (!cp) return RDP_ERR_INVALID;
+	cp->validation_cb = cb;
+	cp->validation_user = user;
+	return RDP_OK;
+}
+
+void *rdp_cp_begin_read_rdram(rdp_cp *cp)
+{
+	if (!cp) return nullptr;
+	cudaSetDevice(cp->device);
+	if (cp->idle() != RDP_OK) return nullptr;
+	return cp->host_rdram;
+}
+
+int rdp_cp_end_write_rdram(rdp_cp *cp)
+{
+	if (!cp) return RDP_ERR_INVALID;
+	cp->host_rdram_dirty = true;
+	return RDP_OK;
+}
+
+void *rdp_cp_begin_read_hidden_rdram(rdp_cp *cp)
+{
+	if (!cp) return nullptr;
+	cudaSetDevice(cp->device);
+	if (cp->idle() != RDP_OK) return nullptr;
+	if (cudaMemcpy(cp->hidden_mirror.data(), cp->d_hidden, cp->hidden_size, cudaMemcpyDeviceToHost) != cudaSuccess)
+		return nullptr;
+	return cp->hidden_mirror.data();
+}
+
+int rdp_cp_end_write_hidden_rdram(rdp_cp *cp)
+{
+	if (!cp) return RDP_ERR_INVALID;
+	cudaSetDevice(cp->device);
+	if (cp->idle() != RDP_OK) return cp->sticky_error;
+	return cp->check(cudaMemcpy(cp->d_hidden, cp->hidden_mirror.data(), cp->hidden_size, cudaMemcpyHostToDevice));
+}
+
+size_t rdp_cp_get_rdram_size(rdp_cp *cp) { return cp ? cp->rdram_size : 0; }
+size_t rdp_cp_get_hidden_rdram_size(rdp_cp *cp) { return cp ? cp->hidden_size : 0; }
+
+int rdp_cp_get_tmem(rdp_cp *cp, uint16_t *out)
+{
+	if (!cp || !out) return RDP_ERR_INVALID;
+	cudaSetDevice(cp->device);
+	int r = cp->idle();
+	if (r != RDP_OK) return r;
+	return cp->check(cudaMemcpy(out, cp->d_tmem, 4096, cudaMemcpyDeviceToHost));
+}
+
+int rdp_cp_set_vi_register(rdp_cp *cp, uint32_t reg, uint32_t value)
+{
+	if (!cp || reg >= 14) return RDP_ERR_INVALID;
+	cp->vi_regs[reg] = value;
+	return RDP_OK;
+}
+
+int rdp_cp_get_stats(rdp_cp *cp, rdp_stats *out)
+{
+	if (!cp || !out) return RDP_ERR_INVALID;
+	cudaSetDevice(cp->device);
+	*out = cp->stats;
+	unsigned long long frags = 0;
+	if (cudaMemcpy(&frags, cp->d_fragments, sizeof(frags), cudaMemcpyDeviceToHost) != cudaSuccess) return RDP_ERR_DEVICE;
+	out->fragments = frags;
+	out->reference_passes = cp->stats.reference_passes + ((cp->ref.prims || cp->ref.uploads) ? 1 : 0);
+	return RDP_OK;
+}
+
+} // extern "C"

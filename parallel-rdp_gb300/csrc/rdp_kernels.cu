@@ -1,0 +1,2455 @@
+/*
+ * GB300 (sm_103a) kernels for the N64 RDP rendering path.
+ *
+ *   k_prim_setup : one thread per primitive.  Decodes the RDP command words and
+ *                  the raw state-register block into edge coefficients,
+ *                  attributes, derived combiner constants and normalised static
+ *                  state (rdp_device.cpp:268-864, rdp_renderer.cpp:717-1562).
+ *   k_bin        : one warp per primitive.  Conservative 8x8-tile binning
+ *                  (shaders/binning.h) into per-tile primitive bitmasks; the
+ *                  bitmask order is primitive order.
+ *   k_tmem       : one CTA per pass with TMEM uploads.  Gathers each 16-bit TMEM
+ *                  word per upload (shaders/tmem_update.comp) and writes one TMEM
+ *                  snapshot per upload.
+ *   k_raster     : one warp per 8x8 tile.  Loads the tile's colour/depth from
+ *                  RDRAM once, walks the binned primitives in order -- span set-up
+ *                  for the tile's rows computed cooperatively into shared memory
+ *                  (shaders/span_setup.comp), per-pixel shading (shaders/shading.h)
+ *                  and depth/blend (shaders/memory_interfacing.h) in registers --
+ *                  and writes back only what was written.
+ *
+ * All arithmetic is the RDP's integer fixed point; wrap-around is explicit
+ * (unsigned multiplies/shifts) so that it matches 32-bit GLSL semantics.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "rdp_types.h"
+#include "rdp_kernels.h"
+
+namespace rdp {
+
+// ============================================================================ small helpers
+__device__ __forceinline__ int mulw(int a, int b) { return int(unsigned(a) * unsigned(b)); }
+__device__ __forceinline__ int shlw(int a, int s) { return int(unsigned(a) << s); }
+__device__ __forceinline__ int bfe_s(int v, int bits) { return int(unsigned(v) << (32 - bits)) >> (32 - bits); }
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return min(max(v, lo), hi); }
+__device__ __forceinline__ int find_msb(int v)
+{
+	if (v < 0) v = ~v;
+	return v ? 31 - __clz(v) : -1;
+}
+__device__ __forceinline__ int find_lsb(unsigned v) { return v ? __ffs(v) - 1 : -1; }
+
+// Hardware tables: blender divider (luts.hpp:7, regenerated in rdp_luts.cpp),
+// magic-square/Bayer dither (dither.h:28-30), perspective reciprocal (perspective.h:27-44).
+__device__ uint8_t g_blender_lut[0x8000];
+
+__device__ const uint8_t g_dither[2][16] = {
+	{ 0, 6, 1, 7, 4, 2, 5, 3, 3, 5, 2, 4, 7, 1, 6, 0 },
+	{ 0, 4, 1, 5, 4, 0, 5, 1, 3, 7, 2, 6, 7, 3, 6, 2 },
+};
+
+__device__ const int16_t g_persp_base[64] = {
+	0x4000, 0x3f04, 0x3e10, 0x3d22, 0x3c3c, 0x3b5d, 0x3a83, 0x39b1, 0x38e4, 0x381c, 0x375a, 0x369d, 0x35e5, 0x3532, 0x3483, 0x33d9,
+	0x3333, 0x3291, 0x31f4, 0x3159, 0x30c3, 0x3030, 0x2fa1, 0x2f15, 0x2e8c, 0x2e06, 0x2d83, 0x2d03, 0x2c86, 0x2c0b, 0x2b93, 0x2b1e,
+	0x2aab, 0x2a3a, 0x29cc, 0x2960, 0x28f6, 0x288e, 0x2828, 0x27c4, 0x2762, 0x2702, 0x26a4, 0x2648, 0x25ed, 0x2594, 0x253d, 0x24e7,
+	0x2492, 0x243f, 0x23ee, 0x239e, 0x234f, 0x2302, 0x22b6, 0x226c, 0x2222, 0x21da, 0x2193, 0x214d, 0x2108, 0x20c5, 0x2082, 0x2041,
+};
+__device__ const int16_t g_persp_slope[64] = {
+	252, 244, 238, 230, 223, 218, 210, 205, 200, 194, 189, 184, 179, 175, 170, 166,
+	162, 157, 155, 150, 147, 143, 140, 137, 134, 131, 128, 125, 123, 120, 117, 115,
+	113, 110, 108, 106, 104, 102, 100, 98, 96, 94, 92, 91, 89, 87, 86, 85,
+	83, 81, 80, 79, 77, 76, 74, 74, 72, 71, 70, 69, 67, 67, 65, 65,
+};
+
+// ============================================================================ k_prim_setup
+__device__ __forceinline__ uint32_t merge_hi(uint32_t hi_word, uint32_t lo_word)
+{
+	return (hi_word & 0xffff0000u) | ((lo_word >> 16) & 0xffffu);
+}
+__device__ __forceinline__ uint32_t merge_lo(uint32_t hi_word, uint32_t lo_word)
+{
+	return (hi_word << 16) | (lo_word & 0xffffu);
+}
+
+__device__ int norm_muladd(int v) { return (v == 7 || v == 1 || v == 2 || v == 0 || v == 6 || v == 4) ? v : 8; }
+__device__ int norm_mulsub(int v) { return (v == 0 || v == 1 || v == 2 || v == 4 || v == 7) ? v : 8; }
+__device__ int norm_mul(int v)
+{
+	return (v == 0 || v == 7 || v == 1 || v == 2 || v == 8 || v == 9 || v == 4 || v == 11 || v == 13 || v == 15) ? v : 16;
+}
+__device__ int norm_add(int v) { return (v == 1 || v == 2 || v == 0 || v == 6 || v == 4) ? v : 7; }
+__device__ int norm_aaddsub(int v) { return (v == 0 || v == 1 || v == 2 || v == 4 || v == 6) ? v : 7; }
+__device__ int norm_amul(int v) { return (v == 0 || v == 1 || v == 2 || v == 4) ? v : 7; }
+
+__device__ bool acc_t0(const int rgb[4], const int a[4])
+{
+	return rgb[0] == 1 || rgb[1] == 1 || rgb[2] == 1 || rgb[3] == 1 || rgb[2] == 8 || a[0] == 1 || a[1] == 1 ||
+	       a[2] == 1 || a[3] == 1;
+}
+__device__ bool acc_t1(const int rgb[4], const int a[4])
+{
+	return rgb[0] == 2 || rgb[1] == 2 || rgb[2] == 2 || rgb[3] == 2 || rgb[2] == 9 || a[0] == 2 || a[1] == 2 ||
+	       a[2] == 2 || a[3] == 2;
+}
+
+__device__ void put_rgb(uint8_t *o, uint32_t c)
+{
+	o[0] = uint8_t(c >> 24);
+	o[1] = uint8_t(c >> 16);
+	o[2] = uint8_t(c >> 8);
+}
+
+// Conservative x range over one y sample (rdp_renderer.cpp:962-992).
+__device__ void interp_x64(const RdpPrimGeom &g, int y, bool flip, long long &xl, long long &xr)
+{
+	long long yh_base = g.yh & ~3;
+	long long xh = (long long)g.xh + (long long)(y - yh_base) * g.dxhdy;
+	long long xm = (long long)g.xm + (long long)(y - yh_base) * g.dxmdy;
+	long long xlv = (long long)g.xl + (long long)(y - (long long)g.ym) * g.dxldy;
+	if (y < g.ym) xlv = xm;
+	long long hs = xh >> 15, ls = xlv >> 15;
+	xl = flip ? hs : ls;
+	xr = flip ? ls : hs;
+	if (xl > 2147483647LL) xl = 2147483647LL;
+	if (xl < -2147483648LL) xl = -2147483648LL;
+	if (xr > 2147483647LL) xr = 2147483647LL;
+	if (xr < -2147483648LL) xr = -2147483648LL;
+}
+
+__global__ void k_prim_setup(const RdpPrimIn *__restrict__ in, uint32_t num_prims, const uint32_t *__restrict__ words,
+                             const uint32_t *__restrict__ state_blocks, const RdpPass *__restrict__ passes,
+                             RdpPrimGeom *__restrict__ geom_out, RdpPrimAttr *__restrict__ attr_out,
+                             RdpPrimShade *__restrict__ shade_out)
+{
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= num_prims) return;
+	RdpPrimIn pi = in[i];
+	const uint32_t *w = words + pi.word_offset;
+	const uint32_t *sb = state_blocks + size_t(pi.state_block) * RDP_STATE_BLOCK_WORDS;
+	const RdpPass &pass = passes[pi.pass];
+
+	// ---- other modes (rdp_device.cpp:474-540)
+	uint32_t om0 = sb[SB_OTHER_MODES], om1 = sb[SB_OTHER_MODES + 1];
+	uint32_t sf = 0, df = 0;
+	if (om0 & (1u << 19)) sf |= RS_PERSPECTIVE;
+	if (om0 & (1u << 18)) sf |= RS_DETAIL;
+	if (om0 & (1u << 17)) sf |= RS_SHARPEN;
+	if (om0 & (1u << 16)) sf |= RS_TEX_LOD;
+	if (om0 & (1u << 15)) sf |= RS_TLUT;
+	if (om0 & (1u << 14)) sf |= RS_TLUT_TYPE;
+	if (om0 & (1u << 13)) sf |= RS_SAMPLE_QUAD;
+	if (om0 & (1u << 12)) sf |= RS_MID_TEXEL;
+	if (om0 & (1u << 11)) sf |= RS_BILERP0;
+	if (om0 & (1u << 10)) sf |= RS_BILERP1;
+	if (om0 & (1u << 9)) sf |= RS_CONVERT_ONE;
+	if (om1 & (1u << 14)) df |= DB_FORCE_BLEND;
+	if (om1 & (1u << 13)) sf |= RS_ALPHA_CVG_SELECT;
+	if (om1 & (1u << 12)) sf |= RS_CVG_TIMES_ALPHA;
+	if (om1 & (1u << 7)) df |= DB_COLOR_ON_CVG;
+	if (om1 & (1u << 6)) df |= DB_IMAGE_READ;
+	if (om1 & (1u << 5)) df |= DB_DEPTH_UPDATE;
+	if (om1 & (1u << 4)) df |= DB_DEPTH_TEST;
+	if (om1 & (1u << 3)) { sf |= RS_AA; df |= DB_AA; }
+	if (om1 & (1u << 1)) sf |= RS_ALPHA_TEST_DITHER;
+	if (om1 & (1u << 0)) sf |= RS_ALPHA_TEST;
+	uint32_t dither = (om0 >> 4) & 0xf;
+	if ((dither >> 2) != 3) df |= DB_DITHER;
+	uint32_t cycle = (om0 >> 20) & 3;
+	if (cycle == 1) { sf |= RS_MULTI_CYCLE; df |= DB_MULTI_CYCLE; }
+	else if (cycle == 3) sf |= RS_FILL;
+	else if (cycle == 2) sf |= RS_COPY;
+	bool use_prim_depth = (om1 & (1u << 2)) != 0;
+
+	// ---- combine (rdp_device.cpp:661-684)
+	uint32_t c0 = sb[SB_COMBINE], c1 = sb[SB_COMBINE + 1];
+	int rgb[2][4], alp[2][4];
+	rgb[0][0] = (c0 >> 20) & 0xf; rgb[0][2] = (c0 >> 15) & 0x1f; rgb[0][1] = (c1 >> 28) & 0xf; rgb[0][3] = (c1 >> 15) & 7;
+	alp[0][0] = (c0 >> 12) & 7; alp[0][1] = (c1 >> 12) & 7; alp[0][2] = (c0 >> 9) & 7; alp[0][3] = (c1 >> 9) & 7;
+	rgb[1][0] = (c0 >> 5) & 0xf; rgb[1][2] = c0 & 0x1f; rgb[1][1] = (c1 >> 24) & 0xf; rgb[1][3] = (c1 >> 6) & 7;
+	alp[1][0] = (c1 >> 21) & 7; alp[1][1] = (c1 >> 3) & 7; alp[1][2] = (c1 >> 18) & 7; alp[1][3] = c1 & 7;
+
+	// ---- scissor (rdp_device.cpp:461-472)
+	uint32_t s0 = sb[SB_SCISSOR], s1 = sb[SB_SCISSOR + 1];
+	RdpPrimGeom g;
+	g.scissor[0] = (s0 >> 12) & 0xfff;
+	g.scissor[1] = s0 & 0xfff;
+	g.scissor[2] = (s1 >> 12) & 0xfff;
+	g.scissor[3] = s1 & 0xfff;
+	if (s1 & (1u << 25)) sf |= RS_INTERLACE_FIELD;
+	if (s1 & (1u << 24)) sf |= RS_INTERLACE_KEEP_ODD;
+	uint32_t quirks = sb[SB_QUIRKS];
+
+	// ---- primitive words
+	RdpPrimAttr a;
+	for (int c = 0; c < 4; c++)
+	{
+		a.rgba[c] = a.drgba_dx[c] = a.drgba_de[c] = a.drgba_dy[c] = 0;
+		a.stzw[c] = a.dstzw_dx[c] = a.dstzw_de[c] = a.dstzw_dy[c] = 0;
+	}
+	uint32_t op = (w[0] >> 24) & 63;
+	uint32_t tflags = 0, tile = 0;
+	if (op >= 0x08 && op <= 0x0f)
+	{
+		// rdp_device.cpp:268-294
+		bool flip = (w[0] & 0x800000u) != 0;
+		bool sign_dxhdy = (w[5] & 0x80000000u) != 0;
+		tflags |= flip ? TRI_FLIP : 0;
+		tflags |= (flip == sign_dxhdy) ? TRI_DO_OFFSET : 0;
+		tflags |= (sf & RS_COPY) ? TRI_SKIP_XFRAC : 0;
+		tflags |= (quirks & 0xff00u) ? TRI_NATIVE_LOD : 0;
+		tile = (w[0] >> 16) & 63;
+		g.yl = bfe_s(int(w[0]), 14);
+		g.ym = bfe_s(int(w[1] >> 16), 14);
+		g.yh = bfe_s(int(w[1]), 14);
+		g.xl = bfe_s(int(w[2]), 28) >> 1;
+		g.xh = bfe_s(int(w[4]), 28) >> 1;
+		g.xm = bfe_s(int(w[6]), 28) >> 1;
+		g.dxldy = bfe_s(int(w[3] >> 2), 28) >> 1;
+		g.dxhdy = bfe_s(int(w[5] >> 2), 28) >> 1;
+		g.dxmdy = bfe_s(int(w[7] >> 2), 28) >> 1;
+		const uint32_t *p = w + 8;
+		if (op & 4)
+		{
+			// rdp_device.cpp:315-336
+			for (int c = 0; c < 4; c++)
+			{
+				int k = c >> 1;
+				bool lo = c & 1;
+				a.rgba[c] = int(lo ? merge_lo(p[0 + k], p[4 + k]) : merge_hi(p[0 + k], p[4 + k]));
+				a.drgba_dx[c] = int(lo ? merge_lo(p[2 + k], p[6 + k]) : merge_hi(p[2 + k], p[6 + k]));
+				a.drgba_de[c] = int(lo ? merge_lo(p[8 + k], p[12 + k]) : merge_hi(p[8 + k], p[12 + k]));
+				a.drgba_dy[c] = int(lo ? merge_lo(p[10 + k], p[14 + k]) : merge_hi(p[10 + k], p[14 + k]));
+			}
+			p += 16;
+		}
+		if (op & 2)
+		{
+			// rdp_device.cpp:296-313
+			a.stzw[0] = int(merge_hi(p[0], p[4]));
+			a.stzw[1] = int(merge_lo(p[0], p[4]));
+			a.stzw[3] = int(merge_hi(p[1], p[5]));
+			a.dstzw_dx[0] = int(merge_hi(p[2], p[6]));
+			a.dstzw_dx[1] = int(merge_lo(p[2], p[6]));
+			a.dstzw_dx[3] = int(merge_hi(p[3], p[7]));
+			a.dstzw_de[0] = int(merge_hi(p[8], p[12]));
+			a.dstzw_de[1] = int(merge_lo(p[8], p[12]));
+			a.dstzw_de[3] = int(merge_hi(p[9], p[13]));
+			a.dstzw_dy[0] = int(merge_hi(p[10], p[14]));
+			a.dstzw_dy[1] = int(merge_lo(p[10], p[14]));
+			a.dstzw_dy[3] = int(merge_hi(p[11], p[15]));
+			p += 16;
+		}
+		if (op & 1)
+		{
+			a.stzw[2] = int(p[0]);
+			a.dstzw_dx[2] = int(p[1]);
+			a.dstzw_de[2] = int(p[2]);
+			a.dstzw_dy[2] = int(p[3]);
+		}
+	}
+	else
+	{
+		// Rectangles (rdp_device.cpp:713-821).
+		uint32_t xl = (w[0] >> 12) & 0xfff, yl = w[0] & 0xfff, xh = (w[1] >> 12) & 0xfff, yh = w[1] & 0xfff;
+		if (sf & (RS_COPY | RS_FILL)) yl |= 3;
+		g.xh = int(xh << 13);
+		g.xl = int(xl << 13);
+		g.xm = int(xl << 13);
+		g.ym = int(yl);
+		g.yl = int(yl);
+		g.yh = int(yh);
+		g.dxhdy = g.dxmdy = g.dxldy = 0;
+		tflags = TRI_FLIP | TRI_DISABLE_UPSCALING;
+		if (op == 0x24 || op == 0x25)
+		{
+			bool rflip = op == 0x25;
+			tile = (w[1] >> 24) & 7;
+			int sv = int((w[2] >> 16) & 0xffff), tv = int(w[2] & 0xffff);
+			int dsdx = bfe_s(int((w[3] >> 16) & 0xffff), 16), dtdy = bfe_s(int(w[3] & 0xffff), 16);
+			tflags = TRI_FLIP | (rflip ? TRI_DISABLE_UPSCALING : 0) | ((quirks & 0xffu) ? TRI_DISABLE_UPSCALING : 0) |
+			         ((quirks & 0xff00u) ? TRI_NATIVE_LOD : 0);
+			a.stzw[0] = shlw(sv, 16);
+			a.stzw[1] = shlw(tv, 16);
+			if (!rflip)
+			{
+				a.dstzw_dx[0] = shlw(dsdx, 11);
+				a.dstzw_de[1] = shlw(dtdy, 11);
+				a.dstzw_dy[1] = shlw(dtdy, 11);
+			}
+			else
+			{
+				a.dstzw_dx[1] = shlw(dtdy, 11);
+				a.dstzw_de[0] = shlw(dsdx, 11);
+				a.dstzw_dy[0] = shlw(dsdx, 11);
+			}
+			if (sf & RS_COPY) tflags |= TRI_SKIP_XFRAC;
+		}
+	}
+
+	// ---- fixup_triangle_setup (rdp_renderer.cpp:1402-1423)
+	if (g.ym < (g.yh & ~3)) g.ym = 0x7fff;
+	if (sf & RS_INTERLACE_FIELD)
+	{
+		tflags |= TRI_INTERLACE_FIELD;
+		if (sf & RS_INTERLACE_KEEP_ODD) tflags |= TRI_INTERLACE_KEEP_ODD;
+	}
+	if (sf & (RS_COPY | RS_FILL)) tflags |= TRI_FILL_COPY_RASTER;
+	g.flags = tflags;
+	g.tile = tile;
+
+	// ---- derived setup (rdp_renderer.cpp:910-948), computed from the attributes before prim depth
+	RdpPrimShade sh;
+	uint32_t prim_color = sb[SB_PRIM_COLOR + 1], env = sb[SB_ENV_COLOR + 1];
+	int prim_lod_frac = sb[SB_PRIM_COLOR] & 0xff;
+	int min_level = (sb[SB_PRIM_COLOR] >> 8) & 31;
+	uint32_t pd = sb[SB_PRIM_DEPTH + 1];
+	{
+		int dz;
+		if (use_prim_depth) dz = pd & 0xffff;
+		else
+		{
+			int dzdx = a.dstzw_dx[2] >> 16, dzdy = a.dstzw_dy[2] >> 16;
+			int dzpix = (dzdx < 0 ? (~dzdx & 0x7fff) : dzdx) + (dzdy < 0 ? (~dzdy & 0x7fff) : dzdy);
+			if (dzpix >= 0x8000) dzpix = 0x8000;
+			else if (dzpix == 0) dzpix = 1;
+			else dzpix = 1 << (find_msb(dzpix) + 1);
+			dz = dzpix;
+		}
+		int v = 0;
+		if (dz & 0xff00) v |= 8;
+		if (dz & 0xf0f0) v |= 4;
+		if (dz & 0xcccc) v |= 2;
+		if (dz & 0xaaaa) v |= 1;
+		sh.dz = uint16_t(dz);
+		sh.dz_compressed = uint8_t(v);
+	}
+	uint64_t conv = (uint64_t(sb[SB_CONVERT]) << 32) | sb[SB_CONVERT + 1];
+	int k[6];
+	for (int j = 0; j < 6; j++) k[j] = int((conv >> (45 - 9 * j)) & 0x1ff);
+	int key_center[3] = { int((sb[SB_KEY_R + 1] >> 8) & 0xff), int((sb[SB_KEY_GB + 1] >> 24) & 0xff),
+	                      int((sb[SB_KEY_GB + 1] >> 8) & 0xff) };
+	int key_scale[3] = { int(sb[SB_KEY_R + 1] & 0xff), int((sb[SB_KEY_GB + 1] >> 16) & 0xff),
+	                     int(sb[SB_KEY_GB + 1] & 0xff) };
+	for (int cy = 0; cy < 2; cy++)
+	{
+		uint8_t *ma = sh.c_muladd[cy], *ms = sh.c_mulsub[cy], *mu = sh.c_mul[cy], *ad = sh.c_add[cy];
+		for (int c = 0; c < 4; c++) ma[c] = ms[c] = mu[c] = ad[c] = 0;
+		// rdp_renderer.cpp:754-908
+		switch (rgb[cy][0]) { case 5: put_rgb(ma, env); break; case 3: put_rgb(ma, prim_color); break; default: break; }
+		switch (rgb[cy][1])
+		{
+		case 5: put_rgb(ms, env); break;
+		case 3: put_rgb(ms, prim_color); break;
+		case 7: put_rgb(ms, uint32_t(k[4]) << 8); break;
+		case 6: ms[0] = uint8_t(key_center[0]); ms[1] = uint8_t(key_center[1]); ms[2] = uint8_t(key_center[2]); break;
+		default: break;
+		}
+		switch (rgb[cy][2])
+		{
+		case 3: put_rgb(mu, prim_color); break;
+		case 5: put_rgb(mu, env); break;
+		case 10: put_rgb(mu, 0x01010101u * (prim_color & 0xff)); break;
+		case 12: put_rgb(mu, 0x01010101u * (env & 0xff)); break;
+		case 14: put_rgb(mu, 0x01010101u * uint32_t(prim_lod_frac)); break;
+		case 15: put_rgb(mu, uint32_t(k[5]) << 8); break;
+		case 6: mu[0] = uint8_t(key_scale[0]); mu[1] = uint8_t(key_scale[1]); mu[2] = uint8_t(key_scale[2]); break;
+		default: break;
+		}
+		switch (rgb[cy][3]) { case 3: put_rgb(ad, prim_color); break; case 5: put_rgb(ad, env); break; default: break; }
+		switch (alp[cy][0]) { case 3: ma[3] = uint8_t(prim_color); break; case 5: ma[3] = uint8_t(env); break; default: break; }
+		switch (alp[cy][1]) { case 3: ms[3] = uint8_t(prim_color); break; case 5: ms[3] = uint8_t(env); break; default: break; }
+		switch (alp[cy][2])
+		{
+		case 3: mu[3] = uint8_t(prim_color); break;
+		case 5: mu[3] = uint8_t(env); break;
+		case 6: mu[3] = uint8_t(prim_lod_frac); break;
+		default: break;
+		}
+		switch (alp[cy][3]) { case 3: ad[3] = uint8_t(prim_color); break; case 5: ad[3] = uint8_t(env); break; default: break; }
+	}
+	uint32_t fog = sb[SB_FOG_COLOR + 1], blendc = sb[SB_BLEND_COLOR + 1];
+	for (int c = 0; c < 4; c++)
+	{
+		sh.fog[c] = uint8_t(fog >> (24 - 8 * c));
+		sh.blend_color[c] = uint8_t(blendc >> (24 - 8 * c));
+	}
+	sh.fill_color = sb[SB_FILL_COLOR + 1];
+	sh.min_lod = uint8_t(min_level);
+	for (int j = 0; j < 4; j++) sh.factors[j] = int16_t(2 * bfe_s(k[j], 9) + 1);
+
+	if (use_prim_depth)
+	{
+		a.stzw[2] = int((pd >> 16) & 0x7fff) << 16;
+		a.dstzw_dx[2] = a.dstzw_de[2] = a.dstzw_dy[2] = 0;
+	}
+
+	// ---- deduce_static_texture_state / deduce_noise_state / normalize_static_state
+	// (rdp_renderer.cpp:1136-1400)
+	if (!(sf & (RS_FILL | RS_COPY)))
+	{
+		bool multi = (sf & RS_MULTI_CYCLE) != 0;
+		bool t0 = multi ? (acc_t0(rgb[0], alp[0]) || acc_t1(rgb[1], alp[1])) : acc_t0(rgb[1], alp[1]);
+		bool t1 = multi ? (acc_t1(rgb[0], alp[0]) || acc_t0(rgb[1], alp[1])) : false;
+		bool pt1 = !multi ? acc_t1(rgb[1], alp[1]) : false;
+		bool lodf = multi ? (rgb[0][2] == 13 || alp[0][2] == 0 || rgb[1][2] == 13 || alp[1][2] == 0) : false;
+		if (t1 && (sf & RS_CONVERT_ONE)) t0 = true;
+		if (t0) sf |= RS_USES_TEXEL0;
+		if (t1) sf |= RS_USES_TEXEL1;
+		if (pt1) sf |= RS_USES_PIPELINED_TEXEL1;
+		if (lodf || (sf & RS_TEX_LOD)) sf |= RS_USES_LOD;
+	}
+	if ((dither & 3) == 2 || ((dither >> 2) & 3) == 2)
+		sf |= RS_NEED_NOISE;
+	else if (!(sf & (RS_COPY | RS_FILL)))
+	{
+		if ((sf & RS_MULTI_CYCLE) && rgb[0][0] == 7) sf |= RS_NEED_NOISE;
+		if (rgb[1][0] == 7) sf |= RS_NEED_NOISE;
+		if ((sf & RS_MULTI_CYCLE) && rgb[0][0] == 7 && rgb[1][0] == 7) sf |= RS_NEED_NOISE_DUAL;
+		if ((sf & (RS_ALPHA_TEST | RS_ALPHA_TEST_DITHER)) == (RS_ALPHA_TEST | RS_ALPHA_TEST_DITHER)) sf |= RS_NEED_NOISE;
+	}
+	if (sf & RS_FILL)
+	{
+		sf = RS_FILL;
+		dither = 0;
+		for (int cy = 0; cy < 2; cy++)
+			for (int j = 0; j < 4; j++) rgb[cy][j] = alp[cy][j] = 0;
+	}
+	else if (sf & RS_COPY)
+	{
+		// USES_TEXEL0 is kept from previous draws in the reference; copy mode never reads it.
+		sf &= (RS_COPY | RS_TLUT | RS_TLUT_TYPE | RS_TEX_LOD | RS_DETAIL | RS_PERSPECTIVE | RS_ALPHA_TEST);
+		dither = 0;
+		for (int cy = 0; cy < 2; cy++)
+			for (int j = 0; j < 4; j++) rgb[cy][j] = alp[cy][j] = 0;
+	}
+	else
+	{
+		if ((sf & (RS_MULTI_CYCLE | RS_USES_PIPELINED_TEXEL1)) == 0) sf &= ~(RS_BILERP1 | RS_CONVERT_ONE);
+		for (int cy = 0; cy < 2; cy++)
+		{
+			rgb[cy][0] = norm_muladd(rgb[cy][0]);
+			rgb[cy][1] = norm_mulsub(rgb[cy][1]);
+			rgb[cy][2] = norm_mul(rgb[cy][2]);
+			rgb[cy][3] = norm_add(rgb[cy][3]);
+			alp[cy][0] = norm_aaddsub(alp[cy][0]);
+			alp[cy][1] = norm_aaddsub(alp[cy][1]);
+			alp[cy][2] = norm_amul(alp[cy][2]);
+			alp[cy][3] = norm_aaddsub(alp[cy][3]);
+		}
+	}
+	sh.static_flags = sf;
+	sh.dither = dither;
+	for (int cy = 0; cy < 2; cy++)
+		for (int j = 0; j < 4; j++)
+		{
+			sh.comb_rgb[cy][j] = uint8_t(rgb[cy][j]);
+			sh.comb_alpha[cy][j] = uint8_t(alp[cy][j]);
+		}
+	sh.db_flags = df;
+	sh.blend[0][0] = (om1 >> 30) & 3; sh.blend[1][0] = (om1 >> 28) & 3;
+	sh.blend[0][1] = (om1 >> 26) & 3; sh.blend[1][1] = (om1 >> 24) & 3;
+	sh.blend[0][2] = (om1 >> 22) & 3; sh.blend[1][2] = (om1 >> 20) & 3;
+	sh.blend[0][3] = (om1 >> 18) & 3; sh.blend[1][3] = (om1 >> 16) & 3;
+	sh.coverage_mode = (om1 >> 8) & 3;
+	sh.z_mode = (om1 >> 10) & 3;
+	sh.tmem_index = pi.tmem_index;
+	sh.tileset = pi.tileset;
+	sh.prim_index = pass.base_prim_index + (i - pass.prim_begin);
+	sh.pass = pi.pass;
+	sh.pad[0] = sh.pad[1] = sh.pad[2] = 0;
+
+	// ---- span job range (rdp_renderer.cpp:1523-1554)
+	int min_sub = max(g.yh, g.scissor[1]);
+	int max_sub = min(g.yl - 1, g.scissor[3] - 1);
+	int ylo = min_sub >> 2, yhi = max_sub >> 2;
+	if (yhi < ylo) { ylo = 0; yhi = -1; }
+	g.span_ylo = ylo;
+	g.span_yhi = yhi;
+
+	// ---- conservative tile bounding box (rdp_renderer.cpp:994-1060)
+	g.bbox[0] = 1; g.bbox[1] = 0; g.bbox[2] = 0; g.bbox[3] = 0;
+	if (g.yl > g.yh && yhi >= ylo)
+	{
+		int start_y = g.yh & ~3;
+		int end_y = (g.yl - 1) | 3;
+		start_y = max(g.scissor[1], start_y);
+		end_y = min(g.scissor[3] - 1, end_y);
+		if (end_y >= start_y)
+		{
+			bool flip = (tflags & TRI_FLIP) != 0;
+			long long l0, r0, l1, r1, l2, r2, l3, r3;
+			interp_x64(g, start_y, flip, l0, r0);
+			interp_x64(g, end_y, flip, l1, r1);
+			l2 = l3 = l0; r2 = r3 = r0;
+			if (g.ym > start_y && g.ym < end_y)
+			{
+				interp_x64(g, g.ym, flip, l2, r2);
+				interp_x64(g, g.ym - 1, flip, l3, r3);
+			}
+			long long sx = min(min(l0, l1), min(l2, l3));
+			long long ex = max(max(r0, r1), max(r2, r3));
+			long long mr = max(sx < 0 ? -sx : sx, ex < 0 ? -ex : ex);
+			if (mr > 2047) { sx = 0; ex = 0x7fffffff; }
+			sx = max(sx, (long long)(g.scissor[0] >> 2));
+			ex = min(ex, (long long)(((g.scissor[2] + 4) >> 2) - 1) + 1);
+			ex = min(ex, (long long)pass.fb_width - 1);
+			int ty0 = start_y / 32, ty1 = min(end_y / 32, int(pass.tiles_y) - 1);
+			if (ex >= sx && ty1 >= ty0)
+			{
+				g.bbox[0] = uint16_t(sx / 8);
+				g.bbox[1] = uint16_t(ty0);
+				g.bbox[2] = uint16_t(min(int(ex / 8), int(pass.tiles_x) - 1));
+				g.bbox[3] = uint16_t(ty1);
+			}
+		}
+	}
+	g.pad[0] = 0;
+	geom_out[i] = g;
+	attr_out[i] = a;
+	shade_out[i] = sh;
+}
+
+// ============================================================================ k_bin
+// binning.h:58-144 at scaling 1.
+__device__ bool bin_primitive(const RdpPrimGeom &g, int lox, int loy, int hix, int hiy)
+{
+	loy = max(loy, g.scissor[1] >> 2);
+	hiy = min(hiy, ((g.scissor[3] + 3) >> 2) - 1);
+	int start_y = max(loy * 4, g.yh);
+	int end_y = min(hiy * 4 + 3, g.yl - 1);
+	if (end_y < start_y) return false;
+	bool flip = (g.flags & TRI_FLIP) != 0;
+	int ys[4] = { start_y, end_y, clampi(g.ym - 1, start_y, end_y), clampi(g.ym, start_y, end_y) };
+	int yh_base = g.yh & ~3;
+	int xmin = 0x7fffffff, xmax = -0x7fffffff - 1, mr = 0;
+#pragma unroll
+	for (int k = 0; k < 4; k++)
+	{
+		long long xh = (long long)g.xh + (long long)(ys[k] - yh_base) * g.dxhdy;
+		long long xm = (long long)g.xm + (long long)(ys[k] - yh_base) * g.dxmdy;
+		long long xl = (long long)g.xl + (long long)(ys[k] - g.ym) * g.dxldy;
+		if (ys[k] < g.ym) xl = xm;
+		xh = min(max(xh, -2147483648LL), 2147483647LL);
+		xl = min(max(xl, -2147483648LL), 2147483647LL);
+		int hs = int(xh) >> 15, ls = int(xl) >> 15;
+		int l = flip ? hs : ls, r = flip ? ls : hs;
+		xmin = min(xmin, l);
+		xmax = max(xmax, r);
+		mr = max(mr, max(abs(l), abs(r)));
+	}
+	int rx0, rx1;
+	if (mr <= 2047) { rx0 = xmin; rx1 = xmax; }
+	else { rx0 = 0; rx1 = 0x7fffffff; }
+	int x_bias = (g.flags & TRI_FILL_COPY_RASTER) ? 4 : 3;
+	int sx0 = g.scissor[0] >> 2, sx1 = ((g.scissor[2] + x_bias) >> 2) - 1;
+	rx0 = clampi(rx0, sx0, sx1);
+	rx1 = clampi(rx1, sx0, sx1);
+	rx0 = max(rx0, lox);
+	rx1 = min(rx1, hix);
+	return rx0 <= rx1;
+}
+
+__global__ void k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom, const RdpPrimShade *__restrict__ shade,
+                      const RdpPass *__restrict__ passes)
+{
+	uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	uint32_t lane = threadIdx.x & 31;
+	if (warp >= num_prims) return;
+	const RdpPrimGeom g = geom[warp];
+	if (g.bbox[2] < g.bbox[0] || g.bbox[3] < g.bbox[1]) return;
+	const RdpPass &pass = passes[shade[warp].pass];
+	uint32_t local = warp - pass.prim_begin;
+	uint32_t bit = 1u << (local & 31);
+	uint32_t word = local >> 5;
+	int tw = g.bbox[2] - g.bbox[0] + 1, th = g.bbox[3] - g.bbox[1] + 1;
+	int count = tw * th;
+	int fbw = int(pass.fb_width), fbh = int(pass.fb_height);
+	for (int t = lane; t < count; t += 32)
+	{
+		int tx = g.bbox[0] + t % tw, ty = g.bbox[1] + t / tw;
+		int lox = tx * 8, loy = ty * 8;
+		int hix = min(lox + 7, fbw - 1), hiy = min(loy + 7, fbh - 1);
+		if (bin_primitive(g, lox, loy, hix, hiy))
+			atomicOr(&pass.masks[size_t(ty * pass.tiles_x + tx) * RDP_MASK_WORDS_PER_TILE + word], bit);
+	}
+}
+
+// ============================================================================ k_tmem
+__device__ __forceinline__ uint8_t rd8(const RdpPass &p, uint32_t a) { return p.rdram[a & (p.rdram_size - 1)]; }
+__device__ __forceinline__ uint16_t rd16(const RdpPass &p, uint32_t i)
+{
+	uint32_t b = (i * 2) & (p.rdram_size - 1);
+	return *reinterpret_cast<const uint16_t *>(p.rdram + b);
+}
+__device__ __forceinline__ uint32_t rd32(const RdpPass &p, uint32_t i)
+{
+	uint32_t b = (i * 4) & (p.rdram_size - 1);
+	return *reinterpret_cast<const uint32_t *>(p.rdram + b);
+}
+
+__device__ __forceinline__ int upload_t(int offset, float inv_stride)
+{
+	return int(__fmul_rn(__fadd_rn(float(offset), 0.5f), inv_stride));
+}
+
+// tmem_update.comp:108-317
+__device__ bool tmem_32(const RdpPass &ps, const RdpUpload &info, int tmem16_index, bool upper, bool yuv, uint32_t &value)
+{
+	int tmem16_offset = (info.tmem_offset & 0x7ff) >> 1;
+	int stride = info.tmem_stride_words;
+	int pixel_offset = (tmem16_index - tmem16_offset) & 0x3ff;
+	int ux, uy, uxx = 0;
+	if (info.mode == 2)
+	{
+		int wo = pixel_offset >> 1;
+		if (stride == 0)
+		{
+			int f = wo & ~1, s = f + 1;
+			int ft = mulw(f, info.dxt) >> 16, st = mulw(s, info.dxt) >> 16;
+			if (ft != st)
+			{
+				int fw = f ^ (ft & 1), sw = s ^ (st & 1);
+				if (sw == wo) uxx = (st & 1) << 1;
+				else if (fw == wo) uxx = (ft & 1) << 1;
+				else return false;
+			}
+			else
+				uxx ^= (ft & 1) << 1;
+		}
+		else
+		{
+			int min_t = upload_t(wo & ~1, info.min_t_mod);
+			int max_t = upload_t(wo | 1, info.max_t_mod);
+			int max_wc = (wo | 1) - stride * min_t;
+			int min_wc = (wo & ~1) - stride * max_t;
+			min_t = max(min_t, mulw(min_wc, info.dxt) >> 16);
+			max_t = min(max_t, mulw(max_wc, info.dxt) >> 16);
+			bool found = false;
+			for (int t = max_t; t >= min_t; t--)
+			{
+				int c1 = (wo & ~1) - stride * t, c2 = (wo | 1) - stride * t;
+				int t1 = mulw(c1, info.dxt) >> 16, t2 = mulw(c2, info.dxt) >> 16;
+				if (((c2 + t2 * stride) ^ (t2 & 1)) == wo)
+				{
+					found = true;
+					pixel_offset = (c2 << 1) + (pixel_offset & 1);
+					break;
+				}
+				else if (((c1 + t1 * stride) ^ (t1 & 1)) == wo)
+				{
+					found = true;
+					pixel_offset = (c1 << 1) + (pixel_offset & 1);
+					break;
+				}
+			}
+			if (!found) return false;
+		}
+		ux = pixel_offset;
+		uy = 0;
+	}
+	else if (stride == 0)
+	{
+		ux = pixel_offset;
+		uy = info.height - 1;
+	}
+	else
+	{
+		uy = upload_t(pixel_offset, info.inv_tmem_stride_words);
+		ux = pixel_offset - uy * stride;
+		if (uy >= info.height)
+		{
+			ux += stride * (uy - info.height + 1);
+			uy = info.height - 1;
+		}
+	}
+	int last_x = ux ^ ((uy & 1) << 1);
+	if (last_x >= info.width && uy > 0)
+	{
+		uy--;
+		ux += stride;
+	}
+	int it = 0;
+	ux ^= ((uy & 1) << 1) | uxx;
+	if (info.vram_size == 3 || yuv) it = 4 * (ux & ~1);
+	else if (info.vram_size == 2)
+	{
+		if (ux & 2)
+		{
+			if (uy > 0)
+			{
+				uy--;
+				ux += stride;
+				ux ^= 2;
+			}
+			else
+				return false;
+		}
+		it = 2 * (ux & ~1);
+	}
+	else if (info.vram_size == 1)
+	{
+		for (int k = 0; k < 4 && uy > 0 && (ux & 6) != 0; k++)
+		{
+			uy--;
+			ux += stride;
+			ux ^= 2;
+		}
+		if (ux & 6) return false;
+		it = ux & ~1;
+	}
+	if (ux >= info.width) return false;
+	int line = info.vram_addr + shlw(mulw(uy, info.vram_width), info.vram_size - 1);
+	int addr = line + it + 4 * (ux & 1);
+	uint32_t word;
+	if ((addr & 3) == 0) word = rd32(ps, uint32_t(addr) >> 2);
+	else
+		word = (uint32_t(rd8(ps, uint32_t(addr) ^ 3)) << 24) | (uint32_t(rd8(ps, uint32_t(addr + 1) ^ 3)) << 16) |
+		       (uint32_t(rd8(ps, uint32_t(addr + 2) ^ 3)) << 8) | uint32_t(rd8(ps, uint32_t(addr + 3) ^ 3));
+	if (yuv)
+	{
+		if (upper) word = (((word >> 16) & 0xffu) << 8) | (word & 0xffu);
+		else word = (((word >> 24) & 0xffu) << 8) | ((word >> 8) & 0xffu);
+	}
+	else
+	{
+		word >>= 16u - 16u * uint32_t(upper);
+		word &= 0xffffu;
+	}
+	value = word;
+	return true;
+}
+
+// tmem_update.comp:319-459
+__device__ bool tmem_16(const RdpPass &ps, const RdpUpload &info, int tmem16_index, uint32_t &value)
+{
+	int tmem16_offset = (info.tmem_offset & 0xfff) >> 1;
+	int stride = info.tmem_stride_words;
+	int pixel_offset = (tmem16_index - tmem16_offset) & 0x7ff;
+	int ux, uy, uxx = 0;
+	if (info.mode == 2)
+	{
+		int wo = pixel_offset >> 2;
+		if (stride == 0)
+			uxx = ((mulw(wo, info.dxt) >> 16) & 1) << 1;
+		else
+		{
+			int min_t = upload_t(wo, info.min_t_mod);
+			int max_t = upload_t(wo, info.max_t_mod);
+			int max_wc = wo - stride * min_t;
+			int min_wc = wo - stride * max_t;
+			min_t = max(min_t, mulw(min_wc, info.dxt) >> 16);
+			max_t = min(max_t, mulw(max_wc, info.dxt) >> 16);
+			bool found = false;
+			for (int t = max_t; t >= min_t; t--)
+			{
+				int cand = wo - stride * t;
+				int ct = mulw(cand, info.dxt) >> 16;
+				if (cand + ct * stride == wo)
+				{
+					found = true;
+					uxx = (ct & 1) << 1;
+					pixel_offset = (cand << 2) + (pixel_offset & 3);
+				}
+			}
+			if (!found) return false;
+		}
+		ux = pixel_offset;
+		uy = 0;
+	}
+	else if (stride == 0)
+	{
+		ux = pixel_offset;
+		uy = info.height - 1;
+	}
+	else
+	{
+		uy = upload_t(pixel_offset, info.inv_tmem_stride_words);
+		ux = pixel_offset - uy * stride;
+		if (uy >= info.height)
+		{
+			ux += stride * (uy - info.height + 1);
+			uy = info.height - 1;
+		}
+	}
+	int it = 0;
+	if (info.tmem_size != info.vram_size)
+	{
+		if (info.vram_size - info.tmem_size == 1)
+		{
+			it = (ux & ~3) * 4;
+			if ((ux & ~3) + 2 < (info.vram_effective_width >> (3 - info.vram_size))) it += 8;
+		}
+		else if (info.tmem_size == 2 && info.vram_size == 1)
+		{
+			if (ux & 4)
+			{
+				if ((stride & 4) != 0 && uy > 0)
+				{
+					uy--;
+					ux += stride;
+				}
+				else
+					return false;
+			}
+			it = ux & ~3;
+		}
+	}
+	else
+		it = (ux & ~3) * 2;
+	if (ux >= info.width) return false;
+	int line = info.vram_addr + shlw(mulw(uy, info.vram_width), info.vram_size - 1);
+	ux ^= ((uy & 1) << 1) | uxx;
+	int addr = line + it + 2 * (ux & 3);
+	uint32_t word;
+	if ((addr & 1) == 0) word = rd16(ps, (uint32_t(addr) >> 1) ^ 1u);
+	else word = (uint32_t(rd8(ps, uint32_t(addr) ^ 3)) << 8) | uint32_t(rd8(ps, uint32_t(addr + 1) ^ 3));
+	value = word;
+	return true;
+}
+
+// tmem_update.comp:461-544
+__device__ bool tmem_lut(const RdpPass &ps, const RdpUpload &info, int tmem16_index, uint32_t &value)
+{
+	int tmem16_offset = (info.tmem_offset & 0xfff) >> 1;
+	int po = (tmem16_index - tmem16_offset) & 0x7ff;
+	int splat;
+	int d = info.vram_size - info.tmem_size;
+	if (d == 2)
+	{
+		splat = (po >> 2) << (info.vram_size - 2);
+		if (splat >= info.vram_effective_width) return false;
+	}
+	else if (d == 1)
+	{
+		if (po & 4) return false;
+		int shamt = info.tmem_size + (info.vram_size == 2 ? 2 : 0);
+		splat = (po & ~7) >> shamt;
+		if (splat >= info.vram_effective_width) return false;
+	}
+	else if (d == 0)
+	{
+		if (po & 0xc) return false;
+		int shamt = info.tmem_size + (info.vram_size == 2 ? 2 : 0);
+		splat = (po & ~3) >> shamt;
+		if (splat >= info.vram_effective_width) return false;
+	}
+	else if (d == -1)
+	{
+		if (po & 0x1c) return false;
+		splat = (po >> info.tmem_size) & ~7;
+		if (splat >= info.vram_effective_width) return false;
+	}
+	else
+	{
+		int sp = ((po >> 2) * 2) * 2;
+		if (sp + 2 < info.vram_effective_width) sp += 2;
+		if (sp >= info.vram_effective_width) return false;
+		splat = sp;
+	}
+	int addr = info.vram_addr + shlw(splat, info.vram_size - 1);
+	addr += 2 * (addr & 1) * (po & 3);
+	uint32_t word;
+	if ((addr & 1) == 0) word = rd16(ps, (uint32_t(addr) >> 1) ^ 1u);
+	else word = (uint32_t(rd8(ps, uint32_t(addr) ^ 3)) << 8) | uint32_t(rd8(ps, uint32_t(addr + 1) ^ 3));
+	value = word;
+	return true;
+}
+
+__global__ void __launch_bounds__(1024) k_tmem(const RdpPass *__restrict__ passes, const uint32_t *__restrict__ pass_list,
+                                               const RdpUpload *__restrict__ uploads)
+{
+	const RdpPass &ps = passes[pass_list[blockIdx.x]];
+	uint16_t *snap = ps.tmem_snapshots;
+	for (int h = 0; h < 2; h++)
+	{
+		int gid = threadIdx.x + h * 1024;
+		uint32_t value = ps.tmem_state[gid];
+		snap[gid] = uint16_t(value);
+		int idx = gid ^ 1;
+		bool upper = idx >= 0x400;
+		for (uint32_t u = 0; u < ps.upload_count; u++)
+		{
+			RdpUpload info = uploads[ps.upload_begin + u];
+			uint32_t v = 0;
+			bool wrote;
+			if (info.mode == 1) wrote = tmem_lut(ps, info, idx, v);
+			else
+			{
+				bool yuv = info.tmem_fmt == 1;
+				if (info.tmem_size == 3 || yuv) wrote = tmem_32(ps, info, idx & 0x3ff, upper, yuv, v);
+				else wrote = tmem_16(ps, info, idx, v);
+			}
+			if (wrote) value = v;
+			snap[size_t(u + 1) * 2048 + gid] = uint16_t(value);
+		}
+		ps.tmem_state[gid] = uint16_t(value);
+	}
+}
+
+// ============================================================================ k_raster: spans
+struct SpanA
+{
+	int rgba[4];
+	int stzw[4];
+	int base_x;
+	int pad[3];
+};
+
+struct SpanX
+{
+	uint16_t xl[4], xr[4];
+	int start_x, end_x;
+	int valid;
+	int pad;
+};
+
+// Attribute half of span_setup.comp:99-150.
+__device__ void span_attr(const RdpPrimGeom &g, const RdpPrimAttr &a, int y, SpanA &out)
+{
+	bool do_offset = (g.flags & TRI_DO_OFFSET) != 0;
+	bool skip_xfrac = (g.flags & TRI_SKIP_XFRAC) != 0;
+	int dy = y - (g.yh >> 2);
+	int xh = g.xh + mulw(dy, shlw(g.dxhdy, 2));
+	int drd[4] = { 0, 0, 0, 0 }, dsd[4] = { 0, 0, 0, 0 };
+	if (do_offset)
+	{
+		xh += mulw(3, g.dxhdy);
+#pragma unroll
+		for (int c = 0; c < 4; c++)
+		{
+			int deh = a.drgba_de[c] & ~0x1ff, dyh = a.drgba_dy[c] & ~0x1ff;
+			drd[c] = deh - (deh >> 2) - dyh + (dyh >> 2);
+			deh = a.dstzw_de[c] & ~0x1ff;
+			dyh = a.dstzw_dy[c] & ~0x1ff;
+			dsd[c] = deh - (deh >> 2) - dyh + (dyh >> 2);
+		}
+	}
+	int xfrac = skip_xfrac ? 0 : ((xh >> 7) & 0xff);
+#pragma unroll
+	for (int c = 0; c < 4; c++)
+	{
+		int v = a.rgba[c] + mulw(dy, a.drgba_de[c]);
+		out.rgba[c] = ((v & ~0x1ff) + drd[c] - mulw(xfrac, (a.drgba_dx[c] >> 8) & ~1)) & ~0x3ff;
+		v = a.stzw[c] + mulw(dy, a.dstzw_de[c]);
+		out.stzw[c] = ((v & ~0x1ff) + dsd[c] - mulw(xfrac, (a.dstzw_dx[c] >> 8) & ~1)) & ~0x3ff;
+	}
+	out.base_x = xh >> 15;
+}
+
+__device__ __forceinline__ int quantize_x(int x) { return (x >> 12) | ((x & 0xfff) != 0 ? 1 : 0); }
+
+// Coverage half of span_setup.comp:152-225.
+__device__ void span_x(const RdpPrimGeom &g, int y, SpanX &out)
+{
+	bool flip = (g.flags & TRI_FLIP) != 0;
+	int yh_base = g.yh & ~3;
+	int ylo = max(g.yh, g.scissor[1]);
+	int yhi = min(g.yl, g.scissor[3]);
+	int lo_sc = g.scissor[0] << 1, hi_sc = g.scissor[2] << 1;
+	bool all_over = true, all_under = true, all_invalid = true;
+	int mn = 0x7fffffff, mx = -0x7fffffff - 1;
+#pragma unroll
+	for (int k = 0; k < 4; k++)
+	{
+		int ys = y * 4 + k;
+		bool clip_y = ys < ylo || ys >= yhi;
+		int xh = g.xh + mulw(ys - yh_base, g.dxhdy);
+		int xm = g.xm + mulw(ys - yh_base, g.dxmdy);
+		int xl = g.xl + mulw(ys - g.ym, g.dxldy);
+		if (ys < g.ym) xl = xm;
+		xl = bfe_s(xl, 27);
+		xh = bfe_s(xh, 27);
+		int hs = quantize_x(xh), ls = quantize_x(xl);
+		int l = flip ? hs : ls, r = flip ? ls : hs;
+		bool invalid = ((l >> 1) > (r >> 1)) || clip_y;
+		all_over = all_over && (min(l, r) >= hi_sc);
+		all_under = all_under && (max(l, r) < lo_sc);
+		l = min(max(l, lo_sc), hi_sc);
+		r = min(max(r, lo_sc), hi_sc);
+		if (invalid) { l = 0xffff; r = 0; }
+		all_invalid = all_invalid && invalid;
+		out.xl[k] = uint16_t(l);
+		out.xr[k] = uint16_t(r);
+		mn = min(mn, l);
+		mx = max(mx, r);
+	}
+	out.start_x = mn >> 3;
+	out.end_x = mx >> 3;
+	bool valid = !all_invalid && !all_over && !all_under;
+	if ((g.flags & TRI_INTERLACE_FIELD) && ((y & 1) != int((g.flags & TRI_INTERLACE_KEEP_ODD) != 0))) valid = false;
+	out.valid = valid ? 1 : 0;
+}
+
+// ============================================================================ k_raster: per-pixel maths
+__device__ __forceinline__ int clamp_9bit(int c) { return clampi(bfe_s(c - 0x80, 9) + 0x80, 0, 0xff); }
+__device__ __forceinline__ int special_expand(int v) { return bfe_s(v - 0x80, 9) + 0x80; }
+
+__device__ __forceinline__ int clamp_z(int z)
+{
+	z -= 1 << 17;
+	z = int(unsigned(z) << 13) >> 13;
+	z += 1 << 17;
+	return clampi(z, 0, 0x3ffff);
+}
+
+__device__ __forceinline__ uint32_t reseed_noise(uint32_t x, uint32_t y, uint32_t p)
+{
+	const uint32_t P = 1103515245u;
+	uint32_t s0 = x, s1 = y, s2 = p;
+#pragma unroll
+	for (int k = 0; k < 3; k++)
+	{
+		uint32_t n0 = ((s0 >> 8) ^ s1) * P;
+		uint32_t n1 = ((s1 >> 8) ^ s2) * P;
+		uint32_t n2 = ((s2 >> 8) ^ s0) * P;
+		s0 = n0; s1 = n1; s2 = n2;
+	}
+	return s0 >> 16;
+}
+
+__device__ void persp_divide(int s, int t, int w, int &os, int &ot, bool &overflow)
+{
+	bool w_carry = w <= 0;
+	w &= 0x7fff;
+	int shift = min(14 - find_msb(w), 14);
+	int normout = shlw(w, shift) & 0x3fff;
+	int wnorm = normout & 0xff;
+	int idx = normout >> 8;
+	int rcp = ((-int(g_persp_slope[idx]) * 4 * wnorm) >> 10) + g_persp_base[idx];
+	int prod0 = mulw(s, rcp), prod1 = mulw(t, rcp);
+	int temp_mask = ((1 << 30) - 1) & -((1 << 29) >> shift);
+	int oob0 = prod0 & temp_mask, oob1 = prod1 & temp_mask;
+	int t0, t1;
+	if (shift != 14)
+	{
+		t0 = prod0 = prod0 >> (13 - shift);
+		t1 = prod1 = prod1 >> (13 - shift);
+	}
+	else
+	{
+		t0 = shlw(prod0, 1);
+		t1 = shlw(prod1, 1);
+	}
+	if (oob0 != 0 && oob0 != temp_mask)
+	{
+		t0 = (prod0 & (1 << 29)) == 0 ? 0x7fff : -0x8000;
+		overflow = true;
+	}
+	if (oob1 != 0 && oob1 != temp_mask)
+	{
+		t1 = (prod1 & (1 << 29)) == 0 ? 0x7fff : -0x8000;
+		overflow = true;
+	}
+	if (w_carry)
+	{
+		t0 = t1 = 0x7fff;
+		overflow = true;
+	}
+	os = clampi(t0, -0x10000, 0xffff);
+	ot = clampi(t1, -0x10000, 0xffff);
+}
+
+__device__ __forceinline__ void st_div(int s, int t, int w, bool persp, int &os, int &ot, bool &ov)
+{
+	if (persp) persp_divide(s, t, w, os, ot, ov);
+	else { os = s; ot = t; }
+}
+
+// ---------------------------------------------------------------------------- textures (texture.h)
+struct T4 { int v[4]; };
+
+__device__ __forceinline__ uint32_t tm16(const uint16_t *tm, uint32_t i) { return __ldg(tm + (i & 2047)); }
+__device__ __forceinline__ uint32_t tm8(const uint16_t *tm, uint32_t i) { return (tm16(tm, i >> 1) >> ((i & 1) * 8)) & 0xff; }
+
+__device__ __forceinline__ T4 cvt_rgba16(uint32_t w)
+{
+	T4 r;
+#pragma unroll
+	for (int c = 0; c < 3; c++)
+	{
+		uint32_t x = (w >> (11 - 5 * c)) & 31u;
+		r.v[c] = int((x << 3) | (x >> 2));
+	}
+	r.v[3] = int((w & 1u) * 0xffu);
+	return r;
+}
+__device__ __forceinline__ T4 cvt_ia16(uint32_t w)
+{
+	int i = int(w >> 8), al = int(w & 0xff);
+	return { { i, i, i, al } };
+}
+__device__ __forceinline__ T4 splat4(int v) { return { { v, v, v, v } }; }
+
+__device__ __forceinline__ uint32_t byte_idx(const RdpTile &t, int sb, int tv, uint32_t wrap)
+{
+	uint32_t off = (t.offset + t.stride * uint32_t(tv) + uint32_t(sb)) & wrap;
+	return (off ^ ((uint32_t(tv) & 1u) << 2)) ^ 3u;
+}
+__device__ __forceinline__ uint32_t hw_idx(const RdpTile &t, int s, int tv, uint32_t wrap)
+{
+	uint32_t off = (t.offset + t.stride * uint32_t(tv) + uint32_t(s) * 2u) & wrap;
+	return ((off >> 1) ^ ((uint32_t(tv) & 1u) << 1)) ^ 1u;
+}
+
+__device__ T4 fetch_texel(const uint16_t *tm, const RdpTile &t, int s, int tv, bool tlut, bool tlut_type, uint32_t lut_off,
+                          uint32_t ax)
+{
+	if (tlut)
+	{
+		uint32_t w;
+		switch (t.size)
+		{
+		case 0:
+		{
+			uint32_t idx = byte_idx(t, s >> 1, tv, 0x7ff);
+			uint32_t v = (tm8(tm, idx) >> ((~uint32_t(s) & 1u) * 4)) & 0xf;
+			v |= uint32_t(t.palette) << 4;
+			w = tm16(tm, 0x400 | (((v << 2) + lut_off) ^ ax));
+			break;
+		}
+		case 1:
+		{
+			uint32_t v = tm8(tm, byte_idx(t, s, tv, 0x7ff));
+			w = tm16(tm, 0x400 | (((v << 2) + lut_off) ^ ax));
+			break;
+		}
+		default:
+		{
+			uint32_t v = tm16(tm, hw_idx(t, s, tv, 0x7ff));
+			w = tm16(tm, 0x400 | ((((v >> 6) & ~3u) + lut_off) ^ ax));
+			break;
+		}
+		}
+		return tlut_type ? cvt_ia16(w) : cvt_rgba16(w);
+	}
+	switch (t.fmt)
+	{
+	case 0: // RGBA
+		switch (t.size)
+		{
+		case 0:
+		{
+			uint32_t v = (tm8(tm, byte_idx(t, s >> 1, tv, 0xfff)) >> ((~uint32_t(s) & 1u) * 4)) & 0xf;
+			return splat4(int(v | (v << 4)));
+		}
+		case 1: return splat4(int(tm8(tm, byte_idx(t, s, tv, 0xfff))));
+		case 2: return cvt_rgba16(tm16(tm, hw_idx(t, s, tv, 0xfff)));
+		default:
+		{
+			uint32_t idx = hw_idx(t, s, tv, 0x7ff) & 2047;
+			uint32_t lo = tm16(tm, idx), hi = tm16(tm, idx | 0x400);
+			return { { int(lo >> 8), int(lo & 0xff), int(hi >> 8), int(hi & 0xff) } };
+		}
+		}
+	case 2: // CI
+		switch (t.size)
+		{
+		case 0:
+		{
+			uint32_t v = (tm8(tm, byte_idx(t, s >> 1, tv, 0xfff)) >> ((~uint32_t(s) & 1u) * 4)) & 0xf;
+			return splat4(int(v | (uint32_t(t.palette) << 4)));
+		}
+		case 1: return splat4(int(tm8(tm, byte_idx(t, s, tv, 0xfff))));
+		default:
+		{
+			uint32_t v = tm16(tm, hw_idx(t, s, tv, 0xfff));
+			int x = int(v >> 8), y = int(v & 0xff);
+			return { { x, y, x, y } };
+		}
+		}
+	case 3: // IA
+		switch (t.size)
+		{
+		case 0:
+		{
+			uint32_t v = (tm8(tm, byte_idx(t, s >> 1, tv, 0xfff)) >> ((~uint32_t(s) & 1u) * 4)) & 0xf;
+			uint32_t i = v & 0xe;
+			i = (i << 4) | (i << 1) | (i >> 2);
+			return { { int(i), int(i), int(i), int((v & 1) * 0xff) } };
+		}
+		case 1:
+		{
+			uint32_t v = tm8(tm, byte_idx(t, s, tv, 0xfff));
+			uint32_t i = v >> 4, al = v & 0xf;
+			al |= al << 4;
+			i |= i << 4;
+			return { { int(i), int(i), int(i), int(al) } };
+		}
+		case 2: return cvt_ia16(tm16(tm, hw_idx(t, s, tv, 0xfff)));
+		default:
+		{
+			uint32_t v = tm16(tm, hw_idx(t, s, tv, 0xfff));
+			int x = int(v >> 8), y = int(v & 0xff);
+			return { { x, y, x, y } };
+		}
+		}
+	case 4: // I
+		switch (t.size)
+		{
+		case 0:
+		{
+			uint32_t v = (tm8(tm, byte_idx(t, s >> 1, tv, 0xfff)) >> ((~uint32_t(s) & 1u) * 4)) & 0xf;
+			return splat4(int(v | (v << 4)));
+		}
+		case 1: return splat4(int(tm8(tm, byte_idx(t, s, tv, 0xfff))));
+		default:
+		{
+			uint32_t v = tm16(tm, hw_idx(t, s, tv, 0xfff));
+			int x = int(v >> 8), y = int(v & 0xff);
+			return { { x, y, x, y } };
+		}
+		}
+	default:
+		return { { 0, 0, 0, 0 } };
+	}
+}
+
+__device__ T4 texel_yuv(const uint16_t *tm, const RdpTile &t, int s, int tv, uint32_t chroma_x)
+{
+	uint32_t base = t.offset + t.stride * uint32_t(tv);
+	uint32_t ol = (base + uint32_t(s)) & 0x7ff;
+	uint32_t oc = (base + chroma_x * 2) & 0x7ff;
+	uint32_t il = (ol ^ ((uint32_t(tv) & 1u) << 2)) ^ 3u;
+	uint32_t ic = ((oc >> 1) ^ ((uint32_t(tv) & 1u) << 1)) ^ 1u;
+	int luma = int(tm8(tm, il | 0x800));
+	uint32_t chroma = tm16(tm, ic);
+	return { { int((chroma >> 8) & 0xff) - 0x80, int(chroma & 0xff) - 0x80, luma, luma } };
+}
+
+__device__ __forceinline__ int tex_mask(int v, int mask_bits, bool mirror)
+{
+	if (mask_bits != 0)
+	{
+		int m = 1 << mask_bits;
+		if (mirror) v ^= max((v & m) - 1, 0);
+		v &= m - 1;
+	}
+	return v;
+}
+
+__device__ __forceinline__ int clamp_shift(bool clamp_bit, int coord, int lo, int hi, int shift)
+{
+	coord = clampi(coord, -0x8000, 0x7fff);
+	if (shift < 11) coord >>= shift;
+	else coord = int(unsigned(coord) << (32 - shift)) >> 16;
+	if (clamp_bit)
+	{
+		if ((coord >> 3) >= hi) coord = (((hi >> 2) - (lo >> 2)) & 0x3ff) << 5;
+		else coord = max(coord - (lo << 3), 0);
+	}
+	else
+		coord -= lo << 3;
+	return coord;
+}
+
+__device__ __forceinline__ int shift_only(int coord, int lo, int shift)
+{
+	coord = clampi(coord, -0x8000, 0x7fff);
+	if (shift < 11) coord >>= shift;
+	else coord = int(unsigned(coord) << (32 - shift)) >> 16;
+	return coord - (lo << 3);
+}
+
+__device__ __forceinline__ T4 convert_factors(const T4 &in, const int16_t f[4])
+{
+	int x0 = bfe_s(in.v[0], 9), x1 = bfe_s(in.v[1], 9), x2 = bfe_s(in.v[2], 9);
+	T4 r;
+	r.v[0] = x2 + ((f[0] * x1 + 0x80) >> 8);
+	r.v[1] = x2 + ((f[1] * x0 + f[2] * x1 + 0x80) >> 8);
+	r.v[2] = x2 + ((f[3] * x0 + 0x80) >> 8);
+	r.v[3] = x2;
+	return r;
+}
+
+// texture.h:498-923
+__device__ T4 sample_texture(const uint16_t *tm, const RdpTile &t, int s_in, int t_in, bool tlut, bool tlut_type,
+                             bool sample_quad, bool mid_state, bool convert_one, bool bilerp, const int16_t *factors,
+                             const T4 &prev)
+{
+	int st0 = clamp_shift((t.flags & TIF_CLAMP_S) != 0, s_in, int(t.slo), int(t.shi), t.shift_s);
+	int st1 = clamp_shift((t.flags & TIF_CLAMP_T) != 0, t_in, int(t.tlo), int(t.thi), t.shift_t);
+	int fx = 0, fy = 0;
+	if (sample_quad || tlut) { fx = st0 & 31; fy = st1 & 31; }
+	int sum_frac = fx + fy;
+	st0 >>= 5;
+	st1 >>= 5;
+	bool ms = (t.flags & TIF_MIRROR_S) != 0, mt = (t.flags & TIF_MIRROR_T) != 0;
+	int s0 = tex_mask(st0, t.mask_s, ms), t0 = tex_mask(st1, t.mask_t, mt);
+	int s1 = tex_mask(st0 + 1, t.mask_s, ms), t1 = tex_mask(st1 + 1, t.mask_t, mt);
+	int tdiff = max(t1 - t0, -255);
+	t1 = (t0 & 0xff) + tdiff;
+	t0 &= 0xff;
+
+	T4 tb = { { 0, 0, 0, 0 } }, t10 = tb, t01 = tb, t11 = tb;
+	bool mid = mid_state && bilerp && fx == 0x10 && fy == 0x10;
+	bool upper_lut = sum_frac >= 0x20;
+	if (mid) sum_frac = 0;
+	bool yuv = t.fmt == 1;
+	int bs = sum_frac >= 0x20 ? s1 : s0;
+	int bt = sum_frac >= 0x20 ? t1 : t0;
+	int chroma_frac = ((s0 & 1) << 4) | (fx >> 1);
+
+	if (tlut)
+	{
+		if (!sample_quad) { bs = s0; bt = t0; s1 = s0; t1 = t0; }
+		if (t.fmt != 1)
+		{
+			bool upper = sum_frac >= 0x20;
+			uint32_t ax = upper_lut ? 2 : 1;
+			tb = fetch_texel(tm, t, bs, bt, true, tlut_type, upper ? 3 : 0, ax);
+			if (bilerp)
+			{
+				t10 = fetch_texel(tm, t, s1, t0, true, tlut_type, 1, ax);
+				t01 = fetch_texel(tm, t, s0, t1, true, tlut_type, 2, ax);
+			}
+			if (mid) t11 = fetch_texel(tm, t, s1, t1, true, tlut_type, 3, ax);
+		}
+	}
+	else if (yuv)
+	{
+		uint32_t cx0 = uint32_t(s0 >> 1), cx1 = uint32_t((s1 + (s1 - s0)) >> 1);
+		tb = texel_yuv(tm, t, s0, t0, cx0);
+		if (sample_quad)
+		{
+			t10 = texel_yuv(tm, t, s1, t0, cx1);
+			t01 = texel_yuv(tm, t, s0, t1, cx0);
+			t11 = texel_yuv(tm, t, s1, t1, cx1);
+		}
+	}
+	else if (t.fmt <= 4)
+	{
+		tb = fetch_texel(tm, t, bs, bt, false, false, 0, 0);
+		if (sample_quad)
+		{
+			t10 = fetch_texel(tm, t, s1, t0, false, false, 0, 0);
+			t01 = fetch_texel(tm, t, s0, t1, false, false, 0, 0);
+		}
+		if (mid) t11 = fetch_texel(tm, t, s1, t1, false, false, 0, 0);
+	}
+
+	T4 acc;
+	if (convert_one)
+	{
+		int ps[4];
+#pragma unroll
+		for (int i = 0; i < 4; i++) ps[i] = bfe_s(prev.v[i], 9);
+		if (sample_quad)
+		{
+			bool mid_rg = yuv ? (mid_state && chroma_frac == 0x10 && fy == 0x10) : mid;
+			bool mid_ba = mid;
+			bool upper_ba = sum_frac >= 32;
+			bool upper_rg = yuv ? ((chroma_frac + fy) >= 32 && !mid_rg) : upper_ba;
+			int frg0 = upper_rg ? ps[1] : ps[0], frg1 = upper_rg ? ps[0] : ps[1];
+			int fba0 = upper_ba ? ps[1] : ps[0], fba1 = upper_ba ? ps[0] : ps[1];
+#pragma unroll
+			for (int i = 0; i < 4; i++)
+			{
+				bool m = i < 2 ? mid_rg : mid_ba;
+				bool up = i < 2 ? upper_rg : upper_ba;
+				int f0 = i < 2 ? frg0 : fba0, f1 = i < 2 ? frg1 : fba1;
+				int cv;
+				if (m)
+					cv = f0 * (t01.v[i] - t11.v[i]) + f1 * (t10.v[i] - t11.v[i]) + ((tb.v[i] - t11.v[i]) << 6) + 0x80;
+				else
+				{
+					int base = (up && yuv) ? t11.v[i] : tb.v[i];
+					cv = f0 * (t10.v[i] - base) + f1 * (t01.v[i] - base) + 0x80;
+				}
+				acc.v[i] = (cv >> 8) + ps[2];
+			}
+		}
+		else
+			acc = splat4(ps[2]);
+	}
+	else if (yuv)
+	{
+		if (sample_quad)
+		{
+			int ch[2], lu[2];
+			if (bilerp)
+			{
+				bool mid_chroma = mid_state && chroma_frac == 0x10 && fy == 0x10;
+				for (int i = 0; i < 2; i++)
+				{
+					if (mid_chroma) ch[i] = (tb.v[i] + t10.v[i] + t11.v[i] + t01.v[i] + 2) >> 2;
+					else
+					{
+						int sum = chroma_frac + fy;
+						int base = sum >= 32 ? t11.v[i] : tb.v[i];
+						int ffx = sum >= 32 ? 32 - fy : chroma_frac, ffy = sum >= 32 ? 32 - chroma_frac : fy;
+						ch[i] = (((t10.v[i] - base) * ffx + (t01.v[i] - base) * ffy + 0x10) >> 5) + base;
+					}
+					if (mid) lu[i] = (tb.v[2 + i] + t10.v[2 + i] + t11.v[2 + i] + t01.v[2 + i] + 2) >> 2;
+					else
+					{
+						int sum = fx + fy;
+						int base = sum >= 32 ? t11.v[2 + i] : tb.v[2 + i];
+						int ffx = sum >= 32 ? 32 - fy : fx, ffy = sum >= 32 ? 32 - fx : fy;
+						lu[i] = (((t10.v[2 + i] - base) * ffx + (t01.v[2 + i] - base) * ffy + 0x10) >> 5) + base;
+					}
+				}
+			}
+			else
+			{
+				for (int i = 0; i < 2; i++)
+				{
+					lu[i] = (fx + fy >= 32) ? t11.v[2 + i] : tb.v[2 + i];
+					ch[i] = (chroma_frac + fy >= 32) ? t11.v[i] : tb.v[i];
+				}
+			}
+			acc = { { ch[0], ch[1], lu[0], lu[1] } };
+		}
+		else
+			acc = tb;
+	}
+	else if (mid)
+	{
+#pragma unroll
+		for (int i = 0; i < 4; i++) acc.v[i] = (tb.v[i] + t01.v[i] + t10.v[i] + t11.v[i] + 2) >> 2;
+	}
+	else if (bilerp && (sample_quad || tlut))
+	{
+		int ffx = sum_frac >= 32 ? 32 - fy : fx;
+		int ffy = sum_frac >= 32 ? 32 - fx : fy;
+#pragma unroll
+		for (int i = 0; i < 4; i++)
+			acc.v[i] = (((t10.v[i] - tb.v[i]) * ffx + (t01.v[i] - tb.v[i]) * ffy + 0x10) >> 5) + tb.v[i];
+	}
+	else
+		acc = tb;
+
+	if (!bilerp && !convert_one) acc = convert_factors(acc, factors);
+	return acc;
+}
+
+// texture.h:361-472 (copy pipe)
+__device__ int copy_word(const uint16_t *tm, const RdpTile &t, int st0, int st1, int s_offset, bool tlut)
+{
+	bool replicate = s_offset < 2 && t.size != 2 && !tlut;
+	int s_shamt = min(int(t.size), 2);
+	uint32_t idx_mask = (t.size == 3 || tlut) ? 0x3ffu : 0x7ffu;
+	bool ms = (t.flags & TIF_MIRROR_S) != 0, mt = (t.flags & TIF_MIRROR_T) != 0;
+	int samp;
+	if (replicate)
+	{
+		st0 += 2 * s_offset;
+		int sa = tex_mask(st0, t.mask_s, ms), sbv = tex_mask(st0 + 1, t.mask_s, ms);
+		int tv = tex_mask(st1, t.mask_t, mt);
+		uint32_t tbase = t.offset + t.stride * uint32_t(tv);
+		uint32_t na = ((tbase * 2 + (uint32_t(sa) << s_shamt)) & 0x1fffu) ^ ((uint32_t(tv) & 1u) * 8u);
+		uint32_t nb = ((tbase * 2 + (uint32_t(sbv) << s_shamt)) & 0x1fffu) ^ ((uint32_t(tv) & 1u) * 8u);
+		int v0 = int(tm16(tm, ((na >> 2) & idx_mask) ^ 1));
+		int v1 = int(tm16(tm, ((nb >> 2) & idx_mask) ^ 1));
+		if (t.size == 1)
+		{
+			v0 = (v0 >> (8 - 4 * int(na & 2))) & 0xff;
+			v1 = (v1 >> (8 - 4 * int(nb & 2))) & 0xff;
+		}
+		else if (t.size == 0)
+		{
+			v0 = ((v0 >> (12 - 4 * int(na & 3u))) & 0xf) * 0x11;
+			v1 = ((v1 >> (12 - 4 * int(nb & 3u))) & 0xf) * 0x11;
+		}
+		else
+		{
+			v0 >>= 8;
+			v1 >>= 8;
+		}
+		samp = (v0 << 8) | v1;
+	}
+	else
+	{
+		st0 += s_offset;
+		int s = tex_mask(st0, t.mask_s, ms);
+		int tv = tex_mask(st1, t.mask_t, mt);
+		uint32_t tbase = t.offset + t.stride * uint32_t(tv);
+		uint32_t nib = ((tbase * 2 + (uint32_t(s) << s_shamt)) & 0x1fffu) ^ ((uint32_t(tv) & 1u) * 8u);
+		samp = int(tm16(tm, ((nib >> 2) & idx_mask) ^ 1));
+		if (tlut)
+		{
+			if (t.size == 0)
+			{
+				samp = (samp >> (12 - 4 * int(nib & 3))) & 0xf;
+				samp |= int(t.palette) << 4;
+			}
+			else
+				samp = (samp >> (8 - 4 * int(nib & 2))) & 0xff;
+			samp = (samp << 2) + s_offset;
+			samp = int(tm16(tm, (uint32_t(samp) | 0x400u) ^ 1u));
+		}
+	}
+	return samp;
+}
+
+// ---------------------------------------------------------------------------- combiner (combiner.h)
+struct CombIn
+{
+	const uint8_t *cma, *cms, *cmu, *cad;
+	int shade[4], comb[4], tex0[4], tex1[4];
+	int lod_frac, noise;
+};
+
+__device__ void combine(const CombIn &in, const uint8_t *rs, const uint8_t *as, int out[4])
+{
+#pragma unroll
+	for (int c = 0; c < 4; c++)
+	{
+		int a, b, m, d;
+		if (c < 3)
+		{
+			switch (rs[0])
+			{
+			case 0: a = in.comb[c]; break;
+			case 1: a = in.tex0[c]; break;
+			case 2: a = in.tex1[c]; break;
+			case 4: a = in.shade[c]; break;
+			case 7: a = in.noise; break;
+			case 6: a = 0x100; break;
+			default: a = in.cma[c]; break;
+			}
+			switch (rs[1])
+			{
+			case 0: b = in.comb[c]; break;
+			case 1: b = in.tex0[c]; break;
+			case 2: b = in.tex1[c]; break;
+			case 4: b = in.shade[c]; break;
+			case 7: b = (int(in.cms[1]) << 8) | in.cms[2]; break;
+			default: b = in.cms[c]; break;
+			}
+			switch (rs[2])
+			{
+			case 0: m = in.comb[c]; break;
+			case 7: m = in.comb[3]; break;
+			case 1: m = in.tex0[c]; break;
+			case 2: m = in.tex1[c]; break;
+			case 4: m = in.shade[c]; break;
+			case 8: m = in.tex0[3]; break;
+			case 9: m = in.tex1[3]; break;
+			case 11: m = in.shade[3]; break;
+			case 13: m = in.lod_frac; break;
+			case 15: m = (int(in.cmu[1]) << 8) | in.cmu[2]; break;
+			default: m = in.cmu[c]; break;
+			}
+			switch (rs[3])
+			{
+			case 0: d = in.comb[c]; break;
+			case 1: d = in.tex0[c]; break;
+			case 2: d = in.tex1[c]; break;
+			case 4: d = in.shade[c]; break;
+			case 6: d = 0x100; break;
+			default: d = in.cad[c]; break;
+			}
+		}
+		else
+		{
+			switch (as[0])
+			{
+			case 0: a = in.comb[3]; break;
+			case 1: a = in.tex0[3]; break;
+			case 2: a = in.tex1[3]; break;
+			case 4: a = in.shade[3]; break;
+			case 6: a = 0x100; break;
+			default: a = in.cma[3]; break;
+			}
+			switch (as[1])
+			{
+			case 0: b = in.comb[3]; break;
+			case 1: b = in.tex0[3]; break;
+			case 2: b = in.tex1[3]; break;
+			case 4: b = in.shade[3]; break;
+			case 6: b = 0x100; break;
+			default: b = in.cms[3]; break;
+			}
+			switch (as[2])
+			{
+			case 0: m = in.lod_frac; break;
+			case 1: m = in.tex0[3]; break;
+			case 2: m = in.tex1[3]; break;
+			case 4: m = in.shade[3]; break;
+			default: m = in.cmu[3]; break;
+			}
+			switch (as[3])
+			{
+			case 0: d = in.comb[3]; break;
+			case 1: d = in.tex0[3]; break;
+			case 2: d = in.tex1[3]; break;
+			case 4: d = in.shade[3]; break;
+			case 6: d = 0x100; break;
+			default: d = in.cad[3]; break;
+			}
+		}
+		int col = (special_expand(a) - special_expand(b)) * bfe_s(m, 9);
+		col += 0x80;
+		out[c] = (col >> 8) + special_expand(d);
+	}
+}
+
+// ---------------------------------------------------------------------------- z encode / depth test / blender
+__device__ __forceinline__ int z_decompress(int z)
+{
+	int e = z >> 11, m = z & 0x7ff;
+	return (m << max(6 - e, 0)) + (0x40000 - (0x40000 >> e));
+}
+__device__ __forceinline__ int z_compress(int z)
+{
+	int inv = max(0x3ffff - z, 1);
+	int e = clampi(17 - find_msb(inv), 0, 7);
+	int m = (z >> max(6 - e, 0)) & 0x7ff;
+	return ((e << 11) + m) & 0xffff;
+}
+
+struct Pix
+{
+	int col[4];
+	int depth, dz;
+	bool cdirty, ddirty;
+	uint32_t cidx;
+};
+
+__device__ void blender(const int pix[4], const int mem[4], const uint8_t fog[4], const uint8_t bc[4], int shade_alpha,
+                        const uint8_t *m, bool force_blend, bool blend_en, bool color_on_cvg, bool cvg_wrap,
+                        const int bshift[2], bool final_cycle, int out[3])
+{
+	int r1[3], r0[3];
+#pragma unroll
+	for (int c = 0; c < 3; c++)
+	{
+		switch (m[2])
+		{
+		case 0: r1[c] = pix[c]; break;
+		case 1: r1[c] = mem[c]; break;
+		case 2: r1[c] = bc[c]; break;
+		default: r1[c] = fog[c]; break;
+		}
+		switch (m[0])
+		{
+		case 0: r0[c] = pix[c]; break;
+		case 1: r0[c] = mem[c]; break;
+		case 2: r0[c] = bc[c]; break;
+		default: r0[c] = fog[c]; break;
+		}
+	}
+	if (final_cycle && color_on_cvg && !cvg_wrap)
+	{
+		out[0] = r1[0]; out[1] = r1[1]; out[2] = r1[2];
+		return;
+	}
+	if (final_cycle && (!blend_en || (m[1] == 0 && m[3] == 0 && pix[3] == 0xff)))
+	{
+		out[0] = r0[0]; out[1] = r0[1]; out[2] = r0[2];
+		return;
+	}
+	int a0, a1;
+	switch (m[1])
+	{
+	case 0: a0 = pix[3]; break;
+	case 1: a0 = fog[3]; break;
+	case 2: a0 = shade_alpha; break;
+	default: a0 = 0; break;
+	}
+	switch (m[3])
+	{
+	case 0: a1 = ~a0 & 0xff; break;
+	case 1: a1 = mem[3]; break;
+	case 2: a1 = 0xff; break;
+	default: a1 = 0; break;
+	}
+	a0 >>= 3;
+	a1 >>= 3;
+	if (m[3] == 1)
+	{
+		a0 = (a0 >> bshift[0]) & 0x3c;
+		a1 = (a1 >> bshift[1]) | 3;
+	}
+	if (!final_cycle || force_blend)
+	{
+#pragma unroll
+		for (int c = 0; c < 3; c++) out[c] = ((r0[c] * a0 + r1[c] * (a1 + 1)) >> 5) & 0xff;
+	}
+	else
+	{
+		int sum = (a0 >> 2) + (a1 >> 2) + 1;
+#pragma unroll
+		for (int c = 0; c < 3; c++)
+		{
+			int v = ((r0[c] * a0 + r1[c] * (a1 + 1)) >> 2) & 0x7ff;
+			out[c] = g_blender_lut[((sum << 11) | v) & 0x7fff];
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------- RDRAM framebuffer I/O
+__device__ __forceinline__ uint16_t ld16(const RdpPass &p, uint32_t i)
+{
+	return *reinterpret_cast<const uint16_t *>(p.rdram + ((i * 2) & (p.rdram_size - 1)));
+}
+__device__ __forceinline__ void st16(const RdpPass &p, uint32_t i, uint16_t v)
+{
+	*reinterpret_cast<uint16_t *>(p.rdram + ((i * 2) & (p.rdram_size - 1))) = v;
+}
+__device__ __forceinline__ uint8_t hid(const RdpPass &p, uint32_t i) { return p.hidden[i & (p.hidden_size - 1)]; }
+__device__ __forceinline__ void whid(const RdpPass &p, uint32_t i, uint8_t v) { p.hidden[i & (p.hidden_size - 1)] = v; }
+
+__device__ void load_pixel(const RdpPass &p, Pix &px, uint32_t ci, uint32_t di)
+{
+	px.cidx = ci;
+	px.cdirty = px.ddirty = false;
+	switch (p.fb_fmt)
+	{
+	case FBF_I4:
+	case FBF_I8:
+	{
+		uint32_t idx = ci & (p.rdram_size - 1);
+		int w = p.rdram[idx ^ 3u];
+		px.col[0] = px.col[1] = px.col[2] = w;
+		px.col[3] = hid(p, idx >> 1);
+		break;
+	}
+	case FBF_RGBA5551:
+	{
+		uint32_t idx = ci & ((p.rdram_size >> 1) - 1);
+		uint32_t w = ld16(p, idx ^ 1u);
+		px.col[0] = int((w >> 8) & 0xf8u);
+		px.col[1] = int((w >> 3) & 0xf8u);
+		px.col[2] = int((w << 2) & 0xf8u);
+		px.col[3] = ((hid(p, idx) << 5) | int((w & 1) << 7)) & 0xff;
+		break;
+	}
+	case FBF_IA88:
+	{
+		uint32_t idx = ci & ((p.rdram_size >> 1) - 1);
+		uint32_t w = ld16(p, idx ^ 1u);
+		px.col[0] = px.col[1] = px.col[2] = int((w >> 8) & 0xff);
+		px.col[3] = int(w & 0xff);
+		break;
+	}
+	default:
+	{
+		uint32_t idx = ci & ((p.rdram_size >> 2) - 1);
+		uint32_t w = *reinterpret_cast<const uint32_t *>(p.rdram + idx * 4);
+#pragma unroll
+		for (int c = 0; c < 4; c++) px.col[c] = int((w >> (24 - 8 * c)) & 0xff);
+		break;
+	}
+	}
+	uint32_t didx = di & ((p.rdram_size >> 1) - 1);
+	uint32_t w = ld16(p, didx ^ 1u);
+	px.depth = int(w >> 2);
+	px.dz = (hid(p, didx) | int((w & 3) << 2)) & 0xff;
+}
+
+__device__ void store_pixel(const RdpPass &p, const Pix &px, uint32_t ci, uint32_t di, bool alias)
+{
+	if (px.cdirty)
+	{
+		switch (p.fb_fmt)
+		{
+		case FBF_I4:
+		{
+			uint32_t idx = ci & (p.rdram_size - 1);
+			p.rdram[idx ^ 3u] = 0;
+			if (idx & 1u) whid(p, idx >> 1, uint8_t(px.col[3]));
+			break;
+		}
+		case FBF_I8:
+		{
+			uint32_t idx = ci & (p.rdram_size - 1);
+			uint32_t col = (idx & 1) ? uint32_t(px.col[1]) : uint32_t(px.col[0]);
+			p.rdram[idx ^ 3u] = uint8_t(col);
+			if (idx & 1u) whid(p, idx >> 1, uint8_t((col & 1) * 3));
+			break;
+		}
+		case FBF_RGBA5551:
+		{
+			uint32_t idx = ci & ((p.rdram_size >> 1) - 1);
+			uint32_t cov = uint32_t(px.col[3]) >> 5;
+			uint32_t w = ((uint32_t(px.col[0]) & 0xf8u) << 8) | ((uint32_t(px.col[1]) & 0xf8u) << 3) |
+			             ((uint32_t(px.col[2]) & 0xf8u) >> 2) | (cov >> 2);
+			st16(p, idx ^ 1u, uint16_t(w));
+			whid(p, idx, uint8_t(cov & 3u));
+			break;
+		}
+		case FBF_IA88:
+		{
+			uint32_t idx = ci & ((p.rdram_size >> 1) - 1);
+			st16(p, idx ^ 1u, uint16_t((uint32_t(px.col[0]) << 8) | uint32_t(px.col[3])));
+			whid(p, idx, uint8_t((px.col[3] & 1) * 3));
+			break;
+		}
+		default:
+		{
+			uint32_t idx = ci & ((p.rdram_size >> 2) - 1);
+			uint32_t w = (uint32_t(px.col[0]) << 24) | (uint32_t(px.col[1]) << 16) | (uint32_t(px.col[2]) << 8) |
+			             uint32_t(px.col[3]);
+			*reinterpret_cast<uint32_t *>(p.rdram + idx * 4) = w;
+			whid(p, 2u * idx, uint8_t((px.col[1] & 1) * 3));
+			whid(p, 2u * idx + 1u, uint8_t((px.col[3] & 1) * 3));
+			break;
+		}
+		}
+	}
+	if (!alias && px.ddirty)
+	{
+		uint32_t idx = di & ((p.rdram_size >> 1) - 1);
+		st16(p, idx ^ 1u, uint16_t((px.depth << 2) | (px.dz >> 2)));
+		whid(p, idx, uint8_t(px.dz & 3));
+	}
+}
+
+__device__ void alias_c2d(uint32_t fmt, Pix &px)
+{
+	if (fmt == FBF_RGBA5551)
+	{
+		px.dz = ((px.col[3] >> 3) | (px.col[2] & 8)) & 0xff;
+		uint32_t w = ((uint32_t(px.col[0]) & 0xf8u) << 6) | ((uint32_t(px.col[1]) & 0xf8u) << 1) |
+		             ((uint32_t(px.col[2]) & 0xf8u) >> 4);
+		px.depth = int(w & 0xffff);
+	}
+	else if (fmt == FBF_IA88)
+	{
+		uint32_t w = (uint32_t(px.col[0]) << 8) | uint32_t(px.col[3]);
+		px.depth = int((w >> 2) & 0xffff);
+		px.dz = int((((w & 3u) << 2) | ((w & 1u) * 3u)) & 0xff);
+	}
+}
+
+__device__ void alias_d2c(uint32_t fmt, Pix &px)
+{
+	uint32_t w = (uint32_t(px.depth) << 4) | uint32_t(px.dz);
+	if (fmt == FBF_RGBA5551)
+	{
+		px.col[0] = int((w >> 10) & 0xf8u);
+		px.col[1] = int((w >> 5) & 0xf8u);
+		px.col[2] = int(w & 0xf8u);
+		px.col[3] = int((w & 7u) << 5);
+	}
+	else if (fmt == FBF_IA88)
+	{
+		px.col[0] = int((w >> 10) & 0xffu);
+		px.col[3] = int((w >> 2) & 0xffu);
+	}
+	px.cdirty = true;
+}
+
+__device__ __forceinline__ void write_color(uint32_t fmt, Pix &px, int r, int g, int b, int a)
+{
+	px.col[0] = r; px.col[1] = g; px.col[2] = b;
+	if (fmt != FBF_I4) px.col[3] = a;
+	px.cdirty = true;
+}
+
+// ---------------------------------------------------------------------------- per pixel: shade + blend
+struct PassConst
+{
+	int fb_size, dx_mask, dx_shift;
+	bool alias;
+};
+
+__device__ bool shade_and_blend(const RdpPass &ps, const PassConst &pc, const RdpPrimGeom &g, const RdpPrimAttr &a,
+                                const RdpPrimShade &sh, const RdpTile *tiles, const uint16_t *tm, const SpanA &sa,
+                                const SpanX &sx, const SpanA &sa_next, const SpanX &sx_next, int x, int y, Pix &px)
+{
+	if (!sx.valid) return false;
+	const uint32_t f = sh.static_flags;
+	const bool flip = (g.flags & TRI_FLIP) != 0;
+	const bool perspective = (f & RS_PERSPECTIVE) != 0;
+	uint32_t noise = 0;
+	if (f & RS_NEED_NOISE) noise = reseed_noise(uint32_t(x), uint32_t(y), sh.prim_index);
+
+	if (f & RS_COPY)
+	{
+		if (!(x >= sx.start_x && x <= sx.end_x)) return false;
+		int dxp = flip ? (x - sx.start_x) : (sx.end_x - x);
+		int s_offset = dxp - (dxp & pc.dx_mask);
+		int lerp_dx = (dxp >> pc.dx_shift) * (flip ? 1 : -1);
+		int s = (sa.stzw[0] + mulw(a.dstzw_dx[0] & ~0x1f, lerp_dx)) >> 16;
+		int t = (sa.stzw[1] + mulw(a.dstzw_dx[1] & ~0x1f, lerp_dx)) >> 16;
+		int w = (sa.stzw[3] + mulw(a.dstzw_dx[3] & ~0x1f, lerp_dx)) >> 16;
+		int os, ot;
+		bool ov = false;
+		st_div(s, t, w, perspective, os, ot, ov);
+		const RdpTile &t0 = tiles[g.tile & 7];
+		int st0 = shift_only(os, int(t0.slo), t0.shift_s) >> 5;
+		int st1 = shift_only(ot, int(t0.tlo), t0.shift_t) >> 5;
+		bool tlut = (f & RS_TLUT) != 0;
+		int texel;
+		if (pc.fb_size == 0) texel = 0;
+		else if (pc.fb_size == 1)
+			texel = (copy_word(tm, t0, st0, st1, s_offset >> 1, tlut) >> (8 - 8 * (s_offset & 1))) & 0xff;
+		else
+			texel = copy_word(tm, t0, st0, st1, s_offset, tlut);
+		if ((f & RS_ALPHA_TEST) && pc.fb_size == 2 && (texel & 1) == 0) return false;
+		// copy_pipeline (memory_interfacing.h:381-420)
+		uint32_t word = uint32_t(texel);
+		switch (ps.fb_fmt)
+		{
+		case FBF_I4: px.col[0] = px.col[1] = px.col[2] = px.col[3] = 0; px.cdirty = true; break;
+		case FBF_I8: { int v = int(word & 0xffu); write_color(ps.fb_fmt, px, v, v, v, v); break; }
+		case FBF_RGBA5551:
+			write_color(ps.fb_fmt, px, int((word >> 8) & 0xf8u), int((word >> 3) & 0xf8u), int((word << 2) & 0xf8u),
+			            int((word & 1) * 0xe0u));
+			break;
+		default: break;
+		}
+		if (pc.alias) alias_c2d(ps.fb_fmt, px);
+		return ps.fb_fmt == FBF_I4 || ps.fb_fmt == FBF_I8 || ps.fb_fmt == FBF_RGBA5551;
+	}
+	if (f & RS_FILL)
+	{
+		if (!(x >= sx.start_x && x <= sx.end_x)) return false;
+		// fill_color (memory_interfacing.h:440-486)
+		uint32_t col = sh.fill_color;
+		switch (ps.fb_fmt)
+		{
+		case FBF_RGBA8888:
+			write_color(ps.fb_fmt, px, int((col >> 24) & 0xff), int((col >> 16) & 0xff), int((col >> 8) & 0xff), int(col & 0xff));
+			break;
+		case FBF_RGBA5551:
+			col >>= ((px.cidx & 1u) ^ 1u) * 16u;
+			write_color(ps.fb_fmt, px, int((col >> 8) & 0xf8u), int((col >> 3) & 0xf8u), int((col << 2) & 0xf8u),
+			            int((col & 1u) * 0xe0u));
+			break;
+		case FBF_IA88:
+		{
+			col >>= ((px.cidx & 1u) ^ 1u) * 16u;
+			int r = int((col >> 8) & 0xff);
+			write_color(ps.fb_fmt, px, r, r, r, int(col & 0xff));
+			break;
+		}
+		case FBF_I8:
+		{
+			col >>= ((px.cidx & 3u) ^ 3u) * 8u;
+			int v = int(col & 0xff);
+			write_color(ps.fb_fmt, px, v, v, v, v);
+			break;
+		}
+		default: break;
+		}
+		if (pc.alias) alias_c2d(ps.fb_fmt, px);
+		return ps.fb_fmt != FBF_I4;
+	}
+
+	// ---- coverage (coverage.h:31-47)
+	int coverage;
+	{
+		int xs = x << 3;
+		int clip = 0;
+#pragma unroll
+		for (int k = 0; k < 4; k++)
+		{
+			int off = (k == 0) ? 0 : (k == 1 ? 4 : (k == 2 ? 2 : 6));
+			int xsh = xs + off;
+			int l0 = k >> 1, l1 = 2 + (k >> 1);
+			if (xsh < sx.xl[l0] || xsh >= sx.xr[l0]) clip |= 1 << k;
+			if (xsh < sx.xl[l1] || xsh >= sx.xr[l1]) clip |= 16 << k;
+		}
+		coverage = ~clip & 0xff;
+	}
+	if (coverage == 0) return false;
+	int cov_count = __popc(coverage);
+	const bool aa = (f & RS_AA) != 0;
+	if (!aa && (coverage & 1) == 0) return false;
+
+	int dx = x - sa.base_x;
+	int idir = flip ? 1 : -1;
+	int first = find_lsb(unsigned(coverage));
+	int yoff = first >> 1;
+	int xoff = ((first & 1) << 1) + (yoff & 1);
+
+	// ---- interpolate_rgba (interpolation.h:30-51)
+	int shade[4];
+#pragma unroll
+	for (int c = 0; c < 4; c++)
+	{
+		int v = sa.rgba[c] + mulw(a.drgba_dx[c] & ~0x1f, dx);
+		int sn = shlw(v >> 14, 2);
+		sn += xoff * (a.drgba_dx[c] >> 14) + yoff * (a.drgba_dy[c] >> 14);
+		sn >>= 4;
+		shade[c] = clamp_9bit(sn);
+	}
+
+	// ---- interpolate_stz (interpolation.h:92-142)
+	const bool uses_lod = (f & RS_USES_LOD) != 0;
+	int s0 = 0, t0v = 0, sdx = 0, tdx = 0, sdy = 0, tdy = 0, z;
+	bool povf = false;
+	{
+		int sw[3], idx3[3] = { 0, 1, 3 };
+#pragma unroll
+		for (int k = 0; k < 3; k++) sw[k] = sa.stzw[idx3[k]] + mulw(a.dstzw_dx[idx3[k]] & ~0x1f, dx);
+		if (f & (RS_USES_TEXEL0 | RS_USES_TEXEL1 | RS_USES_PIPELINED_TEXEL1 | RS_USES_LOD))
+		{
+			st_div(sw[0] >> 16, sw[1] >> 16, sw[2] >> 16, perspective, s0, t0v, povf);
+			if (uses_lod)
+			{
+				int wx[3], wy[3];
+#pragma unroll
+				for (int k = 0; k < 3; k++)
+				{
+					wx[k] = sw[k] + mulw(idir, a.dstzw_dx[idx3[k]] & ~0x1f);
+					wy[k] = sw[k] + (a.dstzw_dy[idx3[k]] & ~0x7fff);
+				}
+				st_div(wx[0] >> 16, wx[1] >> 16, wx[2] >> 16, perspective, sdx, tdx, povf);
+				st_div(wy[0] >> 16, wy[1] >> 16, wy[2] >> 16, perspective, sdy, tdy, povf);
+			}
+		}
+		z = sa.stzw[2] + mulw(a.dstzw_dx[2], dx);
+		int sz = shlw(z >> 10, 2);
+		sz += xoff * (a.dstzw_dx[2] >> 10) + yoff * (a.dstzw_dy[2] >> 10);
+		sz >>= 5;
+		z = clamp_z(sz);
+	}
+
+	// ---- LOD (texture.h:925-1003)
+	uint32_t tile0 = g.tile & 7u, tile1 = (tile0 + 1) & 7u, max_level = g.tile >> 3;
+	int lod_frac = 0;
+	if (uses_lod)
+	{
+		bool sharpen = (f & RS_SHARPEN) != 0, detail = (f & RS_DETAIL) != 0;
+		bool magnify = false, distant = false;
+		uint32_t tofs = 0;
+		if (povf)
+		{
+			distant = true;
+			lod_frac = 0xff;
+		}
+		else
+		{
+			int dxs = sdx - s0, dxt = tdx - t0v, dys = sdy - s0, dyt = tdy - t0v;
+			dxs ^= dxs >> 31; dxt ^= dxt >> 31; dys ^= dys >> 31; dyt ^= dyt >> 31;
+			int max_d = max(max(dxs, dys), max(dxt, dyt));
+			if (max_d >= 0x4000)
+			{
+				distant = true;
+				lod_frac = 0xff;
+				tofs = max_level;
+			}
+			else if (max_d < 32)
+			{
+				distant = max_level == 0u;
+				magnify = true;
+				if (!sharpen && !detail) lod_frac = distant ? 0xff : 0;
+				else lod_frac = (max(int(sh.min_lod), max_d) << 3) + (sharpen ? -0x100 : 0);
+			}
+			else
+			{
+				int mip_base = max(find_msb(max_d >> 5), 0);
+				distant = uint32_t(mip_base) >= max_level;
+				if (distant && !sharpen && !detail) lod_frac = 0xff;
+				else
+				{
+					lod_frac = ((max_d << 3) >> mip_base) & 0xff;
+					tofs = uint32_t(mip_base);
+				}
+			}
+		}
+		if (f & RS_TEX_LOD)
+		{
+			if (distant) tofs = max_level;
+			if (!detail)
+			{
+				tile0 = (tile0 + tofs) & 7u;
+				tile1 = (distant || (!sharpen && magnify)) ? tile0 : ((tile0 + 1) & 7u);
+			}
+			else
+			{
+				tile1 = (tile0 + tofs + ((distant || magnify) ? 1 : 2)) & 7u;
+				tile0 = (tile0 + tofs + (magnify ? 0 : 1)) & 7u;
+			}
+		}
+	}
+
+	// ---- texels
+	const bool tlut = (f & RS_TLUT) != 0, tlut_type = (f & RS_TLUT_TYPE) != 0;
+	const bool quad = (f & RS_SAMPLE_QUAD) != 0, midt = (f & RS_MID_TEXEL) != 0;
+	T4 tex0 = { { 0, 0, 0, 0 } }, tex1 = tex0;
+	if (f & RS_USES_TEXEL0)
+		tex0 = sample_texture(tm, tiles[tile0], s0, t0v, tlut, tlut_type, quad, midt, false, (f & RS_BILERP0) != 0,
+		                      sh.factors, tex0);
+	bool uses_t1 = (f & RS_USES_TEXEL1) != 0;
+	if (f & RS_USES_PIPELINED_TEXEL1)
+	{
+		int lodlength = int16_t(flip ? (sx.end_x - sa.base_x) : (sa.base_x - sx.start_x));
+		bool end_span = x == (flip ? sx.end_x : sx.start_x);
+		if (end_span && lodlength >= 8 && sx_next.valid)
+		{
+			bool dummy = false;
+			st_div(sa_next.stzw[0] >> 16, sa_next.stzw[1] >> 16, sa_next.stzw[3] >> 16, perspective, s0, t0v, dummy);
+		}
+		else
+		{
+			int ndx = dx + idir;
+			int ss = (sa.stzw[0] + mulw(a.dstzw_dx[0] & ~0x1f, ndx)) >> 16;
+			int tt = (sa.stzw[1] + mulw(a.dstzw_dx[1] & ~0x1f, ndx)) >> 16;
+			int ww = (sa.stzw[3] + mulw(a.dstzw_dx[3] & ~0x1f, ndx)) >> 16;
+			bool dummy = false;
+			st_div(ss, tt, ww, perspective, s0, t0v, dummy);
+		}
+		tile1 = tile0;
+		uses_t1 = true;
+	}
+	if (uses_t1)
+	{
+		bool c1 = (f & RS_CONVERT_ONE) != 0, b1 = (f & RS_BILERP1) != 0;
+		if (c1 && !b1) tex1 = convert_factors(tex0, sh.factors);
+		else tex1 = sample_texture(tm, tiles[tile1], s0, t0v, tlut, tlut_type, quad, midt, c1, b1, sh.factors, tex0);
+	}
+
+	// ---- dither coefficients (dither.h:39-68)
+	int rgb_d, alpha_d;
+	{
+		int yy = y >> int((f & RS_INTERLACE_FIELD) != 0);
+		int mr = int(sh.dither >> 2), ma = int(sh.dither & 3);
+		int cell = (yy & 3) * 4 + (x & 3);
+		if (mr < 2) rgb_d = g_dither[mr][cell] * (1 | 8 | 64);
+		else if (mr == 2) rgb_d = int(noise & 0x1ffu);
+		else rgb_d = 0;
+		if (ma == 3) alpha_d = 0;
+		else if (ma == 2) alpha_d = int(noise & 7u);
+		else
+		{
+			alpha_d = mr >= 2 ? g_dither[mr & 1][cell] : (rgb_d & 7);
+			if (ma == 1) alpha_d = ~alpha_d & 7;
+		}
+	}
+
+	// ---- combiner (shading.h:263-333, combiner.h:196-282)
+	const bool cvg_times_alpha = (f & RS_CVG_TIMES_ALPHA) != 0, alpha_cvg_select = (f & RS_ALPHA_CVG_SELECT) != 0;
+	const bool alpha_test = (f & RS_ALPHA_TEST) != 0;
+	int combined[4];
+	int alpha_ref = 0;
+	CombIn in;
+#pragma unroll
+	for (int c = 0; c < 4; c++)
+	{
+		in.shade[c] = shade[c];
+		in.comb[c] = 0;
+		in.tex0[c] = tex0.v[c];
+		in.tex1[c] = tex1.v[c];
+	}
+	in.lod_frac = lod_frac;
+	in.noise = int(((noise & 7u) << 6) | 0x20u);
+	if (f & RS_MULTI_CYCLE)
+	{
+		in.cma = sh.c_muladd[0]; in.cms = sh.c_mulsub[0]; in.cmu = sh.c_mul[0]; in.cad = sh.c_add[0];
+		int c0[4];
+		combine(in, sh.comb_rgb[0], sh.comb_alpha[0], c0);
+		if (alpha_test)
+		{
+			int ca = clamp_9bit(c0[3]);
+			int ea = ca + ((ca + 1) >> 8);
+			if (alpha_cvg_select) ea = cvg_times_alpha ? ((ea * cov_count + 4) >> 3) : (cov_count << 5);
+			else ea += alpha_d;
+			alpha_ref = clampi(ea, 0, 0xff);
+		}
+#pragma unroll
+		for (int c = 0; c < 4; c++)
+		{
+			in.comb[c] = c0[c];
+			int tmp = in.tex0[c];
+			in.tex0[c] = in.tex1[c];
+			in.tex1[c] = tmp;
+		}
+		in.cma = sh.c_muladd[1]; in.cms = sh.c_mulsub[1]; in.cmu = sh.c_mul[1]; in.cad = sh.c_add[1];
+		if (f & RS_NEED_NOISE_DUAL)
+		{
+			// The second seed also feeds the later alpha-test threshold (shading.h:309-347).
+			noise = reseed_noise(uint32_t(x + 1023), uint32_t(y + 7), sh.prim_index + 11);
+			in.noise = int(((noise & 7u) << 6) | 0x20u);
+		}
+		combine(in, sh.comb_rgb[1], sh.comb_alpha[1], combined);
+	}
+	else
+	{
+		in.cma = sh.c_muladd[1]; in.cms = sh.c_mulsub[1]; in.cmu = sh.c_mul[1]; in.cad = sh.c_add[1];
+		combine(in, sh.comb_rgb[1], sh.comb_alpha[1], combined);
+	}
+	// combiner_cycle1 tail
+#pragma unroll
+	for (int c = 0; c < 4; c++) combined[c] = clamp_9bit(combined[c]);
+	{
+		int ea = combined[3] + ((combined[3] + 1) >> 8);
+		int mod;
+		if (cvg_times_alpha)
+		{
+			mod = (ea * cov_count + 4) >> 3;
+			cov_count = mod >> 5;
+		}
+		else
+			mod = cov_count << 5;
+		if (alpha_cvg_select) ea = mod;
+		else ea += alpha_d;
+		combined[3] = clampi(ea, 0, 0xff);
+	}
+	if (!(f & RS_MULTI_CYCLE)) alpha_ref = combined[3];
+	if (aa && cov_count == 0) return false;
+	if (alpha_test)
+	{
+		int thr = (f & RS_ALPHA_TEST_DITHER) ? int(noise & 0xffu) : int(sh.blend_color[3]);
+		if (alpha_ref < thr) return false;
+	}
+	int shade_alpha = min(shade[3] + alpha_d, 0xff);
+
+	// ---- depth_blend (memory_interfacing.h:488-571)
+	const uint32_t df = sh.db_flags;
+	const bool force_blend = (df & DB_FORCE_BLEND) != 0, image_read = (df & DB_IMAGE_READ) != 0;
+	const bool dba = (df & DB_AA) != 0;
+	int mem[4];
+	{
+		int mc = image_read ? (px.col[3] & 0xe0) : 0xe0;
+		switch (ps.fb_fmt)
+		{
+		case FBF_I4: mem[0] = mem[1] = mem[2] = 0; mc = 0xe0; break;
+		case FBF_I8: mem[0] = mem[1] = mem[2] = px.col[0]; mc = 0xe0; break;
+		case FBF_RGBA5551: mem[0] = px.col[0] & 0xf8; mem[1] = px.col[1] & 0xf8; mem[2] = px.col[2] & 0xf8; break;
+		case FBF_IA88: mem[0] = mem[1] = mem[2] = px.col[0]; break;
+		default: mem[0] = px.col[0]; mem[1] = px.col[1]; mem[2] = px.col[2]; break;
+		}
+		mem[3] = mc;
+	}
+	int mem_cov = mem[3] >> 5;
+	bool blend_en, cvg_wrap, pass;
+	int bshift[2];
+	if (df & DB_DEPTH_TEST)
+	{
+		int memory_z = z_decompress(px.depth);
+		int memory_dz = 1 << px.dz;
+		int precision = (px.depth >> 11) & 0xf;
+		bool coplanar = false;
+		bshift[0] = clampi(int(sh.dz_compressed) - px.dz, 0, 4);
+		bshift[1] = clampi(px.dz - int(sh.dz_compressed), 0, 4);
+		if (precision < 3)
+		{
+			if (memory_dz != 0x8000) memory_dz = max(memory_dz << 1, 16 >> precision);
+			else { coplanar = true; memory_dz = 0xffff; }
+		}
+		int cdz = int(sh.dz) | memory_dz;
+		if (cdz != 0) cdz = 1 << find_msb(cdz);
+		int cdz_i = cdz;
+		cdz <<= 3;
+		bool farther = coplanar || ((z + cdz) >= memory_z);
+		bool overflow = (cov_count + mem_cov) >= 8;
+		blend_en = force_blend || (!overflow && dba && farther);
+		cvg_wrap = overflow;
+		bool max_z = memory_z == 0x3ffff;
+		bool front = z < memory_z;
+		bool nearer = coplanar || ((z - cdz) <= memory_z);
+		switch (sh.z_mode)
+		{
+		case 0: pass = max_z || (overflow ? front : nearer); break;
+		case 1:
+			if (!front || !farther || !overflow) pass = max_z || (overflow ? front : nearer);
+			else
+			{
+				int e = max(find_msb(cdz_i & 0xffff), 0);
+				int coeff = ((memory_z >> e) - (z >> e)) & 0xf;
+				cov_count = min((coeff * cov_count) >> 3, 8);
+				pass = true;
+			}
+			break;
+		case 2: pass = front || max_z; break;
+		default: pass = farther && nearer && !max_z; break;
+		}
+	}
+	else
+	{
+		bshift[0] = 0;
+		bshift[1] = min(0xf - int(sh.dz_compressed), 4);
+		bool overflow = (cov_count + mem_cov) >= 8;
+		blend_en = force_blend || (!overflow && dba);
+		cvg_wrap = overflow;
+		pass = true;
+	}
+	if (!(pass && (!dba || cov_count != 0))) return false;
+
+	const bool color_on_cvg = (df & DB_COLOR_ON_CVG) != 0;
+	int pixc[4] = { combined[0], combined[1], combined[2], combined[3] };
+	const uint8_t *bm = sh.blend[0];
+	if (df & DB_MULTI_CYCLE)
+	{
+		int tmp[3];
+		blender(pixc, mem, sh.fog, sh.blend_color, shade_alpha, bm, force_blend, blend_en, color_on_cvg, cvg_wrap, bshift,
+		        false, tmp);
+		pixc[0] = tmp[0]; pixc[1] = tmp[1]; pixc[2] = tmp[2];
+		bm = sh.blend[1];
+	}
+	int rgb[3];
+	blender(pixc, mem, sh.fog, sh.blend_color, shade_alpha, bm, force_blend, blend_en, color_on_cvg, cvg_wrap, bshift,
+	        true, rgb);
+	if (df & DB_DITHER)
+	{
+		int dith = ((z << 9) | rgb_d) & 0x1ff;
+#pragma unroll
+		for (int c = 0; c < 3; c++)
+		{
+			int d = (dith >> (3 * c)) & 7;
+			int o = rgb[c];
+			int r = o > 247 ? 255 : ((o & 0xf8) + 8);
+			int rs = (d - (o & 7)) >> 31;
+			rgb[c] = (o + ((r - o) & rs)) & 0xff;
+		}
+	}
+	int new_cov;
+	switch (sh.coverage_mode)
+	{
+	case 0: new_cov = blend_en ? min(7, mem_cov + cov_count) : ((cov_count - 1) & 7); break;
+	case 1: new_cov = (cov_count + mem_cov) & 7; break;
+	case 2: new_cov = 7; break;
+	default: new_cov = mem_cov; break;
+	}
+	write_color(ps.fb_fmt, px, rgb[0], rgb[1], rgb[2], (new_cov << 5) & 0xff);
+	if (df & DB_DEPTH_UPDATE)
+	{
+		px.depth = z_compress(z);
+		px.dz = sh.dz_compressed;
+		px.ddirty = true;
+		if (pc.alias) alias_d2c(ps.fb_fmt, px);
+	}
+	else if (pc.alias)
+		alias_c2d(ps.fb_fmt, px);
+	return true;
+}
+
+// ============================================================================ k_raster
+constexpr int RASTER_WARPS = 4;
+
+__global__ void __launch_bounds__(RASTER_WARPS * 32) k_raster(const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                                             uint32_t num_items, const RdpPrimGeom *__restrict__ geom,
+                                                             const RdpPrimAttr *__restrict__ attr,
+                                                             const RdpPrimShade *__restrict__ shade,
+                                                             const RdpTile *__restrict__ tilesets,
+                                                             unsigned long long *__restrict__ fragments)
+{
+	__shared__ SpanA s_sa[RASTER_WARPS][9];
+	__shared__ SpanX s_sx[RASTER_WARPS][9];
+	const int wib = threadIdx.x >> 5;
+	const int lane = threadIdx.x & 31;
+	const uint32_t item = blockIdx.x * RASTER_WARPS + wib;
+	if (item >= num_items) return;
+
+	// Locate the pass owning this tile item.
+	uint32_t pi = 0;
+	for (uint32_t k = 1; k < num_passes; k++)
+		if (passes[k].tile_item_begin <= item) pi = k;
+	const RdpPass &ps = passes[pi];
+	const uint32_t tile_linear = item - ps.tile_item_begin;
+	const int tx = int(tile_linear % ps.tiles_x), ty = int(tile_linear / ps.tiles_x);
+	uint32_t *masks = ps.masks + size_t(tile_linear) * RDP_MASK_WORDS_PER_TILE;
+	const uint32_t nwords = (ps.prim_count + 31) / 32;
+
+	PassConst pc;
+	switch (ps.fb_fmt)
+	{
+	case FBF_I4: pc.fb_size = 0; pc.dx_mask = 0; pc.dx_shift = 0; break;
+	case FBF_I8: pc.fb_size = 1; pc.dx_mask = ~7; pc.dx_shift = 3; break;
+	case FBF_RGBA5551:
+	case FBF_IA88: pc.fb_size = 2; pc.dx_mask = ~3; pc.dx_shift = 2; break;
+	default: pc.fb_size = 4; pc.dx_mask = ~1; pc.dx_shift = 1; break;
+	}
+	pc.alias = ps.fb_addr == ps.depth_addr;
+	uint32_t addr_index;
+	switch (ps.fb_fmt)
+	{
+	case FBF_I4:
+	case FBF_I8: addr_index = ps.fb_addr; break;
+	case FBF_RGBA5551:
+	case FBF_IA88: addr_index = ps.fb_addr >> 1; break;
+	default: addr_index = ps.fb_addr >> 2; break;
+	}
+	const uint32_t depth_index = ps.depth_addr >> 1;
+
+	const int px_x = tx * 8 + (lane & 7);
+	const int px_y0 = ty * 8 + (lane >> 3);
+	const bool in0 = px_x < int(ps.fb_width) && px_y0 < int(ps.fb_height);
+	const bool in1 = px_x < int(ps.fb_width) && (px_y0 + 4) < int(ps.fb_height);
+	const uint32_t ci0 = addr_index + ps.fb_width * uint32_t(px_y0) + uint32_t(px_x);
+	const uint32_t di0 = depth_index + ps.fb_width * uint32_t(px_y0) + uint32_t(px_x);
+	const uint32_t ci1 = ci0 + ps.fb_width * 4u, di1 = di0 + ps.fb_width * 4u;
+
+	Pix p0, p1;
+	bool loaded = false;
+	uint32_t frags = 0;
+
+	for (uint32_t base = 0; base < nwords; base += 32)
+	{
+		uint32_t wi = base + lane;
+		uint32_t wv = wi < nwords ? masks[wi] : 0u;
+		unsigned nz = __ballot_sync(0xffffffffu, wv != 0);
+		if (wv) masks[wi] = 0u; // self-clean for the next pass using this slot
+		while (nz)
+		{
+			int src = __ffs(nz) - 1;
+			nz &= nz - 1;
+			uint32_t bits = __shfl_sync(0xffffffffu, wv, src);
+			if (!loaded)
+			{
+				if (in0) load_pixel(ps, p0, ci0, di0);
+				if (in1) load_pixel(ps, p1, ci1, di1);
+				loaded = true;
+			}
+			while (bits)
+			{
+				int b = __ffs(bits) - 1;
+				bits &= bits - 1;
+				uint32_t prim = ps.prim_begin + (base + src) * 32 + b;
+				const RdpPrimGeom &g = geom[prim];
+				// Cooperative span set-up for rows ty*8 .. ty*8+8 (the last row feeds pipelined texel1).
+				if (lane < 9)
+					span_attr(g, attr[prim], ty * 8 + lane, s_sa[wib][lane]);
+				else if (lane >= 16 && lane < 25)
+					span_x(g, ty * 8 + (lane - 16), s_sx[wib][lane - 16]);
+				__syncwarp();
+				const RdpPrimShade &sh = shade[prim];
+				const RdpPrimAttr &a = attr[prim];
+				const RdpTile *tiles = tilesets + size_t(sh.tileset) * 8;
+				const uint16_t *tm = ps.tmem_snapshots + size_t(sh.tmem_index) * 2048;
+				const int r0 = lane >> 3;
+				if (in0 && px_y0 >= g.span_ylo && px_y0 <= g.span_yhi)
+					frags += shade_and_blend(ps, pc, g, a, sh, tiles, tm, s_sa[wib][r0], s_sx[wib][r0],
+					                         s_sa[wib][r0 + 1], s_sx[wib][r0 + 1], px_x, px_y0, p0);
+				if (in1 && px_y0 + 4 >= g.span_ylo && px_y0 + 4 <= g.span_yhi)
+					frags += shade_and_blend(ps, pc, g, a, sh, tiles, tm, s_sa[wib][r0 + 4], s_sx[wib][r0 + 4],
+					                         s_sa[wib][r0 + 5], s_sx[wib][r0 + 5], px_x, px_y0 + 4, p1);
+				__syncwarp();
+			}
+		}
+	}
+	if (loaded)
+	{
+		if (in0) store_pixel(ps, p0, ci0, di0, pc.alias);
+		if (in1) store_pixel(ps, p1, ci1, di1, pc.alias);
+	}
+	if (fragments)
+	{
+		unsigned long long total = frags;
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+		if (lane == 0 && total) atomicAdd(fragments, total);
+	}
+}
+
+} // namespace rdp
+
+// ============================================================================ host launchers
+extern "C" cudaError_t rdp_kernels_init_luts(const uint8_t *blender_lut)
+{
+	return cudaMemcpyToSymbol(rdp::g_blender_lut, blender_lut, 0x8000);
+}
+
+extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t stream)
+{
+	if (L->num_prims)
+	{
+		rdp::k_prim_setup<<<(L->num_prims + 127) / 128, 128, 0, stream>>>(L->prims_in, L->num_prims, L->words,
+		                                                                   L->state_blocks, L->passes, L->geom,
+		                                                                   L->attr, L->shade);
+		rdp::k_bin<<<(L->num_prims * 32 + 255) / 256, 256, 0, stream>>>(L->num_prims, L->geom, L->shade, L->passes);
+	}
+	if (L->num_tmem_passes)
+		rdp::k_tmem<<<L->num_tmem_passes, 1024, 0, stream>>>(L->passes, L->tmem_pass_list, L->uploads);
+	if (L->num_prims && L->num_tile_items)
+		rdp::k_raster<<<(L->num_tile_items + rdp::RASTER_WARPS - 1) / rdp::RASTER_WARPS, rdp::RASTER_WARPS * 32, 0,
+		                stream>>>(L->passes, L->num_passes, L->num_tile_items, L->geom, L->attr, L->shade,
+		                          L->tilesets, L->fragments);
+	return cudaGetLastError();
+}

@@ -1,0 +1,16 @@
+"""Python host API of the GB300-native N64 RDP path.
+
+`CommandProcessor` mirrors the reference's RDP::CommandProcessor
+(parallel-rdp/rdp_device.hpp:111-197) method for method, over the C ABI of
+librdp_cuda.so (include/rdp_cuda.h).  There is no CPU fallback: importing this
+package fails loudly when the native library has not been built.
+"""
+from .native import (  # noqa: F401
+    CommandProcessor,
+    RdpError,
+    RdpTimeout,
+    VIRegister,
+    device_is_supported,
+    library_path,
+)
+from .cmdgen import GenParams, generate_stream, CONFIG_PLAIN, CONFIG_TEXTURED, CONFIG_MIXED  # noqa: F401

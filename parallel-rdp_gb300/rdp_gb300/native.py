@@ -1,0 +1,241 @@
+"""ctypes binding of librdp_cuda.so (include/rdp_cuda.h)."""
+import ctypes
+import enum
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(os.path.dirname(_HERE), "csrc", "_build")
+
+RDP_OK = 0
+RDP_ERR_UNSUPPORTED = 1
+RDP_ERR_OOM = 2
+RDP_ERR_TIMEOUT = 3
+RDP_ERR_INVALID = 4
+RDP_ERR_DEVICE = 5
+_ERR_NAMES = {1: "unsupported", 2: "out of memory", 3: "timeout", 4: "invalid argument", 5: "CUDA error"}
+
+
+class RdpError(RuntimeError):
+    def __init__(self, code, what):
+        super().__init__("%s failed: %s (%d)" % (what, _ERR_NAMES.get(code, "error"), code))
+        self.code = code
+
+
+class RdpTimeout(RdpError):
+    pass
+
+
+class VIRegister(enum.IntEnum):
+    """rdp_common.hpp:286-302"""
+    Control = 0
+    Origin = 1
+    Width = 2
+    Intr = 3
+    VCurrentLine = 4
+    Timing = 5
+    VSync = 6
+    HSync = 7
+    Leap = 8
+    HStart = 9
+    VStart = 10
+    VBurst = 11
+    XScale = 12
+    YScale = 13
+
+
+class _CreateInfo(ctypes.Structure):
+    _fields_ = [("rdram", ctypes.c_void_p), ("rdram_offset", ctypes.c_size_t), ("rdram_size", ctypes.c_size_t),
+                ("hidden_rdram_size", ctypes.c_size_t), ("flags", ctypes.c_uint32), ("device", ctypes.c_int)]
+
+
+class _ScanoutOptions(ctypes.Structure):
+    _fields_ = [("persist_frame_on_invalid_input", ctypes.c_uint32), ("blend_previous_frame", ctypes.c_uint32),
+                ("upscale_deinterlacing", ctypes.c_uint32), ("crop_overscan_pixels", ctypes.c_uint32)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("primitives", ctypes.c_uint64), ("passes", ctypes.c_uint64), ("reference_passes", ctypes.c_uint64),
+                ("fragments", ctypes.c_uint64), ("tmem_uploads", ctypes.c_uint64)]
+
+
+_VALIDATION_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p)
+
+EXPORTED_SYMBOLS = [
+    "rdp_cp_create", "rdp_cp_destroy", "rdp_device_is_supported", "rdp_cp_enqueue", "rdp_cp_signal_timeline",
+    "rdp_cp_wait_timeline", "rdp_cp_flush", "rdp_cp_idle", "rdp_cp_begin_frame_context", "rdp_cp_set_quirks",
+    "rdp_cp_set_validation_callback", "rdp_cp_begin_read_rdram", "rdp_cp_end_write_rdram",
+    "rdp_cp_begin_read_hidden_rdram", "rdp_cp_end_write_hidden_rdram", "rdp_cp_get_rdram_size",
+    "rdp_cp_get_hidden_rdram_size", "rdp_cp_get_tmem", "rdp_cp_set_vi_register", "rdp_cp_scanout_sync",
+    "rdp_cp_get_stats",
+]
+
+
+def library_path():
+    return os.path.join(_BUILD, "librdp_cuda.so")
+
+
+_lib = None
+
+
+def lib():
+    """Loads librdp_cuda.so; raises when it is missing (no fallback path exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError("librdp_cuda.so is not built (%s); run parallel-rdp_gb300/build.py" % path)
+    L = ctypes.CDLL(path)
+    vp, u32, u64, sz = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_size_t
+    L.rdp_cp_create.argtypes = [ctypes.POINTER(_CreateInfo), ctypes.POINTER(vp)]
+    L.rdp_cp_destroy.argtypes = [vp]
+    L.rdp_cp_destroy.restype = None
+    L.rdp_device_is_supported.argtypes = [ctypes.c_int]
+    L.rdp_cp_enqueue.argtypes = [vp, u32, vp]
+    L.rdp_cp_signal_timeline.argtypes = [vp, ctypes.POINTER(u64)]
+    L.rdp_cp_wait_timeline.argtypes = [vp, u64, u64]
+    for n in ("rdp_cp_flush", "rdp_cp_idle", "rdp_cp_begin_frame_context", "rdp_cp_end_write_rdram",
+              "rdp_cp_end_write_hidden_rdram"):
+        getattr(L, n).argtypes = [vp]
+    L.rdp_cp_set_quirks.argtypes = [vp, u32]
+    L.rdp_cp_set_validation_callback.argtypes = [vp, _VALIDATION_CB, vp]
+    L.rdp_cp_begin_read_rdram.argtypes = [vp]
+    L.rdp_cp_begin_read_rdram.restype = vp
+    L.rdp_cp_begin_read_hidden_rdram.argtypes = [vp]
+    L.rdp_cp_begin_read_hidden_rdram.restype = vp
+    L.rdp_cp_get_rdram_size.argtypes = [vp]
+    L.rdp_cp_get_rdram_size.restype = sz
+    L.rdp_cp_get_hidden_rdram_size.argtypes = [vp]
+    L.rdp_cp_get_hidden_rdram_size.restype = sz
+    L.rdp_cp_get_tmem.argtypes = [vp, vp]
+    L.rdp_cp_set_vi_register.argtypes = [vp, u32, u32]
+    L.rdp_cp_scanout_sync.argtypes = [vp, ctypes.POINTER(_ScanoutOptions), vp, ctypes.POINTER(u32),
+                                      ctypes.POINTER(u32)]
+    L.rdp_cp_get_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
+    _lib = L
+    return L
+
+
+def device_is_supported(device=0):
+    return bool(lib().rdp_device_is_supported(device))
+
+
+def _check(code, what):
+    if code == RDP_ERR_TIMEOUT:
+        raise RdpTimeout(code, what)
+    if code != RDP_OK:
+        raise RdpError(code, what)
+
+
+class CommandProcessor:
+    """RDP::CommandProcessor over librdp_cuda (rdp_device.hpp:111-197).
+
+    `rdram` is a caller-owned numpy uint8 array (RDRAM as host-order 32-bit
+    words, N64 byte address a at index a ^ 3), or None to let the processor own
+    a zero-initialised one.
+    """
+
+    def __init__(self, rdram=None, rdram_size=8 << 20, hidden_rdram_size=None, device=0):
+        if hidden_rdram_size is None:
+            hidden_rdram_size = rdram_size // 2
+        if rdram is None:
+            rdram = np.zeros(rdram_size, dtype=np.uint8)
+        assert rdram.dtype == np.uint8 and rdram.flags["C_CONTIGUOUS"] and rdram.size >= rdram_size
+        self._rdram = rdram
+        info = _CreateInfo(rdram.ctypes.data, 0, rdram_size, hidden_rdram_size, 0, device)
+        h = ctypes.c_void_p()
+        _check(lib().rdp_cp_create(ctypes.byref(info), ctypes.byref(h)), "rdp_cp_create")
+        self._h = h
+        self.rdram_size = rdram_size
+        self.hidden_rdram_size = hidden_rdram_size
+        self._cb = None
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().rdp_cp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- command stream ---------------------------------------------------
+    def enqueue_command(self, words):
+        w = np.ascontiguousarray(words, dtype=np.uint32)
+        _check(lib().rdp_cp_enqueue(self._h, w.size, w.ctypes.data), "enqueue_command")
+
+    def signal_timeline(self):
+        v = ctypes.c_uint64()
+        _check(lib().rdp_cp_signal_timeline(self._h, ctypes.byref(v)), "signal_timeline")
+        return v.value
+
+    def wait_for_timeline(self, value, timeout_s=30.0):
+        _check(lib().rdp_cp_wait_timeline(self._h, value, int(timeout_s * 1e9)), "wait_for_timeline")
+
+    def flush(self):
+        _check(lib().rdp_cp_flush(self._h), "flush")
+
+    def idle(self):
+        _check(lib().rdp_cp_idle(self._h), "idle")
+
+    def begin_frame_context(self):
+        _check(lib().rdp_cp_begin_frame_context(self._h), "begin_frame_context")
+
+    def set_quirks(self, quirks_word):
+        _check(lib().rdp_cp_set_quirks(self._h, quirks_word), "set_quirks")
+
+    def set_validation_interface(self, fn):
+        """fn(error_code, message) is called for illegal RDP state (rdp_renderer.hpp:75-95)."""
+        if fn is None:
+            self._cb = None
+            _check(lib().rdp_cp_set_validation_callback(self._h, _VALIDATION_CB(), None), "set_validation")
+            return
+        self._cb = _VALIDATION_CB(lambda user, err, msg: fn(err, msg.decode()))
+        _check(lib().rdp_cp_set_validation_callback(self._h, self._cb, None), "set_validation")
+
+    # -- memory -----------------------------------------------------------
+    def begin_read_rdram(self):
+        p = lib().rdp_cp_begin_read_rdram(self._h)
+        if not p:
+            raise RdpError(RDP_ERR_DEVICE, "begin_read_rdram")
+        return self._rdram[:self.rdram_size]
+
+    def end_write_rdram(self):
+        _check(lib().rdp_cp_end_write_rdram(self._h), "end_write_rdram")
+
+    def begin_read_hidden_rdram(self):
+        p = lib().rdp_cp_begin_read_hidden_rdram(self._h)
+        if not p:
+            raise RdpError(RDP_ERR_DEVICE, "begin_read_hidden_rdram")
+        return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint8)),
+                                     shape=(self.hidden_rdram_size,)).copy()
+
+    def get_tmem(self):
+        out = np.zeros(2048, dtype=np.uint16)
+        _check(lib().rdp_cp_get_tmem(self._h, out.ctypes.data), "get_tmem")
+        return out
+
+    # -- video interface ----------------------------------------------------
+    def set_vi_register(self, reg, value):
+        _check(lib().rdp_cp_set_vi_register(self._h, int(reg), value & 0xffffffff), "set_vi_register")
+
+    def scanout_sync(self, blend_previous_frame=True, persist_frame_on_invalid_input=False, crop_overscan_pixels=0):
+        opts = _ScanoutOptions(int(persist_frame_on_invalid_input), int(blend_previous_frame), 0,
+                               crop_overscan_pixels)
+        buf = np.zeros(640 * 576, dtype=np.uint32)
+        w, h = ctypes.c_uint32(), ctypes.c_uint32()
+        _check(lib().rdp_cp_scanout_sync(self._h, ctypes.byref(opts), buf.ctypes.data, ctypes.byref(w),
+                                         ctypes.byref(h)), "scanout_sync")
+        return buf[:w.value * h.value].reshape(h.value, w.value) if w.value else None
+
+    def stats(self):
+        s = _Stats()
+        _check(lib().rdp_cp_get_stats(self._h, ctypes.byref(s)), "get_stats")
+        return {k: getattr(s, k) for k, _ in _Stats._fields_}

@@ -135,8 +135,30 @@ typedef struct rdp_stats
 	uint64_t reference_passes;
 	uint64_t fragments;
 	uint64_t tmem_uploads;
+	uint64_t touched_tiles;   /* 8x8 tiles the rasteriser loaded and stored */
+	uint64_t kernel_launches; /* kernels this processor launched (graph replays included) */
+	uint64_t staging_bytes;   /* host->device bytes of command/state data */
 } rdp_stats;
 int rdp_cp_get_stats(rdp_cp *cp, rdp_stats *out);
+
+/* Sync-point capture (the reference submits each sync point's render passes as one
+ * command buffer, rdp_renderer.cpp:2909-2986; here they become one CUDA graph).
+ * Between rdp_cp_capture_begin and rdp_cp_capture_end, flushed passes are not run:
+ * their command data is copied once into device memory and their kernels are
+ * recorded.  rdp_graph_replay launches the recorded kernels `count` times on the
+ * processor's stream, with every input already resident in HBM, and waits. */
+typedef struct rdp_graph rdp_graph;
+int rdp_cp_capture_begin(rdp_cp *cp);
+int rdp_cp_capture_end(rdp_cp *cp, rdp_graph **out);
+/* Replays; when elapsed_ms is non-NULL it receives the GPU time of the replays
+ * measured with CUDA events on the processor's stream. */
+int rdp_graph_replay(rdp_graph *g, uint32_t count, float *elapsed_ms);
+uint32_t rdp_graph_kernel_count(rdp_graph *g);
+/* GPU time (ms) of the rasteriser launches in the last replay, from CUDA events
+ * recorded on the processor's stream around each k_raster launch, and their number. */
+float rdp_graph_last_raster_ms(rdp_graph *g);
+uint32_t rdp_graph_raster_launches(rdp_graph *g);
+void rdp_graph_destroy(rdp_graph *g);
 
 #ifdef __cplusplus
 }

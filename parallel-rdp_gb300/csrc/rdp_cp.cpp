@@ -107,6 +107,13 @@ struct rdp_cp
 	uint8_t *d_rdram = nullptr, *d_hidden = nullptr;
 	uint16_t *d_tmem = nullptr, *d_snapshots = nullptr;
 	uint32_t *d_masks = nullptr;
+	uint32_t *d_tmem_keep = nullptr;
+	uint32_t *d_tile_counts = nullptr, *d_pair_offsets = nullptr, *d_ctrl = nullptr;
+	uint2 *d_pairs = nullptr;
+	uint32_t *d_sc_color = nullptr;
+	int *d_sc_zdith = nullptr;
+	uint16_t *d_sc_misc = nullptr;
+	uint32_t pair_capacity = 0, shade_ctas = 0;
 	RdpPrimGeom *d_geom = nullptr;
 	RdpPrimAttr *d_attr = nullptr;
 	RdpPrimShade *d_shade = nullptr;
@@ -166,6 +173,11 @@ struct rdp_cp
 		uint32_t prims = 0, uploads = 0, span_jobs = 0;
 		std::vector<uint64_t> static_keys, depth_keys;
 	} ref;
+
+	// Sync-point capture: recorded launches with device-resident inputs.
+	bool capturing = false;
+	std::vector<RdpLaunch> captured;
+	std::vector<void *> captured_buffers;
 
 	uint32_t vi_regs[16] = {};
 	rdp_validation_cb validation_cb = nullptr;
@@ -248,20 +260,35 @@ struct rdp_cp
 		if (cudaMalloc(&d_tmem, 4096) != cudaSuccess) return RDP_ERR_OOM;
 		if (cudaMalloc(&d_snapshots, size_t(RDP_MAX_UPLOADS_PER_PASS + 1) * 4096) != cudaSuccess) return RDP_ERR_OOM;
 		if (cudaMalloc(&d_masks, size_t(kMaxTiles) * RDP_MASK_WORDS_PER_TILE * 4) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_tmem_keep, size_t(RDP_MAX_UPLOADS_PER_PASS) * 64 * 4) != cudaSuccess) return RDP_ERR_OOM;
+		pair_capacity = 1u << 20;
+		if (cudaMalloc(&d_tile_counts, size_t(kMaxTiles + 1) * 4) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_pair_offsets, size_t(kMaxTiles + 1) * 4) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_ctrl, 16) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_pairs, size_t(pair_capacity) * sizeof(uint2)) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_sc_color, size_t(pair_capacity) * 64 * 4) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_sc_zdith, size_t(pair_capacity) * 64 * 4) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_sc_misc, size_t(pair_capacity) * 64 * 2) != cudaSuccess) return RDP_ERR_OOM;
+		{
+			int sms = 0;
+			cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+			shade_ctas = uint32_t(std::max(sms, 1)) * uint32_t(rdp_kernels_shade_ctas_per_sm());
+		}
 		if (cudaMalloc(&d_geom, sizeof(RdpPrimGeom) * RDP_MAX_PRIMS_PER_PASS) != cudaSuccess) return RDP_ERR_OOM;
 		if (cudaMalloc(&d_attr, sizeof(RdpPrimAttr) * RDP_MAX_PRIMS_PER_PASS) != cudaSuccess) return RDP_ERR_OOM;
 		if (cudaMalloc(&d_shade, sizeof(RdpPrimShade) * RDP_MAX_PRIMS_PER_PASS) != cudaSuccess) return RDP_ERR_OOM;
 		if (cudaMalloc(&d_staging, staging_cap) != cudaSuccess) return RDP_ERR_OOM;
-		if (cudaMalloc(&d_fragments, sizeof(unsigned long long)) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_fragments, 2 * sizeof(unsigned long long)) != cudaSuccess) return RDP_ERR_OOM;
 		for (auto &s : staging)
 		{
 			if (cudaMallocHost(&s.h, staging_cap) != cudaSuccess) return RDP_ERR_OOM;
 			if (cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess) return RDP_ERR_DEVICE;
 		}
 		if (check(cudaMemsetAsync(d_masks, 0, size_t(kMaxTiles) * RDP_MASK_WORDS_PER_TILE * 4, stream))) return RDP_ERR_DEVICE;
+		if (check(cudaMemsetAsync(d_tile_counts, 0, size_t(kMaxTiles + 1) * 4, stream))) return RDP_ERR_DEVICE;
 		if (check(cudaMemsetAsync(d_hidden, 0x03, hidden_size, stream))) return RDP_ERR_DEVICE;
 		if (check(cudaMemsetAsync(d_tmem, 0, 4096, stream))) return RDP_ERR_DEVICE;
-		if (check(cudaMemsetAsync(d_fragments, 0, sizeof(unsigned long long), stream))) return RDP_ERR_DEVICE;
+		if (check(cudaMemsetAsync(d_fragments, 0, 2 * sizeof(unsigned long long), stream))) return RDP_ERR_DEVICE;
 		if (check(cudaMemcpyAsync(d_rdram, host_rdram, rdram_size, cudaMemcpyHostToDevice, stream))) return RDP_ERR_DEVICE;
 		if (check(cudaStreamSynchronize(stream))) return RDP_ERR_DEVICE;
 
@@ -292,6 +319,14 @@ struct rdp_cp
 		cudaFree(d_tmem);
 		cudaFree(d_snapshots);
 		cudaFree(d_masks);
+		cudaFree(d_tmem_keep);
+		cudaFree(d_tile_counts);
+		cudaFree(d_pair_offsets);
+		cudaFree(d_ctrl);
+		cudaFree(d_pairs);
+		cudaFree(d_sc_color);
+		cudaFree(d_sc_zdith);
+		cudaFree(d_sc_misc);
 		cudaFree(d_geom);
 		cudaFree(d_attr);
 		cudaFree(d_shade);
@@ -394,11 +429,25 @@ struct rdp_cp
 		size_t o_up = put(uploads.data(), uploads.size() * sizeof(RdpUpload));
 		uint32_t zero = 0;
 		size_t o_list = put(&zero, 4);
-		if (check(cudaMemcpyAsync(d_staging, h, off, cudaMemcpyHostToDevice, stream))) return sticky_error;
-		if (check(cudaEventRecord(st.done, stream))) return sticky_error;
-		st.in_flight = true;
+		uint8_t *dst = d_staging;
+		if (capturing)
+		{
+			// The pass's data stays resident for graph replay.
+			if (check(cudaStreamSynchronize(stream))) return sticky_error;
+			if (check(cudaMalloc(&dst, off))) return sticky_error;
+			captured_buffers.push_back(dst);
+			if (check(cudaMemcpy(dst, h, off, cudaMemcpyHostToDevice))) return sticky_error;
+		}
+		else
+		{
+			if (check(cudaMemcpyAsync(d_staging, h, off, cudaMemcpyHostToDevice, stream))) return sticky_error;
+			if (check(cudaEventRecord(st.done, stream))) return sticky_error;
+			st.in_flight = true;
+		}
+		stats.staging_bytes += off;
 
 		RdpLaunch L = {};
+		uint8_t *d_staging = dst;
 		L.prims_in = reinterpret_cast<const RdpPrimIn *>(d_staging + o_prims);
 		L.num_prims = render ? uint32_t(prims.size()) : 0;
 		L.words = reinterpret_cast<const uint32_t *>(d_staging + o_words);
@@ -412,9 +461,30 @@ struct rdp_cp
 		L.tmem_pass_list = reinterpret_cast<const uint32_t *>(d_staging + o_list);
 		L.num_tmem_passes = uploads.empty() ? 0 : 1;
 		L.uploads = reinterpret_cast<const RdpUpload *>(d_staging + o_up);
+		L.max_uploads = uint32_t(uploads.size());
+		L.tmem_keep = d_tmem_keep;
+		L.tile_counts = d_tile_counts;
+		L.pair_offsets = d_pair_offsets;
+		L.pairs = d_pairs;
+		L.ctrl = d_ctrl;
+		L.pair_capacity = pair_capacity;
+		L.shade_ctas = shade_ctas;
+		L.sc_color = d_sc_color;
+		L.sc_zdith = d_sc_zdith;
+		L.sc_misc = d_sc_misc;
 		L.num_tile_items = pass.tiles_x * pass.tiles_y;
 		L.fragments = d_fragments;
-		if (check(rdp_kernels_launch(&L, stream))) return sticky_error;
+		if (capturing)
+		{
+			for (auto &e : L.raster_events)
+				if (check(cudaEventCreate(&e))) return sticky_error;
+			captured.push_back(L);
+		}
+		else
+		{
+			if (check(rdp_kernels_launch(&L, stream))) return sticky_error;
+			stats.kernel_launches += rdp_kernels_count(&L);
+		}
 
 		if (render)
 		{
@@ -882,7 +952,9 @@ struct rdp_cp
 
 	int wait_timeline(uint64_t value, uint64_t timeout_ns)
 	{
-		auto deadline = std::chrono::steady_clock::now() + std::chrono::nanoseconds(timeout_ns);
+		// Timeouts beyond ~11 days mean "no deadline" (and must not overflow the clock).
+		const bool bounded = timeout_ns < (uint64_t(1) << 50);
+		auto deadline = std::chrono::steady_clock::now() + std::chrono::nanoseconds(bounded ? int64_t(timeout_ns) : 0);
 		while (!pending.empty() && pending.front().first <= value)
 		{
 			cudaEvent_t e = pending.front().second;
@@ -891,7 +963,7 @@ struct rdp_cp
 				cudaError_t q = cudaEventQuery(e);
 				if (q == cudaSuccess) break;
 				if (q != cudaErrorNotReady) return check(q);
-				if (std::chrono::steady_clock::now() >= deadline) return RDP_ERR_TIMEOUT;
+				if (bounded && std::chrono::steady_clock::now() >= deadline) return RDP_ERR_TIMEOUT;
 				std::this_thread::yield();
 			}
 			completed_value = pending.front().first;
@@ -1066,8 +1138,123 @@ int rdp_cp_get_stats(rdp_cp *cp, rdp_stats *out)
 	unsigned long long frags = 0;
 	if (cudaMemcpy(&frags, cp->d_fragments, sizeof(frags), cudaMemcpyDeviceToHost) != cudaSuccess) return RDP_ERR_DEVICE;
 	out->fragments = frags;
+	unsigned long long counters[2] = { 0, 0 };
+	if (cudaMemcpy(counters, cp->d_fragments, sizeof(counters), cudaMemcpyDeviceToHost) != cudaSuccess) return RDP_ERR_DEVICE;
+	out->touched_tiles = counters[1];
 	out->reference_passes = cp->stats.reference_passes + ((cp->ref.prims || cp->ref.uploads) ? 1 : 0);
 	return RDP_OK;
+}
+
+struct rdp_graph
+{
+	rdp_cp *cp = nullptr;
+	cudaGraph_t graph = nullptr;
+	cudaGraphExec_t exec = nullptr;
+	std::vector<void *> buffers;
+	std::vector<std::pair<cudaEvent_t, cudaEvent_t>> raster_events;
+	uint32_t kernels = 0, raster_launches = 0;
+	float last_raster_ms = 0.0f;
+	cudaEvent_t ev[2] = { nullptr, nullptr };
+};
+
+int rdp_cp_capture_begin(rdp_cp *cp)
+{
+	if (!cp || cp->capturing) return RDP_ERR_INVALID;
+	cudaSetDevice(cp->device);
+	int r = cp->hard_flush();
+	if (r != RDP_OK) return r;
+	cp->capturing = true;
+	cp->captured.clear();
+	cp->captured_buffers.clear();
+	return RDP_OK;
+}
+
+int rdp_cp_capture_end(rdp_cp *cp, rdp_graph **out)
+{
+	if (!cp || !out || !cp->capturing) return RDP_ERR_INVALID;
+	cudaSetDevice(cp->device);
+	int r = cp->hard_flush();
+	cp->capturing = false;
+	if (r != RDP_OK) return r;
+	rdp_graph *g = new rdp_graph();
+	g->cp = cp;
+	g->buffers.swap(cp->captured_buffers);
+	if (cp->check(cudaStreamBeginCapture(cp->stream, cudaStreamCaptureModeThreadLocal)) == RDP_OK)
+	{
+		for (auto &L : cp->captured)
+		{
+			rdp_kernels_launch(&L, cp->stream);
+			g->kernels += rdp_kernels_count(&L);
+			if (L.num_prims && L.num_tile_items)
+			{
+				g->raster_events.emplace_back(L.raster_events[0], L.raster_events[1]);
+				g->raster_launches++;
+			}
+			else
+			{
+				cudaEventDestroy(L.raster_events[0]);
+				cudaEventDestroy(L.raster_events[1]);
+			}
+		}
+		cp->check(cudaStreamEndCapture(cp->stream, &g->graph));
+	}
+	cp->captured.clear();
+	if (cp->sticky_error == RDP_OK) cp->check(cudaGraphInstantiate(&g->exec, g->graph, 0));
+	if (cp->sticky_error == RDP_OK) cp->check(cudaEventCreate(&g->ev[0]));
+	if (cp->sticky_error == RDP_OK) cp->check(cudaEventCreate(&g->ev[1]));
+	if (cp->sticky_error != RDP_OK)
+	{
+		rdp_graph_destroy(g);
+		return cp->sticky_error;
+	}
+	*out = g;
+	return RDP_OK;
+}
+
+int rdp_graph_replay(rdp_graph *g, uint32_t count, float *elapsed_ms)
+{
+	if (!g) return RDP_ERR_INVALID;
+	rdp_cp *cp = g->cp;
+	cudaSetDevice(cp->device);
+	if (cp->check(cudaEventRecord(g->ev[0], cp->stream))) return cp->sticky_error;
+	for (uint32_t i = 0; i < count; i++)
+		if (cp->check(cudaGraphLaunch(g->exec, cp->stream))) return cp->sticky_error;
+	if (cp->check(cudaEventRecord(g->ev[1], cp->stream))) return cp->sticky_error;
+	if (cp->check(cudaEventSynchronize(g->ev[1]))) return cp->sticky_error;
+	cp->stats.kernel_launches += uint64_t(g->kernels) * count;
+	if (elapsed_ms) cp->check(cudaEventElapsedTime(elapsed_ms, g->ev[0], g->ev[1]));
+	// GPU time of the rasteriser launches of the last replay.
+	g->last_raster_ms = 0.0f;
+	for (auto &pr : g->raster_events)
+	{
+		float ms = 0.0f;
+		if (cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) g->last_raster_ms += ms;
+		else cudaGetLastError(); // keep the thread's last-error slot clean for other CUDA users
+	}
+	return cp->sticky_error;
+}
+
+float rdp_graph_last_raster_ms(rdp_graph *g) { return g ? g->last_raster_ms : 0.0f; }
+uint32_t rdp_graph_raster_launches(rdp_graph *g) { return g ? g->raster_launches : 0; }
+
+uint32_t rdp_graph_kernel_count(rdp_graph *g) { return g ? g->kernels : 0; }
+
+void rdp_graph_destroy(rdp_graph *g)
+{
+	if (!g) return;
+	cudaSetDevice(g->cp->device);
+	cudaStreamSynchronize(g->cp->stream);
+	if (g->exec) cudaGraphExecDestroy(g->exec);
+	if (g->graph) cudaGraphDestroy(g->graph);
+	for (void *b : g->buffers) cudaFree(b);
+	for (auto &pr : g->raster_events)
+	{
+		cudaEventDestroy(pr.first);
+		cudaEventDestroy(pr.second);
+	}
+	for (auto e : g->ev)
+		if (e) cudaEventDestroy(e);
+	delete g;
 }
 
 } // extern "C"

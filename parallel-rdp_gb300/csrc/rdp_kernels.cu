@@ -551,7 +551,7 @@ __device__ bool bin_primitive(const RdpPrimGeom &g, int lox, int loy, int hix, i
 }
 
 __global__ void k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom, const RdpPrimShade *__restrict__ shade,
-                      const RdpPass *__restrict__ passes)
+                      const RdpPass *__restrict__ passes, uint32_t *__restrict__ tile_counts)
 {
 	uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	uint32_t lane = threadIdx.x & 31;
@@ -571,7 +571,11 @@ __global__ void k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom, 
 		int lox = tx * 8, loy = ty * 8;
 		int hix = min(lox + 7, fbw - 1), hiy = min(loy + 7, fbh - 1);
 		if (bin_primitive(g, lox, loy, hix, hiy))
-			atomicOr(&pass.masks[size_t(ty * pass.tiles_x + tx) * RDP_MASK_WORDS_PER_TILE + word], bit);
+		{
+			uint32_t tl = uint32_t(ty) * pass.tiles_x + uint32_t(tx);
+			atomicOr(&pass.masks[size_t(tl) * RDP_MASK_WORDS_PER_TILE + word], bit);
+			atomicAdd(&tile_counts[pass.tile_item_begin + tl], 1u);
+		}
 	}
 }
 
@@ -856,35 +860,58 @@ __device__ bool tmem_lut(const RdpPass &ps, const RdpUpload &info, int tmem16_in
 	return true;
 }
 
-__global__ void __launch_bounds__(1024) k_tmem(const RdpPass *__restrict__ passes, const uint32_t *__restrict__ pass_list,
-                                               const RdpUpload *__restrict__ uploads)
+// Phase 1: every (upload, TMEM word) pair independently -- does upload u write word w, and with
+// what value?  Written values land in snapshot u+1; unwritten words are marked in a bitmask.
+__global__ void k_tmem_apply(const RdpPass *__restrict__ passes, const uint32_t *__restrict__ pass_list,
+                             const RdpUpload *__restrict__ uploads, uint32_t *__restrict__ keep_bits)
 {
-	const RdpPass &ps = passes[pass_list[blockIdx.x]];
-	uint16_t *snap = ps.tmem_snapshots;
-	for (int h = 0; h < 2; h++)
+	const RdpPass &ps = passes[pass_list[blockIdx.y]];
+	uint32_t u = blockIdx.x;
+	if (u >= ps.upload_count) return;
+	RdpUpload info = uploads[ps.upload_begin + u];
+	uint16_t *dst = ps.tmem_snapshots + size_t(u + 1) * 2048;
+	uint32_t *keep = keep_bits + (size_t(blockIdx.y) * RDP_MAX_UPLOADS_PER_PASS + u) * 64;
+	for (int gid = threadIdx.x; gid < 2048; gid += blockDim.x)
 	{
-		int gid = threadIdx.x + h * 1024;
-		uint32_t value = ps.tmem_state[gid];
-		snap[gid] = uint16_t(value);
 		int idx = gid ^ 1;
 		bool upper = idx >= 0x400;
-		for (uint32_t u = 0; u < ps.upload_count; u++)
+		uint32_t v = 0;
+		bool wrote;
+		if (info.mode == 1) wrote = tmem_lut(ps, info, idx, v);
+		else
 		{
-			RdpUpload info = uploads[ps.upload_begin + u];
-			uint32_t v = 0;
-			bool wrote;
-			if (info.mode == 1) wrote = tmem_lut(ps, info, idx, v);
-			else
-			{
-				bool yuv = info.tmem_fmt == 1;
-				if (info.tmem_size == 3 || yuv) wrote = tmem_32(ps, info, idx & 0x3ff, upper, yuv, v);
-				else wrote = tmem_16(ps, info, idx, v);
-			}
-			if (wrote) value = v;
-			snap[size_t(u + 1) * 2048 + gid] = uint16_t(value);
+			bool yuv = info.tmem_fmt == 1;
+			if (info.tmem_size == 3 || yuv) wrote = tmem_32(ps, info, idx & 0x3ff, upper, yuv, v);
+			else wrote = tmem_16(ps, info, idx, v);
 		}
-		ps.tmem_state[gid] = uint16_t(value);
+		if (wrote) dst[gid] = uint16_t(v);
+		unsigned m = __ballot_sync(0xffffffffu, !wrote);
+		if ((threadIdx.x & 31) == 0) keep[gid >> 5] = m;
 	}
+}
+
+// Phase 2: per TMEM word, carry the previous snapshot's value through uploads that did not
+// write it (tmem_update.comp:546-576: instance i+1 = instance i with upload i applied).
+__global__ void k_tmem_carry(const RdpPass *__restrict__ passes, const uint32_t *__restrict__ pass_list,
+                             const uint32_t *__restrict__ keep_bits)
+{
+	const RdpPass &ps = passes[pass_list[blockIdx.y]];
+	int gid = blockIdx.x * blockDim.x + threadIdx.x;
+	if (gid >= 2048) return;
+	uint16_t *snap = ps.tmem_snapshots;
+	uint16_t value = ps.tmem_state[gid];
+	snap[gid] = value;
+	const uint32_t *keep = keep_bits + size_t(blockIdx.y) * RDP_MAX_UPLOADS_PER_PASS * 64;
+#pragma unroll 8
+	for (uint32_t u = 0; u < ps.upload_count; u++)
+	{
+		size_t at = size_t(u + 1) * 2048 + gid;
+		uint16_t written = snap[at]; // independent of the carried value: loads overlap
+		bool keep_prev = (keep[u * 64 + (gid >> 5)] >> (gid & 31)) & 1u;
+		if (keep_prev) snap[at] = value;
+		value = keep_prev ? value : written;
+	}
+	ps.tmem_state[gid] = value;
 }
 
 // ============================================================================ k_raster: spans
@@ -1092,7 +1119,7 @@ __device__ __forceinline__ uint32_t hw_idx(const RdpTile &t, int s, int tv, uint
 	return ((off >> 1) ^ ((uint32_t(tv) & 1u) << 1)) ^ 1u;
 }
 
-__device__ T4 fetch_texel(const uint16_t *tm, const RdpTile &t, int s, int tv, bool tlut, bool tlut_type, uint32_t lut_off,
+__device__ __noinline__ T4 fetch_texel(const uint16_t *tm, const RdpTile &t, int s, int tv, bool tlut, bool tlut_type, uint32_t lut_off,
                           uint32_t ax)
 {
 	if (tlut)
@@ -1263,7 +1290,7 @@ __device__ __forceinline__ T4 convert_factors(const T4 &in, const int16_t f[4])
 }
 
 // texture.h:498-923
-__device__ T4 sample_texture(const uint16_t *tm, const RdpTile &t, int s_in, int t_in, bool tlut, bool tlut_type,
+__device__ __noinline__ T4 sample_texture(const uint16_t *tm, const RdpTile &t, int s_in, int t_in, bool tlut, bool tlut_type,
                              bool sample_quad, bool mid_state, bool convert_one, bool bilerp, const int16_t *factors,
                              const T4 &prev)
 {
@@ -1490,7 +1517,7 @@ struct CombIn
 	int lod_frac, noise;
 };
 
-__device__ void combine(const CombIn &in, const uint8_t *rs, const uint8_t *as, int out[4])
+__device__ __noinline__ void combine(const CombIn &in, const uint8_t *rs, const uint8_t *as, int out[4])
 {
 #pragma unroll
 	for (int c = 0; c < 4; c++)
@@ -1607,7 +1634,7 @@ struct Pix
 	uint32_t cidx;
 };
 
-__device__ void blender(const int pix[4], const int mem[4], const uint8_t fog[4], const uint8_t bc[4], int shade_alpha,
+__device__ __noinline__ void blender(const int pix[4], const int mem[4], const uint8_t fog[4], const uint8_t bc[4], int shade_alpha,
                         const uint8_t *m, bool force_blend, bool blend_en, bool color_on_cvg, bool cvg_wrap,
                         const int bshift[2], bool final_cycle, int out[3])
 {
@@ -1846,9 +1873,20 @@ struct PassConst
 	bool alias;
 };
 
-__device__ bool shade_and_blend(const RdpPass &ps, const PassConst &pc, const RdpPrimGeom &g, const RdpPrimAttr &a,
-                                const RdpPrimShade &sh, const RdpTile *tiles, const uint16_t *tm, const SpanA &sa,
-                                const SpanX &sx, const SpanA &sa_next, const SpanX &sx_next, int x, int y, Pix &px)
+// Output of the shading stage for one pixel and primitive (the reference's ShadedData,
+// data_structures.h:319-325): coverage 0..8, or COPY (0x20) / FILL (0x40) flags.
+struct Shaded
+{
+	uint32_t combined; // r | g << 8 | b << 16 | a << 24
+	int z_dith;        // z << 9 | rgb dither, or the copy-pipe texel word
+	int coverage;
+	int shade_alpha;
+};
+
+// shading.h:38-359: everything that does not depend on the framebuffer.
+__device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const RdpPrimAttr &a, const RdpPrimShade &sh,
+                            const RdpTile *tiles, const uint16_t *tm, const SpanA &sa, const SpanX &sx,
+                            const SpanA &sa_next, const SpanX &sx_next, int x, int y, Shaded &out)
 {
 	if (!sx.valid) return false;
 	const uint32_t f = sh.static_flags;
@@ -1880,54 +1918,14 @@ __device__ bool shade_and_blend(const RdpPass &ps, const PassConst &pc, const Rd
 		else
 			texel = copy_word(tm, t0, st0, st1, s_offset, tlut);
 		if ((f & RS_ALPHA_TEST) && pc.fb_size == 2 && (texel & 1) == 0) return false;
-		// copy_pipeline (memory_interfacing.h:381-420)
-		uint32_t word = uint32_t(texel);
-		switch (ps.fb_fmt)
-		{
-		case FBF_I4: px.col[0] = px.col[1] = px.col[2] = px.col[3] = 0; px.cdirty = true; break;
-		case FBF_I8: { int v = int(word & 0xffu); write_color(ps.fb_fmt, px, v, v, v, v); break; }
-		case FBF_RGBA5551:
-			write_color(ps.fb_fmt, px, int((word >> 8) & 0xf8u), int((word >> 3) & 0xf8u), int((word << 2) & 0xf8u),
-			            int((word & 1) * 0xe0u));
-			break;
-		default: break;
-		}
-		if (pc.alias) alias_c2d(ps.fb_fmt, px);
-		return ps.fb_fmt == FBF_I4 || ps.fb_fmt == FBF_I8 || ps.fb_fmt == FBF_RGBA5551;
+		out.z_dith = texel;
+		out.coverage = 0x20;
+		return true;
 	}
 	if (f & RS_FILL)
 	{
-		if (!(x >= sx.start_x && x <= sx.end_x)) return false;
-		// fill_color (memory_interfacing.h:440-486)
-		uint32_t col = sh.fill_color;
-		switch (ps.fb_fmt)
-		{
-		case FBF_RGBA8888:
-			write_color(ps.fb_fmt, px, int((col >> 24) & 0xff), int((col >> 16) & 0xff), int((col >> 8) & 0xff), int(col & 0xff));
-			break;
-		case FBF_RGBA5551:
-			col >>= ((px.cidx & 1u) ^ 1u) * 16u;
-			write_color(ps.fb_fmt, px, int((col >> 8) & 0xf8u), int((col >> 3) & 0xf8u), int((col << 2) & 0xf8u),
-			            int((col & 1u) * 0xe0u));
-			break;
-		case FBF_IA88:
-		{
-			col >>= ((px.cidx & 1u) ^ 1u) * 16u;
-			int r = int((col >> 8) & 0xff);
-			write_color(ps.fb_fmt, px, r, r, r, int(col & 0xff));
-			break;
-		}
-		case FBF_I8:
-		{
-			col >>= ((px.cidx & 3u) ^ 3u) * 8u;
-			int v = int(col & 0xff);
-			write_color(ps.fb_fmt, px, v, v, v, v);
-			break;
-		}
-		default: break;
-		}
-		if (pc.alias) alias_c2d(ps.fb_fmt, px);
-		return ps.fb_fmt != FBF_I4;
+		out.coverage = 0x40;
+		return x >= sx.start_x && x <= sx.end_x;
 	}
 
 	// ---- coverage (coverage.h:31-47)
@@ -2188,8 +2186,73 @@ __device__ bool shade_and_blend(const RdpPass &ps, const PassConst &pc, const Rd
 		int thr = (f & RS_ALPHA_TEST_DITHER) ? int(noise & 0xffu) : int(sh.blend_color[3]);
 		if (alpha_ref < thr) return false;
 	}
-	int shade_alpha = min(shade[3] + alpha_d, 0xff);
 
+	out.combined = uint32_t(combined[0] & 0xff) | (uint32_t(combined[1] & 0xff) << 8) |
+	               (uint32_t(combined[2] & 0xff) << 16) | (uint32_t(combined[3] & 0xff) << 24);
+	out.z_dith = (z << 9) | rgb_d;
+	out.coverage = cov_count;
+	out.shade_alpha = min(shade[3] + alpha_d, 0xff);
+	return true;
+}
+
+// The framebuffer half: fill pipe, copy pipe or depth test + blender + dither + coverage
+// (memory_interfacing.h:381-571).  Returns whether the pixel was written.
+__device__ bool blend_pixel(const RdpPass &ps, const PassConst &pc, const RdpPrimShade &sh, const Shaded &in, Pix &px)
+{
+	if (in.coverage & 0x40)
+	{
+		uint32_t col = sh.fill_color;
+		switch (ps.fb_fmt)
+		{
+		case FBF_RGBA8888:
+			write_color(ps.fb_fmt, px, int((col >> 24) & 0xff), int((col >> 16) & 0xff), int((col >> 8) & 0xff), int(col & 0xff));
+			break;
+		case FBF_RGBA5551:
+			col >>= ((px.cidx & 1u) ^ 1u) * 16u;
+			write_color(ps.fb_fmt, px, int((col >> 8) & 0xf8u), int((col >> 3) & 0xf8u), int((col << 2) & 0xf8u),
+			            int((col & 1u) * 0xe0u));
+			break;
+		case FBF_IA88:
+		{
+			col >>= ((px.cidx & 1u) ^ 1u) * 16u;
+			int r = int((col >> 8) & 0xff);
+			write_color(ps.fb_fmt, px, r, r, r, int(col & 0xff));
+			break;
+		}
+		case FBF_I8:
+		{
+			col >>= ((px.cidx & 3u) ^ 3u) * 8u;
+			int v = int(col & 0xff);
+			write_color(ps.fb_fmt, px, v, v, v, v);
+			break;
+		}
+		default: break;
+		}
+		if (pc.alias) alias_c2d(ps.fb_fmt, px);
+		return ps.fb_fmt != FBF_I4;
+	}
+	if (in.coverage & 0x20)
+	{
+		uint32_t word = uint32_t(in.z_dith);
+		switch (ps.fb_fmt)
+		{
+		case FBF_I4: px.col[0] = px.col[1] = px.col[2] = px.col[3] = 0; px.cdirty = true; break;
+		case FBF_I8: { int v = int(word & 0xffu); write_color(ps.fb_fmt, px, v, v, v, v); break; }
+		case FBF_RGBA5551:
+			write_color(ps.fb_fmt, px, int((word >> 8) & 0xf8u), int((word >> 3) & 0xf8u), int((word << 2) & 0xf8u),
+			            int((word & 1) * 0xe0u));
+			break;
+		default: break;
+		}
+		if (pc.alias) alias_c2d(ps.fb_fmt, px);
+		return ps.fb_fmt == FBF_I4 || ps.fb_fmt == FBF_I8 || ps.fb_fmt == FBF_RGBA5551;
+	}
+	const int z = in.z_dith >> 9;
+	const int rgb_d = in.z_dith & 0x1ff;
+	int cov_count = in.coverage;
+	const int shade_alpha = in.shade_alpha;
+	int combined[4] = { int(in.combined & 0xff), int((in.combined >> 8) & 0xff), int((in.combined >> 16) & 0xff),
+	                    int(in.combined >> 24) };
 	// ---- depth_blend (memory_interfacing.h:488-571)
 	const uint32_t df = sh.db_flags;
 	const bool force_blend = (df & DB_FORCE_BLEND) != 0, image_read = (df & DB_IMAGE_READ) != 0;
@@ -2278,7 +2341,7 @@ __device__ bool shade_and_blend(const RdpPass &ps, const PassConst &pc, const Rd
 	        true, rgb);
 	if (df & DB_DITHER)
 	{
-		int dith = ((z << 9) | rgb_d) & 0x1ff;
+		int dith = rgb_d;
 #pragma unroll
 		for (int c = 0; c < 3; c++)
 		{
@@ -2310,24 +2373,282 @@ __device__ bool shade_and_blend(const RdpPass &ps, const PassConst &pc, const Rd
 	return true;
 }
 
-// ============================================================================ k_raster
-constexpr int RASTER_WARPS = 4;
 
-__global__ void __launch_bounds__(RASTER_WARPS * 32) k_raster(const RdpPass *__restrict__ passes, uint32_t num_passes,
-                                                             uint32_t num_items, const RdpPrimGeom *__restrict__ geom,
-                                                             const RdpPrimAttr *__restrict__ attr,
-                                                             const RdpPrimShade *__restrict__ shade,
-                                                             const RdpTile *__restrict__ tilesets,
-                                                             unsigned long long *__restrict__ fragments)
+__device__ __forceinline__ bool shade_and_blend(const RdpPass &ps, const PassConst &pc, const RdpPrimGeom &g,
+                                                const RdpPrimAttr &a, const RdpPrimShade &sh, const RdpTile *tiles,
+                                                const uint16_t *tm, const SpanA &sa, const SpanX &sx,
+                                                const SpanA &sa_next, const SpanX &sx_next, int x, int y, Pix &px)
 {
-	__shared__ SpanA s_sa[RASTER_WARPS][9];
-	__shared__ SpanX s_sx[RASTER_WARPS][9];
+	Shaded out;
+	if (!shade_pixel(pc, g, a, sh, tiles, tm, sa, sx, sa_next, sx_next, x, y, out)) return false;
+	return blend_pixel(ps, pc, sh, out, px);
+}
+
+// ============================================================================ pair list
+// Exclusive scan of the per-tile pair counts into offsets; counts are cleared for the next
+// launch.  ctrl[0] = total pairs, ctrl[1] = 1 when the pairs exceed the scratch capacity.
+__global__ void __launch_bounds__(1024) k_scan(uint32_t num_items, uint32_t *__restrict__ counts,
+                                               uint32_t *__restrict__ offsets, uint32_t *__restrict__ ctrl,
+                                               uint32_t capacity)
+{
+	__shared__ uint32_t warp_sums[32];
+	__shared__ uint32_t carry;
+	if (threadIdx.x == 0) carry = 0;
+	__syncthreads();
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	for (uint32_t base = 0; base < num_items; base += 1024)
+	{
+		uint32_t i = base + threadIdx.x;
+		uint32_t v = i < num_items ? counts[i] : 0u;
+		if (i < num_items) counts[i] = 0u;
+		uint32_t x = v;
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1)
+		{
+			uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+			if (lane >= o) x += y;
+		}
+		if (lane == 31) warp_sums[wid] = x;
+		__syncthreads();
+		if (wid == 0)
+		{
+			uint32_t w = warp_sums[lane];
+#pragma unroll
+			for (int o = 1; o < 32; o <<= 1)
+			{
+				uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+				if (lane >= o) w += y;
+			}
+			warp_sums[lane] = w;
+		}
+		__syncthreads();
+		uint32_t prefix = carry + (wid ? warp_sums[wid - 1] : 0u) + x - v;
+		if (i < num_items) offsets[i] = prefix;
+		__syncthreads();
+		if (threadIdx.x == 1023) carry = prefix + v;
+		__syncthreads();
+	}
+	if (threadIdx.x == 0)
+	{
+		offsets[num_items] = carry;
+		ctrl[0] = carry;
+		ctrl[1] = carry > capacity ? 1u : 0u;
+	}
+}
+
+// One warp per tile: turns the tile's primitive bitmask into its ordered run of
+// (primitive, tile) pairs and clears the bitmask.
+__global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes, uint32_t num_items,
+                         const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ ctrl, uint2 *__restrict__ pairs)
+{
+	uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	int lane = threadIdx.x & 31;
+	if (item >= num_items || ctrl[1]) return;
+	uint32_t pi = 0;
+	for (uint32_t k = 1; k < num_passes; k++)
+		if (passes[k].tile_item_begin <= item) pi = k;
+	const RdpPass &ps = passes[pi];
+	uint32_t tl = item - ps.tile_item_begin;
+	uint32_t *masks = ps.masks + size_t(tl) * RDP_MASK_WORDS_PER_TILE;
+	uint32_t nwords = (ps.prim_count + 31) / 32;
+	uint32_t out = offsets[item];
+	if (offsets[item + 1] == out) return;
+	for (uint32_t base = 0; base < nwords; base += 32)
+	{
+		uint32_t wi = base + lane;
+		uint32_t wv = wi < nwords ? masks[wi] : 0u;
+		uint32_t c = __popc(wv);
+		uint32_t x = c;
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1)
+		{
+			uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+			if (lane >= o) x += y;
+		}
+		uint32_t pos = out + x - c;
+		if (wv)
+		{
+			masks[wi] = 0u;
+			while (wv)
+			{
+				int b = __ffs(wv) - 1;
+				wv &= wv - 1;
+				pairs[pos++] = make_uint2(ps.prim_begin + wi * 32 + uint32_t(b), item);
+			}
+		}
+		out += __shfl_sync(0xffffffffu, x, 31);
+	}
+}
+
+// ============================================================================ k_shade
+// Shading of every (tile, primitive) pair in parallel (the reference's rasterizer.comp):
+// one 64-thread CTA per pair at a time, one pixel per thread.  Results go to scratch as
+// structure-of-arrays per pair: combined colour, z | dither, coverage | shade alpha << 8.
+constexpr int SHADE_THREADS = 64;
+
+__global__ void __launch_bounds__(SHADE_THREADS) k_shade(const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                                        const uint2 *__restrict__ pairs, const uint32_t *__restrict__ ctrl,
+                                                        const RdpPrimGeom *__restrict__ geom,
+                                                        const RdpPrimAttr *__restrict__ attr,
+                                                        const RdpPrimShade *__restrict__ shade,
+                                                        const RdpTile *__restrict__ tilesets,
+                                                        uint32_t *__restrict__ sc_color, int *__restrict__ sc_zdith,
+                                                        uint16_t *__restrict__ sc_misc)
+{
+	__shared__ SpanA s_sa[9];
+	__shared__ SpanX s_sx[9];
+	if (ctrl[1]) return;
+	const uint32_t total = ctrl[0];
+	const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+	for (uint32_t pr = blockIdx.x; pr < total; pr += gridDim.x)
+	{
+		uint2 pa = pairs[pr];
+		uint32_t prim = pa.x, item = pa.y;
+		uint32_t pi = 0;
+		for (uint32_t k = 1; k < num_passes; k++)
+			if (passes[k].tile_item_begin <= item) pi = k;
+		const RdpPass &ps = passes[pi];
+		uint32_t tl = item - ps.tile_item_begin;
+		int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
+		const RdpPrimGeom &g = geom[prim];
+		if (lane < 9)
+		{
+			if (wid == 0) span_attr(g, attr[prim], ty * 8 + lane, s_sa[lane]);
+			else span_x(g, ty * 8 + lane, s_sx[lane]);
+		}
+		__syncthreads();
+		PassConst pc;
+		switch (ps.fb_fmt)
+		{
+		case FBF_I4: pc.fb_size = 0; pc.dx_mask = 0; pc.dx_shift = 0; break;
+		case FBF_I8: pc.fb_size = 1; pc.dx_mask = ~7; pc.dx_shift = 3; break;
+		case FBF_RGBA5551:
+		case FBF_IA88: pc.fb_size = 2; pc.dx_mask = ~3; pc.dx_shift = 2; break;
+		default: pc.fb_size = 4; pc.dx_mask = ~1; pc.dx_shift = 1; break;
+		}
+		pc.alias = ps.fb_addr == ps.depth_addr;
+		int r = tid >> 3;
+		int x = tx * 8 + (tid & 7), y = ty * 8 + r;
+		Shaded out;
+		bool ok = false;
+		if (x < int(ps.fb_width) && y < int(ps.fb_height) && y >= g.span_ylo && y <= g.span_yhi)
+		{
+			const RdpPrimShade &sh = shade[prim];
+			ok = shade_pixel(pc, g, attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
+			                 ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, s_sa[r], s_sx[r], s_sa[r + 1], s_sx[r + 1],
+			                 x, y, out);
+		}
+		size_t at = size_t(pr) * SHADE_THREADS + tid;
+		if (ok)
+		{
+			sc_color[at] = out.combined;
+			sc_zdith[at] = out.z_dith;
+			sc_misc[at] = uint16_t((out.coverage & 0xff) | (out.shade_alpha << 8));
+		}
+		else
+			sc_misc[at] = 0x00ffu;
+		__syncthreads();
+	}
+}
+
+// ============================================================================ k_blend
+// One 64-thread CTA per tile: the tile's colour/depth stay in registers while its pairs are
+// applied in primitive order (the reference's depth_blend.comp), then written back.
+__global__ void __launch_bounds__(SHADE_THREADS) k_blend(const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                                        uint32_t num_items, const uint32_t *__restrict__ offsets,
+                                                        const uint2 *__restrict__ pairs, const uint32_t *__restrict__ ctrl,
+                                                        const RdpPrimShade *__restrict__ shade,
+                                                        const uint32_t *__restrict__ sc_color,
+                                                        const int *__restrict__ sc_zdith,
+                                                        const uint16_t *__restrict__ sc_misc,
+                                                        unsigned long long *__restrict__ counters)
+{
+	const uint32_t item = blockIdx.x;
+	if (item >= num_items || ctrl[1]) return;
+	const uint32_t p0 = offsets[item], p1 = offsets[item + 1];
+	if (p0 == p1) return;
+	uint32_t pi = 0;
+	for (uint32_t k = 1; k < num_passes; k++)
+		if (passes[k].tile_item_begin <= item) pi = k;
+	const RdpPass &ps = passes[pi];
+	const uint32_t tl = item - ps.tile_item_begin;
+	const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
+	const int tid = threadIdx.x;
+	const int x = tx * 8 + (tid & 7), y = ty * 8 + (tid >> 3);
+	const bool inside = x < int(ps.fb_width) && y < int(ps.fb_height);
+	PassConst pc;
+	switch (ps.fb_fmt)
+	{
+	case FBF_I4: pc.fb_size = 0; pc.dx_mask = 0; pc.dx_shift = 0; break;
+	case FBF_I8: pc.fb_size = 1; pc.dx_mask = ~7; pc.dx_shift = 3; break;
+	case FBF_RGBA5551:
+	case FBF_IA88: pc.fb_size = 2; pc.dx_mask = ~3; pc.dx_shift = 2; break;
+	default: pc.fb_size = 4; pc.dx_mask = ~1; pc.dx_shift = 1; break;
+	}
+	pc.alias = ps.fb_addr == ps.depth_addr;
+	uint32_t addr_index;
+	switch (ps.fb_fmt)
+	{
+	case FBF_I4:
+	case FBF_I8: addr_index = ps.fb_addr; break;
+	case FBF_RGBA5551:
+	case FBF_IA88: addr_index = ps.fb_addr >> 1; break;
+	default: addr_index = ps.fb_addr >> 2; break;
+	}
+	const uint32_t ci = addr_index + ps.fb_width * uint32_t(y) + uint32_t(x);
+	const uint32_t di = (ps.depth_addr >> 1) + ps.fb_width * uint32_t(y) + uint32_t(x);
+	Pix px;
+	uint32_t frags = 0;
+	if (inside)
+	{
+		load_pixel(ps, px, ci, di);
+		for (uint32_t pr = p0; pr < p1; pr++)
+		{
+			size_t at = size_t(pr) * SHADE_THREADS + tid;
+			uint32_t misc = sc_misc[at];
+			if ((misc & 0xff) == 0xff) continue;
+			Shaded in;
+			in.coverage = int(misc & 0xff);
+			in.shade_alpha = int(misc >> 8);
+			in.combined = sc_color[at];
+			in.z_dith = sc_zdith[at];
+			frags += blend_pixel(ps, pc, shade[pairs[pr].x], in, px);
+		}
+		store_pixel(ps, px, ci, di, pc.alias);
+	}
+	if (counters)
+	{
+		unsigned long long total = frags;
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+		if ((tid & 31) == 0 && total) atomicAdd(counters, total);
+		if (tid == 0) atomicAdd(counters + 1, 1ull);
+	}
+}
+
+// ============================================================================ k_raster
+// One CTA of 64 threads per 8x8 tile, one pixel per thread; warp w owns rows 4w..4w+3.
+// Both warps walk the tile's primitive bitmask in primitive order; pixel state stays in
+// registers for the whole pass (init_tile/finish_tile, memory_interfacing.h:286-362).
+constexpr int RASTER_THREADS = 64;
+
+__global__ void __launch_bounds__(RASTER_THREADS) k_raster(const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                                          uint32_t num_items, const RdpPrimGeom *__restrict__ geom,
+                                                          const RdpPrimAttr *__restrict__ attr,
+                                                          const RdpPrimShade *__restrict__ shade,
+                                                          const RdpTile *__restrict__ tilesets,
+                                                          unsigned long long *__restrict__ fragments,
+                                                          const uint32_t *__restrict__ ctrl)
+{
+	__shared__ SpanA s_sa[2][5];
+	__shared__ SpanX s_sx[2][5];
+	__shared__ int s_any;
 	const int wib = threadIdx.x >> 5;
 	const int lane = threadIdx.x & 31;
-	const uint32_t item = blockIdx.x * RASTER_WARPS + wib;
-	if (item >= num_items) return;
+	const uint32_t item = blockIdx.x;
+	// Only runs when the pair list overflowed the scratch capacity (ctrl[1]).
+	if (item >= num_items || !ctrl[1]) return;
 
-	// Locate the pass owning this tile item.
 	uint32_t pi = 0;
 	for (uint32_t k = 1; k < num_passes; k++)
 		if (passes[k].tile_item_begin <= item) pi = k;
@@ -2358,15 +2679,15 @@ __global__ void __launch_bounds__(RASTER_WARPS * 32) k_raster(const RdpPass *__r
 	}
 	const uint32_t depth_index = ps.depth_addr >> 1;
 
+	const int row0 = ty * 8 + wib * 4; // first row of this warp
 	const int px_x = tx * 8 + (lane & 7);
-	const int px_y0 = ty * 8 + (lane >> 3);
-	const bool in0 = px_x < int(ps.fb_width) && px_y0 < int(ps.fb_height);
-	const bool in1 = px_x < int(ps.fb_width) && (px_y0 + 4) < int(ps.fb_height);
-	const uint32_t ci0 = addr_index + ps.fb_width * uint32_t(px_y0) + uint32_t(px_x);
-	const uint32_t di0 = depth_index + ps.fb_width * uint32_t(px_y0) + uint32_t(px_x);
-	const uint32_t ci1 = ci0 + ps.fb_width * 4u, di1 = di0 + ps.fb_width * 4u;
+	const int px_y = row0 + (lane >> 3);
+	const int r = lane >> 3;
+	const bool inside = px_x < int(ps.fb_width) && px_y < int(ps.fb_height);
+	const uint32_t ci = addr_index + ps.fb_width * uint32_t(px_y) + uint32_t(px_x);
+	const uint32_t di = depth_index + ps.fb_width * uint32_t(px_y) + uint32_t(px_x);
 
-	Pix p0, p1;
+	Pix px;
 	bool loaded = false;
 	uint32_t frags = 0;
 
@@ -2375,7 +2696,6 @@ __global__ void __launch_bounds__(RASTER_WARPS * 32) k_raster(const RdpPass *__r
 		uint32_t wi = base + lane;
 		uint32_t wv = wi < nwords ? masks[wi] : 0u;
 		unsigned nz = __ballot_sync(0xffffffffu, wv != 0);
-		if (wv) masks[wi] = 0u; // self-clean for the next pass using this slot
 		while (nz)
 		{
 			int src = __ffs(nz) - 1;
@@ -2383,8 +2703,7 @@ __global__ void __launch_bounds__(RASTER_WARPS * 32) k_raster(const RdpPass *__r
 			uint32_t bits = __shfl_sync(0xffffffffu, wv, src);
 			if (!loaded)
 			{
-				if (in0) load_pixel(ps, p0, ci0, di0);
-				if (in1) load_pixel(ps, p1, ci1, di1);
+				if (inside) load_pixel(ps, px, ci, di);
 				loaded = true;
 			}
 			while (bits)
@@ -2393,38 +2712,42 @@ __global__ void __launch_bounds__(RASTER_WARPS * 32) k_raster(const RdpPass *__r
 				bits &= bits - 1;
 				uint32_t prim = ps.prim_begin + (base + src) * 32 + b;
 				const RdpPrimGeom &g = geom[prim];
-				// Cooperative span set-up for rows ty*8 .. ty*8+8 (the last row feeds pipelined texel1).
-				if (lane < 9)
-					span_attr(g, attr[prim], ty * 8 + lane, s_sa[wib][lane]);
-				else if (lane >= 16 && lane < 25)
-					span_x(g, ty * 8 + (lane - 16), s_sx[wib][lane - 16]);
+				const int ylo = g.span_ylo, yhi = g.span_yhi;
+				if (yhi < row0 || ylo > row0 + 3) continue; // no row of this warp is covered
+				// Spans for the warp's 4 rows plus the next row (pipelined texel1 peek).
+				if (lane < 5)
+					span_attr(g, attr[prim], row0 + lane, s_sa[wib][lane]);
+				else if (lane >= 16 && lane < 21)
+					span_x(g, row0 + (lane - 16), s_sx[wib][lane - 16]);
 				__syncwarp();
-				const RdpPrimShade &sh = shade[prim];
-				const RdpPrimAttr &a = attr[prim];
-				const RdpTile *tiles = tilesets + size_t(sh.tileset) * 8;
-				const uint16_t *tm = ps.tmem_snapshots + size_t(sh.tmem_index) * 2048;
-				const int r0 = lane >> 3;
-				if (in0 && px_y0 >= g.span_ylo && px_y0 <= g.span_yhi)
-					frags += shade_and_blend(ps, pc, g, a, sh, tiles, tm, s_sa[wib][r0], s_sx[wib][r0],
-					                         s_sa[wib][r0 + 1], s_sx[wib][r0 + 1], px_x, px_y0, p0);
-				if (in1 && px_y0 + 4 >= g.span_ylo && px_y0 + 4 <= g.span_yhi)
-					frags += shade_and_blend(ps, pc, g, a, sh, tiles, tm, s_sa[wib][r0 + 4], s_sx[wib][r0 + 4],
-					                         s_sa[wib][r0 + 5], s_sx[wib][r0 + 5], px_x, px_y0 + 4, p1);
+				if (inside && px_y >= ylo && px_y <= yhi)
+				{
+					const RdpPrimShade &sh = shade[prim];
+					frags += shade_and_blend(ps, pc, g, attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
+					                         ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, s_sa[wib][r],
+					                         s_sx[wib][r], s_sa[wib][r + 1], s_sx[wib][r + 1], px_x, px_y, px);
+				}
 				__syncwarp();
 			}
 		}
 	}
-	if (loaded)
-	{
-		if (in0) store_pixel(ps, p0, ci0, di0, pc.alias);
-		if (in1) store_pixel(ps, p1, ci1, di1, pc.alias);
-	}
+	if (loaded && inside) store_pixel(ps, px, ci, di, pc.alias);
+
+	// Both warps have consumed the bitmask: clear it for the next pass using this slot.
+	if (threadIdx.x == 0) s_any = 0;
+	__syncthreads();
+	if (loaded && lane == 0) s_any = 1;
+	__syncthreads();
+	if (s_any)
+		for (uint32_t wi = threadIdx.x; wi < nwords; wi += RASTER_THREADS) masks[wi] = 0u;
+
 	if (fragments)
 	{
 		unsigned long long total = frags;
 #pragma unroll
 		for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
 		if (lane == 0 && total) atomicAdd(fragments, total);
+		if (threadIdx.x == 0 && s_any) atomicAdd(fragments + 1, 1ull);
 	}
 }
 
@@ -2436,20 +2759,56 @@ extern "C" cudaError_t rdp_kernels_init_luts(const uint8_t *blender_lut)
 	return cudaMemcpyToSymbol(rdp::g_blender_lut, blender_lut, 0x8000);
 }
 
+extern "C" int rdp_kernels_shade_ctas_per_sm(void)
+{
+	int n = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, rdp::k_shade, rdp::SHADE_THREADS, 0) != cudaSuccess) n = 8;
+	return n > 0 ? n : 1;
+}
+
+extern "C" uint32_t rdp_kernels_count(const RdpLaunch *L)
+{
+	uint32_t n = 0;
+	if (L->num_prims) n += 2;
+	if (L->num_tmem_passes) n += 2;
+	if (L->num_prims && L->num_tile_items) n += 5;
+	return n;
+}
+
 extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t stream)
 {
+	const bool raster = L->num_prims && L->num_tile_items;
 	if (L->num_prims)
 	{
 		rdp::k_prim_setup<<<(L->num_prims + 127) / 128, 128, 0, stream>>>(L->prims_in, L->num_prims, L->words,
 		                                                                   L->state_blocks, L->passes, L->geom,
 		                                                                   L->attr, L->shade);
-		rdp::k_bin<<<(L->num_prims * 32 + 255) / 256, 256, 0, stream>>>(L->num_prims, L->geom, L->shade, L->passes);
+		rdp::k_bin<<<(L->num_prims * 32 + 255) / 256, 256, 0, stream>>>(L->num_prims, L->geom, L->shade, L->passes,
+		                                                                 L->tile_counts);
 	}
 	if (L->num_tmem_passes)
-		rdp::k_tmem<<<L->num_tmem_passes, 1024, 0, stream>>>(L->passes, L->tmem_pass_list, L->uploads);
-	if (L->num_prims && L->num_tile_items)
-		rdp::k_raster<<<(L->num_tile_items + rdp::RASTER_WARPS - 1) / rdp::RASTER_WARPS, rdp::RASTER_WARPS * 32, 0,
-		                stream>>>(L->passes, L->num_passes, L->num_tile_items, L->geom, L->attr, L->shade,
-		                          L->tilesets, L->fragments);
+	{
+		rdp::k_tmem_apply<<<dim3(L->max_uploads, L->num_tmem_passes), 256, 0, stream>>>(L->passes, L->tmem_pass_list,
+		                                                                                 L->uploads, L->tmem_keep);
+		rdp::k_tmem_carry<<<dim3(2048 / 32, L->num_tmem_passes), 32, 0, stream>>>(L->passes, L->tmem_pass_list,
+		                                                                         L->tmem_keep);
+	}
+	if (raster && L->raster_events[0]) cudaEventRecordWithFlags(L->raster_events[0], stream, cudaEventRecordExternal);
+	if (raster)
+	{
+		rdp::k_scan<<<1, 1024, 0, stream>>>(L->num_tile_items, L->tile_counts, L->pair_offsets, L->ctrl,
+		                                    L->pair_capacity);
+		rdp::k_expand<<<(L->num_tile_items * 32 + 255) / 256, 256, 0, stream>>>(
+			L->passes, L->num_passes, L->num_tile_items, L->pair_offsets, L->ctrl, L->pairs);
+		rdp::k_shade<<<L->shade_ctas, rdp::SHADE_THREADS, 0, stream>>>(L->passes, L->num_passes, L->pairs, L->ctrl,
+		                                                               L->geom, L->attr, L->shade, L->tilesets,
+		                                                               L->sc_color, L->sc_zdith, L->sc_misc);
+		rdp::k_blend<<<L->num_tile_items, rdp::SHADE_THREADS, 0, stream>>>(
+			L->passes, L->num_passes, L->num_tile_items, L->pair_offsets, L->pairs, L->ctrl, L->shade, L->sc_color,
+			L->sc_zdith, L->sc_misc, L->fragments);
+		rdp::k_raster<<<L->num_tile_items, rdp::RASTER_THREADS, 0, stream>>>(
+			L->passes, L->num_passes, L->num_tile_items, L->geom, L->attr, L->shade, L->tilesets, L->fragments, L->ctrl);
+	}
+	if (raster && L->raster_events[1]) cudaEventRecordWithFlags(L->raster_events[1], stream, cudaEventRecordExternal);
 	return cudaGetLastError();
 }

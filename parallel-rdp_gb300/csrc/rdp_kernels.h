@@ -20,8 +20,21 @@ typedef struct RdpLaunch
 	const uint32_t *tmem_pass_list;
 	uint32_t num_tmem_passes;
 	const RdpUpload *uploads;
+	uint32_t max_uploads;     /* largest upload count of the TMEM passes */
+	uint32_t *tmem_keep;      /* [num_tmem_passes][RDP_MAX_UPLOADS_PER_PASS][64] scratch bitmask */
 	uint32_t num_tile_items;
-	unsigned long long *fragments;
+	unsigned long long *fragments; /* [0] fragments, [1] touched tiles */
+	cudaEvent_t raster_events[2];   /* optional: recorded around the rasterisation kernels */
+	/* pair list + shading scratch */
+	uint32_t *tile_counts;          /* [num_tile_items], zero between launches */
+	uint32_t *pair_offsets;         /* [num_tile_items + 1] */
+	uint2 *pairs;                   /* [pair_capacity] (global primitive index, tile item) */
+	uint32_t *ctrl;                 /* [0] total pairs, [1] overflow */
+	uint32_t pair_capacity;
+	uint32_t shade_ctas;
+	uint32_t *sc_color;             /* [pair_capacity * 64] */
+	int *sc_zdith;
+	uint16_t *sc_misc;
 } RdpLaunch;
 
 #ifdef __cplusplus
@@ -29,6 +42,8 @@ extern "C" {
 #endif
 cudaError_t rdp_kernels_init_luts(const uint8_t *blender_lut);
 cudaError_t rdp_kernels_launch(const RdpLaunch *launch, cudaStream_t stream);
+uint32_t rdp_kernels_count(const RdpLaunch *launch);
+int rdp_kernels_shade_ctas_per_sm(void);
 #ifdef __cplusplus
 }
 #endif

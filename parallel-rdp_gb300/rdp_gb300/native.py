@@ -57,7 +57,8 @@ class _ScanoutOptions(ctypes.Structure):
 
 class _Stats(ctypes.Structure):
     _fields_ = [("primitives", ctypes.c_uint64), ("passes", ctypes.c_uint64), ("reference_passes", ctypes.c_uint64),
-                ("fragments", ctypes.c_uint64), ("tmem_uploads", ctypes.c_uint64)]
+                ("fragments", ctypes.c_uint64), ("tmem_uploads", ctypes.c_uint64), ("touched_tiles", ctypes.c_uint64),
+                ("kernel_launches", ctypes.c_uint64), ("staging_bytes", ctypes.c_uint64)]
 
 
 _VALIDATION_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p)
@@ -68,7 +69,8 @@ EXPORTED_SYMBOLS = [
     "rdp_cp_set_validation_callback", "rdp_cp_begin_read_rdram", "rdp_cp_end_write_rdram",
     "rdp_cp_begin_read_hidden_rdram", "rdp_cp_end_write_hidden_rdram", "rdp_cp_get_rdram_size",
     "rdp_cp_get_hidden_rdram_size", "rdp_cp_get_tmem", "rdp_cp_set_vi_register", "rdp_cp_scanout_sync",
-    "rdp_cp_get_stats",
+    "rdp_cp_get_stats", "rdp_cp_capture_begin", "rdp_cp_capture_end", "rdp_graph_replay", "rdp_graph_kernel_count",
+    "rdp_graph_destroy", "rdp_graph_last_raster_ms", "rdp_graph_raster_launches",
 ]
 
 
@@ -114,6 +116,17 @@ def lib():
     L.rdp_cp_scanout_sync.argtypes = [vp, ctypes.POINTER(_ScanoutOptions), vp, ctypes.POINTER(u32),
                                       ctypes.POINTER(u32)]
     L.rdp_cp_get_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
+    L.rdp_cp_capture_begin.argtypes = [vp]
+    L.rdp_cp_capture_end.argtypes = [vp, ctypes.POINTER(vp)]
+    L.rdp_graph_replay.argtypes = [vp, u32, ctypes.POINTER(ctypes.c_float)]
+    L.rdp_graph_kernel_count.argtypes = [vp]
+    L.rdp_graph_kernel_count.restype = u32
+    L.rdp_graph_destroy.argtypes = [vp]
+    L.rdp_graph_destroy.restype = None
+    L.rdp_graph_last_raster_ms.argtypes = [vp]
+    L.rdp_graph_last_raster_ms.restype = ctypes.c_float
+    L.rdp_graph_raster_launches.argtypes = [vp]
+    L.rdp_graph_raster_launches.restype = u32
     _lib = L
     return L
 
@@ -235,7 +248,40 @@ class CommandProcessor:
                                          ctypes.byref(h)), "scanout_sync")
         return buf[:w.value * h.value].reshape(h.value, w.value) if w.value else None
 
+    def capture(self, words):
+        """Records the passes of `words` into a CUDA graph (inputs resident in HBM)."""
+        _check(lib().rdp_cp_capture_begin(self._h), "capture_begin")
+        self.enqueue_command(words)
+        g = ctypes.c_void_p()
+        _check(lib().rdp_cp_capture_end(self._h, ctypes.byref(g)), "capture_end")
+        return Graph(g)
+
     def stats(self):
         s = _Stats()
         _check(lib().rdp_cp_get_stats(self._h, ctypes.byref(s)), "get_stats")
         return {k: getattr(s, k) for k, _ in _Stats._fields_}
+
+
+class Graph:
+    """A captured sync point (rdp_cp_capture_*): replay with inputs resident in HBM."""
+
+    def __init__(self, handle):
+        self._h = handle
+        self.kernels = lib().rdp_graph_kernel_count(handle)
+        self.raster_launches = lib().rdp_graph_raster_launches(handle)
+
+    def replay(self, count=1):
+        ms = ctypes.c_float()
+        _check(lib().rdp_graph_replay(self._h, count, ctypes.byref(ms)), "graph_replay")
+        return ms.value
+
+    def last_raster_ms(self):
+        return lib().rdp_graph_last_raster_ms(self._h)
+
+    def close(self):
+        if self._h:
+            lib().rdp_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

@@ -38,7 +38,8 @@ enum
 	RDP_ERR_OOM = 2,         /* device or pinned-host allocation failed */
 	RDP_ERR_TIMEOUT = 3,     /* a bounded wait expired */
 	RDP_ERR_INVALID = 4,     /* bad argument */
-	RDP_ERR_DEVICE = 5       /* a CUDA call failed */
+	RDP_ERR_DEVICE = 5,      /* a CUDA call failed */
+	RDP_ERR_TOO_LARGE = 6    /* a request exceeds a fixed capacity of an allocation-free entry point */
 };
 
 /* Validation errors reported through the callback (rdp_renderer.hpp:75-95). */
@@ -159,6 +160,44 @@ uint32_t rdp_graph_kernel_count(rdp_graph *g);
 float rdp_graph_last_raster_ms(rdp_graph *g);
 uint32_t rdp_graph_raster_launches(rdp_graph *g);
 void rdp_graph_destroy(rdp_graph *g);
+
+/* ---------------------------------------------------------------------------------------------
+ * Allocation-free TMEM update.  No counterpart in the reference: it exists for callers that must
+ * not allocate device memory -- for example an emulator frame loop that runs inside a CUDA stream
+ * capture (cudaMalloc is not allowed while a stream is being captured) or that must never stall on
+ * cudaMalloc/cudaFree, or a host application that owns all device memory through its own
+ * allocator and hands this library finished buffers only.
+ *
+ * It applies `num_uploads` TMEM upload descriptors to `tmem` (2048 16-bit words, updated in place),
+ * reading texels from `rdram`, and writes the TMEM image after each upload to `snapshots`
+ * ((num_uploads + 1) x 2048 words; snapshot 0 is the TMEM on entry).  All pointers are device
+ * pointers owned by the caller; the work is queued on `stream` (a cudaStream_t, NULL for the
+ * legacy stream) and the call returns without waiting.
+ *
+ * The stage's scratch bitmask lives in a fixed device array inside this library (256 KiB, held by
+ * every GPU that loads the library until the process exits), so num_uploads is limited to
+ * RDP_NOALLOC_MAX_UPLOADS; larger requests return RDP_ERR_TOO_LARGE without doing anything.
+ * The first call on each device looks up that array's device address (with the device current);
+ * make that first call before starting any stream capture.  All calls on a device share that
+ * device's one array and it keeps the last call's contents, so calls whose GPU work overlaps in
+ * time on the same device (for example on two streams) race: order them on one stream.  No call
+ * allocates memory. */
+#define RDP_NOALLOC_MAX_UPLOADS 1024
+
+typedef struct rdp_tmem_upload /* one TMEM upload plan; same layout as the reference's UploadInfo */
+{
+	int32_t width, height;
+	float min_t_mod, max_t_mod;
+	int32_t vram_addr, vram_width, vram_size, vram_effective_width;
+	int32_t tmem_offset, tmem_stride_words, tmem_size, tmem_fmt;
+	int32_t mode; /* 0 tile, 1 TLUT, 2 block */
+	float inv_tmem_stride_words;
+	int32_t dxt;
+	int32_t padding;
+} rdp_tmem_upload;
+
+int rdp_tmem_update_noalloc(const rdp_tmem_upload *uploads, uint32_t num_uploads, const uint8_t *rdram,
+                            uint32_t rdram_size, uint16_t *tmem, uint16_t *snapshots, void *stream);
 
 #ifdef __cplusplus
 }

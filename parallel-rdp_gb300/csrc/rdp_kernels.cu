@@ -2812,3 +2812,110 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 	if (raster && L->raster_events[1]) cudaEventRecordWithFlags(L->raster_events[1], stream, cudaEventRecordExternal);
 	return cudaGetLastError();
 }
+
+// ============================================================================ allocation-free TMEM update
+// A variant of k_tmem_apply / k_tmem_carry for callers that cannot allocate device memory: the
+// per-upload "word kept" bitmask lives in this file-scope array instead of a cudaMalloc'd buffer.
+// It is fully rewritten for every upload a call applies before it is read, so it needs no clearing.
+#include "../../include/rdp_cuda.h"
+#include <mutex>
+
+static_assert(sizeof(rdp_tmem_upload) == sizeof(RdpUpload), "rdp_tmem_upload must mirror RdpUpload");
+
+static __device__ __align__(256) uint32_t g_noalloc_tmem_keep[RDP_NOALLOC_MAX_UPLOADS * 64];
+
+namespace rdp {
+struct NoallocTmem
+{
+	const uint8_t *rdram;
+	uint32_t rdram_size;
+	uint16_t *tmem;
+	uint16_t *snapshots;
+	uint32_t count;
+};
+
+__global__ void k_tmem_apply_noalloc(NoallocTmem a, const RdpUpload *__restrict__ uploads, uint32_t *__restrict__ keep_bits)
+{
+	RdpPass ps = {};
+	ps.rdram = const_cast<uint8_t *>(a.rdram);
+	ps.rdram_size = a.rdram_size;
+	uint32_t u = blockIdx.x;
+	if (u >= a.count) return;
+	RdpUpload info = uploads[u];
+	uint16_t *dst = a.snapshots + size_t(u + 1) * 2048;
+	uint32_t *keep = keep_bits + size_t(u) * 64;
+	for (int gid = threadIdx.x; gid < 2048; gid += blockDim.x)
+	{
+		int idx = gid ^ 1;
+		bool upper = idx >= 0x400;
+		uint32_t v = 0;
+		bool wrote;
+		if (info.mode == 1) wrote = tmem_lut(ps, info, idx, v);
+		else
+		{
+			bool yuv = info.tmem_fmt == 1;
+			if (info.tmem_size == 3 || yuv) wrote = tmem_32(ps, info, idx & 0x3ff, upper, yuv, v);
+			else wrote = tmem_16(ps, info, idx, v);
+		}
+		if (wrote) dst[gid] = uint16_t(v);
+		unsigned m = __ballot_sync(0xffffffffu, !wrote);
+		if ((threadIdx.x & 31) == 0) keep[gid >> 5] = m;
+	}
+}
+
+__global__ void k_tmem_carry_noalloc(NoallocTmem a, const uint32_t *__restrict__ keep_bits)
+{
+	int gid = blockIdx.x * blockDim.x + threadIdx.x;
+	if (gid >= 2048) return;
+	uint16_t value = a.tmem[gid];
+	a.snapshots[gid] = value;
+	for (uint32_t u = 0; u < a.count; u++)
+	{
+		size_t at = size_t(u + 1) * 2048 + gid;
+		uint16_t written = a.snapshots[at];
+		bool keep_prev = (keep_bits[u * 64 + (gid >> 5)] >> (gid & 31)) & 1u;
+		if (keep_prev) a.snapshots[at] = value;
+		value = keep_prev ? value : written;
+	}
+	a.tmem[gid] = value;
+}
+} // namespace rdp
+
+namespace {
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+uint32_t *g_noalloc_keep_ptr[kNoallocMaxDevices] = {};
+}
+
+extern "C" int rdp_tmem_update_noalloc(const rdp_tmem_upload *uploads, uint32_t num_uploads, const uint8_t *rdram,
+                                       uint32_t rdram_size, uint16_t *tmem, uint16_t *snapshots, void *stream)
+{
+	if (num_uploads > RDP_NOALLOC_MAX_UPLOADS) return RDP_ERR_TOO_LARGE;
+	if (!rdram || !tmem || !snapshots || (num_uploads && !uploads)) return RDP_ERR_INVALID;
+	if (!rdram_size || (rdram_size & (rdram_size - 1))) return RDP_ERR_INVALID;
+	int device = 0;
+	if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kNoallocMaxDevices) return RDP_ERR_DEVICE;
+	uint32_t *keep;
+	{
+		// Per-device set-up, with that device current: the host-side name of the array is not a
+		// device address, so ask the runtime for the device address once.
+		std::lock_guard<std::mutex> hold(g_noalloc_mutex);
+		if (!g_noalloc_keep_ptr[device])
+		{
+			void *ptr = nullptr;
+			if (cudaGetSymbolAddress(&ptr, g_noalloc_tmem_keep) != cudaSuccess || !ptr)
+			{
+				cudaGetLastError();
+				return RDP_ERR_DEVICE;
+			}
+			g_noalloc_keep_ptr[device] = static_cast<uint32_t *>(ptr);
+		}
+		keep = g_noalloc_keep_ptr[device];
+	}
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	rdp::NoallocTmem a = { rdram, rdram_size, tmem, snapshots, num_uploads };
+	if (num_uploads)
+		rdp::k_tmem_apply_noalloc<<<num_uploads, 256, 0, s>>>(a, reinterpret_cast<const RdpUpload *>(uploads), keep);
+	rdp::k_tmem_carry_noalloc<<<2048 / 32, 32, 0, s>>>(a, keep);
+	return cudaGetLastError() == cudaSuccess ? RDP_OK : RDP_ERR_DEVICE;
+}

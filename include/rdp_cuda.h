@@ -110,21 +110,32 @@ int rdp_cp_get_tmem(rdp_cp *cp, uint16_t *out_2048_words);
 /* CommandProcessor::set_vi_register (rdp_device.cpp:970-975); reg is VIRegister (rdp_common.hpp:286-302). */
 int rdp_cp_set_vi_register(rdp_cp *cp, uint32_t reg, uint32_t value);
 
-/* ScanoutOptions subset (video_interface.hpp:31-81) honoured by rdp_cp_scanout_sync. */
+/* ScanoutOptions (video_interface.hpp:31-81) at 1x scale. */
 typedef struct rdp_scanout_options
 {
+	uint32_t crop_overscan_pixels;
+	uint32_t crop_rect_enable, crop_left, crop_right, crop_top, crop_bottom;
 	uint32_t persist_frame_on_invalid_input;
 	uint32_t blend_previous_frame;
-	uint32_t upscale_deinterlacing; /* must be 0 */
-	uint32_t crop_overscan_pixels;
+	uint32_t upscale_deinterlacing; /* 1 (default): serrate is not woven at 1x; 0: weave the fields */
+	uint32_t vi_aa, vi_scale, vi_serrate, vi_dither_filter, vi_divot_filter, vi_gamma_dither;
 } rdp_scanout_options;
+/* Fills the reference's defaults (every VI filter on, upscale deinterlacing on). */
+void rdp_scanout_options_default(rdp_scanout_options *opts);
 
-/* CommandProcessor::scanout_sync (rdp_device.cpp:1130-1182): renders the VI
- * output as RGBA8 into `rgba_out` (capacity in pixels given by *width x *height
- * on entry is not required: the buffer must hold 640 x 576 pixels), returning
- * the image size.  A width/height of 0 means no image (blank or invalid VI). */
+/* CommandProcessor::scanout_sync (rdp_device.cpp:1130-1182): renders everything
+ * queued, runs the VI filters on the device and writes the RGBA8 image
+ * (r | g << 8 | b << 16 | a << 24 per pixel) into `rgba_out`, which must hold
+ * 640 x 576 pixels.  A width/height of 0 means no image (blank or invalid VI
+ * state).  opts may be NULL for the defaults. */
 int rdp_cp_scanout_sync(rdp_cp *cp, const rdp_scanout_options *opts, uint32_t *rgba_out, uint32_t *width,
                         uint32_t *height);
+/* Per-scanline HStart/XScale (video_interface.hpp PerScanlineRegisterBits: 1 = HStart, 2 = XScale):
+ * CommandProcessor::begin/set/latch/end_vi_register_per_scanline (rdp_device.cpp:977-995). */
+int rdp_cp_begin_vi_register_per_scanline(rdp_cp *cp, uint32_t flags);
+int rdp_cp_set_vi_register_for_scanline(rdp_cp *cp, uint32_t reg_bit, uint32_t value);
+int rdp_cp_latch_vi_register_for_scanline(rdp_cp *cp, uint32_t vi_line);
+int rdp_cp_end_vi_register_per_scanline(rdp_cp *cp);
 
 /* Counters for benchmarking: primitives drawn, passes submitted, reference-equivalent
  * render passes (the reference's <=256-primitive segmentation, rdp_renderer.cpp:1564-1590),

@@ -45,6 +45,12 @@ def _load():
             getattr(L, n).restype = ctypes.c_int
         L.oracle_perspective_divide.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                 ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+        L.oracle_set_vi_register.argtypes = [vp, u32, u32]
+        L.oracle_vi_begin_per_scanline.argtypes = [vp, u32]
+        L.oracle_vi_set_for_scanline.argtypes = [vp, u32, u32]
+        L.oracle_vi_latch_scanline.argtypes = [vp, u32]
+        L.oracle_vi_end_per_scanline.argtypes = [vp]
+        L.oracle_scanout.argtypes = [vp, vp, vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
         L.oracle_noise.argtypes = [u32, u32, u32]
         L.oracle_noise.restype = ctypes.c_int
         _lib = L
@@ -101,6 +107,33 @@ class Oracle:
 
     def fragments(self):
         return self.L.oracle_fragments(self.h)
+
+    def write_hidden(self, data, offset=0):
+        d = np.ascontiguousarray(data, dtype=np.uint8)
+        self.L.oracle_write_hidden(self.h, d.ctypes.data, offset, d.size)
+
+    def set_vi_register(self, reg, value):
+        self.L.oracle_set_vi_register(self.h, int(reg), value & 0xffffffff)
+
+    def begin_vi_register_per_scanline(self, flags):
+        self.L.oracle_vi_begin_per_scanline(self.h, flags)
+
+    def set_vi_register_for_scanline(self, reg_bit, value):
+        self.L.oracle_vi_set_for_scanline(self.h, reg_bit, value & 0xffffffff)
+
+    def latch_vi_register_for_scanline(self, line):
+        self.L.oracle_vi_latch_scanline(self.h, line)
+
+    def end_vi_register_per_scanline(self):
+        self.L.oracle_vi_end_per_scanline(self.h)
+
+    def scanout(self, option_words):
+        """option_words: the 15 ScanoutOptions fields in C-ABI order.  Returns uint32[h, w] or None."""
+        opts = np.array(option_words, dtype=np.uint32)
+        buf = np.zeros(640 * 576, dtype=np.uint32)
+        w, h = ctypes.c_uint32(), ctypes.c_uint32()
+        self.L.oracle_scanout(self.h, opts.ctypes.data, buf.ctypes.data, ctypes.byref(w), ctypes.byref(h))
+        return buf[:w.value * h.value].reshape(h.value, w.value) if w.value else None
 
     def primitive_count(self):
         return self.L.oracle_primitive_count(self.h)

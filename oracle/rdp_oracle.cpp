@@ -229,6 +229,7 @@ struct Oracle
 	} constants;
 
 	uint32_t quirks = 1; // native_resolution_tex_rect on by default (rdp_device.hpp:79-83)
+	void *vi_state = nullptr; // owned VI oracle state (vi_oracle.cpp)
 
 	// Render-pass model.  The reference keeps a tile's colour/depth in registers for a
 	// whole render pass (init_tile/finish_tile, memory_interfacing.h:286-362): pixels are
@@ -3322,7 +3323,17 @@ void *oracle_create(uint32_t rdram_size, uint32_t hidden_size)
 	return o;
 }
 
-void oracle_destroy(void *h) { delete static_cast<Oracle *>(h); }
+void oracle_vi_destroy(void *vi);
+void oracle_destroy(void *h)
+{
+	Oracle *o = static_cast<Oracle *>(h);
+	if (o->vi_state) oracle_vi_destroy(o->vi_state);
+	delete o;
+}
+uint32_t oracle_rdram_size(void *h) { return static_cast<Oracle *>(h)->rdram_size; }
+uint32_t oracle_hidden_size(void *h) { return static_cast<Oracle *>(h)->hidden_size; }
+void *oracle_vi_state(void *h) { return static_cast<Oracle *>(h)->vi_state; }
+void oracle_set_vi_state(void *h, void *vi) { static_cast<Oracle *>(h)->vi_state = vi; }
 
 void oracle_write_rdram(void *h, const uint8_t *data, uint32_t offset, uint32_t size)
 {

@@ -22,6 +22,7 @@
 #include <stdlib.h>
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <deque>
 #include <mutex>
 #include <thread>
@@ -31,6 +32,7 @@
 #include "../../include/rdp_cuda.h"
 #include "rdp_types.h"
 #include "rdp_kernels.h"
+#include "vi.h"
 #include "blender_divider_runs.inc"
 
 namespace {
@@ -180,6 +182,26 @@ struct rdp_cp
 	std::vector<void *> captured_buffers;
 
 	uint32_t vi_regs[16] = {};
+	struct ViHost
+	{
+		// Per-scanline registers (video_interface.cpp:1102-1213).
+		uint32_t flags = 0;
+		bool ended = false;
+		unsigned line = 0;
+		uint32_t hs_latched = 0, xs_latched = 0;
+		uint32_t hs_line[640] = {}, xs_line[640] = {};
+		// Frame state (video_interface.hpp:149-161).
+		bool previous_frame_blank = false;
+		uint32_t frame_count = 0, last_valid_frame_count = 0;
+		bool have_prev = false;
+		int prev_w = 0, prev_h = 0;
+		// Device images.
+		uint32_t *d_aa = nullptr, *d_dv = nullptr, *d_out[2] = { nullptr, nullptr };
+		size_t aa_cap = 0, dv_cap = 0;
+		int cur = 0;
+		RdpViLine *d_lines = nullptr;
+		bool tables = false;
+	} vi;
 	rdp_validation_cb validation_cb = nullptr;
 	void *validation_user = nullptr;
 	int sticky_error = RDP_OK;
@@ -332,6 +354,11 @@ struct rdp_cp
 		cudaFree(d_shade);
 		cudaFree(d_staging);
 		cudaFree(d_fragments);
+		cudaFree(vi.d_aa);
+		cudaFree(vi.d_dv);
+		cudaFree(vi.d_out[0]);
+		cudaFree(vi.d_out[1]);
+		cudaFree(vi.d_lines);
 		if (host_registered) cudaHostUnregister(host_rdram);
 		if (own_host_rdram) free(host_rdram);
 		if (stream) cudaStreamDestroy(stream);
@@ -368,15 +395,17 @@ struct rdp_cp
 
 	int flush()
 	{
-		if (prims.empty() && uploads.empty())
-		{
-			reset_pass();
-			return sticky_error;
-		}
+		// CPU writes announced by end_write_rdram reach the device copy first, also for
+		// consumers that are not passes (scanout).
 		if (host_rdram_dirty)
 		{
 			if (check(cudaMemcpyAsync(d_rdram, host_rdram, rdram_size, cudaMemcpyHostToDevice, stream))) return sticky_error;
 			host_rdram_dirty = false;
+		}
+		if (prims.empty() && uploads.empty())
+		{
+			reset_pass();
+			return sticky_error;
 		}
 
 		Staging &st = staging[staging_index];
@@ -901,6 +930,307 @@ struct rdp_cp
 		return sticky_error;
 	}
 
+
+	// ================================================================= Video Interface
+	struct ViRegs
+	{
+		int vi_width, vi_offset, v_current_line, v_start, init_y_add, v_res, is_pal, max_x, max_y;
+		int h_start, h_res, h_start_clamp, h_res_clamp;
+		uint32_t status;
+	};
+
+	// decode_vi_registers (video_interface.cpp:177-367).
+	ViRegs vi_decode(RdpViLine *lines)
+	{
+		const uint32_t *R = vi_regs;
+		ViRegs r = {};
+		r.status = R[0];
+		r.vi_width = R[2] & 0xfff;
+		r.vi_offset = R[1] & 0xffffff;
+		r.v_current_line = R[4] & 1;
+		r.v_start = (R[10] >> 16) & 0x3ff;
+		int y_start = (R[13] >> 16) & 0xfff, y_add = R[13] & 0xfff;
+		r.init_y_add = y_add;
+		int v_end = R[10] & 0x3ff, v_sync = R[6] & 0x3ff;
+		r.is_pal = unsigned(v_sync) > 525u + 25u;
+		const int v_end_max = r.is_pal ? ((44 + 576) | 1) : ((34 + 480) | 1);
+		if (v_end > v_end_max) v_end = v_end_max;
+		if (r.v_start > v_end_max) r.v_start = v_end_max;
+		int v_start_offset = r.is_pal ? 44 : 34;
+		r.v_res = (v_end - r.v_start) >> 1;
+		r.v_start = (r.v_start - v_start_offset) / 2;
+		if (r.v_start < 0)
+		{
+			y_start -= y_add * r.v_start;
+			r.v_start = 0;
+		}
+		r.v_res = std::min(r.v_res, RDP_VI_MAX_LINES - r.v_start);
+		int hsc_lo = INT32_MAX, hec_hi = 0, hs_lo = INT32_MAX, he_hi = 0;
+		r.max_x = 0;
+		bool degenerate_y = r.v_res <= 0;
+		for (int i = 0; i < RDP_VI_MAX_LINES; i++)
+			if (degenerate_y || i < r.v_start || i >= r.v_start + r.v_res) lines[i] = RdpViLine{};
+		const int h_offset = r.is_pal ? 128 : 108;
+		auto analyze = [&](int x_start, int x_add, int h_start, int h_end, RdpViLine *line) {
+			bool lc = false, rc = false;
+			h_start -= h_offset;
+			h_end -= h_offset;
+			if (h_start < 0)
+			{
+				x_start -= x_add * h_start;
+				h_start = 0;
+				lc = true;
+			}
+			if (h_end > 640)
+			{
+				h_end = 640;
+				rc = true;
+			}
+			int hsc = h_start + (lc ? 0 : 8), hec = h_end - (rc ? 0 : 7);
+			int h_res = h_end - h_start;
+			r.max_x = std::max(r.max_x, (x_start + h_res * x_add) >> 10);
+			hs_lo = std::min(hs_lo, h_start);
+			he_hi = std::max(he_hi, h_end);
+			hsc_lo = std::min(hsc_lo, hsc);
+			hec_hi = std::max(hec_hi, hec);
+			if (line) *line = RdpViLine{ h_start, hsc, hec, x_start, x_add, y_start, y_add, 0 };
+		};
+		if (degenerate_y || !vi.ended)
+		{
+			RdpViLine li;
+			analyze((R[12] >> 16) & 0xfff, R[12] & 0xfff, (R[9] >> 16) & 0x3ff, R[9] & 0x3ff, &li);
+			for (int i = r.v_start; i < r.v_start + r.v_res; i++) lines[i] = li;
+		}
+		else
+		{
+			for (int i = r.v_start; i < r.v_start + r.v_res; i++)
+			{
+				int eff = 2 * i + v_start_offset + int(r.v_current_line == 0);
+				analyze((vi.xs_line[eff] >> 16) & 0xfff, vi.xs_line[eff] & 0xfff, (vi.hs_line[eff] >> 16) & 0x3ff,
+				        vi.hs_line[eff] & 0x3ff, &lines[i]);
+			}
+		}
+		r.max_y = (y_start + r.v_res * y_add) >> 10;
+		r.h_start = hs_lo;
+		r.h_res = he_hi - hs_lo;
+		r.h_start_clamp = hsc_lo;
+		r.h_res_clamp = hec_hi - hsc_lo;
+		return r;
+	}
+
+	int vi_ensure(uint32_t **buf, size_t *cap, size_t words)
+	{
+		if (*cap >= words) return RDP_OK;
+		cudaStreamSynchronize(stream);
+		cudaFree(*buf);
+		*buf = nullptr;
+		*cap = 0;
+		if (check(cudaMalloc(buf, words * 4))) return RDP_ERR_OOM;
+		*cap = words;
+		return RDP_OK;
+	}
+
+	// VideoInterface::scanout (video_interface.cpp:1215-1426) at 1x scale.
+	int scanout(const rdp_scanout_options *o, uint32_t *out, uint32_t *width, uint32_t *height)
+	{
+		*width = *height = 0;
+		int r0 = hard_flush();
+		if (r0 != RDP_OK) return r0;
+		if (!vi.tables)
+		{
+			if (check(rdp_vi_init_tables())) return sticky_error;
+			if (check(cudaMalloc(&vi.d_lines, sizeof(RdpViLine) * RDP_VI_MAX_LINES))) return RDP_ERR_OOM;
+			for (auto &b : vi.d_out)
+				if (check(cudaMalloc(&b, size_t(640) * 576 * 4))) return RDP_ERR_OOM;
+			vi.tables = true;
+		}
+		RdpViLine lines[RDP_VI_MAX_LINES];
+		ViRegs r = vi_decode(lines);
+		vi.flags = 0;
+		vi.ended = false;
+		if (r.vi_offset == 0)
+		{
+			vi.have_prev = false;
+			return RDP_OK;
+		}
+		if (!o->vi_serrate) r.status &= ~(1u << 6);
+		bool is_aa = (r.status & (3u << 8)) < (2u << 8) && o->vi_aa;
+		bool is_bilinear = (r.status & (3u << 8)) < (3u << 8) && o->vi_scale;
+		r.status &= ~((3u << 8) | (1u << 17) | (1u << 18));
+		if (is_aa) r.status |= 1u << 17;
+		if (is_bilinear) r.status |= 1u << 18;
+		if (!o->vi_gamma_dither) r.status &= ~(1u << 2);
+		if (!o->vi_divot_filter) r.status &= ~(1u << 4);
+		if (!o->vi_dither_filter) r.status &= ~(1u << 16);
+		bool is_blank = (r.status & 2u) == 0;
+		if (is_blank && vi.previous_frame_blank)
+		{
+			vi.frame_count++;
+			vi.have_prev = false;
+			return RDP_OK;
+		}
+		if (is_blank) vi.have_prev = false;
+		r.status |= 2u;
+		vi.previous_frame_blank = is_blank;
+		bool divot = (r.status & (1u << 4)) != 0;
+		if (r.h_res <= 0 || r.h_start >= 640)
+		{
+			vi.frame_count++;
+			if (o->persist_frame_on_invalid_input && (vi.frame_count - vi.last_valid_frame_count < 4) && vi.have_prev)
+			{
+				*width = uint32_t(vi.prev_w);
+				*height = uint32_t(vi.prev_h);
+				return check(cudaMemcpy(out, vi.d_out[vi.cur ^ 1], size_t(vi.prev_w) * vi.prev_h * 4, cudaMemcpyDeviceToHost));
+			}
+			vi.have_prev = false;
+			return RDP_OK;
+		}
+		vi.last_valid_frame_count = vi.frame_count;
+		bool degenerate = r.h_res <= 0 || r.v_res <= 0;
+		bool is_8888 = (r.status & 3u) == 3u;
+
+		RdpViParams p = {};
+		p.rdram = d_rdram;
+		p.hidden = d_hidden;
+		p.rdram_size = rdram_size;
+		p.fb_offset = is_8888 ? (r.vi_offset >> 2) : (r.vi_offset >> 1);
+		p.fb_width = r.vi_width;
+		p.is_8888 = is_8888;
+		p.fetch_aa = (r.status & (1u << 17)) != 0;
+		p.dither_filter = (r.status & (1u << 16)) != 0;
+		p.divot = divot;
+		p.fetch_bug = r.init_y_add < 1024;
+		p.degenerate = degenerate;
+		if (!degenerate)
+		{
+			p.aa_w = r.max_x + 3 + int(divot) * 2;
+			p.aa_h = r.max_y + 2;
+			if (vi_ensure(&vi.d_aa, &vi.aa_cap, size_t(p.aa_w) * p.aa_h * 2) != RDP_OK) return RDP_ERR_OOM;
+			p.aa = vi.d_aa;
+			if (divot)
+			{
+				p.dv_w = r.max_x + 2;
+				p.dv_h = r.max_y + 2;
+				if (vi_ensure(&vi.d_dv, &vi.dv_cap, size_t(p.dv_w) * p.dv_h * 2) != RDP_OK) return RDP_ERR_OOM;
+				p.dv = vi.d_dv;
+			}
+			else
+			{
+				p.dv = p.aa;
+				p.dv_w = p.aa_w;
+				p.dv_h = p.aa_h;
+			}
+		}
+
+		bool serrate = (r.status & (1u << 6)) != 0 && !o->upscale_deinterlacing;
+		int w = 640, h = (r.is_pal ? 576 : 480) >> int(!serrate);
+		unsigned cl, cr, ct, cb;
+		if (o->crop_rect_enable)
+		{
+			cl = o->crop_left; cr = o->crop_right; ct = o->crop_top; cb = o->crop_bottom;
+			if (serrate) { ct *= 2; cb *= 2; }
+		}
+		else
+		{
+			unsigned cy = o->crop_overscan_pixels * (serrate ? 2 : 1);
+			unsigned cx = unsigned(std::round(float(cy) * (float(w) / float(h))));
+			cl = cr = cx;
+			ct = cb = cy;
+		}
+		if (cl + cr < unsigned(w) && ct + cb < unsigned(h))
+		{
+			w -= int(cl + cr);
+			h -= int(ct + cb);
+		}
+		p.lines = vi.d_lines;
+		p.out = vi.d_out[vi.cur];
+		p.out_w = w;
+		p.out_h = h;
+		p.prev = vi.d_out[vi.cur ^ 1];
+		p.prev_w = vi.prev_w;
+		p.prev_h = vi.prev_h;
+		p.crop_left = int(cl);
+		p.crop_top = int(ct);
+		p.v_start = r.v_start;
+		p.v_res = r.v_res;
+		if (serrate)
+		{
+			p.v_start *= 2;
+			p.v_res *= 2;
+			p.serrate_shift = 1;
+			p.serrate_mask = 1;
+			p.serrate_select = int(r.v_current_line == 0);
+			p.info_y_shift = 1;
+		}
+		p.h_start = r.h_start;
+		p.h_res = r.h_res;
+		p.h_start_clamp = r.h_start_clamp;
+		p.h_res_clamp = r.h_res_clamp;
+		p.draw = !degenerate && r.h_res > 0 && r.v_res > 0;
+		p.init_y_add = r.init_y_add;
+		p.frame_count = vi.frame_count;
+		p.scale_aa = (r.status & (1u << 18)) != 0;
+		p.gamma = (r.status & (1u << 3)) != 0;
+		p.gamma_dither = (r.status & (1u << 2)) != 0;
+		p.blend_prev = vi.have_prev && o->blend_previous_frame;
+		if (check(cudaMemcpyAsync(vi.d_lines, lines, sizeof(lines), cudaMemcpyHostToDevice, stream))) return sticky_error;
+		if (check(rdp_vi_launch(&p, stream))) return sticky_error;
+		if (check(cudaMemcpyAsync(out, p.out, size_t(w) * h * 4, cudaMemcpyDeviceToHost, stream))) return sticky_error;
+		if (check(cudaStreamSynchronize(stream))) return sticky_error;
+		*width = uint32_t(w);
+		*height = uint32_t(h);
+		vi.prev_w = w;
+		vi.prev_h = h;
+		vi.have_prev = true;
+		vi.cur ^= 1;
+		vi.frame_count++;
+		return RDP_OK;
+	}
+
+	void vi_begin_per_scanline(uint32_t flags)
+	{
+		vi.flags = flags;
+		vi.hs_latched = vi_regs[9];
+		vi.xs_latched = vi_regs[12];
+		vi.hs_line[0] = vi_regs[9];
+		vi.xs_line[0] = vi_regs[12];
+		vi.line = 0;
+		vi.ended = false;
+	}
+	void vi_set_for_scanline(uint32_t reg, uint32_t value)
+	{
+		if ((vi.flags & reg) == 0) return;
+		if (reg == 1) vi.hs_latched = value;
+		else if (reg == 2) vi.xs_latched = value;
+	}
+	void vi_latch_scanline(unsigned line)
+	{
+		const unsigned v_end_max = (44 + 576) | 1;
+		line = std::min(line, v_end_max - 1);
+		if (line <= vi.line) return;
+		unsigned c = vi.line;
+		while (++c < line)
+		{
+			vi.hs_line[c] = vi.hs_line[vi.line];
+			vi.xs_line[c] = vi.xs_line[vi.line];
+		}
+		vi.hs_line[c] = vi.hs_latched;
+		vi.xs_line[c] = vi.xs_latched;
+		vi.line = c;
+	}
+	void vi_end_per_scanline()
+	{
+		const unsigned v_end_max = (44 + 576) | 1;
+		if (vi.flags == 0 || vi.ended) return;
+		unsigned c = vi.line;
+		while (++c < v_end_max)
+		{
+			vi.hs_line[c] = vi.hs_line[vi.line];
+			vi.xs_line[c] = vi.xs_line[vi.line];
+		}
+		vi.ended = true;
+	}
+
 	// ================================================================= timeline + coherency
 	cudaEvent_t get_event()
 	{
@@ -1127,6 +1457,52 @@ int rdp_cp_set_vi_register(rdp_cp *cp, uint32_t reg, uint32_t value)
 {
 	if (!cp || reg >= 14) return RDP_ERR_INVALID;
 	cp->vi_regs[reg] = value;
+	return RDP_OK;
+}
+
+void rdp_scanout_options_default(rdp_scanout_options *o)
+{
+	if (!o) return;
+	memset(o, 0, sizeof(*o));
+	o->upscale_deinterlacing = 1;
+	o->vi_aa = o->vi_scale = o->vi_serrate = o->vi_dither_filter = o->vi_divot_filter = o->vi_gamma_dither = 1;
+}
+
+int rdp_cp_scanout_sync(rdp_cp *cp, const rdp_scanout_options *opts, uint32_t *rgba_out, uint32_t *width,
+                        uint32_t *height)
+{
+	if (!cp || !rgba_out || !width || !height) return RDP_ERR_INVALID;
+	rdp_scanout_options defaults;
+	rdp_scanout_options_default(&defaults);
+	cudaSetDevice(cp->device);
+	return cp->scanout(opts ? opts : &defaults, rgba_out, width, height);
+}
+
+int rdp_cp_begin_vi_register_per_scanline(rdp_cp *cp, uint32_t flags)
+{
+	if (!cp) return RDP_ERR_INVALID;
+	cp->vi_begin_per_scanline(flags);
+	return RDP_OK;
+}
+
+int rdp_cp_set_vi_register_for_scanline(rdp_cp *cp, uint32_t reg_bit, uint32_t value)
+{
+	if (!cp) return RDP_ERR_INVALID;
+	cp->vi_set_for_scanline(reg_bit, value);
+	return RDP_OK;
+}
+
+int rdp_cp_latch_vi_register_for_scanline(rdp_cp *cp, uint32_t vi_line)
+{
+	if (!cp) return RDP_ERR_INVALID;
+	cp->vi_latch_scanline(vi_line);
+	return RDP_OK;
+}
+
+int rdp_cp_end_vi_register_per_scanline(rdp_cp *cp)
+{
+	if (!cp) return RDP_ERR_INVALID;
+	cp->vi_end_per_scanline();
 	return RDP_OK;
 }
 

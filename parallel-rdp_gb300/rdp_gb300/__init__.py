@@ -9,6 +9,7 @@ from .native import (  # noqa: F401
     CommandProcessor,
     RdpError,
     RdpTimeout,
+    ScanoutOptions,
     VIRegister,
     device_is_supported,
     library_path,

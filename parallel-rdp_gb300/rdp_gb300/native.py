@@ -50,9 +50,26 @@ class _CreateInfo(ctypes.Structure):
                 ("hidden_rdram_size", ctypes.c_size_t), ("flags", ctypes.c_uint32), ("device", ctypes.c_int)]
 
 
-class _ScanoutOptions(ctypes.Structure):
-    _fields_ = [("persist_frame_on_invalid_input", ctypes.c_uint32), ("blend_previous_frame", ctypes.c_uint32),
-                ("upscale_deinterlacing", ctypes.c_uint32), ("crop_overscan_pixels", ctypes.c_uint32)]
+class ScanoutOptions(ctypes.Structure):
+    """ScanoutOptions (video_interface.hpp:31-81) at 1x scale; defaults as the reference."""
+    _fields_ = [("crop_overscan_pixels", ctypes.c_uint32), ("crop_rect_enable", ctypes.c_uint32),
+                ("crop_left", ctypes.c_uint32), ("crop_right", ctypes.c_uint32), ("crop_top", ctypes.c_uint32),
+                ("crop_bottom", ctypes.c_uint32), ("persist_frame_on_invalid_input", ctypes.c_uint32),
+                ("blend_previous_frame", ctypes.c_uint32), ("upscale_deinterlacing", ctypes.c_uint32),
+                ("vi_aa", ctypes.c_uint32), ("vi_scale", ctypes.c_uint32), ("vi_serrate", ctypes.c_uint32),
+                ("vi_dither_filter", ctypes.c_uint32), ("vi_divot_filter", ctypes.c_uint32),
+                ("vi_gamma_dither", ctypes.c_uint32)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.upscale_deinterlacing = 1
+        for k in ("vi_aa", "vi_scale", "vi_serrate", "vi_dither_filter", "vi_divot_filter", "vi_gamma_dither"):
+            setattr(self, k, 1)
+        for k, v in kw.items():
+            setattr(self, k, int(v))
+
+    def as_words(self):
+        return [getattr(self, k) for k, _ in self._fields_]
 
 
 class _Stats(ctypes.Structure):
@@ -70,7 +87,9 @@ EXPORTED_SYMBOLS = [
     "rdp_cp_begin_read_hidden_rdram", "rdp_cp_end_write_hidden_rdram", "rdp_cp_get_rdram_size",
     "rdp_cp_get_hidden_rdram_size", "rdp_cp_get_tmem", "rdp_cp_set_vi_register", "rdp_cp_scanout_sync",
     "rdp_cp_get_stats", "rdp_cp_capture_begin", "rdp_cp_capture_end", "rdp_graph_replay", "rdp_graph_kernel_count",
-    "rdp_graph_destroy", "rdp_graph_last_raster_ms", "rdp_graph_raster_launches",
+    "rdp_graph_destroy", "rdp_graph_last_raster_ms", "rdp_graph_raster_launches", "rdp_scanout_options_default",
+    "rdp_cp_begin_vi_register_per_scanline", "rdp_cp_set_vi_register_for_scanline",
+    "rdp_cp_latch_vi_register_for_scanline", "rdp_cp_end_vi_register_per_scanline",
 ]
 
 
@@ -113,8 +132,12 @@ def lib():
     L.rdp_cp_get_hidden_rdram_size.restype = sz
     L.rdp_cp_get_tmem.argtypes = [vp, vp]
     L.rdp_cp_set_vi_register.argtypes = [vp, u32, u32]
-    L.rdp_cp_scanout_sync.argtypes = [vp, ctypes.POINTER(_ScanoutOptions), vp, ctypes.POINTER(u32),
+    L.rdp_cp_scanout_sync.argtypes = [vp, ctypes.POINTER(ScanoutOptions), vp, ctypes.POINTER(u32),
                                       ctypes.POINTER(u32)]
+    L.rdp_cp_begin_vi_register_per_scanline.argtypes = [vp, u32]
+    L.rdp_cp_set_vi_register_for_scanline.argtypes = [vp, u32, u32]
+    L.rdp_cp_latch_vi_register_for_scanline.argtypes = [vp, u32]
+    L.rdp_cp_end_vi_register_per_scanline.argtypes = [vp]
     L.rdp_cp_get_stats.argtypes = [vp, ctypes.POINTER(_Stats)]
     L.rdp_cp_capture_begin.argtypes = [vp]
     L.rdp_cp_capture_end.argtypes = [vp, ctypes.POINTER(vp)]
@@ -239,9 +262,9 @@ class CommandProcessor:
     def set_vi_register(self, reg, value):
         _check(lib().rdp_cp_set_vi_register(self._h, int(reg), value & 0xffffffff), "set_vi_register")
 
-    def scanout_sync(self, blend_previous_frame=True, persist_frame_on_invalid_input=False, crop_overscan_pixels=0):
-        opts = _ScanoutOptions(int(persist_frame_on_invalid_input), int(blend_previous_frame), 0,
-                               crop_overscan_pixels)
+    def scanout_sync(self, options=None, **kw):
+        """Returns the RGBA8 scanout as uint32[h, w] (r | g << 8 | b << 16 | a << 24), or None."""
+        opts = options if options is not None else ScanoutOptions(**kw)
         buf = np.zeros(640 * 576, dtype=np.uint32)
         w, h = ctypes.c_uint32(), ctypes.c_uint32()
         _check(lib().rdp_cp_scanout_sync(self._h, ctypes.byref(opts), buf.ctypes.data, ctypes.byref(w),
@@ -255,6 +278,33 @@ class CommandProcessor:
         g = ctypes.c_void_p()
         _check(lib().rdp_cp_capture_end(self._h, ctypes.byref(g)), "capture_end")
         return Graph(g)
+
+    def begin_vi_register_per_scanline(self, flags):
+        _check(lib().rdp_cp_begin_vi_register_per_scanline(self._h, flags), "begin_vi_register_per_scanline")
+
+    def set_vi_register_for_scanline(self, reg_bit, value):
+        _check(lib().rdp_cp_set_vi_register_for_scanline(self._h, reg_bit, value & 0xffffffff), "set_for_scanline")
+
+    def latch_vi_register_for_scanline(self, line):
+        _check(lib().rdp_cp_latch_vi_register_for_scanline(self._h, line), "latch_for_scanline")
+
+    def end_vi_register_per_scanline(self):
+        _check(lib().rdp_cp_end_vi_register_per_scanline(self._h), "end_vi_register_per_scanline")
+
+    def write_hidden_rdram(self, data):
+        """Replaces hidden RDRAM (begin_read_hidden_rdram + end_write_hidden_rdram)."""
+        p = lib().rdp_cp_begin_read_hidden_rdram(self._h)
+        if not p:
+            raise RdpError(RDP_ERR_DEVICE, "begin_read_hidden_rdram")
+        d = np.ascontiguousarray(data, dtype=np.uint8)[:self.hidden_rdram_size]
+        ctypes.memmove(p, d.ctypes.data, d.size)
+        _check(lib().rdp_cp_end_write_hidden_rdram(self._h), "end_write_hidden_rdram")
+
+    def write_rdram(self, data):
+        """Replaces RDRAM contents in the caller-owned buffer and uploads it (end_write_rdram)."""
+        self.idle()
+        self._rdram[:self.rdram_size] = np.ascontiguousarray(data, dtype=np.uint8)[:self.rdram_size]
+        self.end_write_rdram()
 
     def stats(self):
         s = _Stats()

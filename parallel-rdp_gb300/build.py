@@ -58,7 +58,7 @@ def build(verbose=False):
     gen_src = os.path.join(CSRC, "cmdgen.cpp")
     gen_lib = os.path.join(OUT, "librdp_cmdgen.so")
     if _newer([gen_src, os.path.join(INCLUDE, "rdp_cmdgen.h")], gen_lib):
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I" + INCLUDE, "-o", gen_lib, gen_src])
+        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I" + INCLUDE, "-o", gen_lib, gen_src])
     return lib, gen_lib
 
 

@@ -55,7 +55,52 @@ struct Rng
 	double normal()
 	{
 		double u1 = std::max(uniform(), 1e-300), u2 = uniform();
-		return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+		return sqrt(-2.0 * det_log(u1)) * det_cos(6.283185307179586 * u2);
+	}
+
+	// exp / log / cos from their series with only +, -, *, / and exact scaling, so
+	// that the generated streams are identical on every host (libm results and FMA
+	// contraction differ between x86-64 and AArch64).
+	static double det_exp(double x)
+	{
+		const double ln2 = 0.6931471805599453;
+		double k = floor(x / ln2 + 0.5);
+		double r = x - k * ln2, term = 1.0, sum = 1.0;
+		for (int n = 1; n < 24; n++)
+		{
+			term = term * r / double(n);
+			sum += term;
+		}
+		return ldexp(sum, int(k));
+	}
+	static double det_log(double x)
+	{
+		int e;
+		double m = frexp(x, &e); // x = m * 2^e, m in [0.5, 1)
+		if (m < 0.7071067811865476)
+		{
+			m *= 2.0;
+			e -= 1;
+		}
+		double z = (m - 1.0) / (m + 1.0), z2 = z * z, term = z, sum = 0.0;
+		for (int n = 1; n < 60; n += 2)
+		{
+			sum += term / double(n);
+			term *= z2;
+		}
+		return 2.0 * sum + double(e) * 0.6931471805599453;
+	}
+	static double det_cos(double a)
+	{
+		const double two_pi = 6.283185307179586;
+		a -= two_pi * floor(a / two_pi + 0.5); // [-pi, pi]
+		double a2 = a * a, term = 1.0, sum = 1.0;
+		for (int n = 2; n < 40; n += 2)
+		{
+			term = -term * a2 / (double(n - 1) * double(n));
+			sum += term;
+		}
+		return sum;
 	}
 };
 
@@ -413,7 +458,7 @@ struct Gen
 	// A random triangle: centroid uniform over the screen, log-normal area.
 	void random_triangle_geometry(Vertex v[3])
 	{
-		double area = p.area_median * exp(p.area_sigma * rng.normal());
+		double area = p.area_median * Rng::det_exp(p.area_sigma * rng.normal());
 		area = std::min(area, double(p.width) * double(p.height));
 		double cx = rng.uniform() * p.width, cy = rng.uniform() * p.height;
 		double px[3], py[3];
@@ -424,8 +469,8 @@ struct Gen
 			{
 				double ang = rng.uniform() * 6.283185307179586;
 				double r = 0.3 + 0.7 * rng.uniform();
-				px[i] = cos(ang) * r;
-				py[i] = sin(ang) * r;
+				px[i] = Rng::det_cos(ang) * r;
+				py[i] = Rng::det_cos(ang - 1.5707963267948966) * r;
 			}
 			a = 0.5 * fabs((px[1] - px[0]) * (py[2] - py[0]) - (px[2] - px[0]) * (py[1] - py[0]));
 			if (a > 0.05) break;

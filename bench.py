@@ -1,24 +1,33 @@
 """Benchmark of the GB300 RDP path.
 
-One step = one frame of the workload: a textured, depth-tested 320x240
-RGBA5551 + Z16 frame, 2-cycle, 10,000 perspective-correct triangles (log-normal
-area, median 48 px), RGBA16 32x32 textures with random wrap/mirror/clamp,
-bilinear filtering, random combiner inputs, fog blender, Z compare + update,
-coverage AA and magic-square dither, generated from seed 0.
+Default workload (--workload batched): the batched-instances configuration --
+64 independent emulator instances, each with its own 8 MiB RDRAM and 4 KiB TMEM,
+resolutions drawn from 320x240 / 640x240 / 640x480, primitive counts log-uniform
+in 500-50,000 per frame, the mixed RGBA8888 primitive mix (40% textured
+triangles, 30% copy-mode TextureRectangles, 20% CI8 + TLUT triangles, 10%
+FillRects; alpha compare, LOD/detail and Z on half the primitives), per-instance
+seeds 0-63.  One step = one frame of every instance (one sync point).
 
-value  : reference-equivalent render passes per second with every input already
-         resident in HBM (the frame's passes replayed as a CUDA graph; CUDA events
-         on the processor's stream; L2 flushed between timed iterations).
-e2e    : the same metric through the C ABI with host buffers: command words in
-         host memory are parsed, packed and copied H2D, the frame renders, and the
-         written framebuffer is copied D2H into the caller's RDRAM, every step.
-roofline: the rasteriser kernel (k_raster) -- algorithmic framebuffer bytes of the
-         touched tiles / its CUDA-event duration, against the measured HBM copy peak.
+value  : reference-equivalent render passes per second (the reference's pass rule,
+         counted by the host emulation of its need_flush) of the BATCHED path with
+         every input resident in HBM: the sync point's rounds replayed as a CUDA
+         graph; CUDA events on the batch's stream; L2 flushed between iterations.
+plain  : the same frames through the plain single-instance path, one processor and
+         one CUDA graph per instance, run one after another.
+e2e    : the batched path through the C ABI with host buffers: every instance's
+         command words are parsed, packed and copied H2D, all instances render, and
+         written framebuffers are copied D2H into each caller's RDRAM, every step.
+roofline: the dominant kernel (k_shade): algorithmic bytes of its output (10 B per
+         pixel of every shaded (primitive, 8x8 tile) instance, the reference's
+         shaded-data record) plus the 8 B pair entry, per launch, over its
+         CUDA-event duration, against the measured HBM copy peak.
 cpu_baseline: the CPU oracle (a scalar restatement of the reference's algorithm)
-         timed on this host on a bounded sample of the same frames.
+         over the instances on all host cores, on a bounded sample (>= 10 s).
 
---impl reference times the reference algorithm on the host CPU (the oracle; the
-reference's own Vulkan/Angrylion build is not available) with the same metric.
+--workload textured measures the single textured, depth-tested 320x240 frame
+(10,000 triangles) instead.  --impl reference times the reference algorithm on the
+host CPU (the oracle, all host threads; the reference's own Vulkan/Angrylion build
+is not available) on the same workload and metric.
 """
 import argparse
 import json
@@ -39,6 +48,11 @@ import numpy as np  # noqa: E402
 
 METRIC = "bit-exact RDP passes/s, Mpix/s on 1 GB300: batched+learned vs plain; p99 ms"
 UNIT = "passes/s"
+BATCH_INSTANCES = 64
+BATCH_WORKLOAD = ("batched instances: 64 emulator instances (8 MiB RDRAM + 4 KiB TMEM each), resolutions from "
+                  "320x240/640x240/640x480, 500-50,000 primitives per frame (log-uniform), mixed RGBA8888 primitive "
+                  "mix (textured / copy TexRect / CI8+TLUT / FillRect, alpha compare, LOD, Z on half), seeds 0-63, "
+                  "one frame per instance per step")
 WORKLOAD = ("textured depth-tested frame: 320x240 RGBA5551 + Z16, 2-cycle, 10,000 perspective-correct triangles "
             "(log-normal area, median 48 px), RGBA16 32x32 LoadTile textures, bilinear, random combiner, fog blender, "
             "Z compare+update, coverage AA, magic-square dither, seed 0")
@@ -178,7 +192,7 @@ def _reference_passes(words, rdram):
     return s
 
 
-def run_ours(args):
+def run_ours_textured(args):
     dist, rank, world, local = _dist()
     import torch
     torch.cuda.set_device(local)
@@ -206,10 +220,11 @@ def run_ours(args):
     for _ in range(args.steps):
         flush()
         step_ms.append(graph.replay(1))
-        raster_ms.append(graph.last_raster_ms())
+        raster_ms.append(graph.last_shade_ms())
     clock_info = clocks.stop()
     _barrier(dist)
     launches = cp.stats()["kernel_launches"] - launches0
+    graph_shade_launches = graph.shade_launches
     t_value = _max_over_ranks(dist, sum(step_ms) / 1e3)
     total_passes = _sum_over_ranks(dist, passes_per_frame * args.steps)
     total_frags = _sum_over_ranks(dist, frags_per_frame * args.steps)
@@ -245,16 +260,18 @@ def run_ours(args):
         pass
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    # Per touched 8x8 tile: colour (2 B) + hidden (1 B) + depth (2 B) + hidden (1 B) per pixel, read and written.
-    bytes_per_tile = 64 * (2 + 1 + 2 + 1) * 2
-    raster_launch_ms = statistics.mean(raster_ms) / max(1, base["passes"])
-    algo_bytes = tiles_per_frame * bytes_per_tile / max(1, base["passes"])
+    # k_shade output: 10 B per pixel of every shaded (primitive, tile) instance + the 8 B pair entry.
+    bytes_per_pair = 64 * 10 + 8
+    shade_launches = max(1, graph_shade_launches)
+    raster_launch_ms = statistics.mean(raster_ms) / shade_launches
+    algo_bytes = base["tile_instances"] * bytes_per_pair / shade_launches
     achieved = algo_bytes / (raster_launch_ms / 1e3) / 1e9 if raster_launch_ms > 0 else 0.0
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "k_raster_traffic.json")
+    tpath = os.path.join(ROOT, "profiles", "k_shade_traffic.json")
     if os.path.exists(tpath):
         try:
-            traffic = json.load(open(tpath)).get("dram_bytes_per_launch")
+            per_pair = json.load(open(tpath)).get("dram_bytes_per_tile_instance")
+            traffic = per_pair * base["tile_instances"] / shade_launches if per_pair else None
         except (OSError, ValueError):
             traffic = None
 
@@ -270,7 +287,7 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "mpix_per_s": total_frags / e2e_t / 1e6},
         "gpu_launches": int(launches),
-        "roofline": {"kernel": "k_raster", "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+        "roofline": {"kernel": "k_shade", "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_source": peak_src, "traffic": traffic,
                      "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": raster_launch_ms},
         "clocks": clock_info,
@@ -286,7 +303,7 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def run_reference(args):
+def run_reference_textured(args):
     """The reference algorithm on the host CPU (the oracle), same metric and config."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -331,6 +348,235 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+# ============================================================================ batched instances
+def _batched_streams(n):
+    from rdp_gb300 import cmdgen
+    out = []
+    for i in range(n):
+        p = cmdgen.batched_instance_params(i)
+        words, rdram, prims = cmdgen.generate_stream(p)
+        out.append((words, rdram, prims, p))
+    return out
+
+
+def _oracle_instances(streams, min_seconds=None, threads=None):
+    """Renders instances through the CPU oracle on `threads` host threads (ctypes drops the
+    GIL, so the threads run in parallel).  With min_seconds, stops starting new instances
+    once that much time has passed.  Returns (instances done, passes, fragments, seconds)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import Oracle
+    threads = threads or os.cpu_count() or 1
+    stop = threading.Event()
+    t0 = time.perf_counter()
+
+    def one(item):
+        words, rdram = item[0], item[1]
+        if stop.is_set():
+            return None
+        o = Oracle(8 << 20)
+        o.write_rdram(rdram)
+        o.enqueue(words)
+        r = (o.reference_passes(), o.fragments())
+        o.close()
+        if min_seconds is not None and time.perf_counter() - t0 >= min_seconds:
+            stop.set()
+        return r
+
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        results = list(ex.map(one, streams))
+    el = time.perf_counter() - t0
+    done = [r for r in results if r is not None]
+    return len(done), sum(r[0] for r in done), sum(r[1] for r in done), el, threads
+
+
+def _run_batch_step(b, insts, streams):
+    for cp, st in zip(insts, streams):
+        cp.enqueue_command(st[0])
+    values = [cp.signal_timeline() for cp in insts]
+    b.submit()
+    for cp, v in zip(insts, values):
+        cp.wait_for_timeline(v)
+
+
+def run_ours_batched(args):
+    dist, rank, world, local = _dist()
+    import torch
+    torch.cuda.set_device(local)
+    from rdp_gb300 import Batch, CommandProcessor
+
+    streams = _batched_streams(args.instances)
+    flush = _l2_flusher(local)
+    prims_per_step = sum(st[2] for st in streams)
+
+    # ---------------- batched processors; the first frame gives the per-step unit counts
+    b = Batch(device=local)
+    insts = [b.add_instance(st[1].copy()) for st in streams]
+    s0 = [cp.stats() for cp in insts]
+    _run_batch_step(b, insts, streams)
+    s1 = [cp.stats() for cp in insts]
+    b.idle()  # grows the pair scratch to what the sync point needed
+    passes_per_step = sum(x["reference_passes"] - y["reference_passes"] for x, y in zip(s1, s0))
+    frags_per_step = sum(x["fragments"] - y["fragments"] for x, y in zip(s1, s0))
+    pairs_per_step = sum(x["tile_instances"] - y["tile_instances"] for x, y in zip(s1, s0))
+
+    # ---------------- value: device-resident graph replay of the whole sync point
+    graph = b.capture([st[0] for st in streams])
+    for _ in range(args.warmup):
+        flush()
+        graph.replay(1)
+    clocks = ClockSampler(local)
+    _barrier(dist)
+    clocks.start()
+    step_ms, shade_ms = [], []
+    for _ in range(args.steps):
+        flush()
+        step_ms.append(graph.replay(1))
+        shade_ms.append(graph.last_shade_ms())
+    clock_info = clocks.stop()
+    _barrier(dist)
+    launches = graph.kernels * args.steps
+    shade_launches = graph.shade_launches
+    t_value = _max_over_ranks(dist, sum(step_ms) / 1e3)
+    total_passes = _sum_over_ranks(dist, passes_per_step * args.steps)
+    total_frags = _sum_over_ranks(dist, frags_per_step * args.steps)
+    value = total_passes / t_value
+    graph.close()
+
+    # ---------------- e2e: C ABI with host buffers, all instances per step
+    for _ in range(args.warmup):
+        _run_batch_step(b, insts, streams)
+    bs0 = b.stats()
+    _barrier(dist)
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        flush()
+        t0 = time.perf_counter()
+        _run_batch_step(b, insts, streams)
+        e2e_s += time.perf_counter() - t0
+    bs1 = b.stats()
+    _barrier(dist)
+    e2e_t = _max_over_ranks(dist, e2e_s)
+    e2e_value = total_passes / e2e_t
+    h2d = (bs1["staging_bytes"] - bs0["staging_bytes"]) / args.steps
+    d2h = sum(st[3].width * st[3].height * (4 + 2) for st in streams)  # colour + depth images copied back
+    rounds_per_step = (bs1["rounds"] - bs0["rounds"]) / args.steps
+    b.close()
+
+    # ---------------- plain: one processor + graph per instance, one after another
+    plain_ms = 0.0
+    for st in streams:
+        cp = CommandProcessor(st[1].copy(), device=local)
+        g = cp.capture(st[0])
+        for _ in range(1):
+            flush()
+            g.replay(1)
+        ms = 0.0
+        for _ in range(args.steps):
+            flush()
+            ms += g.replay(1)
+        plain_ms += ms
+        g.close()
+        cp.close()
+    t_plain = _max_over_ranks(dist, plain_ms / 1e3)
+    plain_value = total_passes / t_plain
+
+    # ---------------- roofline of the dominant kernel
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    bytes_per_pair = 64 * 10 + 8
+    shade_launch_ms = statistics.mean(shade_ms) / max(1, shade_launches)
+    algo_bytes = pairs_per_step * bytes_per_pair / max(1, shade_launches)
+    achieved = algo_bytes / (shade_launch_ms / 1e3) / 1e9 if shade_launch_ms > 0 else 0.0
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "k_shade_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            per_pair = json.load(open(tpath)).get("dram_bytes_per_tile_instance")
+            traffic = per_pair * pairs_per_step / max(1, shade_launches) if per_pair else None
+        except (OSError, ValueError):
+            traffic = None
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_value * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32", "data": "synthetic (seeded RDP command words)",
+        "config": {"workload": BATCH_WORKLOAD, "instances": args.instances, "primitives_per_step": prims_per_step,
+                   "reference_passes_per_step": passes_per_step, "fragments_per_step": frags_per_step,
+                   "tile_instances_per_step": pairs_per_step, "rounds_per_step": rounds_per_step,
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "flushed between timed iterations", "tile_order": "static"},
+        "mpix_per_s": total_frags / t_value / 1e6,
+        "frames_per_s": world * args.steps * args.instances / t_value,
+        "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": t_plain * 1e3 / args.steps,
+                  "mpix_per_s": total_frags / t_plain / 1e6},
+        "batched_over_plain": value / plain_value,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "mpix_per_s": total_frags / e2e_t / 1e6},
+        "gpu_launches": int(launches),
+        "roofline": {"kernel": "k_shade", "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "peak_source": peak_src, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": shade_launch_ms,
+                     "launches_per_step": shade_launches,
+                     "share_of_step": statistics.mean(shade_ms) / statistics.mean(step_ms)},
+        "clocks": clock_info,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        n, passes, frags, el, threads = _oracle_instances(streams, min_seconds=10.0)
+        line["cpu_baseline"] = {"value": passes / el, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "%d of the %d instances' frames through the CPU oracle, instances spread "
+                                          "over %d host threads" % (n, len(streams), threads),
+                                "mpix_per_s": frags / el / 1e6}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_reference_batched(args):
+    """The reference algorithm on the host CPU (the oracle on every host thread), same
+    workload, metric and unit; each step renders every instance's frame."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    streams = _batched_streams(args.instances)
+    # Each step renders half of the instances (even, then odd indices), so that a run of
+    # --steps K --warmup W stays within a few minutes of CPU time.
+    halves = [streams[0::2], streams[1::2]] if len(streams) > 1 else [streams]
+    for k in range(args.warmup):
+        _oracle_instances(halves[k % len(halves)])
+    passes = frags = 0
+    el = 0.0
+    threads = 1
+    for k in range(args.steps):
+        n, p, f, t, threads = _oracle_instances(halves[k % len(halves)])
+        passes += p
+        frags += f
+        el += t
+    value = passes / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32", "data": "synthetic (seeded RDP command words)",
+        "config": {"workload": BATCH_WORKLOAD, "instances": args.instances,
+                   "primitives_per_step": sum(st[2] for st in streams)},
+        "mpix_per_s": frags / el / 1e6,
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "half of the instances' frames per step (even / odd indices alternating) through "
+                                   "the CPU oracle (scalar restatement of the reference algorithm; the reference's "
+                                   "Vulkan build needs a graphics stack), instances spread over %d host threads"
+                                   % threads},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -338,12 +584,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="batched", choices=["batched", "textured"])
+    ap.add_argument("--instances", type=int, default=BATCH_INSTANCES)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":
-        run_reference(args)
+        (run_reference_batched if args.workload == "batched" else run_reference_textured)(args)
     else:
-        run_ours(args)
+        (run_ours_batched if args.workload == "batched" else run_ours_textured)(args)
 
 
 if __name__ == "__main__":

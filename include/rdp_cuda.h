@@ -150,6 +150,7 @@ typedef struct rdp_stats
 	uint64_t touched_tiles;   /* 8x8 tiles the rasteriser loaded and stored */
 	uint64_t kernel_launches; /* kernels this processor launched (graph replays included) */
 	uint64_t staging_bytes;   /* host->device bytes of command/state data */
+	uint64_t tile_instances;  /* (primitive, 8x8 tile) pairs shaded */
 } rdp_stats;
 int rdp_cp_get_stats(rdp_cp *cp, rdp_stats *out);
 
@@ -166,11 +167,58 @@ int rdp_cp_capture_end(rdp_cp *cp, rdp_graph **out);
  * measured with CUDA events on the processor's stream. */
 int rdp_graph_replay(rdp_graph *g, uint32_t count, float *elapsed_ms);
 uint32_t rdp_graph_kernel_count(rdp_graph *g);
-/* GPU time (ms) of the rasteriser launches in the last replay, from CUDA events
- * recorded on the processor's stream around each k_raster launch, and their number. */
-float rdp_graph_last_raster_ms(rdp_graph *g);
-uint32_t rdp_graph_raster_launches(rdp_graph *g);
+/* GPU time (ms) of the shading kernel (k_shade, the dominant kernel) in the last replay,
+ * from CUDA events recorded on the stream around each of its launches, and their number. */
+float rdp_graph_last_shade_ms(rdp_graph *g);
+uint32_t rdp_graph_shade_launches(rdp_graph *g);
 void rdp_graph_destroy(rdp_graph *g);
+
+/* ---------------------------------------------------------------------------------------------
+ * Batched instances.  No single counterpart in the reference, which runs one CommandProcessor
+ * per emulator (rdp_device.hpp:111-197); a batch runs many of them on one GPU.  Each instance is
+ * an ordinary rdp_cp (every rdp_cp_* call above works on it, with the same results as a
+ * stand-alone processor), but its render passes are deferred: rdp_batch_submit launches them for
+ * all instances together, one kernel chain per "round" holding the next pass of every instance
+ * that has one.  rdp_cp_wait_timeline / rdp_cp_idle / rdp_cp_scanout_sync on an instance submit
+ * the batch when they need work that is still deferred.  All instances share the batch's stream
+ * and launch buffers; a batch and its instances are used from one thread at a time. */
+typedef struct rdp_batch rdp_batch;
+
+enum
+{
+	RDP_BATCH_TILE_ORDER_LEARNED = 1u << 0, /* start tiles longest-predicted-first (rdp_batch_set_schedule) */
+	RDP_BATCH_RECORD_TILE_CYCLES = 1u << 1  /* measure per-tile blend cycles (training data) */
+};
+
+typedef struct rdp_batch_create_info
+{
+	int device;
+	uint32_t flags; /* RDP_BATCH_* */
+} rdp_batch_create_info;
+
+typedef struct rdp_batch_stats
+{
+	uint64_t instances;       /* live instances */
+	uint64_t rounds;          /* launches of the kernel chain */
+	uint64_t passes;          /* passes launched (sum over rounds) */
+	uint64_t kernel_launches; /* kernels launched, graph replays included */
+	uint64_t staging_bytes;   /* host->device bytes of command/state data */
+} rdp_batch_stats;
+
+int rdp_batch_create(const rdp_batch_create_info *info, rdp_batch **out);
+/* Destroys the batch; its instances must have been destroyed (rdp_cp_destroy) first. */
+int rdp_batch_destroy(rdp_batch *b);
+/* Creates an instance of the batch (same arguments and rules as rdp_cp_create). */
+int rdp_batch_add_instance(rdp_batch *b, const rdp_create_info *info, rdp_cp **out);
+/* Launches every deferred pass of every instance (rounds of at most one pass per instance). */
+int rdp_batch_submit(rdp_batch *b);
+/* rdp_batch_submit, then waits until the batch's stream is idle. */
+int rdp_batch_idle(rdp_batch *b);
+int rdp_batch_get_stats(rdp_batch *b, rdp_batch_stats *out);
+/* Sync-point capture over all instances: between begin and end, deferred passes are recorded
+ * (as rdp_cp_capture_begin/end do for one processor) and the graph replays all rounds. */
+int rdp_batch_capture_begin(rdp_batch *b);
+int rdp_batch_capture_end(rdp_batch *b, rdp_graph **out);
 
 /* ---------------------------------------------------------------------------------------------
  * Allocation-free TMEM update.  No counterpart in the reference: it exists for callers that must

@@ -38,6 +38,8 @@ def _load():
         L.oracle_fragments.restype = ctypes.c_uint64
         L.oracle_primitive_count.argtypes = [vp]
         L.oracle_primitive_count.restype = u32
+        L.oracle_reference_passes.argtypes = [vp]
+        L.oracle_reference_passes.restype = ctypes.c_uint64
         L.oracle_blender_lut.argtypes = [vp, vp]
         for n in ("oracle_z_compress", "oracle_z_decompress", "oracle_dz_compress", "oracle_clamp_9bit",
                   "oracle_clamp_z"):
@@ -137,3 +139,7 @@ class Oracle:
 
     def primitive_count(self):
         return self.L.oracle_primitive_count(self.h)
+
+    def reference_passes(self):
+        """Render passes the reference would submit for the stream so far (rdp_renderer.cpp:1564-1590)."""
+        return self.L.oracle_reference_passes(self.h)

@@ -197,6 +197,39 @@ static const int16_t persp_slope[64] = {
 // The oracle processor state.
 struct Oracle
 {
+	// Reference render-pass count (the unit of the throughput metric): the reference ends a
+	// pass on need_flush (rdp_renderer.cpp:1564-1590: 256 primitives, 64 distinct static
+	// states, 64 distinct depth-blend states, span-job budget), before the 256th TMEM
+	// upload (3484-3485) and on every hard flush (image changes, SyncFull, load hazards).
+	struct RefPasses
+	{
+		uint64_t passes = 0;
+		uint32_t prims = 0, uploads = 0, span_jobs = 0;
+		std::vector<uint64_t> static_keys, depth_keys;
+		void cut()
+		{
+			passes++;
+			prims = uploads = span_jobs = 0;
+			static_keys.clear();
+			depth_keys.clear();
+		}
+		void hard() { if (prims || uploads) cut(); }
+		void upload() { if (++uploads + 1 >= 256) cut(); }
+		void prim(uint32_t om0, uint32_t om1, uint32_t c0, uint32_t c1, int lines)
+		{
+			uint64_t skey = (uint64_t(om0) << 32) ^ (uint64_t(om1 & 0x3f0fu) << 20) ^ uint64_t(c0) ^ (uint64_t(c1) << 7);
+			uint64_t dkey = (uint64_t(om1) << 8) | ((om0 >> 20) & 3);
+			if (std::find(static_keys.begin(), static_keys.end(), skey) == static_keys.end()) static_keys.push_back(skey);
+			if (std::find(depth_keys.begin(), depth_keys.end(), dkey) == depth_keys.end()) depth_keys.push_back(dkey);
+			prims++;
+			if (lines > 0) span_jobs += uint32_t((lines + 2 + 63) / 64);
+			if (prims >= 256 || static_keys.size() >= 64 || depth_keys.size() >= 64 || span_jobs * 64 + 1024 > 32 * 1024)
+				cut();
+		}
+		uint64_t total() const { return passes + ((prims || uploads) ? 1 : 0); }
+	} ref;
+	uint32_t raw_other_modes[2] = { 0, 0 }, raw_combine[2] = { 0, 0 };
+
 	std::vector<uint8_t> rdram;
 	std::vector<uint8_t> hidden;
 	uint32_t rdram_size = 0;
@@ -2437,6 +2470,7 @@ struct Oracle
 		// Span job range (rdp_renderer.cpp:1523-1554).
 		int min_sub = std::max(int(setup.yh), scissor.ylo);
 		int max_sub = std::min(int(setup.yl) - 1, scissor.yhi - 1);
+		ref.prim(raw_other_modes[0], raw_other_modes[1], raw_combine[0], raw_combine[1], (max_sub >> 2) - (min_sub >> 2) + 1);
 		int ylo = min_sub >> 2, yhi = max_sub >> 2;
 		if (yhi < ylo) { ylo = 0; yhi = -1; }
 		p.span_ylo = ylo;
@@ -2872,7 +2906,11 @@ struct Oracle
 	// rdp_renderer.cpp:3099-3220 / 3222-3486.
 	void load_tile(uint32_t tile, uint32_t slo, uint32_t tlo, uint32_t shi, uint32_t thi, int mode)
 	{
-		if (upload_needs_flush(texture_image.addr)) end_pass();
+		if (upload_needs_flush(texture_image.addr))
+		{
+			ref.hard();
+			end_pass();
+		}
 		uint32_t tex_addr = texture_image.addr, tex_width = texture_image.width;
 		int isize = int(texture_image.size);
 		if (mode != MODE_BLOCK)
@@ -3031,6 +3069,7 @@ struct Oracle
 		up.mode = upload_mode;
 		up.inv_tmem_stride_words = 1.0f / float(up.tmem_stride_words);
 		apply_upload(up);
+		ref.upload();
 		if (++pass_uploads + 1 >= 256) end_pass();
 	}
 
@@ -3244,7 +3283,11 @@ struct Oracle
 			constants.prim_depth = int((w[1] >> 16) & 0x7fff) << 16;
 			constants.prim_dz = int(w[1] & 0xffff);
 			break;
-		case 0x2f: set_other_modes(w); break;
+		case 0x2f:
+			raw_other_modes[0] = w[0];
+			raw_other_modes[1] = w[1];
+			set_other_modes(w);
+			break;
 		case 0x30: load_tile((w[1] >> 24) & 7, (w[0] >> 12) & 0xfff, w[0] & 0xfff, (w[1] >> 12) & 0xfff, w[1] & 0xfff, MODE_TLUT); break;
 		case 0x32:
 		{
@@ -3268,16 +3311,27 @@ struct Oracle
 			constants.primitive_color = w[1];
 			break;
 		case 0x3b: constants.env_color = w[1]; break;
-		case 0x3c: set_combine(w); break;
+		case 0x3c:
+			raw_combine[0] = w[0];
+			raw_combine[1] = w[1];
+			set_combine(w);
+			break;
 		case 0x3d:
 			texture_image.fmt = int((w[0] >> 21) & 7);
 			texture_image.size = (w[0] >> 19) & 3;
 			texture_image.width = (w[0] & 0x3ff) + 1;
 			texture_image.addr = w[1] & 0xffffff;
 			break;
-		case 0x29: end_pass(); break;
+		case 0x29:
+			ref.hard();
+			end_pass();
+			break;
 		case 0x3e:
-			if ((w[1] & 0xffffff) != fb.depth_addr) end_pass();
+			if ((w[1] & 0xffffff) != fb.depth_addr)
+			{
+				ref.hard();
+				end_pass();
+			}
 			fb.depth_addr = w[1] & 0xffffff;
 			break;
 		case 0x3f:
@@ -3292,7 +3346,11 @@ struct Oracle
 			case 2: fmt = f ? FB_IA88 : FB_RGBA5551; break;
 			default: fmt = FB_RGBA8888; break;
 			}
-			if (width != fb.width || addr != fb.addr || fmt != fb.fmt) end_pass();
+			if (width != fb.width || addr != fb.addr || fmt != fb.fmt)
+			{
+				ref.hard();
+				end_pass();
+			}
 			fb.width = width;
 			fb.addr = addr;
 			fb.fmt = fmt;
@@ -3382,6 +3440,7 @@ uint32_t oracle_enqueue(void *h, const uint32_t *words, uint32_t num_words)
 
 uint64_t oracle_fragments(void *h) { return static_cast<Oracle *>(h)->fragments; }
 uint32_t oracle_primitive_count(void *h) { return static_cast<Oracle *>(h)->primitive_counter; }
+uint64_t oracle_reference_passes(void *h) { return static_cast<Oracle *>(h)->ref.total(); }
 
 void oracle_blender_lut(void *h, uint8_t *out)
 {

@@ -21,6 +21,9 @@
 
 namespace {
 
+// Every draw from the generator's RNG is its own statement: the order in which C++
+// evaluates function arguments and operands is unspecified and differs between
+// compilers and targets, and the streams must be identical on every host.
 struct Rng
 {
 	uint64_t s[4];
@@ -596,7 +599,9 @@ struct Gen
 		set_tile(7, 2, 2, 0, 0, 0, 0, 0, 0, 0, 0, 0);
 		uint32_t dxt = (2048 + 3) / 4;
 		tile_cmd(OP_LOAD_BLOCK, 7, 0, 0, 511, dxt);
-		set_tile(0, 2, 1, 4, 0, 0, rng.below(4), 5, 0, rng.below(4), 5, 0);
+		uint32_t cm_t0 = rng.below(4);
+		uint32_t cm_s0 = rng.below(4);
+		set_tile(0, 2, 1, 4, 0, 0, cm_t0, 5, 0, cm_s0, 5, 0);
 		tile_cmd(OP_SET_TILE_SIZE, 0, 0, 0, 31 << 2, 31 << 2);
 		emit2(uint32_t(OP_SYNC_TILE) << 24, 0);
 	}
@@ -677,7 +682,9 @@ struct Gen
 		uint32_t bits = 4u << siz;
 		uint32_t row_bytes = std::max(8u, (w * bits) / 8);
 		while (row_bytes * h > (siz == 3 || fmt == 1 ? 2048u : 4096u) && h > 1) h >>= 1;
-		uint32_t blob = FUZZ_BLOB + rng.below(8) * 0x1000 + (rng.below(4) << 3);
+		uint32_t blob_index = rng.below(8);
+		uint32_t blob_offset = rng.below(4) << 3;
+		uint32_t blob = FUZZ_BLOB + blob_index * 0x1000 + blob_offset;
 		uint32_t line_qw = row_bytes / 8;
 		uint32_t tmem_qw = (siz == 3 || fmt == 1) ? rng.below(2) * 8 : rng.below(4) * 16;
 		emit2(uint32_t(OP_SYNC_LOAD) << 24, 0);
@@ -712,7 +719,9 @@ struct Gen
 		{
 			set_tile(t, fmt, siz, line_qw >> (t ? 1 : 0), tmem_qw + t * 32, rng.below(16), cm_t, mk_t, sh_t, cm_s, mk_s, sh_s);
 			uint32_t sl = rng.below(3) == 0 ? rng.below(16) : 0, tl = rng.below(3) == 0 ? rng.below(16) : 0;
-			tile_cmd(OP_SET_TILE_SIZE, t, sl, tl, sl + ((w - 1) << 2) + rng.below(4), tl + ((h - 1) << 2) + rng.below(4));
+			uint32_t sh_frac = rng.below(4);
+			uint32_t th_frac = rng.below(4);
+			tile_cmd(OP_SET_TILE_SIZE, t, sl, tl, sl + ((w - 1) << 2) + sh_frac, tl + ((h - 1) << 2) + th_frac);
 		}
 		emit2(uint32_t(OP_SYNC_TILE) << 24, 0);
 	}
@@ -777,15 +786,21 @@ struct Gen
 					uint32_t x0 = rng.below(p.width / 2), y0 = rng.below(p.height / 2);
 					uint32_t x1 = p.width / 2 + rng.below(p.width / 2 + 1), y1 = p.height / 2 + rng.below(p.height / 2 + 1);
 					uint32_t il = (rng.u32() & 3) == 0 ? (2u | (rng.u32() & 1)) : 0;
-					emit2((uint32_t(OP_SET_SCISSOR) << 24) | (((x0 << 2) + rng.below(4)) << 12) | ((y0 << 2) + rng.below(4)),
-					      (il << 24) | (((x1 << 2) - rng.below(4)) << 12) | ((y1 << 2) - rng.below(4)));
+					uint32_t f[4];
+					for (auto &v : f) v = rng.below(4);
+					emit2((uint32_t(OP_SET_SCISSOR) << 24) | (((x0 << 2) + f[0]) << 12) | ((y0 << 2) + f[1]),
+					      (il << 24) | (((x1 << 2) - f[2]) << 12) | ((y1 << 2) - f[3]));
 				}
 				if (r < 12) fuzz_texture();
 				if (r < 20)
 				{
-					emit2(uint32_t(OP_SET_CONVERT) << 24 | (rng.u32() & 0x3fffff), rng.u32());
+					uint32_t cv0 = rng.u32() & 0x3fffff;
+					uint32_t cv1 = rng.u32();
+					emit2(uint32_t(OP_SET_CONVERT) << 24 | cv0, cv1);
 					emit2(uint32_t(0x2b) << 24, rng.u32() & 0x0fffffff);
-					emit2(uint32_t(0x2a) << 24 | (rng.u32() & 0xffffff), rng.u32());
+					uint32_t ky0 = rng.u32() & 0xffffff;
+					uint32_t ky1 = rng.u32();
+					emit2(uint32_t(0x2a) << 24 | ky0, ky1);
 					emit2(uint32_t(OP_SET_PRIM_DEPTH) << 24, rng.u32());
 					color_reg(OP_SET_FOG_COLOR, rng.u32());
 					color_reg(OP_SET_BLEND_COLOR, rng.u32());
@@ -799,7 +814,10 @@ struct Gen
 				if (cycle == 3) { m.z_compare = false; m.image_read = false; m.z_update = false; }
 				set_other_modes(m);
 				set_combiner(random_combiner(cycle == 1));
-				emit2((uint32_t(OP_SET_PRIM_COLOR) << 24) | (rng.below(32) << 8) | rng.below(256), rng.u32());
+				uint32_t pc_level = rng.below(32) << 8;
+				uint32_t pc_frac = rng.below(256);
+				uint32_t pc_color = rng.u32();
+				emit2((uint32_t(OP_SET_PRIM_COLOR) << 24) | pc_level | pc_frac, pc_color);
 				color_reg(OP_SET_ENV_COLOR, rng.u32());
 				if (cycle == 3) color_reg(OP_SET_FILL_COLOR, rng.u32());
 				if (kind < 6 || (kind == 8 && !fill_ok))
@@ -809,14 +827,17 @@ struct Gen
 					random_colors(v);
 					random_texcoords(v, 32.0, m.persp);
 					bool shade = rng.u32() & 1, tex = rng.u32() & 1, z = rng.u32() & 1;
-					if (emit_triangle(v, shade, tex, z, rng.below(8), rng.below(8))) emitted++;
+					uint32_t tri_tile = rng.below(8);
+					uint32_t tri_level = rng.below(8);
+					if (emit_triangle(v, shade, tex, z, tri_tile, tri_level)) emitted++;
 				}
 				else if (kind == 8)
 				{
 					uint32_t w = 1 + rng.below(48), h = 1 + rng.below(48);
 					uint32_t x0 = rng.below(p.width), y0 = rng.below(p.height);
-					fill_rect((x0 << 2) + rng.below(4), (y0 << 2) + rng.below(4), ((x0 + w) << 2) + rng.below(4),
-					          ((y0 + h) << 2) + rng.below(4));
+					uint32_t q[4];
+					for (auto &v : q) v = rng.below(4);
+					fill_rect((x0 << 2) + q[0], (y0 << 2) + q[1], ((x0 + w) << 2) + q[2], ((y0 + h) << 2) + q[3]);
 					prims++;
 					emitted++;
 				}
@@ -828,9 +849,14 @@ struct Gen
 					int dtdy = int(rng.below(0x1000)) - 0x400;
 					uint32_t wq[4];
 					uint32_t op = (rng.u32() & 1) ? OP_TEXRECT : (OP_TEXRECT + 1);
-					wq[0] = (op << 24) | ((((x0 + w) << 2) + rng.below(4)) << 12) | (((y0 + h) << 2) + rng.below(4));
-					wq[1] = (rng.below(8) << 24) | (((x0 << 2) + rng.below(4)) << 12) | ((y0 << 2) + rng.below(4));
-					wq[2] = (rng.u32() & 0xffffu) << 16 | (rng.u32() & 0xffffu);
+					uint32_t q[8];
+					for (auto &v : q) v = rng.below(4);
+					uint32_t rect_tile = rng.below(8);
+					uint32_t s16 = rng.u32() & 0xffffu;
+					uint32_t t16 = rng.u32() & 0xffffu;
+					wq[0] = (op << 24) | ((((x0 + w) << 2) + q[0]) << 12) | (((y0 + h) << 2) + q[1]);
+					wq[1] = (rect_tile << 24) | (((x0 << 2) + q[2]) << 12) | ((y0 << 2) + q[3]);
+					wq[2] = s16 << 16 | t16;
 					wq[3] = ((uint32_t(dsdx) & 0xffff) << 16) | (uint32_t(dtdy) & 0xffff);
 					emit(wq, 4);
 					prims++;
@@ -914,7 +940,8 @@ struct Gen
 					if (p.flags & RDPGEN_RANDOM_COMBINER)
 					{
 						comb(random_combiner(m.cycle == 1));
-						emit2((uint32_t(OP_SET_PRIM_COLOR) << 24) | (rng.below(256)), random_color());
+						uint32_t lod_frac = rng.below(256);
+						emit2((uint32_t(OP_SET_PRIM_COLOR) << 24) | lod_frac, random_color());
 						color_reg(OP_SET_ENV_COLOR, random_color());
 					}
 					else
@@ -954,7 +981,9 @@ struct Gen
 					if (p.flags & RDPGEN_RANDOM_COMBINER)
 					{
 						comb(random_combiner(m.cycle == 1));
-						emit2((uint32_t(OP_SET_PRIM_COLOR) << 24) | (rng.below(256)) | (rng.below(3) << 8), random_color());
+						uint32_t lod_frac = rng.below(256);
+						uint32_t min_level = rng.below(3) << 8;
+						emit2((uint32_t(OP_SET_PRIM_COLOR) << 24) | lod_frac | min_level, random_color());
 						color_reg(OP_SET_ENV_COLOR, random_color());
 					}
 					else
@@ -980,8 +1009,9 @@ struct Gen
 					modes(m);
 					uint32_t w = 8 + rng.below(48), h = 8 + rng.below(48);
 					uint32_t x0 = rng.below(p.width > w ? p.width - w : 1), y0 = rng.below(p.height > h ? p.height - h : 1);
-					texrect(0, x0 << 2, y0 << 2, (x0 + w) << 2, (y0 + h) << 2, int(rng.below(32)) << 5,
-					        int(rng.below(32)) << 5, 4 << 10, 1 << 10);
+					int s0 = int(rng.below(32)) << 5;
+					int t0 = int(rng.below(32)) << 5;
+					texrect(0, x0 << 2, y0 << 2, (x0 + w) << 2, (y0 + h) << 2, s0, t0, 4 << 10, 1 << 10);
 					emitted++;
 					break;
 				}

@@ -32,6 +32,7 @@
 #include "../../include/rdp_cuda.h"
 #include "rdp_types.h"
 #include "rdp_kernels.h"
+#include "rdp_exec.h"
 #include "vi.h"
 #include "blender_divider_runs.inc"
 
@@ -42,7 +43,6 @@ constexpr uint32_t kMaxStateBlocks = RDP_MAX_PRIMS_PER_PASS;
 constexpr uint32_t kMaxTilesets = 4096;
 constexpr uint32_t kMaxTiles = RDP_MAX_TILES_X * RDP_MAX_TILES_Y;
 
-static inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
 
 static uint32_t command_length(uint32_t op)
 {
@@ -94,6 +94,8 @@ static cudaError_t ensure_luts(int device)
 
 } // namespace
 
+struct rdp_batch;
+
 struct rdp_cp
 {
 	// ---------------------------------------------------------------- configuration
@@ -106,30 +108,15 @@ struct rdp_cp
 	std::vector<uint8_t> hidden_mirror;
 
 	// ---------------------------------------------------------------- device memory
+	// The instance's own state; launch buffers belong to the executor.
 	uint8_t *d_rdram = nullptr, *d_hidden = nullptr;
 	uint16_t *d_tmem = nullptr, *d_snapshots = nullptr;
-	uint32_t *d_masks = nullptr;
-	uint32_t *d_tmem_keep = nullptr;
-	uint32_t *d_tile_counts = nullptr, *d_pair_offsets = nullptr, *d_ctrl = nullptr;
-	uint2 *d_pairs = nullptr;
-	uint32_t *d_sc_color = nullptr;
-	int *d_sc_zdith = nullptr;
-	uint16_t *d_sc_misc = nullptr;
-	uint32_t pair_capacity = 0, shade_ctas = 0;
-	RdpPrimGeom *d_geom = nullptr;
-	RdpPrimAttr *d_attr = nullptr;
-	RdpPrimShade *d_shade = nullptr;
-	uint8_t *d_staging = nullptr;
-	unsigned long long *d_fragments = nullptr;
-	size_t staging_cap = 0;
-
-	struct Staging
-	{
-		uint8_t *h = nullptr;
-		cudaEvent_t done = nullptr;
-		bool in_flight = false;
-	} staging[2];
-	int staging_index = 0;
+	unsigned long long *d_fragments = nullptr; // [0] fragments, [1] touched tiles, [2] tile instances
+	rdpx::Executor own_exec;
+	rdpx::Executor *exec = &own_exec;
+	rdp_batch *batch = nullptr;
+	std::deque<rdpx::PassPacket> deferred;   // batched: passes waiting for the batch's next launch
+	std::vector<uint64_t> unsubmitted;       // batched: timeline values signalled before that launch
 
 	// ---------------------------------------------------------------- pass being recorded
 	std::vector<RdpPrimIn> prims;
@@ -178,8 +165,7 @@ struct rdp_cp
 
 	// Sync-point capture: recorded launches with device-resident inputs.
 	bool capturing = false;
-	std::vector<RdpLaunch> captured;
-	std::vector<void *> captured_buffers;
+	rdpx::CaptureSink capture_sink;
 
 	uint32_t vi_regs[16] = {};
 	struct ViHost
@@ -250,14 +236,22 @@ struct rdp_cp
 	}
 
 	// ================================================================= creation
-	int init(const rdp_create_info *info)
+	// `shared` is the batch's executor (whose stream the instance then uses), or null.
+	int init(const rdp_create_info *info, rdp_batch *owner = nullptr, rdpx::Executor *shared = nullptr)
 	{
 		device = info->device;
 		rdram_size = uint32_t(info->rdram_size);
 		hidden_size = uint32_t(info->hidden_rdram_size);
 		if (cudaSetDevice(device) != cudaSuccess) return RDP_ERR_UNSUPPORTED;
 		if (ensure_luts(device) != cudaSuccess) return RDP_ERR_DEVICE;
-		if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return RDP_ERR_DEVICE;
+		if (owner)
+		{
+			batch = owner;
+			exec = shared;
+			stream = shared->stream;
+		}
+		else if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess)
+			return RDP_ERR_DEVICE;
 
 		if (info->rdram)
 			host_rdram = static_cast<uint8_t *>(info->rdram) + info->rdram_offset;
@@ -271,46 +265,29 @@ struct rdp_cp
 		if (!host_registered) cudaGetLastError();
 		hidden_mirror.assign(hidden_size, 0x03);
 
-		staging_cap = align16(sizeof(RdpPass)) + align16(sizeof(RdpPrimIn) * RDP_MAX_PRIMS_PER_PASS) +
-		              align16(sizeof(uint32_t) * kMaxWordsPerPass) +
-		              align16(sizeof(uint32_t) * RDP_STATE_BLOCK_WORDS * kMaxStateBlocks) +
-		              align16(sizeof(RdpTile) * 8 * kMaxTilesets) +
-		              align16(sizeof(RdpUpload) * RDP_MAX_UPLOADS_PER_PASS) + 64;
-
 		if (cudaMalloc(&d_rdram, rdram_size) != cudaSuccess) return RDP_ERR_OOM;
 		if (cudaMalloc(&d_hidden, hidden_size) != cudaSuccess) return RDP_ERR_OOM;
 		if (cudaMalloc(&d_tmem, 4096) != cudaSuccess) return RDP_ERR_OOM;
 		if (cudaMalloc(&d_snapshots, size_t(RDP_MAX_UPLOADS_PER_PASS + 1) * 4096) != cudaSuccess) return RDP_ERR_OOM;
-		if (cudaMalloc(&d_masks, size_t(kMaxTiles) * RDP_MASK_WORDS_PER_TILE * 4) != cudaSuccess) return RDP_ERR_OOM;
-		if (cudaMalloc(&d_tmem_keep, size_t(RDP_MAX_UPLOADS_PER_PASS) * 64 * 4) != cudaSuccess) return RDP_ERR_OOM;
-		pair_capacity = 1u << 20;
-		if (cudaMalloc(&d_tile_counts, size_t(kMaxTiles + 1) * 4) != cudaSuccess) return RDP_ERR_OOM;
-		if (cudaMalloc(&d_pair_offsets, size_t(kMaxTiles + 1) * 4) != cudaSuccess) return RDP_ERR_OOM;
-		if (cudaMalloc(&d_ctrl, 16) != cudaSuccess) return RDP_ERR_OOM;
-		if (cudaMalloc(&d_pairs, size_t(pair_capacity) * sizeof(uint2)) != cudaSuccess) return RDP_ERR_OOM;
-		if (cudaMalloc(&d_sc_color, size_t(pair_capacity) * 64 * 4) != cudaSuccess) return RDP_ERR_OOM;
-		if (cudaMalloc(&d_sc_zdith, size_t(pair_capacity) * 64 * 4) != cudaSuccess) return RDP_ERR_OOM;
-		if (cudaMalloc(&d_sc_misc, size_t(pair_capacity) * 64 * 2) != cudaSuccess) return RDP_ERR_OOM;
+		if (cudaMalloc(&d_fragments, 4 * sizeof(unsigned long long)) != cudaSuccess) return RDP_ERR_OOM;
+		if (!batch)
 		{
-			int sms = 0;
-			cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-			shade_ctas = uint32_t(std::max(sms, 1)) * uint32_t(rdp_kernels_shade_ctas_per_sm());
+			// A stand-alone processor sizes its executor for one full pass up front.
+			rdpx::ExecCaps c;
+			c.passes = 1;
+			c.prims = RDP_MAX_PRIMS_PER_PASS;
+			c.tile_items = kMaxTiles;
+			c.pairs = 1u << 20;
+			c.staging = rdpx::align16(sizeof(RdpPass)) + rdpx::align16(sizeof(RdpPrimIn) * RDP_MAX_PRIMS_PER_PASS) +
+			            rdpx::align16(sizeof(uint32_t) * kMaxWordsPerPass) +
+			            rdpx::align16(sizeof(uint32_t) * RDP_STATE_BLOCK_WORDS * kMaxStateBlocks) +
+			            rdpx::align16(sizeof(RdpTile) * 8 * kMaxTilesets) +
+			            rdpx::align16(sizeof(RdpUpload) * RDP_MAX_UPLOADS_PER_PASS) + 512;
+			if (!own_exec.init(device, stream) || !own_exec.ensure(c)) return RDP_ERR_OOM;
 		}
-		if (cudaMalloc(&d_geom, sizeof(RdpPrimGeom) * RDP_MAX_PRIMS_PER_PASS) != cudaSuccess) return RDP_ERR_OOM;
-		if (cudaMalloc(&d_attr, sizeof(RdpPrimAttr) * RDP_MAX_PRIMS_PER_PASS) != cudaSuccess) return RDP_ERR_OOM;
-		if (cudaMalloc(&d_shade, sizeof(RdpPrimShade) * RDP_MAX_PRIMS_PER_PASS) != cudaSuccess) return RDP_ERR_OOM;
-		if (cudaMalloc(&d_staging, staging_cap) != cudaSuccess) return RDP_ERR_OOM;
-		if (cudaMalloc(&d_fragments, 2 * sizeof(unsigned long long)) != cudaSuccess) return RDP_ERR_OOM;
-		for (auto &s : staging)
-		{
-			if (cudaMallocHost(&s.h, staging_cap) != cudaSuccess) return RDP_ERR_OOM;
-			if (cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess) return RDP_ERR_DEVICE;
-		}
-		if (check(cudaMemsetAsync(d_masks, 0, size_t(kMaxTiles) * RDP_MASK_WORDS_PER_TILE * 4, stream))) return RDP_ERR_DEVICE;
-		if (check(cudaMemsetAsync(d_tile_counts, 0, size_t(kMaxTiles + 1) * 4, stream))) return RDP_ERR_DEVICE;
 		if (check(cudaMemsetAsync(d_hidden, 0x03, hidden_size, stream))) return RDP_ERR_DEVICE;
 		if (check(cudaMemsetAsync(d_tmem, 0, 4096, stream))) return RDP_ERR_DEVICE;
-		if (check(cudaMemsetAsync(d_fragments, 0, 2 * sizeof(unsigned long long), stream))) return RDP_ERR_DEVICE;
+		if (check(cudaMemsetAsync(d_fragments, 0, 4 * sizeof(unsigned long long), stream))) return RDP_ERR_DEVICE;
 		if (check(cudaMemcpyAsync(d_rdram, host_rdram, rdram_size, cudaMemcpyHostToDevice, stream))) return RDP_ERR_DEVICE;
 		if (check(cudaStreamSynchronize(stream))) return RDP_ERR_DEVICE;
 
@@ -331,28 +308,12 @@ struct rdp_cp
 		}
 		for (auto &p : pending) cudaEventDestroy(p.second);
 		for (auto e : free_events) cudaEventDestroy(e);
-		for (auto &s : staging)
-		{
-			if (s.h) cudaFreeHost(s.h);
-			if (s.done) cudaEventDestroy(s.done);
-		}
+		if (!batch) own_exec.destroy();
+		deferred.clear();
 		cudaFree(d_rdram);
 		cudaFree(d_hidden);
 		cudaFree(d_tmem);
 		cudaFree(d_snapshots);
-		cudaFree(d_masks);
-		cudaFree(d_tmem_keep);
-		cudaFree(d_tile_counts);
-		cudaFree(d_pair_offsets);
-		cudaFree(d_ctrl);
-		cudaFree(d_pairs);
-		cudaFree(d_sc_color);
-		cudaFree(d_sc_zdith);
-		cudaFree(d_sc_misc);
-		cudaFree(d_geom);
-		cudaFree(d_attr);
-		cudaFree(d_shade);
-		cudaFree(d_staging);
 		cudaFree(d_fragments);
 		cudaFree(vi.d_aa);
 		cudaFree(vi.d_dv);
@@ -361,7 +322,7 @@ struct rdp_cp
 		cudaFree(vi.d_lines);
 		if (host_registered) cudaHostUnregister(host_rdram);
 		if (own_host_rdram) free(host_rdram);
-		if (stream) cudaStreamDestroy(stream);
+		if (stream && !batch) cudaStreamDestroy(stream);
 	}
 
 	// ================================================================= pass submission
@@ -408,20 +369,11 @@ struct rdp_cp
 			return sticky_error;
 		}
 
-		Staging &st = staging[staging_index];
-		staging_index ^= 1;
-		if (st.in_flight)
-		{
-			if (check(cudaEventSynchronize(st.done))) return sticky_error;
-			st.in_flight = false;
-		}
-
 		bool render = fb.width != 0 && fb.deduced_height != 0 && !prims.empty();
-		RdpPass pass = {};
+		rdpx::PassView v = {};
+		RdpPass &pass = v.pass;
 		pass.rdram = d_rdram;
 		pass.hidden = d_hidden;
-		pass.masks = d_masks;
-		pass.coarse = nullptr;
 		pass.tmem_snapshots = uploads.empty() ? d_tmem : d_snapshots;
 		pass.tmem_state = d_tmem;
 		pass.rdram_size = rdram_size;
@@ -433,86 +385,36 @@ struct rdp_cp
 		pass.fb_fmt = fb.fmt;
 		pass.tiles_x = render ? (fb.width + 7) / 8 : 0;
 		pass.tiles_y = render ? (pass.fb_height + 7) / 8 : 0;
-		pass.prim_begin = 0;
-		pass.prim_count = uint32_t(prims.size());
-		pass.upload_begin = 0;
-		pass.upload_count = uint32_t(uploads.size());
-		pass.tile_item_begin = 0;
-		pass.instance = 0;
 		pass.base_prim_index = uint32_t(base_prim_index);
+		pass.counters = d_fragments;
+		// A pass that does not render keeps its TMEM uploads but no primitives.
+		v.prims = prims.data();
+		v.num_prims = render ? uint32_t(prims.size()) : 0;
+		v.words = words.data();
+		v.num_words = uint32_t(words.size());
+		v.state_blocks = state_blocks.data();
+		v.num_state_blocks = uint32_t(state_blocks.size() / RDP_STATE_BLOCK_WORDS);
+		v.tilesets = tilesets.data();
+		v.num_tilesets = uint32_t(tilesets.size() / 8);
+		v.uploads = uploads.data();
+		v.num_uploads = uint32_t(uploads.size());
 
-		// Pack the staging buffer: pass | prims | words | state blocks | tilesets | uploads | tmem pass list.
-		uint8_t *h = st.h;
-		size_t off = 0;
-		auto put = [&](const void *src, size_t bytes) -> size_t {
-			size_t at = off;
-			if (bytes) memcpy(h + off, src, bytes);
-			off = align16(off + bytes);
-			return at;
-		};
-		size_t o_pass = put(&pass, sizeof(pass));
-		size_t o_prims = put(prims.data(), prims.size() * sizeof(RdpPrimIn));
-		size_t o_words = put(words.data(), words.size() * 4);
-		size_t o_sb = put(state_blocks.data(), state_blocks.size() * 4);
-		size_t o_ts = put(tilesets.data(), tilesets.size() * sizeof(RdpTile));
-		size_t o_up = put(uploads.data(), uploads.size() * sizeof(RdpUpload));
-		uint32_t zero = 0;
-		size_t o_list = put(&zero, 4);
-		uint8_t *dst = d_staging;
-		if (capturing)
+		if (batch)
 		{
-			// The pass's data stays resident for graph replay.
-			if (check(cudaStreamSynchronize(stream))) return sticky_error;
-			if (check(cudaMalloc(&dst, off))) return sticky_error;
-			captured_buffers.push_back(dst);
-			if (check(cudaMemcpy(dst, h, off, cudaMemcpyHostToDevice))) return sticky_error;
+			rdpx::PassPacket pk;
+			pk.pass = pass;
+			pk.prims.assign(prims.begin(), prims.begin() + v.num_prims);
+			pk.words = words;
+			pk.state_blocks = state_blocks;
+			pk.tilesets = tilesets;
+			pk.uploads = uploads;
+			deferred.push_back(std::move(pk));
 		}
 		else
 		{
-			if (check(cudaMemcpyAsync(d_staging, h, off, cudaMemcpyHostToDevice, stream))) return sticky_error;
-			if (check(cudaEventRecord(st.done, stream))) return sticky_error;
-			st.in_flight = true;
-		}
-		stats.staging_bytes += off;
-
-		RdpLaunch L = {};
-		uint8_t *d_staging = dst;
-		L.prims_in = reinterpret_cast<const RdpPrimIn *>(d_staging + o_prims);
-		L.num_prims = render ? uint32_t(prims.size()) : 0;
-		L.words = reinterpret_cast<const uint32_t *>(d_staging + o_words);
-		L.state_blocks = reinterpret_cast<const uint32_t *>(d_staging + o_sb);
-		L.passes = reinterpret_cast<const RdpPass *>(d_staging + o_pass);
-		L.num_passes = 1;
-		L.geom = d_geom;
-		L.attr = d_attr;
-		L.shade = d_shade;
-		L.tilesets = reinterpret_cast<const RdpTile *>(d_staging + o_ts);
-		L.tmem_pass_list = reinterpret_cast<const uint32_t *>(d_staging + o_list);
-		L.num_tmem_passes = uploads.empty() ? 0 : 1;
-		L.uploads = reinterpret_cast<const RdpUpload *>(d_staging + o_up);
-		L.max_uploads = uint32_t(uploads.size());
-		L.tmem_keep = d_tmem_keep;
-		L.tile_counts = d_tile_counts;
-		L.pair_offsets = d_pair_offsets;
-		L.pairs = d_pairs;
-		L.ctrl = d_ctrl;
-		L.pair_capacity = pair_capacity;
-		L.shade_ctas = shade_ctas;
-		L.sc_color = d_sc_color;
-		L.sc_zdith = d_sc_zdith;
-		L.sc_misc = d_sc_misc;
-		L.num_tile_items = pass.tiles_x * pass.tiles_y;
-		L.fragments = d_fragments;
-		if (capturing)
-		{
-			for (auto &e : L.raster_events)
-				if (check(cudaEventCreate(&e))) return sticky_error;
-			captured.push_back(L);
-		}
-		else
-		{
-			if (check(rdp_kernels_launch(&L, stream))) return sticky_error;
-			stats.kernel_launches += rdp_kernels_count(&L);
+			uint64_t before = exec->kernel_launches;
+			if (!exec->launch(&v, 1, capturing ? &capture_sink : nullptr)) return check(cudaErrorUnknown);
+			stats.kernel_launches += exec->kernel_launches - before;
 		}
 
 		if (render)
@@ -1034,7 +936,7 @@ struct rdp_cp
 	int scanout(const rdp_scanout_options *o, uint32_t *out, uint32_t *width, uint32_t *height)
 	{
 		*width = *height = 0;
-		int r0 = hard_flush();
+		int r0 = sync_point();
 		if (r0 != RDP_OK) return r0;
 		if (!vi.tables)
 		{
@@ -1267,9 +1169,43 @@ struct rdp_cp
 		return sticky_error;
 	}
 
+	int batch_submit(); // defined after rdp_batch
+
+	// A batched instance's deferred passes have been launched (rdp_batch::submit): its
+	// signalled timeline values complete after them and after the copy-back.
+	int complete_submitted()
+	{
+		if (unsubmitted.empty()) return sticky_error;
+		if (copy_back() != RDP_OK) return sticky_error;
+		for (uint64_t v : unsubmitted)
+		{
+			cudaEvent_t e = get_event();
+			if (!e) return RDP_ERR_DEVICE;
+			if (check(cudaEventRecord(e, stream))) return sticky_error;
+			pending.emplace_back(v, e);
+		}
+		unsubmitted.clear();
+		return sticky_error;
+	}
+
+	// Work that must be on the stream before the caller reads device state.
+	int sync_point()
+	{
+		int r = hard_flush();
+		if (r != RDP_OK || !batch) return r;
+		return batch_submit();
+	}
+
 	int signal_timeline(uint64_t *value)
 	{
 		if (hard_flush() != RDP_OK) return sticky_error;
+		if (batch)
+		{
+			uint64_t v = ++timeline_counter;
+			unsubmitted.push_back(v);
+			if (value) *value = v;
+			return sticky_error;
+		}
 		if (copy_back() != RDP_OK) return sticky_error;
 		cudaEvent_t e = get_event();
 		if (!e) return RDP_ERR_DEVICE;
@@ -1283,6 +1219,11 @@ struct rdp_cp
 	int wait_timeline(uint64_t value, uint64_t timeout_ns)
 	{
 		// Timeouts beyond ~11 days mean "no deadline" (and must not overflow the clock).
+		if (batch && !unsubmitted.empty() && unsubmitted.front() <= value)
+		{
+			int r = batch_submit();
+			if (r != RDP_OK) return r;
+		}
 		const bool bounded = timeout_ns < (uint64_t(1) << 50);
 		auto deadline = std::chrono::steady_clock::now() + std::chrono::nanoseconds(bounded ? int64_t(timeout_ns) : 0);
 		while (!pending.empty() && pending.front().first <= value)
@@ -1312,6 +1253,87 @@ struct rdp_cp
 		return wait_timeline(v, UINT64_MAX / 2);
 	}
 };
+
+// ============================================================================ batch
+// Many instances, one executor: each round launches the next deferred pass of every
+// instance that has one, so one kernel chain renders all instances' passes together.
+struct rdp_batch
+{
+	int device = 0;
+	uint32_t flags = 0;
+	cudaStream_t stream = nullptr;
+	rdpx::Executor exec;
+	std::vector<rdp_cp *> instances;
+	bool capturing = false;
+	rdpx::CaptureSink sink;
+	uint64_t rounds = 0, passes = 0;
+	int sticky_error = RDP_OK;
+
+	bool reserve_for_capture();
+
+	int submit()
+	{
+		if (sticky_error != RDP_OK) return sticky_error;
+		std::vector<rdpx::PassView> views;
+		std::vector<rdp_cp *> owners;
+		views.reserve(instances.size());
+		owners.reserve(instances.size());
+		if (capturing && !reserve_for_capture()) return sticky_error = RDP_ERR_DEVICE;
+		for (;;)
+		{
+			views.clear();
+			owners.clear();
+			for (rdp_cp *cp : instances)
+				if (!cp->deferred.empty())
+				{
+					views.push_back(cp->deferred.front().view());
+					owners.push_back(cp);
+				}
+			if (views.empty()) break;
+			if (!exec.launch(views.data(), uint32_t(views.size()), capturing ? &sink : nullptr))
+				return sticky_error = RDP_ERR_DEVICE;
+			rounds++;
+			passes += views.size();
+			for (rdp_cp *cp : owners) cp->deferred.pop_front();
+		}
+		for (rdp_cp *cp : instances)
+		{
+			int r = cp->complete_submitted();
+			if (r != RDP_OK) return sticky_error = r;
+		}
+		return RDP_OK;
+	}
+};
+
+int rdp_cp::batch_submit() { return batch->submit(); }
+
+// Recorded launches keep pointers to the executor's buffers, so the buffers are sized for
+// every round of a capture before the first one is recorded.
+bool rdp_batch::reserve_for_capture()
+{
+	rdpx::ExecCaps need = exec.caps;
+	size_t depth = 0;
+	for (rdp_cp *cp : instances) depth = std::max(depth, cp->deferred.size());
+	std::vector<rdpx::PassView> views;
+	for (size_t r = 0; r < depth; r++)
+	{
+		views.clear();
+		uint32_t prims = 0, tiles = 0;
+		for (rdp_cp *cp : instances)
+			if (r < cp->deferred.size())
+			{
+				views.push_back(cp->deferred[r].view());
+				prims += views.back().num_prims;
+				tiles += views.back().pass.tiles_x * views.back().pass.tiles_y;
+			}
+		need.passes = std::max(need.passes, uint32_t(views.size()));
+		need.prims = std::max(need.prims, prims);
+		need.tile_items = std::max(need.tile_items, tiles);
+		need.staging = std::max(need.staging, rdpx::Executor::staging_bytes_for(views.data(), uint32_t(views.size())));
+	}
+	need.pairs = std::max(need.pairs, 1u << 20);
+	return exec.ensure(need);
+}
 
 // ============================================================================ C ABI
 extern "C" {
@@ -1347,6 +1369,14 @@ int rdp_cp_create(const rdp_create_info *info, rdp_cp **out)
 void rdp_cp_destroy(rdp_cp *cp)
 {
 	if (!cp) return;
+	cudaSetDevice(cp->device);
+	if (cp->batch)
+	{
+		// Finish the instance's deferred work (the batch's other instances keep theirs).
+		cp->idle();
+		auto &v = cp->batch->instances;
+		v.erase(std::remove(v.begin(), v.end(), cp), v.end());
+	}
 	cp->destroy();
 	delete cp;
 }
@@ -1511,37 +1541,81 @@ int rdp_cp_get_stats(rdp_cp *cp, rdp_stats *out)
 	if (!cp || !out) return RDP_ERR_INVALID;
 	cudaSetDevice(cp->device);
 	*out = cp->stats;
-	unsigned long long frags = 0;
-	if (cudaMemcpy(&frags, cp->d_fragments, sizeof(frags), cudaMemcpyDeviceToHost) != cudaSuccess) return RDP_ERR_DEVICE;
-	out->fragments = frags;
-	unsigned long long counters[2] = { 0, 0 };
+	unsigned long long counters[3] = { 0, 0, 0 };
 	if (cudaMemcpy(counters, cp->d_fragments, sizeof(counters), cudaMemcpyDeviceToHost) != cudaSuccess) return RDP_ERR_DEVICE;
+	out->fragments = counters[0];
 	out->touched_tiles = counters[1];
+	out->tile_instances = counters[2];
 	out->reference_passes = cp->stats.reference_passes + ((cp->ref.prims || cp->ref.uploads) ? 1 : 0);
+	if (!cp->batch) out->staging_bytes = cp->exec->staging_bytes;
 	return RDP_OK;
 }
 
+// A CUDA graph of recorded launches.  It replays on the executor's stream with the
+// executor's scratch buffers, so it is valid while the executor keeps its generation.
 struct rdp_graph
 {
-	rdp_cp *cp = nullptr;
+	rdpx::Executor *exec = nullptr;
+	uint64_t generation = 0;
+	rdp_stats *stats = nullptr; // receives kernel_launches, when the graph belongs to one processor
 	cudaGraph_t graph = nullptr;
-	cudaGraphExec_t exec = nullptr;
+	cudaGraphExec_t gexec = nullptr;
 	std::vector<void *> buffers;
-	std::vector<std::pair<cudaEvent_t, cudaEvent_t>> raster_events;
-	uint32_t kernels = 0, raster_launches = 0;
-	float last_raster_ms = 0.0f;
+	std::vector<std::pair<cudaEvent_t, cudaEvent_t>> shade_events;
+	uint32_t kernels = 0, shade_launches = 0;
+	float last_shade_ms = 0.0f;
 	cudaEvent_t ev[2] = { nullptr, nullptr };
 };
 
+static int build_graph(rdpx::Executor *exec, rdpx::CaptureSink &sink, rdp_stats *stats, rdp_graph **out)
+{
+	rdp_graph *g = new (std::nothrow) rdp_graph();
+	if (!g) return RDP_ERR_OOM;
+	g->exec = exec;
+	g->generation = exec->generation;
+	g->stats = stats;
+	g->buffers.swap(sink.buffers);
+	bool ok = cudaStreamBeginCapture(exec->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+	if (ok)
+	{
+		for (auto &L : sink.launches)
+		{
+			rdp_kernels_launch(&L, exec->stream);
+			g->kernels += rdp_kernels_count(&L);
+			if (L.num_prims && L.num_tile_items)
+			{
+				g->shade_events.emplace_back(L.shade_events[0], L.shade_events[1]);
+				g->shade_launches++;
+			}
+			else
+			{
+				cudaEventDestroy(L.shade_events[0]);
+				cudaEventDestroy(L.shade_events[1]);
+			}
+		}
+		ok = cudaStreamEndCapture(exec->stream, &g->graph) == cudaSuccess;
+	}
+	sink.launches.clear();
+	ok = ok && cudaGraphInstantiate(&g->gexec, g->graph, 0) == cudaSuccess;
+	ok = ok && cudaEventCreate(&g->ev[0]) == cudaSuccess && cudaEventCreate(&g->ev[1]) == cudaSuccess;
+	if (!ok)
+	{
+		cudaGetLastError();
+		rdp_graph_destroy(g);
+		return RDP_ERR_DEVICE;
+	}
+	*out = g;
+	return RDP_OK;
+}
+
 int rdp_cp_capture_begin(rdp_cp *cp)
 {
-	if (!cp || cp->capturing) return RDP_ERR_INVALID;
+	if (!cp || cp->capturing || cp->batch) return RDP_ERR_INVALID;
 	cudaSetDevice(cp->device);
 	int r = cp->hard_flush();
 	if (r != RDP_OK) return r;
 	cp->capturing = true;
-	cp->captured.clear();
-	cp->captured_buffers.clear();
+	cp->capture_sink = rdpx::CaptureSink{};
 	return RDP_OK;
 }
 
@@ -1552,78 +1626,50 @@ int rdp_cp_capture_end(rdp_cp *cp, rdp_graph **out)
 	int r = cp->hard_flush();
 	cp->capturing = false;
 	if (r != RDP_OK) return r;
-	rdp_graph *g = new rdp_graph();
-	g->cp = cp;
-	g->buffers.swap(cp->captured_buffers);
-	if (cp->check(cudaStreamBeginCapture(cp->stream, cudaStreamCaptureModeThreadLocal)) == RDP_OK)
-	{
-		for (auto &L : cp->captured)
-		{
-			rdp_kernels_launch(&L, cp->stream);
-			g->kernels += rdp_kernels_count(&L);
-			if (L.num_prims && L.num_tile_items)
-			{
-				g->raster_events.emplace_back(L.raster_events[0], L.raster_events[1]);
-				g->raster_launches++;
-			}
-			else
-			{
-				cudaEventDestroy(L.raster_events[0]);
-				cudaEventDestroy(L.raster_events[1]);
-			}
-		}
-		cp->check(cudaStreamEndCapture(cp->stream, &g->graph));
-	}
-	cp->captured.clear();
-	if (cp->sticky_error == RDP_OK) cp->check(cudaGraphInstantiate(&g->exec, g->graph, 0));
-	if (cp->sticky_error == RDP_OK) cp->check(cudaEventCreate(&g->ev[0]));
-	if (cp->sticky_error == RDP_OK) cp->check(cudaEventCreate(&g->ev[1]));
-	if (cp->sticky_error != RDP_OK)
-	{
-		rdp_graph_destroy(g);
-		return cp->sticky_error;
-	}
-	*out = g;
-	return RDP_OK;
+	r = build_graph(cp->exec, cp->capture_sink, &cp->stats, out);
+	if (r != RDP_OK) cp->sticky_error = r;
+	return r;
 }
 
 int rdp_graph_replay(rdp_graph *g, uint32_t count, float *elapsed_ms)
 {
 	if (!g) return RDP_ERR_INVALID;
-	rdp_cp *cp = g->cp;
-	cudaSetDevice(cp->device);
-	if (cp->check(cudaEventRecord(g->ev[0], cp->stream))) return cp->sticky_error;
+	rdpx::Executor *ex = g->exec;
+	if (ex->generation != g->generation) return RDP_ERR_INVALID; // scratch was reallocated since capture
+	cudaSetDevice(ex->device);
+	if (cudaEventRecord(g->ev[0], ex->stream) != cudaSuccess) return RDP_ERR_DEVICE;
 	for (uint32_t i = 0; i < count; i++)
-		if (cp->check(cudaGraphLaunch(g->exec, cp->stream))) return cp->sticky_error;
-	if (cp->check(cudaEventRecord(g->ev[1], cp->stream))) return cp->sticky_error;
-	if (cp->check(cudaEventSynchronize(g->ev[1]))) return cp->sticky_error;
-	cp->stats.kernel_launches += uint64_t(g->kernels) * count;
-	if (elapsed_ms) cp->check(cudaEventElapsedTime(elapsed_ms, g->ev[0], g->ev[1]));
+		if (cudaGraphLaunch(g->gexec, ex->stream) != cudaSuccess) return RDP_ERR_DEVICE;
+	if (cudaEventRecord(g->ev[1], ex->stream) != cudaSuccess) return RDP_ERR_DEVICE;
+	if (cudaEventSynchronize(g->ev[1]) != cudaSuccess) return RDP_ERR_DEVICE;
+	ex->kernel_launches += uint64_t(g->kernels) * count;
+	if (g->stats) g->stats->kernel_launches += uint64_t(g->kernels) * count;
+	if (elapsed_ms && cudaEventElapsedTime(elapsed_ms, g->ev[0], g->ev[1]) != cudaSuccess) return RDP_ERR_DEVICE;
 	// GPU time of the rasteriser launches of the last replay.
-	g->last_raster_ms = 0.0f;
-	for (auto &pr : g->raster_events)
+	g->last_shade_ms = 0.0f;
+	for (auto &pr : g->shade_events)
 	{
 		float ms = 0.0f;
-		if (cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) g->last_raster_ms += ms;
+		if (cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) g->last_shade_ms += ms;
 		else cudaGetLastError(); // keep the thread's last-error slot clean for other CUDA users
 	}
-	return cp->sticky_error;
+	return RDP_OK;
 }
 
-float rdp_graph_last_raster_ms(rdp_graph *g) { return g ? g->last_raster_ms : 0.0f; }
-uint32_t rdp_graph_raster_launches(rdp_graph *g) { return g ? g->raster_launches : 0; }
+float rdp_graph_last_shade_ms(rdp_graph *g) { return g ? g->last_shade_ms : 0.0f; }
+uint32_t rdp_graph_shade_launches(rdp_graph *g) { return g ? g->shade_launches : 0; }
 
 uint32_t rdp_graph_kernel_count(rdp_graph *g) { return g ? g->kernels : 0; }
 
 void rdp_graph_destroy(rdp_graph *g)
 {
 	if (!g) return;
-	cudaSetDevice(g->cp->device);
-	cudaStreamSynchronize(g->cp->stream);
-	if (g->exec) cudaGraphExecDestroy(g->exec);
+	cudaSetDevice(g->exec->device);
+	cudaStreamSynchronize(g->exec->stream);
+	if (g->gexec) cudaGraphExecDestroy(g->gexec);
 	if (g->graph) cudaGraphDestroy(g->graph);
 	for (void *b : g->buffers) cudaFree(b);
-	for (auto &pr : g->raster_events)
+	for (auto &pr : g->shade_events)
 	{
 		cudaEventDestroy(pr.first);
 		cudaEventDestroy(pr.second);
@@ -1631,6 +1677,119 @@ void rdp_graph_destroy(rdp_graph *g)
 	for (auto e : g->ev)
 		if (e) cudaEventDestroy(e);
 	delete g;
+}
+
+int rdp_batch_create(const rdp_batch_create_info *info, rdp_batch **out)
+{
+	if (!info || !out) return RDP_ERR_INVALID;
+	*out = nullptr;
+	if (!rdp_device_is_supported(info->device)) return RDP_ERR_UNSUPPORTED;
+	if (info->flags & ~uint32_t(RDP_BATCH_TILE_ORDER_LEARNED | RDP_BATCH_RECORD_TILE_CYCLES)) return RDP_ERR_INVALID;
+	if (cudaSetDevice(info->device) != cudaSuccess) return RDP_ERR_UNSUPPORTED;
+	rdp_batch *b = new (std::nothrow) rdp_batch();
+	if (!b) return RDP_ERR_OOM;
+	b->device = info->device;
+	b->flags = info->flags;
+	if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess || !b->exec.init(b->device, b->stream))
+	{
+		b->exec.destroy();
+		if (b->stream) cudaStreamDestroy(b->stream);
+		delete b;
+		return RDP_ERR_DEVICE;
+	}
+	b->exec.record_cycles = (info->flags & RDP_BATCH_RECORD_TILE_CYCLES) != 0;
+	*out = b;
+	return RDP_OK;
+}
+
+int rdp_batch_destroy(rdp_batch *b)
+{
+	if (!b) return RDP_ERR_INVALID;
+	if (!b->instances.empty()) return RDP_ERR_INVALID;
+	cudaSetDevice(b->device);
+	b->exec.destroy();
+	for (void *p : b->sink.buffers) cudaFree(p);
+	cudaStreamDestroy(b->stream);
+	delete b;
+	return RDP_OK;
+}
+
+int rdp_batch_add_instance(rdp_batch *b, const rdp_create_info *info, rdp_cp **out)
+{
+	if (!b || !info || !out) return RDP_ERR_INVALID;
+	*out = nullptr;
+	size_t rs = info->rdram_size, hs = info->hidden_rdram_size;
+	if (!rs || (rs & (rs - 1)) || !hs || (hs & (hs - 1)) || rs > (64u << 20) || info->flags != 0 ||
+	    info->device != b->device)
+		return RDP_ERR_INVALID;
+	rdp_cp *cp = new (std::nothrow) rdp_cp();
+	if (!cp) return RDP_ERR_OOM;
+	int r = cp->init(info, b, &b->exec);
+	if (r != RDP_OK)
+	{
+		cp->destroy();
+		delete cp;
+		return r;
+	}
+	b->instances.push_back(cp);
+	*out = cp;
+	return RDP_OK;
+}
+
+int rdp_batch_submit(rdp_batch *b)
+{
+	if (!b) return RDP_ERR_INVALID;
+	cudaSetDevice(b->device);
+	for (rdp_cp *cp : b->instances)
+	{
+		int r = cp->hard_flush();
+		if (r != RDP_OK) return r;
+	}
+	return b->submit();
+}
+
+int rdp_batch_idle(rdp_batch *b)
+{
+	int r = rdp_batch_submit(b);
+	if (r != RDP_OK) return r;
+	if (cudaStreamSynchronize(b->stream) != cudaSuccess) return b->sticky_error = RDP_ERR_DEVICE;
+	for (rdp_cp *cp : b->instances)
+	{
+		uint64_t v = 0;
+		if ((r = cp->signal_timeline(&v)) != RDP_OK || (r = cp->wait_timeline(v, UINT64_MAX / 2)) != RDP_OK) return r;
+	}
+	if (!b->capturing && !b->exec.adapt_pairs()) return b->sticky_error = RDP_ERR_DEVICE;
+	return RDP_OK;
+}
+
+int rdp_batch_get_stats(rdp_batch *b, rdp_batch_stats *out)
+{
+	if (!b || !out) return RDP_ERR_INVALID;
+	out->instances = b->instances.size();
+	out->rounds = b->rounds;
+	out->passes = b->passes;
+	out->kernel_launches = b->exec.kernel_launches;
+	out->staging_bytes = b->exec.staging_bytes;
+	return RDP_OK;
+}
+
+int rdp_batch_capture_begin(rdp_batch *b)
+{
+	if (!b || b->capturing) return RDP_ERR_INVALID;
+	int r = rdp_batch_submit(b);
+	if (r != RDP_OK) return r;
+	b->capturing = true;
+	b->sink = rdpx::CaptureSink{};
+	return RDP_OK;
+}
+
+int rdp_batch_capture_end(rdp_batch *b, rdp_graph **out)
+{
+	if (!b || !out || !b->capturing) return RDP_ERR_INVALID;
+	int r = rdp_batch_submit(b);
+	b->capturing = false;
+	if (r != RDP_OK) return r;
+	return build_graph(&b->exec, b->sink, nullptr, out);
 }
 
 } // extern "C"

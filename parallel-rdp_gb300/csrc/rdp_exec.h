@@ -1,0 +1,450 @@
+/*
+ * Launch executor of the GB300 RDP path: packs one or more recorded passes --
+ * each from a different emulator instance -- into one staging buffer, copies it
+ * to the device with one H2D copy and launches the kernel chain once for all of
+ * them (rdp_kernels.cu).  A stand-alone command processor owns an executor and
+ * submits one pass per launch; a batch shares one executor between its
+ * instances and submits one pass of every instance per launch.
+ *
+ * Device buffers grow on demand.  Growth changes the executor's generation;
+ * CUDA graphs recorded against an older generation refuse to replay.
+ */
+#ifndef RDP_EXEC_H
+#define RDP_EXEC_H
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+#include <algorithm>
+#include <vector>
+
+#include "rdp_types.h"
+#include "rdp_kernels.h"
+
+namespace rdpx {
+
+static inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
+
+// One recorded pass, as plain pointers into the recorder's buffers.  The pass
+// descriptor carries the instance's pointers; the executor fills in the bases.
+struct PassView
+{
+	RdpPass pass;
+	const RdpPrimIn *prims;
+	uint32_t num_prims;
+	const uint32_t *words;
+	uint32_t num_words;
+	const uint32_t *state_blocks;
+	uint32_t num_state_blocks;
+	const RdpTile *tilesets;
+	uint32_t num_tilesets;
+	const RdpUpload *uploads;
+	uint32_t num_uploads;
+};
+
+// An owned copy of a recorded pass (batched instances defer their passes).
+struct PassPacket
+{
+	RdpPass pass;
+	std::vector<RdpPrimIn> prims;
+	std::vector<uint32_t> words, state_blocks;
+	std::vector<RdpTile> tilesets;
+	std::vector<RdpUpload> uploads;
+
+	PassView view() const
+	{
+		PassView v;
+		v.pass = pass;
+		v.prims = prims.data();
+		v.num_prims = uint32_t(prims.size());
+		v.words = words.data();
+		v.num_words = uint32_t(words.size());
+		v.state_blocks = state_blocks.data();
+		v.num_state_blocks = uint32_t(state_blocks.size() / RDP_STATE_BLOCK_WORDS);
+		v.tilesets = tilesets.data();
+		v.num_tilesets = uint32_t(tilesets.size() / 8);
+		v.uploads = uploads.data();
+		v.num_uploads = uint32_t(uploads.size());
+		return v;
+	}
+};
+
+struct ExecCaps
+{
+	uint32_t passes = 0, prims = 0, tile_items = 0, pairs = 0;
+	size_t staging = 0;
+};
+
+// Launches recorded for a CUDA graph, with their device-resident inputs.
+struct CaptureSink
+{
+	std::vector<RdpLaunch> launches;
+	std::vector<void *> buffers;
+};
+
+struct Executor
+{
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	ExecCaps caps;
+	uint64_t generation = 0;
+	uint64_t kernel_launches = 0, staging_bytes = 0, launches = 0;
+	uint32_t shade_ctas = 0;
+	bool failed = false;
+
+	RdpPrimGeom *d_geom = nullptr;
+	RdpPrimAttr *d_attr = nullptr;
+	RdpPrimShade *d_shade = nullptr;
+	uint32_t *d_masks = nullptr, *d_tmem_keep = nullptr;
+	uint32_t *d_tile_counts = nullptr, *d_pair_offsets = nullptr, *d_ctrl = nullptr;
+	uint32_t *d_tile_order = nullptr, *d_tile_cycles = nullptr;
+	uint2 *d_pairs = nullptr;
+	uint32_t *d_sc_color = nullptr;
+	int *d_sc_zdith = nullptr;
+	uint16_t *d_sc_misc = nullptr;
+	uint8_t *d_staging = nullptr;
+
+	struct Staging
+	{
+		uint8_t *h = nullptr;
+		cudaEvent_t done = nullptr;
+		bool in_flight = false;
+	} staging[2];
+	int staging_index = 0;
+
+	bool record_cycles = false;
+
+	bool check(cudaError_t e)
+	{
+		if (e != cudaSuccess) failed = true;
+		return e != cudaSuccess;
+	}
+
+	bool init(int dev, cudaStream_t s)
+	{
+		device = dev;
+		stream = s;
+		int sms = 0;
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+		shade_ctas = uint32_t(std::max(sms, 1)) * uint32_t(rdp_kernels_shade_ctas_per_sm());
+		for (auto &st : staging)
+			if (check(cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming))) return false;
+		if (check(cudaMalloc(&d_ctrl, 16))) return false;
+		return !check(cudaMemsetAsync(d_ctrl, 0, 16, stream));
+	}
+
+	void free_all()
+	{
+		cudaFree(d_geom);
+		cudaFree(d_attr);
+		cudaFree(d_shade);
+		cudaFree(d_masks);
+		cudaFree(d_tmem_keep);
+		cudaFree(d_tile_counts);
+		cudaFree(d_pair_offsets);
+		cudaFree(d_tile_order);
+		cudaFree(d_tile_cycles);
+		cudaFree(d_pairs);
+		cudaFree(d_sc_color);
+		cudaFree(d_sc_zdith);
+		cudaFree(d_sc_misc);
+		cudaFree(d_staging);
+		d_geom = nullptr;
+		d_attr = nullptr;
+		d_shade = nullptr;
+		d_masks = d_tmem_keep = d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = nullptr;
+		d_pairs = nullptr;
+		d_sc_color = nullptr;
+		d_sc_zdith = nullptr;
+		d_sc_misc = nullptr;
+		d_staging = nullptr;
+	}
+
+	void destroy()
+	{
+		if (stream) cudaStreamSynchronize(stream);
+		free_all();
+		cudaFree(d_ctrl);
+		d_ctrl = nullptr;
+		for (auto &st : staging)
+		{
+			if (st.h) cudaFreeHost(st.h);
+			if (st.done) cudaEventDestroy(st.done);
+			st = Staging{};
+		}
+	}
+
+	// Grows the buffers to hold `need`.  Called with the stream idle.
+	bool ensure(const ExecCaps &need)
+	{
+		bool grow_prims = need.prims > caps.prims, grow_tiles = need.tile_items > caps.tile_items;
+		bool grow_passes = need.passes > caps.passes, grow_pairs = need.pairs > caps.pairs;
+		bool grow_staging = need.staging > caps.staging;
+		if (!(grow_prims || grow_tiles || grow_passes || grow_pairs || grow_staging)) return true;
+		if (check(cudaStreamSynchronize(stream))) return false;
+		for (auto &st : staging) st.in_flight = false;
+		generation++;
+		if (grow_prims)
+		{
+			uint32_t n = std::max(need.prims, caps.prims * 2);
+			cudaFree(d_geom);
+			cudaFree(d_attr);
+			cudaFree(d_shade);
+			d_geom = nullptr;
+			d_attr = nullptr;
+			d_shade = nullptr;
+			if (check(cudaMalloc(&d_geom, sizeof(RdpPrimGeom) * n)) || check(cudaMalloc(&d_attr, sizeof(RdpPrimAttr) * n)) ||
+			    check(cudaMalloc(&d_shade, sizeof(RdpPrimShade) * n)))
+				return false;
+			caps.prims = n;
+		}
+		if (grow_tiles)
+		{
+			uint32_t n = std::max(need.tile_items, caps.tile_items + caps.tile_items / 2);
+			cudaFree(d_masks);
+			cudaFree(d_tile_counts);
+			cudaFree(d_pair_offsets);
+			cudaFree(d_tile_order);
+			cudaFree(d_tile_cycles);
+			d_masks = d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = nullptr;
+			if (check(cudaMalloc(&d_masks, size_t(n) * RDP_MASK_WORDS_PER_TILE * 4)) ||
+			    check(cudaMalloc(&d_tile_counts, size_t(n + 1) * 4)) || check(cudaMalloc(&d_pair_offsets, size_t(n + 1) * 4)) ||
+			    check(cudaMalloc(&d_tile_order, size_t(n) * 4)) || check(cudaMalloc(&d_tile_cycles, size_t(n) * 4)))
+				return false;
+			// Bitmasks and counts are self-clearing between launches; they start at zero.
+			if (check(cudaMemsetAsync(d_masks, 0, size_t(n) * RDP_MASK_WORDS_PER_TILE * 4, stream)) ||
+			    check(cudaMemsetAsync(d_tile_counts, 0, size_t(n + 1) * 4, stream)))
+				return false;
+			caps.tile_items = n;
+		}
+		if (grow_passes)
+		{
+			uint32_t n = std::max(need.passes, caps.passes * 2);
+			cudaFree(d_tmem_keep);
+			d_tmem_keep = nullptr;
+			if (check(cudaMalloc(&d_tmem_keep, size_t(n) * RDP_MAX_UPLOADS_PER_PASS * 64 * 4))) return false;
+			caps.passes = n;
+		}
+		if (grow_pairs)
+		{
+			uint32_t n = std::max(need.pairs, caps.pairs * 2);
+			cudaFree(d_pairs);
+			cudaFree(d_sc_color);
+			cudaFree(d_sc_zdith);
+			cudaFree(d_sc_misc);
+			d_pairs = nullptr;
+			d_sc_color = nullptr;
+			d_sc_zdith = nullptr;
+			d_sc_misc = nullptr;
+			if (check(cudaMalloc(&d_pairs, size_t(n) * sizeof(uint2))) ||
+			    check(cudaMalloc(&d_sc_color, size_t(n) * 64 * 4)) || check(cudaMalloc(&d_sc_zdith, size_t(n) * 64 * 4)) ||
+			    check(cudaMalloc(&d_sc_misc, size_t(n) * 64 * 2)))
+				return false;
+			caps.pairs = n;
+		}
+		if (grow_staging)
+		{
+			size_t n = std::max(need.staging, caps.staging + caps.staging / 2);
+			cudaFree(d_staging);
+			d_staging = nullptr;
+			if (check(cudaMalloc(&d_staging, n))) return false;
+			for (auto &st : staging)
+			{
+				if (st.h) cudaFreeHost(st.h);
+				st.h = nullptr;
+				if (check(cudaMallocHost(&st.h, n))) return false;
+			}
+			caps.staging = n;
+		}
+		return !check(cudaStreamSynchronize(stream));
+	}
+
+	// With the stream idle: grows the pair scratch to the largest pair count a launch has
+	// needed, so that later launches take the pair path instead of the fused fallback.
+	bool adapt_pairs()
+	{
+		uint32_t seen[3] = { 0, 0, 0 };
+		if (check(cudaMemcpy(seen, d_ctrl, sizeof(seen), cudaMemcpyDeviceToHost))) return false;
+		if (seen[2] <= caps.pairs) return true;
+		ExecCaps need = caps;
+		need.pairs = 1u;
+		while (need.pairs < seen[2] && need.pairs < (1u << 30)) need.pairs <<= 1;
+		return ensure(need);
+	}
+
+	static size_t staging_bytes_for(const PassView *v, uint32_t n)
+	{
+		size_t b = align16(sizeof(RdpPass) * n) + align16(4 * n) + 256;
+		for (uint32_t i = 0; i < n; i++)
+			b += align16(sizeof(RdpPrimIn) * v[i].num_prims) + align16(4 * v[i].num_words) +
+			     align16(4 * RDP_STATE_BLOCK_WORDS * v[i].num_state_blocks) + align16(sizeof(RdpTile) * 8 * v[i].num_tilesets) +
+			     align16(sizeof(RdpUpload) * v[i].num_uploads);
+		return b;
+	}
+
+	// Launches the kernel chain once for the passes v[0..n) (distinct instances).
+	// With `cap`, the launch is recorded with device-resident inputs instead.
+	bool launch(const PassView *v, uint32_t n, CaptureSink *cap)
+	{
+		if (!n || failed) return !failed;
+		ExecCaps need = caps;
+		uint32_t prims = 0, tiles = 0;
+		for (uint32_t i = 0; i < n; i++)
+		{
+			prims += v[i].num_prims;
+			tiles += v[i].pass.tiles_x * v[i].pass.tiles_y;
+		}
+		need.passes = std::max(need.passes, n);
+		need.prims = std::max(need.prims, std::max(prims, 1u));
+		need.tile_items = std::max(need.tile_items, std::max(tiles, 1u));
+		need.pairs = std::max(need.pairs, 1u << 20);
+		need.staging = std::max(need.staging, staging_bytes_for(v, n));
+		if (!ensure(need)) return false;
+
+		Staging &st = staging[staging_index];
+		staging_index ^= 1;
+		if (st.in_flight)
+		{
+			if (check(cudaEventSynchronize(st.done))) return false;
+			st.in_flight = false;
+		}
+		uint8_t *h = st.h;
+		size_t off = 0;
+		auto reserve = [&](size_t bytes) -> size_t {
+			size_t at = off;
+			off = align16(off + bytes);
+			return at;
+		};
+		size_t o_pass = reserve(sizeof(RdpPass) * n);
+		size_t o_list = reserve(4 * n);
+		RdpPass *passes = reinterpret_cast<RdpPass *>(h + o_pass);
+		uint32_t *tmem_list = reinterpret_cast<uint32_t *>(h + o_list);
+		uint32_t num_tmem = 0, max_uploads = 0;
+		uint32_t prim_base = 0, word_base = 0, sb_base = 0, ts_base = 0, up_base = 0, tile_base = 0;
+		// Sections: all prims, then all words, state blocks, tile sets, uploads.
+		size_t o_prims = reserve(0), cursor;
+		cursor = o_prims;
+		for (uint32_t i = 0; i < n; i++)
+		{
+			memcpy(h + cursor, v[i].prims, sizeof(RdpPrimIn) * v[i].num_prims);
+			cursor += sizeof(RdpPrimIn) * v[i].num_prims;
+		}
+		off = align16(cursor);
+		size_t o_words = off;
+		cursor = o_words;
+		for (uint32_t i = 0; i < n; i++)
+		{
+			memcpy(h + cursor, v[i].words, 4 * size_t(v[i].num_words));
+			cursor += 4 * size_t(v[i].num_words);
+		}
+		off = align16(cursor);
+		size_t o_sb = off;
+		cursor = o_sb;
+		for (uint32_t i = 0; i < n; i++)
+		{
+			memcpy(h + cursor, v[i].state_blocks, 4 * size_t(RDP_STATE_BLOCK_WORDS) * v[i].num_state_blocks);
+			cursor += 4 * size_t(RDP_STATE_BLOCK_WORDS) * v[i].num_state_blocks;
+		}
+		off = align16(cursor);
+		size_t o_ts = off;
+		cursor = o_ts;
+		for (uint32_t i = 0; i < n; i++)
+		{
+			memcpy(h + cursor, v[i].tilesets, sizeof(RdpTile) * 8 * v[i].num_tilesets);
+			cursor += sizeof(RdpTile) * 8 * v[i].num_tilesets;
+		}
+		off = align16(cursor);
+		size_t o_up = off;
+		cursor = o_up;
+		for (uint32_t i = 0; i < n; i++)
+		{
+			memcpy(h + cursor, v[i].uploads, sizeof(RdpUpload) * v[i].num_uploads);
+			cursor += sizeof(RdpUpload) * v[i].num_uploads;
+		}
+		off = align16(cursor) + 16;
+		for (uint32_t i = 0; i < n; i++)
+		{
+			RdpPass p = v[i].pass;
+			p.prim_begin = prim_base;
+			p.prim_count = v[i].num_prims;
+			p.word_base = word_base;
+			p.sb_base = sb_base;
+			p.ts_base = ts_base;
+			p.upload_begin = up_base;
+			p.upload_count = v[i].num_uploads;
+			p.tile_item_begin = tile_base;
+			p.masks = d_masks + size_t(tile_base) * RDP_MASK_WORDS_PER_TILE;
+			passes[i] = p;
+			if (v[i].num_uploads)
+			{
+				tmem_list[num_tmem++] = i;
+				max_uploads = std::max(max_uploads, v[i].num_uploads);
+			}
+			prim_base += v[i].num_prims;
+			word_base += v[i].num_words;
+			sb_base += v[i].num_state_blocks;
+			ts_base += v[i].num_tilesets;
+			up_base += v[i].num_uploads;
+			tile_base += p.tiles_x * p.tiles_y;
+		}
+
+		uint8_t *dst = d_staging;
+		if (cap)
+		{
+			if (check(cudaMalloc(&dst, off))) return false;
+			cap->buffers.push_back(dst);
+			if (check(cudaMemcpy(dst, h, off, cudaMemcpyHostToDevice))) return false;
+		}
+		else
+		{
+			if (check(cudaMemcpyAsync(d_staging, h, off, cudaMemcpyHostToDevice, stream))) return false;
+			if (check(cudaEventRecord(st.done, stream))) return false;
+			st.in_flight = true;
+		}
+		staging_bytes += off;
+
+		RdpLaunch L = {};
+		L.prims_in = reinterpret_cast<const RdpPrimIn *>(dst + o_prims);
+		L.num_prims = prim_base;
+		L.words = reinterpret_cast<const uint32_t *>(dst + o_words);
+		L.state_blocks = reinterpret_cast<const uint32_t *>(dst + o_sb);
+		L.passes = reinterpret_cast<const RdpPass *>(dst + o_pass);
+		L.num_passes = n;
+		L.geom = d_geom;
+		L.attr = d_attr;
+		L.shade = d_shade;
+		L.tilesets = reinterpret_cast<const RdpTile *>(dst + o_ts);
+		L.tmem_pass_list = reinterpret_cast<const uint32_t *>(dst + o_list);
+		L.num_tmem_passes = num_tmem;
+		L.uploads = reinterpret_cast<const RdpUpload *>(dst + o_up);
+		L.max_uploads = max_uploads;
+		L.tmem_keep = d_tmem_keep;
+		L.tile_counts = d_tile_counts;
+		L.pair_offsets = d_pair_offsets;
+		L.pairs = d_pairs;
+		L.ctrl = d_ctrl;
+		L.pair_capacity = caps.pairs;
+		L.shade_ctas = shade_ctas;
+		L.sc_color = d_sc_color;
+		L.sc_zdith = d_sc_zdith;
+		L.sc_misc = d_sc_misc;
+		L.num_tile_items = tile_base;
+		L.tile_cycles = record_cycles ? d_tile_cycles : nullptr;
+		L.tile_order = nullptr;
+		launches++;
+		if (cap)
+		{
+			for (auto &e : L.shade_events)
+				if (check(cudaEventCreate(&e))) return false;
+			cap->launches.push_back(L);
+			return true;
+		}
+		if (check(rdp_kernels_launch(&L, stream))) return false;
+		kernel_launches += rdp_kernels_count(&L);
+		return true;
+	}
+};
+
+} // namespace rdpx
+
+#endif

@@ -117,17 +117,42 @@ __device__ void interp_x64(const RdpPrimGeom &g, int y, bool flip, long long &xl
 	if (xr < -2147483648LL) xr = -2147483648LL;
 }
 
+// Pass of a launch that holds primitive i / tile item `item` (passes are sorted by both).
+__device__ __forceinline__ uint32_t pass_of_prim(const RdpPass *__restrict__ passes, uint32_t num_passes, uint32_t i)
+{
+	uint32_t lo = 0, hi = num_passes - 1;
+	while (lo < hi)
+	{
+		uint32_t mid = (lo + hi + 1) >> 1;
+		if (passes[mid].prim_begin <= i) lo = mid;
+		else hi = mid - 1;
+	}
+	return lo;
+}
+__device__ __forceinline__ uint32_t pass_of_item(const RdpPass *__restrict__ passes, uint32_t num_passes, uint32_t item)
+{
+	uint32_t lo = 0, hi = num_passes - 1;
+	while (lo < hi)
+	{
+		uint32_t mid = (lo + hi + 1) >> 1;
+		if (passes[mid].tile_item_begin <= item) lo = mid;
+		else hi = mid - 1;
+	}
+	return lo;
+}
+
 __global__ void k_prim_setup(const RdpPrimIn *__restrict__ in, uint32_t num_prims, const uint32_t *__restrict__ words,
                              const uint32_t *__restrict__ state_blocks, const RdpPass *__restrict__ passes,
-                             RdpPrimGeom *__restrict__ geom_out, RdpPrimAttr *__restrict__ attr_out,
+                             uint32_t num_passes, RdpPrimGeom *__restrict__ geom_out, RdpPrimAttr *__restrict__ attr_out,
                              RdpPrimShade *__restrict__ shade_out)
 {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= num_prims) return;
 	RdpPrimIn pi = in[i];
-	const uint32_t *w = words + pi.word_offset;
-	const uint32_t *sb = state_blocks + size_t(pi.state_block) * RDP_STATE_BLOCK_WORDS;
-	const RdpPass &pass = passes[pi.pass];
+	const uint32_t pass_index = pass_of_prim(passes, num_passes, i);
+	const RdpPass &pass = passes[pass_index];
+	const uint32_t *w = words + pass.word_base + pi.word_offset;
+	const uint32_t *sb = state_blocks + size_t(pass.sb_base + pi.state_block) * RDP_STATE_BLOCK_WORDS;
 
 	// ---- other modes (rdp_device.cpp:474-540)
 	uint32_t om0 = sb[SB_OTHER_MODES], om1 = sb[SB_OTHER_MODES + 1];
@@ -454,9 +479,9 @@ __global__ void k_prim_setup(const RdpPrimIn *__restrict__ in, uint32_t num_prim
 	sh.coverage_mode = (om1 >> 8) & 3;
 	sh.z_mode = (om1 >> 10) & 3;
 	sh.tmem_index = pi.tmem_index;
-	sh.tileset = pi.tileset;
+	sh.tileset = pass.ts_base + pi.tileset;
 	sh.prim_index = pass.base_prim_index + (i - pass.prim_begin);
-	sh.pass = pi.pass;
+	sh.pass = pass_index;
 	sh.pad[0] = sh.pad[1] = sh.pad[2] = 0;
 
 	// ---- span job range (rdp_renderer.cpp:1523-1554)
@@ -2433,6 +2458,7 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t num_items, uint32_t *__r
 		offsets[num_items] = carry;
 		ctrl[0] = carry;
 		ctrl[1] = carry > capacity ? 1u : 0u;
+		ctrl[2] = max(ctrl[2], carry); // largest pair count seen: the host grows the scratch to it
 	}
 }
 
@@ -2444,9 +2470,7 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 	uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	int lane = threadIdx.x & 31;
 	if (item >= num_items || ctrl[1]) return;
-	uint32_t pi = 0;
-	for (uint32_t k = 1; k < num_passes; k++)
-		if (passes[k].tile_item_begin <= item) pi = k;
+	const uint32_t pi = pass_of_item(passes, num_passes, item);
 	const RdpPass &ps = passes[pi];
 	uint32_t tl = item - ps.tile_item_begin;
 	uint32_t *masks = ps.masks + size_t(tl) * RDP_MASK_WORDS_PER_TILE;
@@ -2504,9 +2528,7 @@ __global__ void __launch_bounds__(SHADE_THREADS) k_shade(const RdpPass *__restri
 	{
 		uint2 pa = pairs[pr];
 		uint32_t prim = pa.x, item = pa.y;
-		uint32_t pi = 0;
-		for (uint32_t k = 1; k < num_passes; k++)
-			if (passes[k].tile_item_begin <= item) pi = k;
+		const uint32_t pi = pass_of_item(passes, num_passes, item);
 		const RdpPass &ps = passes[pi];
 		uint32_t tl = item - ps.tile_item_begin;
 		int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
@@ -2561,15 +2583,20 @@ __global__ void __launch_bounds__(SHADE_THREADS) k_blend(const RdpPass *__restri
                                                         const uint32_t *__restrict__ sc_color,
                                                         const int *__restrict__ sc_zdith,
                                                         const uint16_t *__restrict__ sc_misc,
-                                                        unsigned long long *__restrict__ counters)
+                                                        const uint32_t *__restrict__ order,
+                                                        uint32_t *__restrict__ cycles)
 {
-	const uint32_t item = blockIdx.x;
-	if (item >= num_items || ctrl[1]) return;
+	if (blockIdx.x >= num_items || ctrl[1]) return;
+	// CTAs start in blockIdx order: `order` puts the tiles expected to take longest first.
+	const uint32_t item = order ? order[blockIdx.x] : blockIdx.x;
 	const uint32_t p0 = offsets[item], p1 = offsets[item + 1];
-	if (p0 == p1) return;
-	uint32_t pi = 0;
-	for (uint32_t k = 1; k < num_passes; k++)
-		if (passes[k].tile_item_begin <= item) pi = k;
+	if (p0 == p1)
+	{
+		if (cycles && threadIdx.x == 0) cycles[item] = 0;
+		return;
+	}
+	const long long t_start = clock64();
+	const uint32_t pi = pass_of_item(passes, num_passes, item);
 	const RdpPass &ps = passes[pi];
 	const uint32_t tl = item - ps.tile_item_begin;
 	const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
@@ -2616,13 +2643,24 @@ __global__ void __launch_bounds__(SHADE_THREADS) k_blend(const RdpPass *__restri
 		}
 		store_pixel(ps, px, ci, di, pc.alias);
 	}
+	unsigned long long *counters = ps.counters;
 	if (counters)
 	{
 		unsigned long long total = frags;
 #pragma unroll
 		for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
 		if ((tid & 31) == 0 && total) atomicAdd(counters, total);
-		if (tid == 0) atomicAdd(counters + 1, 1ull);
+		if (tid == 0)
+		{
+			atomicAdd(counters + 1, 1ull);
+			atomicAdd(counters + 2, (unsigned long long)(p1 - p0));
+		}
+	}
+	if (cycles)
+	{
+		// Per-tile cost sample for the learned tile-order model: the slower warp's cycles.
+		__syncthreads();
+		if (tid == 0) cycles[item] = uint32_t(min(clock64() - t_start, 0xffffffffll));
 	}
 }
 
@@ -2637,7 +2675,6 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const RdpPass *__rest
                                                           const RdpPrimAttr *__restrict__ attr,
                                                           const RdpPrimShade *__restrict__ shade,
                                                           const RdpTile *__restrict__ tilesets,
-                                                          unsigned long long *__restrict__ fragments,
                                                           const uint32_t *__restrict__ ctrl)
 {
 	__shared__ SpanA s_sa[2][5];
@@ -2649,9 +2686,7 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const RdpPass *__rest
 	// Only runs when the pair list overflowed the scratch capacity (ctrl[1]).
 	if (item >= num_items || !ctrl[1]) return;
 
-	uint32_t pi = 0;
-	for (uint32_t k = 1; k < num_passes; k++)
-		if (passes[k].tile_item_begin <= item) pi = k;
+	const uint32_t pi = pass_of_item(passes, num_passes, item);
 	const RdpPass &ps = passes[pi];
 	const uint32_t tile_linear = item - ps.tile_item_begin;
 	const int tx = int(tile_linear % ps.tiles_x), ty = int(tile_linear / ps.tiles_x);
@@ -2738,15 +2773,26 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const RdpPass *__rest
 	__syncthreads();
 	if (loaded && lane == 0) s_any = 1;
 	__syncthreads();
+	unsigned long long pairs_here = 0;
 	if (s_any)
-		for (uint32_t wi = threadIdx.x; wi < nwords; wi += RASTER_THREADS) masks[wi] = 0u;
+		for (uint32_t wi = threadIdx.x; wi < nwords; wi += RASTER_THREADS)
+		{
+			pairs_here += __popc(masks[wi]);
+			masks[wi] = 0u;
+		}
 
+	unsigned long long *fragments = ps.counters;
 	if (fragments)
 	{
 		unsigned long long total = frags;
 #pragma unroll
-		for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+		for (int o = 16; o > 0; o >>= 1)
+		{
+			total += __shfl_xor_sync(0xffffffffu, total, o);
+			pairs_here += __shfl_xor_sync(0xffffffffu, pairs_here, o);
+		}
 		if (lane == 0 && total) atomicAdd(fragments, total);
+		if (lane == 0 && pairs_here) atomicAdd(fragments + 2, pairs_here);
 		if (threadIdx.x == 0 && s_any) atomicAdd(fragments + 1, 1ull);
 	}
 }
@@ -2781,8 +2827,8 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 	if (L->num_prims)
 	{
 		rdp::k_prim_setup<<<(L->num_prims + 127) / 128, 128, 0, stream>>>(L->prims_in, L->num_prims, L->words,
-		                                                                   L->state_blocks, L->passes, L->geom,
-		                                                                   L->attr, L->shade);
+		                                                                   L->state_blocks, L->passes, L->num_passes,
+		                                                                   L->geom, L->attr, L->shade);
 		rdp::k_bin<<<(L->num_prims * 32 + 255) / 256, 256, 0, stream>>>(L->num_prims, L->geom, L->shade, L->passes,
 		                                                                 L->tile_counts);
 	}
@@ -2793,23 +2839,23 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		rdp::k_tmem_carry<<<dim3(2048 / 32, L->num_tmem_passes), 32, 0, stream>>>(L->passes, L->tmem_pass_list,
 		                                                                         L->tmem_keep);
 	}
-	if (raster && L->raster_events[0]) cudaEventRecordWithFlags(L->raster_events[0], stream, cudaEventRecordExternal);
 	if (raster)
 	{
 		rdp::k_scan<<<1, 1024, 0, stream>>>(L->num_tile_items, L->tile_counts, L->pair_offsets, L->ctrl,
 		                                    L->pair_capacity);
 		rdp::k_expand<<<(L->num_tile_items * 32 + 255) / 256, 256, 0, stream>>>(
 			L->passes, L->num_passes, L->num_tile_items, L->pair_offsets, L->ctrl, L->pairs);
+		if (L->shade_events[0]) cudaEventRecordWithFlags(L->shade_events[0], stream, cudaEventRecordExternal);
 		rdp::k_shade<<<L->shade_ctas, rdp::SHADE_THREADS, 0, stream>>>(L->passes, L->num_passes, L->pairs, L->ctrl,
 		                                                               L->geom, L->attr, L->shade, L->tilesets,
 		                                                               L->sc_color, L->sc_zdith, L->sc_misc);
+		if (L->shade_events[1]) cudaEventRecordWithFlags(L->shade_events[1], stream, cudaEventRecordExternal);
 		rdp::k_blend<<<L->num_tile_items, rdp::SHADE_THREADS, 0, stream>>>(
 			L->passes, L->num_passes, L->num_tile_items, L->pair_offsets, L->pairs, L->ctrl, L->shade, L->sc_color,
-			L->sc_zdith, L->sc_misc, L->fragments);
+			L->sc_zdith, L->sc_misc, L->tile_order, L->tile_cycles);
 		rdp::k_raster<<<L->num_tile_items, rdp::RASTER_THREADS, 0, stream>>>(
-			L->passes, L->num_passes, L->num_tile_items, L->geom, L->attr, L->shade, L->tilesets, L->fragments, L->ctrl);
+			L->passes, L->num_passes, L->num_tile_items, L->geom, L->attr, L->shade, L->tilesets, L->ctrl);
 	}
-	if (raster && L->raster_events[1]) cudaEventRecordWithFlags(L->raster_events[1], stream, cudaEventRecordExternal);
 	return cudaGetLastError();
 }
 

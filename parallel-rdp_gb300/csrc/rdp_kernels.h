@@ -23,8 +23,9 @@ typedef struct RdpLaunch
 	uint32_t max_uploads;     /* largest upload count of the TMEM passes */
 	uint32_t *tmem_keep;      /* [num_tmem_passes][RDP_MAX_UPLOADS_PER_PASS][64] scratch bitmask */
 	uint32_t num_tile_items;
-	unsigned long long *fragments; /* [0] fragments, [1] touched tiles */
-	cudaEvent_t raster_events[2];   /* optional: recorded around the rasterisation kernels */
+	cudaEvent_t shade_events[2];    /* optional: recorded around the k_shade launch */
+	const uint32_t *tile_order;     /* optional [num_tile_items]: order in which k_blend starts tiles */
+	uint32_t *tile_cycles;          /* optional [num_tile_items]: measured k_blend cycles per tile */
 	/* pair list + shading scratch */
 	uint32_t *tile_counts;          /* [num_tile_items], zero between launches */
 	uint32_t *pair_offsets;         /* [num_tile_items + 1] */

@@ -210,6 +210,10 @@ typedef struct __attribute__((aligned(16))) RdpPass
 	uint32_t tile_item_begin; /* prefix over passes of tiles_x * tiles_y */
 	uint32_t instance;
 	uint32_t base_prim_index; /* primitives drawn by this instance before the pass (noise seed base) */
+	/* Offsets of the pass's command words, state blocks and tile sets in the launch's buffers
+	   (a primitive's word_offset / state_block / tileset are relative to its pass). */
+	uint32_t word_base, sb_base, ts_base, pad0;
+	unsigned long long *counters; /* the instance's [0] fragments, [1] touched tiles, [2] tile instances */
 } RdpPass;
 
 /* Device-side error word bits (bounded waits and bounds checks report here). */

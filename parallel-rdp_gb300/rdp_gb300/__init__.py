@@ -6,6 +6,7 @@ librdp_cuda.so (include/rdp_cuda.h).  There is no CPU fallback: importing this
 package fails loudly when the native library has not been built.
 """
 from .native import (  # noqa: F401
+    Batch,
     CommandProcessor,
     RdpError,
     RdpTimeout,

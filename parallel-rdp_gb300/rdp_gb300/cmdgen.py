@@ -84,3 +84,20 @@ def color_addr():
 
 def depth_addr():
     return _load().rdpgen_depth_addr()
+
+
+BATCH_RESOLUTIONS = ((320, 240), (640, 240), (640, 480))
+
+
+def batched_instance_params(instance, min_prims=500, max_prims=50000, seed_base=0):
+    """Generator parameters of one instance of the batched-instances workload: the
+    mixed RGBA8888 primitive mix of CONFIG_MIXED, one frame, a resolution drawn from
+    BATCH_RESOLUTIONS and a primitive count log-uniform in [min_prims, max_prims],
+    both drawn from the instance seed (seed_base + instance)."""
+    import math
+    seed = seed_base + instance
+    rng = np.random.default_rng(0x5EED0000 + seed)
+    w, h = BATCH_RESOLUTIONS[int(rng.integers(0, len(BATCH_RESOLUTIONS)))]
+    u = float(rng.random())
+    n = int(round(math.exp(math.log(min_prims) + u * (math.log(max_prims) - math.log(min_prims)))))
+    return default_params(CONFIG_MIXED, seed=seed, width=w, height=h, num_prims=n, num_frames=1)

@@ -75,7 +75,8 @@ class ScanoutOptions(ctypes.Structure):
 class _Stats(ctypes.Structure):
     _fields_ = [("primitives", ctypes.c_uint64), ("passes", ctypes.c_uint64), ("reference_passes", ctypes.c_uint64),
                 ("fragments", ctypes.c_uint64), ("tmem_uploads", ctypes.c_uint64), ("touched_tiles", ctypes.c_uint64),
-                ("kernel_launches", ctypes.c_uint64), ("staging_bytes", ctypes.c_uint64)]
+                ("kernel_launches", ctypes.c_uint64), ("staging_bytes", ctypes.c_uint64),
+                ("tile_instances", ctypes.c_uint64)]
 
 
 _VALIDATION_CB = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p)
@@ -87,10 +88,25 @@ EXPORTED_SYMBOLS = [
     "rdp_cp_begin_read_hidden_rdram", "rdp_cp_end_write_hidden_rdram", "rdp_cp_get_rdram_size",
     "rdp_cp_get_hidden_rdram_size", "rdp_cp_get_tmem", "rdp_cp_set_vi_register", "rdp_cp_scanout_sync",
     "rdp_cp_get_stats", "rdp_cp_capture_begin", "rdp_cp_capture_end", "rdp_graph_replay", "rdp_graph_kernel_count",
-    "rdp_graph_destroy", "rdp_graph_last_raster_ms", "rdp_graph_raster_launches", "rdp_scanout_options_default",
+    "rdp_graph_destroy", "rdp_graph_last_shade_ms", "rdp_graph_shade_launches", "rdp_scanout_options_default",
     "rdp_cp_begin_vi_register_per_scanline", "rdp_cp_set_vi_register_for_scanline",
     "rdp_cp_latch_vi_register_for_scanline", "rdp_cp_end_vi_register_per_scanline",
+    "rdp_batch_create", "rdp_batch_destroy", "rdp_batch_add_instance", "rdp_batch_submit", "rdp_batch_idle",
+    "rdp_batch_get_stats", "rdp_batch_capture_begin", "rdp_batch_capture_end",
 ]
+
+
+class _BatchCreateInfo(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("flags", ctypes.c_uint32)]
+
+
+class _BatchStats(ctypes.Structure):
+    _fields_ = [("instances", ctypes.c_uint64), ("rounds", ctypes.c_uint64), ("passes", ctypes.c_uint64),
+                ("kernel_launches", ctypes.c_uint64), ("staging_bytes", ctypes.c_uint64)]
+
+
+BATCH_TILE_ORDER_LEARNED = 1 << 0
+BATCH_RECORD_TILE_CYCLES = 1 << 1
 
 
 def library_path():
@@ -146,10 +162,18 @@ def lib():
     L.rdp_graph_kernel_count.restype = u32
     L.rdp_graph_destroy.argtypes = [vp]
     L.rdp_graph_destroy.restype = None
-    L.rdp_graph_last_raster_ms.argtypes = [vp]
-    L.rdp_graph_last_raster_ms.restype = ctypes.c_float
-    L.rdp_graph_raster_launches.argtypes = [vp]
-    L.rdp_graph_raster_launches.restype = u32
+    L.rdp_graph_last_shade_ms.argtypes = [vp]
+    L.rdp_graph_last_shade_ms.restype = ctypes.c_float
+    L.rdp_graph_shade_launches.argtypes = [vp]
+    L.rdp_graph_shade_launches.restype = u32
+    L.rdp_batch_create.argtypes = [ctypes.POINTER(_BatchCreateInfo), ctypes.POINTER(vp)]
+    L.rdp_batch_destroy.argtypes = [vp]
+    L.rdp_batch_add_instance.argtypes = [vp, ctypes.POINTER(_CreateInfo), ctypes.POINTER(vp)]
+    L.rdp_batch_submit.argtypes = [vp]
+    L.rdp_batch_idle.argtypes = [vp]
+    L.rdp_batch_get_stats.argtypes = [vp, ctypes.POINTER(_BatchStats)]
+    L.rdp_batch_capture_begin.argtypes = [vp]
+    L.rdp_batch_capture_end.argtypes = [vp, ctypes.POINTER(vp)]
     _lib = L
     return L
 
@@ -173,16 +197,21 @@ class CommandProcessor:
     a zero-initialised one.
     """
 
-    def __init__(self, rdram=None, rdram_size=8 << 20, hidden_rdram_size=None, device=0):
+    def __init__(self, rdram=None, rdram_size=8 << 20, hidden_rdram_size=None, device=0, batch=None):
         if hidden_rdram_size is None:
             hidden_rdram_size = rdram_size // 2
         if rdram is None:
             rdram = np.zeros(rdram_size, dtype=np.uint8)
         assert rdram.dtype == np.uint8 and rdram.flags["C_CONTIGUOUS"] and rdram.size >= rdram_size
         self._rdram = rdram
+        self._batch = batch
         info = _CreateInfo(rdram.ctypes.data, 0, rdram_size, hidden_rdram_size, 0, device)
         h = ctypes.c_void_p()
-        _check(lib().rdp_cp_create(ctypes.byref(info), ctypes.byref(h)), "rdp_cp_create")
+        if batch is None:
+            _check(lib().rdp_cp_create(ctypes.byref(info), ctypes.byref(h)), "rdp_cp_create")
+        else:
+            _check(lib().rdp_batch_add_instance(batch._h, ctypes.byref(info), ctypes.byref(h)),
+                   "rdp_batch_add_instance")
         self._h = h
         self.rdram_size = rdram_size
         self.hidden_rdram_size = hidden_rdram_size
@@ -318,15 +347,15 @@ class Graph:
     def __init__(self, handle):
         self._h = handle
         self.kernels = lib().rdp_graph_kernel_count(handle)
-        self.raster_launches = lib().rdp_graph_raster_launches(handle)
+        self.shade_launches = lib().rdp_graph_shade_launches(handle)
 
     def replay(self, count=1):
         ms = ctypes.c_float()
         _check(lib().rdp_graph_replay(self._h, count, ctypes.byref(ms)), "graph_replay")
         return ms.value
 
-    def last_raster_ms(self):
-        return lib().rdp_graph_last_raster_ms(self._h)
+    def last_shade_ms(self):
+        return lib().rdp_graph_last_shade_ms(self._h)
 
     def close(self):
         if self._h:
@@ -334,4 +363,61 @@ class Graph:
             self._h = None
 
     def __del__(self):
+        self.close()
+
+
+class Batch:
+    """Many emulator instances rendered together (rdp_batch_*): every instance is a
+    CommandProcessor whose passes are deferred; submit() launches one kernel chain
+    per round of at most one pass per instance."""
+
+    def __init__(self, device=0, learned_order=False, record_tile_cycles=False):
+        flags = (BATCH_TILE_ORDER_LEARNED if learned_order else 0) | (BATCH_RECORD_TILE_CYCLES if record_tile_cycles else 0)
+        info = _BatchCreateInfo(device, flags)
+        h = ctypes.c_void_p()
+        _check(lib().rdp_batch_create(ctypes.byref(info), ctypes.byref(h)), "rdp_batch_create")
+        self._h = h
+        self.device = device
+        self._instances = []
+
+    def add_instance(self, rdram=None, rdram_size=8 << 20, hidden_rdram_size=None):
+        cp = CommandProcessor(rdram, rdram_size, hidden_rdram_size, self.device, batch=self)
+        self._instances.append(cp)
+        return cp
+
+    def submit(self):
+        _check(lib().rdp_batch_submit(self._h), "batch_submit")
+
+    def idle(self):
+        _check(lib().rdp_batch_idle(self._h), "batch_idle")
+
+    def stats(self):
+        s = _BatchStats()
+        _check(lib().rdp_batch_get_stats(self._h, ctypes.byref(s)), "batch_get_stats")
+        return {k: getattr(s, k) for k, _ in _BatchStats._fields_}
+
+    def capture(self, per_instance_words):
+        """Records one sync point of every instance (words[i] for instance i) into a CUDA graph."""
+        _check(lib().rdp_batch_capture_begin(self._h), "batch_capture_begin")
+        for cp, w in zip(self._instances, per_instance_words):
+            cp.enqueue_command(w)
+        g = ctypes.c_void_p()
+        _check(lib().rdp_batch_capture_end(self._h, ctypes.byref(g)), "batch_capture_end")
+        return Graph(g)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            for cp in self._instances:
+                cp.close()
+            self._instances = []
+            lib().rdp_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
         self.close()

@@ -9,6 +9,7 @@ def run_oracle(words, rdram_init, rdram_size=8 << 20):
     o.write_rdram(rdram_init[:rdram_size])
     consumed = o.enqueue(words)
     assert consumed == len(words)
+    run_oracle.reference_passes = o.reference_passes()
     return o.rdram(), o.hidden(), o.tmem(), o.fragments()
 
 
@@ -46,4 +47,7 @@ def assert_parity(words, rdram_init, rdram_size=8 << 20, chunks=1):
                         diff_report("tmem", g_tmem.view(np.uint8), o_tmem.view(np.uint8))) if e]
     assert not errs, "; ".join(errs)
     assert stats["fragments"] == frags, (stats["fragments"], frags)
+    # The throughput unit: both sides count the reference's render passes the same way.
+    assert stats["reference_passes"] == run_oracle.reference_passes, (stats["reference_passes"],
+                                                                      run_oracle.reference_passes)
     return stats

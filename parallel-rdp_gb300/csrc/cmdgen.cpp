@@ -685,6 +685,10 @@ struct Gen
 		uint32_t blob_index = rng.below(8);
 		uint32_t blob_offset = rng.below(4) << 3;
 		uint32_t blob = FUZZ_BLOB + blob_index * 0x1000 + blob_offset;
+		// Sometimes load from an image this stream renders into (a read-after-write hazard).
+		uint32_t rt = rng.below(16);
+		if (rt == 0) blob = COLOR_ADDR + (rng.below(64) << 6);
+		else if (rt == 1) blob = LAYER_ADDR + (rng.below(64) << 6);
 		uint32_t line_qw = row_bytes / 8;
 		uint32_t tmem_qw = (siz == 3 || fmt == 1) ? rng.below(2) * 8 : rng.below(4) * 16;
 		emit2(uint32_t(OP_SYNC_LOAD) << 24, 0);
@@ -792,6 +796,21 @@ struct Gen
 					      (il << 24) | (((x1 << 2) - f[2]) << 12) | ((y1 << 2) - f[3]));
 				}
 				if (r < 12) fuzz_texture();
+				if (r >= 96)
+				{
+					// Switch the colour image: the main image, or a second image at LAYER_ADDR in
+					// a random format and width (several images per pass, I8 among them).
+					uint32_t pick = rng.below(3);
+					if (pick == 0)
+						set_color_image(COLOR_ADDR, fb_size_bits(), p.width, fb_fmt_bits());
+					else
+					{
+						static const uint32_t fmts[][2] = { { 2, 0 }, { 2, 3 }, { 1, 0 }, { 3, 0 }, { 0, 0 } }; // size, fmt bits
+						const uint32_t *f = fmts[rng.below(5)];
+						uint32_t lw = pick == 1 ? p.width : 64 + rng.below(p.width - 63);
+						set_color_image(LAYER_ADDR, f[0], lw, f[1]);
+					}
+				}
 				if (r < 20)
 				{
 					uint32_t cv0 = rng.u32() & 0x3fffff;

@@ -120,6 +120,7 @@ struct rdp_cp
 
 	// ---------------------------------------------------------------- pass being recorded
 	std::vector<RdpPrimIn> prims;
+	std::vector<RdpPrimIn> grouped; // prims regrouped by target at flush
 	std::vector<uint32_t> words;
 	std::vector<uint32_t> state_blocks;
 	std::vector<RdpTile> tilesets;
@@ -134,18 +135,46 @@ struct rdp_cp
 	struct
 	{
 		uint32_t addr = 0, width = 0, fmt = FBF_RGBA5551, depth_addr = 0;
-		uint32_t deduced_height = 0;
-		bool color_pending = false, depth_pending = false;
-	} fb;
+	} fb; // image registers (SetColorImage / SetMaskImage)
 	uint64_t base_prim_index = 0;
 	std::vector<uint32_t> carry;
 
-	// The reference keeps pixel state in registers for a whole render pass; for I8 colour
-	// images and colour/depth aliasing the store/reload round trip is not transparent, so
-	// those passes are cut exactly where the reference cuts them: after 256 primitives
-	// (Limits::MaxPrimitives) and before the 256th TMEM upload (rdp_renderer.cpp:3484-3485).
-	uint32_t rsr_prims = 0, rsr_uploads = 0;
-	bool pass_boundaries_visible() const { return fb.fmt == FBF_I8 || fb.addr == fb.depth_addr; }
+	// A pass may draw into several colour images ("targets") as long as their memory --
+	// colour, and depth where a target uses it -- does not overlap: their pixels are then
+	// independent and the order between them does not matter.  The reference ends its pass
+	// at every image change; it keeps pixel state for the pass (init_tile/finish_tile,
+	// memory_interfacing.h:286-362), and for RGBA5551, RGBA8888, IA88 and I4 images that
+	// store/reload round trip is transparent, so longer passes give identical results.
+	struct Target
+	{
+		uint32_t addr = 0, width = 0, fmt = 0, depth_addr = 0, deduced_height = 0;
+		bool color_pending = false, depth_pending = false, depth_used = false;
+		std::vector<uint32_t> prim_ids; // indices into `prims`
+	};
+	std::vector<Target> targets;
+
+	// The reference's own pass (it ends after 256 primitives, before the 256th TMEM upload,
+	// at image changes, load hazards and SyncFull; rdp_renderer.cpp:1564-1590, 3051-3097,
+	// 3484-3485): the state its load-hazard check sees.  For I8 images and colour/depth
+	// aliasing the round trip is NOT transparent (odd I8 pixels store green but blending
+	// reads red; aliased colour and depth share memory), so there the passes of this
+	// processor end exactly where the reference's do.
+	struct RefView
+	{
+		uint32_t prims = 0, uploads = 0, deduced_height = 0;
+		bool color_pending = false, depth_pending = false;
+	} rv;
+	static bool boundaries_visible(uint32_t fmt, uint32_t addr, uint32_t depth_addr)
+	{
+		return fmt == FBF_I8 || addr == depth_addr;
+	}
+	bool pass_boundaries_visible() const { return boundaries_visible(fb.fmt, fb.addr, fb.depth_addr); }
+	// The reference's pass ends: with visible boundaries this processor's pass ends too.
+	void rv_end()
+	{
+		rv = RefView{};
+		if (pass_boundaries_visible()) flush();
+	}
 
 	// ---------------------------------------------------------------- coherency + timeline
 	std::vector<std::pair<uint32_t, uint32_t>> dirty_ranges;
@@ -326,15 +355,47 @@ struct rdp_cp
 	}
 
 	// ================================================================= pass submission
-	uint32_t fb_bytes_per_pixel() const
+	static uint32_t bytes_per_pixel(uint32_t fmt)
 	{
-		switch (fb.fmt)
+		switch (fmt)
 		{
 		case FBF_I4:
 		case FBF_I8: return 1;
 		case FBF_RGBA8888: return 4;
 		default: return 2;
 		}
+	}
+
+	// RDRAM byte range [lo, hi) of `rows` rows of a target's colour (or depth) image;
+	// ranges that wrap around RDRAM cover all of it.
+	std::pair<uint64_t, uint64_t> image_range(uint32_t addr, uint32_t width, uint32_t bpp, uint32_t rows) const
+	{
+		uint64_t lo = addr & (rdram_size - 1), hi = lo + uint64_t(width) * rows * bpp;
+		if (hi > rdram_size) return { 0, rdram_size };
+		return { lo, hi };
+	}
+	static bool overlap(std::pair<uint64_t, uint64_t> a, std::pair<uint64_t, uint64_t> b)
+	{
+		return a.first < a.second && b.first < b.second && a.first < b.second && b.first < a.second;
+	}
+	// Would target `ti`, grown to `rows` rows (using depth if `depth`), touch memory that
+	// another target of the pass touches?
+	bool target_conflicts(size_t ti, uint32_t rows, bool depth) const
+	{
+		const Target &n = targets[ti];
+		auto nc = image_range(n.addr, n.width, bytes_per_pixel(n.fmt), rows);
+		std::pair<uint64_t, uint64_t> nd = { 0, 0 };
+		if (depth || n.depth_used) nd = image_range(n.depth_addr, n.width, 2, rows);
+		for (size_t k = 0; k < targets.size(); k++)
+		{
+			if (k == ti) continue;
+			const Target &o = targets[k];
+			auto oc = image_range(o.addr, o.width, bytes_per_pixel(o.fmt), o.deduced_height);
+			std::pair<uint64_t, uint64_t> od = { 0, 0 };
+			if (o.depth_used) od = image_range(o.depth_addr, o.width, 2, o.deduced_height);
+			if (overlap(nc, oc) || overlap(nc, od) || overlap(nd, oc) || overlap(nd, od)) return true;
+		}
+		return false;
 	}
 
 	void add_dirty(uint32_t addr, uint32_t bytes)
@@ -369,27 +430,60 @@ struct rdp_cp
 			return sticky_error;
 		}
 
-		bool render = fb.width != 0 && fb.deduced_height != 0 && !prims.empty();
 		rdpx::PassView v = {};
-		RdpPass &pass = v.pass;
-		pass.rdram = d_rdram;
-		pass.hidden = d_hidden;
-		pass.tmem_snapshots = uploads.empty() ? d_tmem : d_snapshots;
-		pass.tmem_state = d_tmem;
-		pass.rdram_size = rdram_size;
-		pass.hidden_size = hidden_size;
-		pass.fb_addr = fb.addr;
-		pass.depth_addr = fb.depth_addr;
-		pass.fb_width = fb.width;
-		pass.fb_height = std::min<uint32_t>(fb.deduced_height, RDP_MAX_TILES_Y * 8);
-		pass.fb_fmt = fb.fmt;
-		pass.tiles_x = render ? (fb.width + 7) / 8 : 0;
-		pass.tiles_y = render ? (pass.fb_height + 7) / 8 : 0;
-		pass.base_prim_index = uint32_t(base_prim_index);
-		pass.counters = d_fragments;
-		// A pass that does not render keeps its TMEM uploads but no primitives.
-		v.prims = prims.data();
-		v.num_prims = render ? uint32_t(prims.size()) : 0;
+		RdpPass common = {};
+		common.rdram = d_rdram;
+		common.hidden = d_hidden;
+		common.tmem_snapshots = uploads.empty() ? d_tmem : d_snapshots;
+		common.tmem_state = d_tmem;
+		common.rdram_size = rdram_size;
+		common.hidden_size = hidden_size;
+		common.base_prim_index = uint32_t(base_prim_index);
+		common.counters = d_fragments;
+		// One descriptor per target; a target that does not render (no colour image, or no
+		// covered line) keeps no primitives.  A pass without targets still applies its uploads.
+		bool single_in_order = targets.size() == 1;
+		if (targets.empty())
+		{
+			v.target[0] = common;
+			v.target_prims[0] = 0;
+			v.num_targets = 1;
+		}
+		for (size_t t = 0; t < targets.size(); t++)
+		{
+			const Target &tg = targets[t];
+			bool render = tg.width != 0 && tg.deduced_height != 0 && !tg.prim_ids.empty();
+			RdpPass d = common;
+			d.fb_addr = tg.addr;
+			d.depth_addr = tg.depth_addr;
+			d.fb_width = tg.width;
+			d.fb_height = std::min<uint32_t>(tg.deduced_height, RDP_MAX_TILES_Y * 8);
+			d.fb_fmt = tg.fmt;
+			d.tiles_x = render ? (tg.width + 7) / 8 : 0;
+			d.tiles_y = render ? (d.fb_height + 7) / 8 : 0;
+			v.target[t] = d;
+			v.target_prims[t] = render ? uint32_t(tg.prim_ids.size()) : 0;
+			if (!render) single_in_order = false;
+			if (render)
+			{
+				add_dirty(tg.addr, tg.width * tg.deduced_height * bytes_per_pixel(tg.fmt));
+				if (tg.depth_pending) add_dirty(tg.depth_addr, tg.width * tg.deduced_height * 2);
+			}
+		}
+		if (!targets.empty()) v.num_targets = uint32_t(targets.size());
+		// Primitives grouped by target (command order within a target).
+		if (single_in_order)
+			v.prims = prims.data();
+		else
+		{
+			grouped.clear();
+			for (size_t t = 0; t < targets.size(); t++)
+				if (v.target_prims[t])
+					for (uint32_t id : targets[t].prim_ids) grouped.push_back(prims[id]);
+			v.prims = grouped.data();
+		}
+		v.num_prims = 0;
+		for (uint32_t t = 0; t < v.num_targets; t++) v.num_prims += v.target_prims[t];
 		v.words = words.data();
 		v.num_words = uint32_t(words.size());
 		v.state_blocks = state_blocks.data();
@@ -402,8 +496,9 @@ struct rdp_cp
 		if (batch)
 		{
 			rdpx::PassPacket pk;
-			pk.pass = pass;
-			pk.prims.assign(prims.begin(), prims.begin() + v.num_prims);
+			pk.targets.assign(v.target, v.target + v.num_targets);
+			pk.target_prims.assign(v.target_prims, v.target_prims + v.num_targets);
+			pk.prims.assign(v.prims, v.prims + v.num_prims);
 			pk.words = words;
 			pk.state_blocks = state_blocks;
 			pk.tilesets = tilesets;
@@ -417,11 +512,6 @@ struct rdp_cp
 			stats.kernel_launches += exec->kernel_launches - before;
 		}
 
-		if (render)
-		{
-			add_dirty(fb.addr, fb.width * fb.deduced_height * fb_bytes_per_pixel());
-			if (fb.depth_pending) add_dirty(fb.depth_addr, fb.width * fb.deduced_height * 2);
-		}
 		stats.passes++;
 		stats.primitives += prims.size();
 		stats.tmem_uploads += uploads.size();
@@ -437,28 +527,87 @@ struct rdp_cp
 		state_blocks.clear();
 		tilesets.clear();
 		uploads.clear();
+		targets.clear();
 		sb_dirty = true;
 		tiles_dirty = true;
-		fb.deduced_height = 0;
-		fb.color_pending = false;
-		fb.depth_pending = false;
-		rsr_prims = rsr_uploads = 0;
 	}
 
 	// A flush the reference would also perform (framebuffer change, hazard, SyncFull).
 	int hard_flush()
 	{
 		if (ref.prims || ref.uploads) ref_pass_break();
+		rv = RefView{};
 		return flush();
 	}
 
 	// ================================================================= primitives
+	// The target of the pass that the current colour image draws into; a new target joins
+	// the pass unless the pass is full or its memory would overlap another target's.
+	size_t select_target(uint32_t rows, bool uses_depth)
+	{
+		for (;;)
+		{
+			size_t ti = targets.size();
+			for (size_t k = 0; k < targets.size(); k++)
+			{
+				const Target &t = targets[k];
+				if (t.addr == fb.addr && t.width == fb.width && t.fmt == fb.fmt && t.depth_addr == fb.depth_addr)
+				{
+					ti = k;
+					break;
+				}
+			}
+			if (ti == targets.size())
+			{
+				if (targets.size() >= rdpx::kMaxTargets)
+				{
+					flush();
+					continue;
+				}
+				Target t;
+				t.addr = fb.addr;
+				t.width = fb.width;
+				t.fmt = fb.fmt;
+				t.depth_addr = fb.depth_addr;
+				targets.push_back(std::move(t));
+			}
+			if (targets.size() > 1 && target_conflicts(ti, std::max(rows, targets[ti].deduced_height), uses_depth))
+			{
+				flush();
+				continue;
+			}
+			return ti;
+		}
+	}
+
 	void record_prim(const uint32_t *w, uint32_t len, uint32_t op)
 	{
 		if (prims.size() >= RDP_MAX_PRIMS_PER_PASS || words.size() + len > kMaxWordsPerPass ||
 		    (sb_dirty && state_blocks.size() / RDP_STATE_BLOCK_WORDS >= kMaxStateBlocks) ||
 		    (tiles_dirty && tilesets.size() / 8 >= kMaxTilesets))
 			flush();
+
+		// Rows the primitive reaches: the deduced framebuffer height (rdp_renderer.cpp:1556-1562).
+		int yl, yh;
+		bool fill_copy = cycle_type() >= 2;
+		if (op >= 0x08 && op <= 0x0f)
+		{
+			yl = sext(w[0], 14);
+			yh = sext(w[1], 14);
+		}
+		else
+		{
+			yl = int(w[0] & 0xfff);
+			if (fill_copy) yl |= 3;
+			yh = int(w[1] & 0xfff);
+		}
+		int scissor_ylo = int(sb[SB_SCISSOR] & 0xfff), scissor_yhi = int(sb[SB_SCISSOR + 1] & 0xfff);
+		int max_sub = std::min(yl - 1, scissor_yhi - 1);
+		uint32_t h = uint32_t(std::max((max_sub >> 2) + 1, 0));
+		uint32_t om1 = sb[SB_OTHER_MODES + 1];
+		bool writes_depth = (om1 & (1u << 5)) != 0;
+		bool uses_depth = !fill_copy && (om1 & ((1u << 4) | (1u << 5))) != 0; // fill / copy never touch depth
+		size_t ti = select_target(h, uses_depth);
 
 		if (sb_dirty)
 		{
@@ -475,37 +624,24 @@ struct rdp_cp
 		pi.state_block = uint32_t(state_blocks.size() / RDP_STATE_BLOCK_WORDS - 1);
 		pi.tileset = uint32_t(tilesets.size() / 8 - 1);
 		pi.tmem_index = uint16_t(uploads.size());
-		pi.pass = 0;
+		pi.seq = uint16_t(prims.size());
 		prims.push_back(pi);
 		words.insert(words.end(), w, w + len);
 
-		// Deduced framebuffer height (rdp_renderer.cpp:1556-1562).
-		int yl, yh;
-		bool fill_copy = cycle_type() >= 2;
-		if (op >= 0x08 && op <= 0x0f)
-		{
-			yl = sext(w[0], 14);
-			yh = sext(w[1], 14);
-		}
-		else
-		{
-			yl = int(w[0] & 0xfff);
-			if (fill_copy) yl |= 3;
-			yh = int(w[1] & 0xfff);
-		}
-		int scissor_ylo = int(sb[SB_SCISSOR] & 0xfff), scissor_yhi = int(sb[SB_SCISSOR + 1] & 0xfff);
-		int max_sub = std::min(yl - 1, scissor_yhi - 1);
-		int h = std::max((max_sub >> 2) + 1, 0);
-		fb.deduced_height = std::max<uint32_t>(fb.deduced_height, uint32_t(h));
-		fb.color_pending = true;
-		if (sb[SB_OTHER_MODES + 1] & (1u << 5)) fb.depth_pending = true;
+		Target &tg = targets[ti];
+		tg.prim_ids.push_back(uint32_t(prims.size() - 1));
+		tg.deduced_height = std::max(tg.deduced_height, h);
+		tg.color_pending = true;
+		tg.depth_pending |= writes_depth;
+		tg.depth_used |= uses_depth;
+		rv.deduced_height = std::max(rv.deduced_height, h);
+		rv.color_pending = true;
+		rv.depth_pending |= writes_depth;
 		int min_line = std::max(yh, scissor_ylo) >> 2;
 		ref_note_prim((max_sub >> 2) - min_line + 1);
-		bool cut = ++rsr_prims >= 256 && pass_boundaries_visible();
 
 		if (validation_cb)
 		{
-			uint32_t om1 = sb[SB_OTHER_MODES + 1];
 			bool prim_depth = (om1 & (1u << 2)) != 0;
 			if (cycle_type() == 3)
 			{
@@ -518,25 +654,40 @@ struct rdp_cp
 			else if (cycle_type() == 2 && fb.fmt == FBF_RGBA8888)
 				report(RDP_VALIDATION_COPY_32BPP, "Attempted to use Copy mode on 32bpp surface.");
 		}
-		if (cut) flush();
+		if (++rv.prims >= 256) rv_end();
 	}
 
 	// ================================================================= TMEM loads (rdp_renderer.cpp:3051-3486)
+	// Does a load from `addr` read pixels of an image with writes pending (tmem_upload_needs_flush)?
+	bool reads_pending(uint32_t addr, uint32_t img_addr, uint32_t width, uint32_t fmt, uint32_t depth_addr,
+	                   uint32_t rows, bool color_pending, bool depth_pending) const
+	{
+		if (color_pending)
+		{
+			uint32_t offset = (addr - img_addr) & (rdram_size - 1);
+			if (fmt == FBF_RGBA5551 || fmt == FBF_I8) offset >>= 1;
+			else if (fmt == FBF_RGBA8888) offset >>= 2;
+			if (offset < rows * width) return true;
+		}
+		if (depth_pending)
+		{
+			uint32_t offset = ((addr - depth_addr) & (rdram_size - 1)) >> 1;
+			if (offset < rows * width) return true;
+		}
+		return false;
+	}
+	// The reference's hazard: its current image, writes since its own pass began.
 	bool upload_needs_flush(uint32_t addr) const
 	{
-		if (fb.color_pending)
-		{
-			uint32_t offset = (addr - fb.addr) & (rdram_size - 1);
-			uint32_t pixels = fb.deduced_height * fb.width;
-			if (fb.fmt == FBF_RGBA5551 || fb.fmt == FBF_I8) offset >>= 1;
-			else if (fb.fmt == FBF_RGBA8888) offset >>= 2;
-			if (offset < pixels) return true;
-		}
-		if (fb.depth_pending)
-		{
-			uint32_t offset = ((addr - fb.depth_addr) & (rdram_size - 1)) >> 1;
-			if (offset < fb.deduced_height * fb.width) return true;
-		}
+		return reads_pending(addr, fb.addr, fb.width, fb.fmt, fb.depth_addr, rv.deduced_height, rv.color_pending,
+		                     rv.depth_pending);
+	}
+	// This processor's hazard: writes of any target of its (longer) pass.
+	bool upload_reads_pass(uint32_t addr) const
+	{
+		for (const Target &t : targets)
+			if (reads_pending(addr, t.addr, t.width, t.fmt, t.depth_addr, t.deduced_height, t.color_pending, t.depth_pending))
+				return true;
 		return false;
 	}
 
@@ -545,6 +696,7 @@ struct rdp_cp
 		if (mode == 1 && (thi >> 2) > (tlo >> 2))
 			report(RDP_VALIDATION_MULTILINE_TLUT, "Attempting to load multiple lines in TLUT.");
 		if (upload_needs_flush(tex_image.addr)) hard_flush();
+		else if (upload_reads_pass(tex_image.addr)) flush();
 		if (mode != 2)
 		{
 			if ((thi >> 2) < (tlo >> 2)) return;
@@ -700,8 +852,8 @@ struct rdp_cp
 		uploads.push_back(up);
 		ref.uploads++;
 		if (ref.uploads + 1 >= 256) ref_pass_break();
-		if (uploads.size() + 1 >= RDP_MAX_UPLOADS_PER_PASS || (++rsr_uploads + 1 >= 256 && pass_boundaries_visible()))
-			flush();
+		if (++rv.uploads + 1 >= 256) rv_end();
+		if (uploads.size() + 1 >= RDP_MAX_UPLOADS_PER_PASS) flush();
 	}
 
 	// ================================================================= command dispatch
@@ -796,7 +948,18 @@ struct rdp_cp
 			uint32_t f = (w[0] >> 21) & 7, size = (w[0] >> 19) & 3;
 			uint32_t width = (w[0] & 1023) + 1, addr = w[1] & 0xffffff;
 			uint32_t fmt = size == 0 ? FBF_I4 : size == 1 ? FBF_I8 : size == 2 ? (f ? FBF_IA88 : FBF_RGBA5551) : FBF_RGBA8888;
-			if (addr != fb.addr || width != fb.width || fmt != fb.fmt) hard_flush();
+			if (addr != fb.addr || width != fb.width || fmt != fb.fmt)
+			{
+				// The reference ends its pass here.  This processor keeps the pass open (the new
+				// image becomes another target) unless either image has visible pass boundaries.
+				if (!pass_boundaries_visible() && !boundaries_visible(fmt, addr, fb.depth_addr))
+				{
+					if (ref.prims || ref.uploads) ref_pass_break();
+					rv = RefView{};
+				}
+				else
+					hard_flush();
+			}
 			fb.addr = addr;
 			fb.width = width;
 			fb.fmt = fmt;
@@ -1324,7 +1487,8 @@ bool rdp_batch::reserve_for_capture()
 			{
 				views.push_back(cp->deferred[r].view());
 				prims += views.back().num_prims;
-				tiles += views.back().pass.tiles_x * views.back().pass.tiles_y;
+				for (uint32_t t = 0; t < views.back().num_targets; t++)
+					tiles += views.back().target[t].tiles_x * views.back().target[t].tiles_y;
 			}
 		need.passes = std::max(need.passes, uint32_t(views.size()));
 		need.prims = std::max(need.prims, prims);

@@ -25,11 +25,19 @@ namespace rdpx {
 
 static inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
 
-// One recorded pass, as plain pointers into the recorder's buffers.  The pass
-// descriptor carries the instance's pointers; the executor fills in the bases.
+constexpr uint32_t kMaxTargets = 8;
+
+// One recorded pass of an instance, as plain pointers into the recorder's buffers.
+// A pass may draw into several colour images ("targets") whose memory does not
+// overlap; each target becomes one RdpPass of the launch.  Its primitives are grouped
+// by target: target t owns prims [sum(target_prims[<t]), +target_prims[t]).  The
+// descriptors carry the instance's pointers; the executor fills in the bases.  The
+// pass's TMEM uploads are applied by the first descriptor.
 struct PassView
 {
-	RdpPass pass;
+	RdpPass target[kMaxTargets];
+	uint32_t target_prims[kMaxTargets];
+	uint32_t num_targets;
 	const RdpPrimIn *prims;
 	uint32_t num_prims;
 	const uint32_t *words;
@@ -45,7 +53,8 @@ struct PassView
 // An owned copy of a recorded pass (batched instances defer their passes).
 struct PassPacket
 {
-	RdpPass pass;
+	std::vector<RdpPass> targets;
+	std::vector<uint32_t> target_prims;
 	std::vector<RdpPrimIn> prims;
 	std::vector<uint32_t> words, state_blocks;
 	std::vector<RdpTile> tilesets;
@@ -54,7 +63,12 @@ struct PassPacket
 	PassView view() const
 	{
 		PassView v;
-		v.pass = pass;
+		v.num_targets = uint32_t(targets.size());
+		for (uint32_t t = 0; t < v.num_targets; t++)
+		{
+			v.target[t] = targets[t];
+			v.target_prims[t] = target_prims[t];
+		}
 		v.prims = prims.data();
 		v.num_prims = uint32_t(prims.size());
 		v.words = words.data();
@@ -71,7 +85,7 @@ struct PassPacket
 
 struct ExecCaps
 {
-	uint32_t passes = 0, prims = 0, tile_items = 0, pairs = 0;
+	uint32_t passes = 0, descs = 0, prims = 0, tile_items = 0, pairs = 0;
 	size_t staging = 0;
 };
 
@@ -274,7 +288,7 @@ struct Executor
 
 	static size_t staging_bytes_for(const PassView *v, uint32_t n)
 	{
-		size_t b = align16(sizeof(RdpPass) * n) + align16(4 * n) + 256;
+		size_t b = align16(sizeof(RdpPass) * kMaxTargets * n) + align16(4 * n) + 256;
 		for (uint32_t i = 0; i < n; i++)
 			b += align16(sizeof(RdpPrimIn) * v[i].num_prims) + align16(4 * v[i].num_words) +
 			     align16(4 * RDP_STATE_BLOCK_WORDS * v[i].num_state_blocks) + align16(sizeof(RdpTile) * 8 * v[i].num_tilesets) +
@@ -288,13 +302,15 @@ struct Executor
 	{
 		if (!n || failed) return !failed;
 		ExecCaps need = caps;
-		uint32_t prims = 0, tiles = 0;
+		uint32_t prims = 0, tiles = 0, descs = 0;
 		for (uint32_t i = 0; i < n; i++)
 		{
 			prims += v[i].num_prims;
-			tiles += v[i].pass.tiles_x * v[i].pass.tiles_y;
+			descs += v[i].num_targets;
+			for (uint32_t t = 0; t < v[i].num_targets; t++) tiles += v[i].target[t].tiles_x * v[i].target[t].tiles_y;
 		}
 		need.passes = std::max(need.passes, n);
+		need.descs = std::max(need.descs, descs);
 		need.prims = std::max(need.prims, std::max(prims, 1u));
 		need.tile_items = std::max(need.tile_items, std::max(tiles, 1u));
 		need.pairs = std::max(need.pairs, 1u << 20);
@@ -315,7 +331,9 @@ struct Executor
 			off = align16(off + bytes);
 			return at;
 		};
-		size_t o_pass = reserve(sizeof(RdpPass) * n);
+		uint32_t num_descs = 0;
+		for (uint32_t i = 0; i < n; i++) num_descs += v[i].num_targets;
+		size_t o_pass = reserve(sizeof(RdpPass) * num_descs);
 		size_t o_list = reserve(4 * n);
 		RdpPass *passes = reinterpret_cast<RdpPass *>(h + o_pass);
 		uint32_t *tmem_list = reinterpret_cast<uint32_t *>(h + o_list);
@@ -362,30 +380,34 @@ struct Executor
 			cursor += sizeof(RdpUpload) * v[i].num_uploads;
 		}
 		off = align16(cursor) + 16;
+		uint32_t d = 0;
 		for (uint32_t i = 0; i < n; i++)
 		{
-			RdpPass p = v[i].pass;
-			p.prim_begin = prim_base;
-			p.prim_count = v[i].num_prims;
-			p.word_base = word_base;
-			p.sb_base = sb_base;
-			p.ts_base = ts_base;
-			p.upload_begin = up_base;
-			p.upload_count = v[i].num_uploads;
-			p.tile_item_begin = tile_base;
-			p.masks = d_masks + size_t(tile_base) * RDP_MASK_WORDS_PER_TILE;
-			passes[i] = p;
-			if (v[i].num_uploads)
+			for (uint32_t t = 0; t < v[i].num_targets; t++, d++)
 			{
-				tmem_list[num_tmem++] = i;
-				max_uploads = std::max(max_uploads, v[i].num_uploads);
+				RdpPass p = v[i].target[t];
+				p.prim_begin = prim_base;
+				p.prim_count = v[i].target_prims[t];
+				p.word_base = word_base;
+				p.sb_base = sb_base;
+				p.ts_base = ts_base;
+				p.upload_begin = up_base;
+				p.upload_count = t == 0 ? v[i].num_uploads : 0;
+				p.tile_item_begin = tile_base;
+				p.masks = d_masks + size_t(tile_base) * RDP_MASK_WORDS_PER_TILE;
+				passes[d] = p;
+				if (t == 0 && v[i].num_uploads)
+				{
+					tmem_list[num_tmem++] = d;
+					max_uploads = std::max(max_uploads, v[i].num_uploads);
+				}
+				prim_base += p.prim_count;
+				tile_base += p.tiles_x * p.tiles_y;
 			}
-			prim_base += v[i].num_prims;
 			word_base += v[i].num_words;
 			sb_base += v[i].num_state_blocks;
 			ts_base += v[i].num_tilesets;
 			up_base += v[i].num_uploads;
-			tile_base += p.tiles_x * p.tiles_y;
 		}
 
 		uint8_t *dst = d_staging;
@@ -409,7 +431,7 @@ struct Executor
 		L.words = reinterpret_cast<const uint32_t *>(dst + o_words);
 		L.state_blocks = reinterpret_cast<const uint32_t *>(dst + o_sb);
 		L.passes = reinterpret_cast<const RdpPass *>(dst + o_pass);
-		L.num_passes = n;
+		L.num_passes = num_descs;
 		L.geom = d_geom;
 		L.attr = d_attr;
 		L.shade = d_shade;

@@ -480,7 +480,7 @@ __global__ void k_prim_setup(const RdpPrimIn *__restrict__ in, uint32_t num_prim
 	sh.z_mode = (om1 >> 10) & 3;
 	sh.tmem_index = pi.tmem_index;
 	sh.tileset = pass.ts_base + pi.tileset;
-	sh.prim_index = pass.base_prim_index + (i - pass.prim_begin);
+	sh.prim_index = pass.base_prim_index + pi.seq;
 	sh.pass = pass_index;
 	sh.pad[0] = sh.pad[1] = sh.pad[2] = 0;
 

@@ -149,7 +149,7 @@ typedef struct RdpPrimIn
 	uint32_t state_block;  /* index of the raw state-register block */
 	uint32_t tileset;      /* index of the 8-tile descriptor set */
 	uint16_t tmem_index;   /* TMEM snapshot the primitive samples (uploads before it in its pass) */
-	uint16_t pass;         /* pass index within the launch */
+	uint16_t seq;          /* position of the primitive in its instance's pass, in command order */
 } RdpPrimIn;
 
 /* Per-primitive device records produced by k_prim_setup. */

@@ -208,6 +208,12 @@ def run_ours_textured(args):
     # ---------------- value: device-resident graph replay
     rd = rdram.copy()
     cp = CommandProcessor(rd, device=local)
+    from rdp_gb300 import get_shade_variant
+    for _ in range(16):  # the autotuner times the shading-kernel variants on the first frames
+        if get_shade_variant(local) >= 0:
+            break
+        cp.enqueue_command(words)
+        cp.idle()
     graph = cp.capture(words)
     for _ in range(args.warmup):
         flush()
@@ -415,6 +421,12 @@ def run_ours_batched(args):
     _run_batch_step(b, insts, streams)
     s1 = [cp.stats() for cp in insts]
     b.idle()  # grows the pair scratch to what the sync point needed
+    from rdp_gb300 import get_shade_variant
+    for _ in range(8):  # the autotuner times the shading-kernel variants on the first sync points
+        if get_shade_variant(local) >= 0:
+            break
+        _run_batch_step(b, insts, streams)
+        b.idle()
     passes_per_step = sum(x["reference_passes"] - y["reference_passes"] for x, y in zip(s1, s0))
     frags_per_step = sum(x["fragments"] - y["fragments"] for x, y in zip(s1, s0))
     pairs_per_step = sum(x["tile_instances"] - y["tile_instances"] for x, y in zip(s1, s0))
@@ -509,7 +521,8 @@ def run_ours_batched(args):
                    "reference_passes_per_step": passes_per_step, "fragments_per_step": frags_per_step,
                    "tile_instances_per_step": pairs_per_step, "rounds_per_step": rounds_per_step,
                    "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "flushed between timed iterations", "tile_order": "static"},
+                   "l2": "flushed between timed iterations", "tile_order": "static",
+                   "shade_variant": get_shade_variant(local)},
         "mpix_per_s": total_frags / t_value / 1e6,
         "frames_per_s": world * args.steps * args.instances / t_value,
         "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": t_plain * 1e3 / args.steps,

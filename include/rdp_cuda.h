@@ -220,6 +220,16 @@ int rdp_batch_get_stats(rdp_batch *b, rdp_batch_stats *out);
 int rdp_batch_capture_begin(rdp_batch *b);
 int rdp_batch_capture_end(rdp_batch *b, rdp_graph **out);
 
+/* Kernel specialisation.  No counterpart in the reference (its shaders are specialised per
+ * render-state variant by its pipeline compiler).  The shading kernel is compiled for
+ * RDP_SHADE_VARIANTS register budgets; by default an autotuner times them on the first
+ * launches of a device and keeps the fastest per shaded (primitive, tile) pair.  All
+ * variants give identical results.  rdp_set_shade_variant forces one (0..3) or restarts
+ * tuning (-1); rdp_get_shade_variant returns the device's choice, -1 while tuning. */
+#define RDP_SHADE_VARIANTS 4
+int rdp_set_shade_variant(int device, int variant);
+int rdp_get_shade_variant(int device);
+
 /* ---------------------------------------------------------------------------------------------
  * Allocation-free TMEM update.  No counterpart in the reference: it exists for callers that must
  * not allocate device memory -- for example an emulator frame loop that runs inside a CUDA stream

@@ -94,6 +94,14 @@ static cudaError_t ensure_luts(int device)
 
 } // namespace
 
+namespace rdpx {
+int &shade_variant_choice(int device)
+{
+	static std::vector<int> choice(64, -1);
+	return choice[device >= 0 && device < 64 ? device : 0];
+}
+} // namespace rdpx
+
 struct rdp_batch;
 
 struct rdp_cp
@@ -1413,7 +1421,9 @@ struct rdp_cp
 		uint64_t v = 0;
 		int r = signal_timeline(&v);
 		if (r != RDP_OK) return r;
-		return wait_timeline(v, UINT64_MAX / 2);
+		r = wait_timeline(v, UINT64_MAX / 2);
+		if (r == RDP_OK && !batch) own_exec.tune_collect();
+		return r;
 	}
 };
 
@@ -1437,6 +1447,7 @@ struct rdp_batch
 	int submit()
 	{
 		if (sticky_error != RDP_OK) return sticky_error;
+		exec.tune_collect();
 		std::vector<rdpx::PassView> views;
 		std::vector<rdp_cp *> owners;
 		views.reserve(instances.size());
@@ -1923,6 +1934,7 @@ int rdp_batch_idle(rdp_batch *b)
 		if ((r = cp->signal_timeline(&v)) != RDP_OK || (r = cp->wait_timeline(v, UINT64_MAX / 2)) != RDP_OK) return r;
 	}
 	if (!b->capturing && !b->exec.adapt_pairs()) return b->sticky_error = RDP_ERR_DEVICE;
+	b->exec.tune_collect();
 	return RDP_OK;
 }
 
@@ -1954,6 +1966,19 @@ int rdp_batch_capture_end(rdp_batch *b, rdp_graph **out)
 	b->capturing = false;
 	if (r != RDP_OK) return r;
 	return build_graph(&b->exec, b->sink, nullptr, out);
+}
+
+int rdp_set_shade_variant(int device, int variant)
+{
+	if (device < 0 || device >= 64 || variant < -1 || variant >= RDP_SHADE_VARIANTS) return RDP_ERR_INVALID;
+	rdpx::shade_variant_choice(device) = variant;
+	return RDP_OK;
+}
+
+int rdp_get_shade_variant(int device)
+{
+	if (device < 0 || device >= 64) return -1;
+	return rdpx::shade_variant_choice(device);
 }
 
 } // extern "C"

@@ -96,6 +96,58 @@ struct CaptureSink
 	std::vector<void *> buffers;
 };
 
+// Process-wide choice of the k_shade variant per device: -1 until tuned (or forced).
+int &shade_variant_choice(int device);
+
+// Autotuner of the shading kernel: while active, launches that rasterise rotate through
+// the compiled k_shade variants; each launch's k_shade time (CUDA events on the stream)
+// and pair count (written by k_scan to a ring) are collected at sync points, and once
+// every variant has kTuneSamples launches of at least kTuneMinPairs pairs, the variant
+// with the least time per pair is kept for the device.  The variants compute identical
+// results, so tuning never changes output.
+struct ShadeTuner
+{
+	static constexpr int kTuneSamples = 3;
+	static constexpr uint32_t kTuneMinPairs = 20000;
+	bool active = false;
+	int next = 0;
+	uint64_t samples_taken = 0;
+	struct Sample
+	{
+		int variant;
+		cudaEvent_t ev[2];
+		uint32_t slot;
+	};
+	std::vector<Sample> pending;
+	std::vector<cudaEvent_t> pool;
+	double ms[RDP_SHADE_VARIANTS] = {}, pairs[RDP_SHADE_VARIANTS] = {};
+	int count[RDP_SHADE_VARIANTS] = {};
+
+	cudaEvent_t event()
+	{
+		if (!pool.empty())
+		{
+			cudaEvent_t e = pool.back();
+			pool.pop_back();
+			return e;
+		}
+		cudaEvent_t e = nullptr;
+		cudaEventCreate(&e);
+		return e;
+	}
+	void destroy()
+	{
+		for (auto &sm : pending)
+		{
+			cudaEventDestroy(sm.ev[0]);
+			cudaEventDestroy(sm.ev[1]);
+		}
+		for (auto e : pool) cudaEventDestroy(e);
+		pending.clear();
+		pool.clear();
+	}
+};
+
 struct Executor
 {
 	int device = 0;
@@ -103,15 +155,17 @@ struct Executor
 	ExecCaps caps;
 	uint64_t generation = 0;
 	uint64_t kernel_launches = 0, staging_bytes = 0, launches = 0;
-	uint32_t shade_ctas = 0;
+	uint32_t shade_ctas_v[RDP_SHADE_VARIANTS] = {}, blend_ctas = 0;
 	bool failed = false;
+	ShadeTuner tuner;
+	uint32_t *d_pair_log = nullptr; // [256]
 
 	RdpPrimGeom *d_geom = nullptr;
 	RdpPrimAttr *d_attr = nullptr;
 	RdpPrimShade *d_shade = nullptr;
 	uint32_t *d_masks = nullptr, *d_tmem_keep = nullptr;
 	uint32_t *d_tile_counts = nullptr, *d_pair_offsets = nullptr, *d_ctrl = nullptr;
-	uint32_t *d_tile_order = nullptr, *d_tile_cycles = nullptr;
+	uint32_t *d_tile_order = nullptr, *d_tile_cycles = nullptr, *d_nonempty = nullptr;
 	uint2 *d_pairs = nullptr;
 	uint32_t *d_sc_color = nullptr;
 	int *d_sc_zdith = nullptr;
@@ -140,11 +194,69 @@ struct Executor
 		stream = s;
 		int sms = 0;
 		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-		shade_ctas = uint32_t(std::max(sms, 1)) * uint32_t(rdp_kernels_shade_ctas_per_sm());
+		sms = std::max(sms, 1);
+		for (int v = 0; v < RDP_SHADE_VARIANTS; v++) shade_ctas_v[v] = uint32_t(sms) * uint32_t(rdp_kernels_shade_ctas_per_sm(v));
+		blend_ctas = uint32_t(sms) * uint32_t(rdp_kernels_blend_ctas_per_sm());
+		tuner.active = shade_variant_choice(device) < 0;
 		for (auto &st : staging)
 			if (check(cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming))) return false;
-		if (check(cudaMalloc(&d_ctrl, 16))) return false;
-		return !check(cudaMemsetAsync(d_ctrl, 0, 16, stream));
+		if (check(cudaMalloc(&d_ctrl, 32)) || check(cudaMalloc(&d_pair_log, 256 * 4))) return false;
+		return !check(cudaMemsetAsync(d_ctrl, 0, 32, stream));
+	}
+
+	int current_variant()
+	{
+		int v = shade_variant_choice(device);
+		return v >= 0 && v < RDP_SHADE_VARIANTS ? v : 0;
+	}
+
+	// At a sync point: folds finished tuning samples in; decides when enough are in.
+	void tune_collect()
+	{
+		if (tuner.pending.empty()) return;
+		uint32_t log[256];
+		if (cudaMemcpy(log, d_pair_log, sizeof(log), cudaMemcpyDeviceToHost) != cudaSuccess)
+		{
+			cudaGetLastError();
+			return;
+		}
+		std::vector<ShadeTuner::Sample> keep;
+		for (auto &sm : tuner.pending)
+		{
+			float ms = 0.0f;
+			cudaError_t q = cudaEventQuery(sm.ev[1]);
+			if (q == cudaErrorNotReady)
+			{
+				keep.push_back(sm);
+				continue;
+			}
+			if (q == cudaSuccess && cudaEventElapsedTime(&ms, sm.ev[0], sm.ev[1]) == cudaSuccess &&
+			    log[sm.slot] >= ShadeTuner::kTuneMinPairs)
+			{
+				tuner.ms[sm.variant] += ms;
+				tuner.pairs[sm.variant] += log[sm.slot];
+				tuner.count[sm.variant]++;
+			}
+			cudaGetLastError();
+			tuner.pool.push_back(sm.ev[0]);
+			tuner.pool.push_back(sm.ev[1]);
+		}
+		tuner.pending.swap(keep);
+		if (!tuner.active) return;
+		int best = -1;
+		double best_rate = 0.0;
+		for (int v = 0; v < RDP_SHADE_VARIANTS; v++)
+		{
+			if (tuner.count[v] < ShadeTuner::kTuneSamples) return;
+			double rate = tuner.ms[v] / tuner.pairs[v];
+			if (best < 0 || rate < best_rate)
+			{
+				best = v;
+				best_rate = rate;
+			}
+		}
+		tuner.active = false;
+		if (shade_variant_choice(device) < 0) shade_variant_choice(device) = best;
 	}
 
 	void free_all()
@@ -158,6 +270,7 @@ struct Executor
 		cudaFree(d_pair_offsets);
 		cudaFree(d_tile_order);
 		cudaFree(d_tile_cycles);
+		cudaFree(d_nonempty);
 		cudaFree(d_pairs);
 		cudaFree(d_sc_color);
 		cudaFree(d_sc_zdith);
@@ -166,7 +279,7 @@ struct Executor
 		d_geom = nullptr;
 		d_attr = nullptr;
 		d_shade = nullptr;
-		d_masks = d_tmem_keep = d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = nullptr;
+		d_masks = d_tmem_keep = d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = d_nonempty = nullptr;
 		d_pairs = nullptr;
 		d_sc_color = nullptr;
 		d_sc_zdith = nullptr;
@@ -179,7 +292,10 @@ struct Executor
 		if (stream) cudaStreamSynchronize(stream);
 		free_all();
 		cudaFree(d_ctrl);
+		cudaFree(d_pair_log);
 		d_ctrl = nullptr;
+		d_pair_log = nullptr;
+		tuner.destroy();
 		for (auto &st : staging)
 		{
 			if (st.h) cudaFreeHost(st.h);
@@ -220,10 +336,12 @@ struct Executor
 			cudaFree(d_pair_offsets);
 			cudaFree(d_tile_order);
 			cudaFree(d_tile_cycles);
-			d_masks = d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = nullptr;
+			cudaFree(d_nonempty);
+			d_masks = d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = d_nonempty = nullptr;
 			if (check(cudaMalloc(&d_masks, size_t(n) * RDP_MASK_WORDS_PER_TILE * 4)) ||
 			    check(cudaMalloc(&d_tile_counts, size_t(n + 1) * 4)) || check(cudaMalloc(&d_pair_offsets, size_t(n + 1) * 4)) ||
-			    check(cudaMalloc(&d_tile_order, size_t(n) * 4)) || check(cudaMalloc(&d_tile_cycles, size_t(n) * 4)))
+			    check(cudaMalloc(&d_tile_order, size_t(n) * 4)) || check(cudaMalloc(&d_tile_cycles, size_t(n) * 4)) ||
+			    check(cudaMalloc(&d_nonempty, size_t(n) * 4)))
 				return false;
 			// Bitmasks and counts are self-clearing between launches; they start at zero.
 			if (check(cudaMemsetAsync(d_masks, 0, size_t(n) * RDP_MASK_WORDS_PER_TILE * 4, stream)) ||
@@ -442,11 +560,24 @@ struct Executor
 		L.max_uploads = max_uploads;
 		L.tmem_keep = d_tmem_keep;
 		L.tile_counts = d_tile_counts;
+		L.nonempty_tiles = d_nonempty;
 		L.pair_offsets = d_pair_offsets;
 		L.pairs = d_pairs;
 		L.ctrl = d_ctrl;
 		L.pair_capacity = caps.pairs;
-		L.shade_ctas = shade_ctas;
+		int variant = current_variant();
+		bool sample = false;
+		if (tuner.active && shade_variant_choice(device) < 0 && !cap && tile_base && tuner.pending.size() < 64)
+		{
+			variant = tuner.next;
+			tuner.next = (tuner.next + 1) % RDP_SHADE_VARIANTS;
+			sample = true;
+		}
+		L.shade_variant = uint32_t(variant);
+		L.shade_ctas = shade_ctas_v[variant];
+		L.blend_ctas = blend_ctas;
+		L.pair_log = sample ? d_pair_log : nullptr;
+		L.log_slot = sample ? uint32_t(tuner.samples_taken++ % 256) : 0u;
 		L.sc_color = d_sc_color;
 		L.sc_zdith = d_sc_zdith;
 		L.sc_misc = d_sc_misc;
@@ -460,6 +591,17 @@ struct Executor
 				if (check(cudaEventCreate(&e))) return false;
 			cap->launches.push_back(L);
 			return true;
+		}
+		if (sample)
+		{
+			ShadeTuner::Sample sm;
+			sm.variant = variant;
+			sm.ev[0] = tuner.event();
+			sm.ev[1] = tuner.event();
+			sm.slot = L.log_slot;
+			L.shade_events[0] = sm.ev[0];
+			L.shade_events[1] = sm.ev[1];
+			tuner.pending.push_back(sm);
 		}
 		if (check(rdp_kernels_launch(&L, stream))) return false;
 		kernel_launches += rdp_kernels_count(&L);

@@ -22,6 +22,7 @@
  * (unsigned multiplies/shifts) so that it matches 32-bit GLSL semantics.
  */
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <stdint.h>
 #include "rdp_types.h"
 #include "rdp_kernels.h"
@@ -915,28 +916,60 @@ __global__ void k_tmem_apply(const RdpPass *__restrict__ passes, const uint32_t 
 	}
 }
 
-// Phase 2: per TMEM word, carry the previous snapshot's value through uploads that did not
-// write it (tmem_update.comp:546-576: instance i+1 = instance i with upload i applied).
-__global__ void k_tmem_carry(const RdpPass *__restrict__ passes, const uint32_t *__restrict__ pass_list,
-                             const uint32_t *__restrict__ keep_bits)
+// Phase 2: carry the previous snapshot's value through uploads that did not write a word
+// (tmem_update.comp:546-576: instance i+1 = instance i with upload i applied).  One CTA per
+// (pass, 32 TMEM words); its TMEM_CARRY_WARPS warps split the uploads into chunks: each
+// warp finds the last value its chunk writes, the chunks' carry-ins are chained in shared
+// memory, then every warp fills its chunk -- 2 * uploads / warps dependent steps per word.
+constexpr int TMEM_CARRY_WARPS = 16;
+
+__global__ void __launch_bounds__(TMEM_CARRY_WARPS * 32) k_tmem_carry(const RdpPass *__restrict__ passes,
+                                                                       const uint32_t *__restrict__ pass_list,
+                                                                       const uint32_t *__restrict__ keep_bits)
 {
+	__shared__ uint16_t s_last[TMEM_CARRY_WARPS][32];
+	__shared__ uint8_t s_has[TMEM_CARRY_WARPS][32];
+	__shared__ uint16_t s_in[TMEM_CARRY_WARPS][32];
 	const RdpPass &ps = passes[pass_list[blockIdx.y]];
-	int gid = blockIdx.x * blockDim.x + threadIdx.x;
-	if (gid >= 2048) return;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const int gid = blockIdx.x * 32 + lane;
+	const uint32_t n = ps.upload_count;
+	const uint32_t chunk = (n + TMEM_CARRY_WARPS - 1) / TMEM_CARRY_WARPS;
+	const uint32_t u0 = min(n, uint32_t(warp) * chunk), u1 = min(n, u0 + chunk);
 	uint16_t *snap = ps.tmem_snapshots;
-	uint16_t value = ps.tmem_state[gid];
-	snap[gid] = value;
-	const uint32_t *keep = keep_bits + size_t(blockIdx.y) * RDP_MAX_UPLOADS_PER_PASS * 64;
-#pragma unroll 8
-	for (uint32_t u = 0; u < ps.upload_count; u++)
+	const uint32_t *keep = keep_bits + size_t(blockIdx.y) * RDP_MAX_UPLOADS_PER_PASS * 64 + (gid >> 5);
+	const uint32_t bit = 1u << (gid & 31);
+
+	uint16_t last = 0;
+	bool has = false;
+	for (uint32_t u = u0; u < u1; u++)
+		if (!(keep[u * 64] & bit))
+		{
+			last = snap[size_t(u + 1) * 2048 + gid];
+			has = true;
+		}
+	s_last[warp][lane] = last;
+	s_has[warp][lane] = has;
+	__syncthreads();
+	if (warp == 0)
+	{
+		uint16_t v = ps.tmem_state[gid];
+		snap[gid] = v;
+		for (int w = 0; w < TMEM_CARRY_WARPS; w++)
+		{
+			s_in[w][lane] = v;
+			if (s_has[w][lane]) v = s_last[w][lane];
+		}
+		ps.tmem_state[gid] = v;
+	}
+	__syncthreads();
+	uint16_t value = s_in[warp][lane];
+	for (uint32_t u = u0; u < u1; u++)
 	{
 		size_t at = size_t(u + 1) * 2048 + gid;
-		uint16_t written = snap[at]; // independent of the carried value: loads overlap
-		bool keep_prev = (keep[u * 64 + (gid >> 5)] >> (gid & 31)) & 1u;
-		if (keep_prev) snap[at] = value;
-		value = keep_prev ? value : written;
+		if (keep[u * 64] & bit) snap[at] = value;
+		else value = snap[at];
 	}
-	ps.tmem_state[gid] = value;
 }
 
 // ============================================================================ k_raster: spans
@@ -2412,13 +2445,21 @@ __device__ __forceinline__ bool shade_and_blend(const RdpPass &ps, const PassCon
 // ============================================================================ pair list
 // Exclusive scan of the per-tile pair counts into offsets; counts are cleared for the next
 // launch.  ctrl[0] = total pairs, ctrl[1] = 1 when the pairs exceed the scratch capacity.
+// Single CTA: exclusive scan of the per-tile pair counts into pair offsets, the list of
+// non-empty tiles in tile order, and the launch's control words: [0] pairs, [1] overflow,
+// [2] largest pair count seen, [3] non-empty tiles, [4] k_blend work counter (reset).
 __global__ void __launch_bounds__(1024) k_scan(uint32_t num_items, uint32_t *__restrict__ counts,
-                                               uint32_t *__restrict__ offsets, uint32_t *__restrict__ ctrl,
-                                               uint32_t capacity)
+                                               uint32_t *__restrict__ offsets, uint32_t *__restrict__ nonempty,
+                                               uint32_t *__restrict__ ctrl, uint32_t capacity,
+                                               uint32_t *__restrict__ pair_log, uint32_t log_slot)
 {
-	__shared__ uint32_t warp_sums[32];
-	__shared__ uint32_t carry;
-	if (threadIdx.x == 0) carry = 0;
+	__shared__ uint32_t warp_sums[32], warp_nz[32];
+	__shared__ uint32_t carry, carry_nz;
+	if (threadIdx.x == 0)
+	{
+		carry = 0;
+		carry_nz = 0;
+	}
 	__syncthreads();
 	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 	for (uint32_t base = 0; base < num_items; base += 1024)
@@ -2433,24 +2474,41 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t num_items, uint32_t *__r
 			uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
 			if (lane >= o) x += y;
 		}
-		if (lane == 31) warp_sums[wid] = x;
+		unsigned nzmask = __ballot_sync(0xffffffffu, v != 0);
+		if (lane == 31)
+		{
+			warp_sums[wid] = x;
+			warp_nz[wid] = __popc(nzmask);
+		}
 		__syncthreads();
 		if (wid == 0)
 		{
-			uint32_t w = warp_sums[lane];
+			uint32_t w = warp_sums[lane], z = warp_nz[lane];
 #pragma unroll
 			for (int o = 1; o < 32; o <<= 1)
 			{
 				uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-				if (lane >= o) w += y;
+				uint32_t yz = __shfl_up_sync(0xffffffffu, z, o);
+				if (lane >= o)
+				{
+					w += y;
+					z += yz;
+				}
 			}
 			warp_sums[lane] = w;
+			warp_nz[lane] = z;
 		}
 		__syncthreads();
 		uint32_t prefix = carry + (wid ? warp_sums[wid - 1] : 0u) + x - v;
+		uint32_t nz_pos = carry_nz + (wid ? warp_nz[wid - 1] : 0u) + __popc(nzmask & ((1u << lane) - 1u));
 		if (i < num_items) offsets[i] = prefix;
+		if (v) nonempty[nz_pos] = i;
 		__syncthreads();
-		if (threadIdx.x == 1023) carry = prefix + v;
+		if (threadIdx.x == 1023)
+		{
+			carry = prefix + v;
+			carry_nz = nz_pos + (v ? 1u : 0u);
+		}
 		__syncthreads();
 	}
 	if (threadIdx.x == 0)
@@ -2459,6 +2517,9 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t num_items, uint32_t *__r
 		ctrl[0] = carry;
 		ctrl[1] = carry > capacity ? 1u : 0u;
 		ctrl[2] = max(ctrl[2], carry); // largest pair count seen: the host grows the scratch to it
+		ctrl[3] = carry_nz;
+		ctrl[4] = 0u;
+		if (pair_log) pair_log[log_slot] = carry; // per-launch pair count for the autotuner
 	}
 }
 
@@ -2510,7 +2571,10 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 // structure-of-arrays per pair: combined colour, z | dither, coverage | shade alpha << 8.
 constexpr int SHADE_THREADS = 64;
 
-__global__ void __launch_bounds__(SHADE_THREADS) k_shade(const RdpPass *__restrict__ passes, uint32_t num_passes,
+// Compiled for several minimum residencies (register budgets); the executor's autotuner
+// picks one.  More resident CTAs hide more latency at the price of some spilling.
+template <int MIN_CTAS>
+__global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass *__restrict__ passes, uint32_t num_passes,
                                                         const uint2 *__restrict__ pairs, const uint32_t *__restrict__ ctrl,
                                                         const RdpPrimGeom *__restrict__ geom,
                                                         const RdpPrimAttr *__restrict__ attr,
@@ -2576,19 +2640,12 @@ __global__ void __launch_bounds__(SHADE_THREADS) k_shade(const RdpPass *__restri
 // ============================================================================ k_blend
 // One 64-thread CTA per tile: the tile's colour/depth stay in registers while its pairs are
 // applied in primitive order (the reference's depth_blend.comp), then written back.
-__global__ void __launch_bounds__(SHADE_THREADS) k_blend(const RdpPass *__restrict__ passes, uint32_t num_passes,
-                                                        uint32_t num_items, const uint32_t *__restrict__ offsets,
-                                                        const uint2 *__restrict__ pairs, const uint32_t *__restrict__ ctrl,
-                                                        const RdpPrimShade *__restrict__ shade,
-                                                        const uint32_t *__restrict__ sc_color,
-                                                        const int *__restrict__ sc_zdith,
-                                                        const uint16_t *__restrict__ sc_misc,
-                                                        const uint32_t *__restrict__ order,
-                                                        uint32_t *__restrict__ cycles)
+__device__ __forceinline__ void blend_tile(uint32_t item, const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                           const uint32_t *__restrict__ offsets, const uint2 *__restrict__ pairs,
+                                           const RdpPrimShade *__restrict__ shade, const uint32_t *__restrict__ sc_color,
+                                           const int *__restrict__ sc_zdith, const uint16_t *__restrict__ sc_misc,
+                                           uint32_t *__restrict__ cycles)
 {
-	if (blockIdx.x >= num_items || ctrl[1]) return;
-	// CTAs start in blockIdx order: `order` puts the tiles expected to take longest first.
-	const uint32_t item = order ? order[blockIdx.x] : blockIdx.x;
 	const uint32_t p0 = offsets[item], p1 = offsets[item + 1];
 	if (p0 == p1)
 	{
@@ -2664,27 +2721,49 @@ __global__ void __launch_bounds__(SHADE_THREADS) k_blend(const RdpPass *__restri
 	}
 }
 
+// Persistent CTAs take non-empty tiles from a shared counter, in the order of `order`
+// (longest predicted first) when given, else in tile order.
+__global__ void __launch_bounds__(SHADE_THREADS) k_blend(const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                                        const uint32_t *__restrict__ offsets,
+                                                        const uint2 *__restrict__ pairs, uint32_t *__restrict__ ctrl,
+                                                        const uint32_t *__restrict__ nonempty,
+                                                        const RdpPrimShade *__restrict__ shade,
+                                                        const uint32_t *__restrict__ sc_color,
+                                                        const int *__restrict__ sc_zdith,
+                                                        const uint16_t *__restrict__ sc_misc,
+                                                        const uint32_t *__restrict__ order,
+                                                        uint32_t *__restrict__ cycles)
+{
+	__shared__ uint32_t s_next;
+	if (ctrl[1]) return;
+	const uint32_t n = ctrl[3];
+	for (;;)
+	{
+		if (threadIdx.x == 0) s_next = atomicAdd(&ctrl[4], 1u);
+		__syncthreads();
+		const uint32_t k = s_next;
+		__syncthreads();
+		if (k >= n) break;
+		const uint32_t item = order ? order[k] : nonempty[k];
+		blend_tile(item, passes, num_passes, offsets, pairs, shade, sc_color, sc_zdith, sc_misc, cycles);
+	}
+}
+
 // ============================================================================ k_raster
 // One CTA of 64 threads per 8x8 tile, one pixel per thread; warp w owns rows 4w..4w+3.
 // Both warps walk the tile's primitive bitmask in primitive order; pixel state stays in
 // registers for the whole pass (init_tile/finish_tile, memory_interfacing.h:286-362).
 constexpr int RASTER_THREADS = 64;
 
-__global__ void __launch_bounds__(RASTER_THREADS) k_raster(const RdpPass *__restrict__ passes, uint32_t num_passes,
-                                                          uint32_t num_items, const RdpPrimGeom *__restrict__ geom,
-                                                          const RdpPrimAttr *__restrict__ attr,
-                                                          const RdpPrimShade *__restrict__ shade,
-                                                          const RdpTile *__restrict__ tilesets,
-                                                          const uint32_t *__restrict__ ctrl)
+__device__ __forceinline__ void raster_tile(uint32_t item, const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                            const RdpPrimGeom *__restrict__ geom, const RdpPrimAttr *__restrict__ attr,
+                                            const RdpPrimShade *__restrict__ shade, const RdpTile *__restrict__ tilesets)
 {
 	__shared__ SpanA s_sa[2][5];
 	__shared__ SpanX s_sx[2][5];
 	__shared__ int s_any;
 	const int wib = threadIdx.x >> 5;
 	const int lane = threadIdx.x & 31;
-	const uint32_t item = blockIdx.x;
-	// Only runs when the pair list overflowed the scratch capacity (ctrl[1]).
-	if (item >= num_items || !ctrl[1]) return;
 
 	const uint32_t pi = pass_of_item(passes, num_passes, item);
 	const RdpPass &ps = passes[pi];
@@ -2797,6 +2876,23 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const RdpPass *__rest
 	}
 }
 
+// Fallback when the pair list overflowed the scratch capacity (ctrl[1]): persistent CTAs,
+// each shading and blending whole tiles; without overflow every CTA returns at once.
+__global__ void __launch_bounds__(RASTER_THREADS) k_raster(const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                                          uint32_t num_items, const RdpPrimGeom *__restrict__ geom,
+                                                          const RdpPrimAttr *__restrict__ attr,
+                                                          const RdpPrimShade *__restrict__ shade,
+                                                          const RdpTile *__restrict__ tilesets,
+                                                          const uint32_t *__restrict__ ctrl)
+{
+	if (!ctrl[1]) return;
+	for (uint32_t item = blockIdx.x; item < num_items; item += gridDim.x)
+	{
+		raster_tile(item, passes, num_passes, geom, attr, shade, tilesets);
+		__syncthreads();
+	}
+}
+
 } // namespace rdp
 
 // ============================================================================ host launchers
@@ -2805,10 +2901,26 @@ extern "C" cudaError_t rdp_kernels_init_luts(const uint8_t *blender_lut)
 	return cudaMemcpyToSymbol(rdp::g_blender_lut, blender_lut, 0x8000);
 }
 
-extern "C" int rdp_kernels_shade_ctas_per_sm(void)
+namespace {
+typedef void (*ShadeKernel)(const RdpPass *, uint32_t, const uint2 *, const uint32_t *, const RdpPrimGeom *,
+                            const RdpPrimAttr *, const RdpPrimShade *, const RdpTile *, uint32_t *, int *, uint16_t *);
+const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = { rdp::k_shade<1>, rdp::k_shade<12>, rdp::k_shade<16>,
+                                                         rdp::k_shade<24> };
+} // namespace
+
+extern "C" int rdp_kernels_blend_ctas_per_sm(void)
 {
 	int n = 0;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, rdp::k_shade, rdp::SHADE_THREADS, 0) != cudaSuccess) n = 8;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, rdp::k_blend, rdp::SHADE_THREADS, 0) != cudaSuccess) n = 8;
+	return n > 0 ? n : 1;
+}
+
+extern "C" int rdp_kernels_shade_ctas_per_sm(int variant)
+{
+	if (variant < 0 || variant >= RDP_SHADE_VARIANTS) variant = 0;
+	int n = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kShadeVariants[variant], rdp::SHADE_THREADS, 0) != cudaSuccess)
+		n = 8;
 	return n > 0 ? n : 1;
 }
 
@@ -2836,24 +2948,30 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 	{
 		rdp::k_tmem_apply<<<dim3(L->max_uploads, L->num_tmem_passes), 256, 0, stream>>>(L->passes, L->tmem_pass_list,
 		                                                                                 L->uploads, L->tmem_keep);
-		rdp::k_tmem_carry<<<dim3(2048 / 32, L->num_tmem_passes), 32, 0, stream>>>(L->passes, L->tmem_pass_list,
-		                                                                         L->tmem_keep);
+		rdp::k_tmem_carry<<<dim3(2048 / 32, L->num_tmem_passes), rdp::TMEM_CARRY_WARPS * 32, 0, stream>>>(
+			L->passes, L->tmem_pass_list, L->tmem_keep);
 	}
 	if (raster)
 	{
-		rdp::k_scan<<<1, 1024, 0, stream>>>(L->num_tile_items, L->tile_counts, L->pair_offsets, L->ctrl,
-		                                    L->pair_capacity);
+		rdp::k_scan<<<1, 1024, 0, stream>>>(L->num_tile_items, L->tile_counts, L->pair_offsets, L->nonempty_tiles,
+		                                    L->ctrl, L->pair_capacity, L->pair_log, L->log_slot);
 		rdp::k_expand<<<(L->num_tile_items * 32 + 255) / 256, 256, 0, stream>>>(
 			L->passes, L->num_passes, L->num_tile_items, L->pair_offsets, L->ctrl, L->pairs);
-		if (L->shade_events[0]) cudaEventRecordWithFlags(L->shade_events[0], stream, cudaEventRecordExternal);
-		rdp::k_shade<<<L->shade_ctas, rdp::SHADE_THREADS, 0, stream>>>(L->passes, L->num_passes, L->pairs, L->ctrl,
+		// Inside a stream capture the events become record nodes of the graph.
+		cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+		if (L->shade_events[0] && cudaStreamIsCapturing(stream, &capture) != cudaSuccess) return cudaGetLastError();
+		const unsigned ev_flags = capture == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
+		if (L->shade_events[0]) cudaEventRecordWithFlags(L->shade_events[0], stream, ev_flags);
+		const ShadeKernel shade_kernel = kShadeVariants[L->shade_variant < RDP_SHADE_VARIANTS ? L->shade_variant : 0];
+		shade_kernel<<<L->shade_ctas, rdp::SHADE_THREADS, 0, stream>>>(L->passes, L->num_passes, L->pairs, L->ctrl,
 		                                                               L->geom, L->attr, L->shade, L->tilesets,
 		                                                               L->sc_color, L->sc_zdith, L->sc_misc);
-		if (L->shade_events[1]) cudaEventRecordWithFlags(L->shade_events[1], stream, cudaEventRecordExternal);
-		rdp::k_blend<<<L->num_tile_items, rdp::SHADE_THREADS, 0, stream>>>(
-			L->passes, L->num_passes, L->num_tile_items, L->pair_offsets, L->pairs, L->ctrl, L->shade, L->sc_color,
+		if (L->shade_events[1]) cudaEventRecordWithFlags(L->shade_events[1], stream, ev_flags);
+		const uint32_t tile_ctas = std::min<uint32_t>(L->num_tile_items, L->blend_ctas);
+		rdp::k_blend<<<tile_ctas, rdp::SHADE_THREADS, 0, stream>>>(
+			L->passes, L->num_passes, L->pair_offsets, L->pairs, L->ctrl, L->nonempty_tiles, L->shade, L->sc_color,
 			L->sc_zdith, L->sc_misc, L->tile_order, L->tile_cycles);
-		rdp::k_raster<<<L->num_tile_items, rdp::RASTER_THREADS, 0, stream>>>(
+		rdp::k_raster<<<tile_ctas, rdp::RASTER_THREADS, 0, stream>>>(
 			L->passes, L->num_passes, L->num_tile_items, L->geom, L->attr, L->shade, L->tilesets, L->ctrl);
 	}
 	return cudaGetLastError();

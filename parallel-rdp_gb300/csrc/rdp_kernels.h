@@ -5,6 +5,11 @@
 #include <cuda_runtime.h>
 #include "rdp_types.h"
 
+/* k_shade is compiled for minimum residencies of 1, 12, 16 and 24 CTAs per SM. */
+#ifndef RDP_SHADE_VARIANTS
+#define RDP_SHADE_VARIANTS 4
+#endif
+
 typedef struct RdpLaunch
 {
 	const RdpPrimIn *prims_in;
@@ -28,11 +33,16 @@ typedef struct RdpLaunch
 	uint32_t *tile_cycles;          /* optional [num_tile_items]: measured k_blend cycles per tile */
 	/* pair list + shading scratch */
 	uint32_t *tile_counts;          /* [num_tile_items], zero between launches */
+	uint32_t *nonempty_tiles;       /* [num_tile_items]: tiles with pairs, in tile order (k_scan) */
 	uint32_t *pair_offsets;         /* [num_tile_items + 1] */
 	uint2 *pairs;                   /* [pair_capacity] (global primitive index, tile item) */
-	uint32_t *ctrl;                 /* [0] total pairs, [1] overflow */
+	uint32_t *ctrl;                 /* [0] pairs, [1] overflow, [2] max pairs, [3] non-empty tiles, [4] counter */
 	uint32_t pair_capacity;
-	uint32_t shade_ctas;
+	uint32_t shade_ctas;            /* persistent CTAs of k_shade (and of k_blend / k_raster) */
+	uint32_t shade_variant;         /* which compiled k_shade (register budget), < RDP_SHADE_VARIANTS */
+	uint32_t blend_ctas;            /* persistent CTAs of k_blend / k_raster */
+	uint32_t *pair_log;             /* optional: k_scan writes the launch's pair count to pair_log[log_slot] */
+	uint32_t log_slot;
 	uint32_t *sc_color;             /* [pair_capacity * 64] */
 	int *sc_zdith;
 	uint16_t *sc_misc;
@@ -44,7 +54,8 @@ extern "C" {
 cudaError_t rdp_kernels_init_luts(const uint8_t *blender_lut);
 cudaError_t rdp_kernels_launch(const RdpLaunch *launch, cudaStream_t stream);
 uint32_t rdp_kernels_count(const RdpLaunch *launch);
-int rdp_kernels_shade_ctas_per_sm(void);
+int rdp_kernels_shade_ctas_per_sm(int variant);
+int rdp_kernels_blend_ctas_per_sm(void);
 #ifdef __cplusplus
 }
 #endif

@@ -12,7 +12,10 @@ from .native import (  # noqa: F401
     RdpTimeout,
     ScanoutOptions,
     VIRegister,
+    SHADE_VARIANTS,
     device_is_supported,
+    get_shade_variant,
+    set_shade_variant,
     library_path,
 )
 from .cmdgen import GenParams, generate_stream, CONFIG_PLAIN, CONFIG_TEXTURED, CONFIG_MIXED  # noqa: F401

@@ -92,7 +92,8 @@ EXPORTED_SYMBOLS = [
     "rdp_cp_begin_vi_register_per_scanline", "rdp_cp_set_vi_register_for_scanline",
     "rdp_cp_latch_vi_register_for_scanline", "rdp_cp_end_vi_register_per_scanline",
     "rdp_batch_create", "rdp_batch_destroy", "rdp_batch_add_instance", "rdp_batch_submit", "rdp_batch_idle",
-    "rdp_batch_get_stats", "rdp_batch_capture_begin", "rdp_batch_capture_end",
+    "rdp_batch_get_stats", "rdp_batch_capture_begin", "rdp_batch_capture_end", "rdp_set_shade_variant",
+    "rdp_get_shade_variant",
 ]
 
 
@@ -166,6 +167,8 @@ def lib():
     L.rdp_graph_last_shade_ms.restype = ctypes.c_float
     L.rdp_graph_shade_launches.argtypes = [vp]
     L.rdp_graph_shade_launches.restype = u32
+    L.rdp_set_shade_variant.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.rdp_get_shade_variant.argtypes = [ctypes.c_int]
     L.rdp_batch_create.argtypes = [ctypes.POINTER(_BatchCreateInfo), ctypes.POINTER(vp)]
     L.rdp_batch_destroy.argtypes = [vp]
     L.rdp_batch_add_instance.argtypes = [vp, ctypes.POINTER(_CreateInfo), ctypes.POINTER(vp)]
@@ -176,6 +179,19 @@ def lib():
     L.rdp_batch_capture_end.argtypes = [vp, ctypes.POINTER(vp)]
     _lib = L
     return L
+
+
+SHADE_VARIANTS = 4
+
+
+def set_shade_variant(variant, device=0):
+    """Forces the shading-kernel variant (0..3) of a device, or restarts autotuning (-1)."""
+    _check(lib().rdp_set_shade_variant(device, variant), "set_shade_variant")
+
+
+def get_shade_variant(device=0):
+    """The device's shading-kernel variant; -1 while the autotuner is still timing them."""
+    return lib().rdp_get_shade_variant(device)
 
 
 def device_is_supported(device=0):

@@ -95,9 +95,18 @@ static cudaError_t ensure_luts(int device)
 } // namespace
 
 namespace rdpx {
+// RDP_SHADE_VARIANT=<0..3> in the environment fixes the variant (profiling, experiments).
 int &shade_variant_choice(int device)
 {
-	static std::vector<int> choice(64, -1);
+	static std::vector<int> choice = [] {
+		int v = -1;
+		if (const char *e = getenv("RDP_SHADE_VARIANT"))
+		{
+			int x = atoi(e);
+			if (x >= 0 && x < RDP_SHADE_VARIANTS) v = x;
+		}
+		return std::vector<int>(64, v);
+	}();
 	return choice[device >= 0 && device < 64 ? device : 0];
 }
 } // namespace rdpx
@@ -1422,7 +1431,7 @@ struct rdp_cp
 		int r = signal_timeline(&v);
 		if (r != RDP_OK) return r;
 		r = wait_timeline(v, UINT64_MAX / 2);
-		if (r == RDP_OK && !batch) own_exec.tune_collect();
+		if (r == RDP_OK && !batch) own_exec.tune_epoch();
 		return r;
 	}
 };
@@ -1934,7 +1943,7 @@ int rdp_batch_idle(rdp_batch *b)
 		if ((r = cp->signal_timeline(&v)) != RDP_OK || (r = cp->wait_timeline(v, UINT64_MAX / 2)) != RDP_OK) return r;
 	}
 	if (!b->capturing && !b->exec.adapt_pairs()) return b->sticky_error = RDP_ERR_DEVICE;
-	b->exec.tune_collect();
+	b->exec.tune_epoch();
 	return RDP_OK;
 }
 

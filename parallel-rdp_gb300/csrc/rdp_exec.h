@@ -99,18 +99,19 @@ struct CaptureSink
 // Process-wide choice of the k_shade variant per device: -1 until tuned (or forced).
 int &shade_variant_choice(int device);
 
-// Autotuner of the shading kernel: while active, launches that rasterise rotate through
-// the compiled k_shade variants; each launch's k_shade time (CUDA events on the stream)
-// and pair count (written by k_scan to a ring) are collected at sync points, and once
-// every variant has kTuneSamples launches of at least kTuneMinPairs pairs, the variant
-// with the least time per pair is kept for the device.  The variants compute identical
-// results, so tuning never changes output.
+// Autotuner of the shading kernel.  Tuning runs for RDP_SHADE_VARIANTS epochs (an epoch
+// ends at each sync point: idle); in epoch e the i-th rasterising launch uses variant
+// (i + e) mod RDP_SHADE_VARIANTS, so over the epochs every variant runs every launch
+// position of a repeating frame once.  Each sampled launch's k_shade time (CUDA events on
+// the stream) and pair count (written by k_scan) are summed per variant; the variant with
+// the least time per pair is kept for the device.  The variants compute identical results,
+// so tuning never changes output.
 struct ShadeTuner
 {
-	static constexpr int kTuneSamples = 3;
-	static constexpr uint32_t kTuneMinPairs = 20000;
+	static constexpr uint32_t kMaxSamplesPerEpoch = 64;
 	bool active = false;
-	int next = 0;
+	int epoch = 0;
+	uint32_t in_epoch = 0;
 	uint64_t samples_taken = 0;
 	struct Sample
 	{
@@ -210,7 +211,7 @@ struct Executor
 		return v >= 0 && v < RDP_SHADE_VARIANTS ? v : 0;
 	}
 
-	// At a sync point: folds finished tuning samples in; decides when enough are in.
+	// Folds finished tuning samples in (non-blocking for unfinished ones).
 	void tune_collect()
 	{
 		if (tuner.pending.empty()) return;
@@ -230,8 +231,7 @@ struct Executor
 				keep.push_back(sm);
 				continue;
 			}
-			if (q == cudaSuccess && cudaEventElapsedTime(&ms, sm.ev[0], sm.ev[1]) == cudaSuccess &&
-			    log[sm.slot] >= ShadeTuner::kTuneMinPairs)
+			if (q == cudaSuccess && cudaEventElapsedTime(&ms, sm.ev[0], sm.ev[1]) == cudaSuccess)
 			{
 				tuner.ms[sm.variant] += ms;
 				tuner.pairs[sm.variant] += log[sm.slot];
@@ -242,12 +242,27 @@ struct Executor
 			tuner.pool.push_back(sm.ev[1]);
 		}
 		tuner.pending.swap(keep);
+	}
+
+	// At a sync point (the stream is idle): ends a tuning epoch; after the last one, keeps
+	// the variant with the least k_shade time per pair.
+	void tune_epoch()
+	{
 		if (!tuner.active) return;
+		if (shade_variant_choice(device) >= 0)
+		{
+			tuner.active = false;
+			return;
+		}
+		tune_collect();
+		if (tuner.in_epoch == 0) return; // nothing rasterised since the last sync point
+		tuner.in_epoch = 0;
+		if (++tuner.epoch < RDP_SHADE_VARIANTS) return;
 		int best = -1;
 		double best_rate = 0.0;
 		for (int v = 0; v < RDP_SHADE_VARIANTS; v++)
 		{
-			if (tuner.count[v] < ShadeTuner::kTuneSamples) return;
+			if (tuner.pairs[v] <= 0.0) continue;
 			double rate = tuner.ms[v] / tuner.pairs[v];
 			if (best < 0 || rate < best_rate)
 			{
@@ -255,6 +270,7 @@ struct Executor
 				best_rate = rate;
 			}
 		}
+		if (best < 0) best = 0;
 		tuner.active = false;
 		if (shade_variant_choice(device) < 0) shade_variant_choice(device) = best;
 	}
@@ -567,10 +583,11 @@ struct Executor
 		L.pair_capacity = caps.pairs;
 		int variant = current_variant();
 		bool sample = false;
-		if (tuner.active && shade_variant_choice(device) < 0 && !cap && tile_base && tuner.pending.size() < 64)
+		if (tuner.active && shade_variant_choice(device) < 0 && !cap && tile_base &&
+		    tuner.in_epoch < ShadeTuner::kMaxSamplesPerEpoch)
 		{
-			variant = tuner.next;
-			tuner.next = (tuner.next + 1) % RDP_SHADE_VARIANTS;
+			variant = int((tuner.in_epoch + uint32_t(tuner.epoch)) % RDP_SHADE_VARIANTS);
+			tuner.in_epoch++;
 			sample = true;
 		}
 		L.shade_variant = uint32_t(variant);

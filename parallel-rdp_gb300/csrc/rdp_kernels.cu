@@ -2624,15 +2624,12 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass
 			                 ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, s_sa[r], s_sx[r], s_sa[r + 1], s_sx[r + 1],
 			                 x, y, out);
 		}
+		// All 64 pixels of the scratch are written (full sectors, no partial-sector
+		// read-modify-write in L2); k_blend skips pixels whose misc word says "not written".
 		size_t at = size_t(pr) * SHADE_THREADS + tid;
-		if (ok)
-		{
-			sc_color[at] = out.combined;
-			sc_zdith[at] = out.z_dith;
-			sc_misc[at] = uint16_t((out.coverage & 0xff) | (out.shade_alpha << 8));
-		}
-		else
-			sc_misc[at] = 0x00ffu;
+		sc_color[at] = ok ? out.combined : 0u;
+		sc_zdith[at] = ok ? out.z_dith : 0;
+		sc_misc[at] = ok ? uint16_t((out.coverage & 0xff) | (out.shade_alpha << 8)) : uint16_t(0x00ffu);
 		__syncthreads();
 	}
 }

@@ -9,9 +9,11 @@ FillRects; alpha compare, LOD/detail and Z on half the primitives), per-instance
 seeds 0-63.  One step = one frame of every instance (one sync point).
 
 value  : reference-equivalent render passes per second (the reference's pass rule,
-         counted by the host emulation of its need_flush) of the BATCHED path with
-         every input resident in HBM: the sync point's rounds replayed as a CUDA
-         graph; CUDA events on the batch's stream; L2 flushed between iterations.
+         counted by the host emulation of its need_flush) of the BATCHED path with the
+         LEARNED tile order (the cost model trains online on the first sync points) and
+         every input resident in HBM: the sync point's rounds replayed as a CUDA graph;
+         CUDA events on the batch's stream; L2 flushed between iterations.  The same
+         replay in plain tile order is reported beside it (tile_order.static).
 plain  : the same frames through the plain single-instance path, one processor and
          one CUDA graph per instance, run one after another.
 e2e    : the batched path through the C ABI with host buffers: every instance's
@@ -431,28 +433,48 @@ def run_ours_batched(args):
     frags_per_step = sum(x["fragments"] - y["fragments"] for x, y in zip(s1, s0))
     pairs_per_step = sum(x["tile_instances"] - y["tile_instances"] for x, y in zip(s1, s0))
 
-    # ---------------- value: device-resident graph replay of the whole sync point
-    graph = b.capture([st[0] for st in streams])
-    for _ in range(args.warmup):
-        flush()
-        graph.replay(1)
-    clocks = ClockSampler(local)
-    _barrier(dist)
-    clocks.start()
-    step_ms, shade_ms = [], []
-    for _ in range(args.steps):
-        flush()
-        step_ms.append(graph.replay(1))
-        shade_ms.append(graph.last_shade_ms())
-    clock_info = clocks.stop()
-    _barrier(dist)
-    launches = graph.kernels * args.steps
-    shade_launches = graph.shade_launches
+    # ---------------- learned tile order: the cost model trains online on the first sync points
+    b.set_schedule(learned_order=True, train=True, learning_rate=3e-3)
+    for _ in range(args.train_steps):
+        _run_batch_step(b, insts, streams)
+        b.idle()
+    model_loss = b.get_model()[1]
+    b.set_schedule(learned_order=True, train=False)
+
+    def timed_graph(tag):
+        graph = b.capture([st[0] for st in streams])
+        for _ in range(args.warmup):
+            flush()
+            graph.replay(1)
+        clocks = ClockSampler(local)
+        _barrier(dist)
+        clocks.start()
+        step_ms, shade_ms, blend_ms = [], [], []
+        for _ in range(args.steps):
+            flush()
+            step_ms.append(graph.replay(1))
+            shade_ms.append(graph.last_shade_ms())
+            blend_ms.append(graph.last_blend_ms())
+        clock_info = clocks.stop()
+        _barrier(dist)
+        out = dict(step_ms=step_ms, shade_ms=shade_ms, blend_ms=blend_ms, clocks=clock_info,
+                   launches=graph.kernels * args.steps, shade_launches=graph.shade_launches)
+        graph.close()
+        return out
+
+    # ---------------- value: device-resident graph replay of the whole sync point (learned order)
+    rl = timed_graph("learned")
+    step_ms, shade_ms, clock_info = rl["step_ms"], rl["shade_ms"], rl["clocks"]
+    launches, shade_launches = rl["launches"], rl["shade_launches"]
     t_value = _max_over_ranks(dist, sum(step_ms) / 1e3)
     total_passes = _sum_over_ranks(dist, passes_per_step * args.steps)
     total_frags = _sum_over_ranks(dist, frags_per_step * args.steps)
     value = total_passes / t_value
-    graph.close()
+    # The same sync point in plain tile order (the fallback the learned order is judged against).
+    b.set_schedule(learned_order=False, train=False)
+    rs = timed_graph("static")
+    t_static = _max_over_ranks(dist, sum(rs["step_ms"]) / 1e3)
+    b.set_schedule(learned_order=True, train=False)
 
     # ---------------- e2e: C ABI with host buffers, all instances per step
     for _ in range(args.warmup):
@@ -521,13 +543,18 @@ def run_ours_batched(args):
                    "reference_passes_per_step": passes_per_step, "fragments_per_step": frags_per_step,
                    "tile_instances_per_step": pairs_per_step, "rounds_per_step": rounds_per_step,
                    "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "flushed between timed iterations", "tile_order": "static",
+                   "l2": "flushed between timed iterations", "tile_order": "learned (longest predicted first)",
                    "shade_variant": get_shade_variant(local)},
         "mpix_per_s": total_frags / t_value / 1e6,
         "frames_per_s": world * args.steps * args.instances / t_value,
         "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": t_plain * 1e3 / args.steps,
                   "mpix_per_s": total_frags / t_plain / 1e6},
         "batched_over_plain": value / plain_value,
+        "tile_order": {"learned": {"ms_per_step": t_value * 1e3 / args.steps,
+                                   "blend_ms_per_step": statistics.mean(rl["blend_ms"])},
+                       "static": {"value": total_passes / t_static, "ms_per_step": t_static * 1e3 / args.steps,
+                                  "blend_ms_per_step": statistics.mean(rs["blend_ms"])},
+                       "model_train_steps": args.train_steps, "model_mse": model_loss},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "mpix_per_s": total_frags / e2e_t / 1e6},
         "gpu_launches": int(launches),
@@ -599,6 +626,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="batched", choices=["batched", "textured"])
     ap.add_argument("--instances", type=int, default=BATCH_INSTANCES)
+    ap.add_argument("--train-steps", type=int, default=8, help="sync points of online cost-model training")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":

@@ -37,7 +37,8 @@ enum
 	RDPGEN_ALPHA_TEST_HALF = 1u << 10, /* alpha compare on half of the primitives */
 	RDPGEN_LOD = 1u << 11,             /* random LOD / detail tiles on textured triangles */
 	RDPGEN_RUNS = 1u << 12,            /* primitives of one kind come in runs */
-	RDPGEN_FUZZ = 1u << 13             /* every mode bit, selector, texture format and load drawn at random */
+	RDPGEN_FUZZ = 1u << 13,            /* every mode bit, selector, texture format and load drawn at random */
+	RDPGEN_HOTSPOT = 1u << 14          /* triangle centroids inside the top-left 16x16 pixels (a few very busy tiles) */
 };
 
 typedef struct rdpgen_params

@@ -170,6 +170,8 @@ uint32_t rdp_graph_kernel_count(rdp_graph *g);
 /* GPU time (ms) of the shading kernel (k_shade, the dominant kernel) in the last replay,
  * from CUDA events recorded on the stream around each of its launches, and their number. */
 float rdp_graph_last_shade_ms(rdp_graph *g);
+/* The same for the blend kernel (k_blend, whose work queue the learned tile order sorts). */
+float rdp_graph_last_blend_ms(rdp_graph *g);
 uint32_t rdp_graph_shade_launches(rdp_graph *g);
 void rdp_graph_destroy(rdp_graph *g);
 
@@ -219,6 +221,29 @@ int rdp_batch_get_stats(rdp_batch *b, rdp_batch_stats *out);
  * (as rdp_cp_capture_begin/end do for one processor) and the graph replays all rounds. */
 int rdp_batch_capture_begin(rdp_batch *b);
 int rdp_batch_capture_end(rdp_batch *b, rdp_graph **out);
+
+/* Learned tile order.  No counterpart in the reference.  A small MLP (16 -> 64 -> 64 -> 1, ReLU,
+ * FP16 weights, FP32 accumulation, RDP_MLP_PARAMS parameters packed as W1[64][16], b1[64],
+ * W2[64][64], b2[64], W3[64], b3) predicts each non-empty tile's blend cost from its binning
+ * features; the blend kernel then starts tiles longest-predicted-first.  Output never depends
+ * on the order.  With `train`, every launch also takes one Adam step (learning_rate) on the
+ * launch's tiles (every train_stride-th), target log2(1 + measured blend cycles) / 16.
+ * rdp_batch_get_model returns the FP32 parameters and the last step's mean squared error;
+ * rdp_batch_set_model loads parameters (and resets the optimiser state). */
+#define RDP_MLP_PARAMS 5313
+int rdp_batch_set_schedule(rdp_batch *b, int learned_order, int train, float learning_rate, uint32_t train_stride);
+int rdp_batch_get_model(rdp_batch *b, float *params, float *last_loss);
+int rdp_batch_set_model(rdp_batch *b, const float *params);
+/* The last launch's non-empty tiles, in tile order: features (16 per tile) and predictions
+ * (when the model ran), measured blend cycles (with RDP_BATCH_RECORD_TILE_CYCLES or training).
+ * Any output may be NULL; *count receives the number of tiles written (<= max_tiles). */
+int rdp_batch_get_tile_samples(rdp_batch *b, float *features, float *predicted, uint32_t *cycles, uint32_t max_tiles,
+                               uint32_t *count);
+/* The scheduler's GPU kernels on caller data (test and tooling entry points): loss gradients
+ * (mean squared error over n samples of RDP_MLP_IN = 16 features) and forward outputs. */
+int rdp_mlp_gradients(int device, const float *params, const float *features, const float *targets, uint32_t n,
+                      float *grads, float *loss);
+int rdp_mlp_forward(int device, const float *params, const float *features, uint32_t n, float *out);
 
 /* Kernel specialisation.  No counterpart in the reference (its shaders are specialised per
  * render-state variant by its pipeline compiler).  The shading kernel is compiled for

@@ -463,7 +463,9 @@ struct Gen
 	{
 		double area = p.area_median * Rng::det_exp(p.area_sigma * rng.normal());
 		area = std::min(area, double(p.width) * double(p.height));
-		double cx = rng.uniform() * p.width, cy = rng.uniform() * p.height;
+		const double span_x = (p.flags & RDPGEN_HOTSPOT) ? 16.0 : double(p.width);
+		const double span_y = (p.flags & RDPGEN_HOTSPOT) ? 16.0 : double(p.height);
+		double cx = rng.uniform() * span_x, cy = rng.uniform() * span_y;
 		double px[3], py[3];
 		double a = 0;
 		for (int tries = 0; tries < 8; tries++)

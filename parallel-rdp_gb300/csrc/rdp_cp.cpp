@@ -33,6 +33,8 @@
 #include "rdp_types.h"
 #include "rdp_kernels.h"
 #include "rdp_exec.h"
+#include "sched.h"
+#include <cuda_fp16.h>
 #include "vi.h"
 #include "blender_divider_runs.inc"
 
@@ -1745,9 +1747,9 @@ struct rdp_graph
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t gexec = nullptr;
 	std::vector<void *> buffers;
-	std::vector<std::pair<cudaEvent_t, cudaEvent_t>> shade_events;
+	std::vector<std::pair<cudaEvent_t, cudaEvent_t>> shade_events, blend_events;
 	uint32_t kernels = 0, shade_launches = 0;
-	float last_shade_ms = 0.0f;
+	float last_shade_ms = 0.0f, last_blend_ms = 0.0f;
 	cudaEvent_t ev[2] = { nullptr, nullptr };
 };
 
@@ -1769,12 +1771,13 @@ static int build_graph(rdpx::Executor *exec, rdpx::CaptureSink &sink, rdp_stats 
 			if (L.num_prims && L.num_tile_items)
 			{
 				g->shade_events.emplace_back(L.shade_events[0], L.shade_events[1]);
+				g->blend_events.emplace_back(L.blend_events[0], L.blend_events[1]);
 				g->shade_launches++;
 			}
 			else
 			{
-				cudaEventDestroy(L.shade_events[0]);
-				cudaEventDestroy(L.shade_events[1]);
+				for (cudaEvent_t e : { L.shade_events[0], L.shade_events[1], L.blend_events[0], L.blend_events[1] })
+					cudaEventDestroy(e);
 			}
 		}
 		ok = cudaStreamEndCapture(exec->stream, &g->graph) == cudaSuccess;
@@ -1831,16 +1834,24 @@ int rdp_graph_replay(rdp_graph *g, uint32_t count, float *elapsed_ms)
 	if (elapsed_ms && cudaEventElapsedTime(elapsed_ms, g->ev[0], g->ev[1]) != cudaSuccess) return RDP_ERR_DEVICE;
 	// GPU time of the rasteriser launches of the last replay.
 	g->last_shade_ms = 0.0f;
+	g->last_blend_ms = 0.0f;
 	for (auto &pr : g->shade_events)
 	{
 		float ms = 0.0f;
 		if (cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) g->last_shade_ms += ms;
 		else cudaGetLastError(); // keep the thread's last-error slot clean for other CUDA users
 	}
+	for (auto &pr : g->blend_events)
+	{
+		float ms = 0.0f;
+		if (cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess) g->last_blend_ms += ms;
+		else cudaGetLastError();
+	}
 	return RDP_OK;
 }
 
 float rdp_graph_last_shade_ms(rdp_graph *g) { return g ? g->last_shade_ms : 0.0f; }
+float rdp_graph_last_blend_ms(rdp_graph *g) { return g ? g->last_blend_ms : 0.0f; }
 uint32_t rdp_graph_shade_launches(rdp_graph *g) { return g ? g->shade_launches : 0; }
 
 uint32_t rdp_graph_kernel_count(rdp_graph *g) { return g ? g->kernels : 0; }
@@ -1853,11 +1864,12 @@ void rdp_graph_destroy(rdp_graph *g)
 	if (g->gexec) cudaGraphExecDestroy(g->gexec);
 	if (g->graph) cudaGraphDestroy(g->graph);
 	for (void *b : g->buffers) cudaFree(b);
-	for (auto &pr : g->shade_events)
-	{
-		cudaEventDestroy(pr.first);
-		cudaEventDestroy(pr.second);
-	}
+	for (auto *list : { &g->shade_events, &g->blend_events })
+		for (auto &pr : *list)
+		{
+			cudaEventDestroy(pr.first);
+			cudaEventDestroy(pr.second);
+		}
 	for (auto e : g->ev)
 		if (e) cudaEventDestroy(e);
 	delete g;
@@ -1881,7 +1893,15 @@ int rdp_batch_create(const rdp_batch_create_info *info, rdp_batch **out)
 		delete b;
 		return RDP_ERR_DEVICE;
 	}
-	b->exec.record_cycles = (info->flags & RDP_BATCH_RECORD_TILE_CYCLES) != 0;
+	b->exec.cycles_requested = (info->flags & RDP_BATCH_RECORD_TILE_CYCLES) != 0;
+	b->exec.record_cycles = b->exec.cycles_requested;
+	if ((info->flags & RDP_BATCH_TILE_ORDER_LEARNED) && !b->exec.sched_enable(true, false, 1e-3f, 1))
+	{
+		b->exec.destroy();
+		cudaStreamDestroy(b->stream);
+		delete b;
+		return RDP_ERR_DEVICE;
+	}
 	*out = b;
 	return RDP_OK;
 }
@@ -1988,6 +2008,155 @@ int rdp_get_shade_variant(int device)
 {
 	if (device < 0 || device >= 64) return -1;
 	return rdpx::shade_variant_choice(device);
+}
+
+int rdp_batch_set_schedule(rdp_batch *b, int learned_order, int train, float learning_rate, uint32_t train_stride)
+{
+	if (!b || learning_rate < 0.0f) return RDP_ERR_INVALID;
+	cudaSetDevice(b->device);
+	if (!learned_order && !train && !b->exec.sched_ready) return RDP_OK;
+	return b->exec.sched_enable(learned_order != 0, train != 0, learning_rate, train_stride) ? RDP_OK : RDP_ERR_DEVICE;
+}
+
+int rdp_batch_get_model(rdp_batch *b, float *params, float *last_loss)
+{
+	if (!b || !params) return RDP_ERR_INVALID;
+	cudaSetDevice(b->device);
+	if (!b->exec.sched_ready && !b->exec.sched_enable(false, false, 0.0f, 1)) return RDP_ERR_DEVICE;
+	if (cudaStreamSynchronize(b->stream) != cudaSuccess) return RDP_ERR_DEVICE;
+	if (cudaMemcpy(params, b->exec.sched.w32, sizeof(float) * RDP_MLP_PARAMS, cudaMemcpyDeviceToHost) != cudaSuccess)
+		return RDP_ERR_DEVICE;
+	if (last_loss)
+	{
+		float l[2] = { 0.0f, 0.0f };
+		if (cudaMemcpy(l, b->exec.sched.loss, sizeof(l), cudaMemcpyDeviceToHost) != cudaSuccess) return RDP_ERR_DEVICE;
+		*last_loss = l[1] > 0.0f ? l[0] / l[1] : 0.0f;
+	}
+	return RDP_OK;
+}
+
+int rdp_batch_set_model(rdp_batch *b, const float *params)
+{
+	if (!b || !params) return RDP_ERR_INVALID;
+	cudaSetDevice(b->device);
+	rdpx::Executor &ex = b->exec;
+	if (!ex.sched_ready && !ex.sched_enable(false, false, 0.0f, 1)) return RDP_ERR_DEVICE;
+	std::vector<__half> h(RDP_MLP_PARAMS);
+	for (int i = 0; i < RDP_MLP_PARAMS; i++) h[i] = __float2half_rn(params[i]);
+	if (cudaStreamSynchronize(b->stream) != cudaSuccess ||
+	    cudaMemcpy(ex.sched.w32, params, sizeof(float) * RDP_MLP_PARAMS, cudaMemcpyHostToDevice) != cudaSuccess ||
+	    cudaMemcpy(ex.sched.w16, h.data(), sizeof(__half) * RDP_MLP_PARAMS, cudaMemcpyHostToDevice) != cudaSuccess ||
+	    cudaMemset(ex.sched.adam_m, 0, sizeof(float) * RDP_MLP_PARAMS) != cudaSuccess ||
+	    cudaMemset(ex.sched.adam_v, 0, sizeof(float) * RDP_MLP_PARAMS) != cudaSuccess ||
+	    cudaMemset(ex.sched.adam_t, 0, sizeof(uint32_t)) != cudaSuccess)
+		return RDP_ERR_DEVICE;
+	return RDP_OK;
+}
+
+// Runs the MLP kernels on caller data (weights rounded to FP16 as the scheduler stores them).
+static int mlp_call(int device, const float *params, const float *features, const float *targets, uint32_t n,
+                    float *grads, float *loss, float *out)
+{
+	if (!params || !features || !n || cudaSetDevice(device) != cudaSuccess) return RDP_ERR_INVALID;
+	std::vector<__half> h(RDP_MLP_PARAMS);
+	for (int i = 0; i < RDP_MLP_PARAMS; i++) h[i] = __float2half_rn(params[i]);
+	__half *dw = nullptr;
+	float *df = nullptr, *dt = nullptr, *dg = nullptr, *dl = nullptr, *dout = nullptr;
+	int r = RDP_ERR_DEVICE;
+	cudaStream_t s = nullptr;
+	if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess &&
+	    cudaMalloc(&dw, sizeof(__half) * RDP_MLP_PARAMS) == cudaSuccess &&
+	    cudaMalloc(&df, sizeof(float) * RDP_MLP_IN * size_t(n)) == cudaSuccess &&
+	    cudaMemcpy(dw, h.data(), sizeof(__half) * RDP_MLP_PARAMS, cudaMemcpyHostToDevice) == cudaSuccess &&
+	    cudaMemcpy(df, features, sizeof(float) * RDP_MLP_IN * size_t(n), cudaMemcpyHostToDevice) == cudaSuccess)
+	{
+		if (out)
+		{
+			if (cudaMalloc(&dout, sizeof(float) * n) == cudaSuccess &&
+			    rdp_sched_launch_forward(dw, df, n, dout, s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess &&
+			    cudaMemcpy(out, dout, sizeof(float) * n, cudaMemcpyDeviceToHost) == cudaSuccess)
+				r = RDP_OK;
+		}
+		else if (targets && grads &&
+		         cudaMalloc(&dt, sizeof(float) * n) == cudaSuccess &&
+		         cudaMalloc(&dg, sizeof(float) * RDP_MLP_PARAMS) == cudaSuccess && cudaMalloc(&dl, 2 * sizeof(float)) == cudaSuccess &&
+		         cudaMemcpy(dt, targets, sizeof(float) * n, cudaMemcpyHostToDevice) == cudaSuccess &&
+		         cudaMemset(dg, 0, sizeof(float) * RDP_MLP_PARAMS) == cudaSuccess && cudaMemset(dl, 0, 2 * sizeof(float)) == cudaSuccess &&
+		         rdp_sched_launch_grad(dw, df, dt, n, dg, dl, s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess &&
+		         cudaMemcpy(grads, dg, sizeof(float) * RDP_MLP_PARAMS, cudaMemcpyDeviceToHost) == cudaSuccess)
+		{
+			float l[2];
+			if (cudaMemcpy(l, dl, sizeof(l), cudaMemcpyDeviceToHost) == cudaSuccess)
+			{
+				if (loss) *loss = l[1] > 0.0f ? l[0] / l[1] : 0.0f;
+				r = RDP_OK;
+			}
+		}
+	}
+	cudaGetLastError();
+	cudaFree(dw);
+	cudaFree(df);
+	cudaFree(dt);
+	cudaFree(dg);
+	cudaFree(dl);
+	cudaFree(dout);
+	if (s) cudaStreamDestroy(s);
+	return r;
+}
+
+int rdp_mlp_gradients(int device, const float *params, const float *features, const float *targets, uint32_t n,
+                      float *grads, float *loss)
+{
+	if (!targets || !grads) return RDP_ERR_INVALID;
+	return mlp_call(device, params, features, targets, n, grads, loss, nullptr);
+}
+
+int rdp_mlp_forward(int device, const float *params, const float *features, uint32_t n, float *out)
+{
+	if (!out) return RDP_ERR_INVALID;
+	return mlp_call(device, params, features, nullptr, n, nullptr, nullptr, out);
+}
+
+int rdp_batch_get_tile_samples(rdp_batch *b, float *features, float *predicted, uint32_t *cycles, uint32_t max_tiles,
+                               uint32_t *count)
+{
+	if (!b || !count) return RDP_ERR_INVALID;
+	cudaSetDevice(b->device);
+	rdpx::Executor &ex = b->exec;
+	*count = 0;
+	if (cudaStreamSynchronize(b->stream) != cudaSuccess) return RDP_ERR_DEVICE;
+	uint32_t ctrl[5];
+	if (cudaMemcpy(ctrl, ex.d_ctrl, sizeof(ctrl), cudaMemcpyDeviceToHost) != cudaSuccess) return RDP_ERR_DEVICE;
+	uint32_t n = std::min(ctrl[3], max_tiles);
+	if (ctrl[1]) n = 0;
+	if (!n) return RDP_OK;
+	std::vector<uint32_t> items(n);
+	if (cudaMemcpy(items.data(), ex.d_nonempty, 4 * size_t(n), cudaMemcpyDeviceToHost) != cudaSuccess) return RDP_ERR_DEVICE;
+	if (features || predicted)
+	{
+		if (!ex.sched_ready || !ex.sched.features) return RDP_ERR_INVALID;
+		if (features)
+		{
+			std::vector<float> all(size_t(ex.sched_capacity) * RDP_MLP_IN);
+			if (cudaMemcpy(all.data(), ex.sched.features, sizeof(float) * all.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+				return RDP_ERR_DEVICE;
+			for (uint32_t k = 0; k < n; k++)
+				for (int f = 0; f < RDP_MLP_IN; f++)
+					features[size_t(k) * RDP_MLP_IN + f] = items[k] < ex.sched_capacity ? all[size_t(items[k]) * RDP_MLP_IN + f] : 0.0f;
+		}
+		if (predicted && cudaMemcpy(predicted, ex.sched.pred, sizeof(float) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+			return RDP_ERR_DEVICE;
+	}
+	if (cycles)
+	{
+		if (!ex.record_cycles) return RDP_ERR_INVALID;
+		std::vector<uint32_t> all(ex.caps.tile_items);
+		if (cudaMemcpy(all.data(), ex.d_tile_cycles, 4 * all.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+			return RDP_ERR_DEVICE;
+		for (uint32_t k = 0; k < n; k++) cycles[k] = items[k] < all.size() ? all[items[k]] : 0u;
+	}
+	*count = n;
+	return RDP_OK;
 }
 
 } // extern "C"

@@ -20,6 +20,7 @@
 
 #include "rdp_types.h"
 #include "rdp_kernels.h"
+#include "sched.h"
 
 namespace rdpx {
 
@@ -181,7 +182,91 @@ struct Executor
 	} staging[2];
 	int staging_index = 0;
 
-	bool record_cycles = false;
+	bool record_cycles = false, cycles_requested = false;
+
+	// Learned tile order (sched.h): model and per-tile buffers, allocated on first use.
+	bool sched_ready = false;
+	RdpSchedDev sched = {};
+	uint32_t sched_capacity = 0;
+
+	bool sched_enable(bool order, bool train, float lr, uint32_t stride)
+	{
+		if (!sched_ready)
+		{
+			if (check(cudaMalloc(&sched.w16, sizeof(__half) * RDP_MLP_PARAMS)) ||
+			    check(cudaMalloc(&sched.w32, sizeof(float) * RDP_MLP_PARAMS)) ||
+			    check(cudaMalloc(&sched.adam_m, sizeof(float) * RDP_MLP_PARAMS)) ||
+			    check(cudaMalloc(&sched.adam_v, sizeof(float) * RDP_MLP_PARAMS)) ||
+			    check(cudaMalloc(&sched.grad, sizeof(float) * RDP_MLP_PARAMS)) ||
+			    check(cudaMalloc(&sched.adam_t, sizeof(uint32_t))) || check(cudaMalloc(&sched.loss, 2 * sizeof(float))) ||
+			    check(cudaMalloc(&sched.hist, sizeof(uint32_t) * RDP_SCHED_BUCKETS)) ||
+			    check(cudaMalloc(&sched.cursor, sizeof(uint32_t) * RDP_SCHED_BUCKETS)))
+				return false;
+			if (check(cudaMemsetAsync(sched.loss, 0, 2 * sizeof(float), stream)) ||
+			    check(cudaMemsetAsync(sched.hist, 0, sizeof(uint32_t) * RDP_SCHED_BUCKETS, stream)))
+				return false;
+			if (check(rdp_sched_init_weights(&sched, 1u, stream))) return false;
+			sched_ready = true;
+			generation++;
+		}
+		sched.order_enabled = order ? 1u : 0u;
+		sched.train_enabled = train ? 1u : 0u;
+		sched.lr = lr;
+		sched.train_stride = stride ? stride : 1u;
+		record_cycles = train || cycles_requested;
+		return sched_buffers(caps.tile_items) && sched_prim_buffers(caps.prims);
+	}
+
+	uint32_t sched_prim_capacity = 0;
+	bool sched_prim_buffers(uint32_t n)
+	{
+		if (!sched_ready || n <= sched_prim_capacity) return true;
+		cudaFree(sched.featbits);
+		sched.featbits = nullptr;
+		if (check(cudaMalloc(&sched.featbits, sizeof(uint16_t) * size_t(n)))) return false;
+		sched_prim_capacity = n;
+		generation++;
+		return true;
+	}
+
+	bool sched_buffers(uint32_t n)
+	{
+		if (!sched_ready || n <= sched_capacity) return true;
+		cudaFree(sched.features);
+		cudaFree(sched.pred);
+		cudaFree(sched.bucket);
+		sched.features = nullptr;
+		sched.pred = nullptr;
+		sched.bucket = nullptr;
+		if (check(cudaMalloc(&sched.features, sizeof(float) * RDP_MLP_IN * size_t(n))) ||
+		    check(cudaMalloc(&sched.pred, sizeof(float) * size_t(n))) || check(cudaMalloc(&sched.bucket, 4 * size_t(n))))
+			return false;
+		sched_capacity = n;
+		sched.capacity = n;
+		generation++;
+		return true;
+	}
+
+	void sched_free()
+	{
+		cudaFree(sched.w16);
+		cudaFree(sched.w32);
+		cudaFree(sched.adam_m);
+		cudaFree(sched.adam_v);
+		cudaFree(sched.grad);
+		cudaFree(sched.adam_t);
+		cudaFree(sched.loss);
+		cudaFree(sched.hist);
+		cudaFree(sched.cursor);
+		cudaFree(sched.featbits);
+		cudaFree(sched.features);
+		cudaFree(sched.pred);
+		cudaFree(sched.bucket);
+		sched = RdpSchedDev{};
+		sched_ready = false;
+		sched_capacity = 0;
+		sched_prim_capacity = 0;
+	}
 
 	bool check(cudaError_t e)
 	{
@@ -307,6 +392,7 @@ struct Executor
 	{
 		if (stream) cudaStreamSynchronize(stream);
 		free_all();
+		sched_free();
 		cudaFree(d_ctrl);
 		cudaFree(d_pair_log);
 		d_ctrl = nullptr;
@@ -343,6 +429,7 @@ struct Executor
 			    check(cudaMalloc(&d_shade, sizeof(RdpPrimShade) * n)))
 				return false;
 			caps.prims = n;
+			if (!sched_prim_buffers(n)) return false;
 		}
 		if (grow_tiles)
 		{
@@ -364,6 +451,7 @@ struct Executor
 			    check(cudaMemsetAsync(d_tile_counts, 0, size_t(n + 1) * 4, stream)))
 				return false;
 			caps.tile_items = n;
+			if (!sched_buffers(n)) return false;
 		}
 		if (grow_passes)
 		{
@@ -601,10 +689,17 @@ struct Executor
 		L.num_tile_items = tile_base;
 		L.tile_cycles = record_cycles ? d_tile_cycles : nullptr;
 		L.tile_order = nullptr;
+		if (sched_ready && (sched.order_enabled || sched.train_enabled))
+		{
+			sched.order = d_tile_order;
+			L.sched = &sched;
+		}
 		launches++;
 		if (cap)
 		{
 			for (auto &e : L.shade_events)
+				if (check(cudaEventCreate(&e))) return false;
+			for (auto &e : L.blend_events)
 				if (check(cudaEventCreate(&e))) return false;
 			cap->launches.push_back(L);
 			return true;

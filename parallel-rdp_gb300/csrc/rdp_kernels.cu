@@ -26,6 +26,7 @@
 #include <stdint.h>
 #include "rdp_types.h"
 #include "rdp_kernels.h"
+#include "sched.h"
 
 namespace rdp {
 
@@ -145,7 +146,7 @@ __device__ __forceinline__ uint32_t pass_of_item(const RdpPass *__restrict__ pas
 __global__ void k_prim_setup(const RdpPrimIn *__restrict__ in, uint32_t num_prims, const uint32_t *__restrict__ words,
                              const uint32_t *__restrict__ state_blocks, const RdpPass *__restrict__ passes,
                              uint32_t num_passes, RdpPrimGeom *__restrict__ geom_out, RdpPrimAttr *__restrict__ attr_out,
-                             RdpPrimShade *__restrict__ shade_out)
+                             RdpPrimShade *__restrict__ shade_out, uint16_t *__restrict__ featbits)
 {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= num_prims) return;
@@ -534,6 +535,7 @@ __global__ void k_prim_setup(const RdpPrimIn *__restrict__ in, uint32_t num_prim
 	geom_out[i] = g;
 	attr_out[i] = a;
 	shade_out[i] = sh;
+	if (featbits) featbits[i] = rdp_feature_bits(sh.static_flags, sh.db_flags);
 }
 
 // ============================================================================ k_bin
@@ -2525,8 +2527,10 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t num_items, uint32_t *__r
 
 // One warp per tile: turns the tile's primitive bitmask into its ordered run of
 // (primitive, tile) pairs and clears the bitmask.
+// With `featbits`, also writes the tile's scheduling features (sched.h) to features[item].
 __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes, uint32_t num_items,
-                         const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ ctrl, uint2 *__restrict__ pairs)
+                         const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ ctrl, uint2 *__restrict__ pairs,
+                         const uint16_t *__restrict__ featbits, float *__restrict__ features)
 {
 	uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	int lane = threadIdx.x & 31;
@@ -2537,7 +2541,11 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 	uint32_t *masks = ps.masks + size_t(tl) * RDP_MASK_WORDS_PER_TILE;
 	uint32_t nwords = (ps.prim_count + 31) / 32;
 	uint32_t out = offsets[item];
-	if (offsets[item + 1] == out) return;
+	const uint32_t npairs = offsets[item + 1] - out;
+	if (!npairs) return;
+	uint32_t fc[RDP_FEAT_COUNT];
+#pragma unroll
+	for (int i = 0; i < RDP_FEAT_COUNT; i++) fc[i] = 0;
 	for (uint32_t base = 0; base < nwords; base += 32)
 	{
 		uint32_t wi = base + lane;
@@ -2558,10 +2566,43 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 			{
 				int b = __ffs(wv) - 1;
 				wv &= wv - 1;
-				pairs[pos++] = make_uint2(ps.prim_begin + wi * 32 + uint32_t(b), item);
+				const uint32_t prim = ps.prim_begin + wi * 32 + uint32_t(b);
+				pairs[pos++] = make_uint2(prim, item);
+				if (featbits)
+				{
+					const uint32_t fb = featbits[prim];
+#pragma unroll
+					for (int i = 0; i < RDP_FEAT_COUNT; i++) fc[i] += (fb >> i) & 1u;
+				}
 			}
 		}
 		out += __shfl_sync(0xffffffffu, x, 31);
+	}
+	if (featbits)
+	{
+#pragma unroll
+		for (int i = 0; i < RDP_FEAT_COUNT; i++)
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) fc[i] += __shfl_xor_sync(0xffffffffu, fc[i], o);
+		if (lane < RDP_MLP_IN)
+		{
+			const float np = float(npairs), inv = 1.0f / np;
+			float v;
+			if (lane == 0) v = fminf(np, 1024.0f) * (1.0f / 64.0f);
+			else if (lane == 1) v = log2f(1.0f + np) * 0.1f;
+			else if (lane == 14)
+				v = ps.fb_fmt == FBF_RGBA8888 ? 1.0f : (ps.fb_fmt == FBF_I8 || ps.fb_fmt == FBF_I4) ? 0.25f : 0.5f;
+			else
+			{
+				const int f = lane == 15 ? RDP_FEAT_NOISE : lane - 2;
+				uint32_t c = 0;
+#pragma unroll
+				for (int i = 0; i < RDP_FEAT_COUNT; i++)
+					if (i == f) c = fc[i];
+				v = float(c) * inv;
+			}
+			features[size_t(item) * RDP_MLP_IN + lane] = v;
+		}
 	}
 }
 
@@ -2926,7 +2967,15 @@ extern "C" uint32_t rdp_kernels_count(const RdpLaunch *L)
 	uint32_t n = 0;
 	if (L->num_prims) n += 2;
 	if (L->num_tmem_passes) n += 2;
-	if (L->num_prims && L->num_tile_items) n += 5;
+	if (L->num_prims && L->num_tile_items)
+	{
+		n += 5;
+		if (L->sched && (L->sched->order_enabled || L->sched->train_enabled))
+		{
+			n += 3;
+			if (L->sched->train_enabled && L->tile_cycles) n += 3;
+		}
+	}
 	return n;
 }
 
@@ -2937,7 +2986,11 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 	{
 		rdp::k_prim_setup<<<(L->num_prims + 127) / 128, 128, 0, stream>>>(L->prims_in, L->num_prims, L->words,
 		                                                                   L->state_blocks, L->passes, L->num_passes,
-		                                                                   L->geom, L->attr, L->shade);
+		                                                                   L->geom, L->attr, L->shade,
+		                                                                   L->sched && (L->sched->order_enabled ||
+		                                                                                L->sched->train_enabled)
+		                                                                       ? L->sched->featbits
+		                                                                       : nullptr);
 		rdp::k_bin<<<(L->num_prims * 32 + 255) / 256, 256, 0, stream>>>(L->num_prims, L->geom, L->shade, L->passes,
 		                                                                 L->tile_counts);
 	}
@@ -2952,11 +3005,14 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 	{
 		rdp::k_scan<<<1, 1024, 0, stream>>>(L->num_tile_items, L->tile_counts, L->pair_offsets, L->nonempty_tiles,
 		                                    L->ctrl, L->pair_capacity, L->pair_log, L->log_slot);
+		const bool sched = L->sched && (L->sched->order_enabled || L->sched->train_enabled);
 		rdp::k_expand<<<(L->num_tile_items * 32 + 255) / 256, 256, 0, stream>>>(
-			L->passes, L->num_passes, L->num_tile_items, L->pair_offsets, L->ctrl, L->pairs);
+			L->passes, L->num_passes, L->num_tile_items, L->pair_offsets, L->ctrl, L->pairs,
+			sched ? L->sched->featbits : nullptr, sched ? L->sched->features : nullptr);
 		// Inside a stream capture the events become record nodes of the graph.
 		cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
-		if (L->shade_events[0] && cudaStreamIsCapturing(stream, &capture) != cudaSuccess) return cudaGetLastError();
+		if ((L->shade_events[0] || L->blend_events[0]) && cudaStreamIsCapturing(stream, &capture) != cudaSuccess)
+			return cudaGetLastError();
 		const unsigned ev_flags = capture == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
 		if (L->shade_events[0]) cudaEventRecordWithFlags(L->shade_events[0], stream, ev_flags);
 		const ShadeKernel shade_kernel = kShadeVariants[L->shade_variant < RDP_SHADE_VARIANTS ? L->shade_variant : 0];
@@ -2965,9 +3021,26 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		                                                               L->sc_color, L->sc_zdith, L->sc_misc);
 		if (L->shade_events[1]) cudaEventRecordWithFlags(L->shade_events[1], stream, ev_flags);
 		const uint32_t tile_ctas = std::min<uint32_t>(L->num_tile_items, L->blend_ctas);
+		const uint32_t *order = L->tile_order;
+		if (L->sched && (L->sched->order_enabled || L->sched->train_enabled))
+		{
+			// Features + predictions (also the training inputs), then the longest-first order.
+			cudaError_t e = rdp_sched_launch_order(L->sched, L->pair_offsets, L->ctrl, L->nonempty_tiles,
+			                                       L->blend_ctas / 4 + 1, stream);
+			if (e != cudaSuccess) return e;
+			if (L->sched->order_enabled) order = L->sched->order;
+		}
+		if (L->blend_events[0]) cudaEventRecordWithFlags(L->blend_events[0], stream, ev_flags);
 		rdp::k_blend<<<tile_ctas, rdp::SHADE_THREADS, 0, stream>>>(
 			L->passes, L->num_passes, L->pair_offsets, L->pairs, L->ctrl, L->nonempty_tiles, L->shade, L->sc_color,
-			L->sc_zdith, L->sc_misc, L->tile_order, L->tile_cycles);
+			L->sc_zdith, L->sc_misc, order, L->tile_cycles);
+		if (L->blend_events[1]) cudaEventRecordWithFlags(L->blend_events[1], stream, ev_flags);
+		if (L->sched && L->sched->train_enabled && L->tile_cycles)
+		{
+			cudaError_t e = rdp_sched_launch_train(L->sched, L->ctrl, L->nonempty_tiles, L->tile_cycles,
+			                                       L->blend_ctas / 8 + 1, stream);
+			if (e != cudaSuccess) return e;
+		}
 		rdp::k_raster<<<tile_ctas, rdp::RASTER_THREADS, 0, stream>>>(
 			L->passes, L->num_passes, L->num_tile_items, L->geom, L->attr, L->shade, L->tilesets, L->ctrl);
 	}

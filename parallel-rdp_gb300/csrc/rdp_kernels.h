@@ -29,6 +29,7 @@ typedef struct RdpLaunch
 	uint32_t *tmem_keep;      /* [num_tmem_passes][RDP_MAX_UPLOADS_PER_PASS][64] scratch bitmask */
 	uint32_t num_tile_items;
 	cudaEvent_t shade_events[2];    /* optional: recorded around the k_shade launch */
+	cudaEvent_t blend_events[2];    /* optional: recorded around the k_blend launch */
 	const uint32_t *tile_order;     /* optional [num_tile_items]: order in which k_blend starts tiles */
 	uint32_t *tile_cycles;          /* optional [num_tile_items]: measured k_blend cycles per tile */
 	/* pair list + shading scratch */
@@ -43,6 +44,7 @@ typedef struct RdpLaunch
 	uint32_t blend_ctas;            /* persistent CTAs of k_blend / k_raster */
 	uint32_t *pair_log;             /* optional: k_scan writes the launch's pair count to pair_log[log_slot] */
 	uint32_t log_slot;
+	const struct RdpSchedDev *sched; /* optional learned tile order / online training (sched.h) */
 	uint32_t *sc_color;             /* [pair_capacity * 64] */
 	int *sc_zdith;
 	uint16_t *sc_misc;

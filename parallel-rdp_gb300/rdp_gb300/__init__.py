@@ -15,6 +15,9 @@ from .native import (  # noqa: F401
     SHADE_VARIANTS,
     device_is_supported,
     get_shade_variant,
+    mlp_forward,
+    mlp_gradients,
+    MLP_PARAMS,
     set_shade_variant,
     library_path,
 )

@@ -13,7 +13,7 @@ CONFIG_MIXED = 2      # 640x480 RGBA8888, 16 frames x 50,000 mixed primitives
 
 FLAGS = dict(CLEAR=1 << 0, Z=1 << 1, TWO_CYCLE=1 << 2, PERSPECTIVE=1 << 3, BILINEAR=1 << 4, AA=1 << 5,
              DITHER=1 << 6, FOG=1 << 7, RANDOM_COMBINER=1 << 8, Z_HALF=1 << 9, ALPHA_TEST_HALF=1 << 10,
-             LOD=1 << 11, RUNS=1 << 12, FUZZ=1 << 13)
+             LOD=1 << 11, RUNS=1 << 12, FUZZ=1 << 13, HOTSPOT=1 << 14)
 
 FB_RGBA5551, FB_RGBA8888, FB_I8, FB_IA88, FB_I4 = 0, 1, 2, 3, 4
 

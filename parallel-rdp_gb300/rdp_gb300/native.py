@@ -93,7 +93,8 @@ EXPORTED_SYMBOLS = [
     "rdp_cp_latch_vi_register_for_scanline", "rdp_cp_end_vi_register_per_scanline",
     "rdp_batch_create", "rdp_batch_destroy", "rdp_batch_add_instance", "rdp_batch_submit", "rdp_batch_idle",
     "rdp_batch_get_stats", "rdp_batch_capture_begin", "rdp_batch_capture_end", "rdp_set_shade_variant",
-    "rdp_get_shade_variant",
+    "rdp_get_shade_variant", "rdp_batch_set_schedule", "rdp_batch_get_model", "rdp_batch_set_model",
+    "rdp_mlp_gradients", "rdp_mlp_forward", "rdp_batch_get_tile_samples", "rdp_graph_last_blend_ms",
 ]
 
 
@@ -165,10 +166,18 @@ def lib():
     L.rdp_graph_destroy.restype = None
     L.rdp_graph_last_shade_ms.argtypes = [vp]
     L.rdp_graph_last_shade_ms.restype = ctypes.c_float
+    L.rdp_graph_last_blend_ms.argtypes = [vp]
+    L.rdp_graph_last_blend_ms.restype = ctypes.c_float
     L.rdp_graph_shade_launches.argtypes = [vp]
     L.rdp_graph_shade_launches.restype = u32
     L.rdp_set_shade_variant.argtypes = [ctypes.c_int, ctypes.c_int]
     L.rdp_get_shade_variant.argtypes = [ctypes.c_int]
+    L.rdp_batch_set_schedule.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, u32]
+    L.rdp_batch_get_model.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_float)]
+    L.rdp_batch_set_model.argtypes = [vp, vp]
+    L.rdp_batch_get_tile_samples.argtypes = [vp, vp, vp, vp, u32, ctypes.POINTER(u32)]
+    L.rdp_mlp_gradients.argtypes = [ctypes.c_int, vp, vp, vp, u32, vp, ctypes.POINTER(ctypes.c_float)]
+    L.rdp_mlp_forward.argtypes = [ctypes.c_int, vp, vp, u32, vp]
     L.rdp_batch_create.argtypes = [ctypes.POINTER(_BatchCreateInfo), ctypes.POINTER(vp)]
     L.rdp_batch_destroy.argtypes = [vp]
     L.rdp_batch_add_instance.argtypes = [vp, ctypes.POINTER(_CreateInfo), ctypes.POINTER(vp)]
@@ -192,6 +201,31 @@ def set_shade_variant(variant, device=0):
 def get_shade_variant(device=0):
     """The device's shading-kernel variant; -1 while the autotuner is still timing them."""
     return lib().rdp_get_shade_variant(device)
+
+
+MLP_PARAMS = 5313
+MLP_IN = 16
+
+
+def mlp_gradients(params, features, targets, device=0):
+    """GPU loss gradients of the tile-cost model (the scheduler's own kernels); (grads, loss)."""
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(features, dtype=np.float32)
+    y = np.ascontiguousarray(targets, dtype=np.float32)
+    assert p.size == MLP_PARAMS and x.shape == (y.size, MLP_IN)
+    g = np.zeros(MLP_PARAMS, dtype=np.float32)
+    loss = ctypes.c_float()
+    _check(lib().rdp_mlp_gradients(device, p.ctypes.data, x.ctypes.data, y.ctypes.data, y.size, g.ctypes.data,
+                                   ctypes.byref(loss)), "mlp_gradients")
+    return g, loss.value
+
+
+def mlp_forward(params, features, device=0):
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(features, dtype=np.float32)
+    out = np.zeros(x.shape[0], dtype=np.float32)
+    _check(lib().rdp_mlp_forward(device, p.ctypes.data, x.ctypes.data, x.shape[0], out.ctypes.data), "mlp_forward")
+    return out
 
 
 def device_is_supported(device=0):
@@ -373,6 +407,9 @@ class Graph:
     def last_shade_ms(self):
         return lib().rdp_graph_last_shade_ms(self._h)
 
+    def last_blend_ms(self):
+        return lib().rdp_graph_last_blend_ms(self._h)
+
     def close(self):
         if self._h:
             lib().rdp_graph_destroy(self._h)
@@ -403,6 +440,36 @@ class Batch:
 
     def submit(self):
         _check(lib().rdp_batch_submit(self._h), "batch_submit")
+
+    def set_schedule(self, learned_order, train=False, learning_rate=1e-3, train_stride=1):
+        """Learned tile order on/off; online training of the tile-cost model on/off."""
+        _check(lib().rdp_batch_set_schedule(self._h, int(learned_order), int(train), learning_rate, train_stride),
+               "batch_set_schedule")
+
+    def get_model(self):
+        """(FP32 parameters of the tile-cost model, mean squared error of the last training step)."""
+        p = np.zeros(MLP_PARAMS, dtype=np.float32)
+        loss = ctypes.c_float()
+        _check(lib().rdp_batch_get_model(self._h, p.ctypes.data, ctypes.byref(loss)), "batch_get_model")
+        return p, loss.value
+
+    def tile_samples(self, max_tiles=1 << 22, features=True, predicted=True, cycles=True):
+        """The last launch's non-empty tiles: dict of features [n,16], predicted [n], cycles [n]."""
+        f = np.zeros((max_tiles, MLP_IN), dtype=np.float32) if features else None
+        p = np.zeros(max_tiles, dtype=np.float32) if predicted else None
+        c = np.zeros(max_tiles, dtype=np.uint32) if cycles else None
+        n = ctypes.c_uint32()
+        _check(lib().rdp_batch_get_tile_samples(self._h, f.ctypes.data if f is not None else None,
+                                                p.ctypes.data if p is not None else None,
+                                                c.ctypes.data if c is not None else None, max_tiles, ctypes.byref(n)),
+               "batch_get_tile_samples")
+        k = n.value
+        return {"features": f[:k] if f is not None else None, "predicted": p[:k] if p is not None else None,
+                "cycles": c[:k] if c is not None else None}
+
+    def set_model(self, params):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        _check(lib().rdp_batch_set_model(self._h, p.ctypes.data), "batch_set_model")
 
     def idle(self):
         _check(lib().rdp_batch_idle(self._h), "batch_idle")

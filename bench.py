@@ -494,6 +494,7 @@ def run_ours_batched(args):
     h2d = (bs1["staging_bytes"] - bs0["staging_bytes"]) / args.steps
     d2h = sum(st[3].width * st[3].height * (4 + 2) for st in streams)  # colour + depth images copied back
     rounds_per_step = (bs1["rounds"] - bs0["rounds"]) / args.steps
+    b_model = b.get_model()[0]
     b.close()
 
     # ---------------- plain: one processor + graph per instance, one after another
@@ -513,6 +514,11 @@ def run_ours_batched(args):
         cp.close()
     t_plain = _max_over_ranks(dist, plain_ms / 1e3)
     plain_value = total_passes / t_plain
+
+    # ---------------- serving: 256 instances, Poisson arrivals, continuous batching
+    serving = None
+    if not args.no_serving:
+        serving = _serving(args, local, model=b_model)
 
     # ---------------- roofline of the dominant kernel
     peaks = {}
@@ -557,6 +563,7 @@ def run_ours_batched(args):
                        "model_train_steps": args.train_steps, "model_mse": model_loss},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "mpix_per_s": total_frags / e2e_t / 1e6},
+        "serving": serving,
         "gpu_launches": int(launches),
         "roofline": {"kernel": "k_shade", "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_source": peak_src, "traffic": traffic,
@@ -575,6 +582,42 @@ def run_ours_batched(args):
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
+
+
+def _serving(args, device, model=None):
+    """The serving configuration: 256 instances with the batched workload's distribution of
+    resolutions and primitive counts submit frames as a Poisson process; requests are admitted by
+    HBM footprint; the learned tile order is on.  Runs the arrival rate of the configuration
+    (20,000 frames/s aggregate, over a short window) and a rate the GPU can sustain."""
+    from rdp_gb300 import Batch
+    from rdp_gb300.serving import latency_summary, poisson_trace
+    streams = _batched_streams(args.serve_instances)
+    frames = [st[0] for st in streams]
+    b = Batch(device=device)
+    if model is not None:
+        b.set_model(model)
+    b.set_schedule(learned_order=True, train=False)
+    insts = [b.add_instance(st[1].copy()) for st in streams]
+    for cp, w in zip(insts, frames):  # warm-up: every instance renders once, buffers settle
+        cp.enqueue_command(w)
+    b.idle()
+    for cp, w in zip(insts, frames):
+        cp.enqueue_command(w)
+    t0 = time.perf_counter()
+    b.idle()
+    capacity_fps = len(insts) / (time.perf_counter() - t0)
+    out = {"instances": len(insts), "hbm_budget_gb": args.serve_budget_gb, "capacity_fps_estimate": capacity_fps}
+    for tag, rate, dur in (("configured_rate", 20000.0, args.serve_window), ("sustainable", 0.5 * capacity_fps, 1.0)):
+        trace = poisson_trace(len(insts), rate, dur, frames, seed=42)
+        res, st = b.serve(insts, trace, hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)))
+        lat = latency_summary(res["latency_s"])
+        span = float(res["done_s"].max() - min(t[2] for t in trace)) if len(trace) else 0.0
+        lat.update({"rate_fps": rate, "window_s": dur, "throughput_fps": len(trace) / span if span > 0 else 0.0,
+                    "submits": st["submits"], "max_in_flight": st["max_in_flight"],
+                    "max_footprint_gb": st["max_footprint"] / (1 << 30)})
+        out[tag] = lat
+    b.close()
+    return out
 
 
 def run_reference_batched(args):
@@ -627,6 +670,10 @@ def main():
     ap.add_argument("--workload", default="batched", choices=["batched", "textured"])
     ap.add_argument("--instances", type=int, default=BATCH_INSTANCES)
     ap.add_argument("--train-steps", type=int, default=8, help="sync points of online cost-model training")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--serve-instances", type=int, default=256)
+    ap.add_argument("--serve-window", type=float, default=0.1, help="seconds of arrivals at the configured rate")
+    ap.add_argument("--serve-budget-gb", type=float, default=16.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":

@@ -245,6 +245,51 @@ int rdp_mlp_gradients(int device, const float *params, const float *features, co
                       float *grads, float *loss);
 int rdp_mlp_forward(int device, const float *params, const float *features, uint32_t n, float *out);
 
+/* Serving loop.  No counterpart in the reference.  Runs a trace of frame requests through a
+ * batch with continuous batching: a request arrives at arrival_s (open loop: seconds after the
+ * start of the call), waits in arrival order until the frames in flight leave room in the HBM
+ * budget (sum of footprint_bytes; 0 = estimated from num_words) and under max_in_flight, is then
+ * enqueued to its instance and signalled; every pass of admission is one rdp_batch_submit, so
+ * requests admitted while others are on the GPU share the following launches.  A request is
+ * complete when its instance's timeline value for it completes (framebuffer copied back to the
+ * instance's RDRAM).  All instance state stays resident on the device throughout.  Frames of one
+ * instance render in arrival order, so each result equals rendering that instance's requests
+ * alone. */
+typedef struct rdp_serve_request
+{
+	uint32_t instance;        /* index into the instances array */
+	uint32_t num_words;
+	const uint32_t *words;    /* the frame's RDP command words (host memory, alive during the call) */
+	double arrival_s;
+	uint64_t footprint_bytes; /* transient HBM the frame needs in flight; 0: estimated */
+} rdp_serve_request;
+
+typedef struct rdp_serve_config
+{
+	uint64_t hbm_budget_bytes; /* admission limit on the summed footprint of frames in flight */
+	uint32_t max_in_flight;    /* 0: no limit */
+	double timeout_s;          /* the call returns RDP_ERR_TIMEOUT after this long */
+} rdp_serve_config;
+
+typedef struct rdp_serve_result
+{
+	double admit_s;   /* admission (enqueue) time */
+	double done_s;    /* completion time as seen by the loop */
+	double latency_s; /* done_s - arrival_s */
+} rdp_serve_result;
+
+typedef struct rdp_serve_stats
+{
+	uint64_t submits;        /* rdp_batch_submit calls */
+	uint64_t max_in_flight;  /* largest number of frames in flight */
+	uint64_t max_footprint;  /* largest summed footprint in flight (bytes) */
+	double elapsed_s;
+} rdp_serve_stats;
+
+int rdp_serve_run(rdp_batch *b, rdp_cp *const *instances, uint32_t num_instances, const rdp_serve_request *requests,
+                  uint32_t num_requests, const rdp_serve_config *config, rdp_serve_result *results,
+                  rdp_serve_stats *stats);
+
 /* Kernel specialisation.  No counterpart in the reference (its shaders are specialised per
  * render-state variant by its pipeline compiler).  The shading kernel is compiled for
  * RDP_SHADE_VARIANTS register budgets; by default an autotuner times them on the first

@@ -2159,4 +2159,108 @@ int rdp_batch_get_tile_samples(rdp_batch *b, float *features, float *predicted, 
 	return RDP_OK;
 }
 
+int rdp_serve_run(rdp_batch *b, rdp_cp *const *instances, uint32_t num_instances, const rdp_serve_request *requests,
+                  uint32_t num_requests, const rdp_serve_config *config, rdp_serve_result *results,
+                  rdp_serve_stats *stats)
+{
+	if (!b || !instances || !num_instances || (num_requests && (!requests || !results)) || !config) return RDP_ERR_INVALID;
+	for (uint32_t i = 0; i < num_instances; i++)
+		if (!instances[i] || instances[i]->batch != b) return RDP_ERR_INVALID;
+	for (uint32_t r = 0; r < num_requests; r++)
+	{
+		if (requests[r].instance >= num_instances || (requests[r].num_words && !requests[r].words)) return RDP_ERR_INVALID;
+		if (r && requests[r].arrival_s < requests[r - 1].arrival_s) return RDP_ERR_INVALID; // sorted by arrival
+	}
+	cudaSetDevice(b->device);
+	using clock = std::chrono::steady_clock;
+	const auto t0 = clock::now();
+	auto now_s = [&] { return std::chrono::duration<double>(clock::now() - t0).count(); };
+	// Footprint estimate: primitive records, staging and ~8 shaded (primitive, tile) pairs per primitive.
+	auto footprint = [](const rdp_serve_request &q) -> uint64_t {
+		if (q.footprint_bytes) return q.footprint_bytes;
+		uint64_t prims = q.num_words / 20 + 1;
+		return prims * (336 + 8 * 648) + uint64_t(q.num_words) * 4;
+	};
+	struct Flight
+	{
+		uint32_t req;
+		uint64_t value, bytes;
+	};
+	std::deque<uint32_t> waiting;
+	std::vector<Flight> flying;
+	uint32_t next = 0, done = 0;
+	uint64_t in_bytes = 0;
+	rdp_serve_stats st = {};
+	int r = RDP_OK;
+	while (done < num_requests)
+	{
+		const double t = now_s();
+		if (t > config->timeout_s)
+		{
+			r = RDP_ERR_TIMEOUT;
+			break;
+		}
+		bool progress = false;
+		while (next < num_requests && requests[next].arrival_s <= t) waiting.push_back(next++);
+		// Completions.
+		for (size_t k = 0; k < flying.size();)
+		{
+			rdp_cp *cp = instances[requests[flying[k].req].instance];
+			int w = cp->wait_timeline(flying[k].value, 0);
+			if (w == RDP_ERR_TIMEOUT)
+			{
+				k++;
+				continue;
+			}
+			if (w != RDP_OK)
+			{
+				r = w;
+				break;
+			}
+			rdp_serve_result &res = results[flying[k].req];
+			res.done_s = now_s();
+			res.latency_s = res.done_s - requests[flying[k].req].arrival_s;
+			in_bytes -= flying[k].bytes;
+			flying[k] = flying.back();
+			flying.pop_back();
+			done++;
+			progress = true;
+		}
+		if (r != RDP_OK) break;
+		// Admission in arrival order while the budget has room (at least one frame always fits).
+		bool admitted = false;
+		while (!waiting.empty())
+		{
+			const uint32_t q = waiting.front();
+			const uint64_t fp = footprint(requests[q]);
+			if (!flying.empty() && (in_bytes + fp > config->hbm_budget_bytes ||
+			                        (config->max_in_flight && flying.size() >= config->max_in_flight)))
+				break;
+			rdp_cp *cp = instances[requests[q].instance];
+			if ((r = cp->enqueue(requests[q].num_words, requests[q].words)) != RDP_OK) break;
+			uint64_t v = 0;
+			if ((r = cp->signal_timeline(&v)) != RDP_OK) break;
+			results[q].admit_s = now_s();
+			flying.push_back(Flight{ q, v, fp });
+			in_bytes += fp;
+			st.max_in_flight = std::max<uint64_t>(st.max_in_flight, flying.size());
+			st.max_footprint = std::max(st.max_footprint, in_bytes);
+			waiting.pop_front();
+			admitted = true;
+		}
+		if (r != RDP_OK) break;
+		if (admitted)
+		{
+			// One submission for everything admitted in this pass: the new frames share launches.
+			if ((r = b->submit()) != RDP_OK) break;
+			st.submits++;
+			progress = true;
+		}
+		if (!progress) std::this_thread::yield();
+	}
+	st.elapsed_s = now_s();
+	if (stats) *stats = st;
+	return r;
+}
+
 } // extern "C"

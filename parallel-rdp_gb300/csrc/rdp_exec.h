@@ -174,13 +174,58 @@ struct Executor
 	uint16_t *d_sc_misc = nullptr;
 	uint8_t *d_staging = nullptr;
 
+	// Pinned host staging buffers, used round-robin; a buffer is reused once the H2D copy
+	// that read it has completed.  Up to kMaxStaging of them let the host record launches
+	// ahead of the GPU (the serving loop keeps admitting while earlier launches run).
+	static constexpr size_t kMaxStaging = 8;
 	struct Staging
 	{
 		uint8_t *h = nullptr;
+		size_t size = 0;
 		cudaEvent_t done = nullptr;
 		bool in_flight = false;
-	} staging[2];
-	int staging_index = 0;
+	};
+	std::vector<Staging> staging;
+	size_t staging_next = 0;
+
+	// A host staging buffer of at least `bytes` whose previous copy has completed.
+	Staging *take_staging(size_t bytes)
+	{
+		Staging *pick = nullptr;
+		for (size_t k = 0; k < staging.size() && !pick; k++)
+		{
+			Staging &st = staging[(staging_next + k) % staging.size()];
+			if (!st.in_flight || cudaEventQuery(st.done) == cudaSuccess)
+			{
+				st.in_flight = false;
+				pick = &st;
+			}
+		}
+		cudaGetLastError();
+		if (!pick && staging.size() < kMaxStaging)
+		{
+			staging.emplace_back();
+			pick = &staging.back();
+			if (check(cudaEventCreateWithFlags(&pick->done, cudaEventDisableTiming))) return nullptr;
+		}
+		if (!pick)
+		{
+			pick = &staging[staging_next % staging.size()];
+			if (check(cudaEventSynchronize(pick->done))) return nullptr;
+			pick->in_flight = false;
+		}
+		staging_next = size_t(pick - staging.data()) + 1;
+		if (pick->size < bytes)
+		{
+			if (pick->h) cudaFreeHost(pick->h);
+			pick->h = nullptr;
+			pick->size = 0;
+			size_t n = std::max(bytes, pick->size + pick->size / 2);
+			if (check(cudaMallocHost(&pick->h, n))) return nullptr;
+			pick->size = n;
+		}
+		return pick;
+	}
 
 	bool record_cycles = false, cycles_requested = false;
 
@@ -284,8 +329,6 @@ struct Executor
 		for (int v = 0; v < RDP_SHADE_VARIANTS; v++) shade_ctas_v[v] = uint32_t(sms) * uint32_t(rdp_kernels_shade_ctas_per_sm(v));
 		blend_ctas = uint32_t(sms) * uint32_t(rdp_kernels_blend_ctas_per_sm());
 		tuner.active = shade_variant_choice(device) < 0;
-		for (auto &st : staging)
-			if (check(cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming))) return false;
 		if (check(cudaMalloc(&d_ctrl, 32)) || check(cudaMalloc(&d_pair_log, 256 * 4))) return false;
 		return !check(cudaMemsetAsync(d_ctrl, 0, 32, stream));
 	}
@@ -402,8 +445,8 @@ struct Executor
 		{
 			if (st.h) cudaFreeHost(st.h);
 			if (st.done) cudaEventDestroy(st.done);
-			st = Staging{};
 		}
+		staging.clear();
 	}
 
 	// Grows the buffers to hold `need`.  Called with the stream idle.
@@ -484,12 +527,6 @@ struct Executor
 			cudaFree(d_staging);
 			d_staging = nullptr;
 			if (check(cudaMalloc(&d_staging, n))) return false;
-			for (auto &st : staging)
-			{
-				if (st.h) cudaFreeHost(st.h);
-				st.h = nullptr;
-				if (check(cudaMallocHost(&st.h, n))) return false;
-			}
 			caps.staging = n;
 		}
 		return !check(cudaStreamSynchronize(stream));
@@ -539,13 +576,9 @@ struct Executor
 		need.staging = std::max(need.staging, staging_bytes_for(v, n));
 		if (!ensure(need)) return false;
 
-		Staging &st = staging[staging_index];
-		staging_index ^= 1;
-		if (st.in_flight)
-		{
-			if (check(cudaEventSynchronize(st.done))) return false;
-			st.in_flight = false;
-		}
+		Staging *stp = take_staging(staging_bytes_for(v, n));
+		if (!stp) return false;
+		Staging &st = *stp;
 		uint8_t *h = st.h;
 		size_t off = 0;
 		auto reserve = [&](size_t bytes) -> size_t {

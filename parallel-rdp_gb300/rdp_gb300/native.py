@@ -95,7 +95,27 @@ EXPORTED_SYMBOLS = [
     "rdp_batch_get_stats", "rdp_batch_capture_begin", "rdp_batch_capture_end", "rdp_set_shade_variant",
     "rdp_get_shade_variant", "rdp_batch_set_schedule", "rdp_batch_get_model", "rdp_batch_set_model",
     "rdp_mlp_gradients", "rdp_mlp_forward", "rdp_batch_get_tile_samples", "rdp_graph_last_blend_ms",
+    "rdp_serve_run",
 ]
+
+
+class _ServeRequest(ctypes.Structure):
+    _fields_ = [("instance", ctypes.c_uint32), ("num_words", ctypes.c_uint32), ("words", ctypes.c_void_p),
+                ("arrival_s", ctypes.c_double), ("footprint_bytes", ctypes.c_uint64)]
+
+
+class _ServeConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_in_flight", ctypes.c_uint32),
+                ("timeout_s", ctypes.c_double)]
+
+
+class _ServeResult(ctypes.Structure):
+    _fields_ = [("admit_s", ctypes.c_double), ("done_s", ctypes.c_double), ("latency_s", ctypes.c_double)]
+
+
+class _ServeStats(ctypes.Structure):
+    _fields_ = [("submits", ctypes.c_uint64), ("max_in_flight", ctypes.c_uint64), ("max_footprint", ctypes.c_uint64),
+                ("elapsed_s", ctypes.c_double)]
 
 
 class _BatchCreateInfo(ctypes.Structure):
@@ -178,6 +198,7 @@ def lib():
     L.rdp_batch_get_tile_samples.argtypes = [vp, vp, vp, vp, u32, ctypes.POINTER(u32)]
     L.rdp_mlp_gradients.argtypes = [ctypes.c_int, vp, vp, vp, u32, vp, ctypes.POINTER(ctypes.c_float)]
     L.rdp_mlp_forward.argtypes = [ctypes.c_int, vp, vp, u32, vp]
+    L.rdp_serve_run.argtypes = [vp, vp, u32, vp, u32, ctypes.POINTER(_ServeConfig), vp, ctypes.POINTER(_ServeStats)]
     L.rdp_batch_create.argtypes = [ctypes.POINTER(_BatchCreateInfo), ctypes.POINTER(vp)]
     L.rdp_batch_destroy.argtypes = [vp]
     L.rdp_batch_add_instance.argtypes = [vp, ctypes.POINTER(_CreateInfo), ctypes.POINTER(vp)]
@@ -466,6 +487,28 @@ class Batch:
         k = n.value
         return {"features": f[:k] if f is not None else None, "predicted": p[:k] if p is not None else None,
                 "cycles": c[:k] if c is not None else None}
+
+    def serve(self, instances, requests, hbm_budget_bytes=16 << 30, max_in_flight=0, timeout_s=600.0):
+        """Runs a request trace through the serving loop (rdp_serve_run).
+
+        instances: CommandProcessors of this batch; requests: sequence of
+        (instance index, words uint32 array, arrival seconds), sorted by arrival.
+        Returns (dict of numpy arrays admit_s / done_s / latency_s, stats dict)."""
+        n = len(requests)
+        reqs = (_ServeRequest * max(n, 1))()
+        keep = []
+        for i, (inst, words, arrival) in enumerate(requests):
+            w = np.ascontiguousarray(words, dtype=np.uint32)
+            keep.append(w)
+            reqs[i] = _ServeRequest(int(inst), w.size, w.ctypes.data, float(arrival), 0)
+        handles = (ctypes.c_void_p * len(instances))(*[cp._h.value for cp in instances])
+        res = (_ServeResult * max(n, 1))()
+        st = _ServeStats()
+        cfg = _ServeConfig(int(hbm_budget_bytes), int(max_in_flight), float(timeout_s))
+        _check(lib().rdp_serve_run(self._h, handles, len(instances), reqs, n, ctypes.byref(cfg), res, ctypes.byref(st)),
+               "serve_run")
+        out = {k: np.array([getattr(res[i], k) for i in range(n)]) for k in ("admit_s", "done_s", "latency_s")}
+        return out, {k: getattr(st, k) for k, _ in _ServeStats._fields_}
 
     def set_model(self, params):
         p = np.ascontiguousarray(params, dtype=np.float32)

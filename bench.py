@@ -398,9 +398,8 @@ def _oracle_instances(streams, min_seconds=None, threads=None):
 
 
 def _run_batch_step(b, insts, streams):
-    for cp, st in zip(insts, streams):
-        cp.enqueue_command(st[0])
-    values = [cp.signal_timeline() for cp in insts]
+    # Command words of every instance parsed on host threads, then one submission.
+    values = b.enqueue_many(insts, [st[0] for st in streams])
     b.submit()
     for cp, v in zip(insts, values):
         cp.wait_for_timeline(v)
@@ -424,7 +423,7 @@ def run_ours_batched(args):
     s1 = [cp.stats() for cp in insts]
     b.idle()  # grows the pair scratch to what the sync point needed
     from rdp_gb300 import get_shade_variant
-    for _ in range(8):  # the autotuner times the shading-kernel variants on the first sync points
+    for _ in range(12):  # the autotuner times the shading-kernel variants on the first sync points
         if get_shade_variant(local) >= 0:
             break
         _run_batch_step(b, insts, streams)

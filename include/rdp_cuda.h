@@ -217,6 +217,11 @@ int rdp_batch_submit(rdp_batch *b);
 /* rdp_batch_submit, then waits until the batch's stream is idle. */
 int rdp_batch_idle(rdp_batch *b);
 int rdp_batch_get_stats(rdp_batch *b, rdp_batch_stats *out);
+/* rdp_cp_enqueue for many instances of the batch at once, parsed on `threads` host threads
+ * (0: one per core); with timeline_values, each instance is also signalled
+ * (rdp_cp_signal_timeline) and its value stored.  Instances must be distinct. */
+int rdp_batch_enqueue_many(rdp_batch *b, uint32_t count, rdp_cp *const *instances, const uint32_t *const *words,
+                           const uint32_t *num_words, uint64_t *timeline_values, uint32_t threads);
 /* Sync-point capture over all instances: between begin and end, deferred passes are recorded
  * (as rdp_cp_capture_begin/end do for one processor) and the graph replays all rounds. */
 int rdp_batch_capture_begin(rdp_batch *b);
@@ -292,11 +297,11 @@ int rdp_serve_run(rdp_batch *b, rdp_cp *const *instances, uint32_t num_instances
 
 /* Kernel specialisation.  No counterpart in the reference (its shaders are specialised per
  * render-state variant by its pipeline compiler).  The shading kernel is compiled for
- * RDP_SHADE_VARIANTS register budgets; by default an autotuner times them on the first
- * launches of a device and keeps the fastest per shaded (primitive, tile) pair.  All
- * variants give identical results.  rdp_set_shade_variant forces one (0..3) or restarts
- * tuning (-1); rdp_get_shade_variant returns the device's choice, -1 while tuning. */
-#define RDP_SHADE_VARIANTS 4
+ * RDP_SHADE_VARIANTS variants (two kernel shapes, four register budgets each); by default an
+ * autotuner times them on the first launches of a device and keeps the fastest per shaded
+ * (primitive, tile) pair.  All variants give identical results.  rdp_set_shade_variant forces
+ * one (0..7) or restarts tuning (-1); rdp_get_shade_variant returns the device's choice, -1 while tuning. */
+#define RDP_SHADE_VARIANTS 8
 int rdp_set_shade_variant(int device, int variant);
 int rdp_get_shade_variant(int device);
 

@@ -21,6 +21,7 @@
 #include <string.h>
 #include <stdlib.h>
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <deque>
@@ -449,6 +450,7 @@ struct rdp_cp
 			return sticky_error;
 		}
 
+		const size_t num_recorded_prims = prims.size(), num_recorded_uploads = uploads.size();
 		rdpx::PassView v = {};
 		RdpPass common = {};
 		common.rdram = d_rdram;
@@ -514,14 +516,18 @@ struct rdp_cp
 
 		if (batch)
 		{
+			// The recorded buffers move into the deferred packet (reset_pass clears them anyway).
 			rdpx::PassPacket pk;
 			pk.targets.assign(v.target, v.target + v.num_targets);
 			pk.target_prims.assign(v.target_prims, v.target_prims + v.num_targets);
-			pk.prims.assign(v.prims, v.prims + v.num_prims);
-			pk.words = words;
-			pk.state_blocks = state_blocks;
-			pk.tilesets = tilesets;
-			pk.uploads = uploads;
+			if (v.prims == prims.data() && v.num_prims == prims.size())
+				pk.prims = std::move(prims);
+			else
+				pk.prims.assign(v.prims, v.prims + v.num_prims);
+			pk.words = std::move(words);
+			pk.state_blocks = std::move(state_blocks);
+			pk.tilesets = std::move(tilesets);
+			pk.uploads = std::move(uploads);
 			deferred.push_back(std::move(pk));
 		}
 		else
@@ -532,9 +538,9 @@ struct rdp_cp
 		}
 
 		stats.passes++;
-		stats.primitives += prims.size();
-		stats.tmem_uploads += uploads.size();
-		base_prim_index += prims.size();
+		stats.primitives += num_recorded_prims;
+		stats.tmem_uploads += num_recorded_uploads;
+		base_prim_index += num_recorded_prims;
 		reset_pass();
 		return sticky_error;
 	}
@@ -2261,6 +2267,40 @@ int rdp_serve_run(rdp_batch *b, rdp_cp *const *instances, uint32_t num_instances
 	st.elapsed_s = now_s();
 	if (stats) *stats = st;
 	return r;
+}
+
+int rdp_batch_enqueue_many(rdp_batch *b, uint32_t count, rdp_cp *const *instances, const uint32_t *const *words,
+                           const uint32_t *num_words, uint64_t *timeline_values, uint32_t threads)
+{
+	if (!b || (count && (!instances || !words || !num_words))) return RDP_ERR_INVALID;
+	for (uint32_t i = 0; i < count; i++)
+		if (!instances[i] || instances[i]->batch != b) return RDP_ERR_INVALID;
+	if (!threads) threads = std::max(1u, std::thread::hardware_concurrency());
+	threads = std::min(threads, std::max(count, 1u));
+	cudaSetDevice(b->device);
+	std::vector<int> status(count, RDP_OK);
+	std::atomic<uint32_t> next(0);
+	auto work = [&] {
+		cudaSetDevice(b->device);
+		for (;;)
+		{
+			uint32_t i = next.fetch_add(1);
+			if (i >= count) break;
+			rdp_cp *cp = instances[i];
+			int r = cp->enqueue(num_words[i], words[i]);
+			uint64_t v = 0;
+			if (r == RDP_OK && timeline_values) r = cp->signal_timeline(&v);
+			if (timeline_values) timeline_values[i] = v;
+			status[i] = r;
+		}
+	};
+	std::vector<std::thread> pool;
+	for (uint32_t t = 1; t < threads; t++) pool.emplace_back(work);
+	work();
+	for (auto &t : pool) t.join();
+	for (int r : status)
+		if (r != RDP_OK) return r;
+	return RDP_OK;
 }
 
 } // extern "C"

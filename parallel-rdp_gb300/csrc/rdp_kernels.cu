@@ -2675,6 +2675,125 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass
 	}
 }
 
+// Compacted shading: a CTA of COMPACT_THREADS takes COMPACT_PAIRS consecutive pairs, computes
+// their spans into shared memory, marks the pixels that lie inside a valid span (only those can
+// have coverage), and shades just those -- about half of a tile's pixels on typical scenes, so
+// lanes no longer idle on uncovered pixels.  Results are identical to k_shade.
+constexpr int COMPACT_THREADS = 128;
+constexpr int COMPACT_PAIRS = 4;
+
+template <int MIN_CTAS>
+__global__ void __launch_bounds__(COMPACT_THREADS, MIN_CTAS)
+	k_shade_compact(const RdpPass *__restrict__ passes, uint32_t num_passes, const uint2 *__restrict__ pairs,
+	                const uint32_t *__restrict__ ctrl, const RdpPrimGeom *__restrict__ geom,
+	                const RdpPrimAttr *__restrict__ attr, const RdpPrimShade *__restrict__ shade,
+	                const RdpTile *__restrict__ tilesets, uint32_t *__restrict__ sc_color, int *__restrict__ sc_zdith,
+	                uint16_t *__restrict__ sc_misc)
+{
+	__shared__ SpanA s_sa[COMPACT_PAIRS][9];
+	__shared__ SpanX s_sx[COMPACT_PAIRS][9];
+	__shared__ uint32_t s_prim[COMPACT_PAIRS], s_pass[COMPACT_PAIRS], s_tile[COMPACT_PAIRS];
+	__shared__ uint16_t s_list[COMPACT_PAIRS * 64];
+	__shared__ uint32_t s_count;
+	if (ctrl[1]) return;
+	const uint32_t total = ctrl[0];
+	const uint32_t groups = (total + COMPACT_PAIRS - 1) / COMPACT_PAIRS;
+	const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+	for (uint32_t grp = blockIdx.x; grp < groups; grp += gridDim.x)
+	{
+		const uint32_t pr0 = grp * COMPACT_PAIRS;
+		const uint32_t npr = min(uint32_t(COMPACT_PAIRS), total - pr0);
+		if (tid < COMPACT_PAIRS)
+		{
+			if (uint32_t(tid) < npr)
+			{
+				const uint2 pa = pairs[pr0 + tid];
+				const uint32_t pi = pass_of_item(passes, num_passes, pa.y);
+				s_prim[tid] = pa.x;
+				s_pass[tid] = pi;
+				s_tile[tid] = pa.y - passes[pi].tile_item_begin;
+			}
+		}
+		if (tid == 0) s_count = 0;
+		__syncthreads();
+		// Spans: COMPACT_PAIRS x 9 rows x {attribute, x} tasks.
+		for (int task = tid; task < COMPACT_PAIRS * 18; task += COMPACT_THREADS)
+		{
+			const int gi = task / 18, kind = (task % 18) / 9, row = task % 9;
+			if (uint32_t(gi) < npr)
+			{
+				const RdpPass &ps = passes[s_pass[gi]];
+				const int ty = int(s_tile[gi] / ps.tiles_x);
+				const RdpPrimGeom &g = geom[s_prim[gi]];
+				if (kind == 0) span_attr(g, attr[s_prim[gi]], ty * 8 + row, s_sa[gi][row]);
+				else span_x(g, ty * 8 + row, s_sx[gi][row]);
+			}
+		}
+		__syncthreads();
+		// Candidate pixels (inside a valid span of their row); the rest are written as empty.
+		for (int slot = tid; slot < COMPACT_PAIRS * 64; slot += COMPACT_THREADS)
+		{
+			const int gi = slot >> 6, px = slot & 63;
+			bool cand = false;
+			if (uint32_t(gi) < npr)
+			{
+				const RdpPass &ps = passes[s_pass[gi]];
+				const uint32_t tl = s_tile[gi];
+				const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
+				const int r = px >> 3, x = tx * 8 + (px & 7), y = ty * 8 + r;
+				const RdpPrimGeom &g = geom[s_prim[gi]];
+				const SpanX &sx = s_sx[gi][r];
+				cand = x < int(ps.fb_width) && y < int(ps.fb_height) && y >= g.span_ylo && y <= g.span_yhi && sx.valid &&
+				       x >= sx.start_x && x <= sx.end_x;
+				if (!cand)
+				{
+					const size_t at = size_t(pr0 + gi) * SHADE_THREADS + px;
+					sc_color[at] = 0u;
+					sc_zdith[at] = 0;
+					sc_misc[at] = 0x00ffu;
+				}
+			}
+			const unsigned m = __ballot_sync(0xffffffffu, cand);
+			uint32_t base = 0;
+			if (lane == 0 && m) base = atomicAdd(&s_count, uint32_t(__popc(m)));
+			base = __shfl_sync(0xffffffffu, base, 0);
+			if (cand) s_list[base + __popc(m & ((1u << lane) - 1u))] = uint16_t(slot);
+		}
+		__syncthreads();
+		const uint32_t count = s_count;
+		for (uint32_t i = tid; i < count; i += COMPACT_THREADS)
+		{
+			const int slot = s_list[i];
+			const int gi = slot >> 6, px = slot & 63;
+			const RdpPass &ps = passes[s_pass[gi]];
+			const uint32_t tl = s_tile[gi];
+			const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
+			const int r = px >> 3, x = tx * 8 + (px & 7), y = ty * 8 + r;
+			PassConst pc;
+			switch (ps.fb_fmt)
+			{
+			case FBF_I4: pc.fb_size = 0; pc.dx_mask = 0; pc.dx_shift = 0; break;
+			case FBF_I8: pc.fb_size = 1; pc.dx_mask = ~7; pc.dx_shift = 3; break;
+			case FBF_RGBA5551:
+			case FBF_IA88: pc.fb_size = 2; pc.dx_mask = ~3; pc.dx_shift = 2; break;
+			default: pc.fb_size = 4; pc.dx_mask = ~1; pc.dx_shift = 1; break;
+			}
+			pc.alias = ps.fb_addr == ps.depth_addr;
+			const uint32_t prim = s_prim[gi];
+			const RdpPrimShade &sh = shade[prim];
+			Shaded out;
+			const bool ok = shade_pixel(pc, geom[prim], attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
+			                            ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, s_sa[gi][r], s_sx[gi][r],
+			                            s_sa[gi][r + 1], s_sx[gi][r + 1], x, y, out);
+			const size_t at = size_t(pr0 + gi) * SHADE_THREADS + px;
+			sc_color[at] = ok ? out.combined : 0u;
+			sc_zdith[at] = ok ? out.z_dith : 0;
+			sc_misc[at] = ok ? uint16_t((out.coverage & 0xff) | (out.shade_alpha << 8)) : uint16_t(0x00ffu);
+		}
+		__syncthreads();
+	}
+}
+
 // ============================================================================ k_blend
 // One 64-thread CTA per tile: the tile's colour/depth stay in registers while its pairs are
 // applied in primitive order (the reference's depth_blend.comp), then written back.
@@ -2942,8 +3061,14 @@ extern "C" cudaError_t rdp_kernels_init_luts(const uint8_t *blender_lut)
 namespace {
 typedef void (*ShadeKernel)(const RdpPass *, uint32_t, const uint2 *, const uint32_t *, const RdpPrimGeom *,
                             const RdpPrimAttr *, const RdpPrimShade *, const RdpTile *, uint32_t *, int *, uint16_t *);
-const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = { rdp::k_shade<1>, rdp::k_shade<12>, rdp::k_shade<16>,
-                                                         rdp::k_shade<24> };
+const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = { rdp::k_shade<1>,         rdp::k_shade<12>,
+                                                         rdp::k_shade<16>,        rdp::k_shade<24>,
+                                                         rdp::k_shade_compact<1>, rdp::k_shade_compact<6>,
+                                                         rdp::k_shade_compact<8>, rdp::k_shade_compact<12> };
+// Threads per CTA of each variant.
+const int kShadeThreads[RDP_SHADE_VARIANTS] = { rdp::SHADE_THREADS,    rdp::SHADE_THREADS,    rdp::SHADE_THREADS,
+                                                rdp::SHADE_THREADS,    rdp::COMPACT_THREADS, rdp::COMPACT_THREADS,
+                                                rdp::COMPACT_THREADS, rdp::COMPACT_THREADS };
 } // namespace
 
 extern "C" int rdp_kernels_blend_ctas_per_sm(void)
@@ -2957,7 +3082,8 @@ extern "C" int rdp_kernels_shade_ctas_per_sm(int variant)
 {
 	if (variant < 0 || variant >= RDP_SHADE_VARIANTS) variant = 0;
 	int n = 0;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kShadeVariants[variant], rdp::SHADE_THREADS, 0) != cudaSuccess)
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kShadeVariants[variant], kShadeThreads[variant], 0) !=
+	    cudaSuccess)
 		n = 8;
 	return n > 0 ? n : 1;
 }
@@ -3015,8 +3141,9 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 			return cudaGetLastError();
 		const unsigned ev_flags = capture == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
 		if (L->shade_events[0]) cudaEventRecordWithFlags(L->shade_events[0], stream, ev_flags);
-		const ShadeKernel shade_kernel = kShadeVariants[L->shade_variant < RDP_SHADE_VARIANTS ? L->shade_variant : 0];
-		shade_kernel<<<L->shade_ctas, rdp::SHADE_THREADS, 0, stream>>>(L->passes, L->num_passes, L->pairs, L->ctrl,
+		const uint32_t sv = L->shade_variant < RDP_SHADE_VARIANTS ? L->shade_variant : 0;
+		const ShadeKernel shade_kernel = kShadeVariants[sv];
+		shade_kernel<<<L->shade_ctas, kShadeThreads[sv], 0, stream>>>(L->passes, L->num_passes, L->pairs, L->ctrl,
 		                                                               L->geom, L->attr, L->shade, L->tilesets,
 		                                                               L->sc_color, L->sc_zdith, L->sc_misc);
 		if (L->shade_events[1]) cudaEventRecordWithFlags(L->shade_events[1], stream, ev_flags);

@@ -5,9 +5,11 @@
 #include <cuda_runtime.h>
 #include "rdp_types.h"
 
-/* k_shade is compiled for minimum residencies of 1, 12, 16 and 24 CTAs per SM. */
+/* Shading kernels: k_shade (one pair per 64-thread CTA) for minimum residencies of 1, 12, 16
+ * and 24 CTAs per SM, and k_shade_compact (4 pairs per 128-thread CTA, covered pixels only)
+ * for 1, 6, 8 and 12. */
 #ifndef RDP_SHADE_VARIANTS
-#define RDP_SHADE_VARIANTS 4
+#define RDP_SHADE_VARIANTS 8
 #endif
 
 typedef struct RdpLaunch

@@ -95,7 +95,7 @@ EXPORTED_SYMBOLS = [
     "rdp_batch_get_stats", "rdp_batch_capture_begin", "rdp_batch_capture_end", "rdp_set_shade_variant",
     "rdp_get_shade_variant", "rdp_batch_set_schedule", "rdp_batch_get_model", "rdp_batch_set_model",
     "rdp_mlp_gradients", "rdp_mlp_forward", "rdp_batch_get_tile_samples", "rdp_graph_last_blend_ms",
-    "rdp_serve_run",
+    "rdp_serve_run", "rdp_batch_enqueue_many",
 ]
 
 
@@ -203,6 +203,7 @@ def lib():
     L.rdp_batch_destroy.argtypes = [vp]
     L.rdp_batch_add_instance.argtypes = [vp, ctypes.POINTER(_CreateInfo), ctypes.POINTER(vp)]
     L.rdp_batch_submit.argtypes = [vp]
+    L.rdp_batch_enqueue_many.argtypes = [vp, u32, vp, vp, vp, vp, u32]
     L.rdp_batch_idle.argtypes = [vp]
     L.rdp_batch_get_stats.argtypes = [vp, ctypes.POINTER(_BatchStats)]
     L.rdp_batch_capture_begin.argtypes = [vp]
@@ -211,11 +212,11 @@ def lib():
     return L
 
 
-SHADE_VARIANTS = 4
+SHADE_VARIANTS = 8
 
 
 def set_shade_variant(variant, device=0):
-    """Forces the shading-kernel variant (0..3) of a device, or restarts autotuning (-1)."""
+    """Forces the shading-kernel variant (0..7) of a device, or restarts autotuning (-1)."""
     _check(lib().rdp_set_shade_variant(device, variant), "set_shade_variant")
 
 
@@ -461,6 +462,17 @@ class Batch:
 
     def submit(self):
         _check(lib().rdp_batch_submit(self._h), "batch_submit")
+
+    def enqueue_many(self, instances, words_list, signal=True, threads=0):
+        """Enqueues words_list[i] to instances[i] on host threads; returns timeline values when signal."""
+        n = len(instances)
+        arrs = [np.ascontiguousarray(w, dtype=np.uint32) for w in words_list]
+        handles = (ctypes.c_void_p * n)(*[cp._h.value for cp in instances])
+        ptrs = (ctypes.c_void_p * n)(*[a.ctypes.data for a in arrs])
+        counts = (ctypes.c_uint32 * n)(*[a.size for a in arrs])
+        values = (ctypes.c_uint64 * n)() if signal else None
+        _check(lib().rdp_batch_enqueue_many(self._h, n, handles, ptrs, counts, values, threads), "batch_enqueue_many")
+        return list(values) if signal else None
 
     def set_schedule(self, learned_order, train=False, learning_rate=1e-3, train_stride=1):
         """Learned tile order on/off; online training of the tile-cost model on/off."""

@@ -100,3 +100,18 @@ def test_batch_instance_destroy_keeps_others():
         for cp, (w, rd) in zip(insts[1:], streams[1:]):
             s_rd, _, _, _ = run_gpu(w, rd)
             assert np.array_equal(cp.begin_read_rdram(), s_rd)
+
+
+def test_enqueue_many_matches_sequential():
+    streams = _instance_streams(8, 1200, seed_base=70)
+    with Batch() as b:
+        insts = [b.add_instance(np.array(rd, copy=True)) for _, rd in streams]
+        values = b.enqueue_many(insts, [w for w, _ in streams])
+        b.submit()
+        for cp, v in zip(insts, values):
+            cp.wait_for_timeline(v)
+        for cp, (w, rd) in zip(insts, streams):
+            s_rd, s_hid, _, stats = run_gpu(w, rd)
+            assert np.array_equal(cp.begin_read_rdram(), s_rd)
+            assert np.array_equal(cp.begin_read_hidden_rdram(), s_hid)
+            assert cp.stats()["reference_passes"] == stats["reference_passes"]

@@ -295,6 +295,23 @@ int rdp_serve_run(rdp_batch *b, rdp_cp *const *instances, uint32_t num_instances
                   uint32_t num_requests, const rdp_serve_config *config, rdp_serve_result *results,
                   rdp_serve_stats *stats);
 
+/* RDPDUMP2 capture files (the reference's format: parallel-rdp/rdp_dump_write.cpp, rdp_dump.cpp).
+ * The writer mirrors RDP::RDPDumpWriter (init, flush_dram, flush_hidden_dram, emit_command,
+ * set_vi_register, end_frame, signal_complete); rdp_dump_replay plays a file into a processor
+ * as the reference's replayer does (replayer_driver_parallel.cpp) and calls on_frame with the
+ * RGBA8 scanout of every end-of-frame record. */
+typedef struct rdp_dump_writer rdp_dump_writer;
+typedef void (*rdp_dump_frame_cb)(void *user, uint32_t frame, const uint32_t *rgba, uint32_t width, uint32_t height);
+int rdp_dump_writer_open(const char *path, uint32_t rdram_size, uint32_t hidden_rdram_size, rdp_dump_writer **out);
+int rdp_dump_writer_flush_rdram(rdp_dump_writer *w, const void *rdram, uint32_t size);
+int rdp_dump_writer_flush_hidden_rdram(rdp_dump_writer *w, const void *hidden, uint32_t size);
+int rdp_dump_writer_command(rdp_dump_writer *w, uint32_t op, const uint32_t *words, uint32_t num_words);
+int rdp_dump_writer_set_vi_register(rdp_dump_writer *w, uint32_t reg, uint32_t value);
+int rdp_dump_writer_end_frame(rdp_dump_writer *w);
+int rdp_dump_writer_signal_complete(rdp_dump_writer *w);
+int rdp_dump_writer_close(rdp_dump_writer *w);
+int rdp_dump_replay(rdp_cp *cp, const char *path, rdp_dump_frame_cb on_frame, void *user, uint32_t *frames);
+
 /* Kernel specialisation.  No counterpart in the reference (its shaders are specialised per
  * render-state variant by its pipeline compiler).  The shading kernel is compiled for
  * RDP_SHADE_VARIANTS variants (two kernel shapes, four register budgets each); by default an

@@ -2843,17 +2843,58 @@ __device__ __forceinline__ void blend_tile(uint32_t item, const RdpPass *__restr
 	if (inside)
 	{
 		load_pixel(ps, px, ci, di);
+		// Software pipeline: the scratch words and primitive of pair pr + BLEND_AHEAD are loaded
+		// (and its shading record prefetched into L1) while pair pr blends.
+		constexpr int BLEND_AHEAD = 2;
+		uint32_t q_misc[BLEND_AHEAD], q_color[BLEND_AHEAD], q_prim[BLEND_AHEAD];
+		int q_zd[BLEND_AHEAD];
+#pragma unroll
+		for (int k = 0; k < BLEND_AHEAD; k++)
+		{
+			const uint32_t pr = p0 + uint32_t(k);
+			q_misc[k] = 0xffu;
+			q_color[k] = 0u;
+			q_zd[k] = 0;
+			q_prim[k] = 0u;
+			if (pr < p1)
+			{
+				const size_t at = size_t(pr) * SHADE_THREADS + tid;
+				q_misc[k] = sc_misc[at];
+				q_color[k] = sc_color[at];
+				q_zd[k] = sc_zdith[at];
+				q_prim[k] = pairs[pr].x;
+				asm volatile("prefetch.global.L1 [%0];" ::"l"(shade + q_prim[k]));
+			}
+		}
 		for (uint32_t pr = p0; pr < p1; pr++)
 		{
-			size_t at = size_t(pr) * SHADE_THREADS + tid;
-			uint32_t misc = sc_misc[at];
+			const uint32_t misc = q_misc[0], color = q_color[0], prim = q_prim[0];
+			const int zd = q_zd[0];
+#pragma unroll
+			for (int k = 0; k + 1 < BLEND_AHEAD; k++)
+			{
+				q_misc[k] = q_misc[k + 1];
+				q_color[k] = q_color[k + 1];
+				q_zd[k] = q_zd[k + 1];
+				q_prim[k] = q_prim[k + 1];
+			}
+			const uint32_t nx = pr + BLEND_AHEAD;
+			if (nx < p1)
+			{
+				const size_t at = size_t(nx) * SHADE_THREADS + tid;
+				q_misc[BLEND_AHEAD - 1] = sc_misc[at];
+				q_color[BLEND_AHEAD - 1] = sc_color[at];
+				q_zd[BLEND_AHEAD - 1] = sc_zdith[at];
+				q_prim[BLEND_AHEAD - 1] = pairs[nx].x;
+				asm volatile("prefetch.global.L1 [%0];" ::"l"(shade + q_prim[BLEND_AHEAD - 1]));
+			}
 			if ((misc & 0xff) == 0xff) continue;
 			Shaded in;
 			in.coverage = int(misc & 0xff);
 			in.shade_alpha = int(misc >> 8);
-			in.combined = sc_color[at];
-			in.z_dith = sc_zdith[at];
-			frags += blend_pixel(ps, pc, shade[pairs[pr].x], in, px);
+			in.combined = color;
+			in.z_dith = zd;
+			frags += blend_pixel(ps, pc, shade[prim], in, px);
 		}
 		store_pixel(ps, px, ci, di, pc.alias);
 	}

@@ -95,7 +95,9 @@ EXPORTED_SYMBOLS = [
     "rdp_batch_get_stats", "rdp_batch_capture_begin", "rdp_batch_capture_end", "rdp_set_shade_variant",
     "rdp_get_shade_variant", "rdp_batch_set_schedule", "rdp_batch_get_model", "rdp_batch_set_model",
     "rdp_mlp_gradients", "rdp_mlp_forward", "rdp_batch_get_tile_samples", "rdp_graph_last_blend_ms",
-    "rdp_serve_run", "rdp_batch_enqueue_many",
+    "rdp_serve_run", "rdp_batch_enqueue_many", "rdp_dump_writer_open", "rdp_dump_writer_flush_rdram",
+    "rdp_dump_writer_flush_hidden_rdram", "rdp_dump_writer_command", "rdp_dump_writer_set_vi_register",
+    "rdp_dump_writer_end_frame", "rdp_dump_writer_signal_complete", "rdp_dump_writer_close", "rdp_dump_replay",
 ]
 
 

@@ -167,7 +167,7 @@ struct Executor
 	RdpPrimShade *d_shade = nullptr;
 	uint32_t *d_masks = nullptr, *d_tmem_keep = nullptr;
 	uint32_t *d_tile_counts = nullptr, *d_pair_offsets = nullptr, *d_ctrl = nullptr;
-	uint32_t *d_tile_order = nullptr, *d_tile_cycles = nullptr, *d_nonempty = nullptr;
+	uint32_t *d_tile_order = nullptr, *d_tile_cycles = nullptr, *d_nonempty = nullptr, *d_scan_blocks = nullptr;
 	uint2 *d_pairs = nullptr;
 	uint32_t *d_sc_color = nullptr;
 	int *d_sc_zdith = nullptr;
@@ -415,6 +415,7 @@ struct Executor
 		cudaFree(d_tile_order);
 		cudaFree(d_tile_cycles);
 		cudaFree(d_nonempty);
+		cudaFree(d_scan_blocks);
 		cudaFree(d_pairs);
 		cudaFree(d_sc_color);
 		cudaFree(d_sc_zdith);
@@ -424,6 +425,7 @@ struct Executor
 		d_attr = nullptr;
 		d_shade = nullptr;
 		d_masks = d_tmem_keep = d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = d_nonempty = nullptr;
+		d_scan_blocks = nullptr;
 		d_pairs = nullptr;
 		d_sc_color = nullptr;
 		d_sc_zdith = nullptr;
@@ -483,11 +485,13 @@ struct Executor
 			cudaFree(d_tile_order);
 			cudaFree(d_tile_cycles);
 			cudaFree(d_nonempty);
-			d_masks = d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = d_nonempty = nullptr;
+			cudaFree(d_scan_blocks);
+			d_masks = d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = d_nonempty = d_scan_blocks = nullptr;
 			if (check(cudaMalloc(&d_masks, size_t(n) * RDP_MASK_WORDS_PER_TILE * 4)) ||
 			    check(cudaMalloc(&d_tile_counts, size_t(n + 1) * 4)) || check(cudaMalloc(&d_pair_offsets, size_t(n + 1) * 4)) ||
 			    check(cudaMalloc(&d_tile_order, size_t(n) * 4)) || check(cudaMalloc(&d_tile_cycles, size_t(n) * 4)) ||
-			    check(cudaMalloc(&d_nonempty, size_t(n) * 4)))
+			    check(cudaMalloc(&d_nonempty, size_t(n) * 4)) ||
+			    check(cudaMalloc(&d_scan_blocks, (size_t(n) / 1024 + 2) * 8)))
 				return false;
 			// Bitmasks and counts are self-clearing between launches; they start at zero.
 			if (check(cudaMemsetAsync(d_masks, 0, size_t(n) * RDP_MASK_WORDS_PER_TILE * 4, stream)) ||
@@ -698,6 +702,7 @@ struct Executor
 		L.tmem_keep = d_tmem_keep;
 		L.tile_counts = d_tile_counts;
 		L.nonempty_tiles = d_nonempty;
+		L.scan_blocks = d_scan_blocks;
 		L.pair_offsets = d_pair_offsets;
 		L.pairs = d_pairs;
 		L.ctrl = d_ctrl;

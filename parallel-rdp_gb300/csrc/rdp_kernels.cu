@@ -2525,12 +2525,147 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t num_items, uint32_t *__r
 	}
 }
 
+// Multi-CTA form of k_scan for launches with many tiles: SCAN_TILE tiles per CTA.
+// k_scan_reduce: per-CTA pair and non-empty counts; k_scan_top (1 CTA): their exclusive
+// prefixes and the control words; k_scan_down: per-CTA scan plus prefix, offsets, tile list.
+constexpr int SCAN_THREADS = 256, SCAN_PER_THREAD = 4, SCAN_TILE = SCAN_THREADS * SCAN_PER_THREAD;
+
+// Block-wide exclusive scan of one value per thread; returns the thread's prefix, *total the sum.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *warp_sums, uint32_t *total)
+{
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	uint32_t x = v;
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1)
+	{
+		uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+		if (lane >= o) x += y;
+	}
+	if (lane == 31) warp_sums[wid] = x;
+	__syncthreads();
+	if (wid == 0)
+	{
+		uint32_t w = lane < nw ? warp_sums[lane] : 0u;
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1)
+		{
+			uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+			if (lane >= o) w += y;
+		}
+		if (lane < nw) warp_sums[lane] = w;
+	}
+	__syncthreads();
+	const uint32_t r = (wid ? warp_sums[wid - 1] : 0u) + x - v;
+	*total = warp_sums[nw - 1];
+	__syncthreads();
+	return r;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(uint32_t num_items, const uint32_t *__restrict__ counts,
+                                                             uint32_t *__restrict__ block_sums)
+{
+	__shared__ uint32_t warp_sums[32];
+	const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+	uint32_t sum = 0, nz = 0;
+#pragma unroll
+	for (int k = 0; k < SCAN_PER_THREAD; k++)
+		if (base + k < num_items)
+		{
+			const uint32_t v = counts[base + k];
+			sum += v;
+			nz += v != 0;
+		}
+	uint32_t tot_sum, tot_nz;
+	block_exclusive_scan(sum, warp_sums, &tot_sum);
+	block_exclusive_scan(nz, warp_sums, &tot_nz);
+	if (threadIdx.x == 0)
+	{
+		block_sums[2 * blockIdx.x] = tot_sum;
+		block_sums[2 * blockIdx.x + 1] = tot_nz;
+	}
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(uint32_t num_blocks, uint32_t *__restrict__ block_sums,
+                                                   uint32_t num_items, uint32_t *__restrict__ offsets,
+                                                   uint32_t *__restrict__ ctrl, uint32_t capacity,
+                                                   uint32_t *__restrict__ pair_log, uint32_t log_slot)
+{
+	__shared__ uint32_t warp_sums[32];
+	__shared__ uint32_t carry, carry_nz;
+	if (threadIdx.x == 0)
+	{
+		carry = 0;
+		carry_nz = 0;
+	}
+	__syncthreads();
+	for (uint32_t b0 = 0; b0 < num_blocks; b0 += 1024)
+	{
+		const uint32_t b = b0 + threadIdx.x;
+		const uint32_t s = b < num_blocks ? block_sums[2 * b] : 0u, z = b < num_blocks ? block_sums[2 * b + 1] : 0u;
+		uint32_t ts, tz;
+		const uint32_t ps = block_exclusive_scan(s, warp_sums, &ts);
+		const uint32_t pz = block_exclusive_scan(z, warp_sums, &tz);
+		if (b < num_blocks)
+		{
+			block_sums[2 * b] = carry + ps;
+			block_sums[2 * b + 1] = carry_nz + pz;
+		}
+		__syncthreads();
+		if (threadIdx.x == 0)
+		{
+			carry += ts;
+			carry_nz += tz;
+		}
+		__syncthreads();
+	}
+	if (threadIdx.x == 0)
+	{
+		offsets[num_items] = carry;
+		ctrl[0] = carry;
+		ctrl[1] = carry > capacity ? 1u : 0u;
+		ctrl[2] = max(ctrl[2], carry);
+		ctrl[3] = carry_nz;
+		ctrl[4] = 0u;
+		if (pair_log) pair_log[log_slot] = carry;
+	}
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(uint32_t num_items, uint32_t *__restrict__ counts,
+                                                           const uint32_t *__restrict__ block_sums,
+                                                           uint32_t *__restrict__ offsets, uint32_t *__restrict__ nonempty)
+{
+	__shared__ uint32_t warp_sums[32];
+	const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+	uint32_t v[SCAN_PER_THREAD], sum = 0, nz = 0;
+#pragma unroll
+	for (int k = 0; k < SCAN_PER_THREAD; k++)
+	{
+		v[k] = base + k < num_items ? counts[base + k] : 0u;
+		if (base + k < num_items) counts[base + k] = 0u;
+		sum += v[k];
+		nz += v[k] != 0;
+	}
+	uint32_t ts, tz;
+	uint32_t ps = block_exclusive_scan(sum, warp_sums, &ts) + block_sums[2 * blockIdx.x];
+	uint32_t pz = block_exclusive_scan(nz, warp_sums, &tz) + block_sums[2 * blockIdx.x + 1];
+#pragma unroll
+	for (int k = 0; k < SCAN_PER_THREAD; k++)
+	{
+		if (base + k < num_items)
+		{
+			offsets[base + k] = ps;
+			if (v[k]) nonempty[pz++] = base + k;
+		}
+		ps += v[k];
+	}
+}
+
 // One warp per tile: turns the tile's primitive bitmask into its ordered run of
 // (primitive, tile) pairs and clears the bitmask.
 // With `featbits`, also writes the tile's scheduling features (sched.h) to features[item].
 __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes, uint32_t num_items,
                          const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ ctrl, uint2 *__restrict__ pairs,
-                         const uint16_t *__restrict__ featbits, float *__restrict__ features)
+                         const uint16_t *__restrict__ featbits, float *__restrict__ features, bool train)
 {
 	uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	int lane = threadIdx.x & 31;
@@ -2546,6 +2681,8 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 	uint32_t fc[RDP_FEAT_COUNT];
 #pragma unroll
 	for (int i = 0; i < RDP_FEAT_COUNT; i++) fc[i] = 0;
+	// Without training, only tiles the model evaluates need features.
+	if (featbits && !train && npairs < RDP_SCHED_MIN_PAIRS) featbits = nullptr;
 	for (uint32_t base = 0; base < nwords; base += 32)
 	{
 		uint32_t wi = base + lane;
@@ -3137,6 +3274,7 @@ extern "C" uint32_t rdp_kernels_count(const RdpLaunch *L)
 	if (L->num_prims && L->num_tile_items)
 	{
 		n += 5;
+		if (L->num_tile_items > RDP_SCAN_SINGLE_CTA_MAX && L->scan_blocks) n += 2;
 		if (L->sched && (L->sched->order_enabled || L->sched->train_enabled))
 		{
 			n += 3;
@@ -3170,12 +3308,23 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 	}
 	if (raster)
 	{
-		rdp::k_scan<<<1, 1024, 0, stream>>>(L->num_tile_items, L->tile_counts, L->pair_offsets, L->nonempty_tiles,
-		                                    L->ctrl, L->pair_capacity, L->pair_log, L->log_slot);
+		if (L->num_tile_items > RDP_SCAN_SINGLE_CTA_MAX && L->scan_blocks)
+		{
+			const uint32_t nb = (L->num_tile_items + rdp::SCAN_TILE - 1) / rdp::SCAN_TILE;
+			rdp::k_scan_reduce<<<nb, rdp::SCAN_THREADS, 0, stream>>>(L->num_tile_items, L->tile_counts, L->scan_blocks);
+			rdp::k_scan_top<<<1, 1024, 0, stream>>>(nb, L->scan_blocks, L->num_tile_items, L->pair_offsets, L->ctrl,
+			                                        L->pair_capacity, L->pair_log, L->log_slot);
+			rdp::k_scan_down<<<nb, rdp::SCAN_THREADS, 0, stream>>>(L->num_tile_items, L->tile_counts, L->scan_blocks,
+			                                                       L->pair_offsets, L->nonempty_tiles);
+		}
+		else
+			rdp::k_scan<<<1, 1024, 0, stream>>>(L->num_tile_items, L->tile_counts, L->pair_offsets, L->nonempty_tiles,
+			                                    L->ctrl, L->pair_capacity, L->pair_log, L->log_slot);
 		const bool sched = L->sched && (L->sched->order_enabled || L->sched->train_enabled);
 		rdp::k_expand<<<(L->num_tile_items * 32 + 255) / 256, 256, 0, stream>>>(
 			L->passes, L->num_passes, L->num_tile_items, L->pair_offsets, L->ctrl, L->pairs,
-			sched ? L->sched->featbits : nullptr, sched ? L->sched->features : nullptr);
+			sched ? L->sched->featbits : nullptr, sched ? L->sched->features : nullptr,
+			sched && L->sched->train_enabled && L->tile_cycles);
 		// Inside a stream capture the events become record nodes of the graph.
 		cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
 		if ((L->shade_events[0] || L->blend_events[0]) && cudaStreamIsCapturing(stream, &capture) != cudaSuccess)

@@ -8,6 +8,9 @@
 /* Shading kernels: k_shade (one pair per 64-thread CTA) for minimum residencies of 1, 12, 16
  * and 24 CTAs per SM, and k_shade_compact (4 pairs per 128-thread CTA, covered pixels only)
  * for 1, 6, 8 and 12. */
+/* Launches with more tiles than this scan their pair counts with several CTAs. */
+#define RDP_SCAN_SINGLE_CTA_MAX 16384
+
 #ifndef RDP_SHADE_VARIANTS
 #define RDP_SHADE_VARIANTS 8
 #endif
@@ -37,6 +40,7 @@ typedef struct RdpLaunch
 	/* pair list + shading scratch */
 	uint32_t *tile_counts;          /* [num_tile_items], zero between launches */
 	uint32_t *nonempty_tiles;       /* [num_tile_items]: tiles with pairs, in tile order (k_scan) */
+	uint32_t *scan_blocks;          /* [2 * ceil(num_tile_items / 1024)]: multi-CTA scan partials */
 	uint32_t *pair_offsets;         /* [num_tile_items + 1] */
 	uint2 *pairs;                   /* [pair_capacity] (global primitive index, tile item) */
 	uint32_t *ctrl;                 /* [0] pairs, [1] overflow, [2] max pairs, [3] non-empty tiles, [4] counter */

@@ -38,7 +38,7 @@ enum
 	RDP_FEAT_NOISE, RDP_FEAT_COUNT
 };
 /* Tiles with fewer pairs than this are not evaluated: they go to the end of the queue. */
-#define RDP_SCHED_MIN_PAIRS 4
+#define RDP_SCHED_MIN_PAIRS 16
 
 #ifdef __CUDACC__
 static __host__ __device__ __forceinline__ uint16_t rdp_feature_bits(uint32_t f, uint32_t d)

@@ -79,7 +79,27 @@ __device__ float warp_forward(const NetS &n, const float *x, float *h1, float *h
 }
 
 // ------------------------------------------------------------------ scheduling
+// Adds `count` lanes' worth of `b` to counter[b] with one atomic per distinct value in the warp
+// (most tiles share the last bucket); returns each lane's position among its peers' slots.
+__device__ __forceinline__ uint32_t warp_aggregated_add(uint32_t *counter, uint32_t b, bool active)
+{
+	const unsigned mask = __ballot_sync(0xffffffffu, active);
+	uint32_t pos = 0;
+	if (active)
+	{
+		const int lane = threadIdx.x & 31;
+		const unsigned peers = __match_any_sync(mask, b);
+		const int leader = __ffs(peers) - 1;
+		uint32_t base = 0;
+		if (lane == leader) base = atomicAdd(&counter[b], uint32_t(__popc(peers)));
+		base = __shfl_sync(peers, base, leader);
+		pos = base + uint32_t(__popc(peers & ((1u << lane) - 1u)));
+	}
+	return pos;
+}
+
 // Per non-empty tile: prediction from the features k_expand wrote, bucket (descending cost).
+// A warp looks at 32 tiles at a time and evaluates the network only for those with enough pairs.
 __global__ void __launch_bounds__(WARPS * 32) k_tile_predict(RdpSchedDev s, const uint32_t *__restrict__ offsets,
                                                              const uint32_t *__restrict__ ctrl,
                                                              const uint32_t *__restrict__ nonempty)
@@ -91,26 +111,36 @@ __global__ void __launch_bounds__(WARPS * 32) k_tile_predict(RdpSchedDev s, cons
 	__syncthreads();
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint32_t n = ctrl[3];
-	for (uint32_t k = blockIdx.x * WARPS + warp; k < n; k += gridDim.x * WARPS)
+	for (uint32_t base = (blockIdx.x * WARPS + warp) * 32u; base < n; base += gridDim.x * WARPS * 32u)
 	{
-		const uint32_t item = nonempty[k];
+		const uint32_t k = base + uint32_t(lane);
+		const bool valid = k < n;
+		const uint32_t item = valid ? nonempty[k] : 0u;
+		const uint32_t np = valid ? offsets[item + 1] - offsets[item] : 0u;
 		float pred = 0.0f;
-		int b = RDP_SCHED_BUCKETS - 1;
-		if (offsets[item + 1] - offsets[item] >= RDP_SCHED_MIN_PAIRS)
+		uint32_t b = RDP_SCHED_BUCKETS - 1;
+		unsigned todo = __ballot_sync(0xffffffffu, valid && np >= RDP_SCHED_MIN_PAIRS);
+		while (todo)
 		{
-			if (lane < IN) s_x[warp][lane] = s.features[size_t(item) * IN + lane];
+			const int src = __ffs(todo) - 1;
+			todo &= todo - 1;
+			const uint32_t it = __shfl_sync(0xffffffffu, item, src);
+			if (lane < IN) s_x[warp][lane] = s.features[size_t(it) * IN + lane];
 			__syncwarp();
-			pred = warp_forward(net, s_x[warp], s_h1[warp], s_h2[warp], lane);
-			b = int((2.0f - pred) * (RDP_SCHED_BUCKETS / 2));
-			b = b < 0 ? 0 : (b >= RDP_SCHED_BUCKETS - 1 ? RDP_SCHED_BUCKETS - 2 : b);
+			const float p = warp_forward(net, s_x[warp], s_h1[warp], s_h2[warp], lane);
+			if (lane == src)
+			{
+				pred = p;
+				int bb = int((2.0f - p) * (RDP_SCHED_BUCKETS / 2));
+				b = uint32_t(bb < 0 ? 0 : (bb >= RDP_SCHED_BUCKETS - 1 ? RDP_SCHED_BUCKETS - 2 : bb));
+			}
 		}
-		if (lane == 0)
+		if (valid)
 		{
 			s.pred[k] = pred;
-			s.bucket[k] = uint32_t(b);
-			atomicAdd(&s.hist[b], 1u);
+			s.bucket[k] = b;
 		}
-		__syncwarp();
+		warp_aggregated_add(s.hist, b, valid);
 	}
 }
 
@@ -149,10 +179,14 @@ __global__ void k_bucket_scatter(RdpSchedDev s, const uint32_t *__restrict__ ctr
 {
 	if (ctrl[1]) return;
 	const uint32_t n = ctrl[3];
-	for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+	const uint32_t stride = gridDim.x * blockDim.x;
+	for (uint32_t k0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); k0 < n; k0 += stride)
 	{
-		uint32_t pos = atomicAdd(&s.cursor[s.bucket[k]], 1u);
-		s.order[pos] = nonempty[k];
+		const uint32_t k = k0 + (threadIdx.x & 31u);
+		const bool valid = k < n;
+		const uint32_t b = valid ? s.bucket[k] : 0u;
+		const uint32_t pos = warp_aggregated_add(s.cursor, b, valid);
+		if (valid) s.order[pos] = nonempty[k];
 	}
 }
 

@@ -314,7 +314,7 @@ int rdp_dump_replay(rdp_cp *cp, const char *path, rdp_dump_frame_cb on_frame, vo
 
 /* Kernel specialisation.  No counterpart in the reference (its shaders are specialised per
  * render-state variant by its pipeline compiler).  The shading kernel is compiled for
- * RDP_SHADE_VARIANTS variants (two kernel shapes, four register budgets each); by default an
+ * RDP_SHADE_VARIANTS variants (two kernel shapes and several register budgets); by default an
  * autotuner times them on the first launches of a device and keeps the fastest per shaded
  * (primitive, tile) pair.  All variants give identical results.  rdp_set_shade_variant forces
  * one (0..7) or restarts tuning (-1); rdp_get_shade_variant returns the device's choice, -1 while tuning. */

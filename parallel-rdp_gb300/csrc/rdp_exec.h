@@ -359,7 +359,7 @@ struct Executor
 				keep.push_back(sm);
 				continue;
 			}
-			if (q == cudaSuccess && cudaEventElapsedTime(&ms, sm.ev[0], sm.ev[1]) == cudaSuccess)
+			if (q == cudaSuccess && log[sm.slot] != 0xffffffffu && cudaEventElapsedTime(&ms, sm.ev[0], sm.ev[1]) == cudaSuccess)
 			{
 				tuner.ms[sm.variant] += ms;
 				tuner.pairs[sm.variant] += log[sm.slot];

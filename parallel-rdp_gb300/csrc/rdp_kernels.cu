@@ -1577,7 +1577,7 @@ struct CombIn
 	int lod_frac, noise;
 };
 
-__device__ __noinline__ void combine(const CombIn &in, const uint8_t *rs, const uint8_t *as, int out[4])
+__device__ __forceinline__ void combine(const CombIn &in, const uint8_t *rs, const uint8_t *as, int out[4])
 {
 #pragma unroll
 	for (int c = 0; c < 4; c++)
@@ -1694,7 +1694,7 @@ struct Pix
 	uint32_t cidx;
 };
 
-__device__ __noinline__ void blender(const int pix[4], const int mem[4], const uint8_t fog[4], const uint8_t bc[4], int shade_alpha,
+__device__ __forceinline__ void blender(const int pix[4], const int mem[4], const uint8_t fog[4], const uint8_t bc[4], int shade_alpha,
                         const uint8_t *m, bool force_blend, bool blend_en, bool color_on_cvg, bool cvg_wrap,
                         const int bshift[2], bool final_cycle, int out[3])
 {
@@ -2521,7 +2521,8 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t num_items, uint32_t *__r
 		ctrl[2] = max(ctrl[2], carry); // largest pair count seen: the host grows the scratch to it
 		ctrl[3] = carry_nz;
 		ctrl[4] = 0u;
-		if (pair_log) pair_log[log_slot] = carry; // per-launch pair count for the autotuner
+		// Per-launch pair count for the autotuner; an overflowing launch is not a sample.
+		if (pair_log) pair_log[log_slot] = carry > capacity ? 0xffffffffu : carry;
 	}
 }
 
@@ -2626,7 +2627,7 @@ __global__ void __launch_bounds__(1024) k_scan_top(uint32_t num_blocks, uint32_t
 		ctrl[2] = max(ctrl[2], carry);
 		ctrl[3] = carry_nz;
 		ctrl[4] = 0u;
-		if (pair_log) pair_log[log_slot] = carry;
+		if (pair_log) pair_log[log_slot] = carry > capacity ? 0xffffffffu : carry;
 	}
 }
 
@@ -3239,14 +3240,13 @@ extern "C" cudaError_t rdp_kernels_init_luts(const uint8_t *blender_lut)
 namespace {
 typedef void (*ShadeKernel)(const RdpPass *, uint32_t, const uint2 *, const uint32_t *, const RdpPrimGeom *,
                             const RdpPrimAttr *, const RdpPrimShade *, const RdpTile *, uint32_t *, int *, uint16_t *);
-const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = { rdp::k_shade<1>,         rdp::k_shade<12>,
-                                                         rdp::k_shade<16>,        rdp::k_shade<24>,
-                                                         rdp::k_shade_compact<1>, rdp::k_shade_compact<6>,
-                                                         rdp::k_shade_compact<8>, rdp::k_shade_compact<12> };
+const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = { rdp::k_shade<1>,  rdp::k_shade<12>, rdp::k_shade<16>,
+                                                         rdp::k_shade<20>, rdp::k_shade<24>, rdp::k_shade<28>,
+                                                         rdp::k_shade<32>, rdp::k_shade_compact<12> };
 // Threads per CTA of each variant.
-const int kShadeThreads[RDP_SHADE_VARIANTS] = { rdp::SHADE_THREADS,    rdp::SHADE_THREADS,    rdp::SHADE_THREADS,
-                                                rdp::SHADE_THREADS,    rdp::COMPACT_THREADS, rdp::COMPACT_THREADS,
-                                                rdp::COMPACT_THREADS, rdp::COMPACT_THREADS };
+const int kShadeThreads[RDP_SHADE_VARIANTS] = { rdp::SHADE_THREADS, rdp::SHADE_THREADS, rdp::SHADE_THREADS,
+                                                rdp::SHADE_THREADS, rdp::SHADE_THREADS, rdp::SHADE_THREADS,
+                                                rdp::SHADE_THREADS, rdp::COMPACT_THREADS };
 } // namespace
 
 extern "C" int rdp_kernels_blend_ctas_per_sm(void)

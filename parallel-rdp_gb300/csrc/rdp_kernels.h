@@ -5,9 +5,9 @@
 #include <cuda_runtime.h>
 #include "rdp_types.h"
 
-/* Shading kernels: k_shade (one pair per 64-thread CTA) for minimum residencies of 1, 12, 16
- * and 24 CTAs per SM, and k_shade_compact (4 pairs per 128-thread CTA, covered pixels only)
- * for 1, 6, 8 and 12. */
+/* Shading kernels: k_shade (one pair per 64-thread CTA) for minimum residencies of 1, 12, 16,
+ * 20, 24, 28 and 32 CTAs per SM, and k_shade_compact (4 pairs per 128-thread CTA, pixels inside
+ * the spans only) for 12. */
 /* Launches with more tiles than this scan their pair counts with several CTAs. */
 #define RDP_SCAN_SINGLE_CTA_MAX 16384
 

@@ -1350,7 +1350,7 @@ __device__ __forceinline__ T4 convert_factors(const T4 &in, const int16_t f[4])
 }
 
 // texture.h:498-923
-__device__ __noinline__ T4 sample_texture(const uint16_t *tm, const RdpTile &t, int s_in, int t_in, bool tlut, bool tlut_type,
+__device__ __forceinline__ T4 sample_texture(const uint16_t *tm, const RdpTile &t, int s_in, int t_in, bool tlut, bool tlut_type,
                              bool sample_quad, bool mid_state, bool convert_one, bool bilerp, const int16_t *factors,
                              const T4 &prev)
 {

@@ -422,7 +422,7 @@ def run_ours_batched(args):
     _run_batch_step(b, insts, streams)
     s1 = [cp.stats() for cp in insts]
     b.idle()  # grows the pair scratch to what the sync point needed
-    from rdp_gb300 import get_shade_variant
+    from rdp_gb300 import get_shade_order, get_shade_variant
     for _ in range(12):  # the autotuner times the shading-kernel variants on the first sync points
         if get_shade_variant(local) >= 0:
             break
@@ -549,7 +549,7 @@ def run_ours_batched(args):
                    "tile_instances_per_step": pairs_per_step, "rounds_per_step": rounds_per_step,
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed between timed iterations", "tile_order": "learned (longest predicted first)",
-                   "shade_variant": get_shade_variant(local)},
+                   "shade_variant": get_shade_variant(local), "shade_order": get_shade_order(local)},
         "mpix_per_s": total_frags / t_value / 1e6,
         "frames_per_s": world * args.steps * args.instances / t_value,
         "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": t_plain * 1e3 / args.steps,
@@ -673,8 +673,13 @@ def main():
     ap.add_argument("--serve-instances", type=int, default=256)
     ap.add_argument("--serve-window", type=float, default=0.1, help="seconds of arrivals at the configured rate")
     ap.add_argument("--serve-budget-gb", type=float, default=16.0)
+    ap.add_argument("--shade-order", type=int, default=None, choices=[0, 1, 2],
+                    help="shading order: 0 tile order strided, 1 per-SM queues, 2 primitive-major (default: library's)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.impl == "ours" and args.shade_order is not None:
+        from rdp_gb300 import set_shade_order
+        set_shade_order(args.shade_order, int(os.environ.get("LOCAL_RANK", "0")))
     if args.impl == "reference":
         (run_reference_batched if args.workload == "batched" else run_reference_textured)(args)
     else:

@@ -322,6 +322,16 @@ int rdp_dump_replay(rdp_cp *cp, const char *path, rdp_dump_frame_cb on_frame, vo
 int rdp_set_shade_variant(int device, int variant);
 int rdp_get_shade_variant(int device);
 
+/* Order in which k_shade takes the (primitive, tile) pairs of a launch, process-wide per device
+ * (default 2, or the RDP_SHADE_ORDER environment variable): 0 = tile order with a fixed stride
+ * per CTA, 1 = tile order dealt through one work queue per SM, 2 = primitive-major order dealt
+ * through the per-SM queues.  Primitive-major order applies to launches of at least 16,384
+ * primitives (RDP_SHADE_PERM_MIN_PRIMS), the queues to launches of at least 64 pairs per CTA
+ * (RDP_SHADE_QUEUE_MIN); smaller launches take the next simpler order.  The variables are read
+ * when a processor or batch is created.  All orders give identical results. */
+int rdp_set_shade_order(int device, int order);
+int rdp_get_shade_order(int device);
+
 /* ---------------------------------------------------------------------------------------------
  * Allocation-free TMEM update.  No counterpart in the reference: it exists for callers that must
  * not allocate device memory -- for example an emulator frame loop that runs inside a CUDA stream

@@ -99,6 +99,20 @@ static cudaError_t ensure_luts(int device)
 
 namespace rdpx {
 // RDP_SHADE_VARIANT=<0..3> in the environment fixes the variant (profiling, experiments).
+int &shade_order_choice(int device)
+{
+	static std::vector<int> choice = [] {
+		int v = 2;
+		if (const char *e = getenv("RDP_SHADE_ORDER"))
+		{
+			int x = atoi(e);
+			if (x >= 0 && x <= 2) v = x;
+		}
+		return std::vector<int>(64, v);
+	}();
+	return choice[device >= 0 && device < 64 ? device : 0];
+}
+
 int &shade_variant_choice(int device)
 {
 	static std::vector<int> choice = [] {
@@ -2014,6 +2028,19 @@ int rdp_get_shade_variant(int device)
 {
 	if (device < 0 || device >= 64) return -1;
 	return rdpx::shade_variant_choice(device);
+}
+
+int rdp_set_shade_order(int device, int order)
+{
+	if (device < 0 || device >= 64 || order < 0 || order > 2) return RDP_ERR_INVALID;
+	rdpx::shade_order_choice(device) = order;
+	return RDP_OK;
+}
+
+int rdp_get_shade_order(int device)
+{
+	if (device < 0 || device >= 64) return -1;
+	return rdpx::shade_order_choice(device);
 }
 
 int rdp_batch_set_schedule(rdp_batch *b, int learned_order, int train, float learning_rate, uint32_t train_stride)

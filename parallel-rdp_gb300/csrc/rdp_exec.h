@@ -16,6 +16,7 @@
 #include <stdint.h>
 #include <string.h>
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 #include "rdp_types.h"
@@ -99,6 +100,7 @@ struct CaptureSink
 
 // Process-wide choice of the k_shade variant per device: -1 until tuned (or forced).
 int &shade_variant_choice(int device);
+int &shade_order_choice(int device);
 
 // Autotuner of the shading kernel.  Tuning runs for RDP_SHADE_VARIANTS epochs (an epoch
 // ends at each sync point: idle); in epoch e the i-th rasterising launch uses variant
@@ -161,6 +163,12 @@ struct Executor
 	bool failed = false;
 	ShadeTuner tuner;
 	uint32_t *d_pair_log = nullptr; // [256]
+	// Size thresholds of the shading orders (RDP_SHADE_PERM_MIN_PRIMS, RDP_SHADE_QUEUE_MIN
+	// override them): primitive-major order for launches of at least perm_min_prims primitives,
+	// per-SM queues for launches of at least queue_min pairs per k_shade CTA.
+	uint32_t perm_min_prims = 16384, queue_min = 64;
+	uint32_t *d_queues = nullptr, num_queues = 0; // per-SM work queues of k_shade + used-up bitmask
+	size_t queue_bytes() const { return (size_t(num_queues) + (num_queues + 31) / 32) * 4; }
 
 	RdpPrimGeom *d_geom = nullptr;
 	RdpPrimAttr *d_attr = nullptr;
@@ -168,6 +176,7 @@ struct Executor
 	uint32_t *d_masks = nullptr, *d_tmem_keep = nullptr;
 	uint32_t *d_tile_counts = nullptr, *d_pair_offsets = nullptr, *d_ctrl = nullptr;
 	uint32_t *d_tile_order = nullptr, *d_tile_cycles = nullptr, *d_nonempty = nullptr, *d_scan_blocks = nullptr;
+	uint32_t *d_prim_pairs = nullptr, *d_prim_offsets = nullptr, *d_prim_blocks = nullptr, *d_perm = nullptr;
 	uint2 *d_pairs = nullptr;
 	uint32_t *d_sc_color = nullptr;
 	int *d_sc_zdith = nullptr;
@@ -329,8 +338,13 @@ struct Executor
 		for (int v = 0; v < RDP_SHADE_VARIANTS; v++) shade_ctas_v[v] = uint32_t(sms) * uint32_t(rdp_kernels_shade_ctas_per_sm(v));
 		blend_ctas = uint32_t(sms) * uint32_t(rdp_kernels_blend_ctas_per_sm());
 		tuner.active = shade_variant_choice(device) < 0;
-		if (check(cudaMalloc(&d_ctrl, 32)) || check(cudaMalloc(&d_pair_log, 256 * 4))) return false;
-		return !check(cudaMemsetAsync(d_ctrl, 0, 32, stream));
+		num_queues = uint32_t(sms);
+		if (const char *e = getenv("RDP_SHADE_PERM_MIN_PRIMS")) perm_min_prims = uint32_t(strtoul(e, nullptr, 10));
+		if (const char *e = getenv("RDP_SHADE_QUEUE_MIN")) queue_min = uint32_t(strtoul(e, nullptr, 10));
+		if (check(cudaMalloc(&d_ctrl, 32)) || check(cudaMalloc(&d_pair_log, 256 * 4)) ||
+		    check(cudaMalloc(&d_queues, queue_bytes())))
+			return false;
+		return !check(cudaMemsetAsync(d_ctrl, 0, 32, stream)) && !check(cudaMemsetAsync(d_queues, 0, queue_bytes(), stream));
 	}
 
 	int current_variant()
@@ -416,6 +430,10 @@ struct Executor
 		cudaFree(d_tile_cycles);
 		cudaFree(d_nonempty);
 		cudaFree(d_scan_blocks);
+		cudaFree(d_prim_pairs);
+		cudaFree(d_prim_offsets);
+		cudaFree(d_prim_blocks);
+		cudaFree(d_perm);
 		cudaFree(d_pairs);
 		cudaFree(d_sc_color);
 		cudaFree(d_sc_zdith);
@@ -426,6 +444,7 @@ struct Executor
 		d_shade = nullptr;
 		d_masks = d_tmem_keep = d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = d_nonempty = nullptr;
 		d_scan_blocks = nullptr;
+		d_prim_pairs = d_prim_offsets = d_prim_blocks = d_perm = nullptr;
 		d_pairs = nullptr;
 		d_sc_color = nullptr;
 		d_sc_zdith = nullptr;
@@ -440,8 +459,10 @@ struct Executor
 		sched_free();
 		cudaFree(d_ctrl);
 		cudaFree(d_pair_log);
+		cudaFree(d_queues);
 		d_ctrl = nullptr;
 		d_pair_log = nullptr;
+		d_queues = nullptr;
 		tuner.destroy();
 		for (auto &st : staging)
 		{
@@ -467,11 +488,17 @@ struct Executor
 			cudaFree(d_geom);
 			cudaFree(d_attr);
 			cudaFree(d_shade);
+			cudaFree(d_prim_pairs);
+			cudaFree(d_prim_offsets);
+			cudaFree(d_prim_blocks);
 			d_geom = nullptr;
 			d_attr = nullptr;
 			d_shade = nullptr;
+			d_prim_pairs = d_prim_offsets = d_prim_blocks = nullptr;
 			if (check(cudaMalloc(&d_geom, sizeof(RdpPrimGeom) * n)) || check(cudaMalloc(&d_attr, sizeof(RdpPrimAttr) * n)) ||
-			    check(cudaMalloc(&d_shade, sizeof(RdpPrimShade) * n)))
+			    check(cudaMalloc(&d_shade, sizeof(RdpPrimShade) * n)) || check(cudaMalloc(&d_prim_pairs, size_t(n) * 4)) ||
+			    check(cudaMalloc(&d_prim_offsets, size_t(n) * 4)) ||
+			    check(cudaMalloc(&d_prim_blocks, (size_t(n) / 1024 + 2) * 8)))
 				return false;
 			caps.prims = n;
 			if (!sched_prim_buffers(n)) return false;
@@ -512,14 +539,16 @@ struct Executor
 		{
 			uint32_t n = std::max(need.pairs, caps.pairs * 2);
 			cudaFree(d_pairs);
+			cudaFree(d_perm);
 			cudaFree(d_sc_color);
 			cudaFree(d_sc_zdith);
 			cudaFree(d_sc_misc);
 			d_pairs = nullptr;
+			d_perm = nullptr;
 			d_sc_color = nullptr;
 			d_sc_zdith = nullptr;
 			d_sc_misc = nullptr;
-			if (check(cudaMalloc(&d_pairs, size_t(n) * sizeof(uint2))) ||
+			if (check(cudaMalloc(&d_pairs, size_t(n) * sizeof(uint2))) || check(cudaMalloc(&d_perm, size_t(n) * 4)) ||
 			    check(cudaMalloc(&d_sc_color, size_t(n) * 64 * 4)) || check(cudaMalloc(&d_sc_zdith, size_t(n) * 64 * 4)) ||
 			    check(cudaMalloc(&d_sc_misc, size_t(n) * 64 * 2)))
 				return false;
@@ -707,6 +736,18 @@ struct Executor
 		L.pairs = d_pairs;
 		L.ctrl = d_ctrl;
 		L.pair_capacity = caps.pairs;
+		// k_shade work order (process-wide per device): 0 = fixed stride over the pairs in tile
+		// order, 1 = per-SM queues over tile order, 2 = per-SM queues over primitive-major order
+		// for launches of at least perm_min_prims primitives (smaller ones gain less from it than
+		// the primitive scan costs), else as 1.
+		const int shade_order = shade_order_choice(device);
+		L.shade_queues = shade_order >= 1 ? d_queues : nullptr;
+		L.num_shade_queues = shade_order >= 1 ? num_queues : 0u;
+		L.shade_queue_min = queue_min;
+		L.pair_perm = shade_order == 2 && prim_base >= perm_min_prims ? d_perm : nullptr;
+		L.prim_pairs = d_prim_pairs;
+		L.prim_offsets = d_prim_offsets;
+		L.prim_scan_blocks = d_prim_blocks;
 		int variant = current_variant();
 		bool sample = false;
 		if (tuner.active && shade_variant_choice(device) < 0 && !cap && tile_base &&

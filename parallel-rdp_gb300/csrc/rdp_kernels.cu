@@ -578,14 +578,20 @@ __device__ bool bin_primitive(const RdpPrimGeom &g, int lox, int loy, int hix, i
 	return rx0 <= rx1;
 }
 
+// With `prim_pairs`, also writes each primitive's number of binned tiles (its pairs).
 __global__ void k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom, const RdpPrimShade *__restrict__ shade,
-                      const RdpPass *__restrict__ passes, uint32_t *__restrict__ tile_counts)
+                      const RdpPass *__restrict__ passes, uint32_t *__restrict__ tile_counts,
+                      uint32_t *__restrict__ prim_pairs)
 {
 	uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	uint32_t lane = threadIdx.x & 31;
 	if (warp >= num_prims) return;
 	const RdpPrimGeom g = geom[warp];
-	if (g.bbox[2] < g.bbox[0] || g.bbox[3] < g.bbox[1]) return;
+	if (g.bbox[2] < g.bbox[0] || g.bbox[3] < g.bbox[1])
+	{
+		if (prim_pairs && lane == 0) prim_pairs[warp] = 0u;
+		return;
+	}
 	const RdpPass &pass = passes[shade[warp].pass];
 	uint32_t local = warp - pass.prim_begin;
 	uint32_t bit = 1u << (local & 31);
@@ -593,18 +599,27 @@ __global__ void k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom, 
 	int tw = g.bbox[2] - g.bbox[0] + 1, th = g.bbox[3] - g.bbox[1] + 1;
 	int count = tw * th;
 	int fbw = int(pass.fb_width), fbh = int(pass.fb_height);
-	for (int t = lane; t < count; t += 32)
+	uint32_t binned = 0;
+	for (int t0 = 0; t0 < count; t0 += 32)
 	{
-		int tx = g.bbox[0] + t % tw, ty = g.bbox[1] + t / tw;
-		int lox = tx * 8, loy = ty * 8;
-		int hix = min(lox + 7, fbw - 1), hiy = min(loy + 7, fbh - 1);
-		if (bin_primitive(g, lox, loy, hix, hiy))
+		const int t = t0 + int(lane);
+		bool hit = false;
+		if (t < count)
 		{
-			uint32_t tl = uint32_t(ty) * pass.tiles_x + uint32_t(tx);
-			atomicOr(&pass.masks[size_t(tl) * RDP_MASK_WORDS_PER_TILE + word], bit);
-			atomicAdd(&tile_counts[pass.tile_item_begin + tl], 1u);
+			int tx = g.bbox[0] + t % tw, ty = g.bbox[1] + t / tw;
+			int lox = tx * 8, loy = ty * 8;
+			int hix = min(lox + 7, fbw - 1), hiy = min(loy + 7, fbh - 1);
+			hit = bin_primitive(g, lox, loy, hix, hiy);
+			if (hit)
+			{
+				uint32_t tl = uint32_t(ty) * pass.tiles_x + uint32_t(tx);
+				atomicOr(&pass.masks[size_t(tl) * RDP_MASK_WORDS_PER_TILE + word], bit);
+				atomicAdd(&tile_counts[pass.tile_item_begin + tl], 1u);
+			}
 		}
+		binned += __popc(__ballot_sync(0xffffffffu, hit));
 	}
+	if (prim_pairs && lane == 0) prim_pairs[warp] = binned;
 }
 
 // ============================================================================ k_tmem
@@ -2445,25 +2460,26 @@ __device__ __forceinline__ bool shade_and_blend(const RdpPass &ps, const PassCon
 }
 
 // ============================================================================ pair list
-// Exclusive scan of the per-tile pair counts into offsets; counts are cleared for the next
-// launch.  ctrl[0] = total pairs, ctrl[1] = 1 when the pairs exceed the scratch capacity.
-// Single CTA: exclusive scan of the per-tile pair counts into pair offsets, the list of
-// non-empty tiles in tile order, and the launch's control words: [0] pairs, [1] overflow,
-// [2] largest pair count seen, [3] non-empty tiles, [4] k_blend work counter (reset).
-__global__ void __launch_bounds__(1024) k_scan(uint32_t num_items, uint32_t *__restrict__ counts,
-                                               uint32_t *__restrict__ offsets, uint32_t *__restrict__ nonempty,
-                                               uint32_t *__restrict__ ctrl, uint32_t capacity,
-                                               uint32_t *__restrict__ pair_log, uint32_t log_slot)
+// Exclusive scans of the per-tile pair counts (into pair offsets, the list of non-empty tiles
+// and the launch's control words) and, for the primitive-major shading order, of the
+// per-primitive pair counts (into each primitive's first position).  Counts are cleared for
+// the next launch (the cleared per-primitive counts are k_expand's cursors).  Control words:
+// [0] pairs, [1] 1 when the pairs exceed the scratch capacity, [2] largest pair count seen,
+// [3] non-empty tiles, [4] k_blend work counter (reset).
+
+// One CTA of 1024 threads scans counts[0, num_items) in steps of 1024; `nonempty` optional.
+// Leaves the total in *carry and the non-empty count in *carry_nz.
+__device__ void cta_scan(uint32_t num_items, uint32_t *__restrict__ counts, uint32_t *__restrict__ offsets,
+                         uint32_t *__restrict__ nonempty, uint32_t *warp_sums, uint32_t *warp_nz, uint32_t *carry,
+                         uint32_t *carry_nz)
 {
-	__shared__ uint32_t warp_sums[32], warp_nz[32];
-	__shared__ uint32_t carry, carry_nz;
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 	if (threadIdx.x == 0)
 	{
-		carry = 0;
-		carry_nz = 0;
+		*carry = 0;
+		*carry_nz = 0;
 	}
 	__syncthreads();
-	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 	for (uint32_t base = 0; base < num_items; base += 1024)
 	{
 		uint32_t i = base + threadIdx.x;
@@ -2501,33 +2517,63 @@ __global__ void __launch_bounds__(1024) k_scan(uint32_t num_items, uint32_t *__r
 			warp_nz[lane] = z;
 		}
 		__syncthreads();
-		uint32_t prefix = carry + (wid ? warp_sums[wid - 1] : 0u) + x - v;
-		uint32_t nz_pos = carry_nz + (wid ? warp_nz[wid - 1] : 0u) + __popc(nzmask & ((1u << lane) - 1u));
+		uint32_t prefix = *carry + (wid ? warp_sums[wid - 1] : 0u) + x - v;
+		uint32_t nz_pos = *carry_nz + (wid ? warp_nz[wid - 1] : 0u) + __popc(nzmask & ((1u << lane) - 1u));
 		if (i < num_items) offsets[i] = prefix;
-		if (v) nonempty[nz_pos] = i;
+		if (v && nonempty) nonempty[nz_pos] = i;
 		__syncthreads();
 		if (threadIdx.x == 1023)
 		{
-			carry = prefix + v;
-			carry_nz = nz_pos + (v ? 1u : 0u);
+			*carry = prefix + v;
+			*carry_nz = nz_pos + (v ? 1u : 0u);
 		}
 		__syncthreads();
 	}
+}
+
+// Writes the launch's control words from the pair total (one thread).
+__device__ __forceinline__ void write_ctrl(uint32_t pairs, uint32_t nonempty_tiles, uint32_t *__restrict__ ctrl,
+                                           uint32_t capacity, uint32_t *__restrict__ pair_log, uint32_t log_slot)
+{
+	ctrl[0] = pairs;
+	ctrl[1] = pairs > capacity ? 1u : 0u;
+	ctrl[2] = max(ctrl[2], pairs); // largest pair count seen: the host grows the scratch to it
+	ctrl[3] = nonempty_tiles;
+	ctrl[4] = 0u;
+	// Per-launch pair count for the autotuner; an overflowing launch is not a sample.
+	if (pair_log) pair_log[log_slot] = pairs > capacity ? 0xffffffffu : pairs;
+}
+
+// Zeroes k_shade's work queues: the per-SM counters and their used-up bitmask.
+__device__ __forceinline__ void clear_queues(uint32_t *__restrict__ queues, uint32_t num_queues)
+{
+	for (uint32_t q = threadIdx.x; q < num_queues + (num_queues + 31) / 32; q += blockDim.x) queues[q] = 0u;
+}
+
+// Single CTA: the tile scan, then (num_prims > 0) the primitive scan.
+__global__ void __launch_bounds__(1024) k_scan(uint32_t num_items, uint32_t *__restrict__ counts,
+                                               uint32_t *__restrict__ offsets, uint32_t *__restrict__ nonempty,
+                                               uint32_t *__restrict__ ctrl, uint32_t capacity,
+                                               uint32_t *__restrict__ pair_log, uint32_t log_slot,
+                                               uint32_t *__restrict__ queues, uint32_t num_queues, uint32_t num_prims,
+                                               uint32_t *__restrict__ prim_counts, uint32_t *__restrict__ prim_offsets)
+{
+	__shared__ uint32_t warp_sums[32], warp_nz[32];
+	__shared__ uint32_t carry, carry_nz;
+	clear_queues(queues, num_queues);
+	cta_scan(num_items, counts, offsets, nonempty, warp_sums, warp_nz, &carry, &carry_nz);
 	if (threadIdx.x == 0)
 	{
 		offsets[num_items] = carry;
-		ctrl[0] = carry;
-		ctrl[1] = carry > capacity ? 1u : 0u;
-		ctrl[2] = max(ctrl[2], carry); // largest pair count seen: the host grows the scratch to it
-		ctrl[3] = carry_nz;
-		ctrl[4] = 0u;
-		// Per-launch pair count for the autotuner; an overflowing launch is not a sample.
-		if (pair_log) pair_log[log_slot] = carry > capacity ? 0xffffffffu : carry;
+		write_ctrl(carry, carry_nz, ctrl, capacity, pair_log, log_slot);
 	}
+	__syncthreads();
+	if (num_prims) cta_scan(num_prims, prim_counts, prim_offsets, nullptr, warp_sums, warp_nz, &carry, &carry_nz);
 }
 
-// Multi-CTA form of k_scan for launches with many tiles: SCAN_TILE tiles per CTA.
-// k_scan_reduce: per-CTA pair and non-empty counts; k_scan_top (1 CTA): their exclusive
+// Multi-CTA form for launches with many tiles or primitives: SCAN_TILE items per CTA.  The
+// first `split` CTAs of k_scan_reduce / k_scan_down take the tiles, the rest the primitives.
+// k_scan_reduce: per-CTA sums and non-empty counts; k_scan_top (1 CTA): their exclusive
 // prefixes and the control words; k_scan_down: per-CTA scan plus prefix, offsets, tile list.
 constexpr int SCAN_THREADS = 256, SCAN_PER_THREAD = 4, SCAN_TILE = SCAN_THREADS * SCAN_PER_THREAD;
 
@@ -2563,10 +2609,20 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *w
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(uint32_t num_items, const uint32_t *__restrict__ counts,
-                                                             uint32_t *__restrict__ block_sums)
+                                                             uint32_t *__restrict__ block_sums, uint32_t split,
+                                                             uint32_t num_prims, const uint32_t *__restrict__ prim_counts,
+                                                             uint32_t *__restrict__ prim_sums)
 {
 	__shared__ uint32_t warp_sums[32];
-	const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+	uint32_t blk = blockIdx.x;
+	if (blk >= split)
+	{
+		blk -= split;
+		num_items = num_prims;
+		counts = prim_counts;
+		block_sums = prim_sums;
+	}
+	const uint32_t base = blk * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
 	uint32_t sum = 0, nz = 0;
 #pragma unroll
 	for (int k = 0; k < SCAN_PER_THREAD; k++)
@@ -2581,22 +2637,19 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(uint32_t num_items
 	block_exclusive_scan(nz, warp_sums, &tot_nz);
 	if (threadIdx.x == 0)
 	{
-		block_sums[2 * blockIdx.x] = tot_sum;
-		block_sums[2 * blockIdx.x + 1] = tot_nz;
+		block_sums[2 * blk] = tot_sum;
+		block_sums[2 * blk + 1] = tot_nz;
 	}
 }
 
-__global__ void __launch_bounds__(1024) k_scan_top(uint32_t num_blocks, uint32_t *__restrict__ block_sums,
-                                                   uint32_t num_items, uint32_t *__restrict__ offsets,
-                                                   uint32_t *__restrict__ ctrl, uint32_t capacity,
-                                                   uint32_t *__restrict__ pair_log, uint32_t log_slot)
+// Exclusive prefixes of num_blocks (sum, non-empty) pairs in place; totals to *carry, *carry_nz.
+__device__ void scan_block_sums(uint32_t num_blocks, uint32_t *__restrict__ block_sums, uint32_t *warp_sums,
+                                uint32_t *carry, uint32_t *carry_nz)
 {
-	__shared__ uint32_t warp_sums[32];
-	__shared__ uint32_t carry, carry_nz;
 	if (threadIdx.x == 0)
 	{
-		carry = 0;
-		carry_nz = 0;
+		*carry = 0;
+		*carry_nz = 0;
 	}
 	__syncthreads();
 	for (uint32_t b0 = 0; b0 < num_blocks; b0 += 1024)
@@ -2608,35 +2661,59 @@ __global__ void __launch_bounds__(1024) k_scan_top(uint32_t num_blocks, uint32_t
 		const uint32_t pz = block_exclusive_scan(z, warp_sums, &tz);
 		if (b < num_blocks)
 		{
-			block_sums[2 * b] = carry + ps;
-			block_sums[2 * b + 1] = carry_nz + pz;
+			block_sums[2 * b] = *carry + ps;
+			block_sums[2 * b + 1] = *carry_nz + pz;
 		}
 		__syncthreads();
 		if (threadIdx.x == 0)
 		{
-			carry += ts;
-			carry_nz += tz;
+			*carry += ts;
+			*carry_nz += tz;
 		}
 		__syncthreads();
 	}
+}
+
+__global__ void __launch_bounds__(1024) k_scan_top(uint32_t num_blocks, uint32_t *__restrict__ block_sums,
+                                                   uint32_t num_items, uint32_t *__restrict__ offsets,
+                                                   uint32_t *__restrict__ ctrl, uint32_t capacity,
+                                                   uint32_t *__restrict__ pair_log, uint32_t log_slot,
+                                                   uint32_t *__restrict__ queues, uint32_t num_queues,
+                                                   uint32_t num_prim_blocks, uint32_t *__restrict__ prim_sums)
+{
+	__shared__ uint32_t warp_sums[32];
+	__shared__ uint32_t carry, carry_nz;
+	clear_queues(queues, num_queues);
+	scan_block_sums(num_blocks, block_sums, warp_sums, &carry, &carry_nz);
 	if (threadIdx.x == 0)
 	{
 		offsets[num_items] = carry;
-		ctrl[0] = carry;
-		ctrl[1] = carry > capacity ? 1u : 0u;
-		ctrl[2] = max(ctrl[2], carry);
-		ctrl[3] = carry_nz;
-		ctrl[4] = 0u;
-		if (pair_log) pair_log[log_slot] = carry > capacity ? 0xffffffffu : carry;
+		write_ctrl(carry, carry_nz, ctrl, capacity, pair_log, log_slot);
 	}
+	__syncthreads();
+	if (num_prim_blocks) scan_block_sums(num_prim_blocks, prim_sums, warp_sums, &carry, &carry_nz);
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(uint32_t num_items, uint32_t *__restrict__ counts,
                                                            const uint32_t *__restrict__ block_sums,
-                                                           uint32_t *__restrict__ offsets, uint32_t *__restrict__ nonempty)
+                                                           uint32_t *__restrict__ offsets, uint32_t *__restrict__ nonempty,
+                                                           uint32_t split, uint32_t num_prims,
+                                                           uint32_t *__restrict__ prim_counts,
+                                                           const uint32_t *__restrict__ prim_sums,
+                                                           uint32_t *__restrict__ prim_offsets)
 {
 	__shared__ uint32_t warp_sums[32];
-	const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
+	uint32_t blk = blockIdx.x;
+	if (blk >= split)
+	{
+		blk -= split;
+		num_items = num_prims;
+		counts = prim_counts;
+		block_sums = prim_sums;
+		offsets = prim_offsets;
+		nonempty = nullptr;
+	}
+	const uint32_t base = blk * SCAN_TILE + threadIdx.x * SCAN_PER_THREAD;
 	uint32_t v[SCAN_PER_THREAD], sum = 0, nz = 0;
 #pragma unroll
 	for (int k = 0; k < SCAN_PER_THREAD; k++)
@@ -2647,15 +2724,15 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(uint32_t num_items, 
 		nz += v[k] != 0;
 	}
 	uint32_t ts, tz;
-	uint32_t ps = block_exclusive_scan(sum, warp_sums, &ts) + block_sums[2 * blockIdx.x];
-	uint32_t pz = block_exclusive_scan(nz, warp_sums, &tz) + block_sums[2 * blockIdx.x + 1];
+	uint32_t ps = block_exclusive_scan(sum, warp_sums, &ts) + block_sums[2 * blk];
+	uint32_t pz = block_exclusive_scan(nz, warp_sums, &tz) + block_sums[2 * blk + 1];
 #pragma unroll
 	for (int k = 0; k < SCAN_PER_THREAD; k++)
 	{
 		if (base + k < num_items)
 		{
 			offsets[base + k] = ps;
-			if (v[k]) nonempty[pz++] = base + k;
+			if (v[k] && nonempty) nonempty[pz++] = base + k;
 		}
 		ps += v[k];
 	}
@@ -2664,9 +2741,14 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(uint32_t num_items, 
 // One warp per tile: turns the tile's primitive bitmask into its ordered run of
 // (primitive, tile) pairs and clears the bitmask.
 // With `featbits`, also writes the tile's scheduling features (sched.h) to features[item].
+// With `perm`, also places each pair in primitive-major order: perm[prim_offsets[prim] + n] =
+// its pair index, n counted by prim_cursor (zeroed by k_scan_down); the order of one
+// primitive's tiles is arbitrary, which changes no result.
 __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes, uint32_t num_items,
                          const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ ctrl, uint2 *__restrict__ pairs,
-                         const uint16_t *__restrict__ featbits, float *__restrict__ features, bool train)
+                         const uint16_t *__restrict__ featbits, float *__restrict__ features, bool train,
+                         const uint32_t *__restrict__ prim_offsets, uint32_t *__restrict__ prim_cursor,
+                         uint32_t *__restrict__ perm)
 {
 	uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	int lane = threadIdx.x & 31;
@@ -2705,6 +2787,7 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 				int b = __ffs(wv) - 1;
 				wv &= wv - 1;
 				const uint32_t prim = ps.prim_begin + wi * 32 + uint32_t(b);
+				if (perm) perm[prim_offsets[prim] + atomicAdd(&prim_cursor[prim], 1u)] = pos;
 				pairs[pos++] = make_uint2(prim, item);
 				if (featbits)
 				{
@@ -2750,6 +2833,60 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 // structure-of-arrays per pair: combined colour, z | dither, coverage | shade alpha << 8.
 constexpr int SHADE_THREADS = 64;
 
+// Work distribution.  Without queues, CTA b shades positions b, b + grid, b + 2 grid, ...
+// With queues (one counter per SM, then a bitmask of used-up queues; zeroed by k_scan),
+// positions are dealt in chunks of SHADE_CHUNK: queue q owns chunks q, q + nq, q + 2 nq, ...,
+// and a CTA takes positions from the queue of the SM it runs on (one atomic per position,
+// issued a position ahead), so the CTAs of one SM shade neighbouring positions at the same
+// time.  A CTA that finds a queue used up marks it in the bitmask and moves to the next queue
+// not marked; it exits only when every queue is marked, so every position is shaded whatever
+// SMs the CTAs land on.  Launches with fewer than `queue_min` positions per CTA use the fixed
+// stride (the queues' first atomic and final sweep cost more than they gain there).  With
+// `perm` (k_expand), position j is pair perm[j]: primitive-major order, so neighbouring
+// positions mostly share a primitive (same shading path, state and texels).
+constexpr uint32_t SHADE_CHUNK = 128;
+
+__device__ __forceinline__ uint32_t sm_id()
+{
+	uint32_t r;
+	asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+	return r;
+}
+
+__device__ __forceinline__ uint32_t queue_pos(uint32_t q, uint32_t k, uint32_t nq)
+{
+	return (q + (k / SHADE_CHUNK) * nq) * SHADE_CHUNK + k % SHADE_CHUNK;
+}
+
+// Next position after queue q was found used up; 0xffffffff once every queue is.  At most nq
+// attempts: each failed one marks another queue.
+__device__ __noinline__ uint32_t queue_steal(uint32_t *queues, uint32_t nq, uint32_t total, uint32_t &q)
+{
+	uint32_t *used = queues + nq;
+	const uint32_t nw = (nq + 31) >> 5;
+	atomicOr(&used[q >> 5], 1u << (q & 31));
+	for (uint32_t attempt = 0; attempt < nq; attempt++)
+	{
+		const uint32_t start = q + 1 < nq ? q + 1 : 0u;
+		uint32_t found = 0xffffffffu;
+		for (uint32_t i = 0; i <= nw && found == 0xffffffffu; i++)
+		{
+			uint32_t w = (start >> 5) + i;
+			w = w < nw ? w : w - nw;
+			uint32_t open = ~*reinterpret_cast<volatile const uint32_t *>(used + w);
+			if (w == nw - 1 && (nq & 31)) open &= (1u << (nq & 31)) - 1u;
+			if (i == 0) open &= ~0u << (start & 31);
+			if (open) found = w * 32 + uint32_t(__ffs(int(open)) - 1);
+		}
+		if (found == 0xffffffffu) return found;
+		q = found;
+		const uint32_t j = queue_pos(q, atomicAdd(&queues[q], 1u), nq);
+		if (j < total) return j;
+		atomicOr(&used[q >> 5], 1u << (q & 31));
+	}
+	return 0xffffffffu;
+}
+
 // Compiled for several minimum residencies (register budgets); the executor's autotuner
 // picks one.  More resident CTAs hide more latency at the price of some spilling.
 template <int MIN_CTAS>
@@ -2760,15 +2897,35 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass
                                                         const RdpPrimShade *__restrict__ shade,
                                                         const RdpTile *__restrict__ tilesets,
                                                         uint32_t *__restrict__ sc_color, int *__restrict__ sc_zdith,
-                                                        uint16_t *__restrict__ sc_misc)
+                                                        uint16_t *__restrict__ sc_misc, const uint32_t *__restrict__ perm,
+                                                        uint32_t *__restrict__ queues, uint32_t num_queues,
+                                                        uint32_t queue_min)
 {
 	__shared__ SpanA s_sa[9];
 	__shared__ SpanX s_sx[9];
+	__shared__ uint32_t s_next;
 	if (ctrl[1]) return;
 	const uint32_t total = ctrl[0];
 	const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-	for (uint32_t pr = blockIdx.x; pr < total; pr += gridDim.x)
+	if (total < gridDim.x * queue_min) queues = nullptr;
+	uint32_t q = 0, k_next = 0, j = blockIdx.x;
+	if (queues)
 	{
+		if (tid == 0)
+		{
+			q = sm_id() % num_queues;
+			uint32_t first = queue_pos(q, atomicAdd(&queues[q], 1u), num_queues);
+			if (first >= total) first = queue_steal(queues, num_queues, total, q);
+			s_next = first;
+		}
+		__syncthreads();
+		j = s_next;
+	}
+	while (j < total)
+	{
+		// The next position's atomic is issued now; its result is first needed after shading.
+		if (queues && tid == 0) k_next = atomicAdd(&queues[q], 1u);
+		const uint32_t pr = perm ? perm[j] : j;
 		uint2 pa = pairs[pr];
 		uint32_t prim = pa.x, item = pa.y;
 		const uint32_t pi = pass_of_item(passes, num_passes, item);
@@ -2809,14 +2966,30 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass
 		sc_color[at] = ok ? out.combined : 0u;
 		sc_zdith[at] = ok ? out.z_dith : 0;
 		sc_misc[at] = ok ? uint16_t((out.coverage & 0xff) | (out.shade_alpha << 8)) : uint16_t(0x00ffu);
-		__syncthreads();
+		if (queues)
+		{
+			if (tid == 0)
+			{
+				uint32_t nj = queue_pos(q, k_next, num_queues);
+				if (nj >= total) nj = queue_steal(queues, num_queues, total, q);
+				s_next = nj;
+			}
+			__syncthreads();
+			j = s_next;
+		}
+		else
+		{
+			__syncthreads();
+			j += gridDim.x;
+		}
 	}
 }
 
 // Compacted shading: a CTA of COMPACT_THREADS takes COMPACT_PAIRS consecutive pairs, computes
 // their spans into shared memory, marks the pixels that lie inside a valid span (only those can
 // have coverage), and shades just those -- about half of a tile's pixels on typical scenes, so
-// lanes no longer idle on uncovered pixels.  Results are identical to k_shade.
+// lanes no longer idle on uncovered pixels.  Results are identical to k_shade.  It takes the
+// pairs in tile order with a fixed stride (no queues, no primitive-major order).
 constexpr int COMPACT_THREADS = 128;
 constexpr int COMPACT_PAIRS = 4;
 
@@ -2826,7 +2999,7 @@ __global__ void __launch_bounds__(COMPACT_THREADS, MIN_CTAS)
 	                const uint32_t *__restrict__ ctrl, const RdpPrimGeom *__restrict__ geom,
 	                const RdpPrimAttr *__restrict__ attr, const RdpPrimShade *__restrict__ shade,
 	                const RdpTile *__restrict__ tilesets, uint32_t *__restrict__ sc_color, int *__restrict__ sc_zdith,
-	                uint16_t *__restrict__ sc_misc)
+	                uint16_t *__restrict__ sc_misc, const uint32_t *, uint32_t *, uint32_t, uint32_t)
 {
 	__shared__ SpanA s_sa[COMPACT_PAIRS][9];
 	__shared__ SpanX s_sx[COMPACT_PAIRS][9];
@@ -3239,7 +3412,8 @@ extern "C" cudaError_t rdp_kernels_init_luts(const uint8_t *blender_lut)
 
 namespace {
 typedef void (*ShadeKernel)(const RdpPass *, uint32_t, const uint2 *, const uint32_t *, const RdpPrimGeom *,
-                            const RdpPrimAttr *, const RdpPrimShade *, const RdpTile *, uint32_t *, int *, uint16_t *);
+                            const RdpPrimAttr *, const RdpPrimShade *, const RdpTile *, uint32_t *, int *, uint16_t *,
+                            const uint32_t *, uint32_t *, uint32_t, uint32_t);
 const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = { rdp::k_shade<1>,  rdp::k_shade<12>, rdp::k_shade<16>,
                                                          rdp::k_shade<20>, rdp::k_shade<24>, rdp::k_shade<28>,
                                                          rdp::k_shade<32>, rdp::k_shade_compact<12> };
@@ -3266,6 +3440,13 @@ extern "C" int rdp_kernels_shade_ctas_per_sm(int variant)
 	return n > 0 ? n : 1;
 }
 
+// Launches with many tiles (or, in primitive-major order, many primitives) scan with several CTAs.
+static bool multi_cta_scan(const RdpLaunch *L)
+{
+	return L->scan_blocks && (L->num_tile_items > RDP_SCAN_SINGLE_CTA_MAX ||
+	                          (L->pair_perm && L->prim_scan_blocks && L->num_prims > RDP_SCAN_SINGLE_CTA_MAX));
+}
+
 extern "C" uint32_t rdp_kernels_count(const RdpLaunch *L)
 {
 	uint32_t n = 0;
@@ -3274,7 +3455,7 @@ extern "C" uint32_t rdp_kernels_count(const RdpLaunch *L)
 	if (L->num_prims && L->num_tile_items)
 	{
 		n += 5;
-		if (L->num_tile_items > RDP_SCAN_SINGLE_CTA_MAX && L->scan_blocks) n += 2;
+		if (multi_cta_scan(L)) n += 2;
 		if (L->sched && (L->sched->order_enabled || L->sched->train_enabled))
 		{
 			n += 3;
@@ -3297,7 +3478,9 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		                                                                       ? L->sched->featbits
 		                                                                       : nullptr);
 		rdp::k_bin<<<(L->num_prims * 32 + 255) / 256, 256, 0, stream>>>(L->num_prims, L->geom, L->shade, L->passes,
-		                                                                 L->tile_counts);
+		                                                                 L->tile_counts,
+		                                                                 L->pair_perm && L->num_tile_items ? L->prim_pairs
+		                                                                                                   : nullptr);
 	}
 	if (L->num_tmem_passes)
 	{
@@ -3308,23 +3491,31 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 	}
 	if (raster)
 	{
-		if (L->num_tile_items > RDP_SCAN_SINGLE_CTA_MAX && L->scan_blocks)
+		// The primitive scan (primitive-major shading order) rides in the tile scan's launches.
+		const uint32_t scan_prims = L->pair_perm ? L->num_prims : 0u;
+		if (multi_cta_scan(L))
 		{
 			const uint32_t nb = (L->num_tile_items + rdp::SCAN_TILE - 1) / rdp::SCAN_TILE;
-			rdp::k_scan_reduce<<<nb, rdp::SCAN_THREADS, 0, stream>>>(L->num_tile_items, L->tile_counts, L->scan_blocks);
+			const uint32_t nbp = (scan_prims + rdp::SCAN_TILE - 1) / rdp::SCAN_TILE;
+			rdp::k_scan_reduce<<<nb + nbp, rdp::SCAN_THREADS, 0, stream>>>(L->num_tile_items, L->tile_counts,
+			                                                               L->scan_blocks, nb, scan_prims,
+			                                                               L->prim_pairs, L->prim_scan_blocks);
 			rdp::k_scan_top<<<1, 1024, 0, stream>>>(nb, L->scan_blocks, L->num_tile_items, L->pair_offsets, L->ctrl,
-			                                        L->pair_capacity, L->pair_log, L->log_slot);
-			rdp::k_scan_down<<<nb, rdp::SCAN_THREADS, 0, stream>>>(L->num_tile_items, L->tile_counts, L->scan_blocks,
-			                                                       L->pair_offsets, L->nonempty_tiles);
+			                                        L->pair_capacity, L->pair_log, L->log_slot, L->shade_queues,
+			                                        L->num_shade_queues, nbp, L->prim_scan_blocks);
+			rdp::k_scan_down<<<nb + nbp, rdp::SCAN_THREADS, 0, stream>>>(
+				L->num_tile_items, L->tile_counts, L->scan_blocks, L->pair_offsets, L->nonempty_tiles, nb, scan_prims,
+				L->prim_pairs, L->prim_scan_blocks, L->prim_offsets);
 		}
 		else
 			rdp::k_scan<<<1, 1024, 0, stream>>>(L->num_tile_items, L->tile_counts, L->pair_offsets, L->nonempty_tiles,
-			                                    L->ctrl, L->pair_capacity, L->pair_log, L->log_slot);
+			                                    L->ctrl, L->pair_capacity, L->pair_log, L->log_slot, L->shade_queues,
+			                                    L->num_shade_queues, scan_prims, L->prim_pairs, L->prim_offsets);
 		const bool sched = L->sched && (L->sched->order_enabled || L->sched->train_enabled);
 		rdp::k_expand<<<(L->num_tile_items * 32 + 255) / 256, 256, 0, stream>>>(
 			L->passes, L->num_passes, L->num_tile_items, L->pair_offsets, L->ctrl, L->pairs,
 			sched ? L->sched->featbits : nullptr, sched ? L->sched->features : nullptr,
-			sched && L->sched->train_enabled && L->tile_cycles);
+			sched && L->sched->train_enabled && L->tile_cycles, L->prim_offsets, L->prim_pairs, L->pair_perm);
 		// Inside a stream capture the events become record nodes of the graph.
 		cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
 		if ((L->shade_events[0] || L->blend_events[0]) && cudaStreamIsCapturing(stream, &capture) != cudaSuccess)
@@ -3335,7 +3526,9 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		const ShadeKernel shade_kernel = kShadeVariants[sv];
 		shade_kernel<<<L->shade_ctas, kShadeThreads[sv], 0, stream>>>(L->passes, L->num_passes, L->pairs, L->ctrl,
 		                                                               L->geom, L->attr, L->shade, L->tilesets,
-		                                                               L->sc_color, L->sc_zdith, L->sc_misc);
+		                                                               L->sc_color, L->sc_zdith, L->sc_misc,
+		                                                               L->pair_perm, L->shade_queues,
+		                                                               L->num_shade_queues, L->shade_queue_min);
 		if (L->shade_events[1]) cudaEventRecordWithFlags(L->shade_events[1], stream, ev_flags);
 		const uint32_t tile_ctas = std::min<uint32_t>(L->num_tile_items, L->blend_ctas);
 		const uint32_t *order = L->tile_order;

@@ -8,7 +8,8 @@
 /* Shading kernels: k_shade (one pair per 64-thread CTA) for minimum residencies of 1, 12, 16,
  * 20, 24, 28 and 32 CTAs per SM, and k_shade_compact (4 pairs per 128-thread CTA, pixels inside
  * the spans only) for 12. */
-/* Launches with more tiles than this scan their pair counts with several CTAs. */
+/* Launches with more tiles (or, in primitive-major order, primitives) than this scan their
+ * pair counts with several CTAs. */
 #define RDP_SCAN_SINGLE_CTA_MAX 16384
 
 #ifndef RDP_SHADE_VARIANTS
@@ -46,6 +47,14 @@ typedef struct RdpLaunch
 	uint32_t *ctrl;                 /* [0] pairs, [1] overflow, [2] max pairs, [3] non-empty tiles, [4] counter */
 	uint32_t pair_capacity;
 	uint32_t shade_ctas;            /* persistent CTAs of k_shade (and of k_blend / k_raster) */
+	uint32_t *shade_queues;         /* optional [num_shade_queues + ceil(num_shade_queues / 32)]: per-SM
+	                                   work queues of k_shade, then their used-up bitmask */
+	uint32_t num_shade_queues;      /* the SM count */
+	uint32_t shade_queue_min;       /* launches with fewer pairs per k_shade CTA take the fixed stride */
+	uint32_t *pair_perm;            /* optional [pair_capacity]: primitive-major shading order (needs queues) */
+	uint32_t *prim_pairs;           /* [num_prims] pair count per primitive (with pair_perm) */
+	uint32_t *prim_offsets;         /* [num_prims] first primitive-major position (with pair_perm) */
+	uint32_t *prim_scan_blocks;     /* [2 * ceil(num_prims / 1024)] (with pair_perm) */
 	uint32_t shade_variant;         /* which compiled k_shade (register budget), < RDP_SHADE_VARIANTS */
 	uint32_t blend_ctas;            /* persistent CTAs of k_blend / k_raster */
 	uint32_t *pair_log;             /* optional: k_scan writes the launch's pair count to pair_log[log_slot] */

@@ -12,12 +12,15 @@ from .native import (  # noqa: F401
     RdpTimeout,
     ScanoutOptions,
     VIRegister,
+    SHADE_ORDERS,
     SHADE_VARIANTS,
     device_is_supported,
+    get_shade_order,
     get_shade_variant,
     mlp_forward,
     mlp_gradients,
     MLP_PARAMS,
+    set_shade_order,
     set_shade_variant,
     library_path,
 )

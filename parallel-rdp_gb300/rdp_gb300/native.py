@@ -93,7 +93,7 @@ EXPORTED_SYMBOLS = [
     "rdp_cp_latch_vi_register_for_scanline", "rdp_cp_end_vi_register_per_scanline",
     "rdp_batch_create", "rdp_batch_destroy", "rdp_batch_add_instance", "rdp_batch_submit", "rdp_batch_idle",
     "rdp_batch_get_stats", "rdp_batch_capture_begin", "rdp_batch_capture_end", "rdp_set_shade_variant",
-    "rdp_get_shade_variant", "rdp_batch_set_schedule", "rdp_batch_get_model", "rdp_batch_set_model",
+    "rdp_get_shade_variant", "rdp_set_shade_order", "rdp_get_shade_order", "rdp_batch_set_schedule", "rdp_batch_get_model", "rdp_batch_set_model",
     "rdp_mlp_gradients", "rdp_mlp_forward", "rdp_batch_get_tile_samples", "rdp_graph_last_blend_ms",
     "rdp_serve_run", "rdp_batch_enqueue_many", "rdp_dump_writer_open", "rdp_dump_writer_flush_rdram",
     "rdp_dump_writer_flush_hidden_rdram", "rdp_dump_writer_command", "rdp_dump_writer_set_vi_register",
@@ -194,6 +194,8 @@ def lib():
     L.rdp_graph_shade_launches.restype = u32
     L.rdp_set_shade_variant.argtypes = [ctypes.c_int, ctypes.c_int]
     L.rdp_get_shade_variant.argtypes = [ctypes.c_int]
+    L.rdp_set_shade_order.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.rdp_get_shade_order.argtypes = [ctypes.c_int]
     L.rdp_batch_set_schedule.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, u32]
     L.rdp_batch_get_model.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_float)]
     L.rdp_batch_set_model.argtypes = [vp, vp]
@@ -225,6 +227,21 @@ def set_shade_variant(variant, device=0):
 def get_shade_variant(device=0):
     """The device's shading-kernel variant; -1 while the autotuner is still timing them."""
     return lib().rdp_get_shade_variant(device)
+
+
+SHADE_ORDERS = {"strided": 0, "sm_queues": 1, "primitive_major": 2}
+
+
+def set_shade_order(order, device=0):
+    """How the shading kernel takes a launch's pairs: 0 = tile order, fixed stride per CTA;
+    1 = tile order through per-SM work queues; 2 (default) = primitive-major order through the
+    queues.  Small launches take the next simpler order (thresholds: RDP_SHADE_PERM_MIN_PRIMS,
+    RDP_SHADE_QUEUE_MIN, read when a processor or batch is created)."""
+    _check(lib().rdp_set_shade_order(device, order), "set_shade_order")
+
+
+def get_shade_order(device=0):
+    return lib().rdp_get_shade_order(device)
 
 
 MLP_PARAMS = 5313

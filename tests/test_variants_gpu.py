@@ -3,7 +3,8 @@ RDRAM / hidden RDRAM / TMEM bytes, and the autotuner settles on one of them."""
 import numpy as np
 import pytest
 
-from rdp_gb300 import SHADE_VARIANTS, Batch, cmdgen, get_shade_variant, set_shade_variant
+from rdp_gb300 import (SHADE_ORDERS, SHADE_VARIANTS, Batch, cmdgen, get_shade_order, get_shade_variant,
+                       set_shade_order, set_shade_variant)
 from rdp_testutil import assert_parity, run_gpu
 
 pytestmark = pytest.mark.gpu
@@ -51,3 +52,62 @@ def test_autotuner_picks_a_variant(restore_tuning):
             if get_shade_variant() >= 0:
                 break
     assert 0 <= get_shade_variant() < SHADE_VARIANTS
+
+
+@pytest.fixture
+def restore_order():
+    before = get_shade_order()
+    yield
+    set_shade_order(before)
+
+
+def _order_run(words, rdram, streams):
+    single = run_gpu(words, rdram)[:3]
+    with Batch() as b:
+        insts = [b.add_instance(rd.copy()) for _, rd in streams]
+        for cp, (w, _) in zip(insts, streams):
+            cp.enqueue_command(w)
+        b.idle()
+        batched = [cp.begin_read_rdram().copy() for cp in insts]
+        batched += [cp.begin_read_hidden_rdram().copy() for cp in insts]
+    return single, batched
+
+
+def test_shade_orders_bit_exact(restore_order, monkeypatch):
+    """Tile order with a fixed stride, per-SM work queues and primitive-major order shade the
+    same pairs: identical bytes, on a single stream and on a batch of instances.  The size
+    thresholds are set to 0 so that every launch, down to the smallest, takes the queues (and
+    their stealing sweep) and the primitive-major order; one more run keeps the default
+    thresholds.  The single stream's big pass (10,000 primitives, 1,200 tiles) takes the one-CTA
+    scans, the batch's launches the multi-CTA ones."""
+    p = cmdgen.default_params(cmdgen.CONFIG_TEXTURED, seed=5, num_prims=10000)
+    words, rdram, _ = cmdgen.generate_stream(p)
+    streams = []
+    for i in range(8):
+        q = cmdgen.batched_instance_params(i, min_prims=3000, max_prims=6000, seed_base=70)
+        w, rd, _ = cmdgen.generate_stream(q)
+        streams.append((w, rd))
+    set_shade_order(SHADE_ORDERS["strided"])
+    base = _order_run(words, rdram, streams)
+    runs = []
+    monkeypatch.setenv("RDP_SHADE_PERM_MIN_PRIMS", "0")
+    monkeypatch.setenv("RDP_SHADE_QUEUE_MIN", "0")
+    for order in (SHADE_ORDERS["sm_queues"], SHADE_ORDERS["primitive_major"]):
+        set_shade_order(order)
+        assert get_shade_order() == order
+        if order == SHADE_ORDERS["primitive_major"]:
+            assert_parity(words, rdram)
+        runs.append(_order_run(words, rdram, streams))
+    monkeypatch.delenv("RDP_SHADE_PERM_MIN_PRIMS")
+    monkeypatch.delenv("RDP_SHADE_QUEUE_MIN")
+    runs.append(_order_run(words, rdram, streams))
+    for single, batched in runs:
+        for x, y in zip(single, base[0]):
+            assert np.array_equal(x, y)
+        for x, y in zip(batched, base[1]):
+            assert np.array_equal(x, y)
+
+
+def test_shade_order_rejects_unknown():
+    with pytest.raises(Exception):
+        set_shade_order(3)

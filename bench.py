@@ -278,7 +278,7 @@ def run_ours_textured(args):
     tpath = os.path.join(ROOT, "profiles", "k_shade_traffic.json")
     if os.path.exists(tpath):
         try:
-            per_pair = json.load(open(tpath)).get("dram_bytes_per_tile_instance")
+            per_pair = json.load(open(tpath)).get("textured_frame", {}).get("dram_bytes_per_tile_instance")
             traffic = per_pair * base["tile_instances"] / shade_launches if per_pair else None
         except (OSError, ValueError):
             traffic = None

@@ -176,7 +176,8 @@ struct Executor
 	uint32_t *d_masks = nullptr, *d_tmem_keep = nullptr;
 	uint32_t *d_tile_counts = nullptr, *d_pair_offsets = nullptr, *d_ctrl = nullptr;
 	uint32_t *d_tile_order = nullptr, *d_tile_cycles = nullptr, *d_nonempty = nullptr, *d_scan_blocks = nullptr;
-	uint32_t *d_prim_pairs = nullptr, *d_prim_offsets = nullptr, *d_prim_blocks = nullptr, *d_perm = nullptr;
+	uint32_t *d_prim_pairs = nullptr, *d_prim_offsets = nullptr, *d_prim_blocks = nullptr;
+	uint4 *d_shade_list = nullptr; // primitive-major shading records
 	uint2 *d_pairs = nullptr;
 	uint32_t *d_sc_color = nullptr;
 	int *d_sc_zdith = nullptr;
@@ -433,7 +434,7 @@ struct Executor
 		cudaFree(d_prim_pairs);
 		cudaFree(d_prim_offsets);
 		cudaFree(d_prim_blocks);
-		cudaFree(d_perm);
+		cudaFree(d_shade_list);
 		cudaFree(d_pairs);
 		cudaFree(d_sc_color);
 		cudaFree(d_sc_zdith);
@@ -444,7 +445,8 @@ struct Executor
 		d_shade = nullptr;
 		d_masks = d_tmem_keep = d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = d_nonempty = nullptr;
 		d_scan_blocks = nullptr;
-		d_prim_pairs = d_prim_offsets = d_prim_blocks = d_perm = nullptr;
+		d_prim_pairs = d_prim_offsets = d_prim_blocks = nullptr;
+		d_shade_list = nullptr;
 		d_pairs = nullptr;
 		d_sc_color = nullptr;
 		d_sc_zdith = nullptr;
@@ -539,16 +541,16 @@ struct Executor
 		{
 			uint32_t n = std::max(need.pairs, caps.pairs * 2);
 			cudaFree(d_pairs);
-			cudaFree(d_perm);
+			cudaFree(d_shade_list);
 			cudaFree(d_sc_color);
 			cudaFree(d_sc_zdith);
 			cudaFree(d_sc_misc);
 			d_pairs = nullptr;
-			d_perm = nullptr;
+			d_shade_list = nullptr;
 			d_sc_color = nullptr;
 			d_sc_zdith = nullptr;
 			d_sc_misc = nullptr;
-			if (check(cudaMalloc(&d_pairs, size_t(n) * sizeof(uint2))) || check(cudaMalloc(&d_perm, size_t(n) * 4)) ||
+			if (check(cudaMalloc(&d_pairs, size_t(n) * sizeof(uint2))) || check(cudaMalloc(&d_shade_list, size_t(n) * sizeof(uint4))) ||
 			    check(cudaMalloc(&d_sc_color, size_t(n) * 64 * 4)) || check(cudaMalloc(&d_sc_zdith, size_t(n) * 64 * 4)) ||
 			    check(cudaMalloc(&d_sc_misc, size_t(n) * 64 * 2)))
 				return false;
@@ -744,7 +746,7 @@ struct Executor
 		L.shade_queues = shade_order >= 1 ? d_queues : nullptr;
 		L.num_shade_queues = shade_order >= 1 ? num_queues : 0u;
 		L.shade_queue_min = queue_min;
-		L.pair_perm = shade_order == 2 && prim_base >= perm_min_prims ? d_perm : nullptr;
+		L.shade_list = shade_order == 2 && prim_base >= perm_min_prims ? d_shade_list : nullptr;
 		L.prim_pairs = d_prim_pairs;
 		L.prim_offsets = d_prim_offsets;
 		L.prim_scan_blocks = d_prim_blocks;

@@ -2741,14 +2741,14 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(uint32_t num_items, 
 // One warp per tile: turns the tile's primitive bitmask into its ordered run of
 // (primitive, tile) pairs and clears the bitmask.
 // With `featbits`, also writes the tile's scheduling features (sched.h) to features[item].
-// With `perm`, also places each pair in primitive-major order: perm[prim_offsets[prim] + n] =
-// its pair index, n counted by prim_cursor (zeroed by k_scan_down); the order of one
-// primitive's tiles is arbitrary, which changes no result.
+// With `list`, also places each pair in primitive-major order: list[prim_offsets[prim] + n] =
+// {primitive, tile item, pair index, pass}, n counted by prim_cursor (zeroed by k_scan_down);
+// the order of one primitive's tiles is arbitrary, which changes no result.
 __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes, uint32_t num_items,
                          const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ ctrl, uint2 *__restrict__ pairs,
                          const uint16_t *__restrict__ featbits, float *__restrict__ features, bool train,
                          const uint32_t *__restrict__ prim_offsets, uint32_t *__restrict__ prim_cursor,
-                         uint32_t *__restrict__ perm)
+                         uint4 *__restrict__ list)
 {
 	uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	int lane = threadIdx.x & 31;
@@ -2787,7 +2787,7 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 				int b = __ffs(wv) - 1;
 				wv &= wv - 1;
 				const uint32_t prim = ps.prim_begin + wi * 32 + uint32_t(b);
-				if (perm) perm[prim_offsets[prim] + atomicAdd(&prim_cursor[prim], 1u)] = pos;
+				if (list) list[prim_offsets[prim] + atomicAdd(&prim_cursor[prim], 1u)] = make_uint4(prim, item, pos, pi);
 				pairs[pos++] = make_uint2(prim, item);
 				if (featbits)
 				{
@@ -2842,9 +2842,27 @@ constexpr int SHADE_THREADS = 64;
 // not marked; it exits only when every queue is marked, so every position is shaded whatever
 // SMs the CTAs land on.  Launches with fewer than `queue_min` positions per CTA use the fixed
 // stride (the queues' first atomic and final sweep cost more than they gain there).  With
-// `perm` (k_expand), position j is pair perm[j]: primitive-major order, so neighbouring
-// positions mostly share a primitive (same shading path, state and texels).
+// `list` (k_expand), position j is the record list[j] = {primitive, tile item, pair index,
+// pass}: primitive-major order, so neighbouring positions mostly share a primitive (same
+// shading path, state and texels); without it, position j is pair j in tile order.  Thread 0
+// copies the next position's record into shared memory with cp.async while the CTA shades the
+// current one, so no global load chain sits between two pairs.
 constexpr uint32_t SHADE_CHUNK = 128;
+
+// 16- or 8-byte asynchronous global -> shared copy (no registers held while in flight).
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(uint32_t(__cvta_generic_to_shared(smem))),
+	             "l"(gmem)
+	             : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(uint32_t(__cvta_generic_to_shared(smem))),
+	             "l"(gmem)
+	             : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 __device__ __forceinline__ uint32_t sm_id()
 {
@@ -2897,39 +2915,59 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass
                                                         const RdpPrimShade *__restrict__ shade,
                                                         const RdpTile *__restrict__ tilesets,
                                                         uint32_t *__restrict__ sc_color, int *__restrict__ sc_zdith,
-                                                        uint16_t *__restrict__ sc_misc, const uint32_t *__restrict__ perm,
+                                                        uint16_t *__restrict__ sc_misc, const uint4 *__restrict__ list,
                                                         uint32_t *__restrict__ queues, uint32_t num_queues,
                                                         uint32_t queue_min)
 {
 	__shared__ SpanA s_sa[9];
 	__shared__ SpanX s_sx[9];
-	__shared__ uint32_t s_next;
+	__shared__ __align__(16) uint4 s_rec[2]; // current / next position's record
+	__shared__ uint32_t s_pos[2];
 	if (ctrl[1]) return;
 	const uint32_t total = ctrl[0];
 	const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
 	if (total < gridDim.x * queue_min) queues = nullptr;
-	uint32_t q = 0, k_next = 0, j = blockIdx.x;
-	if (queues)
+	uint32_t q = 0, k_next = 0;
+	int buf = 0;
+	// Thread 0: the record of position j into s_rec[b] (asynchronous).
+	auto fetch = [&](uint32_t j, int b) {
+		if (list) cp_async16(&s_rec[b], list + j);
+		else cp_async8(&s_rec[b], pairs + j);
+	};
+	if (tid == 0)
 	{
-		if (tid == 0)
+		uint32_t first = blockIdx.x;
+		if (queues)
 		{
 			q = sm_id() % num_queues;
-			uint32_t first = queue_pos(q, atomicAdd(&queues[q], 1u), num_queues);
+			first = queue_pos(q, atomicAdd(&queues[q], 1u), num_queues);
 			if (first >= total) first = queue_steal(queues, num_queues, total, q);
-			s_next = first;
+			if (first < total) k_next = atomicAdd(&queues[q], 1u);
 		}
-		__syncthreads();
-		j = s_next;
+		if (first < total) fetch(first, 0);
+		s_pos[0] = first;
+		cp_async_wait_all();
 	}
+	__syncthreads();
+	uint32_t j = s_pos[0];
 	while (j < total)
 	{
-		// The next position's atomic is issued now; its result is first needed after shading.
-		if (queues && tid == 0) k_next = atomicAdd(&queues[q], 1u);
-		const uint32_t pr = perm ? perm[j] : j;
-		uint2 pa = pairs[pr];
-		uint32_t prim = pa.x, item = pa.y;
-		const uint32_t pi = pass_of_item(passes, num_passes, item);
-		const RdpPass &ps = passes[pi];
+		const uint4 rec = s_rec[buf];
+		const uint32_t prim = rec.x, item = rec.y, pr = list ? rec.z : j;
+		// Thread 0: the next position (its queue atomic was issued a position ago) and its record.
+		if (tid == 0)
+		{
+			uint32_t nj = j + gridDim.x;
+			if (queues)
+			{
+				nj = queue_pos(q, k_next, num_queues);
+				if (nj >= total) nj = queue_steal(queues, num_queues, total, q);
+				if (nj < total) k_next = atomicAdd(&queues[q], 1u);
+			}
+			if (nj < total) fetch(nj, buf ^ 1);
+			s_pos[buf ^ 1] = nj;
+		}
+		const RdpPass &ps = passes[list ? rec.w : shade[prim].pass];
 		uint32_t tl = item - ps.tile_item_begin;
 		int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
 		const RdpPrimGeom &g = geom[prim];
@@ -2966,22 +3004,10 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass
 		sc_color[at] = ok ? out.combined : 0u;
 		sc_zdith[at] = ok ? out.z_dith : 0;
 		sc_misc[at] = ok ? uint16_t((out.coverage & 0xff) | (out.shade_alpha << 8)) : uint16_t(0x00ffu);
-		if (queues)
-		{
-			if (tid == 0)
-			{
-				uint32_t nj = queue_pos(q, k_next, num_queues);
-				if (nj >= total) nj = queue_steal(queues, num_queues, total, q);
-				s_next = nj;
-			}
-			__syncthreads();
-			j = s_next;
-		}
-		else
-		{
-			__syncthreads();
-			j += gridDim.x;
-		}
+		if (tid == 0) cp_async_wait_all();
+		__syncthreads();
+		buf ^= 1;
+		j = s_pos[buf];
 	}
 }
 
@@ -2999,7 +3025,7 @@ __global__ void __launch_bounds__(COMPACT_THREADS, MIN_CTAS)
 	                const uint32_t *__restrict__ ctrl, const RdpPrimGeom *__restrict__ geom,
 	                const RdpPrimAttr *__restrict__ attr, const RdpPrimShade *__restrict__ shade,
 	                const RdpTile *__restrict__ tilesets, uint32_t *__restrict__ sc_color, int *__restrict__ sc_zdith,
-	                uint16_t *__restrict__ sc_misc, const uint32_t *, uint32_t *, uint32_t, uint32_t)
+	                uint16_t *__restrict__ sc_misc, const uint4 *, uint32_t *, uint32_t, uint32_t)
 {
 	__shared__ SpanA s_sa[COMPACT_PAIRS][9];
 	__shared__ SpanX s_sx[COMPACT_PAIRS][9];
@@ -3413,7 +3439,7 @@ extern "C" cudaError_t rdp_kernels_init_luts(const uint8_t *blender_lut)
 namespace {
 typedef void (*ShadeKernel)(const RdpPass *, uint32_t, const uint2 *, const uint32_t *, const RdpPrimGeom *,
                             const RdpPrimAttr *, const RdpPrimShade *, const RdpTile *, uint32_t *, int *, uint16_t *,
-                            const uint32_t *, uint32_t *, uint32_t, uint32_t);
+                            const uint4 *, uint32_t *, uint32_t, uint32_t);
 const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = { rdp::k_shade<1>,  rdp::k_shade<12>, rdp::k_shade<16>,
                                                          rdp::k_shade<20>, rdp::k_shade<24>, rdp::k_shade<28>,
                                                          rdp::k_shade<32>, rdp::k_shade_compact<12> };
@@ -3444,7 +3470,7 @@ extern "C" int rdp_kernels_shade_ctas_per_sm(int variant)
 static bool multi_cta_scan(const RdpLaunch *L)
 {
 	return L->scan_blocks && (L->num_tile_items > RDP_SCAN_SINGLE_CTA_MAX ||
-	                          (L->pair_perm && L->prim_scan_blocks && L->num_prims > RDP_SCAN_SINGLE_CTA_MAX));
+	                          (L->shade_list && L->prim_scan_blocks && L->num_prims > RDP_SCAN_SINGLE_CTA_MAX));
 }
 
 extern "C" uint32_t rdp_kernels_count(const RdpLaunch *L)
@@ -3479,7 +3505,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		                                                                       : nullptr);
 		rdp::k_bin<<<(L->num_prims * 32 + 255) / 256, 256, 0, stream>>>(L->num_prims, L->geom, L->shade, L->passes,
 		                                                                 L->tile_counts,
-		                                                                 L->pair_perm && L->num_tile_items ? L->prim_pairs
+		                                                                 L->shade_list && L->num_tile_items ? L->prim_pairs
 		                                                                                                   : nullptr);
 	}
 	if (L->num_tmem_passes)
@@ -3492,7 +3518,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 	if (raster)
 	{
 		// The primitive scan (primitive-major shading order) rides in the tile scan's launches.
-		const uint32_t scan_prims = L->pair_perm ? L->num_prims : 0u;
+		const uint32_t scan_prims = L->shade_list ? L->num_prims : 0u;
 		if (multi_cta_scan(L))
 		{
 			const uint32_t nb = (L->num_tile_items + rdp::SCAN_TILE - 1) / rdp::SCAN_TILE;
@@ -3515,7 +3541,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		rdp::k_expand<<<(L->num_tile_items * 32 + 255) / 256, 256, 0, stream>>>(
 			L->passes, L->num_passes, L->num_tile_items, L->pair_offsets, L->ctrl, L->pairs,
 			sched ? L->sched->featbits : nullptr, sched ? L->sched->features : nullptr,
-			sched && L->sched->train_enabled && L->tile_cycles, L->prim_offsets, L->prim_pairs, L->pair_perm);
+			sched && L->sched->train_enabled && L->tile_cycles, L->prim_offsets, L->prim_pairs, L->shade_list);
 		// Inside a stream capture the events become record nodes of the graph.
 		cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
 		if ((L->shade_events[0] || L->blend_events[0]) && cudaStreamIsCapturing(stream, &capture) != cudaSuccess)
@@ -3527,7 +3553,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		shade_kernel<<<L->shade_ctas, kShadeThreads[sv], 0, stream>>>(L->passes, L->num_passes, L->pairs, L->ctrl,
 		                                                               L->geom, L->attr, L->shade, L->tilesets,
 		                                                               L->sc_color, L->sc_zdith, L->sc_misc,
-		                                                               L->pair_perm, L->shade_queues,
+		                                                               L->shade_list, L->shade_queues,
 		                                                               L->num_shade_queues, L->shade_queue_min);
 		if (L->shade_events[1]) cudaEventRecordWithFlags(L->shade_events[1], stream, ev_flags);
 		const uint32_t tile_ctas = std::min<uint32_t>(L->num_tile_items, L->blend_ctas);

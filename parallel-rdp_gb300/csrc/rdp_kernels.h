@@ -51,10 +51,11 @@ typedef struct RdpLaunch
 	                                   work queues of k_shade, then their used-up bitmask */
 	uint32_t num_shade_queues;      /* the SM count */
 	uint32_t shade_queue_min;       /* launches with fewer pairs per k_shade CTA take the fixed stride */
-	uint32_t *pair_perm;            /* optional [pair_capacity]: primitive-major shading order (needs queues) */
-	uint32_t *prim_pairs;           /* [num_prims] pair count per primitive (with pair_perm) */
-	uint32_t *prim_offsets;         /* [num_prims] first primitive-major position (with pair_perm) */
-	uint32_t *prim_scan_blocks;     /* [2 * ceil(num_prims / 1024)] (with pair_perm) */
+	uint4 *shade_list;              /* optional [pair_capacity]: primitive-major shading order, one
+	                                   {primitive, tile item, pair index, pass} record per position */
+	uint32_t *prim_pairs;           /* [num_prims] pair count per primitive (with shade_list) */
+	uint32_t *prim_offsets;         /* [num_prims] first primitive-major position (with shade_list) */
+	uint32_t *prim_scan_blocks;     /* [2 * ceil(num_prims / 1024)] (with shade_list) */
 	uint32_t shade_variant;         /* which compiled k_shade (register budget), < RDP_SHADE_VARIANTS */
 	uint32_t blend_ctas;            /* persistent CTAs of k_blend / k_raster */
 	uint32_t *pair_log;             /* optional: k_scan writes the launch's pair count to pair_log[log_slot] */

@@ -16,7 +16,12 @@
 #include <stdint.h>
 #include <string.h>
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
 #include <cstdlib>
+#include <functional>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "rdp_types.h"
@@ -28,6 +33,92 @@ namespace rdpx {
 static inline size_t align16(size_t v) { return (v + 15) & ~size_t(15); }
 
 constexpr uint32_t kMaxTargets = 8;
+
+// Persistent host worker threads for data-parallel host work (filling a launch's staging
+// buffer): run(n, fn) calls fn(0..n-1) spread over the workers and the calling thread and
+// returns when all calls have finished.  Workers start on first use.
+class HostPool
+{
+public:
+	~HostPool()
+	{
+		{
+			std::lock_guard<std::mutex> lk(mu_);
+			stop_ = true;
+		}
+		cv_.notify_all();
+		for (auto &t : workers_) t.join();
+	}
+
+	void run(uint32_t n, const std::function<void(uint32_t)> &fn)
+	{
+		if (n <= 1 || max_workers() == 0)
+		{
+			for (uint32_t i = 0; i < n; i++) fn(i);
+			return;
+		}
+		start();
+		{
+			std::lock_guard<std::mutex> lk(mu_);
+			fn_ = &fn;
+			n_ = n;
+			next_.store(0);
+			busy_ = uint32_t(workers_.size());
+			gen_++;
+		}
+		cv_.notify_all();
+		drain();
+		std::unique_lock<std::mutex> lk(mu_);
+		done_cv_.wait(lk, [&] { return busy_ == 0; });
+		fn_ = nullptr;
+	}
+
+private:
+	static uint32_t max_workers()
+	{
+		const uint32_t hw = std::max(1u, std::thread::hardware_concurrency());
+		return std::min(hw, 16u) - 1;
+	}
+	void start()
+	{
+		if (!workers_.empty()) return;
+		for (uint32_t t = 0; t < max_workers(); t++) workers_.emplace_back([this] { loop(); });
+	}
+	void drain()
+	{
+		for (;;)
+		{
+			const uint32_t i = next_.fetch_add(1);
+			if (i >= n_) break;
+			(*fn_)(i);
+		}
+	}
+	void loop()
+	{
+		uint64_t seen = 0;
+		for (;;)
+		{
+			{
+				std::unique_lock<std::mutex> lk(mu_);
+				cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+				if (stop_) return;
+				seen = gen_;
+			}
+			drain();
+			std::lock_guard<std::mutex> lk(mu_);
+			if (--busy_ == 0) done_cv_.notify_all();
+		}
+	}
+
+	std::vector<std::thread> workers_;
+	std::mutex mu_;
+	std::condition_variable cv_, done_cv_;
+	const std::function<void(uint32_t)> *fn_ = nullptr;
+	uint32_t n_ = 0, busy_ = 0;
+	std::atomic<uint32_t> next_{ 0 };
+	uint64_t gen_ = 0;
+	bool stop_ = false;
+};
 
 // One recorded pass of an instance, as plain pointers into the recorder's buffers.
 // A pass may draw into several colour images ("targets") whose memory does not
@@ -162,6 +253,8 @@ struct Executor
 	uint32_t shade_ctas_v[RDP_SHADE_VARIANTS] = {}, blend_ctas = 0;
 	bool failed = false;
 	ShadeTuner tuner;
+	HostPool pool;                                      // staging fill of large launches
+	static constexpr size_t kParallelFillBytes = 1u << 20;
 	uint32_t *d_pair_log = nullptr; // [256]
 	// Size thresholds of the shading orders (RDP_SHADE_PERM_MIN_PRIMS, RDP_SHADE_QUEUE_MIN
 	// override them): primitive-major order for launches of at least perm_min_prims primitives,
@@ -196,7 +289,7 @@ struct Executor
 		bool in_flight = false;
 	};
 	std::vector<Staging> staging;
-	size_t staging_next = 0;
+	size_t staging_next = 0, staging_largest = 0;
 
 	// A host staging buffer of at least `bytes` whose previous copy has completed.
 	Staging *take_staging(size_t bytes)
@@ -227,12 +320,15 @@ struct Executor
 		staging_next = size_t(pick - staging.data()) + 1;
 		if (pick->size < bytes)
 		{
+			// A new or grown buffer takes the largest size any buffer has needed, so that
+			// the ring stops reallocating (cudaFreeHost waits for the device) once warm.
+			size_t n = std::max(bytes, std::max(staging_largest, pick->size + pick->size / 2));
 			if (pick->h) cudaFreeHost(pick->h);
 			pick->h = nullptr;
 			pick->size = 0;
-			size_t n = std::max(bytes, pick->size + pick->size / 2);
 			if (check(cudaMallocHost(&pick->h, n))) return nullptr;
 			pick->size = n;
+			staging_largest = std::max(staging_largest, n);
 		}
 		return pick;
 	}
@@ -629,46 +725,35 @@ struct Executor
 		uint32_t *tmem_list = reinterpret_cast<uint32_t *>(h + o_list);
 		uint32_t num_tmem = 0, max_uploads = 0;
 		uint32_t prim_base = 0, word_base = 0, sb_base = 0, ts_base = 0, up_base = 0, tile_base = 0;
-		// Sections: all prims, then all words, state blocks, tile sets, uploads.
-		size_t o_prims = reserve(0), cursor;
-		cursor = o_prims;
+		// Sections: all prims, then all words, state blocks, tile sets, uploads; each view's
+		// share of a section is contiguous.  The views are copied in parallel.
+		std::vector<size_t> at(size_t(n) * 5);
+		size_t cursor = off;
+		size_t o_prims = cursor;
+		for (uint32_t i = 0; i < n; i++) at[i * 5 + 0] = cursor, cursor += sizeof(RdpPrimIn) * v[i].num_prims;
+		cursor = align16(cursor);
+		size_t o_words = cursor;
+		for (uint32_t i = 0; i < n; i++) at[i * 5 + 1] = cursor, cursor += 4 * size_t(v[i].num_words);
+		cursor = align16(cursor);
+		size_t o_sb = cursor;
 		for (uint32_t i = 0; i < n; i++)
-		{
-			memcpy(h + cursor, v[i].prims, sizeof(RdpPrimIn) * v[i].num_prims);
-			cursor += sizeof(RdpPrimIn) * v[i].num_prims;
-		}
-		off = align16(cursor);
-		size_t o_words = off;
-		cursor = o_words;
-		for (uint32_t i = 0; i < n; i++)
-		{
-			memcpy(h + cursor, v[i].words, 4 * size_t(v[i].num_words));
-			cursor += 4 * size_t(v[i].num_words);
-		}
-		off = align16(cursor);
-		size_t o_sb = off;
-		cursor = o_sb;
-		for (uint32_t i = 0; i < n; i++)
-		{
-			memcpy(h + cursor, v[i].state_blocks, 4 * size_t(RDP_STATE_BLOCK_WORDS) * v[i].num_state_blocks);
-			cursor += 4 * size_t(RDP_STATE_BLOCK_WORDS) * v[i].num_state_blocks;
-		}
-		off = align16(cursor);
-		size_t o_ts = off;
-		cursor = o_ts;
-		for (uint32_t i = 0; i < n; i++)
-		{
-			memcpy(h + cursor, v[i].tilesets, sizeof(RdpTile) * 8 * v[i].num_tilesets);
-			cursor += sizeof(RdpTile) * 8 * v[i].num_tilesets;
-		}
-		off = align16(cursor);
-		size_t o_up = off;
-		cursor = o_up;
-		for (uint32_t i = 0; i < n; i++)
-		{
-			memcpy(h + cursor, v[i].uploads, sizeof(RdpUpload) * v[i].num_uploads);
-			cursor += sizeof(RdpUpload) * v[i].num_uploads;
-		}
+			at[i * 5 + 2] = cursor, cursor += 4 * size_t(RDP_STATE_BLOCK_WORDS) * v[i].num_state_blocks;
+		cursor = align16(cursor);
+		size_t o_ts = cursor;
+		for (uint32_t i = 0; i < n; i++) at[i * 5 + 3] = cursor, cursor += sizeof(RdpTile) * 8 * v[i].num_tilesets;
+		cursor = align16(cursor);
+		size_t o_up = cursor;
+		for (uint32_t i = 0; i < n; i++) at[i * 5 + 4] = cursor, cursor += sizeof(RdpUpload) * v[i].num_uploads;
+		auto fill = [&](uint32_t i) {
+			memcpy(h + at[i * 5 + 0], v[i].prims, sizeof(RdpPrimIn) * v[i].num_prims);
+			memcpy(h + at[i * 5 + 1], v[i].words, 4 * size_t(v[i].num_words));
+			memcpy(h + at[i * 5 + 2], v[i].state_blocks, 4 * size_t(RDP_STATE_BLOCK_WORDS) * v[i].num_state_blocks);
+			memcpy(h + at[i * 5 + 3], v[i].tilesets, sizeof(RdpTile) * 8 * v[i].num_tilesets);
+			memcpy(h + at[i * 5 + 4], v[i].uploads, sizeof(RdpUpload) * v[i].num_uploads);
+		};
+		if (cursor - o_prims >= kParallelFillBytes) pool.run(n, fill);
+		else
+			for (uint32_t i = 0; i < n; i++) fill(i);
 		off = align16(cursor) + 16;
 		uint32_t d = 0;
 		for (uint32_t i = 0; i < n; i++)

@@ -341,6 +341,7 @@ struct rdp_cp
 			c.prims = RDP_MAX_PRIMS_PER_PASS;
 			c.tile_items = kMaxTiles;
 			c.pairs = 1u << 20;
+			c.span_rows = rdpx::kInitialSpanRows;
 			c.staging = rdpx::align16(sizeof(RdpPass)) + rdpx::align16(sizeof(RdpPrimIn) * RDP_MAX_PRIMS_PER_PASS) +
 			            rdpx::align16(sizeof(uint32_t) * kMaxWordsPerPass) +
 			            rdpx::align16(sizeof(uint32_t) * RDP_STATE_BLOCK_WORDS * kMaxStateBlocks) +
@@ -1538,6 +1539,7 @@ bool rdp_batch::reserve_for_capture()
 		need.staging = std::max(need.staging, rdpx::Executor::staging_bytes_for(views.data(), uint32_t(views.size())));
 	}
 	need.pairs = std::max(need.pairs, 1u << 20);
+	need.span_rows = std::max(need.span_rows, rdpx::kInitialSpanRows);
 	return exec.ensure(need);
 }
 

@@ -178,9 +178,13 @@ struct PassPacket
 
 struct ExecCaps
 {
-	uint32_t passes = 0, descs = 0, prims = 0, tile_items = 0, pairs = 0;
+	uint32_t passes = 0, descs = 0, prims = 0, tile_items = 0, pairs = 0, span_rows = 0;
 	size_t staging = 0;
 };
+
+// Span rows a launch buffer starts with (RDP_SPAN_ROW_BYTES each); batches grow it at idle to
+// the largest count a launch needed.
+constexpr uint32_t kInitialSpanRows = 1u << 21;
 
 // Launches recorded for a CUDA graph, with their device-resident inputs.
 struct CaptureSink
@@ -270,6 +274,8 @@ struct Executor
 	uint32_t *d_tile_counts = nullptr, *d_pair_offsets = nullptr, *d_ctrl = nullptr;
 	uint32_t *d_tile_order = nullptr, *d_tile_cycles = nullptr, *d_nonempty = nullptr, *d_scan_blocks = nullptr;
 	uint32_t *d_prim_pairs = nullptr, *d_prim_offsets = nullptr, *d_prim_blocks = nullptr;
+	uint32_t *d_prim_rows = nullptr; // first span row of each primitive
+	void *d_spans = nullptr;         // span rows written by k_bin
 	uint4 *d_shade_list = nullptr; // primitive-major shading records
 	uint2 *d_pairs = nullptr;
 	uint32_t *d_sc_color = nullptr;
@@ -530,6 +536,8 @@ struct Executor
 		cudaFree(d_prim_pairs);
 		cudaFree(d_prim_offsets);
 		cudaFree(d_prim_blocks);
+		cudaFree(d_prim_rows);
+		cudaFree(d_spans);
 		cudaFree(d_shade_list);
 		cudaFree(d_pairs);
 		cudaFree(d_sc_color);
@@ -541,7 +549,8 @@ struct Executor
 		d_shade = nullptr;
 		d_masks = d_tmem_keep = d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = d_nonempty = nullptr;
 		d_scan_blocks = nullptr;
-		d_prim_pairs = d_prim_offsets = d_prim_blocks = nullptr;
+		d_prim_pairs = d_prim_offsets = d_prim_blocks = d_prim_rows = nullptr;
+		d_spans = nullptr;
 		d_shade_list = nullptr;
 		d_pairs = nullptr;
 		d_sc_color = nullptr;
@@ -575,8 +584,8 @@ struct Executor
 	{
 		bool grow_prims = need.prims > caps.prims, grow_tiles = need.tile_items > caps.tile_items;
 		bool grow_passes = need.passes > caps.passes, grow_pairs = need.pairs > caps.pairs;
-		bool grow_staging = need.staging > caps.staging;
-		if (!(grow_prims || grow_tiles || grow_passes || grow_pairs || grow_staging)) return true;
+		bool grow_staging = need.staging > caps.staging, grow_spans = need.span_rows > caps.span_rows;
+		if (!(grow_prims || grow_tiles || grow_passes || grow_pairs || grow_staging || grow_spans)) return true;
 		if (check(cudaStreamSynchronize(stream))) return false;
 		for (auto &st : staging) st.in_flight = false;
 		generation++;
@@ -589,13 +598,14 @@ struct Executor
 			cudaFree(d_prim_pairs);
 			cudaFree(d_prim_offsets);
 			cudaFree(d_prim_blocks);
+			cudaFree(d_prim_rows);
 			d_geom = nullptr;
 			d_attr = nullptr;
 			d_shade = nullptr;
-			d_prim_pairs = d_prim_offsets = d_prim_blocks = nullptr;
+			d_prim_pairs = d_prim_offsets = d_prim_blocks = d_prim_rows = nullptr;
 			if (check(cudaMalloc(&d_geom, sizeof(RdpPrimGeom) * n)) || check(cudaMalloc(&d_attr, sizeof(RdpPrimAttr) * n)) ||
 			    check(cudaMalloc(&d_shade, sizeof(RdpPrimShade) * n)) || check(cudaMalloc(&d_prim_pairs, size_t(n) * 4)) ||
-			    check(cudaMalloc(&d_prim_offsets, size_t(n) * 4)) ||
+			    check(cudaMalloc(&d_prim_offsets, size_t(n) * 4)) || check(cudaMalloc(&d_prim_rows, size_t(n) * 4)) ||
 			    check(cudaMalloc(&d_prim_blocks, (size_t(n) / 1024 + 2) * 8)))
 				return false;
 			caps.prims = n;
@@ -652,6 +662,14 @@ struct Executor
 				return false;
 			caps.pairs = n;
 		}
+		if (grow_spans)
+		{
+			uint32_t n = std::max(need.span_rows, caps.span_rows + caps.span_rows / 2);
+			cudaFree(d_spans);
+			d_spans = nullptr;
+			if (check(cudaMalloc(&d_spans, size_t(n) * RDP_SPAN_ROW_BYTES))) return false;
+			caps.span_rows = n;
+		}
 		if (grow_staging)
 		{
 			size_t n = std::max(need.staging, caps.staging + caps.staging / 2);
@@ -663,16 +681,24 @@ struct Executor
 		return !check(cudaStreamSynchronize(stream));
 	}
 
-	// With the stream idle: grows the pair scratch to the largest pair count a launch has
-	// needed, so that later launches take the pair path instead of the fused fallback.
+	// With the stream idle: grows the pair scratch and the span rows to the largest counts a
+	// launch has needed, so that later launches take the pair path instead of the fused fallback.
 	bool adapt_pairs()
 	{
-		uint32_t seen[3] = { 0, 0, 0 };
+		uint32_t seen[6] = { 0, 0, 0, 0, 0, 0 };
 		if (check(cudaMemcpy(seen, d_ctrl, sizeof(seen), cudaMemcpyDeviceToHost))) return false;
-		if (seen[2] <= caps.pairs) return true;
+		if (seen[2] <= caps.pairs && seen[5] <= caps.span_rows) return true;
 		ExecCaps need = caps;
-		need.pairs = 1u;
-		while (need.pairs < seen[2] && need.pairs < (1u << 30)) need.pairs <<= 1;
+		if (seen[2] > caps.pairs)
+		{
+			need.pairs = 1u;
+			while (need.pairs < seen[2] && need.pairs < (1u << 30)) need.pairs <<= 1;
+		}
+		if (seen[5] > caps.span_rows)
+		{
+			need.span_rows = 1u;
+			while (need.span_rows < seen[5] && need.span_rows < (1u << 30)) need.span_rows <<= 1;
+		}
 		return ensure(need);
 	}
 
@@ -704,6 +730,7 @@ struct Executor
 		need.prims = std::max(need.prims, std::max(prims, 1u));
 		need.tile_items = std::max(need.tile_items, std::max(tiles, 1u));
 		need.pairs = std::max(need.pairs, 1u << 20);
+		need.span_rows = std::max(need.span_rows, kInitialSpanRows);
 		need.staging = std::max(need.staging, staging_bytes_for(v, n));
 		if (!ensure(need)) return false;
 
@@ -849,6 +876,10 @@ struct Executor
 		L.blend_ctas = blend_ctas;
 		L.pair_log = sample ? d_pair_log : nullptr;
 		L.log_slot = sample ? uint32_t(tuner.samples_taken++ % 256) : 0u;
+		L.spans = d_spans;
+		L.span_capacity = caps.span_rows;
+		L.prim_rows = d_prim_rows;
+		L.num_sms = num_queues;
 		L.sc_color = d_sc_color;
 		L.sc_zdith = d_sc_zdith;
 		L.sc_misc = d_sc_misc;

@@ -6,17 +6,20 @@
  *                  attributes, derived combiner constants and normalised static
  *                  state (rdp_device.cpp:268-864, rdp_renderer.cpp:717-1562).
  *   k_bin        : one warp per primitive.  Conservative 8x8-tile binning
- *                  (shaders/binning.h) into per-tile primitive bitmasks; the
- *                  bitmask order is primitive order.
- *   k_tmem       : one CTA per pass with TMEM uploads.  Gathers each 16-bit TMEM
- *                  word per upload (shaders/tmem_update.comp) and writes one TMEM
- *                  snapshot per upload.
- *   k_raster     : one warp per 8x8 tile.  Loads the tile's colour/depth from
- *                  RDRAM once, walks the binned primitives in order -- span set-up
- *                  for the tile's rows computed cooperatively into shared memory
- *                  (shaders/span_setup.comp), per-pixel shading (shaders/shading.h)
- *                  and depth/blend (shaders/memory_interfacing.h) in registers --
- *                  and writes back only what was written.
+ *                  (shaders/binning.h) into per-tile primitive bitmasks and counts.
+ *   k_span       : one warp per primitive.  The spans of its scanlines
+ *                  (shaders/span_setup.comp), once for all its tiles.
+ *   k_tmem_*     : TMEM uploads (shaders/tmem_update.comp), one snapshot per upload.
+ *   k_scan_*     : pair offsets per tile (and per primitive), control words.
+ *   k_expand     : the (primitive, tile) pair list, in primitive order per tile.
+ *   k_shade      : per-pixel shading of every pair (shaders/shading.h) into scratch,
+ *                  one warp per half pair, pairs in parallel.
+ *   k_blend      : per tile, the pairs' shaded pixels in primitive order through
+ *                  depth test, blender, dither and coverage against the tile's
+ *                  colour/depth held in registers (shaders/memory_interfacing.h,
+ *                  depth_blend.comp); writes back only what was written.
+ *   k_raster     : fused shading + blending per tile, taken only when a launch's
+ *                  pairs or span rows overflow the scratch.
  *
  * All arithmetic is the RDP's integer fixed point; wrap-around is explicit
  * (unsigned multiplies/shifts) so that it matches 32-bit GLSL semantics.
@@ -538,6 +541,98 @@ __global__ void k_prim_setup(const RdpPrimIn *__restrict__ in, uint32_t num_prim
 	if (featbits) featbits[i] = rdp_feature_bits(sh.static_flags, sh.db_flags);
 }
 
+// ============================================================================ k_raster: spans
+// One scanline of a primitive (the reference's SpanSetup, span_setup.comp): the attribute half
+// (RGBA / STZW at the span's base x) and the coverage half (4 sub-scanline x ranges in 16.3,
+// the pixel range they touch, validity).  64 bytes, so a row is two full sectors.
+struct __align__(16) SpanRow
+{
+	int rgba[4];
+	int stzw[4];
+	uint16_t xl[4], xr[4];
+	int base_x;
+	int start_x, end_x;
+	int valid;
+};
+static_assert(sizeof(SpanRow) == RDP_SPAN_ROW_BYTES, "span row layout");
+
+// Attribute half of span_setup.comp:99-150.
+__device__ void span_attr(const RdpPrimGeom &g, const RdpPrimAttr &a, int y, SpanRow &out)
+{
+	bool do_offset = (g.flags & TRI_DO_OFFSET) != 0;
+	bool skip_xfrac = (g.flags & TRI_SKIP_XFRAC) != 0;
+	int dy = y - (g.yh >> 2);
+	int xh = g.xh + mulw(dy, shlw(g.dxhdy, 2));
+	int drd[4] = { 0, 0, 0, 0 }, dsd[4] = { 0, 0, 0, 0 };
+	if (do_offset)
+	{
+		xh += mulw(3, g.dxhdy);
+#pragma unroll
+		for (int c = 0; c < 4; c++)
+		{
+			int deh = a.drgba_de[c] & ~0x1ff, dyh = a.drgba_dy[c] & ~0x1ff;
+			drd[c] = deh - (deh >> 2) - dyh + (dyh >> 2);
+			deh = a.dstzw_de[c] & ~0x1ff;
+			dyh = a.dstzw_dy[c] & ~0x1ff;
+			dsd[c] = deh - (deh >> 2) - dyh + (dyh >> 2);
+		}
+	}
+	int xfrac = skip_xfrac ? 0 : ((xh >> 7) & 0xff);
+#pragma unroll
+	for (int c = 0; c < 4; c++)
+	{
+		int v = a.rgba[c] + mulw(dy, a.drgba_de[c]);
+		out.rgba[c] = ((v & ~0x1ff) + drd[c] - mulw(xfrac, (a.drgba_dx[c] >> 8) & ~1)) & ~0x3ff;
+		v = a.stzw[c] + mulw(dy, a.dstzw_de[c]);
+		out.stzw[c] = ((v & ~0x1ff) + dsd[c] - mulw(xfrac, (a.dstzw_dx[c] >> 8) & ~1)) & ~0x3ff;
+	}
+	out.base_x = xh >> 15;
+}
+
+__device__ __forceinline__ int quantize_x(int x) { return (x >> 12) | ((x & 0xfff) != 0 ? 1 : 0); }
+
+// Coverage half of span_setup.comp:152-225.
+__device__ void span_x(const RdpPrimGeom &g, int y, SpanRow &out)
+{
+	bool flip = (g.flags & TRI_FLIP) != 0;
+	int yh_base = g.yh & ~3;
+	int ylo = max(g.yh, g.scissor[1]);
+	int yhi = min(g.yl, g.scissor[3]);
+	int lo_sc = g.scissor[0] << 1, hi_sc = g.scissor[2] << 1;
+	bool all_over = true, all_under = true, all_invalid = true;
+	int mn = 0x7fffffff, mx = -0x7fffffff - 1;
+#pragma unroll
+	for (int k = 0; k < 4; k++)
+	{
+		int ys = y * 4 + k;
+		bool clip_y = ys < ylo || ys >= yhi;
+		int xh = g.xh + mulw(ys - yh_base, g.dxhdy);
+		int xm = g.xm + mulw(ys - yh_base, g.dxmdy);
+		int xl = g.xl + mulw(ys - g.ym, g.dxldy);
+		if (ys < g.ym) xl = xm;
+		xl = bfe_s(xl, 27);
+		xh = bfe_s(xh, 27);
+		int hs = quantize_x(xh), ls = quantize_x(xl);
+		int l = flip ? hs : ls, r = flip ? ls : hs;
+		bool invalid = ((l >> 1) > (r >> 1)) || clip_y;
+		all_over = all_over && (min(l, r) >= hi_sc);
+		all_under = all_under && (max(l, r) < lo_sc);
+		l = min(max(l, lo_sc), hi_sc);
+		r = min(max(r, lo_sc), hi_sc);
+		if (invalid) { l = 0xffff; r = 0; }
+		all_invalid = all_invalid && invalid;
+		out.xl[k] = uint16_t(l);
+		out.xr[k] = uint16_t(r);
+		mn = min(mn, l);
+		mx = max(mx, r);
+	}
+	out.start_x = mn >> 3;
+	out.end_x = mx >> 3;
+	bool valid = !all_invalid && !all_over && !all_under;
+	if ((g.flags & TRI_INTERLACE_FIELD) && ((y & 1) != int((g.flags & TRI_INTERLACE_KEEP_ODD) != 0))) valid = false;
+	out.valid = valid ? 1 : 0;
+}
+
 // ============================================================================ k_bin
 // binning.h:58-144 at scaling 1.
 __device__ bool bin_primitive(const RdpPrimGeom &g, int lox, int loy, int hix, int hiy)
@@ -620,6 +715,92 @@ __global__ void k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom, 
 		binned += __popc(__ballot_sync(0xffffffffu, hit));
 	}
 	if (prim_pairs && lane == 0) prim_pairs[warp] = binned;
+}
+
+// ============================================================================ k_span
+// Spans of the scanlines of every primitive that can have tiles (span_setup.comp), computed once
+// per primitive row for all the primitive's tiles: rows span_ylo .. the last shaded row + 1 (the
+// pipelined texel1 peek reads the next row).  A CTA takes `chunk` (<= SPAN_THREADS) consecutive
+// primitives: one thread per primitive counts its rows, a CTA scan gives each primitive its first
+// row, one atomic on the launch's 64-bit row counter (k_scan resets it) places the CTA's rows,
+// and then one thread per row computes it (the row's primitive found by binary search of the
+// scan).  The host sizes `chunk` to the launch, so that a few tall primitives (a clear) still
+// spread over many CTAs while large launches take few atomics.  A CTA whose rows would not fit
+// `capacity` writes none; the launch then takes k_raster (write_ctrl flags it) and the host
+// grows the buffer to the count seen.
+constexpr int SPAN_THREADS = 256;
+
+__global__ void __launch_bounds__(SPAN_THREADS) k_span(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom,
+                                                      const RdpPrimAttr *__restrict__ attr,
+                                                      const RdpPrimShade *__restrict__ shade,
+                                                      const RdpPass *__restrict__ passes, SpanRow *__restrict__ spans,
+                                                      uint32_t capacity, uint32_t *__restrict__ prim_rows,
+                                                      unsigned long long *__restrict__ row_counter, uint32_t chunk)
+{
+	constexpr int NW = SPAN_THREADS / 32;
+	__shared__ uint32_t s_first[SPAN_THREADS + 1]; // first row of each primitive in the CTA, then the total
+	__shared__ uint32_t s_warp[NW];
+	__shared__ unsigned long long s_base;
+	const uint32_t t = threadIdx.x, lane = t & 31, wid = t >> 5;
+	const uint32_t p0 = blockIdx.x * chunk, prim = p0 + t;
+	uint32_t nrows = 0;
+	if (t < chunk && prim < num_prims)
+	{
+		const RdpPrimGeom &g = geom[prim];
+		const int r_last = min(g.span_yhi, int(passes[shade[prim].pass].fb_height) - 1);
+		const bool has_tiles = g.bbox[2] >= g.bbox[0] && g.bbox[3] >= g.bbox[1];
+		if (has_tiles && r_last >= g.span_ylo) nrows = uint32_t(r_last - g.span_ylo + 2);
+	}
+	uint32_t x = nrows;
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1)
+	{
+		const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+		if (lane >= uint32_t(o)) x += y;
+	}
+	if (lane == 31) s_warp[wid] = x;
+	__syncthreads();
+	if (wid == 0)
+	{
+		uint32_t w = lane < uint32_t(NW) ? s_warp[lane] : 0u;
+#pragma unroll
+		for (int o = 1; o < NW; o <<= 1)
+		{
+			const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+			if (lane >= uint32_t(o)) w += y;
+		}
+		if (lane < uint32_t(NW)) s_warp[lane] = w;
+	}
+	__syncthreads();
+	const uint32_t first = (wid ? s_warp[wid - 1] : 0u) + x - nrows, total = s_warp[NW - 1];
+	s_first[t] = first;
+	if (t == 0)
+	{
+		s_first[SPAN_THREADS] = total;
+		s_base = total ? atomicAdd(row_counter, (unsigned long long)total) : 0ull;
+	}
+	__syncthreads();
+	const unsigned long long base = s_base;
+	if (t < chunk && prim < num_prims) prim_rows[prim] = uint32_t(base + first);
+	if (base + total > capacity) return;
+	for (uint32_t i = t; i < total; i += SPAN_THREADS)
+	{
+		// The largest k with s_first[k] <= i: the primitive whose rows hold row i.
+		uint32_t lo = 0, hi = chunk;
+		while (hi - lo > 1)
+		{
+			const uint32_t mid = (lo + hi) >> 1;
+			if (s_first[mid] <= i) lo = mid;
+			else hi = mid;
+		}
+		const uint32_t pk = p0 + lo;
+		const RdpPrimGeom &g = geom[pk];
+		const int y = g.span_ylo + int(i - s_first[lo]);
+		SpanRow row;
+		span_x(g, y, row);
+		span_attr(g, attr[pk], y, row);
+		spans[base + i] = row;
+	}
 }
 
 // ============================================================================ k_tmem
@@ -987,100 +1168,6 @@ __global__ void __launch_bounds__(TMEM_CARRY_WARPS * 32) k_tmem_carry(const RdpP
 		if (keep[u * 64] & bit) snap[at] = value;
 		else value = snap[at];
 	}
-}
-
-// ============================================================================ k_raster: spans
-struct SpanA
-{
-	int rgba[4];
-	int stzw[4];
-	int base_x;
-	int pad[3];
-};
-
-struct SpanX
-{
-	uint16_t xl[4], xr[4];
-	int start_x, end_x;
-	int valid;
-	int pad;
-};
-
-// Attribute half of span_setup.comp:99-150.
-__device__ void span_attr(const RdpPrimGeom &g, const RdpPrimAttr &a, int y, SpanA &out)
-{
-	bool do_offset = (g.flags & TRI_DO_OFFSET) != 0;
-	bool skip_xfrac = (g.flags & TRI_SKIP_XFRAC) != 0;
-	int dy = y - (g.yh >> 2);
-	int xh = g.xh + mulw(dy, shlw(g.dxhdy, 2));
-	int drd[4] = { 0, 0, 0, 0 }, dsd[4] = { 0, 0, 0, 0 };
-	if (do_offset)
-	{
-		xh += mulw(3, g.dxhdy);
-#pragma unroll
-		for (int c = 0; c < 4; c++)
-		{
-			int deh = a.drgba_de[c] & ~0x1ff, dyh = a.drgba_dy[c] & ~0x1ff;
-			drd[c] = deh - (deh >> 2) - dyh + (dyh >> 2);
-			deh = a.dstzw_de[c] & ~0x1ff;
-			dyh = a.dstzw_dy[c] & ~0x1ff;
-			dsd[c] = deh - (deh >> 2) - dyh + (dyh >> 2);
-		}
-	}
-	int xfrac = skip_xfrac ? 0 : ((xh >> 7) & 0xff);
-#pragma unroll
-	for (int c = 0; c < 4; c++)
-	{
-		int v = a.rgba[c] + mulw(dy, a.drgba_de[c]);
-		out.rgba[c] = ((v & ~0x1ff) + drd[c] - mulw(xfrac, (a.drgba_dx[c] >> 8) & ~1)) & ~0x3ff;
-		v = a.stzw[c] + mulw(dy, a.dstzw_de[c]);
-		out.stzw[c] = ((v & ~0x1ff) + dsd[c] - mulw(xfrac, (a.dstzw_dx[c] >> 8) & ~1)) & ~0x3ff;
-	}
-	out.base_x = xh >> 15;
-}
-
-__device__ __forceinline__ int quantize_x(int x) { return (x >> 12) | ((x & 0xfff) != 0 ? 1 : 0); }
-
-// Coverage half of span_setup.comp:152-225.
-__device__ void span_x(const RdpPrimGeom &g, int y, SpanX &out)
-{
-	bool flip = (g.flags & TRI_FLIP) != 0;
-	int yh_base = g.yh & ~3;
-	int ylo = max(g.yh, g.scissor[1]);
-	int yhi = min(g.yl, g.scissor[3]);
-	int lo_sc = g.scissor[0] << 1, hi_sc = g.scissor[2] << 1;
-	bool all_over = true, all_under = true, all_invalid = true;
-	int mn = 0x7fffffff, mx = -0x7fffffff - 1;
-#pragma unroll
-	for (int k = 0; k < 4; k++)
-	{
-		int ys = y * 4 + k;
-		bool clip_y = ys < ylo || ys >= yhi;
-		int xh = g.xh + mulw(ys - yh_base, g.dxhdy);
-		int xm = g.xm + mulw(ys - yh_base, g.dxmdy);
-		int xl = g.xl + mulw(ys - g.ym, g.dxldy);
-		if (ys < g.ym) xl = xm;
-		xl = bfe_s(xl, 27);
-		xh = bfe_s(xh, 27);
-		int hs = quantize_x(xh), ls = quantize_x(xl);
-		int l = flip ? hs : ls, r = flip ? ls : hs;
-		bool invalid = ((l >> 1) > (r >> 1)) || clip_y;
-		all_over = all_over && (min(l, r) >= hi_sc);
-		all_under = all_under && (max(l, r) < lo_sc);
-		l = min(max(l, lo_sc), hi_sc);
-		r = min(max(r, lo_sc), hi_sc);
-		if (invalid) { l = 0xffff; r = 0; }
-		all_invalid = all_invalid && invalid;
-		out.xl[k] = uint16_t(l);
-		out.xr[k] = uint16_t(r);
-		mn = min(mn, l);
-		mx = max(mx, r);
-	}
-	out.start_x = mn >> 3;
-	out.end_x = mx >> 3;
-	bool valid = !all_invalid && !all_over && !all_under;
-	if ((g.flags & TRI_INTERLACE_FIELD) && ((y & 1) != int((g.flags & TRI_INTERLACE_KEEP_ODD) != 0))) valid = false;
-	out.valid = valid ? 1 : 0;
 }
 
 // ============================================================================ k_raster: per-pixel maths
@@ -1960,10 +2047,10 @@ struct Shaded
 
 // shading.h:38-359: everything that does not depend on the framebuffer.
 __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const RdpPrimAttr &a, const RdpPrimShade &sh,
-                            const RdpTile *tiles, const uint16_t *tm, const SpanA &sa, const SpanX &sx,
-                            const SpanA &sa_next, const SpanX &sx_next, int x, int y, Shaded &out)
+                            const RdpTile *tiles, const uint16_t *tm, const SpanRow &sp, const SpanRow &sp_next,
+                            int x, int y, Shaded &out)
 {
-	if (!sx.valid) return false;
+	if (!sp.valid) return false;
 	const uint32_t f = sh.static_flags;
 	const bool flip = (g.flags & TRI_FLIP) != 0;
 	const bool perspective = (f & RS_PERSPECTIVE) != 0;
@@ -1972,13 +2059,13 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 
 	if (f & RS_COPY)
 	{
-		if (!(x >= sx.start_x && x <= sx.end_x)) return false;
-		int dxp = flip ? (x - sx.start_x) : (sx.end_x - x);
+		if (!(x >= sp.start_x && x <= sp.end_x)) return false;
+		int dxp = flip ? (x - sp.start_x) : (sp.end_x - x);
 		int s_offset = dxp - (dxp & pc.dx_mask);
 		int lerp_dx = (dxp >> pc.dx_shift) * (flip ? 1 : -1);
-		int s = (sa.stzw[0] + mulw(a.dstzw_dx[0] & ~0x1f, lerp_dx)) >> 16;
-		int t = (sa.stzw[1] + mulw(a.dstzw_dx[1] & ~0x1f, lerp_dx)) >> 16;
-		int w = (sa.stzw[3] + mulw(a.dstzw_dx[3] & ~0x1f, lerp_dx)) >> 16;
+		int s = (sp.stzw[0] + mulw(a.dstzw_dx[0] & ~0x1f, lerp_dx)) >> 16;
+		int t = (sp.stzw[1] + mulw(a.dstzw_dx[1] & ~0x1f, lerp_dx)) >> 16;
+		int w = (sp.stzw[3] + mulw(a.dstzw_dx[3] & ~0x1f, lerp_dx)) >> 16;
 		int os, ot;
 		bool ov = false;
 		st_div(s, t, w, perspective, os, ot, ov);
@@ -2000,7 +2087,7 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	if (f & RS_FILL)
 	{
 		out.coverage = 0x40;
-		return x >= sx.start_x && x <= sx.end_x;
+		return x >= sp.start_x && x <= sp.end_x;
 	}
 
 	// ---- coverage (coverage.h:31-47)
@@ -2014,8 +2101,8 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 			int off = (k == 0) ? 0 : (k == 1 ? 4 : (k == 2 ? 2 : 6));
 			int xsh = xs + off;
 			int l0 = k >> 1, l1 = 2 + (k >> 1);
-			if (xsh < sx.xl[l0] || xsh >= sx.xr[l0]) clip |= 1 << k;
-			if (xsh < sx.xl[l1] || xsh >= sx.xr[l1]) clip |= 16 << k;
+			if (xsh < sp.xl[l0] || xsh >= sp.xr[l0]) clip |= 1 << k;
+			if (xsh < sp.xl[l1] || xsh >= sp.xr[l1]) clip |= 16 << k;
 		}
 		coverage = ~clip & 0xff;
 	}
@@ -2024,7 +2111,7 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	const bool aa = (f & RS_AA) != 0;
 	if (!aa && (coverage & 1) == 0) return false;
 
-	int dx = x - sa.base_x;
+	int dx = x - sp.base_x;
 	int idir = flip ? 1 : -1;
 	int first = find_lsb(unsigned(coverage));
 	int yoff = first >> 1;
@@ -2035,7 +2122,7 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 #pragma unroll
 	for (int c = 0; c < 4; c++)
 	{
-		int v = sa.rgba[c] + mulw(a.drgba_dx[c] & ~0x1f, dx);
+		int v = sp.rgba[c] + mulw(a.drgba_dx[c] & ~0x1f, dx);
 		int sn = shlw(v >> 14, 2);
 		sn += xoff * (a.drgba_dx[c] >> 14) + yoff * (a.drgba_dy[c] >> 14);
 		sn >>= 4;
@@ -2049,7 +2136,7 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	{
 		int sw[3], idx3[3] = { 0, 1, 3 };
 #pragma unroll
-		for (int k = 0; k < 3; k++) sw[k] = sa.stzw[idx3[k]] + mulw(a.dstzw_dx[idx3[k]] & ~0x1f, dx);
+		for (int k = 0; k < 3; k++) sw[k] = sp.stzw[idx3[k]] + mulw(a.dstzw_dx[idx3[k]] & ~0x1f, dx);
 		if (f & (RS_USES_TEXEL0 | RS_USES_TEXEL1 | RS_USES_PIPELINED_TEXEL1 | RS_USES_LOD))
 		{
 			st_div(sw[0] >> 16, sw[1] >> 16, sw[2] >> 16, perspective, s0, t0v, povf);
@@ -2066,7 +2153,7 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 				st_div(wy[0] >> 16, wy[1] >> 16, wy[2] >> 16, perspective, sdy, tdy, povf);
 			}
 		}
-		z = sa.stzw[2] + mulw(a.dstzw_dx[2], dx);
+		z = sp.stzw[2] + mulw(a.dstzw_dx[2], dx);
 		int sz = shlw(z >> 10, 2);
 		sz += xoff * (a.dstzw_dx[2] >> 10) + yoff * (a.dstzw_dy[2] >> 10);
 		sz >>= 5;
@@ -2142,19 +2229,19 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	bool uses_t1 = (f & RS_USES_TEXEL1) != 0;
 	if (f & RS_USES_PIPELINED_TEXEL1)
 	{
-		int lodlength = int16_t(flip ? (sx.end_x - sa.base_x) : (sa.base_x - sx.start_x));
-		bool end_span = x == (flip ? sx.end_x : sx.start_x);
-		if (end_span && lodlength >= 8 && sx_next.valid)
+		int lodlength = int16_t(flip ? (sp.end_x - sp.base_x) : (sp.base_x - sp.start_x));
+		bool end_span = x == (flip ? sp.end_x : sp.start_x);
+		if (end_span && lodlength >= 8 && sp_next.valid)
 		{
 			bool dummy = false;
-			st_div(sa_next.stzw[0] >> 16, sa_next.stzw[1] >> 16, sa_next.stzw[3] >> 16, perspective, s0, t0v, dummy);
+			st_div(sp_next.stzw[0] >> 16, sp_next.stzw[1] >> 16, sp_next.stzw[3] >> 16, perspective, s0, t0v, dummy);
 		}
 		else
 		{
 			int ndx = dx + idir;
-			int ss = (sa.stzw[0] + mulw(a.dstzw_dx[0] & ~0x1f, ndx)) >> 16;
-			int tt = (sa.stzw[1] + mulw(a.dstzw_dx[1] & ~0x1f, ndx)) >> 16;
-			int ww = (sa.stzw[3] + mulw(a.dstzw_dx[3] & ~0x1f, ndx)) >> 16;
+			int ss = (sp.stzw[0] + mulw(a.dstzw_dx[0] & ~0x1f, ndx)) >> 16;
+			int tt = (sp.stzw[1] + mulw(a.dstzw_dx[1] & ~0x1f, ndx)) >> 16;
+			int ww = (sp.stzw[3] + mulw(a.dstzw_dx[3] & ~0x1f, ndx)) >> 16;
 			bool dummy = false;
 			st_div(ss, tt, ww, perspective, s0, t0v, dummy);
 		}
@@ -2451,11 +2538,11 @@ __device__ bool blend_pixel(const RdpPass &ps, const PassConst &pc, const RdpPri
 
 __device__ __forceinline__ bool shade_and_blend(const RdpPass &ps, const PassConst &pc, const RdpPrimGeom &g,
                                                 const RdpPrimAttr &a, const RdpPrimShade &sh, const RdpTile *tiles,
-                                                const uint16_t *tm, const SpanA &sa, const SpanX &sx,
-                                                const SpanA &sa_next, const SpanX &sx_next, int x, int y, Pix &px)
+                                                const uint16_t *tm, const SpanRow &sp, const SpanRow &sp_next, int x,
+                                                int y, Pix &px)
 {
 	Shaded out;
-	if (!shade_pixel(pc, g, a, sh, tiles, tm, sa, sx, sa_next, sx_next, x, y, out)) return false;
+	if (!shade_pixel(pc, g, a, sh, tiles, tm, sp, sp_next, x, y, out)) return false;
 	return blend_pixel(ps, pc, sh, out, px);
 }
 
@@ -2464,8 +2551,9 @@ __device__ __forceinline__ bool shade_and_blend(const RdpPass &ps, const PassCon
 // and the launch's control words) and, for the primitive-major shading order, of the
 // per-primitive pair counts (into each primitive's first position).  Counts are cleared for
 // the next launch (the cleared per-primitive counts are k_expand's cursors).  Control words:
-// [0] pairs, [1] 1 when the pairs exceed the scratch capacity, [2] largest pair count seen,
-// [3] non-empty tiles, [4] k_blend work counter (reset).
+// [0] pairs, [1] 1 when the pairs or the span rows exceed the scratch capacity, [2] largest
+// pair count seen, [3] non-empty tiles, [4] k_blend work counter (reset), [5] largest span-row
+// count seen, [6..7] k_bin's 64-bit span-row counter (reset).
 
 // One CTA of 1024 threads scans counts[0, num_items) in steps of 1024; `nonempty` optional.
 // Leaves the total in *carry and the non-empty count in *carry_nz.
@@ -2531,17 +2619,23 @@ __device__ void cta_scan(uint32_t num_items, uint32_t *__restrict__ counts, uint
 	}
 }
 
-// Writes the launch's control words from the pair total (one thread).
+// Writes the launch's control words from the pair total (one thread).  `capacity`: pairs (x)
+// and span rows (y) the scratch holds; k_bin has counted the span rows in ctrl[6..7].
 __device__ __forceinline__ void write_ctrl(uint32_t pairs, uint32_t nonempty_tiles, uint32_t *__restrict__ ctrl,
-                                           uint32_t capacity, uint32_t *__restrict__ pair_log, uint32_t log_slot)
+                                           uint2 capacity, uint32_t *__restrict__ pair_log, uint32_t log_slot)
 {
+	unsigned long long *row_counter = reinterpret_cast<unsigned long long *>(ctrl + 6);
+	const unsigned long long rows = *row_counter;
+	const bool over = pairs > capacity.x || rows > capacity.y;
 	ctrl[0] = pairs;
-	ctrl[1] = pairs > capacity ? 1u : 0u;
+	ctrl[1] = over ? 1u : 0u;
 	ctrl[2] = max(ctrl[2], pairs); // largest pair count seen: the host grows the scratch to it
 	ctrl[3] = nonempty_tiles;
 	ctrl[4] = 0u;
+	ctrl[5] = max(ctrl[5], uint32_t(min(rows, 0xffffffffull))); // largest span-row count seen
+	*row_counter = 0ull;
 	// Per-launch pair count for the autotuner; an overflowing launch is not a sample.
-	if (pair_log) pair_log[log_slot] = pairs > capacity ? 0xffffffffu : pairs;
+	if (pair_log) pair_log[log_slot] = over ? 0xffffffffu : pairs;
 }
 
 // Zeroes k_shade's work queues: the per-SM counters and their used-up bitmask.
@@ -2553,7 +2647,7 @@ __device__ __forceinline__ void clear_queues(uint32_t *__restrict__ queues, uint
 // Single CTA: the tile scan, then (num_prims > 0) the primitive scan.
 __global__ void __launch_bounds__(1024) k_scan(uint32_t num_items, uint32_t *__restrict__ counts,
                                                uint32_t *__restrict__ offsets, uint32_t *__restrict__ nonempty,
-                                               uint32_t *__restrict__ ctrl, uint32_t capacity,
+                                               uint32_t *__restrict__ ctrl, uint2 capacity,
                                                uint32_t *__restrict__ pair_log, uint32_t log_slot,
                                                uint32_t *__restrict__ queues, uint32_t num_queues, uint32_t num_prims,
                                                uint32_t *__restrict__ prim_counts, uint32_t *__restrict__ prim_offsets)
@@ -2676,7 +2770,7 @@ __device__ void scan_block_sums(uint32_t num_blocks, uint32_t *__restrict__ bloc
 
 __global__ void __launch_bounds__(1024) k_scan_top(uint32_t num_blocks, uint32_t *__restrict__ block_sums,
                                                    uint32_t num_items, uint32_t *__restrict__ offsets,
-                                                   uint32_t *__restrict__ ctrl, uint32_t capacity,
+                                                   uint32_t *__restrict__ ctrl, uint2 capacity,
                                                    uint32_t *__restrict__ pair_log, uint32_t log_slot,
                                                    uint32_t *__restrict__ queues, uint32_t num_queues,
                                                    uint32_t num_prim_blocks, uint32_t *__restrict__ prim_sums)
@@ -2828,25 +2922,27 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 }
 
 // ============================================================================ k_shade
-// Shading of every (tile, primitive) pair in parallel (the reference's rasterizer.comp):
-// one 64-thread CTA per pair at a time, one pixel per thread.  Results go to scratch as
-// structure-of-arrays per pair: combined colour, z | dither, coverage | shade alpha << 8.
+// Shading of every (tile, primitive) pair in parallel (the reference's rasterizer.comp): one
+// warp per half pair at a time, one pixel per lane; two independent warps per CTA.  Results go
+// to scratch as structure-of-arrays per pair: combined colour, z | dither, coverage | shade
+// alpha << 8.
 constexpr int SHADE_THREADS = 64;
 
-// Work distribution.  Without queues, CTA b shades positions b, b + grid, b + 2 grid, ...
-// With queues (one counter per SM, then a bitmask of used-up queues; zeroed by k_scan),
-// positions are dealt in chunks of SHADE_CHUNK: queue q owns chunks q, q + nq, q + 2 nq, ...,
-// and a CTA takes positions from the queue of the SM it runs on (one atomic per position,
-// issued a position ahead), so the CTAs of one SM shade neighbouring positions at the same
-// time.  A CTA that finds a queue used up marks it in the bitmask and moves to the next queue
-// not marked; it exits only when every queue is marked, so every position is shaded whatever
-// SMs the CTAs land on.  Launches with fewer than `queue_min` positions per CTA use the fixed
-// stride (the queues' first atomic and final sweep cost more than they gain there).  With
-// `list` (k_expand), position j is the record list[j] = {primitive, tile item, pair index,
-// pass}: primitive-major order, so neighbouring positions mostly share a primitive (same
-// shading path, state and texels); without it, position j is pair j in tile order.  Thread 0
-// copies the next position's record into shared memory with cp.async while the CTA shades the
-// current one, so no global load chain sits between two pairs.
+// Work distribution over positions (half pairs).  Without queues, warp w of the grid shades
+// positions w, w + warps, w + 2 warps, ...  With queues (one counter per SM, then a bitmask of
+// used-up queues; zeroed by k_scan), positions are dealt in chunks of SHADE_CHUNK: queue q owns
+// chunks q, q + nq, q + 2 nq, ..., and a warp takes positions from the queue of the SM it runs
+// on (one atomic per position, issued a position ahead), so the warps of one SM shade
+// neighbouring positions at the same time.  A warp that finds a queue used up marks it in the
+// bitmask and moves to the next queue not marked; it exits only when every queue is marked, so
+// every position is shaded whatever SMs the warps land on.  Launches with fewer than
+// `queue_min` pairs per CTA use the fixed stride (the queues' first atomic and final sweep
+// cost more than they gain there).  With `list` (k_expand), pair position j is the record
+// list[j] = {primitive, tile item, pair index, pass}: primitive-major order, so neighbouring
+// positions mostly share a primitive (same shading path, state, spans and texels); without
+// it, pair position j is pair j in tile order.  Lane 0 copies the next position's record into
+// shared memory with cp.async while the warp shades the current one, so no global load chain
+// sits between two positions.
 constexpr uint32_t SHADE_CHUNK = 128;
 
 // 16- or 8-byte asynchronous global -> shared copy (no registers held while in flight).
@@ -2907,6 +3003,12 @@ __device__ __noinline__ uint32_t queue_steal(uint32_t *queues, uint32_t nq, uint
 
 // Compiled for several minimum residencies (register budgets); the executor's autotuner
 // picks one.  More resident CTAs hide more latency at the price of some spilling.
+//
+// Work unit: half a pair (rows 0-3 or 4-7 of the tile, one pixel per lane), position p =
+// 2 x pair position + half.  Each warp takes positions on its own (no CTA barrier: a warp whose
+// rows the primitive misses moves on at once), reads the rows' spans that k_bin computed once
+// per primitive (row y of primitive i is spans[prim_rows[i] + y - span_ylo]), shades, and
+// writes its 32 pixels of the pair's scratch.
 template <int MIN_CTAS>
 __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass *__restrict__ passes, uint32_t num_passes,
                                                         const uint2 *__restrict__ pairs, const uint32_t *__restrict__ ctrl,
@@ -2917,26 +3019,29 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass
                                                         uint32_t *__restrict__ sc_color, int *__restrict__ sc_zdith,
                                                         uint16_t *__restrict__ sc_misc, const uint4 *__restrict__ list,
                                                         uint32_t *__restrict__ queues, uint32_t num_queues,
-                                                        uint32_t queue_min)
+                                                        uint32_t queue_min, const SpanRow *__restrict__ spans,
+                                                        const uint32_t *__restrict__ prim_rows)
 {
-	__shared__ SpanA s_sa[9];
-	__shared__ SpanX s_sx[9];
-	__shared__ __align__(16) uint4 s_rec[2]; // current / next position's record
-	__shared__ uint32_t s_pos[2];
+	constexpr int WARPS = SHADE_THREADS / 32;
+	__shared__ __align__(16) uint4 s_rec_all[WARPS][2]; // current / next position's record, per warp
+	__shared__ uint32_t s_pos_all[WARPS][2];
 	if (ctrl[1]) return;
-	const uint32_t total = ctrl[0];
-	const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-	if (total < gridDim.x * queue_min) queues = nullptr;
+	const uint32_t num_pairs = ctrl[0], total = num_pairs * 2u;
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	uint4 *s_rec = s_rec_all[wid];
+	uint32_t *s_pos = s_pos_all[wid];
+	const uint32_t worker = blockIdx.x * WARPS + uint32_t(wid), workers = gridDim.x * WARPS;
+	if (num_pairs < gridDim.x * queue_min) queues = nullptr;
 	uint32_t q = 0, k_next = 0;
 	int buf = 0;
-	// Thread 0: the record of position j into s_rec[b] (asynchronous).
-	auto fetch = [&](uint32_t j, int b) {
-		if (list) cp_async16(&s_rec[b], list + j);
-		else cp_async8(&s_rec[b], pairs + j);
+	// Lane 0: the record of position p's pair into s_rec[b] (asynchronous).
+	auto fetch = [&](uint32_t p, int b) {
+		if (list) cp_async16(&s_rec[b], list + (p >> 1));
+		else cp_async8(&s_rec[b], pairs + (p >> 1));
 	};
-	if (tid == 0)
+	if (lane == 0)
 	{
-		uint32_t first = blockIdx.x;
+		uint32_t first = worker;
 		if (queues)
 		{
 			q = sm_id() % num_queues;
@@ -2948,164 +3053,35 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass
 		s_pos[0] = first;
 		cp_async_wait_all();
 	}
-	__syncthreads();
-	uint32_t j = s_pos[0];
-	while (j < total)
+	__syncwarp();
+	uint32_t p = s_pos[0];
+	while (p < total)
 	{
 		const uint4 rec = s_rec[buf];
-		const uint32_t prim = rec.x, item = rec.y, pr = list ? rec.z : j;
-		// Thread 0: the next position (its queue atomic was issued a position ago) and its record.
-		if (tid == 0)
+		const uint32_t prim = rec.x, item = rec.y, pr = list ? rec.z : (p >> 1);
+		const int half = int(p & 1u);
+		// Lane 0: the next position (its queue atomic was issued a position ago) and its record.
+		if (lane == 0)
 		{
-			uint32_t nj = j + gridDim.x;
+			uint32_t np = p + workers;
 			if (queues)
 			{
-				nj = queue_pos(q, k_next, num_queues);
-				if (nj >= total) nj = queue_steal(queues, num_queues, total, q);
-				if (nj < total) k_next = atomicAdd(&queues[q], 1u);
+				np = queue_pos(q, k_next, num_queues);
+				if (np >= total) np = queue_steal(queues, num_queues, total, q);
+				if (np < total) k_next = atomicAdd(&queues[q], 1u);
 			}
-			if (nj < total) fetch(nj, buf ^ 1);
-			s_pos[buf ^ 1] = nj;
+			if (np < total) fetch(np, buf ^ 1);
+			s_pos[buf ^ 1] = np;
 		}
 		const RdpPass &ps = passes[list ? rec.w : shade[prim].pass];
-		uint32_t tl = item - ps.tile_item_begin;
-		int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
+		const uint32_t tl = item - ps.tile_item_begin;
+		const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
 		const RdpPrimGeom &g = geom[prim];
-		if (lane < 9)
-		{
-			if (wid == 0) span_attr(g, attr[prim], ty * 8 + lane, s_sa[lane]);
-			else span_x(g, ty * 8 + lane, s_sx[lane]);
-		}
-		__syncthreads();
-		PassConst pc;
-		switch (ps.fb_fmt)
-		{
-		case FBF_I4: pc.fb_size = 0; pc.dx_mask = 0; pc.dx_shift = 0; break;
-		case FBF_I8: pc.fb_size = 1; pc.dx_mask = ~7; pc.dx_shift = 3; break;
-		case FBF_RGBA5551:
-		case FBF_IA88: pc.fb_size = 2; pc.dx_mask = ~3; pc.dx_shift = 2; break;
-		default: pc.fb_size = 4; pc.dx_mask = ~1; pc.dx_shift = 1; break;
-		}
-		pc.alias = ps.fb_addr == ps.depth_addr;
-		int r = tid >> 3;
-		int x = tx * 8 + (tid & 7), y = ty * 8 + r;
+		const int x = tx * 8 + (lane & 7), y = ty * 8 + half * 4 + (lane >> 3);
 		Shaded out;
 		bool ok = false;
 		if (x < int(ps.fb_width) && y < int(ps.fb_height) && y >= g.span_ylo && y <= g.span_yhi)
 		{
-			const RdpPrimShade &sh = shade[prim];
-			ok = shade_pixel(pc, g, attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
-			                 ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, s_sa[r], s_sx[r], s_sa[r + 1], s_sx[r + 1],
-			                 x, y, out);
-		}
-		// All 64 pixels of the scratch are written (full sectors, no partial-sector
-		// read-modify-write in L2); k_blend skips pixels whose misc word says "not written".
-		size_t at = size_t(pr) * SHADE_THREADS + tid;
-		sc_color[at] = ok ? out.combined : 0u;
-		sc_zdith[at] = ok ? out.z_dith : 0;
-		sc_misc[at] = ok ? uint16_t((out.coverage & 0xff) | (out.shade_alpha << 8)) : uint16_t(0x00ffu);
-		if (tid == 0) cp_async_wait_all();
-		__syncthreads();
-		buf ^= 1;
-		j = s_pos[buf];
-	}
-}
-
-// Compacted shading: a CTA of COMPACT_THREADS takes COMPACT_PAIRS consecutive pairs, computes
-// their spans into shared memory, marks the pixels that lie inside a valid span (only those can
-// have coverage), and shades just those -- about half of a tile's pixels on typical scenes, so
-// lanes no longer idle on uncovered pixels.  Results are identical to k_shade.  It takes the
-// pairs in tile order with a fixed stride (no queues, no primitive-major order).
-constexpr int COMPACT_THREADS = 128;
-constexpr int COMPACT_PAIRS = 4;
-
-template <int MIN_CTAS>
-__global__ void __launch_bounds__(COMPACT_THREADS, MIN_CTAS)
-	k_shade_compact(const RdpPass *__restrict__ passes, uint32_t num_passes, const uint2 *__restrict__ pairs,
-	                const uint32_t *__restrict__ ctrl, const RdpPrimGeom *__restrict__ geom,
-	                const RdpPrimAttr *__restrict__ attr, const RdpPrimShade *__restrict__ shade,
-	                const RdpTile *__restrict__ tilesets, uint32_t *__restrict__ sc_color, int *__restrict__ sc_zdith,
-	                uint16_t *__restrict__ sc_misc, const uint4 *, uint32_t *, uint32_t, uint32_t)
-{
-	__shared__ SpanA s_sa[COMPACT_PAIRS][9];
-	__shared__ SpanX s_sx[COMPACT_PAIRS][9];
-	__shared__ uint32_t s_prim[COMPACT_PAIRS], s_pass[COMPACT_PAIRS], s_tile[COMPACT_PAIRS];
-	__shared__ uint16_t s_list[COMPACT_PAIRS * 64];
-	__shared__ uint32_t s_count;
-	if (ctrl[1]) return;
-	const uint32_t total = ctrl[0];
-	const uint32_t groups = (total + COMPACT_PAIRS - 1) / COMPACT_PAIRS;
-	const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-	for (uint32_t grp = blockIdx.x; grp < groups; grp += gridDim.x)
-	{
-		const uint32_t pr0 = grp * COMPACT_PAIRS;
-		const uint32_t npr = min(uint32_t(COMPACT_PAIRS), total - pr0);
-		if (tid < COMPACT_PAIRS)
-		{
-			if (uint32_t(tid) < npr)
-			{
-				const uint2 pa = pairs[pr0 + tid];
-				const uint32_t pi = pass_of_item(passes, num_passes, pa.y);
-				s_prim[tid] = pa.x;
-				s_pass[tid] = pi;
-				s_tile[tid] = pa.y - passes[pi].tile_item_begin;
-			}
-		}
-		if (tid == 0) s_count = 0;
-		__syncthreads();
-		// Spans: COMPACT_PAIRS x 9 rows x {attribute, x} tasks.
-		for (int task = tid; task < COMPACT_PAIRS * 18; task += COMPACT_THREADS)
-		{
-			const int gi = task / 18, kind = (task % 18) / 9, row = task % 9;
-			if (uint32_t(gi) < npr)
-			{
-				const RdpPass &ps = passes[s_pass[gi]];
-				const int ty = int(s_tile[gi] / ps.tiles_x);
-				const RdpPrimGeom &g = geom[s_prim[gi]];
-				if (kind == 0) span_attr(g, attr[s_prim[gi]], ty * 8 + row, s_sa[gi][row]);
-				else span_x(g, ty * 8 + row, s_sx[gi][row]);
-			}
-		}
-		__syncthreads();
-		// Candidate pixels (inside a valid span of their row); the rest are written as empty.
-		for (int slot = tid; slot < COMPACT_PAIRS * 64; slot += COMPACT_THREADS)
-		{
-			const int gi = slot >> 6, px = slot & 63;
-			bool cand = false;
-			if (uint32_t(gi) < npr)
-			{
-				const RdpPass &ps = passes[s_pass[gi]];
-				const uint32_t tl = s_tile[gi];
-				const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
-				const int r = px >> 3, x = tx * 8 + (px & 7), y = ty * 8 + r;
-				const RdpPrimGeom &g = geom[s_prim[gi]];
-				const SpanX &sx = s_sx[gi][r];
-				cand = x < int(ps.fb_width) && y < int(ps.fb_height) && y >= g.span_ylo && y <= g.span_yhi && sx.valid &&
-				       x >= sx.start_x && x <= sx.end_x;
-				if (!cand)
-				{
-					const size_t at = size_t(pr0 + gi) * SHADE_THREADS + px;
-					sc_color[at] = 0u;
-					sc_zdith[at] = 0;
-					sc_misc[at] = 0x00ffu;
-				}
-			}
-			const unsigned m = __ballot_sync(0xffffffffu, cand);
-			uint32_t base = 0;
-			if (lane == 0 && m) base = atomicAdd(&s_count, uint32_t(__popc(m)));
-			base = __shfl_sync(0xffffffffu, base, 0);
-			if (cand) s_list[base + __popc(m & ((1u << lane) - 1u))] = uint16_t(slot);
-		}
-		__syncthreads();
-		const uint32_t count = s_count;
-		for (uint32_t i = tid; i < count; i += COMPACT_THREADS)
-		{
-			const int slot = s_list[i];
-			const int gi = slot >> 6, px = slot & 63;
-			const RdpPass &ps = passes[s_pass[gi]];
-			const uint32_t tl = s_tile[gi];
-			const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
-			const int r = px >> 3, x = tx * 8 + (px & 7), y = ty * 8 + r;
 			PassConst pc;
 			switch (ps.fb_fmt)
 			{
@@ -3116,18 +3092,161 @@ __global__ void __launch_bounds__(COMPACT_THREADS, MIN_CTAS)
 			default: pc.fb_size = 4; pc.dx_mask = ~1; pc.dx_shift = 1; break;
 			}
 			pc.alias = ps.fb_addr == ps.depth_addr;
-			const uint32_t prim = s_prim[gi];
+			const SpanRow *sp = spans + prim_rows[prim] + uint32_t(y - g.span_ylo);
 			const RdpPrimShade &sh = shade[prim];
-			Shaded out;
-			const bool ok = shade_pixel(pc, geom[prim], attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
-			                            ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, s_sa[gi][r], s_sx[gi][r],
-			                            s_sa[gi][r + 1], s_sx[gi][r + 1], x, y, out);
-			const size_t at = size_t(pr0 + gi) * SHADE_THREADS + px;
-			sc_color[at] = ok ? out.combined : 0u;
-			sc_zdith[at] = ok ? out.z_dith : 0;
-			sc_misc[at] = ok ? uint16_t((out.coverage & 0xff) | (out.shade_alpha << 8)) : uint16_t(0x00ffu);
+			ok = shade_pixel(pc, g, attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
+			                 ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, sp[0], sp[1], x, y, out);
 		}
-		__syncthreads();
+		// All 64 pixels of the scratch are written (full sectors, no partial-sector
+		// read-modify-write in L2); k_blend skips pixels whose misc word says "not written".
+		const size_t at = size_t(pr) * SHADE_THREADS + size_t(half) * 32 + size_t(lane);
+		sc_color[at] = ok ? out.combined : 0u;
+		sc_zdith[at] = ok ? out.z_dith : 0;
+		sc_misc[at] = ok ? uint16_t((out.coverage & 0xff) | (out.shade_alpha << 8)) : uint16_t(0x00ffu);
+		if (lane == 0) cp_async_wait_all();
+		__syncwarp();
+		buf ^= 1;
+		p = s_pos[buf];
+	}
+}
+
+// Packed shading: one warp per pair (no CTA barrier), same work order and scratch as k_shade.
+// The warp first picks the pair's candidate pixels -- inside the image and inside the valid span
+// of their row (k_span's rows), the only ones that can be covered -- and shades just those,
+// packed into as few 32-lane rounds as they fill: one round for most pairs at a primitive's
+// edge, where k_shade's half-pair warps would each run a round with idle lanes.  The other
+// pixels are written as empty.  Same results as k_shade.
+template <int MIN_CTAS>
+__global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
+	k_shade_packed(const RdpPass *__restrict__ passes, uint32_t num_passes, const uint2 *__restrict__ pairs,
+	               const uint32_t *__restrict__ ctrl, const RdpPrimGeom *__restrict__ geom,
+	               const RdpPrimAttr *__restrict__ attr, const RdpPrimShade *__restrict__ shade,
+	               const RdpTile *__restrict__ tilesets, uint32_t *__restrict__ sc_color, int *__restrict__ sc_zdith,
+	               uint16_t *__restrict__ sc_misc, const uint4 *__restrict__ list, uint32_t *__restrict__ queues,
+	               uint32_t num_queues, uint32_t queue_min, const SpanRow *__restrict__ spans,
+	               const uint32_t *__restrict__ prim_rows)
+{
+	constexpr int WARPS = SHADE_THREADS / 32;
+	__shared__ __align__(16) uint4 s_rec_all[WARPS][2]; // current / next position's record, per warp
+	__shared__ uint32_t s_pos_all[WARPS][2];
+	__shared__ uint8_t s_px_all[WARPS][64];              // candidate pixels, in pixel order
+	if (ctrl[1]) return;
+	const uint32_t total = ctrl[0];
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	uint4 *s_rec = s_rec_all[wid];
+	uint32_t *s_pos = s_pos_all[wid];
+	uint8_t *s_px = s_px_all[wid];
+	const uint32_t worker = blockIdx.x * WARPS + uint32_t(wid), workers = gridDim.x * WARPS;
+	if (total < gridDim.x * queue_min) queues = nullptr;
+	uint32_t q = 0, k_next = 0;
+	int buf = 0;
+	auto fetch = [&](uint32_t j, int b) {
+		if (list) cp_async16(&s_rec[b], list + j);
+		else cp_async8(&s_rec[b], pairs + j);
+	};
+	if (lane == 0)
+	{
+		uint32_t first = worker;
+		if (queues)
+		{
+			q = sm_id() % num_queues;
+			first = queue_pos(q, atomicAdd(&queues[q], 1u), num_queues);
+			if (first >= total) first = queue_steal(queues, num_queues, total, q);
+			if (first < total) k_next = atomicAdd(&queues[q], 1u);
+		}
+		if (first < total) fetch(first, 0);
+		s_pos[0] = first;
+		cp_async_wait_all();
+	}
+	__syncwarp();
+	uint32_t j = s_pos[0];
+	const unsigned below = (1u << lane) - 1u;
+	while (j < total)
+	{
+		const uint4 rec = s_rec[buf];
+		const uint32_t prim = rec.x, item = rec.y, pr = list ? rec.z : j;
+		if (lane == 0)
+		{
+			uint32_t nj = j + workers;
+			if (queues)
+			{
+				nj = queue_pos(q, k_next, num_queues);
+				if (nj >= total) nj = queue_steal(queues, num_queues, total, q);
+				if (nj < total) k_next = atomicAdd(&queues[q], 1u);
+			}
+			if (nj < total) fetch(nj, buf ^ 1);
+			s_pos[buf ^ 1] = nj;
+		}
+		const RdpPass &ps = passes[list ? rec.w : shade[prim].pass];
+		const uint32_t tl = item - ps.tile_item_begin;
+		const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
+		const RdpPrimGeom &g = geom[prim];
+		const int fbw = int(ps.fb_width), fbh = int(ps.fb_height), ylo = g.span_ylo, yhi = g.span_yhi;
+		// Row y of the primitive is rows[y - ylo].
+		const SpanRow *rows = spans + prim_rows[prim];
+		// Candidates among pixels lane (rows 0-3) and lane + 32 (rows 4-7).
+		const int x = tx * 8 + (lane & 7), y0 = ty * 8 + (lane >> 3), y1 = y0 + 4;
+		bool c0 = x < fbw && y0 < fbh && y0 >= ylo && y0 <= yhi;
+		bool c1 = x < fbw && y1 < fbh && y1 >= ylo && y1 <= yhi;
+		if (c0)
+		{
+			const SpanRow &r = rows[y0 - ylo];
+			c0 = r.valid && x >= r.start_x && x <= r.end_x;
+		}
+		if (c1)
+		{
+			const SpanRow &r = rows[y1 - ylo];
+			c1 = r.valid && x >= r.start_x && x <= r.end_x;
+		}
+		const unsigned m0 = __ballot_sync(0xffffffffu, c0), m1 = __ballot_sync(0xffffffffu, c1);
+		const int n0 = __popc(m0), count = n0 + __popc(m1);
+		if (c0) s_px[__popc(m0 & below)] = uint8_t(lane);
+		if (c1) s_px[n0 + __popc(m1 & below)] = uint8_t(lane + 32);
+		const size_t base = size_t(pr) * SHADE_THREADS;
+		// Every pixel of the scratch is written (full sectors); k_blend skips "not written".
+		if (!c0)
+		{
+			sc_color[base + lane] = 0u;
+			sc_zdith[base + lane] = 0;
+			sc_misc[base + lane] = 0x00ffu;
+		}
+		if (!c1)
+		{
+			sc_color[base + 32 + lane] = 0u;
+			sc_zdith[base + 32 + lane] = 0;
+			sc_misc[base + 32 + lane] = 0x00ffu;
+		}
+		__syncwarp();
+		if (count)
+		{
+			PassConst pc;
+			switch (ps.fb_fmt)
+			{
+			case FBF_I4: pc.fb_size = 0; pc.dx_mask = 0; pc.dx_shift = 0; break;
+			case FBF_I8: pc.fb_size = 1; pc.dx_mask = ~7; pc.dx_shift = 3; break;
+			case FBF_RGBA5551:
+			case FBF_IA88: pc.fb_size = 2; pc.dx_mask = ~3; pc.dx_shift = 2; break;
+			default: pc.fb_size = 4; pc.dx_mask = ~1; pc.dx_shift = 1; break;
+			}
+			pc.alias = ps.fb_addr == ps.depth_addr;
+			const RdpPrimShade &sh = shade[prim];
+			for (int s = lane; s < count; s += 32)
+			{
+				const int px = s_px[s], y = ty * 8 + (px >> 3);
+				const SpanRow *sp = rows + (y - ylo);
+				Shaded out;
+				const bool ok = shade_pixel(pc, g, attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
+				                            ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, sp[0], sp[1],
+				                            tx * 8 + (px & 7), y, out);
+				sc_color[base + px] = ok ? out.combined : 0u;
+				sc_zdith[base + px] = ok ? out.z_dith : 0;
+				sc_misc[base + px] = ok ? uint16_t((out.coverage & 0xff) | (out.shade_alpha << 8)) : uint16_t(0x00ffu);
+			}
+		}
+		if (lane == 0) cp_async_wait_all();
+		__syncwarp();
+		buf ^= 1;
+		j = s_pos[buf];
 	}
 }
 
@@ -3294,8 +3413,7 @@ __device__ __forceinline__ void raster_tile(uint32_t item, const RdpPass *__rest
                                             const RdpPrimGeom *__restrict__ geom, const RdpPrimAttr *__restrict__ attr,
                                             const RdpPrimShade *__restrict__ shade, const RdpTile *__restrict__ tilesets)
 {
-	__shared__ SpanA s_sa[2][5];
-	__shared__ SpanX s_sx[2][5];
+	__shared__ SpanRow s_sp[2][5];
 	__shared__ int s_any;
 	const int wib = threadIdx.x >> 5;
 	const int lane = threadIdx.x & 31;
@@ -3365,16 +3483,16 @@ __device__ __forceinline__ void raster_tile(uint32_t item, const RdpPass *__rest
 				if (yhi < row0 || ylo > row0 + 3) continue; // no row of this warp is covered
 				// Spans for the warp's 4 rows plus the next row (pipelined texel1 peek).
 				if (lane < 5)
-					span_attr(g, attr[prim], row0 + lane, s_sa[wib][lane]);
+					span_attr(g, attr[prim], row0 + lane, s_sp[wib][lane]);
 				else if (lane >= 16 && lane < 21)
-					span_x(g, row0 + (lane - 16), s_sx[wib][lane - 16]);
+					span_x(g, row0 + (lane - 16), s_sp[wib][lane - 16]);
 				__syncwarp();
 				if (inside && px_y >= ylo && px_y <= yhi)
 				{
 					const RdpPrimShade &sh = shade[prim];
 					frags += shade_and_blend(ps, pc, g, attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
-					                         ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, s_sa[wib][r],
-					                         s_sx[wib][r], s_sa[wib][r + 1], s_sx[wib][r + 1], px_x, px_y, px);
+					                         ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, s_sp[wib][r],
+					                         s_sp[wib][r + 1], px_x, px_y, px);
 				}
 				__syncwarp();
 			}
@@ -3439,14 +3557,11 @@ extern "C" cudaError_t rdp_kernels_init_luts(const uint8_t *blender_lut)
 namespace {
 typedef void (*ShadeKernel)(const RdpPass *, uint32_t, const uint2 *, const uint32_t *, const RdpPrimGeom *,
                             const RdpPrimAttr *, const RdpPrimShade *, const RdpTile *, uint32_t *, int *, uint16_t *,
-                            const uint4 *, uint32_t *, uint32_t, uint32_t);
-const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = { rdp::k_shade<1>,  rdp::k_shade<12>, rdp::k_shade<16>,
-                                                         rdp::k_shade<20>, rdp::k_shade<24>, rdp::k_shade<28>,
-                                                         rdp::k_shade<32>, rdp::k_shade_compact<12> };
-// Threads per CTA of each variant.
-const int kShadeThreads[RDP_SHADE_VARIANTS] = { rdp::SHADE_THREADS, rdp::SHADE_THREADS, rdp::SHADE_THREADS,
-                                                rdp::SHADE_THREADS, rdp::SHADE_THREADS, rdp::SHADE_THREADS,
-                                                rdp::SHADE_THREADS, rdp::COMPACT_THREADS };
+                            const uint4 *, uint32_t *, uint32_t, uint32_t, const rdp::SpanRow *, const uint32_t *);
+const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = {
+	rdp::k_shade<16>,        rdp::k_shade<18>,        rdp::k_shade<20>,        rdp::k_shade<24>,
+	rdp::k_shade_packed<16>, rdp::k_shade_packed<18>, rdp::k_shade_packed<20>, rdp::k_shade_packed<24>
+};
 } // namespace
 
 extern "C" int rdp_kernels_blend_ctas_per_sm(void)
@@ -3460,7 +3575,7 @@ extern "C" int rdp_kernels_shade_ctas_per_sm(int variant)
 {
 	if (variant < 0 || variant >= RDP_SHADE_VARIANTS) variant = 0;
 	int n = 0;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kShadeVariants[variant], kShadeThreads[variant], 0) !=
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kShadeVariants[variant], rdp::SHADE_THREADS, 0) !=
 	    cudaSuccess)
 		n = 8;
 	return n > 0 ? n : 1;
@@ -3477,6 +3592,7 @@ extern "C" uint32_t rdp_kernels_count(const RdpLaunch *L)
 {
 	uint32_t n = 0;
 	if (L->num_prims) n += 2;
+	if (L->num_prims && L->num_tile_items && L->spans) n += 1;
 	if (L->num_tmem_passes) n += 2;
 	if (L->num_prims && L->num_tile_items)
 	{
@@ -3507,6 +3623,15 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		                                                                 L->tile_counts,
 		                                                                 L->shade_list && L->num_tile_items ? L->prim_pairs
 		                                                                                                   : nullptr);
+		// Span rows only when the pair path follows (k_scan resets their counter).
+		if (L->num_tile_items && L->spans)
+		{
+			const uint32_t chunk = std::min<uint32_t>(
+				std::max<uint32_t>(L->num_prims / (4u * std::max<uint32_t>(L->num_sms, 1u)), 1u), rdp::SPAN_THREADS);
+			rdp::k_span<<<(L->num_prims + chunk - 1) / chunk, rdp::SPAN_THREADS, 0, stream>>>(
+				L->num_prims, L->geom, L->attr, L->shade, L->passes, static_cast<rdp::SpanRow *>(L->spans),
+				L->span_capacity, L->prim_rows, reinterpret_cast<unsigned long long *>(L->ctrl + 6), chunk);
+		}
 	}
 	if (L->num_tmem_passes)
 	{
@@ -3519,6 +3644,8 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 	{
 		// The primitive scan (primitive-major shading order) rides in the tile scan's launches.
 		const uint32_t scan_prims = L->shade_list ? L->num_prims : 0u;
+		// Without a span buffer every launch takes k_raster (capacity 0 rows).
+		const uint2 capacity = make_uint2(L->pair_capacity, L->spans ? L->span_capacity : 0u);
 		if (multi_cta_scan(L))
 		{
 			const uint32_t nb = (L->num_tile_items + rdp::SCAN_TILE - 1) / rdp::SCAN_TILE;
@@ -3527,7 +3654,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 			                                                               L->scan_blocks, nb, scan_prims,
 			                                                               L->prim_pairs, L->prim_scan_blocks);
 			rdp::k_scan_top<<<1, 1024, 0, stream>>>(nb, L->scan_blocks, L->num_tile_items, L->pair_offsets, L->ctrl,
-			                                        L->pair_capacity, L->pair_log, L->log_slot, L->shade_queues,
+			                                        capacity, L->pair_log, L->log_slot, L->shade_queues,
 			                                        L->num_shade_queues, nbp, L->prim_scan_blocks);
 			rdp::k_scan_down<<<nb + nbp, rdp::SCAN_THREADS, 0, stream>>>(
 				L->num_tile_items, L->tile_counts, L->scan_blocks, L->pair_offsets, L->nonempty_tiles, nb, scan_prims,
@@ -3535,7 +3662,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		}
 		else
 			rdp::k_scan<<<1, 1024, 0, stream>>>(L->num_tile_items, L->tile_counts, L->pair_offsets, L->nonempty_tiles,
-			                                    L->ctrl, L->pair_capacity, L->pair_log, L->log_slot, L->shade_queues,
+			                                    L->ctrl, capacity, L->pair_log, L->log_slot, L->shade_queues,
 			                                    L->num_shade_queues, scan_prims, L->prim_pairs, L->prim_offsets);
 		const bool sched = L->sched && (L->sched->order_enabled || L->sched->train_enabled);
 		rdp::k_expand<<<(L->num_tile_items * 32 + 255) / 256, 256, 0, stream>>>(
@@ -3550,11 +3677,10 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		if (L->shade_events[0]) cudaEventRecordWithFlags(L->shade_events[0], stream, ev_flags);
 		const uint32_t sv = L->shade_variant < RDP_SHADE_VARIANTS ? L->shade_variant : 0;
 		const ShadeKernel shade_kernel = kShadeVariants[sv];
-		shade_kernel<<<L->shade_ctas, kShadeThreads[sv], 0, stream>>>(L->passes, L->num_passes, L->pairs, L->ctrl,
-		                                                               L->geom, L->attr, L->shade, L->tilesets,
-		                                                               L->sc_color, L->sc_zdith, L->sc_misc,
-		                                                               L->shade_list, L->shade_queues,
-		                                                               L->num_shade_queues, L->shade_queue_min);
+		shade_kernel<<<L->shade_ctas, rdp::SHADE_THREADS, 0, stream>>>(
+			L->passes, L->num_passes, L->pairs, L->ctrl, L->geom, L->attr, L->shade, L->tilesets, L->sc_color,
+			L->sc_zdith, L->sc_misc, L->shade_list, L->shade_queues, L->num_shade_queues, L->shade_queue_min,
+			static_cast<const rdp::SpanRow *>(L->spans), L->prim_rows);
 		if (L->shade_events[1]) cudaEventRecordWithFlags(L->shade_events[1], stream, ev_flags);
 		const uint32_t tile_ctas = std::min<uint32_t>(L->num_tile_items, L->blend_ctas);
 		const uint32_t *order = L->tile_order;

@@ -5,9 +5,11 @@
 #include <cuda_runtime.h>
 #include "rdp_types.h"
 
-/* Shading kernels: k_shade (one pair per 64-thread CTA) for minimum residencies of 1, 12, 16,
- * 20, 24, 28 and 32 CTAs per SM, and k_shade_compact (4 pairs per 128-thread CTA, pixels inside
- * the spans only) for 12. */
+/* Shading kernel variants (the autotuner chooses among them): k_shade (one warp per half pair)
+ * and k_shade_packed (one warp per pair, candidate pixels packed), each compiled for minimum
+ * residencies of 16, 18, 20 and 24 64-thread CTAs per SM. */
+/* Bytes of one span row (one scanline of one primitive, computed by k_bin). */
+#define RDP_SPAN_ROW_BYTES 64
 /* Launches with more tiles (or, in primitive-major order, primitives) than this scan their
  * pair counts with several CTAs. */
 #define RDP_SCAN_SINGLE_CTA_MAX 16384
@@ -61,6 +63,10 @@ typedef struct RdpLaunch
 	uint32_t *pair_log;             /* optional: k_scan writes the launch's pair count to pair_log[log_slot] */
 	uint32_t log_slot;
 	const struct RdpSchedDev *sched; /* optional learned tile order / online training (sched.h) */
+	void *spans;                    /* [span_capacity] span rows (RDP_SPAN_ROW_BYTES each) */
+	uint32_t span_capacity;
+	uint32_t *prim_rows;            /* [num_prims] first span row of each primitive */
+	uint32_t num_sms;               /* the device's SM count (sizes k_span's CTAs) */
 	uint32_t *sc_color;             /* [pair_capacity * 64] */
 	int *sc_zdith;
 	uint16_t *sc_misc;

@@ -2210,11 +2210,12 @@ int rdp_serve_run(rdp_batch *b, rdp_cp *const *instances, uint32_t num_instances
 	using clock = std::chrono::steady_clock;
 	const auto t0 = clock::now();
 	auto now_s = [&] { return std::chrono::duration<double>(clock::now() - t0).count(); };
-	// Footprint estimate: primitive records, staging and ~8 shaded (primitive, tile) pairs per primitive.
+	// Footprint estimate: primitive records, staging, ~8 shaded (primitive, tile) pairs and ~24
+	// span rows per primitive.
 	auto footprint = [](const rdp_serve_request &q) -> uint64_t {
 		if (q.footprint_bytes) return q.footprint_bytes;
 		uint64_t prims = q.num_words / 20 + 1;
-		return prims * (336 + 8 * 648) + uint64_t(q.num_words) * 4;
+		return prims * (336 + 8 * 648 + 24 * RDP_SPAN_ROW_BYTES) + uint64_t(q.num_words) * 4;
 	};
 	struct Flight
 	{

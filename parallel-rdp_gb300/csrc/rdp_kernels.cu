@@ -1679,99 +1679,103 @@ struct CombIn
 	int lod_frac, noise;
 };
 
+__device__ __forceinline__ void pick3(int v[3], const int *src) { v[0] = src[0]; v[1] = src[1]; v[2] = src[2]; }
+__device__ __forceinline__ void pick3(int v[3], const uint8_t *src) { v[0] = src[0]; v[1] = src[1]; v[2] = src[2]; }
+__device__ __forceinline__ void splat3(int v[3], int x) { v[0] = v[1] = v[2] = x; }
+
+// One combiner cycle, (A - B) * C + D per channel (combiner.h:196-282).  The selectors are the
+// same for the three colour channels, so each is decoded once for all three.
 __device__ __forceinline__ void combine(const CombIn &in, const uint8_t *rs, const uint8_t *as, int out[4])
 {
-#pragma unroll
-	for (int c = 0; c < 4; c++)
+	int a[3], b[3], m[3], d[3];
+	switch (rs[0])
 	{
-		int a, b, m, d;
-		if (c < 3)
-		{
-			switch (rs[0])
-			{
-			case 0: a = in.comb[c]; break;
-			case 1: a = in.tex0[c]; break;
-			case 2: a = in.tex1[c]; break;
-			case 4: a = in.shade[c]; break;
-			case 7: a = in.noise; break;
-			case 6: a = 0x100; break;
-			default: a = in.cma[c]; break;
-			}
-			switch (rs[1])
-			{
-			case 0: b = in.comb[c]; break;
-			case 1: b = in.tex0[c]; break;
-			case 2: b = in.tex1[c]; break;
-			case 4: b = in.shade[c]; break;
-			case 7: b = (int(in.cms[1]) << 8) | in.cms[2]; break;
-			default: b = in.cms[c]; break;
-			}
-			switch (rs[2])
-			{
-			case 0: m = in.comb[c]; break;
-			case 7: m = in.comb[3]; break;
-			case 1: m = in.tex0[c]; break;
-			case 2: m = in.tex1[c]; break;
-			case 4: m = in.shade[c]; break;
-			case 8: m = in.tex0[3]; break;
-			case 9: m = in.tex1[3]; break;
-			case 11: m = in.shade[3]; break;
-			case 13: m = in.lod_frac; break;
-			case 15: m = (int(in.cmu[1]) << 8) | in.cmu[2]; break;
-			default: m = in.cmu[c]; break;
-			}
-			switch (rs[3])
-			{
-			case 0: d = in.comb[c]; break;
-			case 1: d = in.tex0[c]; break;
-			case 2: d = in.tex1[c]; break;
-			case 4: d = in.shade[c]; break;
-			case 6: d = 0x100; break;
-			default: d = in.cad[c]; break;
-			}
-		}
-		else
-		{
-			switch (as[0])
-			{
-			case 0: a = in.comb[3]; break;
-			case 1: a = in.tex0[3]; break;
-			case 2: a = in.tex1[3]; break;
-			case 4: a = in.shade[3]; break;
-			case 6: a = 0x100; break;
-			default: a = in.cma[3]; break;
-			}
-			switch (as[1])
-			{
-			case 0: b = in.comb[3]; break;
-			case 1: b = in.tex0[3]; break;
-			case 2: b = in.tex1[3]; break;
-			case 4: b = in.shade[3]; break;
-			case 6: b = 0x100; break;
-			default: b = in.cms[3]; break;
-			}
-			switch (as[2])
-			{
-			case 0: m = in.lod_frac; break;
-			case 1: m = in.tex0[3]; break;
-			case 2: m = in.tex1[3]; break;
-			case 4: m = in.shade[3]; break;
-			default: m = in.cmu[3]; break;
-			}
-			switch (as[3])
-			{
-			case 0: d = in.comb[3]; break;
-			case 1: d = in.tex0[3]; break;
-			case 2: d = in.tex1[3]; break;
-			case 4: d = in.shade[3]; break;
-			case 6: d = 0x100; break;
-			default: d = in.cad[3]; break;
-			}
-		}
-		int col = (special_expand(a) - special_expand(b)) * bfe_s(m, 9);
-		col += 0x80;
-		out[c] = (col >> 8) + special_expand(d);
+	case 0: pick3(a, in.comb); break;
+	case 1: pick3(a, in.tex0); break;
+	case 2: pick3(a, in.tex1); break;
+	case 4: pick3(a, in.shade); break;
+	case 7: splat3(a, in.noise); break;
+	case 6: splat3(a, 0x100); break;
+	default: pick3(a, in.cma); break;
 	}
+	switch (rs[1])
+	{
+	case 0: pick3(b, in.comb); break;
+	case 1: pick3(b, in.tex0); break;
+	case 2: pick3(b, in.tex1); break;
+	case 4: pick3(b, in.shade); break;
+	case 7: splat3(b, (int(in.cms[1]) << 8) | in.cms[2]); break;
+	default: pick3(b, in.cms); break;
+	}
+	switch (rs[2])
+	{
+	case 0: pick3(m, in.comb); break;
+	case 7: splat3(m, in.comb[3]); break;
+	case 1: pick3(m, in.tex0); break;
+	case 2: pick3(m, in.tex1); break;
+	case 4: pick3(m, in.shade); break;
+	case 8: splat3(m, in.tex0[3]); break;
+	case 9: splat3(m, in.tex1[3]); break;
+	case 11: splat3(m, in.shade[3]); break;
+	case 13: splat3(m, in.lod_frac); break;
+	case 15: splat3(m, (int(in.cmu[1]) << 8) | in.cmu[2]); break;
+	default: pick3(m, in.cmu); break;
+	}
+	switch (rs[3])
+	{
+	case 0: pick3(d, in.comb); break;
+	case 1: pick3(d, in.tex0); break;
+	case 2: pick3(d, in.tex1); break;
+	case 4: pick3(d, in.shade); break;
+	case 6: splat3(d, 0x100); break;
+	default: pick3(d, in.cad); break;
+	}
+#pragma unroll
+	for (int c = 0; c < 3; c++)
+	{
+		int col = (special_expand(a[c]) - special_expand(b[c])) * bfe_s(m[c], 9);
+		col += 0x80;
+		out[c] = (col >> 8) + special_expand(d[c]);
+	}
+	int aa, ab, am, ad;
+	switch (as[0])
+	{
+	case 0: aa = in.comb[3]; break;
+	case 1: aa = in.tex0[3]; break;
+	case 2: aa = in.tex1[3]; break;
+	case 4: aa = in.shade[3]; break;
+	case 6: aa = 0x100; break;
+	default: aa = in.cma[3]; break;
+	}
+	switch (as[1])
+	{
+	case 0: ab = in.comb[3]; break;
+	case 1: ab = in.tex0[3]; break;
+	case 2: ab = in.tex1[3]; break;
+	case 4: ab = in.shade[3]; break;
+	case 6: ab = 0x100; break;
+	default: ab = in.cms[3]; break;
+	}
+	switch (as[2])
+	{
+	case 0: am = in.lod_frac; break;
+	case 1: am = in.tex0[3]; break;
+	case 2: am = in.tex1[3]; break;
+	case 4: am = in.shade[3]; break;
+	default: am = in.cmu[3]; break;
+	}
+	switch (as[3])
+	{
+	case 0: ad = in.comb[3]; break;
+	case 1: ad = in.tex0[3]; break;
+	case 2: ad = in.tex1[3]; break;
+	case 4: ad = in.shade[3]; break;
+	case 6: ad = 0x100; break;
+	default: ad = in.cad[3]; break;
+	}
+	int col = (special_expand(aa) - special_expand(ab)) * bfe_s(am, 9);
+	col += 0x80;
+	out[3] = (col >> 8) + special_expand(ad);
 }
 
 // ---------------------------------------------------------------------------- z encode / depth test / blender
@@ -1800,24 +1804,21 @@ __device__ __forceinline__ void blender(const int pix[4], const int mem[4], cons
                         const uint8_t *m, bool force_blend, bool blend_en, bool color_on_cvg, bool cvg_wrap,
                         const int bshift[2], bool final_cycle, int out[3])
 {
+	// Each selector decoded once for the three channels.
 	int r1[3], r0[3];
-#pragma unroll
-	for (int c = 0; c < 3; c++)
+	switch (m[2])
 	{
-		switch (m[2])
-		{
-		case 0: r1[c] = pix[c]; break;
-		case 1: r1[c] = mem[c]; break;
-		case 2: r1[c] = bc[c]; break;
-		default: r1[c] = fog[c]; break;
-		}
-		switch (m[0])
-		{
-		case 0: r0[c] = pix[c]; break;
-		case 1: r0[c] = mem[c]; break;
-		case 2: r0[c] = bc[c]; break;
-		default: r0[c] = fog[c]; break;
-		}
+	case 0: pick3(r1, pix); break;
+	case 1: pick3(r1, mem); break;
+	case 2: pick3(r1, bc); break;
+	default: pick3(r1, fog); break;
+	}
+	switch (m[0])
+	{
+	case 0: pick3(r0, pix); break;
+	case 1: pick3(r0, mem); break;
+	case 2: pick3(r0, bc); break;
+	default: pick3(r0, fog); break;
 	}
 	if (final_cycle && color_on_cvg && !cvg_wrap)
 	{
@@ -2836,7 +2837,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(uint32_t num_items, 
 // (primitive, tile) pairs and clears the bitmask.
 // With `featbits`, also writes the tile's scheduling features (sched.h) to features[item].
 // With `list`, also places each pair in primitive-major order: list[prim_offsets[prim] + n] =
-// {primitive, tile item, pair index, pass}, n counted by prim_cursor (zeroed by k_scan_down);
+// {primitive, tx | ty << 16, pair index, pass}, n counted by prim_cursor (zeroed by k_scan_down);
 // the order of one primitive's tiles is arbitrary, which changes no result.
 __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes, uint32_t num_items,
                          const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ ctrl, uint2 *__restrict__ pairs,
@@ -2855,6 +2856,7 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 	uint32_t out = offsets[item];
 	const uint32_t npairs = offsets[item + 1] - out;
 	if (!npairs) return;
+	const uint32_t tile_xy = (tl % ps.tiles_x) | ((tl / ps.tiles_x) << 16); // tx | ty << 16
 	uint32_t fc[RDP_FEAT_COUNT];
 #pragma unroll
 	for (int i = 0; i < RDP_FEAT_COUNT; i++) fc[i] = 0;
@@ -2881,7 +2883,7 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 				int b = __ffs(wv) - 1;
 				wv &= wv - 1;
 				const uint32_t prim = ps.prim_begin + wi * 32 + uint32_t(b);
-				if (list) list[prim_offsets[prim] + atomicAdd(&prim_cursor[prim], 1u)] = make_uint4(prim, item, pos, pi);
+				if (list) list[prim_offsets[prim] + atomicAdd(&prim_cursor[prim], 1u)] = make_uint4(prim, tile_xy, pos, pi);
 				pairs[pos++] = make_uint2(prim, item);
 				if (featbits)
 				{
@@ -2938,7 +2940,7 @@ constexpr int SHADE_THREADS = 64;
 // every position is shaded whatever SMs the warps land on.  Launches with fewer than
 // `queue_min` pairs per CTA use the fixed stride (the queues' first atomic and final sweep
 // cost more than they gain there).  With `list` (k_expand), pair position j is the record
-// list[j] = {primitive, tile item, pair index, pass}: primitive-major order, so neighbouring
+// list[j] = {primitive, tx | ty << 16, pair index, pass}: primitive-major order, so neighbouring
 // positions mostly share a primitive (same shading path, state, spans and texels); without
 // it, pair position j is pair j in tile order.  Lane 0 copies the next position's record into
 // shared memory with cp.async while the warp shades the current one, so no global load chain
@@ -2999,6 +3001,21 @@ __device__ __noinline__ uint32_t queue_steal(uint32_t *queues, uint32_t nq, uint
 		atomicOr(&used[q >> 5], 1u << (q & 31));
 	}
 	return 0xffffffffu;
+}
+
+// Tile coordinates of a position's record: primitive-major records (k_expand) carry them packed
+// as tx | ty << 16, tile-order pair entries carry the tile item.
+__device__ __forceinline__ void record_tile(const RdpPass &ps, uint32_t y, bool packed, int &tx, int &ty)
+{
+	if (packed)
+	{
+		tx = int(y & 0xffffu);
+		ty = int(y >> 16);
+		return;
+	}
+	const uint32_t tl = y - ps.tile_item_begin;
+	tx = int(tl % ps.tiles_x);
+	ty = int(tl / ps.tiles_x);
 }
 
 // Compiled for several minimum residencies (register budgets); the executor's autotuner
@@ -3074,8 +3091,8 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass
 			s_pos[buf ^ 1] = np;
 		}
 		const RdpPass &ps = passes[list ? rec.w : shade[prim].pass];
-		const uint32_t tl = item - ps.tile_item_begin;
-		const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
+		int tx, ty;
+		record_tile(ps, item, list != nullptr, tx, ty);
 		const RdpPrimGeom &g = geom[prim];
 		const int x = tx * 8 + (lane & 7), y = ty * 8 + half * 4 + (lane >> 3);
 		Shaded out;
@@ -3178,8 +3195,8 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 			s_pos[buf ^ 1] = nj;
 		}
 		const RdpPass &ps = passes[list ? rec.w : shade[prim].pass];
-		const uint32_t tl = item - ps.tile_item_begin;
-		const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
+		int tx, ty;
+		record_tile(ps, item, list != nullptr, tx, ty);
 		const RdpPrimGeom &g = geom[prim];
 		const int fbw = int(ps.fb_width), fbh = int(ps.fb_height), ylo = g.span_ylo, yhi = g.span_yhi;
 		// Row y of the primitive is rows[y - ylo].

@@ -54,7 +54,7 @@ typedef struct RdpLaunch
 	uint32_t num_shade_queues;      /* the SM count */
 	uint32_t shade_queue_min;       /* launches with fewer pairs per k_shade CTA take the fixed stride */
 	uint4 *shade_list;              /* optional [pair_capacity]: primitive-major shading order, one
-	                                   {primitive, tile item, pair index, pass} record per position */
+	                                   {primitive, tx | ty << 16, pair index, pass} record per position */
 	uint32_t *prim_pairs;           /* [num_prims] pair count per primitive (with shade_list) */
 	uint32_t *prim_offsets;         /* [num_prims] first primitive-major position (with shade_list) */
 	uint32_t *prim_scan_blocks;     /* [2 * ceil(num_prims / 1024)] (with shade_list) */

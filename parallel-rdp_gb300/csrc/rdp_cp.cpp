@@ -2215,7 +2215,7 @@ int rdp_serve_run(rdp_batch *b, rdp_cp *const *instances, uint32_t num_instances
 	auto footprint = [](const rdp_serve_request &q) -> uint64_t {
 		if (q.footprint_bytes) return q.footprint_bytes;
 		uint64_t prims = q.num_words / 20 + 1;
-		return prims * (336 + 8 * 648 + 24 * RDP_SPAN_ROW_BYTES) + uint64_t(q.num_words) * 4;
+		return prims * (336 + 8 * 520 + 24 * RDP_SPAN_ROW_BYTES) + uint64_t(q.num_words) * 4;
 	};
 	struct Flight
 	{

@@ -278,9 +278,7 @@ struct Executor
 	void *d_spans = nullptr;         // span rows written by k_bin
 	uint4 *d_shade_list = nullptr; // primitive-major shading records
 	uint2 *d_pairs = nullptr;
-	uint32_t *d_sc_color = nullptr;
-	int *d_sc_zdith = nullptr;
-	uint16_t *d_sc_misc = nullptr;
+	uint2 *d_scratch = nullptr; // shaded records, 64 per pair
 	uint8_t *d_staging = nullptr;
 
 	// Pinned host staging buffers, used round-robin; a buffer is reused once the H2D copy
@@ -540,9 +538,7 @@ struct Executor
 		cudaFree(d_spans);
 		cudaFree(d_shade_list);
 		cudaFree(d_pairs);
-		cudaFree(d_sc_color);
-		cudaFree(d_sc_zdith);
-		cudaFree(d_sc_misc);
+		cudaFree(d_scratch);
 		cudaFree(d_staging);
 		d_geom = nullptr;
 		d_attr = nullptr;
@@ -553,9 +549,7 @@ struct Executor
 		d_spans = nullptr;
 		d_shade_list = nullptr;
 		d_pairs = nullptr;
-		d_sc_color = nullptr;
-		d_sc_zdith = nullptr;
-		d_sc_misc = nullptr;
+		d_scratch = nullptr;
 		d_staging = nullptr;
 	}
 
@@ -648,17 +642,12 @@ struct Executor
 			uint32_t n = std::max(need.pairs, caps.pairs * 2);
 			cudaFree(d_pairs);
 			cudaFree(d_shade_list);
-			cudaFree(d_sc_color);
-			cudaFree(d_sc_zdith);
-			cudaFree(d_sc_misc);
+			cudaFree(d_scratch);
 			d_pairs = nullptr;
 			d_shade_list = nullptr;
-			d_sc_color = nullptr;
-			d_sc_zdith = nullptr;
-			d_sc_misc = nullptr;
+			d_scratch = nullptr;
 			if (check(cudaMalloc(&d_pairs, size_t(n) * sizeof(uint2))) || check(cudaMalloc(&d_shade_list, size_t(n) * sizeof(uint4))) ||
-			    check(cudaMalloc(&d_sc_color, size_t(n) * 64 * 4)) || check(cudaMalloc(&d_sc_zdith, size_t(n) * 64 * 4)) ||
-			    check(cudaMalloc(&d_sc_misc, size_t(n) * 64 * 2)))
+			    check(cudaMalloc(&d_scratch, size_t(n) * 64 * sizeof(uint2))))
 				return false;
 			caps.pairs = n;
 		}
@@ -880,9 +869,7 @@ struct Executor
 		L.span_capacity = caps.span_rows;
 		L.prim_rows = d_prim_rows;
 		L.num_sms = num_queues;
-		L.sc_color = d_sc_color;
-		L.sc_zdith = d_sc_zdith;
-		L.sc_misc = d_sc_misc;
+		L.scratch = d_scratch;
 		L.num_tile_items = tile_base;
 		L.tile_cycles = record_cycles ? d_tile_cycles : nullptr;
 		L.tile_order = nullptr;

@@ -2030,6 +2030,24 @@ __device__ __forceinline__ void write_color(uint32_t fmt, Pix &px, int r, int g,
 }
 
 // ---------------------------------------------------------------------------- per pixel: shade + blend
+// RGB dither value of a pixel (dither.h:39-58): a cell of the magic-square or Bayer matrix
+// replicated over the three channels, the low 9 bits of the pixel's noise, or none.
+__device__ __forceinline__ int rgb_dither_value(uint32_t static_flags, uint32_t dither, int x, int y, uint32_t noise)
+{
+	const int yy = y >> int((static_flags & RS_INTERLACE_FIELD) != 0);
+	const int mr = int(dither >> 2), cell = (yy & 3) * 4 + (x & 3);
+	if (mr < 2) return g_dither[mr][cell] * (1 | 8 | 64);
+	if (mr == 2) return int(noise & 0x1ffu);
+	return 0;
+}
+
+// Shaded record of one pixel in the shading scratch (8 bytes): x = combined RGBA; y = z (18
+// bits; the copy pipe's texel word, 16 bits) | code << 18 | shade alpha << 22, code = coverage
+// 0-8, SC_COPY, SC_FILL or SC_NONE (not written).  The RGB dither bits are not stored: k_blend
+// recomputes them from the pixel and the primitive (rgb_dither_value).
+constexpr uint32_t SC_COPY = 9, SC_FILL = 10, SC_NONE = 15;
+constexpr uint2 kScratchEmpty = { 0u, 0xffffffffu };
+
 struct PassConst
 {
 	int fb_size, dx_mask, dx_shift;
@@ -2257,14 +2275,12 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	}
 
 	// ---- dither coefficients (dither.h:39-68)
-	int rgb_d, alpha_d;
+	const int rgb_d = rgb_dither_value(f, sh.dither, x, y, noise);
+	int alpha_d;
 	{
 		int yy = y >> int((f & RS_INTERLACE_FIELD) != 0);
 		int mr = int(sh.dither >> 2), ma = int(sh.dither & 3);
 		int cell = (yy & 3) * 4 + (x & 3);
-		if (mr < 2) rgb_d = g_dither[mr][cell] * (1 | 8 | 64);
-		else if (mr == 2) rgb_d = int(noise & 0x1ffu);
-		else rgb_d = 0;
 		if (ma == 3) alpha_d = 0;
 		else if (ma == 2) alpha_d = int(noise & 7u);
 		else
@@ -2360,6 +2376,15 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 
 // The framebuffer half: fill pipe, copy pipe or depth test + blender + dither + coverage
 // (memory_interfacing.h:381-571).  Returns whether the pixel was written.
+__device__ __forceinline__ uint2 pack_shaded(const Shaded &o)
+{
+	uint32_t y;
+	if (o.coverage & 0x40) y = SC_FILL << 18;
+	else if (o.coverage & 0x20) y = (uint32_t(o.z_dith) & 0xffffu) | (SC_COPY << 18);
+	else y = (uint32_t(o.z_dith) >> 9) | (uint32_t(o.coverage) << 18) | (uint32_t(o.shade_alpha) << 22);
+	return make_uint2(o.combined, y);
+}
+
 __device__ bool blend_pixel(const RdpPass &ps, const PassConst &pc, const RdpPrimShade &sh, const Shaded &in, Pix &px)
 {
 	if (in.coverage & 0x40)
@@ -3033,8 +3058,7 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass
                                                         const RdpPrimAttr *__restrict__ attr,
                                                         const RdpPrimShade *__restrict__ shade,
                                                         const RdpTile *__restrict__ tilesets,
-                                                        uint32_t *__restrict__ sc_color, int *__restrict__ sc_zdith,
-                                                        uint16_t *__restrict__ sc_misc, const uint4 *__restrict__ list,
+                                                        uint2 *__restrict__ sc, const uint4 *__restrict__ list,
                                                         uint32_t *__restrict__ queues, uint32_t num_queues,
                                                         uint32_t queue_min, const SpanRow *__restrict__ spans,
                                                         const uint32_t *__restrict__ prim_rows)
@@ -3116,10 +3140,7 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass
 		}
 		// All 64 pixels of the scratch are written (full sectors, no partial-sector
 		// read-modify-write in L2); k_blend skips pixels whose misc word says "not written".
-		const size_t at = size_t(pr) * SHADE_THREADS + size_t(half) * 32 + size_t(lane);
-		sc_color[at] = ok ? out.combined : 0u;
-		sc_zdith[at] = ok ? out.z_dith : 0;
-		sc_misc[at] = ok ? uint16_t((out.coverage & 0xff) | (out.shade_alpha << 8)) : uint16_t(0x00ffu);
+		sc[size_t(pr) * SHADE_THREADS + size_t(half) * 32 + size_t(lane)] = ok ? pack_shaded(out) : kScratchEmpty;
 		if (lane == 0) cp_async_wait_all();
 		__syncwarp();
 		buf ^= 1;
@@ -3138,9 +3159,9 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 	k_shade_packed(const RdpPass *__restrict__ passes, uint32_t num_passes, const uint2 *__restrict__ pairs,
 	               const uint32_t *__restrict__ ctrl, const RdpPrimGeom *__restrict__ geom,
 	               const RdpPrimAttr *__restrict__ attr, const RdpPrimShade *__restrict__ shade,
-	               const RdpTile *__restrict__ tilesets, uint32_t *__restrict__ sc_color, int *__restrict__ sc_zdith,
-	               uint16_t *__restrict__ sc_misc, const uint4 *__restrict__ list, uint32_t *__restrict__ queues,
-	               uint32_t num_queues, uint32_t queue_min, const SpanRow *__restrict__ spans,
+	               const RdpTile *__restrict__ tilesets, uint2 *__restrict__ sc, const uint4 *__restrict__ list,
+	               uint32_t *__restrict__ queues, uint32_t num_queues, uint32_t queue_min,
+	               const SpanRow *__restrict__ spans,
 	               const uint32_t *__restrict__ prim_rows)
 {
 	constexpr int WARPS = SHADE_THREADS / 32;
@@ -3221,18 +3242,8 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 		if (c1) s_px[n0 + __popc(m1 & below)] = uint8_t(lane + 32);
 		const size_t base = size_t(pr) * SHADE_THREADS;
 		// Every pixel of the scratch is written (full sectors); k_blend skips "not written".
-		if (!c0)
-		{
-			sc_color[base + lane] = 0u;
-			sc_zdith[base + lane] = 0;
-			sc_misc[base + lane] = 0x00ffu;
-		}
-		if (!c1)
-		{
-			sc_color[base + 32 + lane] = 0u;
-			sc_zdith[base + 32 + lane] = 0;
-			sc_misc[base + 32 + lane] = 0x00ffu;
-		}
+		if (!c0) sc[base + lane] = kScratchEmpty;
+		if (!c1) sc[base + 32 + lane] = kScratchEmpty;
 		__syncwarp();
 		if (count)
 		{
@@ -3255,9 +3266,7 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 				const bool ok = shade_pixel(pc, g, attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
 				                            ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, sp[0], sp[1],
 				                            tx * 8 + (px & 7), y, out);
-				sc_color[base + px] = ok ? out.combined : 0u;
-				sc_zdith[base + px] = ok ? out.z_dith : 0;
-				sc_misc[base + px] = ok ? uint16_t((out.coverage & 0xff) | (out.shade_alpha << 8)) : uint16_t(0x00ffu);
+				sc[base + px] = ok ? pack_shaded(out) : kScratchEmpty;
 			}
 		}
 		if (lane == 0) cp_async_wait_all();
@@ -3272,8 +3281,7 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 // applied in primitive order (the reference's depth_blend.comp), then written back.
 __device__ __forceinline__ void blend_tile(uint32_t item, const RdpPass *__restrict__ passes, uint32_t num_passes,
                                            const uint32_t *__restrict__ offsets, const uint2 *__restrict__ pairs,
-                                           const RdpPrimShade *__restrict__ shade, const uint32_t *__restrict__ sc_color,
-                                           const int *__restrict__ sc_zdith, const uint16_t *__restrict__ sc_misc,
+                                           const RdpPrimShade *__restrict__ shade, const uint2 *__restrict__ sc,
                                            uint32_t *__restrict__ cycles)
 {
 	const uint32_t p0 = offsets[item], p1 = offsets[item + 1];
@@ -3316,58 +3324,65 @@ __device__ __forceinline__ void blend_tile(uint32_t item, const RdpPass *__restr
 	if (inside)
 	{
 		load_pixel(ps, px, ci, di);
-		// Software pipeline: the scratch words and primitive of pair pr + BLEND_AHEAD are loaded
-		// (and its shading record prefetched into L1) while pair pr blends.
+		// Software pipeline: the shaded record and primitive of pair pr + BLEND_AHEAD are loaded
+		// (and its primitive's shading state prefetched into L1) while pair pr blends.
 		constexpr int BLEND_AHEAD = 2;
-		uint32_t q_misc[BLEND_AHEAD], q_color[BLEND_AHEAD], q_prim[BLEND_AHEAD];
-		int q_zd[BLEND_AHEAD];
+		uint2 q_rec[BLEND_AHEAD];
+		uint32_t q_prim[BLEND_AHEAD];
 #pragma unroll
 		for (int k = 0; k < BLEND_AHEAD; k++)
 		{
 			const uint32_t pr = p0 + uint32_t(k);
-			q_misc[k] = 0xffu;
-			q_color[k] = 0u;
-			q_zd[k] = 0;
+			q_rec[k] = kScratchEmpty;
 			q_prim[k] = 0u;
 			if (pr < p1)
 			{
-				const size_t at = size_t(pr) * SHADE_THREADS + tid;
-				q_misc[k] = sc_misc[at];
-				q_color[k] = sc_color[at];
-				q_zd[k] = sc_zdith[at];
+				q_rec[k] = sc[size_t(pr) * SHADE_THREADS + tid];
 				q_prim[k] = pairs[pr].x;
 				asm volatile("prefetch.global.L1 [%0];" ::"l"(shade + q_prim[k]));
 			}
 		}
 		for (uint32_t pr = p0; pr < p1; pr++)
 		{
-			const uint32_t misc = q_misc[0], color = q_color[0], prim = q_prim[0];
-			const int zd = q_zd[0];
+			const uint2 rec = q_rec[0];
+			const uint32_t prim = q_prim[0];
 #pragma unroll
 			for (int k = 0; k + 1 < BLEND_AHEAD; k++)
 			{
-				q_misc[k] = q_misc[k + 1];
-				q_color[k] = q_color[k + 1];
-				q_zd[k] = q_zd[k + 1];
+				q_rec[k] = q_rec[k + 1];
 				q_prim[k] = q_prim[k + 1];
 			}
 			const uint32_t nx = pr + BLEND_AHEAD;
 			if (nx < p1)
 			{
-				const size_t at = size_t(nx) * SHADE_THREADS + tid;
-				q_misc[BLEND_AHEAD - 1] = sc_misc[at];
-				q_color[BLEND_AHEAD - 1] = sc_color[at];
-				q_zd[BLEND_AHEAD - 1] = sc_zdith[at];
+				q_rec[BLEND_AHEAD - 1] = sc[size_t(nx) * SHADE_THREADS + tid];
 				q_prim[BLEND_AHEAD - 1] = pairs[nx].x;
 				asm volatile("prefetch.global.L1 [%0];" ::"l"(shade + q_prim[BLEND_AHEAD - 1]));
 			}
-			if ((misc & 0xff) == 0xff) continue;
+			const uint32_t code = (rec.y >> 18) & 15u;
+			if (code == SC_NONE) continue;
+			const RdpPrimShade &sh = shade[prim];
 			Shaded in;
-			in.coverage = int(misc & 0xff);
-			in.shade_alpha = int(misc >> 8);
-			in.combined = color;
-			in.z_dith = zd;
-			frags += blend_pixel(ps, pc, shade[prim], in, px);
+			in.combined = rec.x;
+			in.shade_alpha = 0;
+			if (code == SC_FILL)
+			{
+				in.coverage = 0x40;
+				in.z_dith = 0;
+			}
+			else if (code == SC_COPY)
+			{
+				in.coverage = 0x20;
+				in.z_dith = int(rec.y & 0xffffu);
+			}
+			else
+			{
+				in.coverage = int(code);
+				in.shade_alpha = int(rec.y >> 22);
+				const uint32_t noise = (sh.static_flags & RS_NEED_NOISE) ? reseed_noise(uint32_t(x), uint32_t(y), sh.prim_index) : 0u;
+				in.z_dith = int((rec.y & 0x3ffffu) << 9) | rgb_dither_value(sh.static_flags, sh.dither, x, y, noise);
+			}
+			frags += blend_pixel(ps, pc, sh, in, px);
 		}
 		store_pixel(ps, px, ci, di, pc.alias);
 	}
@@ -3399,9 +3414,7 @@ __global__ void __launch_bounds__(SHADE_THREADS) k_blend(const RdpPass *__restri
                                                         const uint2 *__restrict__ pairs, uint32_t *__restrict__ ctrl,
                                                         const uint32_t *__restrict__ nonempty,
                                                         const RdpPrimShade *__restrict__ shade,
-                                                        const uint32_t *__restrict__ sc_color,
-                                                        const int *__restrict__ sc_zdith,
-                                                        const uint16_t *__restrict__ sc_misc,
+                                                        const uint2 *__restrict__ sc,
                                                         const uint32_t *__restrict__ order,
                                                         uint32_t *__restrict__ cycles)
 {
@@ -3416,7 +3429,7 @@ __global__ void __launch_bounds__(SHADE_THREADS) k_blend(const RdpPass *__restri
 		__syncthreads();
 		if (k >= n) break;
 		const uint32_t item = order ? order[k] : nonempty[k];
-		blend_tile(item, passes, num_passes, offsets, pairs, shade, sc_color, sc_zdith, sc_misc, cycles);
+		blend_tile(item, passes, num_passes, offsets, pairs, shade, sc, cycles);
 	}
 }
 
@@ -3573,8 +3586,8 @@ extern "C" cudaError_t rdp_kernels_init_luts(const uint8_t *blender_lut)
 
 namespace {
 typedef void (*ShadeKernel)(const RdpPass *, uint32_t, const uint2 *, const uint32_t *, const RdpPrimGeom *,
-                            const RdpPrimAttr *, const RdpPrimShade *, const RdpTile *, uint32_t *, int *, uint16_t *,
-                            const uint4 *, uint32_t *, uint32_t, uint32_t, const rdp::SpanRow *, const uint32_t *);
+                            const RdpPrimAttr *, const RdpPrimShade *, const RdpTile *, uint2 *, const uint4 *,
+                            uint32_t *, uint32_t, uint32_t, const rdp::SpanRow *, const uint32_t *);
 const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = {
 	rdp::k_shade<16>,        rdp::k_shade<18>,        rdp::k_shade<20>,        rdp::k_shade<24>,
 	rdp::k_shade_packed<16>, rdp::k_shade_packed<18>, rdp::k_shade_packed<20>, rdp::k_shade_packed<24>
@@ -3695,8 +3708,8 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		const uint32_t sv = L->shade_variant < RDP_SHADE_VARIANTS ? L->shade_variant : 0;
 		const ShadeKernel shade_kernel = kShadeVariants[sv];
 		shade_kernel<<<L->shade_ctas, rdp::SHADE_THREADS, 0, stream>>>(
-			L->passes, L->num_passes, L->pairs, L->ctrl, L->geom, L->attr, L->shade, L->tilesets, L->sc_color,
-			L->sc_zdith, L->sc_misc, L->shade_list, L->shade_queues, L->num_shade_queues, L->shade_queue_min,
+			L->passes, L->num_passes, L->pairs, L->ctrl, L->geom, L->attr, L->shade, L->tilesets, L->scratch,
+			L->shade_list, L->shade_queues, L->num_shade_queues, L->shade_queue_min,
 			static_cast<const rdp::SpanRow *>(L->spans), L->prim_rows);
 		if (L->shade_events[1]) cudaEventRecordWithFlags(L->shade_events[1], stream, ev_flags);
 		const uint32_t tile_ctas = std::min<uint32_t>(L->num_tile_items, L->blend_ctas);
@@ -3711,8 +3724,8 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		}
 		if (L->blend_events[0]) cudaEventRecordWithFlags(L->blend_events[0], stream, ev_flags);
 		rdp::k_blend<<<tile_ctas, rdp::SHADE_THREADS, 0, stream>>>(
-			L->passes, L->num_passes, L->pair_offsets, L->pairs, L->ctrl, L->nonempty_tiles, L->shade, L->sc_color,
-			L->sc_zdith, L->sc_misc, order, L->tile_cycles);
+			L->passes, L->num_passes, L->pair_offsets, L->pairs, L->ctrl, L->nonempty_tiles, L->shade, L->scratch,
+			order, L->tile_cycles);
 		if (L->blend_events[1]) cudaEventRecordWithFlags(L->blend_events[1], stream, ev_flags);
 		if (L->sched && L->sched->train_enabled && L->tile_cycles)
 		{

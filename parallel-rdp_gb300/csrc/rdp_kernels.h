@@ -67,9 +67,7 @@ typedef struct RdpLaunch
 	uint32_t span_capacity;
 	uint32_t *prim_rows;            /* [num_prims] first span row of each primitive */
 	uint32_t num_sms;               /* the device's SM count (sizes k_span's CTAs) */
-	uint32_t *sc_color;             /* [pair_capacity * 64] */
-	int *sc_zdith;
-	uint16_t *sc_misc;
+	uint2 *scratch;                 /* [pair_capacity * 64] shaded records, 8 bytes per pixel */
 } RdpLaunch;
 
 #ifdef __cplusplus

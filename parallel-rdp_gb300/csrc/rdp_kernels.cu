@@ -2306,40 +2306,37 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	}
 	in.lod_frac = lod_frac;
 	in.noise = int(((noise & 7u) << 6) | 0x20u);
-	if (f & RS_MULTI_CYCLE)
+	// Cycle 0 (2-cycle mode only), then cycle 1, through one inlined copy of the combiner.
+#pragma unroll 1
+	for (int cy = (f & RS_MULTI_CYCLE) ? 0 : 1; cy < 2; cy++)
 	{
-		in.cma = sh.c_muladd[0]; in.cms = sh.c_mulsub[0]; in.cmu = sh.c_mul[0]; in.cad = sh.c_add[0];
-		int c0[4];
-		combine(in, sh.comb_rgb[0], sh.comb_alpha[0], c0);
-		if (alpha_test)
+		in.cma = sh.c_muladd[cy]; in.cms = sh.c_mulsub[cy]; in.cmu = sh.c_mul[cy]; in.cad = sh.c_add[cy];
+		combine(in, sh.comb_rgb[cy], sh.comb_alpha[cy], combined);
+		if (cy == 0)
 		{
-			int ca = clamp_9bit(c0[3]);
-			int ea = ca + ((ca + 1) >> 8);
-			if (alpha_cvg_select) ea = cvg_times_alpha ? ((ea * cov_count + 4) >> 3) : (cov_count << 5);
-			else ea += alpha_d;
-			alpha_ref = clampi(ea, 0, 0xff);
-		}
+			if (alpha_test)
+			{
+				int ca = clamp_9bit(combined[3]);
+				int ea = ca + ((ca + 1) >> 8);
+				if (alpha_cvg_select) ea = cvg_times_alpha ? ((ea * cov_count + 4) >> 3) : (cov_count << 5);
+				else ea += alpha_d;
+				alpha_ref = clampi(ea, 0, 0xff);
+			}
 #pragma unroll
-		for (int c = 0; c < 4; c++)
-		{
-			in.comb[c] = c0[c];
-			int tmp = in.tex0[c];
-			in.tex0[c] = in.tex1[c];
-			in.tex1[c] = tmp;
+			for (int c = 0; c < 4; c++)
+			{
+				in.comb[c] = combined[c];
+				int tmp = in.tex0[c];
+				in.tex0[c] = in.tex1[c];
+				in.tex1[c] = tmp;
+			}
+			if (f & RS_NEED_NOISE_DUAL)
+			{
+				// The second seed also feeds the later alpha-test threshold (shading.h:309-347).
+				noise = reseed_noise(uint32_t(x + 1023), uint32_t(y + 7), sh.prim_index + 11);
+				in.noise = int(((noise & 7u) << 6) | 0x20u);
+			}
 		}
-		in.cma = sh.c_muladd[1]; in.cms = sh.c_mulsub[1]; in.cmu = sh.c_mul[1]; in.cad = sh.c_add[1];
-		if (f & RS_NEED_NOISE_DUAL)
-		{
-			// The second seed also feeds the later alpha-test threshold (shading.h:309-347).
-			noise = reseed_noise(uint32_t(x + 1023), uint32_t(y + 7), sh.prim_index + 11);
-			in.noise = int(((noise & 7u) << 6) | 0x20u);
-		}
-		combine(in, sh.comb_rgb[1], sh.comb_alpha[1], combined);
-	}
-	else
-	{
-		in.cma = sh.c_muladd[1]; in.cms = sh.c_mulsub[1]; in.cmu = sh.c_mul[1]; in.cad = sh.c_add[1];
-		combine(in, sh.comb_rgb[1], sh.comb_alpha[1], combined);
 	}
 	// combiner_cycle1 tail
 #pragma unroll
@@ -3408,8 +3405,10 @@ __device__ __forceinline__ void blend_tile(uint32_t item, const RdpPass *__restr
 }
 
 // Persistent CTAs take non-empty tiles from a shared counter, in the order of `order`
-// (longest predicted first) when given, else in tile order.
-__global__ void __launch_bounds__(SHADE_THREADS) k_blend(const RdpPass *__restrict__ passes, uint32_t num_passes,
+// (longest predicted first) when given, else in tile order.  Each pixel's pairs form a serial
+// dependency chain, so residency matters more than the few spills of a 40-register budget
+// (24 CTAs per SM measured 8 % faster than 16 with 64 registers, 32 CTAs slower).
+__global__ void __launch_bounds__(SHADE_THREADS, 24) k_blend(const RdpPass *__restrict__ passes, uint32_t num_passes,
                                                         const uint32_t *__restrict__ offsets,
                                                         const uint2 *__restrict__ pairs, uint32_t *__restrict__ ctrl,
                                                         const uint32_t *__restrict__ nonempty,

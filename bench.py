@@ -632,7 +632,10 @@ def _serving(args, device, model=None):
     b.idle()
     capacity_fps = len(insts) / (time.perf_counter() - t0)
     out = {"instances": len(insts), "hbm_budget_gb": args.serve_budget_gb, "capacity_fps_estimate": capacity_fps}
-    for tag, rate, dur in (("configured_rate", 20000.0, args.serve_window), ("sustainable", 0.5 * capacity_fps, 1.0)):
+    # The configured rate first; the sustainable rate is 80 % of what the serving loop delivered
+    # under that overload (its own capacity with Poisson-sized batches, below the full-batch one).
+    for tag, dur in (("configured_rate", args.serve_window), ("sustainable", 1.0)):
+        rate = 20000.0 if tag == "configured_rate" else 0.8 * out["configured_rate"]["throughput_fps"]
         trace = poisson_trace(len(insts), rate, dur, frames, seed=42)
         res, st = b.serve(insts, trace, hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)))
         lat = latency_summary(res["latency_s"])

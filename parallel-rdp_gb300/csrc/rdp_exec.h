@@ -279,7 +279,13 @@ struct Executor
 	uint4 *d_shade_list = nullptr; // primitive-major shading records
 	uint2 *d_pairs = nullptr;
 	uint2 *d_scratch = nullptr; // shaded records, 64 per pair
-	uint8_t *d_staging = nullptr;
+	uint8_t *d_staging = nullptr; // two slots of caps.staging bytes
+	// Launch inputs are copied on copy_stream into alternating device slots, so that the copy of
+	// the next launch overlaps this launch's kernels.  slot_copied[s] orders the kernels after the
+	// copy; slot_free[s] (recorded after the kernels that read slot s) orders the next copy into it.
+	cudaStream_t copy_stream = nullptr;
+	cudaEvent_t slot_copied[2] = {}, slot_free[2] = {};
+	int staging_slot = 0;
 
 	// Pinned host staging buffers, used round-robin; a buffer is reused once the H2D copy
 	// that read it has completed.  Up to kMaxStaging of them let the host record launches
@@ -443,8 +449,13 @@ struct Executor
 		if (const char *e = getenv("RDP_SHADE_PERM_MIN_PRIMS")) perm_min_prims = uint32_t(strtoul(e, nullptr, 10));
 		if (const char *e = getenv("RDP_SHADE_QUEUE_MIN")) queue_min = uint32_t(strtoul(e, nullptr, 10));
 		if (check(cudaMalloc(&d_ctrl, 32)) || check(cudaMalloc(&d_pair_log, 256 * 4)) ||
-		    check(cudaMalloc(&d_queues, queue_bytes())))
+		    check(cudaMalloc(&d_queues, queue_bytes())) ||
+		    check(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking)))
 			return false;
+		for (int k = 0; k < 2; k++)
+			if (check(cudaEventCreateWithFlags(&slot_copied[k], cudaEventDisableTiming)) ||
+			    check(cudaEventCreateWithFlags(&slot_free[k], cudaEventDisableTiming)))
+				return false;
 		return !check(cudaMemsetAsync(d_ctrl, 0, 32, stream)) && !check(cudaMemsetAsync(d_queues, 0, queue_bytes(), stream));
 	}
 
@@ -556,6 +567,7 @@ struct Executor
 	void destroy()
 	{
 		if (stream) cudaStreamSynchronize(stream);
+		if (copy_stream) cudaStreamSynchronize(copy_stream);
 		free_all();
 		sched_free();
 		cudaFree(d_ctrl);
@@ -564,6 +576,14 @@ struct Executor
 		d_ctrl = nullptr;
 		d_pair_log = nullptr;
 		d_queues = nullptr;
+		for (int k = 0; k < 2; k++)
+		{
+			if (slot_copied[k]) cudaEventDestroy(slot_copied[k]);
+			if (slot_free[k]) cudaEventDestroy(slot_free[k]);
+			slot_copied[k] = slot_free[k] = nullptr;
+		}
+		if (copy_stream) cudaStreamDestroy(copy_stream);
+		copy_stream = nullptr;
 		tuner.destroy();
 		for (auto &st : staging)
 		{
@@ -580,7 +600,8 @@ struct Executor
 		bool grow_passes = need.passes > caps.passes, grow_pairs = need.pairs > caps.pairs;
 		bool grow_staging = need.staging > caps.staging, grow_spans = need.span_rows > caps.span_rows;
 		if (!(grow_prims || grow_tiles || grow_passes || grow_pairs || grow_staging || grow_spans)) return true;
-		if (check(cudaStreamSynchronize(stream))) return false;
+		if (check(cudaStreamSynchronize(stream)) || (copy_stream && check(cudaStreamSynchronize(copy_stream))))
+			return false;
 		for (auto &st : staging) st.in_flight = false;
 		generation++;
 		if (grow_prims)
@@ -664,7 +685,7 @@ struct Executor
 			size_t n = std::max(need.staging, caps.staging + caps.staging / 2);
 			cudaFree(d_staging);
 			d_staging = nullptr;
-			if (check(cudaMalloc(&d_staging, n))) return false;
+			if (check(cudaMalloc(&d_staging, 2 * n))) return false;
 			caps.staging = n;
 		}
 		return !check(cudaStreamSynchronize(stream));
@@ -801,7 +822,8 @@ struct Executor
 			up_base += v[i].num_uploads;
 		}
 
-		uint8_t *dst = d_staging;
+		const int slot = staging_slot;
+		uint8_t *dst = d_staging + size_t(slot) * caps.staging;
 		if (cap)
 		{
 			if (check(cudaMalloc(&dst, off))) return false;
@@ -810,8 +832,12 @@ struct Executor
 		}
 		else
 		{
-			if (check(cudaMemcpyAsync(d_staging, h, off, cudaMemcpyHostToDevice, stream))) return false;
-			if (check(cudaEventRecord(st.done, stream))) return false;
+			staging_slot ^= 1;
+			if (check(cudaStreamWaitEvent(copy_stream, slot_free[slot], 0)) ||
+			    check(cudaMemcpyAsync(dst, h, off, cudaMemcpyHostToDevice, copy_stream)) ||
+			    check(cudaEventRecord(st.done, copy_stream)) || check(cudaEventRecord(slot_copied[slot], copy_stream)) ||
+			    check(cudaStreamWaitEvent(stream, slot_copied[slot], 0)))
+				return false;
 			st.in_flight = true;
 		}
 		staging_bytes += off;
@@ -899,7 +925,7 @@ struct Executor
 			L.shade_events[1] = sm.ev[1];
 			tuner.pending.push_back(sm);
 		}
-		if (check(rdp_kernels_launch(&L, stream))) return false;
+		if (check(rdp_kernels_launch(&L, stream)) || check(cudaEventRecord(slot_free[slot], stream))) return false;
 		kernel_launches += rdp_kernels_count(&L);
 		return true;
 	}

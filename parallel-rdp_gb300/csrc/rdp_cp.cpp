@@ -340,14 +340,15 @@ struct rdp_cp
 			c.passes = 1;
 			c.prims = RDP_MAX_PRIMS_PER_PASS;
 			c.tile_items = kMaxTiles;
-			c.pairs = 1u << 20;
-			c.span_rows = rdpx::kInitialSpanRows;
 			c.staging = rdpx::align16(sizeof(RdpPass)) + rdpx::align16(sizeof(RdpPrimIn) * RDP_MAX_PRIMS_PER_PASS) +
 			            rdpx::align16(sizeof(uint32_t) * kMaxWordsPerPass) +
 			            rdpx::align16(sizeof(uint32_t) * RDP_STATE_BLOCK_WORDS * kMaxStateBlocks) +
 			            rdpx::align16(sizeof(RdpTile) * 8 * kMaxTilesets) +
 			            rdpx::align16(sizeof(RdpUpload) * RDP_MAX_UPLOADS_PER_PASS) + 512;
-			if (!own_exec.init(device, stream) || !own_exec.ensure(c)) return RDP_ERR_OOM;
+			if (!own_exec.init(device, stream)) return RDP_ERR_OOM;
+			c.pairs = own_exec.initial_pairs;
+			c.span_rows = own_exec.initial_span_rows;
+			if (!own_exec.ensure(c)) return RDP_ERR_OOM;
 		}
 		if (check(cudaMemsetAsync(d_hidden, 0x03, hidden_size, stream))) return RDP_ERR_DEVICE;
 		if (check(cudaMemsetAsync(d_tmem, 0, 4096, stream))) return RDP_ERR_DEVICE;
@@ -1538,8 +1539,8 @@ bool rdp_batch::reserve_for_capture()
 		need.tile_items = std::max(need.tile_items, tiles);
 		need.staging = std::max(need.staging, rdpx::Executor::staging_bytes_for(views.data(), uint32_t(views.size())));
 	}
-	need.pairs = std::max(need.pairs, 1u << 20);
-	need.span_rows = std::max(need.span_rows, rdpx::kInitialSpanRows);
+	need.pairs = std::max(need.pairs, exec.initial_pairs);
+	need.span_rows = std::max(need.span_rows, exec.initial_span_rows);
 	return exec.ensure(need);
 }
 

@@ -264,6 +264,9 @@ struct Executor
 	// override them): primitive-major order for launches of at least perm_min_prims primitives,
 	// per-SM queues for launches of at least queue_min pairs per k_shade CTA.
 	uint32_t perm_min_prims = 16384, queue_min = 64;
+	// Pair-scratch and span-row capacities a new executor starts with (RDP_PAIR_CAPACITY and
+	// RDP_SPAN_ROW_CAPACITY override them; launches beyond them take the fused fallback).
+	uint32_t initial_pairs = 1u << 20, initial_span_rows = kInitialSpanRows;
 	uint32_t *d_queues = nullptr, num_queues = 0; // per-SM work queues of k_shade + used-up bitmask
 	size_t queue_bytes() const { return (size_t(num_queues) + (num_queues + 31) / 32) * 4; }
 
@@ -448,6 +451,9 @@ struct Executor
 		num_queues = uint32_t(sms);
 		if (const char *e = getenv("RDP_SHADE_PERM_MIN_PRIMS")) perm_min_prims = uint32_t(strtoul(e, nullptr, 10));
 		if (const char *e = getenv("RDP_SHADE_QUEUE_MIN")) queue_min = uint32_t(strtoul(e, nullptr, 10));
+		if (const char *e = getenv("RDP_PAIR_CAPACITY")) initial_pairs = std::max(1u, uint32_t(strtoul(e, nullptr, 10)));
+		if (const char *e = getenv("RDP_SPAN_ROW_CAPACITY"))
+			initial_span_rows = std::max(1u, uint32_t(strtoul(e, nullptr, 10)));
 		if (check(cudaMalloc(&d_ctrl, 32)) || check(cudaMalloc(&d_pair_log, 256 * 4)) ||
 		    check(cudaMalloc(&d_queues, queue_bytes())) ||
 		    check(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking)))
@@ -739,8 +745,8 @@ struct Executor
 		need.descs = std::max(need.descs, descs);
 		need.prims = std::max(need.prims, std::max(prims, 1u));
 		need.tile_items = std::max(need.tile_items, std::max(tiles, 1u));
-		need.pairs = std::max(need.pairs, 1u << 20);
-		need.span_rows = std::max(need.span_rows, kInitialSpanRows);
+		need.pairs = std::max(need.pairs, initial_pairs);
+		need.span_rows = std::max(need.span_rows, initial_span_rows);
 		need.staging = std::max(need.staging, staging_bytes_for(v, n));
 		if (!ensure(need)) return false;
 

@@ -1119,7 +1119,7 @@ __global__ void k_tmem_apply(const RdpPass *__restrict__ passes, const uint32_t 
 // (pass, 32 TMEM words); its TMEM_CARRY_WARPS warps split the uploads into chunks: each
 // warp finds the last value its chunk writes, the chunks' carry-ins are chained in shared
 // memory, then every warp fills its chunk -- 2 * uploads / warps dependent steps per word.
-constexpr int TMEM_CARRY_WARPS = 16;
+constexpr int TMEM_CARRY_WARPS = 32; // 8: +0.19 ms per batched sync point, 16: +0.05 ms
 
 __global__ void __launch_bounds__(TMEM_CARRY_WARPS * 32) k_tmem_carry(const RdpPass *__restrict__ passes,
                                                                        const uint32_t *__restrict__ pass_list,

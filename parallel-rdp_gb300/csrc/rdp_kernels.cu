@@ -3273,6 +3273,168 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 	}
 }
 
+// Packed shading over two pairs at a time: a warp takes two positions per step (consecutive ones,
+// so mostly two tiles of one primitive in primitive-major order), picks both pairs' candidate
+// pixels and shades them together in as few 32-lane rounds as they fill -- two pairs with few
+// covered pixels share one round.  Per-pair data sits in shared memory for the shading rounds.
+// Same work order, scratch and results as k_shade_packed.
+template <int MIN_CTAS>
+__global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
+	k_shade_packed2(const RdpPass *__restrict__ passes, uint32_t num_passes, const uint2 *__restrict__ pairs,
+	                const uint32_t *__restrict__ ctrl, const RdpPrimGeom *__restrict__ geom,
+	                const RdpPrimAttr *__restrict__ attr, const RdpPrimShade *__restrict__ shade,
+	                const RdpTile *__restrict__ tilesets, uint2 *__restrict__ sc, const uint4 *__restrict__ list,
+	                uint32_t *__restrict__ queues, uint32_t num_queues, uint32_t queue_min,
+	                const SpanRow *__restrict__ spans, const uint32_t *__restrict__ prim_rows)
+{
+	constexpr int WARPS = SHADE_THREADS / 32;
+	constexpr uint32_t NONE = 0xffffffffu;
+	struct Slot
+	{
+		uint32_t prim, pass, pr;
+		int tx, ty, ylo;
+		const SpanRow *rows;
+	};
+	__shared__ __align__(16) uint4 s_rec_all[WARPS][2][2]; // [buffer][slot]: the positions' records
+	__shared__ uint32_t s_pos_all[WARPS][2][2];             // [buffer][slot]: positions (NONE: no pair)
+	__shared__ Slot s_slot_all[WARPS][2];
+	__shared__ uint8_t s_px_all[WARPS][128];                // candidates: slot << 6 | pixel, in order
+	if (ctrl[1]) return;
+	const uint32_t total = ctrl[0];
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	uint4(*s_rec)[2] = s_rec_all[wid];
+	uint32_t(*s_pos)[2] = s_pos_all[wid];
+	Slot *s_slot = s_slot_all[wid];
+	uint8_t *s_px = s_px_all[wid];
+	const uint32_t worker = blockIdx.x * WARPS + uint32_t(wid), workers = gridDim.x * WARPS;
+	if (total < gridDim.x * queue_min) queues = nullptr;
+	uint32_t q = 0, k_next = 0;
+	int buf = 0;
+	// Lane 0: the next step's two positions into s_pos[b] and their records into s_rec[b].
+	// With queues a take reserves two consecutive slots of the SM's queue; a take after stealing
+	// reserves one.
+	auto take = [&](int b, bool first) {
+		uint32_t pa, pb = NONE;
+		if (queues)
+		{
+			if (first)
+			{
+				q = sm_id() % num_queues;
+				k_next = atomicAdd(&queues[q], 2u);
+			}
+			pa = queue_pos(q, k_next, num_queues);
+			if (pa < total)
+			{
+				pb = queue_pos(q, k_next + 1, num_queues);
+				if (pb >= total) pb = NONE;
+			}
+			else
+				pa = queue_steal(queues, num_queues, total, q);
+			if (pa < total) k_next = atomicAdd(&queues[q], 2u);
+		}
+		else
+		{
+			pa = first ? 2u * worker : s_pos[b ^ 1][0] + 2u * workers;
+			pb = pa + 1 < total ? pa + 1 : NONE;
+		}
+		if (pa >= total) pa = pb = NONE;
+		if (pa != NONE)
+		{
+			if (list) cp_async16(&s_rec[b][0], list + pa);
+			else cp_async8(&s_rec[b][0], pairs + pa);
+		}
+		if (pb != NONE)
+		{
+			if (list) cp_async16(&s_rec[b][1], list + pb);
+			else cp_async8(&s_rec[b][1], pairs + pb);
+		}
+		s_pos[b][0] = pa;
+		s_pos[b][1] = pb;
+	};
+	if (lane == 0)
+	{
+		take(0, true);
+		cp_async_wait_all();
+	}
+	__syncwarp();
+	const unsigned below = (1u << lane) - 1u;
+	while (s_pos[buf][0] != NONE)
+	{
+		const uint32_t pa = s_pos[buf][0], pb = s_pos[buf][1];
+		const uint4 rec_a = s_rec[buf][0], rec_b = s_rec[buf][1];
+		__syncwarp();
+		if (lane == 0) take(buf ^ 1, false);
+		// Candidates of both pairs: pixels lane (rows 0-3) and lane + 32 (rows 4-7) of each.
+		int count = 0;
+#pragma unroll
+		for (int s = 0; s < 2; s++)
+		{
+			const uint32_t pos = s ? pb : pa;
+			if (pos == NONE) break;
+			const uint4 rec = s ? rec_b : rec_a;
+			const uint32_t prim = rec.x, pi = list ? rec.w : shade[prim].pass;
+			const RdpPass &ps = passes[pi];
+			int tx, ty;
+			record_tile(ps, rec.y, list != nullptr, tx, ty);
+			const RdpPrimGeom &g = geom[prim];
+			const int fbw = int(ps.fb_width), fbh = int(ps.fb_height), ylo = g.span_ylo, yhi = g.span_yhi;
+			const SpanRow *rows = spans + prim_rows[prim];
+			const int x = tx * 8 + (lane & 7), y0 = ty * 8 + (lane >> 3), y1 = y0 + 4;
+			bool c0 = x < fbw && y0 < fbh && y0 >= ylo && y0 <= yhi;
+			bool c1 = x < fbw && y1 < fbh && y1 >= ylo && y1 <= yhi;
+			if (c0)
+			{
+				const SpanRow &r = rows[y0 - ylo];
+				c0 = r.valid && x >= r.start_x && x <= r.end_x;
+			}
+			if (c1)
+			{
+				const SpanRow &r = rows[y1 - ylo];
+				c1 = r.valid && x >= r.start_x && x <= r.end_x;
+			}
+			const unsigned m0 = __ballot_sync(0xffffffffu, c0), m1 = __ballot_sync(0xffffffffu, c1);
+			const int n0 = __popc(m0);
+			if (c0) s_px[count + __popc(m0 & below)] = uint8_t((s << 6) | lane);
+			if (c1) s_px[count + n0 + __popc(m1 & below)] = uint8_t((s << 6) | (lane + 32));
+			count += n0 + __popc(m1);
+			const uint32_t pr = list ? rec.z : pos;
+			const size_t base = size_t(pr) * SHADE_THREADS;
+			if (!c0) sc[base + lane] = kScratchEmpty;
+			if (!c1) sc[base + 32 + lane] = kScratchEmpty;
+			if (lane == 0) s_slot[s] = Slot{ prim, pi, pr, tx, ty, ylo, rows };
+		}
+		__syncwarp();
+		for (int e = lane; e < count; e += 32)
+		{
+			const int ent = s_px[e], px = ent & 63;
+			const Slot &sl = s_slot[ent >> 6];
+			const RdpPass &ps = passes[sl.pass];
+			PassConst pc;
+			switch (ps.fb_fmt)
+			{
+			case FBF_I4: pc.fb_size = 0; pc.dx_mask = 0; pc.dx_shift = 0; break;
+			case FBF_I8: pc.fb_size = 1; pc.dx_mask = ~7; pc.dx_shift = 3; break;
+			case FBF_RGBA5551:
+			case FBF_IA88: pc.fb_size = 2; pc.dx_mask = ~3; pc.dx_shift = 2; break;
+			default: pc.fb_size = 4; pc.dx_mask = ~1; pc.dx_shift = 1; break;
+			}
+			pc.alias = ps.fb_addr == ps.depth_addr;
+			const uint32_t prim = sl.prim;
+			const RdpPrimShade &sh = shade[prim];
+			const int y = sl.ty * 8 + (px >> 3);
+			const SpanRow *sp = sl.rows + (y - sl.ylo);
+			Shaded out;
+			const bool ok = shade_pixel(pc, geom[prim], attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
+			                            ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, sp[0], sp[1],
+			                            sl.tx * 8 + (px & 7), y, out);
+			sc[size_t(sl.pr) * SHADE_THREADS + px] = ok ? pack_shaded(out) : kScratchEmpty;
+		}
+		if (lane == 0) cp_async_wait_all();
+		__syncwarp();
+		buf ^= 1;
+	}
+}
+
 // ============================================================================ k_blend
 // One 64-thread CTA per tile: the tile's colour/depth stay in registers while its pairs are
 // applied in primitive order (the reference's depth_blend.comp), then written back.
@@ -3588,8 +3750,8 @@ typedef void (*ShadeKernel)(const RdpPass *, uint32_t, const uint2 *, const uint
                             const RdpPrimAttr *, const RdpPrimShade *, const RdpTile *, uint2 *, const uint4 *,
                             uint32_t *, uint32_t, uint32_t, const rdp::SpanRow *, const uint32_t *);
 const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = {
-	rdp::k_shade<16>,        rdp::k_shade<18>,        rdp::k_shade<20>,        rdp::k_shade<24>,
-	rdp::k_shade_packed<16>, rdp::k_shade_packed<18>, rdp::k_shade_packed<20>, rdp::k_shade_packed<24>
+	rdp::k_shade<18>,         rdp::k_shade<20>,         rdp::k_shade_packed2<18>, rdp::k_shade_packed2<20>,
+	rdp::k_shade_packed<16>,  rdp::k_shade_packed<18>,  rdp::k_shade_packed<20>,  rdp::k_shade_packed<24>
 };
 } // namespace
 

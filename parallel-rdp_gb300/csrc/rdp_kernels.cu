@@ -12,8 +12,8 @@
  *   k_tmem_*     : TMEM uploads (shaders/tmem_update.comp), one snapshot per upload.
  *   k_scan_*     : pair offsets per tile (and per primitive), control words.
  *   k_expand     : the (primitive, tile) pair list, in primitive order per tile.
- *   k_shade      : per-pixel shading of every pair (shaders/shading.h) into scratch,
- *                  one warp per half pair, pairs in parallel.
+ *   k_shade_*    : per-pixel shading of every pair (shaders/shading.h) into scratch,
+ *                  pairs in parallel, the pixels a pair can cover packed into warps.
  *   k_blend      : per tile, the pairs' shaded pixels in primitive order through
  *                  depth test, blender, dither and coverage against the tile's
  *                  colour/depth held in registers (shaders/memory_interfacing.h,
@@ -2947,12 +2947,12 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 
 // ============================================================================ k_shade
 // Shading of every (tile, primitive) pair in parallel (the reference's rasterizer.comp): one
-// warp per half pair at a time, one pixel per lane; two independent warps per CTA.  Results go
-// to scratch as structure-of-arrays per pair: combined colour, z | dither, coverage | shade
-// alpha << 8.
+// pair (k_shade_packed) or a few pairs (k_shade_packedn) per warp step, the pixels that can be
+// covered packed one per lane; two independent warps per CTA.  Results go to scratch as one
+// 8-byte shaded record per pixel (pack_shaded).
 constexpr int SHADE_THREADS = 64;
 
-// Work distribution over positions (half pairs).  Without queues, warp w of the grid shades
+// Work distribution over positions (pairs).  Without queues, warp w of the grid shades
 // positions w, w + warps, w + 2 warps, ...  With queues (one counter per SM, then a bitmask of
 // used-up queues; zeroed by k_scan), positions are dealt in chunks of SHADE_CHUNK: queue q owns
 // chunks q, q + nq, q + 2 nq, ..., and a warp takes positions from the queue of the SM it runs
@@ -3040,117 +3040,14 @@ __device__ __forceinline__ void record_tile(const RdpPass &ps, uint32_t y, bool 
 	ty = int(tl / ps.tiles_x);
 }
 
-// Compiled for several minimum residencies (register budgets); the executor's autotuner
-// picks one.  More resident CTAs hide more latency at the price of some spilling.
-//
-// Work unit: half a pair (rows 0-3 or 4-7 of the tile, one pixel per lane), position p =
-// 2 x pair position + half.  Each warp takes positions on its own (no CTA barrier: a warp whose
-// rows the primitive misses moves on at once), reads the rows' spans that k_bin computed once
-// per primitive (row y of primitive i is spans[prim_rows[i] + y - span_ylo]), shades, and
-// writes its 32 pixels of the pair's scratch.
-template <int MIN_CTAS>
-__global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS) k_shade(const RdpPass *__restrict__ passes, uint32_t num_passes,
-                                                        const uint2 *__restrict__ pairs, const uint32_t *__restrict__ ctrl,
-                                                        const RdpPrimGeom *__restrict__ geom,
-                                                        const RdpPrimAttr *__restrict__ attr,
-                                                        const RdpPrimShade *__restrict__ shade,
-                                                        const RdpTile *__restrict__ tilesets,
-                                                        uint2 *__restrict__ sc, const uint4 *__restrict__ list,
-                                                        uint32_t *__restrict__ queues, uint32_t num_queues,
-                                                        uint32_t queue_min, const SpanRow *__restrict__ spans,
-                                                        const uint32_t *__restrict__ prim_rows)
-{
-	constexpr int WARPS = SHADE_THREADS / 32;
-	__shared__ __align__(16) uint4 s_rec_all[WARPS][2]; // current / next position's record, per warp
-	__shared__ uint32_t s_pos_all[WARPS][2];
-	if (ctrl[1]) return;
-	const uint32_t num_pairs = ctrl[0], total = num_pairs * 2u;
-	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-	uint4 *s_rec = s_rec_all[wid];
-	uint32_t *s_pos = s_pos_all[wid];
-	const uint32_t worker = blockIdx.x * WARPS + uint32_t(wid), workers = gridDim.x * WARPS;
-	if (num_pairs < gridDim.x * queue_min) queues = nullptr;
-	uint32_t q = 0, k_next = 0;
-	int buf = 0;
-	// Lane 0: the record of position p's pair into s_rec[b] (asynchronous).
-	auto fetch = [&](uint32_t p, int b) {
-		if (list) cp_async16(&s_rec[b], list + (p >> 1));
-		else cp_async8(&s_rec[b], pairs + (p >> 1));
-	};
-	if (lane == 0)
-	{
-		uint32_t first = worker;
-		if (queues)
-		{
-			q = sm_id() % num_queues;
-			first = queue_pos(q, atomicAdd(&queues[q], 1u), num_queues);
-			if (first >= total) first = queue_steal(queues, num_queues, total, q);
-			if (first < total) k_next = atomicAdd(&queues[q], 1u);
-		}
-		if (first < total) fetch(first, 0);
-		s_pos[0] = first;
-		cp_async_wait_all();
-	}
-	__syncwarp();
-	uint32_t p = s_pos[0];
-	while (p < total)
-	{
-		const uint4 rec = s_rec[buf];
-		const uint32_t prim = rec.x, item = rec.y, pr = list ? rec.z : (p >> 1);
-		const int half = int(p & 1u);
-		// Lane 0: the next position (its queue atomic was issued a position ago) and its record.
-		if (lane == 0)
-		{
-			uint32_t np = p + workers;
-			if (queues)
-			{
-				np = queue_pos(q, k_next, num_queues);
-				if (np >= total) np = queue_steal(queues, num_queues, total, q);
-				if (np < total) k_next = atomicAdd(&queues[q], 1u);
-			}
-			if (np < total) fetch(np, buf ^ 1);
-			s_pos[buf ^ 1] = np;
-		}
-		const RdpPass &ps = passes[list ? rec.w : shade[prim].pass];
-		int tx, ty;
-		record_tile(ps, item, list != nullptr, tx, ty);
-		const RdpPrimGeom &g = geom[prim];
-		const int x = tx * 8 + (lane & 7), y = ty * 8 + half * 4 + (lane >> 3);
-		Shaded out;
-		bool ok = false;
-		if (x < int(ps.fb_width) && y < int(ps.fb_height) && y >= g.span_ylo && y <= g.span_yhi)
-		{
-			PassConst pc;
-			switch (ps.fb_fmt)
-			{
-			case FBF_I4: pc.fb_size = 0; pc.dx_mask = 0; pc.dx_shift = 0; break;
-			case FBF_I8: pc.fb_size = 1; pc.dx_mask = ~7; pc.dx_shift = 3; break;
-			case FBF_RGBA5551:
-			case FBF_IA88: pc.fb_size = 2; pc.dx_mask = ~3; pc.dx_shift = 2; break;
-			default: pc.fb_size = 4; pc.dx_mask = ~1; pc.dx_shift = 1; break;
-			}
-			pc.alias = ps.fb_addr == ps.depth_addr;
-			const SpanRow *sp = spans + prim_rows[prim] + uint32_t(y - g.span_ylo);
-			const RdpPrimShade &sh = shade[prim];
-			ok = shade_pixel(pc, g, attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
-			                 ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, sp[0], sp[1], x, y, out);
-		}
-		// All 64 pixels of the scratch are written (full sectors, no partial-sector
-		// read-modify-write in L2); k_blend skips pixels whose misc word says "not written".
-		sc[size_t(pr) * SHADE_THREADS + size_t(half) * 32 + size_t(lane)] = ok ? pack_shaded(out) : kScratchEmpty;
-		if (lane == 0) cp_async_wait_all();
-		__syncwarp();
-		buf ^= 1;
-		p = s_pos[buf];
-	}
-}
+// The shading kernels are compiled for several minimum residencies (register budgets); the
+// executor's autotuner picks one.  More resident CTAs hide more latency at the price of some
+// spilling.
 
-// Packed shading: one warp per pair (no CTA barrier), same work order and scratch as k_shade.
-// The warp first picks the pair's candidate pixels -- inside the image and inside the valid span
-// of their row (k_span's rows), the only ones that can be covered -- and shades just those,
-// packed into as few 32-lane rounds as they fill: one round for most pairs at a primitive's
-// edge, where k_shade's half-pair warps would each run a round with idle lanes.  The other
-// pixels are written as empty.  Same results as k_shade.
+// Packed shading: one warp per pair (no CTA barrier).  The warp first picks the pair's candidate
+// pixels -- inside the image and inside the valid span of their row (k_span's rows), the only
+// ones that can be covered -- and shades just those, packed into as few 32-lane rounds as they
+// fill (one round for most pairs at a primitive's edge).  The other pixels are written as empty.
 template <int MIN_CTAS>
 __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 	k_shade_packed(const RdpPass *__restrict__ passes, uint32_t num_passes, const uint2 *__restrict__ pairs,
@@ -3273,20 +3170,22 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 	}
 }
 
-// Packed shading over two pairs at a time: a warp takes two positions per step (consecutive ones,
-// so mostly two tiles of one primitive in primitive-major order), picks both pairs' candidate
-// pixels and shades them together in as few 32-lane rounds as they fill -- two pairs with few
-// covered pixels share one round.  Per-pair data sits in shared memory for the shading rounds.
-// Same work order, scratch and results as k_shade_packed.
-template <int MIN_CTAS>
+// Packed shading over NP pairs at a time: a warp takes NP positions per step (consecutive ones,
+// so mostly tiles of one primitive in primitive-major order), picks the pairs' candidate pixels
+// and shades them together in as few 32-lane rounds as they fill -- pairs with few covered
+// pixels share rounds.  Per-pair data sits in shared memory for the shading rounds.  Same work
+// order, scratch and results as k_shade_packed.  On the batched workload two pairs per step
+// measured best (four: slower than one, the rounds mix primitives).
+template <int NP, int MIN_CTAS>
 __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
-	k_shade_packed2(const RdpPass *__restrict__ passes, uint32_t num_passes, const uint2 *__restrict__ pairs,
+	k_shade_packedn(const RdpPass *__restrict__ passes, uint32_t num_passes, const uint2 *__restrict__ pairs,
 	                const uint32_t *__restrict__ ctrl, const RdpPrimGeom *__restrict__ geom,
 	                const RdpPrimAttr *__restrict__ attr, const RdpPrimShade *__restrict__ shade,
 	                const RdpTile *__restrict__ tilesets, uint2 *__restrict__ sc, const uint4 *__restrict__ list,
 	                uint32_t *__restrict__ queues, uint32_t num_queues, uint32_t queue_min,
 	                const SpanRow *__restrict__ spans, const uint32_t *__restrict__ prim_rows)
 {
+	static_assert(NP >= 2 && NP <= 4, "a candidate entry is slot << 6 | pixel in 8 bits");
 	constexpr int WARPS = SHADE_THREADS / 32;
 	constexpr uint32_t NONE = 0xffffffffu;
 	struct Slot
@@ -3295,61 +3194,70 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 		int tx, ty, ylo;
 		const SpanRow *rows;
 	};
-	__shared__ __align__(16) uint4 s_rec_all[WARPS][2][2]; // [buffer][slot]: the positions' records
-	__shared__ uint32_t s_pos_all[WARPS][2][2];             // [buffer][slot]: positions (NONE: no pair)
-	__shared__ Slot s_slot_all[WARPS][2];
-	__shared__ uint8_t s_px_all[WARPS][128];                // candidates: slot << 6 | pixel, in order
+	__shared__ __align__(16) uint4 s_rec_all[WARPS][2][NP]; // [buffer][slot]: the positions' records
+	__shared__ uint32_t s_pos_all[WARPS][2][NP];             // [buffer][slot]: positions (NONE: no pair)
+	__shared__ Slot s_slot_all[WARPS][NP];
+	__shared__ uint8_t s_px_all[WARPS][64 * NP];             // candidates: slot << 6 | pixel, in order
 	if (ctrl[1]) return;
 	const uint32_t total = ctrl[0];
 	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-	uint4(*s_rec)[2] = s_rec_all[wid];
-	uint32_t(*s_pos)[2] = s_pos_all[wid];
+	uint4(*s_rec)[NP] = s_rec_all[wid];
+	uint32_t(*s_pos)[NP] = s_pos_all[wid];
 	Slot *s_slot = s_slot_all[wid];
 	uint8_t *s_px = s_px_all[wid];
 	const uint32_t worker = blockIdx.x * WARPS + uint32_t(wid), workers = gridDim.x * WARPS;
 	if (total < gridDim.x * queue_min) queues = nullptr;
 	uint32_t q = 0, k_next = 0;
 	int buf = 0;
-	// Lane 0: the next step's two positions into s_pos[b] and their records into s_rec[b].
-	// With queues a take reserves two consecutive slots of the SM's queue; a take after stealing
+	// Lane 0: the next step's positions into s_pos[b] and their records into s_rec[b].  With
+	// queues a take reserves NP consecutive slots of the SM's queue; a take after stealing
 	// reserves one.
 	auto take = [&](int b, bool first) {
-		uint32_t pa, pb = NONE;
+		uint32_t pos[NP];
+#pragma unroll
+		for (int i = 0; i < NP; i++) pos[i] = NONE;
 		if (queues)
 		{
 			if (first)
 			{
 				q = sm_id() % num_queues;
-				k_next = atomicAdd(&queues[q], 2u);
+				k_next = atomicAdd(&queues[q], uint32_t(NP));
 			}
-			pa = queue_pos(q, k_next, num_queues);
+			uint32_t pa = queue_pos(q, k_next, num_queues);
 			if (pa < total)
 			{
-				pb = queue_pos(q, k_next + 1, num_queues);
-				if (pb >= total) pb = NONE;
+				pos[0] = pa;
+#pragma unroll
+				for (int i = 1; i < NP; i++)
+				{
+					const uint32_t pi = queue_pos(q, k_next + uint32_t(i), num_queues);
+					pos[i] = pi < total ? pi : NONE;
+				}
 			}
 			else
+			{
 				pa = queue_steal(queues, num_queues, total, q);
-			if (pa < total) k_next = atomicAdd(&queues[q], 2u);
+				pos[0] = pa < total ? pa : NONE;
+			}
+			if (pa < total) k_next = atomicAdd(&queues[q], uint32_t(NP));
 		}
 		else
 		{
-			pa = first ? 2u * worker : s_pos[b ^ 1][0] + 2u * workers;
-			pb = pa + 1 < total ? pa + 1 : NONE;
+			const uint32_t pa = first ? uint32_t(NP) * worker : s_pos[b ^ 1][0] + uint32_t(NP) * workers;
+			if (pa < total)
+#pragma unroll
+				for (int i = 0; i < NP; i++) pos[i] = pa + uint32_t(i) < total ? pa + uint32_t(i) : NONE;
 		}
-		if (pa >= total) pa = pb = NONE;
-		if (pa != NONE)
+#pragma unroll
+		for (int i = 0; i < NP; i++)
 		{
-			if (list) cp_async16(&s_rec[b][0], list + pa);
-			else cp_async8(&s_rec[b][0], pairs + pa);
+			if (pos[i] != NONE)
+			{
+				if (list) cp_async16(&s_rec[b][i], list + pos[i]);
+				else cp_async8(&s_rec[b][i], pairs + pos[i]);
+			}
+			s_pos[b][i] = pos[i];
 		}
-		if (pb != NONE)
-		{
-			if (list) cp_async16(&s_rec[b][1], list + pb);
-			else cp_async8(&s_rec[b][1], pairs + pb);
-		}
-		s_pos[b][0] = pa;
-		s_pos[b][1] = pb;
 	};
 	if (lane == 0)
 	{
@@ -3360,18 +3268,16 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 	const unsigned below = (1u << lane) - 1u;
 	while (s_pos[buf][0] != NONE)
 	{
-		const uint32_t pa = s_pos[buf][0], pb = s_pos[buf][1];
-		const uint4 rec_a = s_rec[buf][0], rec_b = s_rec[buf][1];
 		__syncwarp();
 		if (lane == 0) take(buf ^ 1, false);
-		// Candidates of both pairs: pixels lane (rows 0-3) and lane + 32 (rows 4-7) of each.
+		// Candidates of the pairs: pixels lane (rows 0-3) and lane + 32 (rows 4-7) of each.
 		int count = 0;
 #pragma unroll
-		for (int s = 0; s < 2; s++)
+		for (int s = 0; s < NP; s++)
 		{
-			const uint32_t pos = s ? pb : pa;
+			const uint32_t pos = s_pos[buf][s];
 			if (pos == NONE) break;
-			const uint4 rec = s ? rec_b : rec_a;
+			const uint4 rec = s_rec[buf][s];
 			const uint32_t prim = rec.x, pi = list ? rec.w : shade[prim].pass;
 			const RdpPass &ps = passes[pi];
 			int tx, ty;
@@ -3750,8 +3656,8 @@ typedef void (*ShadeKernel)(const RdpPass *, uint32_t, const uint2 *, const uint
                             const RdpPrimAttr *, const RdpPrimShade *, const RdpTile *, uint2 *, const uint4 *,
                             uint32_t *, uint32_t, uint32_t, const rdp::SpanRow *, const uint32_t *);
 const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = {
-	rdp::k_shade<18>,         rdp::k_shade<20>,         rdp::k_shade_packed2<18>, rdp::k_shade_packed2<20>,
-	rdp::k_shade_packed<16>,  rdp::k_shade_packed<18>,  rdp::k_shade_packed<20>,  rdp::k_shade_packed<24>
+	rdp::k_shade_packedn<2, 16>, rdp::k_shade_packedn<2, 18>, rdp::k_shade_packedn<2, 20>, rdp::k_shade_packedn<2, 24>,
+	rdp::k_shade_packed<16>,     rdp::k_shade_packed<18>,     rdp::k_shade_packed<20>,     rdp::k_shade_packed<24>
 };
 } // namespace
 

@@ -5,10 +5,9 @@
 #include <cuda_runtime.h>
 #include "rdp_types.h"
 
-/* Shading kernel variants (the autotuner chooses among them): k_shade (one warp per half pair)
- * for minimum residencies of 18 and 20 64-thread CTAs per SM, k_shade_packed2 (two pairs per
- * warp step, candidate pixels packed together) for 18 and 20, and k_shade_packed (one warp per
- * pair, candidate pixels packed) for 16, 18, 20 and 24. */
+/* Shading kernel variants (the autotuner chooses among them): k_shade_packedn with two pairs per
+ * warp step (candidate pixels of both pairs packed together) and k_shade_packed (one pair per
+ * warp step), each for minimum residencies of 16, 18, 20 and 24 64-thread CTAs per SM. */
 /* Bytes of one span row (one scanline of one primitive, computed by k_bin). */
 #define RDP_SPAN_ROW_BYTES 64
 /* Launches with more tiles (or, in primitive-major order, primitives) than this scan their

@@ -73,11 +73,11 @@ def _order_run(words, rdram, streams):
     return single, batched
 
 
-@pytest.mark.parametrize("variant", [0, 2, 5], ids=["half_pair", "two_pairs_packed", "packed_pair"])
+@pytest.mark.parametrize("variant", [1, 5], ids=["two_pairs", "one_pair"])
 def test_shade_orders_bit_exact(restore_order, restore_tuning, monkeypatch, variant):
     """Tile order with a fixed stride, per-SM work queues and primitive-major order shade the
-    same pairs: identical bytes, on a single stream and on a batch of instances, with a
-    half-pair, a two-pairs-per-step and a packed-pair shading kernel.  The size thresholds are
+    same pairs: identical bytes, on a single stream and on a batch of instances, with shading
+    kernels that take two and one pair per warp step.  The size thresholds are
     set to 0 so that every launch, down to the smallest, takes the queues (and their stealing
     sweep) and the primitive-major order; one more run keeps the default thresholds.  The
     single stream's big pass (10,000 primitives, 1,200 tiles) takes the one-CTA scans, the

@@ -472,7 +472,7 @@ def run_ours_batched(args):
     total_passes = _sum_over_ranks(dist, passes_per_step * args.steps)
     total_frags = _sum_over_ranks(dist, frags_per_step * args.steps)
     value = total_passes / t_value
-    # The same sync point in plain tile order (the fallback the learned order is judged against).
+    # The same sync point in plain tile order (the fallback the learned order is compared with).
     b.set_schedule(learned_order=False, train=False)
     rs = timed_graph("static")
     t_static = _max_over_ranks(dist, sum(rs["step_ms"]) / 1e3)

@@ -235,7 +235,9 @@ int rdp_batch_capture_end(rdp_batch *b, rdp_graph **out);
  * launch's tiles (every train_stride-th), target log2(1 + measured blend cycles) / 16.
  * rdp_batch_get_model returns the FP32 parameters and the last step's mean squared error;
  * rdp_batch_set_model loads parameters (and resets the optimiser state). */
+#ifndef RDP_MLP_PARAMS
 #define RDP_MLP_PARAMS 5313
+#endif
 int rdp_batch_set_schedule(rdp_batch *b, int learned_order, int train, float learning_rate, uint32_t train_stride);
 int rdp_batch_get_model(rdp_batch *b, float *params, float *last_loss);
 int rdp_batch_set_model(rdp_batch *b, const float *params);

@@ -27,7 +27,10 @@
 #define RDP_MLP_B2 (RDP_MLP_W2 + RDP_MLP_HIDDEN * RDP_MLP_HIDDEN)
 #define RDP_MLP_W3 (RDP_MLP_B2 + RDP_MLP_HIDDEN)
 #define RDP_MLP_B3 (RDP_MLP_W3 + RDP_MLP_HIDDEN)
+#ifndef RDP_MLP_PARAMS /* also defined by the public header rdp_cuda.h */
 #define RDP_MLP_PARAMS (RDP_MLP_B3 + 1)
+#endif
+static_assert(RDP_MLP_PARAMS == RDP_MLP_B3 + 1, "packed MLP parameter count");
 #define RDP_SCHED_BUCKETS 1024
 
 /* Per-primitive feature bits (k_prim_setup) that the tile features count (k_expand). */

@@ -18,7 +18,7 @@ def _stream(config, **kw):
 
 
 def test_plain_frame_full_size():
-    # configs[0]: 320x240 RGBA5551, FillRect clear + 2,000 Gouraud triangles, seed 0.
+    # The plain frame: 320x240 RGBA5551, FillRect clear + 2,000 Gouraud triangles, seed 0.
     words, rdram = _stream(cmdgen.CONFIG_PLAIN, seed=0)
     assert_parity(words, rdram)
 
@@ -30,7 +30,7 @@ def test_plain_frame_seeds(seed):
 
 
 def test_textured_depth_frame():
-    # configs[1] shape at reduced primitive count.
+    # The textured, depth-tested 2-cycle frame at reduced primitive count.
     words, rdram = _stream(cmdgen.CONFIG_TEXTURED, seed=0, num_prims=1500)
     assert_parity(words, rdram)
 

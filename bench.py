@@ -108,14 +108,20 @@ class ClockSampler:
         self.path = None
 
     def start(self):
+        """Starts sampling every 50 ms and returns once the first sample is in (at most ~1 s),
+        so that the samples cover the timed region that follows."""
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        deadline = time.time() + 1.0
+        while time.time() < deadline and self.proc.poll() is None and os.path.getsize(self.path) == 0:
+            time.sleep(0.01)
 
     def stop(self):
         out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}

@@ -1,0 +1,50 @@
+"""Host side of bench.py (no GPU): the clock sampler that records SM clocks and throttle reasons
+during the timed region, driven by a stand-in `nvidia-smi` that prints CSV samples."""
+import os
+import stat
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+# Prints one sample every 20 ms, like `nvidia-smi --query-gpu=... --format=csv,noheader,nounits -lms N`:
+# index, clocks.sm, clocks.max.sm, power.draw, reasons.active, hw_slowdown, hw_thermal_slowdown,
+# sw_thermal_slowdown, sw_power_cap.
+_FAKE = """#!{python}
+import sys, time
+rows = ["0, 2070, 2070, 900.5, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "0, 1965, 2070, 1390.1, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "0, 2070, 2070, 1100.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active"]
+k = 0
+while True:
+    print(rows[k % len(rows)], flush=True)
+    k += 1
+    time.sleep(0.02)
+"""
+
+
+def test_clock_sampler_parses_samples_and_reasons(tmp_path, monkeypatch):
+    fake = tmp_path / "nvidia-smi"
+    fake.write_text(_FAKE.format(python=sys.executable))
+    fake.chmod(fake.stat().st_mode | stat.S_IEXEC)
+    monkeypatch.setenv("PATH", str(tmp_path) + os.pathsep + os.environ.get("PATH", ""))
+    sys.path.insert(0, ROOT)
+    import bench
+    c = bench.ClockSampler(0)
+    c.start()
+    assert os.path.getsize(c.path) > 0  # sampling is live when start() returns
+    time.sleep(0.2)
+    out = c.stop()
+    assert out["samples"] >= 3
+    assert out["sm_max_mhz"] == 2070.0
+    assert out["sm_mhz"] in (1965.0, 2070.0)
+    assert out["reasons"] == ["sw_power_cap"]
+
+
+def test_clock_sampler_without_nvidia_smi(tmp_path, monkeypatch):
+    monkeypatch.setenv("PATH", str(tmp_path))
+    sys.path.insert(0, ROOT)
+    import bench
+    c = bench.ClockSampler(0)
+    c.start()
+    assert c.stop() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}

@@ -48,3 +48,20 @@ def test_clock_sampler_without_nvidia_smi(tmp_path, monkeypatch):
     c = bench.ClockSampler(0)
     c.start()
     assert c.stop() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+
+def test_reference_arm_prints_its_contract_line():
+    # The reference arm (the CPU restatement of the reference's algorithm on the host cores),
+    # on two instances: one JSON line with the base metric, the reference marker, the CPU
+    # baseline it measured and an end-to-end entry without device copies.
+    import json
+    import subprocess
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--instances", "2",
+                        "--steps", "1", "--warmup", "0"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "passes/s" and line["value"] > 0
+    assert line["higher_is_better"] is True and line["n_gpus"] == 1
+    assert line["cpu_baseline"]["value"] == line["value"] and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": "passes/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}

@@ -22,10 +22,17 @@ e2e    : the batched path through the C ABI with host buffers: every instance's
          steps run as a frame server's loop: step s+1 is parsed and submitted while step
          s renders, then step s's results are waited for (e2e.serial_value: one step at
          a time).
-roofline: the dominant kernel (k_shade): algorithmic bytes of its output (10 B per
-         pixel of every shaded (primitive, 8x8 tile) instance, the reference's
-         shaded-data record) plus the 8 B pair entry, per launch, over its
-         CUDA-event duration, against the measured HBM copy peak.
+roofline: the dominant kernel (k_shade): bytes of its output (the 8 B shaded record per
+         pixel of every shaded (primitive, 8x8 tile) pair -- the reference writes a 10 B
+         record -- plus the 8 B pair entry), per launch, over its CUDA-event duration,
+         against the HBM copy peak; `traffic` scales the DRAM bytes per pair of a scoped
+         one-kernel ncu capture.  roofline.int_alu: the integer-op roofline that binds this
+         integer fixed-point work -- the reference algorithm's integer ops per step, counted
+         on the CPU oracle per stage (oracle/op_table.json, made by oracle/make_op_table.py),
+         over the measured time, against the integer issue peak (SMs x 4 sub-partitions x 32
+         lanes x the sampled SM clock).  roofline.step_hbm: the step's algorithmic bytes
+         (command words, the touched tiles' framebuffer loads and stores, texture sources)
+         over the step time, against the HBM peak.
 cpu_baseline: the CPU oracle (a scalar restatement of the reference's algorithm)
          over the instances on all host cores, on a bounded sample (>= 10 s).
 
@@ -192,6 +199,63 @@ def _cpu_baseline(words, rdram, min_seconds=10.0, max_frames=30):
     return frames, el, frags
 
 
+def _peaks():
+    """HBM peak (GB/s) and its source: the measured copy bandwidth when the driver has written
+    MEASURED_PEAKS.json, else the recipe's fallback figure."""
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        peaks = {}
+    if "hbm_gbs" in peaks:
+        return float(peaks["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _sm_count(device):
+    import torch
+    return torch.cuda.get_device_properties(device).multi_processor_count
+
+
+def _int_alu_roofline(workload, step_ms, shade_ms, sm_count, sm_mhz):
+    """Integer-op roofline of the step and of the shading kernel.  Ops are the reference
+    algorithm's integer / logic ops per step, counted per stage on the CPU oracle (data in
+    oracle/op_table.json); the peak is the integer issue rate, one 32-lane instruction per SM
+    sub-partition per cycle at the SM clock sampled during the timed region."""
+    try:
+        table = json.load(open(os.path.join(ROOT, "oracle", "op_table.json")))["workloads"][workload]
+    except (OSError, ValueError, KeyError):
+        return None
+    mhz = sm_mhz or 2070.0
+    peak = sm_count * 4 * 32 * mhz * 1e6 / 1e12  # Tops/s
+    step_ops, shade_ops = table["ops_total"], table["ops_shading_stages"]
+    step_t = step_ops / (step_ms / 1e3) / 1e12
+    shade_t = shade_ops / (shade_ms / 1e3) / 1e12 if shade_ms > 0 else 0.0
+    return {"bound": "int_alu", "unit": "Tops/s", "peak": peak,
+            "peak_source": "spec: %d SMs x 4 sub-partitions x 32 lanes x %.0f MHz (sampled SM clock)" % (sm_count, mhz),
+            "ops_per_step": step_ops, "achieved": step_t, "frac": step_t / peak,
+            "k_shade": {"ops_per_step": shade_ops, "achieved": shade_t, "frac": shade_t / peak},
+            "ops_source": "oracle/op_table.json (%s): per-stage integer ops of the reference algorithm" % workload}
+
+
+def _step_hbm_roofline(cmd_bytes, touched_tiles, fb_bytes_per_tile, uploads, step_ms, peak, peak_src):
+    """The step's algorithmic bytes: command words, each touched 8x8 tile's framebuffer loaded and
+    stored once (colour + hidden bytes, and 16-bit depth + hidden for images with a depth
+    buffer), and at most one 4 KiB TMEM image of texture source per upload."""
+    algo = cmd_bytes + touched_tiles * fb_bytes_per_tile + uploads * 4096
+    achieved = algo / (step_ms / 1e3) / 1e9
+    return {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes_per_step": algo, "achieved": achieved, "peak": peak,
+            "peak_source": peak_src, "frac": achieved / peak}
+
+
+def _shade_traffic_per_pair():
+    """DRAM bytes per shaded pair of the shading kernel, from the scoped ncu capture summarised in
+    profiles/k_shade_traffic.json (one kernel, a few launches, the 16-instance case)."""
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "k_shade_traffic.json"))).get("dram_bytes_per_pair")
+    except (OSError, ValueError):
+        return None
+
+
 def _reference_passes(words, rdram):
     """Reference-equivalent pass count of one frame (host-side need_flush emulation)."""
     from rdp_gb300 import CommandProcessor
@@ -270,27 +334,21 @@ def run_ours_textured(args):
     cp.close()
 
     # ---------------- roofline of the rasteriser
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    # k_shade output: 10 B per pixel of every shaded (primitive, tile) instance + the 8 B pair entry.
+    hbm_peak, peak_src = _peaks()
     bytes_per_pair = 64 * 8 + 8  # the 8-byte shaded record per pixel + the 8-byte pair entry
     shade_launches = max(1, graph_shade_launches)
     raster_launch_ms = statistics.mean(raster_ms) / shade_launches
     algo_bytes = base["tile_instances"] * bytes_per_pair / shade_launches
     achieved = algo_bytes / (raster_launch_ms / 1e3) / 1e9 if raster_launch_ms > 0 else 0.0
+    # The scoped capture's DRAM bytes per pair were measured on the batched workload; this frame is
+    # not captured, so its traffic is not reported.
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "k_shade_traffic.json")
-    if os.path.exists(tpath):
-        try:
-            per_pair = json.load(open(tpath)).get("textured_frame", {}).get("dram_bytes_per_tile_instance")
-            traffic = per_pair * base["tile_instances"] / shade_launches if per_pair else None
-        except (OSError, ValueError):
-            traffic = None
+    step_ms_mean = t_value * 1e3 / args.steps
+    int_alu = _int_alu_roofline("textured", step_ms_mean, statistics.mean(raster_ms), _sm_count(local),
+                                clock_info.get("sm_mhz"))
+    # RGBA5551 colour (2 B) + hidden (1 B) and Z16 (2 B) + hidden (1 B), loaded and stored.
+    step_hbm = _step_hbm_roofline(len(words) * 4, base["touched_tiles"], 64 * 2 * (3 + 3), base["tmem_uploads"],
+                                  step_ms_mean, hbm_peak, peak_src)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -306,7 +364,8 @@ def run_ours_textured(args):
         "gpu_launches": int(launches),
         "roofline": {"kernel": "k_shade", "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_source": peak_src, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": raster_launch_ms},
+                     "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": raster_launch_ms,
+                     "int_alu": int_alu, "step_hbm": step_hbm},
         "clocks": clock_info,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -440,6 +499,8 @@ def run_ours_batched(args):
     passes_per_step = sum(x["reference_passes"] - y["reference_passes"] for x, y in zip(s1, s0))
     frags_per_step = sum(x["fragments"] - y["fragments"] for x, y in zip(s1, s0))
     pairs_per_step = sum(x["tile_instances"] - y["tile_instances"] for x, y in zip(s1, s0))
+    tiles_per_step = sum(x["touched_tiles"] - y["touched_tiles"] for x, y in zip(s1, s0))
+    uploads_per_step = sum(x["tmem_uploads"] - y["tmem_uploads"] for x, y in zip(s1, s0))
 
     # ---------------- learned tile order: the cost model trains online on the first sync points
     b.set_schedule(learned_order=True, train=True, learning_rate=3e-3)
@@ -551,25 +612,19 @@ def run_ours_batched(args):
         serving = _serving(args, local, model=b_model)
 
     # ---------------- roofline of the dominant kernel
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    hbm_peak, peak_src = _peaks()
     bytes_per_pair = 64 * 8 + 8  # the 8-byte shaded record per pixel + the 8-byte pair entry
     shade_launch_ms = statistics.mean(shade_ms) / max(1, shade_launches)
     algo_bytes = pairs_per_step * bytes_per_pair / max(1, shade_launches)
     achieved = algo_bytes / (shade_launch_ms / 1e3) / 1e9 if shade_launch_ms > 0 else 0.0
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "k_shade_traffic.json")
-    if os.path.exists(tpath):
-        try:
-            per_pair = json.load(open(tpath)).get("dram_bytes_per_tile_instance")
-            traffic = per_pair * pairs_per_step / max(1, shade_launches) if per_pair else None
-        except (OSError, ValueError):
-            traffic = None
+    per_pair = _shade_traffic_per_pair()
+    traffic = per_pair * pairs_per_step / max(1, shade_launches) if per_pair else None
+    step_ms_mean = t_value * 1e3 / args.steps
+    int_alu = _int_alu_roofline("batched64", step_ms_mean, statistics.mean(shade_ms), _sm_count(local),
+                                clock_info.get("sm_mhz")) if args.instances == BATCH_INSTANCES else None
+    # RGBA8888 colour (4 B) + 2 hidden bytes and Z16 (2 B) + hidden (1 B) per pixel, loaded and stored.
+    step_hbm = _step_hbm_roofline(sum(len(st[0]) for st in streams) * 4, tiles_per_step, 64 * 2 * (6 + 3),
+                                  uploads_per_step, step_ms_mean, hbm_peak, peak_src)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -600,7 +655,8 @@ def run_ours_batched(args):
                      "frac": achieved / hbm_peak, "peak_source": peak_src, "traffic": traffic,
                      "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": shade_launch_ms,
                      "launches_per_step": shade_launches,
-                     "share_of_step": statistics.mean(shade_ms) / statistics.mean(step_ms)},
+                     "share_of_step": statistics.mean(shade_ms) / statistics.mean(step_ms),
+                     "int_alu": int_alu, "step_hbm": step_hbm},
         "clocks": clock_info,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

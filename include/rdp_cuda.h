@@ -357,15 +357,23 @@ int rdp_get_shade_order(int device);
  * allocates memory. */
 #define RDP_NOALLOC_MAX_UPLOADS 1024
 
-typedef struct rdp_tmem_upload /* one TMEM upload plan; same layout as the reference's UploadInfo */
+/* One TMEM upload plan, 64 bytes: the region of RDRAM a texture load reads and where in TMEM it
+ * lands, as this library's command processor derives it from a LoadTile / LoadTLUT / LoadBlock
+ * command and the tile descriptor it names. */
+typedef struct rdp_tmem_upload
 {
-	int32_t width, height;
-	float min_t_mod, max_t_mod;
-	int32_t vram_addr, vram_width, vram_size, vram_effective_width;
-	int32_t tmem_offset, tmem_stride_words, tmem_size, tmem_fmt;
-	int32_t mode; /* 0 tile, 1 TLUT, 2 block */
-	float inv_tmem_stride_words;
-	int32_t dxt;
+	int32_t width, height;                 /* texels per line written to TMEM (rounded to whole words), lines */
+	float min_t_mod, max_t_mod;            /* LoadBlock: reciprocals of the longest and shortest line lengths */
+	int32_t vram_addr;                     /* RDRAM byte address of the first texel */
+	int32_t vram_width;                    /* texels per RDRAM line */
+	int32_t vram_size;                     /* RDRAM texel size: 1 = 8, 2 = 16, 3 = 32 bits */
+	int32_t vram_effective_width;          /* texels per line actually read (rounded to 64-bit words) */
+	int32_t tmem_offset;                   /* TMEM byte offset of the first line */
+	int32_t tmem_stride_words;             /* TMEM line stride in 16-bit words (LoadBlock: in 64-bit words) */
+	int32_t tmem_size, tmem_fmt;           /* the tile descriptor's texel size and format */
+	int32_t mode;                          /* 0 LoadTile, 1 LoadTLUT, 2 LoadBlock */
+	float inv_tmem_stride_words;           /* 1 / tmem_stride_words, rounded to fp32 on the host */
+	int32_t dxt;                           /* LoadBlock: line step in 1/65536 lines per 64-bit word */
 	int32_t padding;
 } rdp_tmem_upload;
 

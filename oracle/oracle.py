@@ -22,9 +22,12 @@ def build():
 def _load():
     global _lib
     if _lib is None:
-        if not os.path.exists(_PATH):
+        # RDP_ORACLE_LIB selects another build of the same sources (the op-count build of
+        # make_op_table.py); by default the optimised build is used.
+        path = os.environ.get("RDP_ORACLE_LIB", _PATH)
+        if path == _PATH and not os.path.exists(_PATH):
             build()
-        L = ctypes.CDLL(_PATH)
+        L = ctypes.CDLL(path)
         vp, u32 = ctypes.c_void_p, ctypes.c_uint32
         L.oracle_create.argtypes = [u32, u32]
         L.oracle_create.restype = vp
@@ -32,6 +35,7 @@ def _load():
         for n in ("oracle_write_rdram", "oracle_read_rdram", "oracle_read_hidden", "oracle_write_hidden"):
             getattr(L, n).argtypes = [vp, vp, u32, u32]
         L.oracle_read_tmem.argtypes = [vp, vp]
+        L.oracle_apply_upload_plans.argtypes = [vp, vp, u32]
         L.oracle_enqueue.argtypes = [vp, vp, u32]
         L.oracle_enqueue.restype = u32
         L.oracle_fragments.argtypes = [vp]

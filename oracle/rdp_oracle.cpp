@@ -1789,11 +1789,33 @@ struct Oracle
 		int shade_alpha;
 	};
 
+	// Span rows of the primitive being rendered, each set up once (span_setup.comp runs one
+	// invocation per scanline of a primitive, shading.h reads the rows; rdp_renderer.cpp:1523-1554).
+	// Rows span_ylo .. span_yhi + 1 (the last for the pipelined texel1 peek at the next line).
+	std::vector<Span> span_rows;
+	std::vector<uint8_t> span_row_ready;
+	void begin_span_rows(const Prim &p)
+	{
+		size_t n = p.span_yhi >= p.span_ylo ? size_t(p.span_yhi - p.span_ylo) + 2 : 0;
+		if (span_rows.size() < n) span_rows.resize(n);
+		span_row_ready.assign(n, 0);
+	}
+	const Span &span_row(const Prim &p, int y)
+	{
+		size_t i = size_t(y - p.span_ylo);
+		if (!span_row_ready[i])
+		{
+			span_rows[i] = span_setup(p.setup, p.attr, p.scissor, y);
+			span_row_ready[i] = 1;
+		}
+		return span_rows[i];
+	}
+
 	// shading.h:38-359, scaling 1.
 	bool shade_pixel(const Prim &p, int x, int y, Shaded &out, int fb_size, int dx_mask, int dx_shift)
 	{
 		if (y < p.span_ylo || y > p.span_yhi) return false;
-		Span sp = span_setup(p.setup, p.attr, p.scissor, y);
+		const Span &sp = span_row(p, y);
 		if (!sp.valid) return false;
 		const StaticState &st = p.st;
 		uint32_t f = st.flags;
@@ -1860,7 +1882,7 @@ struct Oracle
 
 		if (uses_pipelined_texel1)
 		{
-			Span next = span_setup(p.setup, p.attr, p.scissor, y + 1);
+			const Span &next = span_row(p, y + 1);
 			bool valid_line = next.valid;
 			bool long_span = sp.lodlength >= 8;
 			bool end_span = x == (flip ? sp.end_x : sp.start_x);
@@ -2539,6 +2561,7 @@ struct Oracle
 		int width = int(fb.width);
 		int tiles_x = (width + 7) / 8;
 		int ty0 = p.span_ylo / 8, ty1 = p.span_yhi / 8;
+		begin_span_rows(p);
 		for (int ty = ty0; ty <= ty1; ty++)
 		{
 			for (int tx = 0; tx < tiles_x; tx++)
@@ -3436,6 +3459,21 @@ uint32_t oracle_enqueue(void *h, const uint32_t *words, uint32_t num_words)
 		i += len;
 	}
 	return i;
+}
+
+// Applies caller-made upload plans (64-byte records: the UploadInfo fields, then 4 bytes of
+// padding) to the oracle's TMEM in order, as tmem_update.comp applies a pass's uploads.  Tests use
+// it to check hand-derived plans against the plans the oracle derives from load commands.
+void oracle_apply_upload_plans(void *h, const uint8_t *plans, uint32_t count)
+{
+	static_assert(sizeof(UploadInfo) == 60, "UploadInfo is the plan record without its padding");
+	Oracle *o = static_cast<Oracle *>(h);
+	for (uint32_t i = 0; i < count; i++)
+	{
+		UploadInfo u;
+		memcpy(&u, plans + size_t(i) * 64, sizeof(u));
+		o->apply_upload(u);
+	}
 }
 
 uint64_t oracle_fragments(void *h) { return static_cast<Oracle *>(h)->fragments; }

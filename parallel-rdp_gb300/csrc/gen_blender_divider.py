@@ -4,9 +4,9 @@ The RDP blender divider (used by the final blender cycle when force-blend is
 off) is hardware behaviour captured as a 16 x 2048 table in the reference
 (parallel-rdp/luts.hpp:7, indexed as (blend_sum << 11) | blended, see
 parallel-rdp/shaders/blender.h:124-136).  Rows whose entries follow
-floor(n / d) & 0xff are regenerated by formula at run time
-(rdp_luts.h: rdp_build_blender_divider); only the entries that deviate from
-that formula are stored, as (row, start, length, value) runs.
+floor(n / d) & 0xff are regenerated by formula at run time (build_blender_lut in
+rdp_cp.cpp, and the oracle's own table builder); only the entries that deviate
+from that formula are stored, as (row, start, length, value) runs.
 
 Usage: python gen_blender_divider.py <path-to-luts.hpp> > blender_divider_runs.inc
 """

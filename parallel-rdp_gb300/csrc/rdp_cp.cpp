@@ -1420,6 +1420,14 @@ struct rdp_cp
 		return RDP_OK;
 	}
 
+	// Completion query for `value` that never launches deferred work (unlike wait_timeline,
+	// which submits the batch when `value` still waits for it): RDP_ERR_TIMEOUT while pending.
+	int poll_timeline(uint64_t value)
+	{
+		if (batch && !unsubmitted.empty() && unsubmitted.front() <= value) return RDP_ERR_TIMEOUT;
+		return wait_timeline(value, 0);
+	}
+
 	int wait_timeline(uint64_t value, uint64_t timeout_ns)
 	{
 		// Timeouts beyond ~11 days mean "no deadline" (and must not overflow the clock).
@@ -1474,6 +1482,11 @@ struct rdp_batch
 	rdpx::CaptureSink sink;
 	uint64_t rounds = 0, passes = 0;
 	int sticky_error = RDP_OK;
+	// Host threads that parse many instances' command words at once (rdp_batch_enqueue_many,
+	// the serving loop's admissions).  A task owns one instance, and run() returns only once
+	// every task has finished, so no instance's recorder is ever touched by two threads, and
+	// nothing reads the recorders (submit, completion polls) while a parse is running.
+	rdpx::HostPool parse_pool;
 
 	bool reserve_for_capture();
 
@@ -2225,6 +2238,10 @@ int rdp_serve_run(rdp_batch *b, rdp_cp *const *instances, uint32_t num_instances
 	};
 	std::deque<uint32_t> waiting;
 	std::vector<Flight> flying;
+	std::vector<uint32_t> admit, group_of(num_instances, UINT32_MAX);
+	std::vector<std::vector<uint32_t>> groups;
+	std::vector<uint64_t> admitted_value(num_requests, 0);
+	std::vector<int> admitted_status(num_requests, RDP_OK);
 	uint32_t next = 0, done = 0;
 	uint64_t in_bytes = 0;
 	rdp_serve_stats st = {};
@@ -2239,11 +2256,11 @@ int rdp_serve_run(rdp_batch *b, rdp_cp *const *instances, uint32_t num_instances
 		}
 		bool progress = false;
 		while (next < num_requests && requests[next].arrival_s <= t) waiting.push_back(next++);
-		// Completions.
+		// Completions: event queries only (no submission happens here).
 		for (size_t k = 0; k < flying.size();)
 		{
 			rdp_cp *cp = instances[requests[flying[k].req].instance];
-			int w = cp->wait_timeline(flying[k].value, 0);
+			int w = cp->poll_timeline(flying[k].value);
 			if (w == RDP_ERR_TIMEOUT)
 			{
 				k++;
@@ -2265,28 +2282,58 @@ int rdp_serve_run(rdp_batch *b, rdp_cp *const *instances, uint32_t num_instances
 		}
 		if (r != RDP_OK) break;
 		// Admission in arrival order while the budget has room (at least one frame always fits).
-		bool admitted = false;
+		// The admitted requests are chosen first; their command words are then parsed on the
+		// batch's parse threads, one task per instance (its requests in arrival order), and all
+		// tasks have finished before the loop submits or polls again.
+		admit.clear();
 		while (!waiting.empty())
 		{
 			const uint32_t q = waiting.front();
 			const uint64_t fp = footprint(requests[q]);
-			if (!flying.empty() && (in_bytes + fp > config->hbm_budget_bytes ||
-			                        (config->max_in_flight && flying.size() >= config->max_in_flight)))
+			const size_t in_flight = flying.size() + admit.size();
+			if (in_flight && (in_bytes + fp > config->hbm_budget_bytes ||
+			                  (config->max_in_flight && in_flight >= config->max_in_flight)))
 				break;
-			rdp_cp *cp = instances[requests[q].instance];
-			if ((r = cp->enqueue(requests[q].num_words, requests[q].words)) != RDP_OK) break;
-			uint64_t v = 0;
-			if ((r = cp->signal_timeline(&v)) != RDP_OK) break;
-			results[q].admit_s = now_s();
-			flying.push_back(Flight{ q, v, fp });
+			admit.push_back(q);
 			in_bytes += fp;
+			waiting.pop_front();
+		}
+		if (!admit.empty())
+		{
+			groups.clear();
+			for (uint32_t q : admit)
+			{
+				const uint32_t inst = requests[q].instance;
+				if (group_of[inst] == UINT32_MAX)
+				{
+					group_of[inst] = uint32_t(groups.size());
+					groups.emplace_back();
+				}
+				groups[group_of[inst]].push_back(q);
+			}
+			b->parse_pool.run(uint32_t(groups.size()), [&](uint32_t g) {
+				cudaSetDevice(b->device);
+				for (uint32_t q : groups[g])
+				{
+					rdp_cp *cp = instances[requests[q].instance];
+					int e = cp->enqueue(requests[q].num_words, requests[q].words);
+					if (e == RDP_OK) e = cp->signal_timeline(&admitted_value[q]);
+					admitted_status[q] = e;
+				}
+			});
+			const double t_admit = now_s();
+			for (const auto &grp : groups) group_of[requests[grp.front()].instance] = UINT32_MAX;
+			for (uint32_t q : admit)
+			{
+				if (admitted_status[q] != RDP_OK && r == RDP_OK) r = admitted_status[q];
+				results[q].admit_s = t_admit;
+				flying.push_back(Flight{ q, admitted_value[q], footprint(requests[q]) });
+			}
 			st.max_in_flight = std::max<uint64_t>(st.max_in_flight, flying.size());
 			st.max_footprint = std::max(st.max_footprint, in_bytes);
-			waiting.pop_front();
-			admitted = true;
 		}
 		if (r != RDP_OK) break;
-		if (admitted)
+		if (!admit.empty())
 		{
 			// One submission for everything admitted in this pass: the new frames share launches.
 			if ((r = b->submit()) != RDP_OK) break;
@@ -2304,31 +2351,40 @@ int rdp_batch_enqueue_many(rdp_batch *b, uint32_t count, rdp_cp *const *instance
                            const uint32_t *num_words, uint64_t *timeline_values, uint32_t threads)
 {
 	if (!b || (count && (!instances || !words || !num_words))) return RDP_ERR_INVALID;
+	// Each instance is parsed by exactly one thread: a handle given twice would put two threads
+	// on one recorder.  Checked before any handle is dereferenced or any thread starts.
+	{
+		std::vector<rdp_cp *> sorted(instances, instances + count);
+		std::sort(sorted.begin(), sorted.end());
+		if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) return RDP_ERR_INVALID;
+	}
 	for (uint32_t i = 0; i < count; i++)
 		if (!instances[i] || instances[i]->batch != b) return RDP_ERR_INVALID;
-	if (!threads) threads = std::max(1u, std::thread::hardware_concurrency());
-	threads = std::min(threads, std::max(count, 1u));
 	cudaSetDevice(b->device);
 	std::vector<int> status(count, RDP_OK);
-	std::atomic<uint32_t> next(0);
-	auto work = [&] {
+	auto one = [&](uint32_t i) {
 		cudaSetDevice(b->device);
-		for (;;)
-		{
-			uint32_t i = next.fetch_add(1);
-			if (i >= count) break;
-			rdp_cp *cp = instances[i];
-			int r = cp->enqueue(num_words[i], words[i]);
-			uint64_t v = 0;
-			if (r == RDP_OK && timeline_values) r = cp->signal_timeline(&v);
-			if (timeline_values) timeline_values[i] = v;
-			status[i] = r;
-		}
+		rdp_cp *cp = instances[i];
+		int r = cp->enqueue(num_words[i], words[i]);
+		uint64_t v = 0;
+		if (r == RDP_OK && timeline_values) r = cp->signal_timeline(&v);
+		if (timeline_values) timeline_values[i] = v;
+		status[i] = r;
 	};
-	std::vector<std::thread> pool;
-	for (uint32_t t = 1; t < threads; t++) pool.emplace_back(work);
-	work();
-	for (auto &t : pool) t.join();
+	if (!threads)
+		b->parse_pool.run(count, one); // the batch's persistent parse threads (one per core, at most 16)
+	else
+	{
+		threads = std::min(threads, std::max(count, 1u));
+		std::atomic<uint32_t> next(0);
+		auto work = [&] {
+			for (uint32_t i; (i = next.fetch_add(1)) < count;) one(i);
+		};
+		std::vector<std::thread> pool;
+		for (uint32_t t = 1; t < threads; t++) pool.emplace_back(work);
+		work();
+		for (auto &t : pool) t.join();
+	}
 	for (int r : status)
 		if (r != RDP_OK) return r;
 	return RDP_OK;

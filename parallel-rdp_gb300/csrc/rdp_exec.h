@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <atomic>
 #include <condition_variable>
+#include <cstdio>
 #include <cstdlib>
 #include <functional>
 #include <mutex>
@@ -260,6 +261,13 @@ struct Executor
 	HostPool pool;                                      // staging fill of large launches
 	static constexpr size_t kParallelFillBytes = 1u << 20;
 	uint32_t *d_pair_log = nullptr; // [256]
+	// Launch log for profiling (RDP_LAUNCH_LOG=<file>): the pair count of every launch that runs
+	// outside a capture and is not a tuning sample is appended to the file at the next sync point,
+	// so that per-launch hardware counters can be scaled to per-pair figures.
+	FILE *launch_log = nullptr;
+	uint32_t *d_launch_pairs = nullptr; // [kLaunchLogSlots]
+	static constexpr uint32_t kLaunchLogSlots = 4096;
+	std::vector<std::pair<uint64_t, uint32_t>> launch_log_pending; // (launch number, slot)
 	// Size thresholds of the shading orders (RDP_SHADE_PERM_MIN_PRIMS, RDP_SHADE_QUEUE_MIN
 	// override them): primitive-major order for launches of at least perm_min_prims primitives,
 	// per-SM queues for launches of at least queue_min pairs per k_shade CTA.
@@ -454,6 +462,11 @@ struct Executor
 		if (const char *e = getenv("RDP_PAIR_CAPACITY")) initial_pairs = std::max(1u, uint32_t(strtoul(e, nullptr, 10)));
 		if (const char *e = getenv("RDP_SPAN_ROW_CAPACITY"))
 			initial_span_rows = std::max(1u, uint32_t(strtoul(e, nullptr, 10)));
+		if (const char *e = getenv("RDP_LAUNCH_LOG"))
+		{
+			launch_log = fopen(e, "a");
+			if (launch_log && check(cudaMalloc(&d_launch_pairs, kLaunchLogSlots * 4))) return false;
+		}
 		if (check(cudaMalloc(&d_ctrl, 32)) || check(cudaMalloc(&d_pair_log, 256 * 4)) ||
 		    check(cudaMalloc(&d_queues, queue_bytes())) ||
 		    check(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking)))
@@ -469,6 +482,21 @@ struct Executor
 	{
 		int v = shade_variant_choice(device);
 		return v >= 0 && v < RDP_SHADE_VARIANTS ? v : 0;
+	}
+
+	// Appends the pair counts of logged launches whose kernels have finished (the stream is idle).
+	void flush_launch_log()
+	{
+		if (!launch_log || launch_log_pending.empty()) return;
+		std::vector<uint32_t> pairs(kLaunchLogSlots);
+		if (cudaMemcpy(pairs.data(), d_launch_pairs, 4 * size_t(kLaunchLogSlots), cudaMemcpyDeviceToHost) != cudaSuccess)
+		{
+			cudaGetLastError();
+			return;
+		}
+		for (auto &e : launch_log_pending) fprintf(launch_log, "launch %llu pairs %u\n", (unsigned long long)e.first, pairs[e.second]);
+		fflush(launch_log);
+		launch_log_pending.clear();
 	}
 
 	// Folds finished tuning samples in (non-blocking for unfinished ones).
@@ -508,6 +536,7 @@ struct Executor
 	// the variant with the least k_shade time per pair.
 	void tune_epoch()
 	{
+		flush_launch_log();
 		if (!tuner.active) return;
 		if (shade_variant_choice(device) >= 0)
 		{
@@ -577,6 +606,15 @@ struct Executor
 		free_all();
 		sched_free();
 		cudaFree(d_ctrl);
+		if (launch_log)
+		{
+			if (stream) cudaStreamSynchronize(stream);
+			flush_launch_log();
+			fclose(launch_log);
+			launch_log = nullptr;
+		}
+		cudaFree(d_launch_pairs);
+		d_launch_pairs = nullptr;
 		cudaFree(d_pair_log);
 		cudaFree(d_queues);
 		d_ctrl = nullptr;
@@ -897,6 +935,12 @@ struct Executor
 		L.blend_ctas = blend_ctas;
 		L.pair_log = sample ? d_pair_log : nullptr;
 		L.log_slot = sample ? uint32_t(tuner.samples_taken++ % 256) : 0u;
+		if (!sample && !cap && launch_log && tile_base && launch_log_pending.size() < kLaunchLogSlots)
+		{
+			L.pair_log = d_launch_pairs;
+			L.log_slot = uint32_t(launch_log_pending.size());
+			launch_log_pending.emplace_back(launches, L.log_slot);
+		}
 		L.spans = d_spans;
 		L.span_capacity = caps.span_rows;
 		L.prim_rows = d_prim_rows;

@@ -216,10 +216,4 @@ typedef struct __attribute__((aligned(16))) RdpPass
 	unsigned long long *counters; /* the instance's [0] fragments, [1] touched tiles, [2] tile instances */
 } RdpPass;
 
-/* Device-side error word bits (bounded waits and bounds checks report here). */
-enum
-{
-	RDP_DEVERR_BOUNDS = 1u << 0
-};
-
 #endif

@@ -65,3 +65,29 @@ def test_reference_arm_prints_its_contract_line():
     assert line["cpu_baseline"]["value"] == line["value"] and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"] == {"value": line["value"], "unit": "passes/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+
+
+def test_int_alu_roofline_reads_the_op_table_and_uses_the_issue_peak():
+    """roofline.int_alu: ops per step from oracle/op_table.json over the step time, against SMs x
+    128 lanes x the sampled clock; the shading kernel's figure uses the shading stages' ops."""
+    import json
+    sys.path.insert(0, ROOT)
+    import bench
+    table = json.load(open(os.path.join(ROOT, "oracle", "op_table.json")))["workloads"]["batched64"]
+    r = bench._int_alu_roofline("batched64", 20.0, 10.0, 152, 2000.0)
+    peak = 152 * 128 * 2000e6 / 1e12
+    assert abs(r["peak"] - peak) < 1e-9
+    assert abs(r["achieved"] - table["ops_total"] / 0.020 / 1e12) < 1e-6
+    assert abs(r["k_shade"]["achieved"] - table["ops_shading_stages"] / 0.010 / 1e12) < 1e-6
+    assert abs(r["frac"] - r["achieved"] / peak) < 1e-12
+    assert 0 < table["ops_shading_stages"] < table["ops_total"]
+    assert bench._int_alu_roofline("no such workload", 20.0, 10.0, 152, 2000.0) is None
+
+
+def test_step_hbm_roofline_counts_commands_tiles_and_texture_sources():
+    sys.path.insert(0, ROOT)
+    import bench
+    r = bench._step_hbm_roofline(1000, 10, 64 * 2 * 9, 3, 1.0, 8000.0, "fallback")
+    assert r["algorithmic_bytes_per_step"] == 1000 + 10 * 64 * 2 * 9 + 3 * 4096
+    assert abs(r["achieved"] - r["algorithmic_bytes_per_step"] / 1e-3 / 1e9) < 1e-9
+    assert abs(r["frac"] - r["achieved"] / 8000.0) < 1e-12

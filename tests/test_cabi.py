@@ -40,3 +40,21 @@ def test_no_cpu_fallback_when_library_missing(monkeypatch, tmp_path):
         assert "not built" in str(e)
     else:
         raise AssertionError("loading a missing library must fail")
+
+
+def test_enqueue_many_rejects_a_handle_given_twice():
+    """Two host threads on one instance's recorder would race: a handle that appears twice is
+    rejected before any handle is dereferenced or any thread starts (the handles here are
+    stand-in addresses, never valid processors)."""
+    lib = ctypes.CDLL(native.library_path())
+    f = lib.rdp_batch_enqueue_many
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p),
+                  ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_uint32), ctypes.c_void_p, ctypes.c_uint32]
+    words = (ctypes.c_uint32 * 2)(0x29 << 24, 0)
+    for handles in ([0x1000, 0x2000, 0x1000], [0x3000, 0x3000]):
+        n = len(handles)
+        insts = (ctypes.c_void_p * n)(*handles)
+        wptrs = (ctypes.c_void_p * n)(*([ctypes.addressof(words)] * n))
+        counts = (ctypes.c_uint32 * n)(*([2] * n))
+        assert f(ctypes.c_void_p(0x10), n, insts, wptrs, counts, None, 2) == native.RDP_ERR_INVALID

@@ -7,7 +7,9 @@ import re
 import numpy as np
 import pytest
 
-REF_LUTS = "/root/reference/parallel-rdp/luts.hpp"
+# The reference tree's luts.hpp, when a copy of the reference is present (RDP_REFERENCE_DIR, the
+# directory that holds parallel-rdp/); the checksum tests below run either way.
+REF_LUTS = os.path.join(os.environ.get("RDP_REFERENCE_DIR", "/nonexistent"), "parallel-rdp", "luts.hpp")
 # sha256 of the 32 KiB blender divider table and of the 16,640-entry gamma table.
 BLENDER_SHA256 = "8072c219888f51694d2cd13cef8e83db02f0a41c0be3ba039415c79374634a3d"
 GAMMA_SHA256 = "4879d9c57ad78e61759e10546fa8bba2bad70bcae1dd5b34b2d4c7b17a8c18a4"

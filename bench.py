@@ -706,8 +706,45 @@ def _serving(args, device, model=None):
                     "submits": st["submits"], "max_in_flight": st["max_in_flight"],
                     "max_footprint_gb": st["max_footprint"] / (1 << 30)})
         out[tag] = lat
+    out["parity_sample"] = _serving_parity_sample(insts, trace)
+    # Latency floor: the largest instance's frame alone on an idle GPU (one request, nothing else
+    # in flight), end to end through the serving loop.
+    big = max(range(len(streams)), key=lambda i: streams[i][2])
+    floor = []
+    for k in range(5):
+        res, _ = b.serve(insts, [(big, frames[big], 0.0)], hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)))
+        floor.append(float(res["latency_s"][0]) * 1e3)
+    out["latency_floor"] = {"instance": big, "primitives": int(streams[big][2]),
+                            "resolution": "%dx%d" % (streams[big][3].width, streams[big][3].height),
+                            "alone_ms_min": min(floor), "alone_ms_median": statistics.median(floor)}
     b.close()
     return out
+
+
+def _serving_parity_sample(insts, trace, fraction=0.01, seed=7):
+    """The serving configuration's output check: a seeded 1 % sample of the requests; each sampled
+    request's instance must hold the oracle's frame (RDRAM and hidden RDRAM digests committed in
+    tests/golden/configs.json by tests/golden/make_golden_configs.py).  Every frame of an instance
+    renders the same command words from a full-screen clear, so its image after the run is the
+    image of each of its frames."""
+    import hashlib
+    try:
+        golden = json.load(open(os.path.join(ROOT, "tests", "golden", "configs.json")))["instances"]
+    except (OSError, ValueError, KeyError):
+        return None
+    if not trace:
+        return {"requests_sampled": 0, "instances_checked": 0, "passed": False}
+    rng = np.random.default_rng(seed)
+    k = max(1, int(round(fraction * len(trace))))
+    picks = sorted(int(i) for i in rng.choice(len(trace), size=min(k, len(trace)), replace=False))
+    inst_ids = sorted({trace[i][0] for i in picks})
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).view(np.uint8).tobytes()).hexdigest()  # noqa: E731
+    bad = [i for i in inst_ids if i >= len(golden) or
+           sha(insts[i].begin_read_rdram()) != golden[i]["rdram_sha256"] or
+           sha(insts[i].begin_read_hidden_rdram()) != golden[i]["hidden_sha256"]]
+    return {"requests_sampled": len(picks), "of_requests": len(trace), "instances_checked": len(inst_ids),
+            "mismatches": bad, "passed": not bad,
+            "reference": "oracle digests (tests/golden/configs.json)"}
 
 
 def run_reference_batched(args):

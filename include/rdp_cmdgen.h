@@ -62,6 +62,9 @@ void rdpgen_destroy(void *g);
 uint32_t rdpgen_num_words(void *g);
 const uint32_t *rdpgen_words(void *g);
 uint32_t rdpgen_num_prims(void *g);
+/* Frames of the stream and the word index where frame `frame` begins (num_words past the last). */
+uint32_t rdpgen_num_frames(void *g);
+uint32_t rdpgen_frame_word_offset(void *g, uint32_t frame);
 /* Writes the generated texture/TLUT data into an RDRAM image (host-order words). */
 void rdpgen_init_rdram(void *g, uint8_t *rdram, uint32_t size);
 uint32_t rdpgen_color_addr(void);

@@ -226,6 +226,7 @@ struct Gen
 	rdpgen_params p;
 	Rng rng;
 	std::vector<uint32_t> words;
+	std::vector<uint32_t> frame_begin; // word index where each frame's prologue starts
 	struct Blob { uint32_t addr; std::vector<uint8_t> bytes; };
 	std::vector<Blob> blobs;
 	uint32_t prims = 0;
@@ -622,6 +623,7 @@ struct Gen
 	// ------------------------------------------------------------------ frames
 	void frame_prologue(uint32_t frame)
 	{
+		frame_begin.push_back(uint32_t(words.size()));
 		set_color_image(COLOR_ADDR, fb_size_bits(), p.width, fb_fmt_bits());
 		emit2(uint32_t(OP_SET_MASK_IMAGE) << 24, DEPTH_ADDR);
 		set_scissor(p.width, p.height);
@@ -1104,6 +1106,12 @@ void rdpgen_destroy(void *h) { delete static_cast<Gen *>(h); }
 uint32_t rdpgen_num_words(void *h) { return uint32_t(static_cast<Gen *>(h)->words.size()); }
 const uint32_t *rdpgen_words(void *h) { return static_cast<Gen *>(h)->words.data(); }
 uint32_t rdpgen_num_prims(void *h) { return static_cast<Gen *>(h)->prims; }
+uint32_t rdpgen_num_frames(void *h) { return uint32_t(static_cast<Gen *>(h)->frame_begin.size()); }
+uint32_t rdpgen_frame_word_offset(void *h, uint32_t frame)
+{
+	const Gen *g = static_cast<Gen *>(h);
+	return frame < g->frame_begin.size() ? g->frame_begin[frame] : uint32_t(g->words.size());
+}
 
 void rdpgen_init_rdram(void *h, uint8_t *rdram, uint32_t size)
 {

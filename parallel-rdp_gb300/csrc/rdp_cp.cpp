@@ -226,9 +226,13 @@ struct rdp_cp
 		std::vector<uint64_t> static_keys, depth_keys;
 	} ref;
 
-	// Sync-point capture: recorded launches with device-resident inputs.
+	// Sync-point capture: recorded launches with device-resident inputs.  capture_written keeps
+	// the RDRAM ranges the recorded passes write: every replay of the graph writes them again, so
+	// the replay marks them for copy-back like a pass does.
 	bool capturing = false;
 	rdpx::CaptureSink capture_sink;
+	std::vector<std::pair<uint32_t, uint32_t>> capture_written;
+	bool in_capture() const; // this processor's passes are being recorded (its own or its batch's capture)
 
 	uint32_t vi_regs[16] = {};
 	struct ViHost
@@ -439,6 +443,11 @@ struct rdp_cp
 		if (!bytes) return;
 		addr &= rdram_size - 1;
 		uint32_t end = std::min<uint64_t>(uint64_t(addr) + bytes, rdram_size);
+		if (in_capture()) capture_written.emplace_back(addr, end);
+		merge_dirty(addr, end);
+	}
+	void merge_dirty(uint32_t addr, uint32_t end)
+	{
 		for (auto &r : dirty_ranges)
 		{
 			if (addr <= r.second && end >= r.first)
@@ -1526,6 +1535,7 @@ struct rdp_batch
 };
 
 int rdp_cp::batch_submit() { return batch->submit(); }
+bool rdp_cp::in_capture() const { return capturing || (batch && batch->capturing); }
 
 // Recorded launches keep pointers to the executor's buffers, so the buffers are sized for
 // every round of a capture before the first one is recorded.
@@ -1778,6 +1788,11 @@ int rdp_cp_get_stats(rdp_cp *cp, rdp_stats *out)
 struct rdp_graph
 {
 	rdpx::Executor *exec = nullptr;
+	// The processors whose passes the graph replays and the RDRAM ranges those passes write
+	// (marked for copy-back after every replay).  A batch's graph looks its instances up in the
+	// batch at replay, so an instance destroyed since the capture is skipped.
+	rdp_batch *batch = nullptr;
+	std::vector<std::pair<rdp_cp *, std::vector<std::pair<uint32_t, uint32_t>>>> written;
 	uint64_t generation = 0;
 	rdp_stats *stats = nullptr; // receives kernel_launches, when the graph belongs to one processor
 	cudaGraph_t graph = nullptr;
@@ -1851,6 +1866,11 @@ int rdp_cp_capture_end(rdp_cp *cp, rdp_graph **out)
 	if (r != RDP_OK) return r;
 	r = build_graph(cp->exec, cp->capture_sink, &cp->stats, out);
 	if (r != RDP_OK) cp->sticky_error = r;
+	else
+	{
+		(*out)->written.emplace_back(cp, std::move(cp->capture_written));
+		cp->capture_written.clear();
+	}
 	return r;
 }
 
@@ -1867,6 +1887,15 @@ int rdp_graph_replay(rdp_graph *g, uint32_t count, float *elapsed_ms)
 	if (cudaEventSynchronize(g->ev[1]) != cudaSuccess) return RDP_ERR_DEVICE;
 	ex->kernel_launches += uint64_t(g->kernels) * count;
 	if (g->stats) g->stats->kernel_launches += uint64_t(g->kernels) * count;
+	// The replayed passes wrote their framebuffer ranges again: the next timeline value of each
+	// processor copies them back to its RDRAM.
+	for (auto &w : g->written)
+	{
+		if (g->batch && std::find(g->batch->instances.begin(), g->batch->instances.end(), w.first) ==
+		                    g->batch->instances.end())
+			continue;
+		for (auto &rg : w.second) w.first->merge_dirty(rg.first, rg.second);
+	}
 	if (elapsed_ms && cudaEventElapsedTime(elapsed_ms, g->ev[0], g->ev[1]) != cudaSuccess) return RDP_ERR_DEVICE;
 	// GPU time of the rasteriser launches of the last replay.
 	g->last_shade_ms = 0.0f;
@@ -2030,7 +2059,14 @@ int rdp_batch_capture_end(rdp_batch *b, rdp_graph **out)
 	int r = rdp_batch_submit(b);
 	b->capturing = false;
 	if (r != RDP_OK) return r;
-	return build_graph(&b->exec, b->sink, nullptr, out);
+	r = build_graph(&b->exec, b->sink, nullptr, out);
+	for (rdp_cp *cp : b->instances)
+	{
+		if (r == RDP_OK && !cp->capture_written.empty()) (*out)->written.emplace_back(cp, std::move(cp->capture_written));
+		cp->capture_written.clear();
+	}
+	if (r == RDP_OK) (*out)->batch = b;
+	return r;
 }
 
 int rdp_set_shade_variant(int device, int variant)

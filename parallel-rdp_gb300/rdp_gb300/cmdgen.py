@@ -50,6 +50,10 @@ def _load():
         L.rdpgen_words.argtypes = [ctypes.c_void_p]
         L.rdpgen_words.restype = ctypes.POINTER(ctypes.c_uint32)
         L.rdpgen_init_rdram.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32]
+        L.rdpgen_num_frames.argtypes = [ctypes.c_void_p]
+        L.rdpgen_num_frames.restype = ctypes.c_uint32
+        L.rdpgen_frame_word_offset.argtypes = [ctypes.c_void_p, ctypes.c_uint32]
+        L.rdpgen_frame_word_offset.restype = ctypes.c_uint32
         L.rdpgen_color_addr.restype = ctypes.c_uint32
         L.rdpgen_depth_addr.restype = ctypes.c_uint32
         _lib = L
@@ -74,6 +78,23 @@ def generate_stream(params):
         rdram = np.zeros(params.rdram_size, dtype=np.uint8)
         L.rdpgen_init_rdram(g, rdram.ctypes.data, rdram.size)
         return words, rdram, L.rdpgen_num_prims(g)
+    finally:
+        L.rdpgen_destroy(g)
+
+
+def generate_frames(params):
+    """Returns (words, rdram_init, num_prims, frame_offsets): frame f's words are
+    words[frame_offsets[f]:frame_offsets[f + 1]]."""
+    L = _load()
+    g = L.rdpgen_build(ctypes.byref(params))
+    try:
+        n = L.rdpgen_num_words(g)
+        words = np.ctypeslib.as_array(L.rdpgen_words(g), shape=(n,)).copy()
+        rdram = np.zeros(params.rdram_size, dtype=np.uint8)
+        L.rdpgen_init_rdram(g, rdram.ctypes.data, rdram.size)
+        nf = L.rdpgen_num_frames(g)
+        offsets = [L.rdpgen_frame_word_offset(g, f) for f in range(nf + 1)]
+        return words, rdram, L.rdpgen_num_prims(g), offsets
     finally:
         L.rdpgen_destroy(g)
 

@@ -61,3 +61,27 @@ def test_gpu_vi_golden(name):
     case = GOLDEN["vi"][name]
     with CommandProcessor(np.zeros(8 << 20, np.uint8)) as cp:
         assert mg.vi_frames(case["variant"], len(case["frames"]), cp) == case["frames"]
+
+
+CONFIGS = json.load(open(os.path.join(HERE, "golden", "configs.json")))
+
+
+def test_configs_golden_generator_and_oracle_still_agree():
+    """CPU side of tests/golden/configs.json: the generator still produces the committed command
+    words of the benchmark-size configurations, and the oracle still renders the smallest batched
+    instance to the committed digests."""
+    from oracle import Oracle
+    b = CONFIGS["instances"][:64]
+    for g in b[:4]:
+        words, _, prims = cmdgen.generate_stream(cmdgen.batched_instance_params(g["instance"]))
+        assert mg.sha(words) == g["words_sha256"] and prims == g["primitives"]
+    small = min(b, key=lambda g: g["primitives"])
+    words, rdram, _ = cmdgen.generate_stream(cmdgen.batched_instance_params(small["instance"]))
+    o = Oracle(8 << 20)
+    o.write_rdram(rdram)
+    o.enqueue(words)
+    assert mg.sha(o.rdram()) == small["rdram_sha256"] and mg.sha(o.hidden()) == small["hidden_sha256"]
+    assert o.fragments() == small["fragments"] and o.reference_passes() == small["reference_passes"]
+    o.close()
+    words, _, _, offsets = cmdgen.generate_frames(cmdgen.default_params(cmdgen.CONFIG_MIXED))
+    assert mg.sha(words) == CONFIGS["mixed16"]["words_sha256"] and len(offsets) == 17

@@ -7,10 +7,13 @@
  * no exception or C++ type crosses it.  Each function names the reference
  * interface it replaces.
  *
- * Threading: a processor is used from one emulator thread at a time.  Command
- * words are decoded synchronously by the calling thread (the reference's
- * PARALLEL_RDP_SINGLE_THREADED_COMMAND mode, rdp_device.cpp:144-158); GPU work
- * is asynchronous and tracked by a monotonically increasing 64-bit timeline.
+ * Threading: a processor is used from one emulator thread at a time.  By default
+ * command words are decoded synchronously by the calling thread (the reference's
+ * PARALLEL_RDP_SINGLE_THREADED_COMMAND mode, rdp_device.cpp:144-158); with
+ * RDP_CREATE_COMMAND_THREAD they go through a 4096-word ring to a decoder thread
+ * of the processor, as in the reference's default mode (command_ring.cpp:71-134).
+ * GPU work is asynchronous and tracked by a monotonically increasing 64-bit
+ * timeline.
  *
  * RDRAM ownership: the caller owns RDRAM (rdp_device.cpp:81-87).  The
  * authoritative copy lives in device memory (HBM).  The caller's buffer is
@@ -65,9 +68,22 @@ typedef struct rdp_create_info
 	size_t rdram_offset;      /* byte offset of RDRAM inside `rdram` */
 	size_t rdram_size;        /* power of two, e.g. 8 MiB */
 	size_t hidden_rdram_size; /* power of two, normally rdram_size / 2 */
-	uint32_t flags;           /* reserved, must be 0 */
+	uint32_t flags;           /* RDP_CREATE_* (batch instances: 0) */
 	int device;               /* CUDA device ordinal */
 } rdp_create_info;
+
+/* Creation flags. */
+enum
+{
+	/* Decode command words on a thread of the processor (the reference's command ring,
+	 * command_ring.cpp:71-134; rdp_device.cpp:144-158).  rdp_cp_enqueue, rdp_cp_signal_timeline,
+	 * rdp_cp_flush and rdp_cp_set_quirks push into a 4096-word ring (blocking while it is full) and
+	 * return; timeline values travel in band (MetaSignalTimeline) and rdp_cp_wait_timeline may be
+	 * called while the thread decodes.  Calls that read or write processor state directly (RDRAM
+	 * and TMEM access, scanout, statistics) first wait until the ring is drained.  Not for batch
+	 * instances or sync-point captures. */
+	RDP_CREATE_COMMAND_THREAD = 1u << 0
+};
 
 /* CommandProcessor::CommandProcessor (rdp_device.cpp:44-162). */
 int rdp_cp_create(const rdp_create_info *info, rdp_cp **out);
@@ -78,7 +94,11 @@ int rdp_device_is_supported(int device);
 
 /* CommandProcessor::enqueue_command (rdp_device.cpp:874-897).  Accepts any
  * number of whole or partial commands; a trailing partial command is kept until
- * the rest of its words arrive. */
+ * the rest of its words arrive.  The in-band meta ops of the reference's command
+ * stream (rdp_common.hpp:37-43; rdp_device.cpp:926-952) are decoded too:
+ * MetaSignalTimeline (op 1, three words: the op word, then the 64-bit value, low
+ * word first), MetaFlush (op 2, one word), MetaIdle (op 3, one word; a hint with
+ * no effect here) and MetaSetQuirks (op 4, two words). */
 int rdp_cp_enqueue(rdp_cp *cp, uint32_t num_words, const uint32_t *words);
 
 /* CommandProcessor::signal_timeline (rdp_device.cpp:1053-1065). */
@@ -130,6 +150,37 @@ void rdp_scanout_options_default(rdp_scanout_options *opts);
  * state).  opts may be NULL for the defaults. */
 int rdp_cp_scanout_sync(rdp_cp *cp, const rdp_scanout_options *opts, uint32_t *rgba_out, uint32_t *width,
                         uint32_t *height);
+/* A scanned-out image in device memory: width x height RGBA8 pixels (r | g << 8 | b << 16 | a << 24),
+ * rows of `width` pixels.  Owned by the processor. */
+typedef struct rdp_vi_image
+{
+	const uint32_t *pixels; /* device pointer; NULL: no image (blank or invalid VI state) */
+	uint32_t width, height;
+} rdp_vi_image;
+/* CommandProcessor::scanout (rdp_device.cpp:1082-1128): renders everything queued and runs the VI
+ * filters on the device; the reference returns a Vulkan image, this returns the image in device
+ * memory.  The VI work has finished when the call returns.  The image stays valid until the second
+ * scanout after this one (two images alternate: the previous one is the source of the
+ * previous-frame blend). */
+int rdp_cp_scanout(rdp_cp *cp, const rdp_scanout_options *opts, rdp_vi_image *out);
+
+/* VIScanoutBuffer (video_interface.hpp:83-89): a host copy of a scanout and the fence of that copy.
+ * Zero-initialise before first use; the library (re)allocates `pixels` (pinned host memory) and
+ * creates `fence`; rdp_vi_scanout_buffer_release frees both. */
+typedef struct rdp_vi_scanout_buffer
+{
+	uint32_t *pixels;       /* width x height RGBA8 pixels once the fence has completed */
+	size_t capacity_pixels;
+	uint32_t width, height; /* 0 x 0: no image */
+	void *fence;            /* the copy's completion event */
+} rdp_vi_scanout_buffer;
+/* CommandProcessor::scanout_async_buffer (rdp_device.cpp:1130-1158): queues the scanout and the copy
+ * of the image into `buf` and returns without waiting for them. */
+int rdp_cp_scanout_async_buffer(rdp_cp *cp, const rdp_scanout_options *opts, rdp_vi_scanout_buffer *buf);
+/* Waits for the buffer's copy (the reference's buffer.fence->wait()), bounded by timeout_ns. */
+int rdp_vi_scanout_buffer_wait(rdp_vi_scanout_buffer *buf, uint64_t timeout_ns);
+void rdp_vi_scanout_buffer_release(rdp_vi_scanout_buffer *buf);
+
 /* Per-scanline HStart/XScale (video_interface.hpp PerScanlineRegisterBits: 1 = HStart, 2 = XScale):
  * CommandProcessor::begin/set/latch/end_vi_register_per_scanline (rdp_device.cpp:977-995). */
 int rdp_cp_begin_vi_register_per_scanline(rdp_cp *cp, uint32_t flags);
@@ -159,7 +210,10 @@ int rdp_cp_get_stats(rdp_cp *cp, rdp_stats *out);
  * Between rdp_cp_capture_begin and rdp_cp_capture_end, flushed passes are not run:
  * their command data is copied once into device memory and their kernels are
  * recorded.  rdp_graph_replay launches the recorded kernels `count` times on the
- * processor's stream, with every input already resident in HBM, and waits. */
+ * processor's stream, with every input already resident in HBM, and waits.  The framebuffer
+ * ranges the recorded passes write are copied back to the caller's RDRAM with the processor's
+ * next timeline value (as for passes run normally).  A graph is destroyed before its processor
+ * (a batch's graph skips instances destroyed since the capture). */
 typedef struct rdp_graph rdp_graph;
 int rdp_cp_capture_begin(rdp_cp *cp);
 int rdp_cp_capture_end(rdp_cp *cp, rdp_graph **out);
@@ -314,12 +368,15 @@ int rdp_dump_writer_signal_complete(rdp_dump_writer *w);
 int rdp_dump_writer_close(rdp_dump_writer *w);
 int rdp_dump_replay(rdp_cp *cp, const char *path, rdp_dump_frame_cb on_frame, void *user, uint32_t *frames);
 
-/* Kernel specialisation.  No counterpart in the reference (its shaders are specialised per
- * render-state variant by its pipeline compiler).  The shading kernel is compiled for
- * RDP_SHADE_VARIANTS variants (two kernel shapes and several register budgets); by default an
- * autotuner times them on the first launches of a device and keeps the fastest per shaded
- * (primitive, tile) pair.  All variants give identical results.  rdp_set_shade_variant forces
- * one (0..7) or restarts tuning (-1); rdp_get_shade_variant returns the device's choice, -1 while tuning. */
+/* Kernel specialisation.  The reference compiles its shading shaders per normalised static render
+ * state with specialisation constants (rdp_renderer.cpp:1294-1331, 1790-1822).  Here the shading
+ * kernel is compiled for RDP_SHADE_VARIANTS variants: 0-3 run one general shader for every
+ * primitive, 4-7 dispatch each primitive to separately compiled code for its render-state class
+ * (fill, copy, untextured, one texel, one texel through a TLUT, two texels, LOD; others take the
+ * general shader), each at register budgets for 16, 18, 20 and 24 resident CTAs per SM.  By default
+ * an autotuner times them on the first launches of a device and keeps the fastest per shaded
+ * (primitive, tile) pair.  All variants give identical results.  rdp_set_shade_variant forces one
+ * (0..7) or restarts tuning (-1); rdp_get_shade_variant returns the device's choice, -1 while tuning. */
 #define RDP_SHADE_VARIANTS 8
 int rdp_set_shade_variant(int device, int variant);
 int rdp_get_shade_variant(int device);

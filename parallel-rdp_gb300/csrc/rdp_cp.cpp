@@ -24,6 +24,8 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
+#include <functional>
 #include <deque>
 #include <mutex>
 #include <thread>
@@ -47,10 +49,16 @@ constexpr uint32_t kMaxTilesets = 4096;
 constexpr uint32_t kMaxTiles = RDP_MAX_TILES_X * RDP_MAX_TILES_Y;
 
 
+// Words of a command (rdp_device.cpp command lengths); the in-band meta ops share the stream
+// (rdp_common.hpp:37-43): MetaSignalTimeline carries a 64-bit value, MetaFlush and MetaIdle are
+// one word, MetaSetQuirks two.
 static uint32_t command_length(uint32_t op)
 {
 	switch (op)
 	{
+	case 0x01: return 3;
+	case 0x02:
+	case 0x03: return 1;
 	case 0x08: return 8;
 	case 0x09: return 12;
 	case 0x0a: return 24;
@@ -94,6 +102,100 @@ static cudaError_t ensure_luts(int device)
 	if (e == cudaSuccess) g_lut_devices.push_back(device);
 	return e;
 }
+
+// The command thread's ring (command_ring.cpp:71-134): the emulator thread pushes command words,
+// blocking while the ring is full; one worker thread decodes them in order.  drain() returns once
+// every pushed word has been decoded.  A chunk longer than the ring is pushed in pieces (the
+// decoder carries a partial command over to the next piece).
+class CommandRing
+{
+public:
+	static constexpr uint32_t kWords = 4096;
+
+	void start(std::function<void(uint32_t, const uint32_t *)> consume)
+	{
+		consume_ = std::move(consume);
+		ring_.assign(kWords, 0u);
+		worker_ = std::thread([this] { loop(); });
+	}
+
+	void push(uint32_t n, const uint32_t *w)
+	{
+		while (n)
+		{
+			const uint32_t k = std::min<uint32_t>(n, kWords - 1);
+			std::unique_lock<std::mutex> lk(mu_);
+			cv_.wait(lk, [&] { return write_ + k + 1 <= read_ + kWords; });
+			ring_[write_++ % kWords] = k;
+			for (uint32_t i = 0; i < k; i++) ring_[write_++ % kWords] = w[i];
+			cv_.notify_all();
+			n -= k;
+			w += k;
+		}
+	}
+
+	void drain()
+	{
+		std::unique_lock<std::mutex> lk(mu_);
+		cv_.wait(lk, [&] { return completed_ == write_; });
+	}
+
+	// Waits until pred() holds (checked after each decoded chunk) or the deadline passes.
+	template <class Pred>
+	bool wait_until(Pred pred, std::chrono::steady_clock::time_point deadline, bool bounded)
+	{
+		std::unique_lock<std::mutex> lk(mu_);
+		if (!bounded)
+		{
+			cv_.wait(lk, pred);
+			return true;
+		}
+		return cv_.wait_until(lk, deadline, pred);
+	}
+
+	void stop()
+	{
+		if (!worker_.joinable()) return;
+		{
+			std::lock_guard<std::mutex> lk(mu_);
+			stop_ = true;
+		}
+		cv_.notify_all();
+		worker_.join();
+	}
+
+	std::mutex &mutex() { return mu_; }
+
+private:
+	void loop()
+	{
+		std::vector<uint32_t> chunk;
+		for (;;)
+		{
+			{
+				std::unique_lock<std::mutex> lk(mu_);
+				cv_.wait(lk, [&] { return stop_ || write_ > read_; });
+				if (write_ == read_ && stop_) return;
+				const uint32_t k = ring_[read_++ % kWords];
+				chunk.resize(k);
+				for (uint32_t i = 0; i < k; i++) chunk[i] = ring_[read_++ % kWords];
+				cv_.notify_all(); // room for the producer
+			}
+			consume_(uint32_t(chunk.size()), chunk.data());
+			std::lock_guard<std::mutex> lk(mu_);
+			completed_ = read_;
+			cv_.notify_all();
+		}
+	}
+
+	std::function<void(uint32_t, const uint32_t *)> consume_;
+	std::vector<uint32_t> ring_;
+	uint64_t write_ = 0, read_ = 0, completed_ = 0;
+	bool stop_ = false;
+	std::mutex mu_;
+	std::condition_variable cv_;
+	std::thread worker_;
+};
 
 } // namespace
 
@@ -252,12 +354,22 @@ struct rdp_cp
 		uint32_t *d_aa = nullptr, *d_dv = nullptr, *d_out[2] = { nullptr, nullptr };
 		size_t aa_cap = 0, dv_cap = 0;
 		int cur = 0;
-		RdpViLine *d_lines = nullptr;
+		RdpViLine *d_lines = nullptr, *h_lines = nullptr;
+		cudaEvent_t lines_copied = nullptr;
 		bool tables = false;
 	} vi;
 	rdp_validation_cb validation_cb = nullptr;
 	void *validation_user = nullptr;
 	int sticky_error = RDP_OK;
+
+	// Command thread (RDP_CREATE_COMMAND_THREAD): the C ABI pushes words into the ring and the
+	// worker decodes them; timeline values are handed out by the caller (api_value) and travel
+	// in band (MetaSignalTimeline), decoded_value is the last one the worker has reached.  The
+	// pending-event list is shared between the worker (signal) and the waiting caller.
+	CommandRing *ring = nullptr;
+	uint64_t api_value = 0;
+	std::atomic<uint64_t> decoded_value{ 0 };
+	std::mutex timeline_mu;
 
 	// ================================================================= helpers
 	void report(int err, const char *msg)
@@ -389,6 +501,8 @@ struct rdp_cp
 		cudaFree(vi.d_out[0]);
 		cudaFree(vi.d_out[1]);
 		cudaFree(vi.d_lines);
+		if (vi.h_lines) cudaFreeHost(vi.h_lines);
+		if (vi.lines_copied) cudaEventDestroy(vi.lines_copied);
 		if (host_registered) cudaHostUnregister(host_rdram);
 		if (own_host_rdram) free(host_rdram);
 		if (stream && !batch) cudaStreamDestroy(stream);
@@ -946,6 +1060,14 @@ struct rdp_cp
 		uint32_t op = (w[0] >> 24) & 63;
 		switch (op)
 		{
+		case 0x01: // MetaSignalTimeline (rdp_device.cpp:926-934): words 1-2 are the value
+			signal_value(uint64_t(w[1]) | (uint64_t(w[2]) << 32));
+			break;
+		case 0x02: // MetaFlush (rdp_device.cpp:936-940)
+			hard_flush();
+			break;
+		case 0x03: // MetaIdle (rdp_device.cpp:942-946): a hint that the command stream went quiet;
+			break;  // this processor submits at flushes and timeline values, so nothing is pending
 		case 0x04: // MetaSetQuirks (rdp_device.cpp:948-952)
 			if (sb[SB_QUIRKS] != w[1]) { sb[SB_QUIRKS] = w[1]; sb_dirty = true; }
 			break;
@@ -1145,9 +1267,22 @@ struct rdp_cp
 		return RDP_OK;
 	}
 
-	// VideoInterface::scanout (video_interface.cpp:1215-1426) at 1x scale.
+	// VideoInterface::scanout (video_interface.cpp:1215-1426) at 1x scale, into `out` (host).
 	int scanout(const rdp_scanout_options *o, uint32_t *out, uint32_t *width, uint32_t *height)
 	{
+		const uint32_t *img = nullptr;
+		int r = scanout_device(o, &img, width, height);
+		if (r != RDP_OK || !img) return r;
+		if (check(cudaMemcpyAsync(out, img, size_t(*width) * *height * 4, cudaMemcpyDeviceToHost, stream))) return sticky_error;
+		return check(cudaStreamSynchronize(stream));
+	}
+
+	// The scanout image in device memory (*img = nullptr: no image).  The VI kernels are queued on
+	// the processor's stream; the image is one of two that alternate (the other is the previous
+	// frame, which the next scanout may blend with).
+	int scanout_device(const rdp_scanout_options *o, const uint32_t **img, uint32_t *width, uint32_t *height)
+	{
+		*img = nullptr;
 		*width = *height = 0;
 		int r0 = sync_point();
 		if (r0 != RDP_OK) return r0;
@@ -1195,7 +1330,8 @@ struct rdp_cp
 			{
 				*width = uint32_t(vi.prev_w);
 				*height = uint32_t(vi.prev_h);
-				return check(cudaMemcpy(out, vi.d_out[vi.cur ^ 1], size_t(vi.prev_w) * vi.prev_h * 4, cudaMemcpyDeviceToHost));
+				*img = vi.d_out[vi.cur ^ 1];
+				return RDP_OK;
 			}
 			vi.have_prev = false;
 			return RDP_OK;
@@ -1288,10 +1424,19 @@ struct rdp_cp
 		p.gamma = (r.status & (1u << 3)) != 0;
 		p.gamma_dither = (r.status & (1u << 2)) != 0;
 		p.blend_prev = vi.have_prev && o->blend_previous_frame;
-		if (check(cudaMemcpyAsync(vi.d_lines, lines, sizeof(lines), cudaMemcpyHostToDevice, stream))) return sticky_error;
+		// The per-line registers are copied from pinned memory that the next scanout rewrites only
+		// after this copy has finished.
+		if (vi.lines_copied && check(cudaEventSynchronize(vi.lines_copied))) return sticky_error;
+		if (!vi.h_lines)
+		{
+			if (check(cudaMallocHost(&vi.h_lines, sizeof(lines)))) return RDP_ERR_OOM;
+			if (check(cudaEventCreateWithFlags(&vi.lines_copied, cudaEventDisableTiming))) return sticky_error;
+		}
+		memcpy(vi.h_lines, lines, sizeof(lines));
+		if (check(cudaMemcpyAsync(vi.d_lines, vi.h_lines, sizeof(lines), cudaMemcpyHostToDevice, stream))) return sticky_error;
+		if (check(cudaEventRecord(vi.lines_copied, stream))) return sticky_error;
 		if (check(rdp_vi_launch(&p, stream))) return sticky_error;
-		if (check(cudaMemcpyAsync(out, p.out, size_t(w) * h * 4, cudaMemcpyDeviceToHost, stream))) return sticky_error;
-		if (check(cudaStreamSynchronize(stream))) return sticky_error;
+		*img = p.out;
 		*width = uint32_t(w);
 		*height = uint32_t(h);
 		vi.prev_w = w;
@@ -1411,21 +1556,33 @@ struct rdp_cp
 
 	int signal_timeline(uint64_t *value)
 	{
+		const uint64_t v = timeline_counter + 1;
+		int r = signal_value(v);
+		if (value) *value = v;
+		return r;
+	}
+
+	// Everything recorded so far completes with timeline value v (values only grow: a value not
+	// above the current one completes together with it).
+	int signal_value(uint64_t v)
+	{
 		if (hard_flush() != RDP_OK) return sticky_error;
+		v = std::max(v, timeline_counter);
+		timeline_counter = v;
 		if (batch)
 		{
-			uint64_t v = ++timeline_counter;
 			unsubmitted.push_back(v);
-			if (value) *value = v;
 			return sticky_error;
 		}
 		if (copy_back() != RDP_OK) return sticky_error;
-		cudaEvent_t e = get_event();
-		if (!e) return RDP_ERR_DEVICE;
-		if (check(cudaEventRecord(e, stream))) return sticky_error;
-		uint64_t v = ++timeline_counter;
-		pending.emplace_back(v, e);
-		if (value) *value = v;
+		{
+			std::lock_guard<std::mutex> hold(timeline_mu);
+			cudaEvent_t e = get_event();
+			if (!e) return RDP_ERR_DEVICE;
+			if (check(cudaEventRecord(e, stream))) return sticky_error;
+			pending.emplace_back(v, e);
+		}
+		decoded_value.store(v);
 		return RDP_OK;
 	}
 
@@ -1447,7 +1604,23 @@ struct rdp_cp
 		}
 		const bool bounded = timeout_ns < (uint64_t(1) << 50);
 		auto deadline = std::chrono::steady_clock::now() + std::chrono::nanoseconds(bounded ? int64_t(timeout_ns) : 0);
-		while (!pending.empty() && pending.front().first <= value)
+		if (ring)
+		{
+			// The worker must first have decoded the value's MetaSignalTimeline.  A value above the
+			// ones handed out here can only come in band: once everything pushed is decoded (the
+			// worker then waits, so its counter can be read), it is known or never signalled.
+			if (value > api_value)
+			{
+				ring->drain();
+				if (value > timeline_counter) return RDP_ERR_INVALID;
+			}
+			else if (!ring->wait_until([&] { return decoded_value.load() >= value; }, deadline, bounded))
+				return RDP_ERR_TIMEOUT;
+		}
+		// Values complete in order; `value` has completed once a value at or above it has (a value
+		// signalled in band may be larger than the caller's own next one).
+		std::unique_lock<std::mutex> hold(timeline_mu);
+		while (!pending.empty() && completed_value < value)
 		{
 			cudaEvent_t e = pending.front().second;
 			for (;;)
@@ -1456,24 +1629,85 @@ struct rdp_cp
 				if (q == cudaSuccess) break;
 				if (q != cudaErrorNotReady) return check(q);
 				if (bounded && std::chrono::steady_clock::now() >= deadline) return RDP_ERR_TIMEOUT;
+				hold.unlock();
 				std::this_thread::yield();
+				hold.lock();
+				if (pending.empty() || pending.front().second != e) break; // another waiter took it
 			}
+			if (pending.empty() || pending.front().second != e) continue;
 			completed_value = pending.front().first;
 			free_events.push_back(e);
 			pending.pop_front();
 		}
-		if (value > timeline_counter) return RDP_ERR_INVALID;
+		if (!ring && value > timeline_counter) return RDP_ERR_INVALID;
 		return sticky_error;
 	}
 
 	int idle()
 	{
+		if (ring)
+		{
+			uint64_t v = 0;
+			int r = api_signal(&v);
+			if (r == RDP_OK) r = wait_timeline(v, UINT64_MAX / 2);
+			if (r == RDP_OK) own_exec.tune_epoch();
+			return r;
+		}
 		uint64_t v = 0;
 		int r = signal_timeline(&v);
 		if (r != RDP_OK) return r;
 		r = wait_timeline(v, UINT64_MAX / 2);
 		if (r == RDP_OK && !batch) own_exec.tune_epoch();
 		return r;
+	}
+
+	// ---------------------------------------------------------------- C ABI side of the command thread
+	// Without a command thread these decode on the calling thread.
+	int api_enqueue(uint32_t n, const uint32_t *w)
+	{
+		if (!ring) return enqueue(n, w);
+		ring->push(n, w);
+		return sticky_error;
+	}
+	int api_signal(uint64_t *value)
+	{
+		if (!ring) return signal_timeline(value);
+		const uint64_t v = ++api_value;
+		const uint32_t w[3] = { 0x01u << 24, uint32_t(v), uint32_t(v >> 32) };
+		ring->push(3, w);
+		if (value) *value = v;
+		return sticky_error;
+	}
+	int api_flush()
+	{
+		if (!ring) return hard_flush();
+		const uint32_t w[1] = { 0x02u << 24 };
+		ring->push(1, w);
+		return sticky_error;
+	}
+	// Before the caller touches decoder or device state directly: every pushed word is decoded
+	// and the worker waits for more.
+	void sync_ring()
+	{
+		if (ring) ring->drain();
+	}
+	int start_command_thread()
+	{
+		ring = new (std::nothrow) CommandRing();
+		if (!ring) return RDP_ERR_OOM;
+		ring->start([this](uint32_t n, const uint32_t *w) {
+			cudaSetDevice(device);
+			enqueue(n, w);
+		});
+		return RDP_OK;
+	}
+	void stop_command_thread()
+	{
+		if (!ring) return;
+		ring->drain();
+		ring->stop();
+		delete ring;
+		ring = nullptr;
 	}
 };
 
@@ -1582,12 +1816,13 @@ int rdp_cp_create(const rdp_create_info *info, rdp_cp **out)
 	if (!info || !out) return RDP_ERR_INVALID;
 	*out = nullptr;
 	size_t rs = info->rdram_size, hs = info->hidden_rdram_size;
-	if (!rs || (rs & (rs - 1)) || !hs || (hs & (hs - 1)) || rs > (64u << 20) || info->flags != 0)
+	if (!rs || (rs & (rs - 1)) || !hs || (hs & (hs - 1)) || rs > (64u << 20) || (info->flags & ~uint32_t(RDP_CREATE_COMMAND_THREAD)))
 		return RDP_ERR_INVALID;
 	if (!rdp_device_is_supported(info->device)) return RDP_ERR_UNSUPPORTED;
 	rdp_cp *cp = new (std::nothrow) rdp_cp();
 	if (!cp) return RDP_ERR_OOM;
 	int r = cp->init(info);
+	if (r == RDP_OK && (info->flags & RDP_CREATE_COMMAND_THREAD)) r = cp->start_command_thread();
 	if (r != RDP_OK)
 	{
 		cp->destroy();
@@ -1602,6 +1837,7 @@ void rdp_cp_destroy(rdp_cp *cp)
 {
 	if (!cp) return;
 	cudaSetDevice(cp->device);
+	cp->stop_command_thread();
 	if (cp->batch)
 	{
 		// Finish the instance's deferred work (the batch's other instances keep theirs).
@@ -1617,14 +1853,14 @@ int rdp_cp_enqueue(rdp_cp *cp, uint32_t num_words, const uint32_t *words)
 {
 	if (!cp || (num_words && !words)) return RDP_ERR_INVALID;
 	cudaSetDevice(cp->device);
-	return cp->enqueue(num_words, words);
+	return cp->api_enqueue(num_words, words);
 }
 
 int rdp_cp_signal_timeline(rdp_cp *cp, uint64_t *value)
 {
 	if (!cp) return RDP_ERR_INVALID;
 	cudaSetDevice(cp->device);
-	return cp->signal_timeline(value);
+	return cp->api_signal(value);
 }
 
 int rdp_cp_wait_timeline(rdp_cp *cp, uint64_t value, uint64_t timeout_ns)
@@ -1638,7 +1874,7 @@ int rdp_cp_flush(rdp_cp *cp)
 {
 	if (!cp) return RDP_ERR_INVALID;
 	cudaSetDevice(cp->device);
-	return cp->hard_flush();
+	return cp->api_flush();
 }
 
 int rdp_cp_idle(rdp_cp *cp)
@@ -1652,14 +1888,15 @@ int rdp_cp_begin_frame_context(rdp_cp *cp)
 {
 	if (!cp) return RDP_ERR_INVALID;
 	cudaSetDevice(cp->device);
-	return cp->hard_flush();
+	return cp->api_flush();
 }
 
 int rdp_cp_set_quirks(rdp_cp *cp, uint32_t quirks)
 {
 	if (!cp) return RDP_ERR_INVALID;
 	const uint32_t w[2] = { 0x04u << 24, quirks };
-	return cp->enqueue(2, w);
+	cudaSetDevice(cp->device);
+	return cp->api_enqueue(2, w);
 }
 
 int rdp_cp_set_validation_callback(rdp_cp *cp, rdp_validation_cb cb, void *user)
@@ -1674,6 +1911,7 @@ void *rdp_cp_begin_read_rdram(rdp_cp *cp)
 {
 	if (!cp) return nullptr;
 	cudaSetDevice(cp->device);
+	cp->sync_ring();
 	if (cp->idle() != RDP_OK) return nullptr;
 	return cp->host_rdram;
 }
@@ -1681,6 +1919,7 @@ void *rdp_cp_begin_read_rdram(rdp_cp *cp)
 int rdp_cp_end_write_rdram(rdp_cp *cp)
 {
 	if (!cp) return RDP_ERR_INVALID;
+	cp->sync_ring();
 	cp->host_rdram_dirty = true;
 	return RDP_OK;
 }
@@ -1689,6 +1928,7 @@ void *rdp_cp_begin_read_hidden_rdram(rdp_cp *cp)
 {
 	if (!cp) return nullptr;
 	cudaSetDevice(cp->device);
+	cp->sync_ring();
 	if (cp->idle() != RDP_OK) return nullptr;
 	if (cudaMemcpy(cp->hidden_mirror.data(), cp->d_hidden, cp->hidden_size, cudaMemcpyDeviceToHost) != cudaSuccess)
 		return nullptr;
@@ -1699,6 +1939,7 @@ int rdp_cp_end_write_hidden_rdram(rdp_cp *cp)
 {
 	if (!cp) return RDP_ERR_INVALID;
 	cudaSetDevice(cp->device);
+	cp->sync_ring();
 	if (cp->idle() != RDP_OK) return cp->sticky_error;
 	return cp->check(cudaMemcpy(cp->d_hidden, cp->hidden_mirror.data(), cp->hidden_size, cudaMemcpyHostToDevice));
 }
@@ -1710,6 +1951,7 @@ int rdp_cp_get_tmem(rdp_cp *cp, uint16_t *out)
 {
 	if (!cp || !out) return RDP_ERR_INVALID;
 	cudaSetDevice(cp->device);
+	cp->sync_ring();
 	int r = cp->idle();
 	if (r != RDP_OK) return r;
 	return cp->check(cudaMemcpy(out, cp->d_tmem, 4096, cudaMemcpyDeviceToHost));
@@ -1737,7 +1979,89 @@ int rdp_cp_scanout_sync(rdp_cp *cp, const rdp_scanout_options *opts, uint32_t *r
 	rdp_scanout_options defaults;
 	rdp_scanout_options_default(&defaults);
 	cudaSetDevice(cp->device);
+	cp->sync_ring(); // scanout drains the command ring first (rdp_device.cpp:1085)
 	return cp->scanout(opts ? opts : &defaults, rgba_out, width, height);
+}
+
+int rdp_cp_scanout(rdp_cp *cp, const rdp_scanout_options *opts, rdp_vi_image *out)
+{
+	if (!cp || !out) return RDP_ERR_INVALID;
+	rdp_scanout_options defaults;
+	rdp_scanout_options_default(&defaults);
+	cudaSetDevice(cp->device);
+	cp->sync_ring();
+	*out = rdp_vi_image{};
+	const uint32_t *img = nullptr;
+	uint32_t w = 0, h = 0;
+	int r = cp->scanout_device(opts ? opts : &defaults, &img, &w, &h);
+	if (r == RDP_OK) r = cp->check(cudaStreamSynchronize(cp->stream));
+	if (r == RDP_OK && img) *out = rdp_vi_image{ img, w, h };
+	return r;
+}
+
+int rdp_cp_scanout_async_buffer(rdp_cp *cp, const rdp_scanout_options *opts, rdp_vi_scanout_buffer *buf)
+{
+	if (!cp || !buf) return RDP_ERR_INVALID;
+	rdp_scanout_options defaults;
+	rdp_scanout_options_default(&defaults);
+	cudaSetDevice(cp->device);
+	cp->sync_ring();
+	// A previous copy into the buffer must have finished before it is reused or grown.
+	if (buf->fence && cp->check(cudaEventSynchronize(static_cast<cudaEvent_t>(buf->fence)))) return cp->sticky_error;
+	const uint32_t *img = nullptr;
+	uint32_t w = 0, h = 0;
+	int r = cp->scanout_device(opts ? opts : &defaults, &img, &w, &h);
+	buf->width = buf->height = 0;
+	if (r != RDP_OK || !img) return r;
+	const size_t n = size_t(w) * h;
+	if (buf->capacity_pixels < n)
+	{
+		if (buf->pixels) cudaFreeHost(buf->pixels);
+		buf->pixels = nullptr;
+		buf->capacity_pixels = 0;
+		if (cp->check(cudaMallocHost(&buf->pixels, n * 4))) return RDP_ERR_OOM;
+		buf->capacity_pixels = n;
+	}
+	if (!buf->fence)
+	{
+		cudaEvent_t e = nullptr;
+		if (cp->check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming))) return cp->sticky_error;
+		buf->fence = e;
+	}
+	if (cp->check(cudaMemcpyAsync(buf->pixels, img, n * 4, cudaMemcpyDeviceToHost, cp->stream)) ||
+	    cp->check(cudaEventRecord(static_cast<cudaEvent_t>(buf->fence), cp->stream)))
+		return cp->sticky_error;
+	buf->width = w;
+	buf->height = h;
+	return RDP_OK;
+}
+
+int rdp_vi_scanout_buffer_wait(rdp_vi_scanout_buffer *buf, uint64_t timeout_ns)
+{
+	if (!buf) return RDP_ERR_INVALID;
+	if (!buf->fence) return RDP_OK;
+	const bool bounded = timeout_ns < (uint64_t(1) << 50);
+	const auto deadline = std::chrono::steady_clock::now() + std::chrono::nanoseconds(bounded ? int64_t(timeout_ns) : 0);
+	for (;;)
+	{
+		cudaError_t q = cudaEventQuery(static_cast<cudaEvent_t>(buf->fence));
+		if (q == cudaSuccess) return RDP_OK;
+		if (q != cudaErrorNotReady) return RDP_ERR_DEVICE;
+		if (bounded && std::chrono::steady_clock::now() >= deadline) return RDP_ERR_TIMEOUT;
+		std::this_thread::yield();
+	}
+}
+
+void rdp_vi_scanout_buffer_release(rdp_vi_scanout_buffer *buf)
+{
+	if (!buf) return;
+	if (buf->fence)
+	{
+		cudaEventSynchronize(static_cast<cudaEvent_t>(buf->fence));
+		cudaEventDestroy(static_cast<cudaEvent_t>(buf->fence));
+	}
+	if (buf->pixels) cudaFreeHost(buf->pixels);
+	*buf = rdp_vi_scanout_buffer{};
 }
 
 int rdp_cp_begin_vi_register_per_scanline(rdp_cp *cp, uint32_t flags)
@@ -1772,6 +2096,7 @@ int rdp_cp_get_stats(rdp_cp *cp, rdp_stats *out)
 {
 	if (!cp || !out) return RDP_ERR_INVALID;
 	cudaSetDevice(cp->device);
+	cp->sync_ring();
 	*out = cp->stats;
 	unsigned long long counters[3] = { 0, 0, 0 };
 	if (cudaMemcpy(counters, cp->d_fragments, sizeof(counters), cudaMemcpyDeviceToHost) != cudaSuccess) return RDP_ERR_DEVICE;
@@ -1848,7 +2173,7 @@ static int build_graph(rdpx::Executor *exec, rdpx::CaptureSink &sink, rdp_stats 
 
 int rdp_cp_capture_begin(rdp_cp *cp)
 {
-	if (!cp || cp->capturing || cp->batch) return RDP_ERR_INVALID;
+	if (!cp || cp->capturing || cp->batch || cp->ring) return RDP_ERR_INVALID;
 	cudaSetDevice(cp->device);
 	int r = cp->hard_flush();
 	if (r != RDP_OK) return r;

@@ -2065,18 +2065,25 @@ struct Shaded
 };
 
 // shading.h:38-359: everything that does not depend on the framebuffer.
-__device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const RdpPrimAttr &a, const RdpPrimShade &sh,
-                            const RdpTile *tiles, const uint16_t *tm, const SpanRow &sp, const SpanRow &sp_next,
-                            int x, int y, Shaded &out)
+//
+// Specialised per static render state (the reference compiles its shading shaders per
+// normalised static state with specialisation constants, rdp_renderer.cpp:1294-1331,
+// 1790-1822): the static flags in KN are known at compile time to equal KV's, so every branch on
+// them folds away; the other flags are read at run time.  KN = 0 is the general shader.
+template <uint32_t KN, uint32_t KV>
+__device__ __forceinline__ bool shade_pixel_v(const PassConst &pc, const RdpPrimGeom &g, const RdpPrimAttr &a,
+                                              const RdpPrimShade &sh, const RdpTile *tiles, const uint16_t *tm,
+                                              const SpanRow &sp, const SpanRow &sp_next, int x, int y, Shaded &out)
 {
 	if (!sp.valid) return false;
 	const uint32_t f = sh.static_flags;
+#define F(bit) ((KN & (bit)) ? ((KV & (bit)) != 0) : ((f & (bit)) != 0))
 	const bool flip = (g.flags & TRI_FLIP) != 0;
-	const bool perspective = (f & RS_PERSPECTIVE) != 0;
+	const bool perspective = F(RS_PERSPECTIVE);
 	uint32_t noise = 0;
-	if (f & RS_NEED_NOISE) noise = reseed_noise(uint32_t(x), uint32_t(y), sh.prim_index);
+	if (F(RS_NEED_NOISE)) noise = reseed_noise(uint32_t(x), uint32_t(y), sh.prim_index);
 
-	if (f & RS_COPY)
+	if (F(RS_COPY))
 	{
 		if (!(x >= sp.start_x && x <= sp.end_x)) return false;
 		int dxp = flip ? (x - sp.start_x) : (sp.end_x - x);
@@ -2091,19 +2098,19 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 		const RdpTile &t0 = tiles[g.tile & 7];
 		int st0 = shift_only(os, int(t0.slo), t0.shift_s) >> 5;
 		int st1 = shift_only(ot, int(t0.tlo), t0.shift_t) >> 5;
-		bool tlut = (f & RS_TLUT) != 0;
+		bool tlut = F(RS_TLUT);
 		int texel;
 		if (pc.fb_size == 0) texel = 0;
 		else if (pc.fb_size == 1)
 			texel = (copy_word(tm, t0, st0, st1, s_offset >> 1, tlut) >> (8 - 8 * (s_offset & 1))) & 0xff;
 		else
 			texel = copy_word(tm, t0, st0, st1, s_offset, tlut);
-		if ((f & RS_ALPHA_TEST) && pc.fb_size == 2 && (texel & 1) == 0) return false;
+		if (F(RS_ALPHA_TEST) && pc.fb_size == 2 && (texel & 1) == 0) return false;
 		out.z_dith = texel;
 		out.coverage = 0x20;
 		return true;
 	}
-	if (f & RS_FILL)
+	if (F(RS_FILL))
 	{
 		out.coverage = 0x40;
 		return x >= sp.start_x && x <= sp.end_x;
@@ -2127,7 +2134,7 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	}
 	if (coverage == 0) return false;
 	int cov_count = __popc(coverage);
-	const bool aa = (f & RS_AA) != 0;
+	const bool aa = F(RS_AA);
 	if (!aa && (coverage & 1) == 0) return false;
 
 	int dx = x - sp.base_x;
@@ -2149,14 +2156,14 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	}
 
 	// ---- interpolate_stz (interpolation.h:92-142)
-	const bool uses_lod = (f & RS_USES_LOD) != 0;
+	const bool uses_lod = F(RS_USES_LOD);
 	int s0 = 0, t0v = 0, sdx = 0, tdx = 0, sdy = 0, tdy = 0, z;
 	bool povf = false;
 	{
 		int sw[3], idx3[3] = { 0, 1, 3 };
 #pragma unroll
 		for (int k = 0; k < 3; k++) sw[k] = sp.stzw[idx3[k]] + mulw(a.dstzw_dx[idx3[k]] & ~0x1f, dx);
-		if (f & (RS_USES_TEXEL0 | RS_USES_TEXEL1 | RS_USES_PIPELINED_TEXEL1 | RS_USES_LOD))
+		if (F(RS_USES_TEXEL0) || F(RS_USES_TEXEL1) || F(RS_USES_PIPELINED_TEXEL1) || F(RS_USES_LOD))
 		{
 			st_div(sw[0] >> 16, sw[1] >> 16, sw[2] >> 16, perspective, s0, t0v, povf);
 			if (uses_lod)
@@ -2184,7 +2191,7 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	int lod_frac = 0;
 	if (uses_lod)
 	{
-		bool sharpen = (f & RS_SHARPEN) != 0, detail = (f & RS_DETAIL) != 0;
+		bool sharpen = F(RS_SHARPEN), detail = F(RS_DETAIL);
 		bool magnify = false, distant = false;
 		uint32_t tofs = 0;
 		if (povf)
@@ -2222,7 +2229,7 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 				}
 			}
 		}
-		if (f & RS_TEX_LOD)
+		if (F(RS_TEX_LOD))
 		{
 			if (distant) tofs = max_level;
 			if (!detail)
@@ -2239,14 +2246,14 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	}
 
 	// ---- texels
-	const bool tlut = (f & RS_TLUT) != 0, tlut_type = (f & RS_TLUT_TYPE) != 0;
-	const bool quad = (f & RS_SAMPLE_QUAD) != 0, midt = (f & RS_MID_TEXEL) != 0;
+	const bool tlut = F(RS_TLUT), tlut_type = F(RS_TLUT_TYPE);
+	const bool quad = F(RS_SAMPLE_QUAD), midt = F(RS_MID_TEXEL);
 	T4 tex0 = { { 0, 0, 0, 0 } }, tex1 = tex0;
-	if (f & RS_USES_TEXEL0)
-		tex0 = sample_texture(tm, tiles[tile0], s0, t0v, tlut, tlut_type, quad, midt, false, (f & RS_BILERP0) != 0,
+	if (F(RS_USES_TEXEL0))
+		tex0 = sample_texture(tm, tiles[tile0], s0, t0v, tlut, tlut_type, quad, midt, false, F(RS_BILERP0),
 		                      sh.factors, tex0);
-	bool uses_t1 = (f & RS_USES_TEXEL1) != 0;
-	if (f & RS_USES_PIPELINED_TEXEL1)
+	bool uses_t1 = F(RS_USES_TEXEL1);
+	if (F(RS_USES_PIPELINED_TEXEL1))
 	{
 		int lodlength = int16_t(flip ? (sp.end_x - sp.base_x) : (sp.base_x - sp.start_x));
 		bool end_span = x == (flip ? sp.end_x : sp.start_x);
@@ -2269,7 +2276,7 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	}
 	if (uses_t1)
 	{
-		bool c1 = (f & RS_CONVERT_ONE) != 0, b1 = (f & RS_BILERP1) != 0;
+		bool c1 = F(RS_CONVERT_ONE), b1 = F(RS_BILERP1);
 		if (c1 && !b1) tex1 = convert_factors(tex0, sh.factors);
 		else tex1 = sample_texture(tm, tiles[tile1], s0, t0v, tlut, tlut_type, quad, midt, c1, b1, sh.factors, tex0);
 	}
@@ -2278,7 +2285,7 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	const int rgb_d = rgb_dither_value(f, sh.dither, x, y, noise);
 	int alpha_d;
 	{
-		int yy = y >> int((f & RS_INTERLACE_FIELD) != 0);
+		int yy = y >> int(F(RS_INTERLACE_FIELD));
 		int mr = int(sh.dither >> 2), ma = int(sh.dither & 3);
 		int cell = (yy & 3) * 4 + (x & 3);
 		if (ma == 3) alpha_d = 0;
@@ -2291,8 +2298,8 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	}
 
 	// ---- combiner (shading.h:263-333, combiner.h:196-282)
-	const bool cvg_times_alpha = (f & RS_CVG_TIMES_ALPHA) != 0, alpha_cvg_select = (f & RS_ALPHA_CVG_SELECT) != 0;
-	const bool alpha_test = (f & RS_ALPHA_TEST) != 0;
+	const bool cvg_times_alpha = F(RS_CVG_TIMES_ALPHA), alpha_cvg_select = F(RS_ALPHA_CVG_SELECT);
+	const bool alpha_test = F(RS_ALPHA_TEST);
 	int combined[4];
 	int alpha_ref = 0;
 	CombIn in;
@@ -2308,7 +2315,7 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	in.noise = int(((noise & 7u) << 6) | 0x20u);
 	// Cycle 0 (2-cycle mode only), then cycle 1, through one inlined copy of the combiner.
 #pragma unroll 1
-	for (int cy = (f & RS_MULTI_CYCLE) ? 0 : 1; cy < 2; cy++)
+	for (int cy = F(RS_MULTI_CYCLE) ? 0 : 1; cy < 2; cy++)
 	{
 		in.cma = sh.c_muladd[cy]; in.cms = sh.c_mulsub[cy]; in.cmu = sh.c_mul[cy]; in.cad = sh.c_add[cy];
 		combine(in, sh.comb_rgb[cy], sh.comb_alpha[cy], combined);
@@ -2330,7 +2337,7 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 				in.tex0[c] = in.tex1[c];
 				in.tex1[c] = tmp;
 			}
-			if (f & RS_NEED_NOISE_DUAL)
+			if (F(RS_NEED_NOISE_DUAL))
 			{
 				// The second seed also feeds the later alpha-test threshold (shading.h:309-347).
 				noise = reseed_noise(uint32_t(x + 1023), uint32_t(y + 7), sh.prim_index + 11);
@@ -2355,11 +2362,11 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 		else ea += alpha_d;
 		combined[3] = clampi(ea, 0, 0xff);
 	}
-	if (!(f & RS_MULTI_CYCLE)) alpha_ref = combined[3];
+	if (!F(RS_MULTI_CYCLE)) alpha_ref = combined[3];
 	if (aa && cov_count == 0) return false;
 	if (alpha_test)
 	{
-		int thr = (f & RS_ALPHA_TEST_DITHER) ? int(noise & 0xffu) : int(sh.blend_color[3]);
+		int thr = F(RS_ALPHA_TEST_DITHER) ? int(noise & 0xffu) : int(sh.blend_color[3]);
 		if (alpha_ref < thr) return false;
 	}
 
@@ -2369,6 +2376,58 @@ __device__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const Rdp
 	out.coverage = cov_count;
 	out.shade_alpha = min(shade[3] + alpha_d, 0xff);
 	return true;
+#undef F
+}
+
+// The general shader: every static flag read at run time.
+__device__ __forceinline__ bool shade_pixel(const PassConst &pc, const RdpPrimGeom &g, const RdpPrimAttr &a,
+                                            const RdpPrimShade &sh, const RdpTile *tiles, const uint16_t *tm,
+                                            const SpanRow &sp, const SpanRow &sp_next, int x, int y, Shaded &out)
+{
+	return shade_pixel_v<0u, 0u>(pc, g, a, sh, tiles, tm, sp, sp_next, x, y, out);
+}
+
+// Render-state variants with their own compiled shading code (the kernels' SPEC instantiations).
+// A primitive takes the first variant whose known flags equal its own: (static_flags & KN) == KV;
+// the rest take the general shader.  The keys are the flags that select whole paths of
+// shading.h -- which pipe (fill, copy, the 1/2-cycle pipeline), which texels and LOD are used, TLUT,
+// noise -- so a variant's code holds only its path.  The variants compute exactly what the
+// general shader computes for the same primitive.
+constexpr uint32_t SV_PIPE = RS_COPY | RS_FILL;
+constexpr uint32_t SV_TEX = RS_USES_TEXEL0 | RS_USES_TEXEL1 | RS_USES_PIPELINED_TEXEL1 | RS_USES_LOD;
+constexpr uint32_t SV_NOISE = RS_NEED_NOISE | RS_NEED_NOISE_DUAL;
+constexpr uint32_t SV_FILL_KN = SV_PIPE, SV_FILL_KV = RS_FILL;
+constexpr uint32_t SV_COPY_KN = SV_PIPE, SV_COPY_KV = RS_COPY;
+constexpr uint32_t SV_FLAT_KN = SV_PIPE | SV_TEX | SV_NOISE, SV_FLAT_KV = 0;
+constexpr uint32_t SV_TEX0_KN = SV_PIPE | SV_TEX | SV_NOISE | RS_TLUT | RS_CONVERT_ONE;
+constexpr uint32_t SV_TEX0_KV = RS_USES_TEXEL0, SV_TLUT0_KV = RS_USES_TEXEL0 | RS_TLUT;
+constexpr uint32_t SV_TEX01_KN = SV_PIPE | SV_TEX | SV_NOISE | RS_TLUT, SV_TEX01_KV = RS_USES_TEXEL0 | RS_USES_TEXEL1;
+constexpr uint32_t SV_LOD_KN = SV_PIPE | RS_USES_LOD | SV_NOISE | RS_TLUT, SV_LOD_KV = RS_USES_LOD;
+
+template <bool SPEC>
+__device__ __forceinline__ bool shade_pixel_any(const PassConst &pc, const RdpPrimGeom &g, const RdpPrimAttr &a,
+                                                const RdpPrimShade &sh, const RdpTile *tiles, const uint16_t *tm,
+                                                const SpanRow &sp, const SpanRow &sp_next, int x, int y, Shaded &out)
+{
+	if (SPEC)
+	{
+		const uint32_t f = sh.static_flags;
+		if ((f & SV_FILL_KN) == SV_FILL_KV)
+			return shade_pixel_v<SV_FILL_KN, SV_FILL_KV>(pc, g, a, sh, tiles, tm, sp, sp_next, x, y, out);
+		if ((f & SV_COPY_KN) == SV_COPY_KV)
+			return shade_pixel_v<SV_COPY_KN, SV_COPY_KV>(pc, g, a, sh, tiles, tm, sp, sp_next, x, y, out);
+		if ((f & SV_FLAT_KN) == SV_FLAT_KV)
+			return shade_pixel_v<SV_FLAT_KN, SV_FLAT_KV>(pc, g, a, sh, tiles, tm, sp, sp_next, x, y, out);
+		if ((f & SV_TEX0_KN) == SV_TEX0_KV)
+			return shade_pixel_v<SV_TEX0_KN, SV_TEX0_KV>(pc, g, a, sh, tiles, tm, sp, sp_next, x, y, out);
+		if ((f & SV_TEX0_KN) == SV_TLUT0_KV)
+			return shade_pixel_v<SV_TEX0_KN, SV_TLUT0_KV>(pc, g, a, sh, tiles, tm, sp, sp_next, x, y, out);
+		if ((f & SV_TEX01_KN) == SV_TEX01_KV)
+			return shade_pixel_v<SV_TEX01_KN, SV_TEX01_KV>(pc, g, a, sh, tiles, tm, sp, sp_next, x, y, out);
+		if ((f & SV_LOD_KN) == SV_LOD_KV)
+			return shade_pixel_v<SV_LOD_KN, SV_LOD_KV>(pc, g, a, sh, tiles, tm, sp, sp_next, x, y, out);
+	}
+	return shade_pixel_v<0u, 0u>(pc, g, a, sh, tiles, tm, sp, sp_next, x, y, out);
 }
 
 // The framebuffer half: fill pipe, copy pipe or depth test + blender + dither + coverage
@@ -2946,9 +3005,9 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 }
 
 // ============================================================================ k_shade
-// Shading of every (tile, primitive) pair in parallel (the reference's rasterizer.comp): one
-// pair (k_shade_packed) or a few pairs (k_shade_packedn) per warp step, the pixels that can be
-// covered packed one per lane; two independent warps per CTA.  Results go to scratch as one
+// Shading of every (tile, primitive) pair in parallel (the reference's rasterizer.comp): a few
+// pairs per warp step (k_shade_packedn), the pixels that can be covered packed one per lane; two
+// independent warps per CTA.  Results go to scratch as one
 // 8-byte shaded record per pixel (pack_shaded).
 constexpr int SHADE_THREADS = 64;
 
@@ -3044,139 +3103,15 @@ __device__ __forceinline__ void record_tile(const RdpPass &ps, uint32_t y, bool 
 // executor's autotuner picks one.  More resident CTAs hide more latency at the price of some
 // spilling.
 
-// Packed shading: one warp per pair (no CTA barrier).  The warp first picks the pair's candidate
-// pixels -- inside the image and inside the valid span of their row (k_span's rows), the only
-// ones that can be covered -- and shades just those, packed into as few 32-lane rounds as they
-// fill (one round for most pairs at a primitive's edge).  The other pixels are written as empty.
-template <int MIN_CTAS>
-__global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
-	k_shade_packed(const RdpPass *__restrict__ passes, uint32_t num_passes, const uint2 *__restrict__ pairs,
-	               const uint32_t *__restrict__ ctrl, const RdpPrimGeom *__restrict__ geom,
-	               const RdpPrimAttr *__restrict__ attr, const RdpPrimShade *__restrict__ shade,
-	               const RdpTile *__restrict__ tilesets, uint2 *__restrict__ sc, const uint4 *__restrict__ list,
-	               uint32_t *__restrict__ queues, uint32_t num_queues, uint32_t queue_min,
-	               const SpanRow *__restrict__ spans,
-	               const uint32_t *__restrict__ prim_rows)
-{
-	constexpr int WARPS = SHADE_THREADS / 32;
-	__shared__ __align__(16) uint4 s_rec_all[WARPS][2]; // current / next position's record, per warp
-	__shared__ uint32_t s_pos_all[WARPS][2];
-	__shared__ uint8_t s_px_all[WARPS][64];              // candidate pixels, in pixel order
-	if (ctrl[1]) return;
-	const uint32_t total = ctrl[0];
-	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-	uint4 *s_rec = s_rec_all[wid];
-	uint32_t *s_pos = s_pos_all[wid];
-	uint8_t *s_px = s_px_all[wid];
-	const uint32_t worker = blockIdx.x * WARPS + uint32_t(wid), workers = gridDim.x * WARPS;
-	if (total < gridDim.x * queue_min) queues = nullptr;
-	uint32_t q = 0, k_next = 0;
-	int buf = 0;
-	auto fetch = [&](uint32_t j, int b) {
-		if (list) cp_async16(&s_rec[b], list + j);
-		else cp_async8(&s_rec[b], pairs + j);
-	};
-	if (lane == 0)
-	{
-		uint32_t first = worker;
-		if (queues)
-		{
-			q = sm_id() % num_queues;
-			first = queue_pos(q, atomicAdd(&queues[q], 1u), num_queues);
-			if (first >= total) first = queue_steal(queues, num_queues, total, q);
-			if (first < total) k_next = atomicAdd(&queues[q], 1u);
-		}
-		if (first < total) fetch(first, 0);
-		s_pos[0] = first;
-		cp_async_wait_all();
-	}
-	__syncwarp();
-	uint32_t j = s_pos[0];
-	const unsigned below = (1u << lane) - 1u;
-	while (j < total)
-	{
-		const uint4 rec = s_rec[buf];
-		const uint32_t prim = rec.x, item = rec.y, pr = list ? rec.z : j;
-		if (lane == 0)
-		{
-			uint32_t nj = j + workers;
-			if (queues)
-			{
-				nj = queue_pos(q, k_next, num_queues);
-				if (nj >= total) nj = queue_steal(queues, num_queues, total, q);
-				if (nj < total) k_next = atomicAdd(&queues[q], 1u);
-			}
-			if (nj < total) fetch(nj, buf ^ 1);
-			s_pos[buf ^ 1] = nj;
-		}
-		const RdpPass &ps = passes[list ? rec.w : shade[prim].pass];
-		int tx, ty;
-		record_tile(ps, item, list != nullptr, tx, ty);
-		const RdpPrimGeom &g = geom[prim];
-		const int fbw = int(ps.fb_width), fbh = int(ps.fb_height), ylo = g.span_ylo, yhi = g.span_yhi;
-		// Row y of the primitive is rows[y - ylo].
-		const SpanRow *rows = spans + prim_rows[prim];
-		// Candidates among pixels lane (rows 0-3) and lane + 32 (rows 4-7).
-		const int x = tx * 8 + (lane & 7), y0 = ty * 8 + (lane >> 3), y1 = y0 + 4;
-		bool c0 = x < fbw && y0 < fbh && y0 >= ylo && y0 <= yhi;
-		bool c1 = x < fbw && y1 < fbh && y1 >= ylo && y1 <= yhi;
-		if (c0)
-		{
-			const SpanRow &r = rows[y0 - ylo];
-			c0 = r.valid && x >= r.start_x && x <= r.end_x;
-		}
-		if (c1)
-		{
-			const SpanRow &r = rows[y1 - ylo];
-			c1 = r.valid && x >= r.start_x && x <= r.end_x;
-		}
-		const unsigned m0 = __ballot_sync(0xffffffffu, c0), m1 = __ballot_sync(0xffffffffu, c1);
-		const int n0 = __popc(m0), count = n0 + __popc(m1);
-		if (c0) s_px[__popc(m0 & below)] = uint8_t(lane);
-		if (c1) s_px[n0 + __popc(m1 & below)] = uint8_t(lane + 32);
-		const size_t base = size_t(pr) * SHADE_THREADS;
-		// Every pixel of the scratch is written (full sectors); k_blend skips "not written".
-		if (!c0) sc[base + lane] = kScratchEmpty;
-		if (!c1) sc[base + 32 + lane] = kScratchEmpty;
-		__syncwarp();
-		if (count)
-		{
-			PassConst pc;
-			switch (ps.fb_fmt)
-			{
-			case FBF_I4: pc.fb_size = 0; pc.dx_mask = 0; pc.dx_shift = 0; break;
-			case FBF_I8: pc.fb_size = 1; pc.dx_mask = ~7; pc.dx_shift = 3; break;
-			case FBF_RGBA5551:
-			case FBF_IA88: pc.fb_size = 2; pc.dx_mask = ~3; pc.dx_shift = 2; break;
-			default: pc.fb_size = 4; pc.dx_mask = ~1; pc.dx_shift = 1; break;
-			}
-			pc.alias = ps.fb_addr == ps.depth_addr;
-			const RdpPrimShade &sh = shade[prim];
-			for (int s = lane; s < count; s += 32)
-			{
-				const int px = s_px[s], y = ty * 8 + (px >> 3);
-				const SpanRow *sp = rows + (y - ylo);
-				Shaded out;
-				const bool ok = shade_pixel(pc, g, attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
-				                            ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, sp[0], sp[1],
-				                            tx * 8 + (px & 7), y, out);
-				sc[base + px] = ok ? pack_shaded(out) : kScratchEmpty;
-			}
-		}
-		if (lane == 0) cp_async_wait_all();
-		__syncwarp();
-		buf ^= 1;
-		j = s_pos[buf];
-	}
-}
-
-// Packed shading over NP pairs at a time: a warp takes NP positions per step (consecutive ones,
-// so mostly tiles of one primitive in primitive-major order), picks the pairs' candidate pixels
-// and shades them together in as few 32-lane rounds as they fill -- pairs with few covered
-// pixels share rounds.  Per-pair data sits in shared memory for the shading rounds.  Same work
-// order, scratch and results as k_shade_packed.  On the batched workload two pairs per step
-// measured best (four: slower than one, the rounds mix primitives).
-template <int NP, int MIN_CTAS>
+// Packed shading: warps, no CTA barrier.  A warp takes NP positions per step (consecutive ones,
+// so mostly tiles of one primitive in primitive-major order), picks the pairs' candidate pixels --
+// inside the image and inside the valid span of their row (k_span's rows), the only ones that can
+// be covered -- and shades just those, packed into as few 32-lane rounds as they fill: pairs with
+// few covered pixels share rounds.  The other pixels are written as empty.  Per-pair data sits in
+// shared memory for the shading rounds.  On the batched workload two pairs per step measured best
+// (one pair 4 % slower, four slower than one: the rounds mix primitives).  SPEC selects the
+// render-state variants of the shading code (shade_pixel_any).
+template <int NP, int MIN_CTAS, bool SPEC>
 __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 	k_shade_packedn(const RdpPass *__restrict__ passes, uint32_t num_passes, const uint2 *__restrict__ pairs,
 	                const uint32_t *__restrict__ ctrl, const RdpPrimGeom *__restrict__ geom,
@@ -3330,9 +3265,9 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 			const int y = sl.ty * 8 + (px >> 3);
 			const SpanRow *sp = sl.rows + (y - sl.ylo);
 			Shaded out;
-			const bool ok = shade_pixel(pc, geom[prim], attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
-			                            ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, sp[0], sp[1],
-			                            sl.tx * 8 + (px & 7), y, out);
+			const bool ok = shade_pixel_any<SPEC>(pc, geom[prim], attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
+			                                      ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, sp[0], sp[1],
+			                                      sl.tx * 8 + (px & 7), y, out);
 			sc[size_t(sl.pr) * SHADE_THREADS + px] = ok ? pack_shaded(out) : kScratchEmpty;
 		}
 		if (lane == 0) cp_async_wait_all();
@@ -3656,8 +3591,9 @@ typedef void (*ShadeKernel)(const RdpPass *, uint32_t, const uint2 *, const uint
                             const RdpPrimAttr *, const RdpPrimShade *, const RdpTile *, uint2 *, const uint4 *,
                             uint32_t *, uint32_t, uint32_t, const rdp::SpanRow *, const uint32_t *);
 const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = {
-	rdp::k_shade_packedn<2, 16>, rdp::k_shade_packedn<2, 18>, rdp::k_shade_packedn<2, 20>, rdp::k_shade_packedn<2, 24>,
-	rdp::k_shade_packed<16>,     rdp::k_shade_packed<18>,     rdp::k_shade_packed<20>,     rdp::k_shade_packed<24>
+	rdp::k_shade_packedn<2, 16, false>, rdp::k_shade_packedn<2, 18, false>, rdp::k_shade_packedn<2, 20, false>,
+	rdp::k_shade_packedn<2, 24, false>, rdp::k_shade_packedn<2, 16, true>,  rdp::k_shade_packedn<2, 18, true>,
+	rdp::k_shade_packedn<2, 20, true>,  rdp::k_shade_packedn<2, 24, true>
 };
 } // namespace
 

@@ -6,8 +6,9 @@
 #include "rdp_types.h"
 
 /* Shading kernel variants (the autotuner chooses among them): k_shade_packedn with two pairs per
- * warp step (candidate pixels of both pairs packed together) and k_shade_packed (one pair per
- * warp step), each for minimum residencies of 16, 18, 20 and 24 64-thread CTAs per SM. */
+ * warp step (candidate pixels of both pairs packed together), with the general shading code
+ * (variants 0-3) or with separate code per render-state class (variants 4-7), each for minimum
+ * residencies of 16, 18, 20 and 24 64-thread CTAs per SM. */
 /* Bytes of one span row (one scanline of one primitive, computed by k_bin). */
 #define RDP_SPAN_ROW_BYTES 64
 /* Launches with more tiles (or, in primitive-major order, primitives) than this scan their

@@ -129,6 +129,7 @@ class _BatchStats(ctypes.Structure):
                 ("kernel_launches", ctypes.c_uint64), ("staging_bytes", ctypes.c_uint64)]
 
 
+CREATE_COMMAND_THREAD = 1 << 0
 BATCH_TILE_ORDER_LEARNED = 1 << 0
 BATCH_RECORD_TILE_CYCLES = 1 << 1
 
@@ -288,7 +289,8 @@ class CommandProcessor:
     a zero-initialised one.
     """
 
-    def __init__(self, rdram=None, rdram_size=8 << 20, hidden_rdram_size=None, device=0, batch=None):
+    def __init__(self, rdram=None, rdram_size=8 << 20, hidden_rdram_size=None, device=0, batch=None,
+                 command_thread=False):
         if hidden_rdram_size is None:
             hidden_rdram_size = rdram_size // 2
         if rdram is None:
@@ -296,7 +298,8 @@ class CommandProcessor:
         assert rdram.dtype == np.uint8 and rdram.flags["C_CONTIGUOUS"] and rdram.size >= rdram_size
         self._rdram = rdram
         self._batch = batch
-        info = _CreateInfo(rdram.ctypes.data, 0, rdram_size, hidden_rdram_size, 0, device)
+        info = _CreateInfo(rdram.ctypes.data, 0, rdram_size, hidden_rdram_size,
+                           CREATE_COMMAND_THREAD if command_thread else 0, device)
         h = ctypes.c_void_p()
         if batch is None:
             _check(lib().rdp_cp_create(ctypes.byref(info), ctypes.byref(h)), "rdp_cp_create")

@@ -78,3 +78,45 @@ def test_quirks_and_frame_contexts_match_the_oracle():
         from rdp_testutil import run_oracle
         o_rd = run_oracle(w2, rd2)[0]
         assert np.array_equal(cp.begin_read_rdram(), o_rd)
+
+
+def _split_commands(words):
+    """Word offsets where each RDP command starts (the RDP's command lengths)."""
+    lengths = {0x08: 8, 0x09: 12, 0x0a: 24, 0x0b: 28, 0x0c: 24, 0x0d: 28, 0x0e: 40, 0x0f: 44, 0x24: 4, 0x25: 4}
+    out, i = [], 0
+    while i < len(words):
+        out.append(i)
+        i += lengths.get((int(words[i]) >> 24) & 63, 2)
+    return out
+
+
+def test_in_band_meta_ops_and_command_thread_match_the_oracle():
+    """The reference's in-band meta ops in the command stream (rdp_device.cpp:926-952): MetaFlush
+    and MetaIdle between commands and MetaSignalTimeline with its 64-bit value, decoded on the
+    calling thread and on the command thread (command ring, command_ring.cpp:71-134).  The image
+    equals the oracle's rendering of the same stream without the meta ops; a value signalled in band
+    completes with everything before it."""
+    from rdp_testutil import run_oracle
+    p = cmdgen.default_params(cmdgen.CONFIG_MIXED, seed=31, num_prims=2500, num_frames=1)
+    words, rdram, _ = cmdgen.generate_stream(p)
+    starts = _split_commands(words)
+    pieces = []
+    for k, (a, b) in enumerate(zip(starts, starts[1:] + [len(words)])):
+        pieces.append(words[a:b])
+        if k % 500 == 499:
+            pieces.append(np.array([0x02 << 24], np.uint32))  # MetaFlush
+        if k % 700 == 699:
+            pieces.append(np.array([0x03 << 24], np.uint32))  # MetaIdle
+    stream = np.concatenate(pieces + [np.array([0x01 << 24, 41, 0], np.uint32)])  # MetaSignalTimeline 41
+    o_rd, o_hid, _, _ = run_oracle(words, rdram)
+    for threaded in (False, True):
+        with CommandProcessor(rdram.copy(), command_thread=threaded) as cp:
+            cuts = np.linspace(0, len(stream), 37).astype(int)  # uneven chunks cut through commands
+            for a, b in zip(cuts[:-1], cuts[1:]):
+                cp.enqueue_command(stream[a:b])
+            cp.wait_for_timeline(41)
+            v = cp.signal_timeline()
+            assert v >= 1
+            cp.wait_for_timeline(v)
+            assert np.array_equal(cp.begin_read_rdram(), o_rd), "threaded=%s" % threaded
+            assert np.array_equal(cp.begin_read_hidden_rdram(), o_hid), "threaded=%s" % threaded

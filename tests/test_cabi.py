@@ -58,3 +58,17 @@ def test_enqueue_many_rejects_a_handle_given_twice():
         wptrs = (ctypes.c_void_p * n)(*([ctypes.addressof(words)] * n))
         counts = (ctypes.c_uint32 * n)(*([2] * n))
         assert f(ctypes.c_void_p(0x10), n, insts, wptrs, counts, None, 2) == native.RDP_ERR_INVALID
+
+
+def test_cpp_facade_header_compiles():
+    """include/rdp_cuda.hpp (RDP::CommandProcessor over the C ABI) and the C++ program that the GPU
+    test drives through it compile as C++17 (no GPU needed)."""
+    import shutil
+    import subprocess
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    if not shutil.which("g++"):
+        import pytest
+        pytest.skip("no g++")
+    subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    "-I", os.path.join(cuda, "include"), os.path.join(ROOT, "tests", "cpp", "facade_test.cpp")],
+                   check=True)

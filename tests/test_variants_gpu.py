@@ -1,5 +1,7 @@
-"""Kernel specialisations: every compiled variant of the shading kernel produces the same
-RDRAM / hidden RDRAM / TMEM bytes, and the autotuner settles on one of them."""
+"""Kernel specialisations: every compiled variant of the shading kernel -- the general shader and
+the render-state-specialised shader (separate code for fill, copy, untextured, one-texel,
+one-texel-through-TLUT, two-texel and LOD primitives), each at four register budgets -- produces
+the same RDRAM / hidden RDRAM / TMEM bytes, and the autotuner settles on one of them."""
 import numpy as np
 import pytest
 
@@ -23,13 +25,21 @@ def test_all_variants_bit_exact(restore_tuning):
     q = cmdgen.default_params(cmdgen.CONFIG_PLAIN, seed=4, num_prims=800, fb_format=cmdgen.FB_RGBA8888,
                               flags=F["FUZZ"] | F["CLEAR"])
     fwords, frdram, _ = cmdgen.generate_stream(q)
+    # Copy-mode rectangles, fill rectangles, CI8 + TLUT and LOD triangles (the mixed primitive mix),
+    # and untextured Gouraud triangles: every render-state variant of the specialised shader runs.
+    m = cmdgen.default_params(cmdgen.CONFIG_MIXED, seed=6, num_prims=3000, num_frames=1)
+    mwords, mrdram, _ = cmdgen.generate_stream(m)
+    g = cmdgen.default_params(cmdgen.CONFIG_PLAIN, seed=7, num_prims=500)
+    gwords, grdram, _ = cmdgen.generate_stream(g)
     results = []
     for v in range(SHADE_VARIANTS):
         set_shade_variant(v)
         assert get_shade_variant() == v
-        if v == SHADE_VARIANTS - 1:
-            assert_parity(words, rdram)  # one variant also against the oracle
-        results.append((run_gpu(words, rdram)[:3], run_gpu(fwords, frdram)[:3]))
+        if v in (0, SHADE_VARIANTS - 1):  # the general and a specialised variant against the oracle
+            assert_parity(words, rdram)
+            assert_parity(mwords, mrdram)
+        results.append((run_gpu(words, rdram)[:3], run_gpu(fwords, frdram)[:3], run_gpu(mwords, mrdram)[:3],
+                        run_gpu(gwords, grdram)[:3]))
     for r in results[1:]:
         for a, b in zip(r, results[0]):
             for x, y in zip(a, b):
@@ -73,11 +83,11 @@ def _order_run(words, rdram, streams):
     return single, batched
 
 
-@pytest.mark.parametrize("variant", [1, 5], ids=["two_pairs", "one_pair"])
+@pytest.mark.parametrize("variant", [1, 5], ids=["general", "specialised"])
 def test_shade_orders_bit_exact(restore_order, restore_tuning, monkeypatch, variant):
     """Tile order with a fixed stride, per-SM work queues and primitive-major order shade the
-    same pairs: identical bytes, on a single stream and on a batch of instances, with shading
-    kernels that take two and one pair per warp step.  The size thresholds are
+    same pairs: identical bytes, on a single stream and on a batch of instances, with the general
+    and the render-state-specialised shading kernels.  The size thresholds are
     set to 0 so that every launch, down to the smallest, takes the queues (and their stealing
     sweep) and the primitive-major order; one more run keeps the default thresholds.  The
     single stream's big pass (10,000 primitives, 1,200 tiles) takes the one-CTA scans, the

@@ -665,6 +665,9 @@ def run_ours_batched(args):
                                 "sample": "%d of the %d instances' frames through the CPU oracle, instances spread "
                                           "over %d host threads" % (n, len(streams), threads),
                                 "mpix_per_s": frags / el / 1e6}
+        # The serving configuration's 1 % output sample, checked against the oracle (untimed).
+        if serving and serving.get("parity_sample"):
+            serving["parity_sample"] = _check_serving_parity(serving["parity_sample"], threads)
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
@@ -692,6 +695,8 @@ def _serving(args, device, model=None):
         cp.enqueue_command(w)
     t0 = time.perf_counter()
     b.idle()
+    renders = [2] * len(insts)  # frames each instance has rendered (for the parity sample)
+    all_requests = []
     capacity_fps = len(insts) / (time.perf_counter() - t0)
     out = {"instances": len(insts), "hbm_budget_gb": args.serve_budget_gb, "capacity_fps_estimate": capacity_fps}
     # The configured rate first; the sustainable rate is 80 % of what the serving loop delivered
@@ -700,13 +705,15 @@ def _serving(args, device, model=None):
         rate = 20000.0 if tag == "configured_rate" else 0.8 * out["configured_rate"]["throughput_fps"]
         trace = poisson_trace(len(insts), rate, dur, frames, seed=42)
         res, st = b.serve(insts, trace, hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)))
+        for t in trace:
+            renders[t[0]] += 1
+            all_requests.append(t[0])
         lat = latency_summary(res["latency_s"])
         span = float(res["done_s"].max() - min(t[2] for t in trace)) if len(trace) else 0.0
         lat.update({"rate_fps": rate, "window_s": dur, "throughput_fps": len(trace) / span if span > 0 else 0.0,
                     "submits": st["submits"], "max_in_flight": st["max_in_flight"],
                     "max_footprint_gb": st["max_footprint"] / (1 << 30)})
         out[tag] = lat
-    out["parity_sample"] = _serving_parity_sample(insts, trace)
     # Latency floor: the largest instance's frame alone on an idle GPU (one request, nothing else
     # in flight), end to end through the serving loop.
     big = max(range(len(streams)), key=lambda i: streams[i][2])
@@ -714,37 +721,62 @@ def _serving(args, device, model=None):
     for k in range(5):
         res, _ = b.serve(insts, [(big, frames[big], 0.0)], hbm_budget_bytes=int(args.serve_budget_gb * (1 << 30)))
         floor.append(float(res["latency_s"][0]) * 1e3)
+        renders[big] += 1
     out["latency_floor"] = {"instance": big, "primitives": int(streams[big][2]),
                             "resolution": "%dx%d" % (streams[big][3].width, streams[big][3].height),
                             "alone_ms_min": min(floor), "alone_ms_median": statistics.median(floor)}
+    out["parity_sample"] = _serving_parity_sample(insts, all_requests, renders)
     b.close()
     return out
 
 
-def _serving_parity_sample(insts, trace, fraction=0.01, seed=7):
-    """The serving configuration's output check: a seeded 1 % sample of the requests; each sampled
-    request's instance must hold the oracle's frame (RDRAM and hidden RDRAM digests committed in
-    tests/golden/configs.json by tests/golden/make_golden_configs.py).  Every frame of an instance
-    renders the same command words from a full-screen clear, so its image after the run is the
-    image of each of its frames."""
+def _serving_parity_sample(insts, requests, renders, fraction=0.01, seed=7):
+    """The serving configuration's output check, first half: a seeded 1 % sample of the served
+    requests; for each sampled request's instance, the digests of its RDRAM and hidden RDRAM after
+    the run and how many times it rendered its frame.  The CPU-baseline leg renders those instances'
+    frames as many times through the oracle and compares (_check_serving_parity)."""
     import hashlib
-    try:
-        golden = json.load(open(os.path.join(ROOT, "tests", "golden", "configs.json")))["instances"]
-    except (OSError, ValueError, KeyError):
-        return None
-    if not trace:
-        return {"requests_sampled": 0, "instances_checked": 0, "passed": False}
+    if not requests:
+        return {"requests_sampled": 0, "instances": {}}
     rng = np.random.default_rng(seed)
-    k = max(1, int(round(fraction * len(trace))))
-    picks = sorted(int(i) for i in rng.choice(len(trace), size=min(k, len(trace)), replace=False))
-    inst_ids = sorted({trace[i][0] for i in picks})
+    k = max(1, int(round(fraction * len(requests))))
+    picks = sorted(int(i) for i in rng.choice(len(requests), size=min(k, len(requests)), replace=False))
     sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).view(np.uint8).tobytes()).hexdigest()  # noqa: E731
-    bad = [i for i in inst_ids if i >= len(golden) or
-           sha(insts[i].begin_read_rdram()) != golden[i]["rdram_sha256"] or
-           sha(insts[i].begin_read_hidden_rdram()) != golden[i]["hidden_sha256"]]
-    return {"requests_sampled": len(picks), "of_requests": len(trace), "instances_checked": len(inst_ids),
-            "mismatches": bad, "passed": not bad,
-            "reference": "oracle digests (tests/golden/configs.json)"}
+    inst = {}
+    for i in sorted({requests[j] for j in picks}):
+        inst[i] = {"renders": renders[i], "rdram_sha256": sha(insts[i].begin_read_rdram()),
+                   "hidden_sha256": sha(insts[i].begin_read_hidden_rdram())}
+    return {"requests_sampled": len(picks), "of_requests": len(requests), "instances": inst}
+
+
+def _check_serving_parity(sample, threads=None):
+    """Second half (CPU-baseline leg): each sampled instance's frame rendered as many times through
+    the CPU oracle; digests must match.  Returns the report put in the bench line."""
+    import hashlib
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import Oracle
+    from rdp_gb300 import cmdgen
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).view(np.uint8).tobytes()).hexdigest()  # noqa: E731
+
+    def one(item):
+        i, want = item
+        words, rdram, _ = cmdgen.generate_stream(cmdgen.batched_instance_params(i))
+        o = Oracle(8 << 20)
+        o.write_rdram(rdram)
+        for _ in range(want["renders"]):
+            o.enqueue(words)
+        ok = sha(o.rdram()) == want["rdram_sha256"] and sha(o.hidden()) == want["hidden_sha256"]
+        o.close()
+        return i, ok
+
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 1) as ex:
+        results = list(ex.map(one, sorted(sample["instances"].items())))
+    bad = [i for i, ok in results if not ok]
+    return {"requests_sampled": sample["requests_sampled"], "of_requests": sample["of_requests"],
+            "instances_checked": len(results), "renders_checked": sum(v["renders"] for v in sample["instances"].values()),
+            "mismatches": bad, "passed": not bad and bool(results), "oracle_s": time.perf_counter() - t0,
+            "reference": "CPU oracle, each sampled instance's frame rendered as often as it was served"}
 
 
 def run_reference_batched(args):

@@ -39,6 +39,7 @@
 #include "sched.h"
 #include <cuda_fp16.h>
 #include "vi.h"
+#include "rdp_coherency.h"
 #include "blender_divider_runs.inc"
 
 namespace {
@@ -197,6 +198,65 @@ private:
 	std::thread worker_;
 };
 
+// Builds the page lists of the coherency kernels (coherency.cu) for any number of instances and
+// pages, launching a list whenever its instance slots or pages are full.
+class CohLauncher
+{
+public:
+	void add(uint8_t *host, uint8_t *dev, uint32_t *wmask, uint32_t page)
+	{
+		if (slot_ < 0 || L_.host[slot_] != host)
+		{
+			if (slots_used_ == RDP_COH_MAX_INSTANCES) flush_list();
+			slot_ = slots_used_++;
+			L_.host[slot_] = host;
+			L_.dev[slot_] = dev;
+			L_.wmask[slot_] = wmask;
+			if ((reinterpret_cast<uintptr_t>(host) & 15u) == 0) L_.host_aligned |= 1u << slot_;
+		}
+		L_.entry[L_.count++] = (uint32_t(slot_) << 24) | page;
+		if (L_.count == RDP_COH_MAX_PAGES)
+		{
+			const int keep = slot_;
+			uint8_t *h = L_.host[keep], *d = L_.dev[keep];
+			uint32_t *m = L_.wmask[keep];
+			flush_list();
+			slot_ = slots_used_++;
+			L_.host[slot_] = h;
+			L_.dev[slot_] = d;
+			L_.wmask[slot_] = m;
+			if ((reinterpret_cast<uintptr_t>(h) & 15u) == 0) L_.host_aligned |= 1u << slot_;
+		}
+	}
+	// Launches what is left; returns the first launch error.
+	cudaError_t finish(cudaStream_t stream, int to_host)
+	{
+		stream_ = stream;
+		to_host_ = to_host;
+		flush_list();
+		return err_;
+	}
+	void begin(cudaStream_t stream, int to_host)
+	{
+		stream_ = stream;
+		to_host_ = to_host;
+	}
+
+private:
+	void flush_list()
+	{
+		if (L_.count && err_ == cudaSuccess) err_ = rdp_coherency_launch(&L_, to_host_, stream_);
+		L_.count = 0;
+		L_.host_aligned = 0;
+		slots_used_ = 0;
+		slot_ = -1;
+	}
+	RdpCohList L_ = {};
+	int slots_used_ = 0, slot_ = -1, to_host_ = 0;
+	cudaStream_t stream_ = nullptr;
+	cudaError_t err_ = cudaSuccess;
+};
+
 } // namespace
 
 namespace rdpx {
@@ -315,6 +375,18 @@ struct rdp_cp
 	// ---------------------------------------------------------------- coherency + timeline
 	std::vector<std::pair<uint32_t, uint32_t>> dirty_ranges;
 	bool host_rdram_dirty = false;
+	// Page-granular coherency with the caller's RDRAM when it is mapped into the device's address
+	// space (rdp_renderer.cpp:2523-2907): every pass first refreshes the pages it reads from the
+	// host (masked: bytes the GPU wrote and has not yet returned stay), and a timeline value writes
+	// the bytes the GPU wrote back into the host pages (masked: other bytes stay the caller's).
+	bool coherent = false;
+	uint8_t *host_mapped = nullptr;    // host_rdram's address in the device's address space
+	uint32_t *d_wmask = nullptr;       // 1 bit per RDRAM byte written by the GPU, not yet returned
+	std::vector<uint8_t> page_written; // pages holding such bytes
+	std::vector<uint32_t> page_stamp;  // last pass that listed a page for refresh
+	uint32_t stamp = 0;
+	std::vector<uint32_t> read_pages;  // pages the pass being recorded reads
+	bool refresh_all = false;          // end_write_rdram: every page is refreshed before the next pass
 	uint64_t timeline_counter = 0;
 	std::deque<std::pair<uint64_t, cudaEvent_t>> pending;
 	std::vector<cudaEvent_t> free_events;
@@ -440,8 +512,12 @@ struct rdp_cp
 			if (!host_rdram) return RDP_ERR_OOM;
 			own_host_rdram = true;
 		}
-		host_registered = cudaHostRegister(host_rdram, rdram_size, cudaHostRegisterDefault) == cudaSuccess;
+		host_registered = cudaHostRegister(host_rdram, rdram_size, cudaHostRegisterMapped) == cudaSuccess;
 		if (!host_registered) cudaGetLastError();
+		if (host_registered && rdram_size >= RDP_RDRAM_PAGE_BYTES &&
+		    cudaHostGetDevicePointer(reinterpret_cast<void **>(&host_mapped), host_rdram, 0) == cudaSuccess)
+			coherent = true;
+		cudaGetLastError();
 		hidden_mirror.assign(hidden_size, 0x03);
 
 		if (cudaMalloc(&d_rdram, rdram_size) != cudaSuccess) return RDP_ERR_OOM;
@@ -449,6 +525,13 @@ struct rdp_cp
 		if (cudaMalloc(&d_tmem, 4096) != cudaSuccess) return RDP_ERR_OOM;
 		if (cudaMalloc(&d_snapshots, size_t(RDP_MAX_UPLOADS_PER_PASS + 1) * 4096) != cudaSuccess) return RDP_ERR_OOM;
 		if (cudaMalloc(&d_fragments, 4 * sizeof(unsigned long long)) != cudaSuccess) return RDP_ERR_OOM;
+		if (coherent)
+		{
+			if (cudaMalloc(&d_wmask, rdram_size / 8) != cudaSuccess) return RDP_ERR_OOM;
+			if (check(cudaMemsetAsync(d_wmask, 0, rdram_size / 8, stream))) return RDP_ERR_DEVICE;
+			page_written.assign(rdram_size / RDP_RDRAM_PAGE_BYTES, 0);
+			page_stamp.assign(rdram_size / RDP_RDRAM_PAGE_BYTES, 0);
+		}
 		if (!batch)
 		{
 			// A stand-alone processor sizes its executor for one full pass up front.
@@ -496,6 +579,7 @@ struct rdp_cp
 		cudaFree(d_tmem);
 		cudaFree(d_snapshots);
 		cudaFree(d_fragments);
+		cudaFree(d_wmask);
 		cudaFree(vi.d_aa);
 		cudaFree(vi.d_dv);
 		cudaFree(vi.d_out[0]);
@@ -558,7 +642,86 @@ struct rdp_cp
 		addr &= rdram_size - 1;
 		uint32_t end = std::min<uint64_t>(uint64_t(addr) + bytes, rdram_size);
 		if (in_capture()) capture_written.emplace_back(addr, end);
-		merge_dirty(addr, end);
+		if (coherent) mark_written_range(addr, end);
+		else merge_dirty(addr, end);
+	}
+	// Pages of RDRAM bytes [addr, addr + bytes), wrapping around RDRAM.
+	template <class F> void for_pages(uint64_t addr, uint64_t bytes, F f) const
+	{
+		if (!bytes) return;
+		const uint32_t np = rdram_size / RDP_RDRAM_PAGE_BYTES;
+		uint64_t first = (addr & (rdram_size - 1)) / RDP_RDRAM_PAGE_BYTES;
+		uint64_t count = ((addr & (RDP_RDRAM_PAGE_BYTES - 1)) + bytes + RDP_RDRAM_PAGE_BYTES - 1) / RDP_RDRAM_PAGE_BYTES;
+		if (count > np) count = np;
+		for (uint64_t k = 0; k < count; k++) f(uint32_t((first + k) % np));
+	}
+	void mark_written_range(uint32_t addr, uint32_t end)
+	{
+		for_pages(addr, uint64_t(end) - addr, [&](uint32_t pg) { page_written[pg] = 1; });
+	}
+	void mark_read_range(uint64_t addr, uint64_t bytes)
+	{
+		for_pages(addr, bytes, [&](uint32_t pg) {
+			if (page_stamp[pg] != stamp)
+			{
+				page_stamp[pg] = stamp;
+				read_pages.push_back(pg);
+			}
+		});
+	}
+	// The pages the recorded pass reads: its texture sources and its images.
+	void begin_page_list()
+	{
+		read_pages.clear();
+		if (++stamp == 0)
+		{
+			std::fill(page_stamp.begin(), page_stamp.end(), 0u);
+			stamp = 1;
+		}
+	}
+	void collect_read_pages()
+	{
+		begin_page_list();
+		if (refresh_all)
+		{
+			mark_read_range(0, rdram_size);
+			refresh_all = false;
+			return;
+		}
+		for (const RdpUpload &u : uploads)
+		{
+			const uint64_t bpt = u.vram_size >= 1 ? (uint64_t(1) << (u.vram_size - 1)) : 1;
+			const uint64_t lines = u.mode == 2 ? 1 : uint64_t(std::max(u.height, 1));
+			const uint64_t span = ((lines - 1) * uint64_t(std::max(u.vram_width, 0)) +
+			                       uint64_t(std::max(u.vram_effective_width, u.width))) * bpt + 8;
+			mark_read_range(uint32_t(u.vram_addr), span);
+		}
+		for (const Target &tg : targets)
+		{
+			if (!tg.width || !tg.deduced_height || tg.prim_ids.empty()) continue;
+			mark_read_range(tg.addr, uint64_t(tg.width) * tg.deduced_height * bytes_per_pixel(tg.fmt));
+			if (tg.depth_used || tg.depth_pending) mark_read_range(tg.depth_addr, uint64_t(tg.width) * tg.deduced_height * 2);
+		}
+	}
+	// Queues the masked host -> device refresh of the listed pages on the stream.
+	int refresh_pages(const std::vector<uint32_t> &pages)
+	{
+		if (pages.empty()) return RDP_OK;
+		CohLauncher cl;
+		cl.begin(stream, 0);
+		for (uint32_t pg : pages) cl.add(host_mapped, d_rdram, d_wmask, pg);
+		return check(cl.finish(stream, 0));
+	}
+	// Queues the masked write-back of every page with GPU writes; `cl` collects pages of several
+	// instances when given.
+	void write_back_pages(CohLauncher &cl)
+	{
+		for (size_t pg = 0; pg < page_written.size(); pg++)
+			if (page_written[pg])
+			{
+				cl.add(host_mapped, d_rdram, d_wmask, uint32_t(pg));
+				page_written[pg] = 0;
+			}
 	}
 	void merge_dirty(uint32_t addr, uint32_t end)
 	{
@@ -588,6 +751,7 @@ struct rdp_cp
 			reset_pass();
 			return sticky_error;
 		}
+		if (coherent) collect_read_pages();
 
 		const size_t num_recorded_prims = prims.size(), num_recorded_uploads = uploads.size();
 		rdpx::PassView v = {};
@@ -600,6 +764,7 @@ struct rdp_cp
 		common.hidden_size = hidden_size;
 		common.base_prim_index = uint32_t(base_prim_index);
 		common.counters = d_fragments;
+		common.wmask = coherent ? d_wmask : nullptr;
 		// One descriptor per target; a target that does not render (no colour image, or no
 		// covered line) keeps no primitives.  A pass without targets still applies its uploads.
 		bool single_in_order = targets.size() == 1;
@@ -667,10 +832,13 @@ struct rdp_cp
 			pk.state_blocks = std::move(state_blocks);
 			pk.tilesets = std::move(tilesets);
 			pk.uploads = std::move(uploads);
+			if (coherent && !in_capture()) pk.read_pages = read_pages;
 			deferred.push_back(std::move(pk));
 		}
 		else
 		{
+			// A capture records the GPU work only: its replays render against the device copy.
+			if (coherent && !capturing && refresh_pages(read_pages) != RDP_OK) return sticky_error;
 			uint64_t before = exec->kernel_launches;
 			if (!exec->launch(&v, 1, capturing ? &capture_sink : nullptr)) return check(cudaErrorUnknown);
 			stats.kernel_launches += exec->kernel_launches - before;
@@ -1424,6 +1592,17 @@ struct rdp_cp
 		p.gamma = (r.status & (1u << 3)) != 0;
 		p.gamma_dither = (r.status & (1u << 2)) != 0;
 		p.blend_prev = vi.have_prev && o->blend_previous_frame;
+		if (coherent && !degenerate)
+		{
+			// The VI reads the framebuffer lines it scans: those pages come from the caller's RDRAM
+			// first (resolve_coherency_external, rdp_device.cpp:1103).
+			begin_page_list();
+			mark_read_range(r.vi_offset, uint64_t(std::max(r.vi_width, 1)) * uint64_t(std::max(r.max_y, 0) + 3) *
+			                                 (is_8888 ? 4u : 2u));
+			if (refresh_all) mark_read_range(0, rdram_size);
+			refresh_all = false;
+			if (refresh_pages(read_pages) != RDP_OK) return sticky_error;
+		}
 		// The per-line registers are copied from pinned memory that the next scanout rewrites only
 		// after this copy has finished.
 		if (vi.lines_copied && check(cudaEventSynchronize(vi.lines_copied))) return sticky_error;
@@ -1507,6 +1686,13 @@ struct rdp_cp
 
 	int copy_back()
 	{
+		if (coherent)
+		{
+			CohLauncher cl;
+			cl.begin(stream, 1);
+			write_back_pages(cl);
+			return check(cl.finish(stream, 1));
+		}
 		for (auto &r : dirty_ranges)
 		{
 			if (host_registered)
@@ -1531,10 +1717,11 @@ struct rdp_cp
 
 	// A batched instance's deferred passes have been launched (rdp_batch::submit): its
 	// signalled timeline values complete after them and after the copy-back.
-	int complete_submitted()
+	int complete_submitted(CohLauncher *write_back)
 	{
 		if (unsubmitted.empty()) return sticky_error;
-		if (copy_back() != RDP_OK) return sticky_error;
+		if (coherent && write_back) write_back_pages(*write_back); // launched by the caller, for all instances
+		else if (copy_back() != RDP_OK) return sticky_error;
 		for (uint64_t v : unsubmitted)
 		{
 			cudaEvent_t e = get_event();
@@ -1746,22 +1933,39 @@ struct rdp_batch
 		{
 			views.clear();
 			owners.clear();
+			CohLauncher refresh;
+			refresh.begin(stream, 0);
 			for (rdp_cp *cp : instances)
 				if (!cp->deferred.empty())
 				{
 					views.push_back(cp->deferred.front().view());
 					owners.push_back(cp);
+					for (uint32_t pg : cp->deferred.front().read_pages) refresh.add(cp->host_mapped, cp->d_rdram, cp->d_wmask, pg);
 				}
 			if (views.empty()) break;
+			// The round's pages come from the callers' RDRAM first (one launch for all instances).
+			if (refresh.finish(stream, 0) != cudaSuccess) return sticky_error = RDP_ERR_DEVICE;
 			if (!exec.launch(views.data(), uint32_t(views.size()), capturing ? &sink : nullptr))
 				return sticky_error = RDP_ERR_DEVICE;
 			rounds++;
 			passes += views.size();
 			for (rdp_cp *cp : owners) cp->deferred.pop_front();
 		}
+		// Masked write-back of every signalled instance's pages in as few launches as possible, then
+		// the instances' timeline events after it.
+		CohLauncher write_back;
+		write_back.begin(stream, 1);
+		std::vector<rdp_cp *> signalled;
 		for (rdp_cp *cp : instances)
+			if (!cp->unsubmitted.empty())
+			{
+				signalled.push_back(cp);
+				if (cp->coherent) cp->write_back_pages(write_back);
+			}
+		if (write_back.finish(stream, 1) != cudaSuccess) return sticky_error = RDP_ERR_DEVICE;
+		for (rdp_cp *cp : signalled)
 		{
-			int r = cp->complete_submitted();
+			int r = cp->complete_submitted(nullptr);
 			if (r != RDP_OK) return sticky_error = r;
 		}
 		return RDP_OK;
@@ -1920,8 +2124,20 @@ int rdp_cp_end_write_rdram(rdp_cp *cp)
 {
 	if (!cp) return RDP_ERR_INVALID;
 	cp->sync_ring();
+	cudaSetDevice(cp->device);
+	if (cp->coherent)
+	{
+		// Pages are refreshed from the caller's RDRAM whenever the GPU reads them; this makes the
+		// next pass refresh all of them (masked), for consumers that rely on the call.
+		cp->refresh_all = true;
+		return RDP_OK;
+	}
+	// Without mapped host memory: the whole RDRAM is uploaded in stream order, after the work
+	// queued so far (a batch instance's deferred passes are launched first).
+	int r = cp->sync_point();
+	if (r != RDP_OK) return r;
 	cp->host_rdram_dirty = true;
-	return RDP_OK;
+	return cp->flush();
 }
 
 void *rdp_cp_begin_read_hidden_rdram(rdp_cp *cp)
@@ -2219,7 +2435,11 @@ int rdp_graph_replay(rdp_graph *g, uint32_t count, float *elapsed_ms)
 		if (g->batch && std::find(g->batch->instances.begin(), g->batch->instances.end(), w.first) ==
 		                    g->batch->instances.end())
 			continue;
-		for (auto &rg : w.second) w.first->merge_dirty(rg.first, rg.second);
+		for (auto &rg : w.second)
+		{
+			if (w.first->coherent) w.first->mark_written_range(rg.first, rg.second);
+			else w.first->merge_dirty(rg.first, rg.second);
+		}
 	}
 	if (elapsed_ms && cudaEventElapsedTime(elapsed_ms, g->ev[0], g->ev[1]) != cudaSuccess) return RDP_ERR_DEVICE;
 	// GPU time of the rasteriser launches of the last replay.

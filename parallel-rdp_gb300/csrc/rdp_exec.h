@@ -153,6 +153,7 @@ struct PassPacket
 	std::vector<uint32_t> words, state_blocks;
 	std::vector<RdpTile> tilesets;
 	std::vector<RdpUpload> uploads;
+	std::vector<uint32_t> read_pages; // RDRAM pages refreshed from the caller's memory before the pass
 
 	PassView view() const
 	{

@@ -1929,6 +1929,39 @@ __device__ void load_pixel(const RdpPass &p, Pix &px, uint32_t ci, uint32_t di)
 	px.dz = (hid(p, didx) | int((w & 3) << 2)) & 0xff;
 }
 
+// Marks RDRAM bytes [addr, addr + n) (n <= 4, not crossing a 32-byte line: the pixel formats'
+// natural alignment) as written by the GPU in the instance's write mask, which the masked
+// write-back to the caller's RDRAM reads.  Called by all 32 lanes of a warp together; lanes whose
+// bytes share a mask word merge them into one atomic.
+__device__ __forceinline__ void mark_written(const RdpPass &p, bool any, uint32_t addr, uint32_t n)
+{
+	if (!p.wmask) return;
+	const uint32_t word = any ? (addr & (p.rdram_size - 1)) >> 5 : 0xffffffffu;
+	const uint32_t bits = any ? ((n >= 32 ? 0xffffffffu : ((1u << n) - 1u)) << (addr & 31u)) : 0u;
+	const unsigned peers = __match_any_sync(0xffffffffu, word);
+	const uint32_t merged = __reduce_or_sync(peers, bits);
+	if (any && (__ffs(int(peers)) - 1) == int(threadIdx.x & 31)) atomicOr(p.wmask + word, merged);
+}
+
+// The bytes a pixel store writes: colour (1, 2 or 4 bytes at the format's address swizzle) and depth
+// (2 bytes).  Mirrors store_pixel's addressing.
+__device__ __forceinline__ void mark_pixel(const RdpPass &p, const Pix &px, uint32_t ci, uint32_t di, bool alias,
+                                           bool stored)
+{
+	bool c = stored && px.cdirty, d = stored && !alias && px.ddirty;
+	uint32_t ca = 0, cn = 0;
+	switch (p.fb_fmt)
+	{
+	case FBF_I4:
+	case FBF_I8: ca = (ci & (p.rdram_size - 1)) ^ 3u; cn = 1; break;
+	case FBF_RGBA5551:
+	case FBF_IA88: ca = ((ci & ((p.rdram_size >> 1) - 1)) ^ 1u) * 2u; cn = 2; break;
+	default: ca = (ci & ((p.rdram_size >> 2) - 1)) * 4u; cn = 4; break;
+	}
+	mark_written(p, c, ca, cn);
+	mark_written(p, d, ((di & ((p.rdram_size >> 1) - 1)) ^ 1u) * 2u, 2);
+}
+
 __device__ void store_pixel(const RdpPass &p, const Pix &px, uint32_t ci, uint32_t di, bool alias)
 {
 	if (px.cdirty)
@@ -3386,6 +3419,7 @@ __device__ __forceinline__ void blend_tile(uint32_t item, const RdpPass *__restr
 		}
 		store_pixel(ps, px, ci, di, pc.alias);
 	}
+	if (ps.wmask) mark_pixel(ps, px, ci, di, pc.alias, inside);
 	unsigned long long *counters = ps.counters;
 	if (counters)
 	{
@@ -3531,6 +3565,7 @@ __device__ __forceinline__ void raster_tile(uint32_t item, const RdpPass *__rest
 		}
 	}
 	if (loaded && inside) store_pixel(ps, px, ci, di, pc.alias);
+	if (ps.wmask) mark_pixel(ps, px, ci, di, pc.alias, loaded && inside);
 
 	// Both warps have consumed the bitmask: clear it for the next pass using this slot.
 	if (threadIdx.x == 0) s_any = 0;

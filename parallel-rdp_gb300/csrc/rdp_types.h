@@ -214,6 +214,12 @@ typedef struct __attribute__((aligned(16))) RdpPass
 	   (a primitive's word_offset / state_block / tileset are relative to its pass). */
 	uint32_t word_base, sb_base, ts_base, pad0;
 	unsigned long long *counters; /* the instance's [0] fragments, [1] touched tiles, [2] tile instances */
+	uint32_t *wmask;              /* the instance's RDRAM write mask (1 bit per byte), or null */
 } RdpPass;
+
+/* RDRAM coherency with the caller's host memory (the reference's incoherent path,
+ * rdp_renderer.cpp:2523-2907): pages of RDRAM_PAGE_BYTES. */
+#define RDP_RDRAM_PAGE_BYTES 4096u
+
 
 #endif

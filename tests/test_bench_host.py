@@ -91,3 +91,28 @@ def test_step_hbm_roofline_counts_commands_tiles_and_texture_sources():
     assert r["algorithmic_bytes_per_step"] == 1000 + 10 * 64 * 2 * 9 + 3 * 4096
     assert abs(r["achieved"] - r["algorithmic_bytes_per_step"] / 1e-3 / 1e9) < 1e-9
     assert abs(r["frac"] - r["achieved"] / 8000.0) < 1e-12
+
+
+def test_serving_parity_check_renders_each_sampled_instance_as_often_as_it_was_served():
+    """The serving bench's 1 % output sample: digests and render counts recorded on the GPU side are
+    checked by rendering the same instance's frame that many times through the oracle."""
+    import hashlib
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import bench
+    from oracle import Oracle
+    from rdp_gb300 import cmdgen
+    sha = lambda a: hashlib.sha256(np.ascontiguousarray(a).view(np.uint8).tobytes()).hexdigest()  # noqa: E731
+    words, rdram, _ = cmdgen.generate_stream(cmdgen.batched_instance_params(5))
+    o = Oracle(8 << 20)
+    o.write_rdram(rdram)
+    for _ in range(3):
+        o.enqueue(words)
+    good = {"renders": 3, "rdram_sha256": sha(o.rdram()), "hidden_sha256": sha(o.hidden())}
+    o.close()
+    r = bench._check_serving_parity({"requests_sampled": 2, "of_requests": 200, "instances": {5: good}}, threads=2)
+    assert r["passed"] and r["instances_checked"] == 1 and r["renders_checked"] == 3
+    # Instance 5's frame is not idempotent: one render gives another image than three.
+    wrong = dict(good, renders=1)
+    r = bench._check_serving_parity({"requests_sampled": 2, "of_requests": 200, "instances": {5: wrong}}, threads=2)
+    assert not r["passed"] and r["mismatches"] == [5]

@@ -15,13 +15,16 @@
  * GPU work is asynchronous and tracked by a monotonically increasing 64-bit
  * timeline.
  *
- * RDRAM ownership: the caller owns RDRAM (rdp_device.cpp:81-87).  The
- * authoritative copy lives in device memory (HBM).  The caller's buffer is
- * uploaded at creation and by rdp_cp_end_write_rdram(); framebuffer bytes the
- * GPU writes are copied back into the caller's buffer before the timeline value
- * that covers them completes (the reference's incoherent path,
- * rdp_renderer.cpp:2523-2907, at framebuffer granularity).  Hidden RDRAM and
- * TMEM are owned by the processor (rdp_device.cpp:120-131).
+ * RDRAM ownership: the caller owns RDRAM (rdp_device.cpp:81-87).  The GPU
+ * renders into a device copy (HBM) kept coherent with the caller's buffer page
+ * by page, as the reference's incoherent-host path does
+ * (rdp_renderer.cpp:2523-2907): the buffer is registered and mapped, every pass
+ * first reads the pages it needs (texture sources, images) from it -- except
+ * bytes the GPU wrote and has not yet returned -- and a timeline value writes
+ * back exactly the bytes the GPU wrote, before it completes.  Pages are read when
+ * the pass runs on the GPU, so the caller does not modify pages that unfinished
+ * work reads.  Hidden RDRAM and TMEM are owned by the processor
+ * (rdp_device.cpp:120-131).
  */
 #ifndef RDP_CUDA_H
 #define RDP_CUDA_H
@@ -118,7 +121,9 @@ int rdp_cp_set_validation_callback(rdp_cp *cp, rdp_validation_cb cb, void *user)
 
 /* CommandProcessor::begin_read_rdram / end_write_rdram / begin_read_hidden_rdram /
  * end_write_hidden_rdram / get_rdram_size / get_hidden_rdram_size / get_tmem
- * (rdp_device.cpp:996-1037). */
+ * (rdp_device.cpp:996-1037).  begin_read_rdram idles and returns the caller's buffer;
+ * end_write_rdram makes the next pass refresh every RDRAM page (writes are also picked
+ * up without it, page by page, when a pass reads them). */
 void *rdp_cp_begin_read_rdram(rdp_cp *cp);
 int rdp_cp_end_write_rdram(rdp_cp *cp);
 void *rdp_cp_begin_read_hidden_rdram(rdp_cp *cp);

@@ -1844,8 +1844,23 @@ struct rdp_cp
 		int r = signal_timeline(&v);
 		if (r != RDP_OK) return r;
 		r = wait_timeline(v, UINT64_MAX / 2);
-		if (r == RDP_OK && !batch) own_exec.tune_epoch();
+		if (r == RDP_OK && !batch)
+		{
+			own_exec.tune_epoch();
+			r = device_error_status(own_exec);
+		}
 		return r;
+	}
+
+	// A bounded wait inside a kernel gave up: the results of the work since the last check are
+	// incomplete.  Reported, and sticky.
+	int device_error_status(rdpx::Executor &ex)
+	{
+		const uint32_t e = ex.take_device_error();
+		if (!e) return sticky_error;
+		report(-1, "a bounded wait on the GPU gave up; the work since the last timeline value is incomplete");
+		sticky_error = RDP_ERR_TIMEOUT;
+		return sticky_error;
 	}
 
 	// ---------------------------------------------------------------- C ABI side of the command thread
@@ -2574,6 +2589,7 @@ int rdp_batch_idle(rdp_batch *b)
 	}
 	if (!b->capturing && !b->exec.adapt_pairs()) return b->sticky_error = RDP_ERR_DEVICE;
 	b->exec.tune_epoch();
+	if (b->exec.take_device_error()) return b->sticky_error = RDP_ERR_TIMEOUT;
 	return RDP_OK;
 }
 

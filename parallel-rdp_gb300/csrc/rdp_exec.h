@@ -468,7 +468,7 @@ struct Executor
 			launch_log = fopen(e, "a");
 			if (launch_log && check(cudaMalloc(&d_launch_pairs, kLaunchLogSlots * 4))) return false;
 		}
-		if (check(cudaMalloc(&d_ctrl, 32)) || check(cudaMalloc(&d_pair_log, 256 * 4)) ||
+		if (check(cudaMalloc(&d_ctrl, 64)) || check(cudaMalloc(&d_pair_log, 256 * 4)) ||
 		    check(cudaMalloc(&d_queues, queue_bytes())) ||
 		    check(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking)))
 			return false;
@@ -476,7 +476,7 @@ struct Executor
 			if (check(cudaEventCreateWithFlags(&slot_copied[k], cudaEventDisableTiming)) ||
 			    check(cudaEventCreateWithFlags(&slot_free[k], cudaEventDisableTiming)))
 				return false;
-		return !check(cudaMemsetAsync(d_ctrl, 0, 32, stream)) && !check(cudaMemsetAsync(d_queues, 0, queue_bytes(), stream));
+		return !check(cudaMemsetAsync(d_ctrl, 0, 64, stream)) && !check(cudaMemsetAsync(d_queues, 0, queue_bytes(), stream));
 	}
 
 	int current_variant()
@@ -734,6 +734,17 @@ struct Executor
 			caps.staging = n;
 		}
 		return !check(cudaStreamSynchronize(stream));
+	}
+
+	// With the stream idle: the device error word (ctrl[8]; bit 0: a k_blend staging wait gave
+	// up), cleared once read.  A non-zero word means a launch's results are incomplete.
+	uint32_t take_device_error()
+	{
+		uint32_t e = 0;
+		if (check(cudaMemcpy(&e, d_ctrl + 8, 4, cudaMemcpyDeviceToHost))) return ~0u;
+		if (e && check(cudaMemset(d_ctrl + 8, 0, 4))) return ~0u;
+		if (e) failed = true;
+		return e;
 	}
 
 	// With the stream idle: grows the pair scratch and the span rows to the largest counts a

@@ -3312,23 +3312,103 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 // ============================================================================ k_blend
 // One 64-thread CTA per tile: the tile's colour/depth stay in registers while its pairs are
 // applied in primitive order (the reference's depth_blend.comp), then written back.
-__device__ __forceinline__ void blend_tile(uint32_t item, const RdpPass *__restrict__ passes, uint32_t num_passes,
+//
+// The per-pair inputs come through shared memory: a ring of BLEND_STAGES stages, each holding up
+// to BLEND_CHUNK consecutive pairs of the tile -- their shaded records (a tile's pairs are
+// consecutive in the scratch, so one 1-D bulk copy moves them all) and each pair's primitive
+// state (one 128-byte bulk copy per pair).  Thread 0 issues the copies a stage ahead; they complete
+// on the stage's mbarrier (transaction bytes).  So no global load sits in a pixel's serial chain of
+// pairs.  Waits are bounded: a wait that gives up sets bit 0 of the launch's error word (ctrl[8])
+// and the CTA stops.
+constexpr int BLEND_STAGES = 2, BLEND_CHUNK = 4;
+constexpr uint32_t BLEND_WAIT_POLLS = 1u << 20; // mbarrier polls before a wait gives up
+constexpr uint32_t BLEND_ERR_WAIT = 1u;
+
+struct __align__(128) BlendStage
+{
+	uint2 rec[BLEND_CHUNK][SHADE_THREADS];     // shaded records, 512 bytes per pair
+	RdpPrimShade shade[BLEND_CHUNK];           // primitive state, 128 bytes per pair
+};
+static_assert(sizeof(RdpPrimShade) == 128, "one bulk copy per primitive state");
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return uint32_t(__cvta_generic_to_shared(p)); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+	uint32_t done;
+	asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+	             : "=r"(done)
+	             : "r"(smem_u32(bar)), "r"(parity)
+	             : "memory");
+	return done != 0;
+}
+// Bounded wait for the phase with parity `parity` of `bar` to complete.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+	for (uint32_t i = 0; i < BLEND_WAIT_POLLS; i++)
+		if (mbar_try_wait(bar, parity)) return true;
+	return false;
+}
+// 1-D bulk copy global -> shared completing on `bar` (16-byte aligned, size a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+	                 smem_u32(dst)),
+	             "l"(src), "r"(bytes), "r"(smem_u32(bar))
+	             : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Thread 0: stage `st` receives pairs [first, first + count) of the scratch and their primitives'
+// state; the copies complete on `bar`.
+__device__ __forceinline__ void blend_issue(BlendStage &st, uint64_t *bar, uint32_t first, uint32_t count,
+                                            const uint2 *__restrict__ pairs, const RdpPrimShade *__restrict__ shade,
+                                            const uint2 *__restrict__ sc)
+{
+	fence_proxy_async_smem(); // the stage's previous contents were read through the generic proxy
+	mbar_arrive_expect_tx(bar, count * (SHADE_THREADS * 8u + uint32_t(sizeof(RdpPrimShade))));
+	bulk_g2s(&st.rec[0][0], sc + size_t(first) * SHADE_THREADS, count * SHADE_THREADS * 8u, bar);
+	for (uint32_t k = 0; k < count; k++)
+		bulk_g2s(&st.shade[k], shade + pairs[first + k].x, uint32_t(sizeof(RdpPrimShade)), bar);
+}
+
+// Returns false when a staging wait gave up (the error word is set; the CTA must stop).
+__device__ __forceinline__ bool blend_tile(uint32_t item, const RdpPass *__restrict__ passes, uint32_t num_passes,
                                            const uint32_t *__restrict__ offsets, const uint2 *__restrict__ pairs,
                                            const RdpPrimShade *__restrict__ shade, const uint2 *__restrict__ sc,
-                                           uint32_t *__restrict__ cycles)
+                                           uint32_t *__restrict__ cycles, BlendStage *stages, uint64_t *bars,
+                                           uint32_t &chunk_seq, uint32_t &issued_seq, uint32_t *__restrict__ err)
 {
 	const uint32_t p0 = offsets[item], p1 = offsets[item + 1];
+	const int tid = threadIdx.x;
 	if (p0 == p1)
 	{
-		if (cycles && threadIdx.x == 0) cycles[item] = 0;
-		return;
+		if (cycles && tid == 0) cycles[item] = 0;
+		return true;
 	}
 	const long long t_start = clock64();
+	const uint32_t nchunks = (p1 - p0 + BLEND_CHUNK - 1) / BLEND_CHUNK;
+	auto chunk_count = [&](uint32_t c) { return min(uint32_t(BLEND_CHUNK), p1 - p0 - c * BLEND_CHUNK); };
+	// The first stages fill while the tile's pixels load.
+	if (tid == 0)
+		for (uint32_t c = 0; c < nchunks && c < uint32_t(BLEND_STAGES); c++)
+		{
+			const uint32_t sidx = (chunk_seq + c) % BLEND_STAGES;
+			blend_issue(stages[sidx], &bars[sidx], p0 + c * BLEND_CHUNK, chunk_count(c), pairs, shade, sc);
+			issued_seq++;
+		}
 	const uint32_t pi = pass_of_item(passes, num_passes, item);
 	const RdpPass &ps = passes[pi];
 	const uint32_t tl = item - ps.tile_item_begin;
 	const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
-	const int tid = threadIdx.x;
 	const int x = tx * 8 + (tid & 7), y = ty * 8 + (tid >> 3);
 	const bool inside = x < int(ps.fb_width) && y < int(ps.fb_height);
 	PassConst pc;
@@ -3354,71 +3434,57 @@ __device__ __forceinline__ void blend_tile(uint32_t item, const RdpPass *__restr
 	const uint32_t di = (ps.depth_addr >> 1) + ps.fb_width * uint32_t(y) + uint32_t(x);
 	Pix px;
 	uint32_t frags = 0;
-	if (inside)
+	if (inside) load_pixel(ps, px, ci, di);
+	for (uint32_t c = 0; c < nchunks; c++)
 	{
-		load_pixel(ps, px, ci, di);
-		// Software pipeline: the shaded record and primitive of pair pr + BLEND_AHEAD are loaded
-		// (and its primitive's shading state prefetched into L1) while pair pr blends.
-		constexpr int BLEND_AHEAD = 2;
-		uint2 q_rec[BLEND_AHEAD];
-		uint32_t q_prim[BLEND_AHEAD];
-#pragma unroll
-		for (int k = 0; k < BLEND_AHEAD; k++)
+		const uint32_t sidx = chunk_seq % BLEND_STAGES, parity = (chunk_seq / BLEND_STAGES) & 1u;
+		const bool ok = mbar_wait(&bars[sidx], parity);
+		if (__syncthreads_or(!ok))
 		{
-			const uint32_t pr = p0 + uint32_t(k);
-			q_rec[k] = kScratchEmpty;
-			q_prim[k] = 0u;
-			if (pr < p1)
-			{
-				q_rec[k] = sc[size_t(pr) * SHADE_THREADS + tid];
-				q_prim[k] = pairs[pr].x;
-				asm volatile("prefetch.global.L1 [%0];" ::"l"(shade + q_prim[k]));
-			}
+			if (tid == 0) atomicOr(err, BLEND_ERR_WAIT);
+			return false;
 		}
-		for (uint32_t pr = p0; pr < p1; pr++)
+		const BlendStage &st = stages[sidx];
+		const uint32_t cnt = chunk_count(c);
+		if (inside)
+			for (uint32_t k = 0; k < cnt; k++)
+			{
+				const uint2 rec = st.rec[k][tid];
+				const uint32_t code = (rec.y >> 18) & 15u;
+				if (code == SC_NONE) continue;
+				const RdpPrimShade &sh = st.shade[k];
+				Shaded in;
+				in.combined = rec.x;
+				in.shade_alpha = 0;
+				if (code == SC_FILL)
+				{
+					in.coverage = 0x40;
+					in.z_dith = 0;
+				}
+				else if (code == SC_COPY)
+				{
+					in.coverage = 0x20;
+					in.z_dith = int(rec.y & 0xffffu);
+				}
+				else
+				{
+					in.coverage = int(code);
+					in.shade_alpha = int(rec.y >> 22);
+					const uint32_t noise = (sh.static_flags & RS_NEED_NOISE) ? reseed_noise(uint32_t(x), uint32_t(y), sh.prim_index) : 0u;
+					in.z_dith = int((rec.y & 0x3ffffu) << 9) | rgb_dither_value(sh.static_flags, sh.dither, x, y, noise);
+				}
+				frags += blend_pixel(ps, pc, sh, in, px);
+			}
+		__syncthreads(); // every thread is done with the stage
+		if (tid == 0 && c + BLEND_STAGES < nchunks)
 		{
-			const uint2 rec = q_rec[0];
-			const uint32_t prim = q_prim[0];
-#pragma unroll
-			for (int k = 0; k + 1 < BLEND_AHEAD; k++)
-			{
-				q_rec[k] = q_rec[k + 1];
-				q_prim[k] = q_prim[k + 1];
-			}
-			const uint32_t nx = pr + BLEND_AHEAD;
-			if (nx < p1)
-			{
-				q_rec[BLEND_AHEAD - 1] = sc[size_t(nx) * SHADE_THREADS + tid];
-				q_prim[BLEND_AHEAD - 1] = pairs[nx].x;
-				asm volatile("prefetch.global.L1 [%0];" ::"l"(shade + q_prim[BLEND_AHEAD - 1]));
-			}
-			const uint32_t code = (rec.y >> 18) & 15u;
-			if (code == SC_NONE) continue;
-			const RdpPrimShade &sh = shade[prim];
-			Shaded in;
-			in.combined = rec.x;
-			in.shade_alpha = 0;
-			if (code == SC_FILL)
-			{
-				in.coverage = 0x40;
-				in.z_dith = 0;
-			}
-			else if (code == SC_COPY)
-			{
-				in.coverage = 0x20;
-				in.z_dith = int(rec.y & 0xffffu);
-			}
-			else
-			{
-				in.coverage = int(code);
-				in.shade_alpha = int(rec.y >> 22);
-				const uint32_t noise = (sh.static_flags & RS_NEED_NOISE) ? reseed_noise(uint32_t(x), uint32_t(y), sh.prim_index) : 0u;
-				in.z_dith = int((rec.y & 0x3ffffu) << 9) | rgb_dither_value(sh.static_flags, sh.dither, x, y, noise);
-			}
-			frags += blend_pixel(ps, pc, sh, in, px);
+			const uint32_t n = c + BLEND_STAGES;
+			blend_issue(stages[sidx], &bars[sidx], p0 + n * BLEND_CHUNK, chunk_count(n), pairs, shade, sc);
+			issued_seq++;
 		}
-		store_pixel(ps, px, ci, di, pc.alias);
+		chunk_seq++;
 	}
+	if (inside) store_pixel(ps, px, ci, di, pc.alias);
 	if (ps.wmask) mark_pixel(ps, px, ci, di, pc.alias, inside);
 	unsigned long long *counters = ps.counters;
 	if (counters)
@@ -3439,6 +3505,7 @@ __device__ __forceinline__ void blend_tile(uint32_t item, const RdpPass *__restr
 		__syncthreads();
 		if (tid == 0) cycles[item] = uint32_t(min(clock64() - t_start, 0xffffffffll));
 	}
+	return true;
 }
 
 // Persistent CTAs take non-empty tiles from a shared counter, in the order of `order`
@@ -3454,9 +3521,18 @@ __global__ void __launch_bounds__(SHADE_THREADS, 24) k_blend(const RdpPass *__re
                                                         const uint32_t *__restrict__ order,
                                                         uint32_t *__restrict__ cycles)
 {
+	__shared__ BlendStage s_stage[BLEND_STAGES];
+	__shared__ __align__(8) uint64_t s_bar[BLEND_STAGES];
 	__shared__ uint32_t s_next;
 	if (ctrl[1]) return;
+	if (threadIdx.x == 0)
+	{
+		for (int i = 0; i < BLEND_STAGES; i++) mbar_init(&s_bar[i], 1);
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	__syncthreads();
 	const uint32_t n = ctrl[3];
+	uint32_t chunk_seq = 0, issued_seq = 0; // chunks consumed / issued by this CTA (issued_seq: thread 0)
 	for (;;)
 	{
 		if (threadIdx.x == 0) s_next = atomicAdd(&ctrl[4], 1u);
@@ -3465,7 +3541,16 @@ __global__ void __launch_bounds__(SHADE_THREADS, 24) k_blend(const RdpPass *__re
 		__syncthreads();
 		if (k >= n) break;
 		const uint32_t item = order ? order[k] : nonempty[k];
-		blend_tile(item, passes, num_passes, offsets, pairs, shade, sc, cycles);
+		if (!blend_tile(item, passes, num_passes, offsets, pairs, shade, sc, cycles, s_stage, s_bar, chunk_seq,
+		                issued_seq, ctrl + 8))
+		{
+			// A wait gave up: the copies still in flight (issued, not consumed) finish before the
+			// CTA's shared memory goes away, each wait bounded again.
+			if (threadIdx.x == 0)
+				for (uint32_t q = chunk_seq; q < issued_seq; q++)
+					mbar_wait(&s_bar[q % BLEND_STAGES], (q / BLEND_STAGES) & 1u);
+			break;
+		}
 	}
 }
 

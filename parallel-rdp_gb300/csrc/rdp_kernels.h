@@ -47,7 +47,8 @@ typedef struct RdpLaunch
 	uint32_t *scan_blocks;          /* [2 * ceil(num_tile_items / 1024)]: multi-CTA scan partials */
 	uint32_t *pair_offsets;         /* [num_tile_items + 1] */
 	uint2 *pairs;                   /* [pair_capacity] (global primitive index, tile item) */
-	uint32_t *ctrl;                 /* [0] pairs, [1] overflow, [2] max pairs, [3] non-empty tiles, [4] counter */
+	uint32_t *ctrl;                 /* [0] pairs, [1] overflow, [2] max pairs, [3] non-empty tiles, [4] counter,
+	                                   [5] max span rows, [6..7] span-row counter, [8] device error word */
 	uint32_t pair_capacity;
 	uint32_t shade_ctas;            /* persistent CTAs of k_shade (and of k_blend / k_raster) */
 	uint32_t *shade_queues;         /* optional [num_shade_queues + ceil(num_shade_queues / 32)]: per-SM

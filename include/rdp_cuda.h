@@ -144,6 +144,9 @@ typedef struct rdp_scanout_options
 	uint32_t blend_previous_frame;
 	uint32_t upscale_deinterlacing; /* 1 (default): serrate is not woven at 1x; 0: weave the fields */
 	uint32_t vi_aa, vi_scale, vi_serrate, vi_dither_filter, vi_divot_filter, vi_gamma_dither;
+	/* Halvings of an upscaled image before output (video_interface.hpp:51); the scanout here is at
+	 * 1x scale, where the reference skips them too (video_interface.cpp:1009, 1354). */
+	uint32_t downscale_steps;
 } rdp_scanout_options;
 /* Fills the reference's defaults (every VI filter on, upscale deinterlacing on). */
 void rdp_scanout_options_default(rdp_scanout_options *opts);

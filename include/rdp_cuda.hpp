@@ -299,6 +299,7 @@ private:
 		o.vi_dither_filter = s.vi.dither_filter;
 		o.vi_divot_filter = s.vi.divot_filter;
 		o.vi_gamma_dither = s.vi.gamma_dither;
+		o.downscale_steps = s.downscale_steps < 8 ? s.downscale_steps : 8; // video_interface.cpp:1217
 		return o;
 	}
 

@@ -58,7 +58,7 @@ class ScanoutOptions(ctypes.Structure):
                 ("blend_previous_frame", ctypes.c_uint32), ("upscale_deinterlacing", ctypes.c_uint32),
                 ("vi_aa", ctypes.c_uint32), ("vi_scale", ctypes.c_uint32), ("vi_serrate", ctypes.c_uint32),
                 ("vi_dither_filter", ctypes.c_uint32), ("vi_divot_filter", ctypes.c_uint32),
-                ("vi_gamma_dither", ctypes.c_uint32)]
+                ("vi_gamma_dither", ctypes.c_uint32), ("downscale_steps", ctypes.c_uint32)]
 
     def __init__(self, **kw):
         super().__init__()

@@ -128,3 +128,51 @@ def test_vi_per_scanline_hstart_xscale():
         got = cp.scanout_sync(opts)
         exp = o.scanout(opts.as_words())
         assert got is not None and np.array_equal(got, exp)
+
+
+def test_vi_crop_persist_and_downscale_options():
+    """ScanoutOptions beyond the filters (video_interface.cpp:1215-1310): the crop rectangle and the
+    aspect-preserving overscan crop (doubled when interlaced), persist_frame_on_invalid_input (an
+    invalid VI state within four frames of a valid one repeats the last image, later ones give no
+    image) and downscale_steps (no effect at 1x scale), against the oracle frame by frame."""
+    from oracle import Oracle
+    rng = np.random.default_rng(11)
+    rd = rng.integers(0, 256, RDRAM, dtype=np.uint8)
+    hid = rng.integers(0, 4, RDRAM // 2, dtype=np.uint8)
+    o = Oracle(RDRAM)
+    o.write_rdram(rd)
+    o.write_hidden(hid)
+    base = dict(aa=0, fmt=2, divot=True, dither=True, gamma=True, gamma_dither=False, serrate=False, pal=False)
+    serr = dict(base, serrate=True)
+    cases = [
+        (base, ScanoutOptions(crop_rect_enable=1, crop_left=13, crop_right=7, crop_top=5, crop_bottom=9), False),
+        (serr, ScanoutOptions(crop_rect_enable=1, crop_left=3, crop_right=21, crop_top=4, crop_bottom=2,
+                              upscale_deinterlacing=0), False),
+        (base, ScanoutOptions(crop_overscan_pixels=8), False),
+        (serr, ScanoutOptions(crop_overscan_pixels=6, upscale_deinterlacing=0), False),
+        (base, ScanoutOptions(downscale_steps=3), False),
+        # valid, then invalid states (h_start beyond the line): repeated within four frames, then none
+        (base, ScanoutOptions(persist_frame_on_invalid_input=1), False),
+    ] + [(base, ScanoutOptions(persist_frame_on_invalid_input=1), True)] * 6
+    with CommandProcessor(np.zeros(RDRAM, np.uint8), rdram_size=RDRAM) as cp:
+        cp.write_rdram(rd)
+        cp.write_hidden_rdram(hid)
+        none_seen = repeat_seen = 0
+        for it, (v, opts, invalid) in enumerate(cases):
+            regs = _variant_regs(rng, v, it)
+            if invalid:
+                regs[VIRegister.HStart] = _start(760, 900)  # h_start past the 640-pixel line
+            for r, val in regs.items():
+                cp.set_vi_register(r, val)
+                o.set_vi_register(r, val)
+            got = cp.scanout_sync(opts)
+            exp = o.scanout(opts.as_words())
+            assert (got is None) == (exp is None), it
+            if got is not None:
+                assert got.shape == exp.shape and np.array_equal(got, exp), it
+            if invalid:
+                none_seen += got is None
+                repeat_seen += got is not None
+        assert repeat_seen >= 1 and none_seen >= 1  # both sides of the four-frame window
+    cropped = ScanoutOptions(crop_rect_enable=1, crop_left=13, crop_right=7, crop_top=5, crop_bottom=9)
+    assert cropped.crop_left == 13

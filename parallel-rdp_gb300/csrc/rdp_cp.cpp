@@ -1944,22 +1944,39 @@ struct rdp_batch
 		views.reserve(instances.size());
 		owners.reserve(instances.size());
 		if (capturing && !reserve_for_capture()) return sticky_error = RDP_ERR_DEVICE;
+		// Every page the submitted passes read comes from the callers' RDRAM first, in one launch for
+		// all instances and rounds (each page once per instance).  Refreshing a later round's pages
+		// before the earlier rounds run is the same as refreshing them just before their round: the
+		// caller's writes all precede the submission, and bytes the earlier rounds write set the mask
+		// after the refresh, so they stay the GPU's.
+		{
+			CohLauncher refresh;
+			refresh.begin(stream, 0);
+			for (rdp_cp *cp : instances)
+			{
+				if (cp->deferred.empty() || !cp->coherent) continue;
+				cp->begin_page_list();
+				for (const rdpx::PassPacket &pk : cp->deferred)
+					for (uint32_t pg : pk.read_pages)
+						if (cp->page_stamp[pg] != cp->stamp)
+						{
+							cp->page_stamp[pg] = cp->stamp;
+							refresh.add(cp->host_mapped, cp->d_rdram, cp->d_wmask, pg);
+						}
+			}
+			if (refresh.finish(stream, 0) != cudaSuccess) return sticky_error = RDP_ERR_DEVICE;
+		}
 		for (;;)
 		{
 			views.clear();
 			owners.clear();
-			CohLauncher refresh;
-			refresh.begin(stream, 0);
 			for (rdp_cp *cp : instances)
 				if (!cp->deferred.empty())
 				{
 					views.push_back(cp->deferred.front().view());
 					owners.push_back(cp);
-					for (uint32_t pg : cp->deferred.front().read_pages) refresh.add(cp->host_mapped, cp->d_rdram, cp->d_wmask, pg);
 				}
 			if (views.empty()) break;
-			// The round's pages come from the callers' RDRAM first (one launch for all instances).
-			if (refresh.finish(stream, 0) != cudaSuccess) return sticky_error = RDP_ERR_DEVICE;
 			if (!exec.launch(views.data(), uint32_t(views.size()), capturing ? &sink : nullptr))
 				return sticky_error = RDP_ERR_DEVICE;
 			rounds++;

@@ -36,8 +36,9 @@ roofline: the dominant kernel (k_shade): bytes of its output (the 8 B shaded rec
 cpu_baseline: the CPU oracle (a scalar restatement of the reference's algorithm)
          over the instances on all host cores, on a bounded sample (>= 10 s).
 
---workload textured measures the single textured, depth-tested 320x240 frame
-(10,000 triangles) instead.  --impl reference times the reference algorithm on the
+--workload plain / textured / mixed measures one processor on the plain 2,000-triangle frame, the
+textured depth-tested frame (10,000 triangles) or the mixed 640x480 sequence (16 frames x 50,000
+primitives, VI scanout of each frame in the end-to-end loop) instead.  --impl reference times the reference algorithm on the
 host CPU (the oracle, all host threads; the reference's own Vulkan/Angrylion build
 is not available) on the same workload and metric.
 """
@@ -160,11 +161,26 @@ class ClockSampler:
         return out
 
 
-def _frame():
+# Single-processor workloads: (generator config, description, op-table key, VI scanout per frame).
+SINGLE = {
+    "plain": (0, "plain single frame: 320x240 RGBA5551, 1-cycle, a FillRect clear then 2,000 Gouraud triangles "
+                 "(vertices uniform over the screen, log-normal area median 64 px sigma 1.5, RGBA shade uniform), SHADE "
+                 "combiner, pass-through blender, dither off, seed 0", "plain", False),
+    "textured": (1, WORKLOAD, "textured", False),
+    "mixed": (2, "mixed 640x480 RGBA8888 sequence: 16 frames x 50,000 primitives (40 % textured triangles, 30 % "
+                 "copy-mode TextureRectangles, 20 % CI8 + 256-entry TLUT triangles, 10 % FillRects; alpha compare, "
+                 "LOD / detail tiles and Z on half), VI scanout of every frame (AA filter, divot, dither filter, "
+                 "interlaced 640x480), seed 0", "mixed16", True),
+}
+
+
+def _frame(workload="textured"):
+    """Command words of one step of a single-processor workload (every frame of it), the initial
+    RDRAM, the primitive count, the generator parameters and each frame's first word."""
     from rdp_gb300 import cmdgen
-    p = cmdgen.default_params(cmdgen.CONFIG_TEXTURED, seed=0)
-    words, rdram, prims = cmdgen.generate_stream(p)
-    return words, rdram, prims, p
+    p = cmdgen.default_params(SINGLE[workload][0], seed=0)
+    words, rdram, prims, offsets = cmdgen.generate_frames(p)
+    return words, rdram, prims, p, offsets
 
 
 def _fb_bytes_per_pixel(p):
@@ -181,22 +197,42 @@ def _l2_flusher(device):
     return flush
 
 
-def _cpu_baseline(words, rdram, min_seconds=10.0, max_frames=30):
-    """Oracle on this host, one thread, whole frames until >= min_seconds."""
+def _cpu_frames(words, rdram, offsets, min_seconds=10.0, max_rounds=30):
+    """The CPU oracle on one thread over the workload's frames in order (the step repeated from a
+    fresh RDRAM when it is short) until >= min_seconds.  Returns (frames, reference passes,
+    fragments, seconds)."""
     from oracle import Oracle
-    frames, t0 = 0, time.perf_counter()
-    passes = frags = 0
-    while True:
+    nf = len(offsets) - 1
+    frames = passes = frags = 0
+    t0 = time.perf_counter()
+    for _ in range(max_rounds):
         o = Oracle(8 << 20)
         o.write_rdram(rdram)
-        o.enqueue(words)
+        for f in range(nf):
+            o.enqueue(words[offsets[f]:offsets[f + 1]])
+            frames += 1
+            if time.perf_counter() - t0 >= min_seconds:
+                break
+        passes += o.reference_passes()
         frags += o.fragments()
-        frames += 1
         o.close()
-        el = time.perf_counter() - t0
-        if el >= min_seconds or frames >= max_frames:
+        if time.perf_counter() - t0 >= min_seconds:
             break
-    return frames, el, frags
+    return frames, passes, frags, time.perf_counter() - t0
+
+
+def _mixed_vi_regs(frame):
+    """VI registers of the mixed sequence's scanout: the 640x480 RGBA8888 colour image, AA filter
+    with resampling, divot, dither filter, interlaced (field = frame parity)."""
+    from rdp_gb300 import VIRegister, cmdgen
+
+    def start(a, b):
+        return ((a & 0x3ff) << 16) | (b & 0x3ff)
+
+    return {VIRegister.Control: 3 | (1 << 4) | (1 << 16) | (1 << 6), VIRegister.Origin: cmdgen.color_addr(),
+            VIRegister.Width: 640, VIRegister.VSync: 525, VIRegister.VStart: start(34, 34 + 480),
+            VIRegister.HStart: start(108, 108 + 640), VIRegister.XScale: 1024, VIRegister.YScale: 2048,
+            VIRegister.VCurrentLine: frame & 1}
 
 
 def _peaks():
@@ -267,13 +303,19 @@ def _reference_passes(words, rdram):
     return s
 
 
-def run_ours_textured(args):
+def run_ours_single(args):
+    """One processor on a single-processor workload (plain frame, textured frame or the mixed
+    16-frame sequence with VI): the whole step replayed from one CUDA graph with inputs resident
+    (value), and the same through the C ABI with host buffers (e2e; the mixed sequence also scans
+    every frame out)."""
     dist, rank, world, local = _dist()
     import torch
     torch.cuda.set_device(local)
     from rdp_gb300 import CommandProcessor
 
-    words, rdram, prims, params = _frame()
+    workload_text, op_key, with_vi = SINGLE[args.workload][1:]
+    words, rdram, prims, params, offsets = _frame(args.workload)
+    frames_per_step = len(offsets) - 1
     base = _reference_passes(words, rdram)
     passes_per_frame = base["reference_passes"]
     frags_per_frame = base["fragments"]
@@ -312,25 +354,43 @@ def run_ours_textured(args):
     value = total_passes / t_value
     graph.close()
 
-    # ---------------- e2e: C ABI with host buffers
+    # ---------------- e2e: C ABI with host buffers (every frame enqueued, signalled and waited for;
+    # the mixed sequence also scanned out after each frame)
+    vi_opts = None
+    if with_vi:
+        from rdp_gb300 import ScanoutOptions
+        vi_opts = ScanoutOptions(blend_previous_frame=1, upscale_deinterlacing=0)
+
+    def e2e_step():
+        out = 0
+        for f in range(frames_per_step):
+            cp.enqueue_command(words[offsets[f]:offsets[f + 1]])
+            if with_vi:
+                for r, v in _mixed_vi_regs(f).items():
+                    cp.set_vi_register(r, v)
+                img = cp.scanout_sync(vi_opts)
+                out += img.nbytes if img is not None else 0
+            else:
+                cp.wait_for_timeline(cp.signal_timeline())
+        return out
+
     for _ in range(args.warmup):
-        cp.enqueue_command(words)
-        cp.wait_for_timeline(cp.signal_timeline())
+        e2e_step()
     s0 = cp.stats()
     _barrier(dist)
-    e2e_s = 0.0
+    e2e_s, vi_bytes = 0.0, 0
     for _ in range(args.steps):
         flush()
         t0 = time.perf_counter()
-        cp.enqueue_command(words)
-        cp.wait_for_timeline(cp.signal_timeline())
+        vi_bytes = e2e_step()
         e2e_s += time.perf_counter() - t0
     s1 = cp.stats()
     _barrier(dist)
     e2e_t = _max_over_ranks(dist, e2e_s)
     e2e_value = total_passes / e2e_t
     h2d = (s1["staging_bytes"] - s0["staging_bytes"]) / args.steps
-    d2h = params.width * params.height * (_fb_bytes_per_pixel(params) + 2)  # colour + depth images copied back
+    # colour + depth images written back each frame, plus the scanned-out images
+    d2h = frames_per_step * params.width * params.height * (_fb_bytes_per_pixel(params) + 2) + vi_bytes
     cp.close()
 
     # ---------------- roofline of the rasteriser
@@ -344,21 +404,24 @@ def run_ours_textured(args):
     # not captured, so its traffic is not reported.
     traffic = None
     step_ms_mean = t_value * 1e3 / args.steps
-    int_alu = _int_alu_roofline("textured", step_ms_mean, statistics.mean(raster_ms), _sm_count(local),
+    int_alu = _int_alu_roofline(op_key, step_ms_mean, statistics.mean(raster_ms), _sm_count(local),
                                 clock_info.get("sm_mhz"))
-    # RGBA5551 colour (2 B) + hidden (1 B) and Z16 (2 B) + hidden (1 B), loaded and stored.
-    step_hbm = _step_hbm_roofline(len(words) * 4, base["touched_tiles"], 64 * 2 * (3 + 3), base["tmem_uploads"],
-                                  step_ms_mean, hbm_peak, peak_src)
+    # Colour + hidden bytes, and (textured, mixed) Z16 + hidden, loaded and stored per touched tile.
+    cbytes = _fb_bytes_per_pixel(params) + (2 if params.fb_format == 1 else 1)
+    zbytes = 3 if args.workload != "plain" else 0
+    step_hbm = _step_hbm_roofline(len(words) * 4, base["touched_tiles"], 64 * 2 * (cbytes + zbytes),
+                                  base["tmem_uploads"], step_ms_mean, hbm_peak, peak_src)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_value * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32", "data": "synthetic (seeded RDP command words)",
-        "config": {"workload": WORKLOAD, "frames_per_step": 1, "primitives_per_frame": prims,
-                   "reference_passes_per_frame": passes_per_frame, "fragments_per_frame": frags_per_frame,
-                   "parallelism": "replicas" if world > 1 else "single", "l2": "flushed between timed iterations"},
+        "config": {"workload": workload_text, "frames_per_step": frames_per_step, "primitives_per_step": prims,
+                   "reference_passes_per_step": passes_per_frame, "fragments_per_step": frags_per_frame,
+                   "parallelism": "replicas" if world > 1 else "single", "l2": "flushed between timed iterations",
+                   "e2e_vi_scanout": with_vi},
         "mpix_per_s": total_frags / t_value / 1e6,
-        "frames_per_s": world * args.steps / t_value,
+        "frames_per_s": world * args.steps * frames_per_step / t_value,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "mpix_per_s": total_frags / e2e_t / 1e6},
         "gpu_launches": int(launches),
@@ -369,56 +432,68 @@ def run_ours_textured(args):
         "clocks": clock_info,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        frames, el, frags = _cpu_baseline(words, rdram)
-        line["cpu_baseline"] = {"value": passes_per_frame * frames / el, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": "%d whole frames of the workload through the CPU oracle, one thread" % frames,
-                                "mpix_per_s": frags / el / 1e6}
+        done, passes, frags, el = _cpu_frames(words, rdram, offsets)
+        line["cpu_baseline"] = {"value": passes / el, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": "%d frames of the workload in order through the CPU oracle, one thread "
+                                          "(>= 10 s)" % done, "mpix_per_s": frags / el / 1e6}
     if rank == 0:
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
 
 
-def run_reference_textured(args):
-    """The reference algorithm on the host CPU (the oracle), same metric and config."""
+def run_reference_single(args):
+    """The reference algorithm on the host CPU (the oracle), same workload, metric and unit: each
+    step renders the workload's frames in order on one thread, bounded to a sample of frames
+    (the mixed sequence: two frames per step, continuing where the last step stopped)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    words, rdram, prims, params = _frame()
+    workload_text = SINGLE[args.workload][1]
+    words, rdram, prims, params, offsets = _frame(args.workload)
     from oracle import Oracle
     ncores = os.cpu_count() or 1
+    nf = len(offsets) - 1
+    per_step = nf if nf <= 2 else 2
+    state = {"o": None, "next": 0}
 
-    def one_frame():
-        o = Oracle(8 << 20)
-        o.write_rdram(rdram)
-        o.enqueue(words)
-        f = o.fragments()
-        o.close()
-        return f
+    def step():
+        passes = frags = 0
+        for _ in range(per_step):
+            if state["o"] is None or state["next"] == nf:
+                if state["o"] is not None:
+                    state["o"].close()
+                state["o"] = Oracle(8 << 20)
+                state["o"].write_rdram(rdram)
+                state["next"] = 0
+            o, f = state["o"], state["next"]
+            p0, g0 = o.reference_passes(), o.fragments()
+            o.enqueue(words[offsets[f]:offsets[f + 1]])
+            passes += o.reference_passes() - p0
+            frags += o.fragments() - g0
+            state["next"] = f + 1
+        return passes, frags
 
-    # Reference-equivalent passes per frame, counted with the same host emulation as our arm.
-    try:
-        passes_per_frame = _reference_passes(words, rdram)["reference_passes"]
-    except Exception:
-        passes_per_frame = (prims + 255) // 256
     for _ in range(args.warmup):
-        one_frame()
+        step()
+    passes = frags = 0
     t0 = time.perf_counter()
-    frags = 0
     for _ in range(args.steps):
-        frags += one_frame()
+        p, f = step()
+        passes += p
+        frags += f
     el = time.perf_counter() - t0
-    value = passes_per_frame * args.steps / el
+    value = passes / el
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded RDP command words)",
-        "config": {"workload": WORKLOAD, "frames_per_step": 1, "primitives_per_frame": prims},
+        "config": {"workload": workload_text, "frames_per_step": per_step, "primitives_per_step": prims * per_step // nf},
         "mpix_per_s": frags / el / 1e6,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": "one whole frame per step through the CPU oracle (scalar restatement of the "
+                         "sample": "%d frame(s) per step in order through the CPU oracle (scalar restatement of the "
                                    "reference algorithm; the reference's Vulkan build needs a graphics stack); "
-                                   "%d host cores available, 1 used" % ncores},
+                                   "%d host cores available, 1 used" % (per_step, ncores)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -826,7 +901,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="batched", choices=["batched", "textured"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "plain", "textured", "mixed"])
     ap.add_argument("--instances", type=int, default=BATCH_INSTANCES)
     ap.add_argument("--train-steps", type=int, default=8, help="sync points of online cost-model training")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving-loop measurement")
@@ -841,9 +916,9 @@ def main():
         from rdp_gb300 import set_shade_order
         set_shade_order(args.shade_order, int(os.environ.get("LOCAL_RANK", "0")))
     if args.impl == "reference":
-        (run_reference_batched if args.workload == "batched" else run_reference_textured)(args)
+        (run_reference_batched if args.workload == "batched" else run_reference_single)(args)
     else:
-        (run_ours_batched if args.workload == "batched" else run_ours_textured)(args)
+        (run_ours_batched if args.workload == "batched" else run_ours_single)(args)
 
 
 if __name__ == "__main__":

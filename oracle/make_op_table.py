@@ -22,7 +22,9 @@ that only mask an address) is kept out by listing the stages' functions explicit
 
 Workloads (the benchmark's, regenerated from their seeds):
   batched64 -- one frame of each of the 64 batched instances (seeds 0-63), one sync point
+  plain     -- the plain 320x240 frame (2,000 Gouraud triangles, seed 0)
   textured  -- the textured, depth-tested 320x240 frame (10,000 triangles, seed 0)
+  mixed16   -- the mixed 640x480 sequence (16 frames of 50,000 primitives, seed 0), one step
 
 Usage: python oracle/make_op_table.py [--jobs N]   -> writes oracle/op_table.json
 """
@@ -175,8 +177,9 @@ sys.path[:0] = [%(pkg)r, %(oracle)r]
 from rdp_gb300 import cmdgen
 from oracle import Oracle
 kind, lo, hi = sys.argv[1], int(sys.argv[2]), int(sys.argv[3])
+configs = {"plain": cmdgen.CONFIG_PLAIN, "textured": cmdgen.CONFIG_TEXTURED, "mixed16": cmdgen.CONFIG_MIXED}
 for i in range(lo, hi):
-    p = cmdgen.batched_instance_params(i) if kind == "batched64" else cmdgen.default_params(cmdgen.CONFIG_TEXTURED, seed=0)
+    p = cmdgen.batched_instance_params(i) if kind == "batched64" else cmdgen.default_params(configs[kind], seed=0)
     words, rdram, prims = cmdgen.generate_stream(p)
     o = Oracle(8 << 20)
     o.write_rdram(rdram)
@@ -292,7 +295,7 @@ def main():
         "shading_stages": SHADING_STAGES,
         "workloads": {},
     }
-    for kind in ("textured", "batched64"):
+    for kind in ("plain", "textured", "mixed16", "batched64"):
         out["workloads"][kind] = table(kind, line_ops, line_calls, args.jobs)
         w = out["workloads"][kind]
         print("%s: %.3e ops, %d fragments, %.1f ops/fragment" % (kind, w["ops_total"], w["fragments"],

@@ -256,7 +256,7 @@ struct Executor
 	ExecCaps caps;
 	uint64_t generation = 0;
 	uint64_t kernel_launches = 0, staging_bytes = 0, launches = 0;
-	uint32_t shade_ctas_v[RDP_SHADE_VARIANTS] = {}, blend_ctas = 0;
+	uint32_t shade_ctas_v[RDP_SHADE_VARIANTS] = {}, blend_ctas = 0, blend_kernel = 0;
 	bool failed = false;
 	ShadeTuner tuner;
 	HostPool pool;                                      // staging fill of large launches
@@ -455,7 +455,10 @@ struct Executor
 		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
 		sms = std::max(sms, 1);
 		for (int v = 0; v < RDP_SHADE_VARIANTS; v++) shade_ctas_v[v] = uint32_t(sms) * uint32_t(rdp_kernels_shade_ctas_per_sm(v));
-		blend_ctas = uint32_t(sms) * uint32_t(rdp_kernels_blend_ctas_per_sm());
+		// RDP_BLEND_KERNEL=0|1 selects the blend kernel (look-ahead through registers / staged by bulk
+		// copies); the default is the one measured faster on the batched workload.
+		if (const char *e = getenv("RDP_BLEND_KERNEL")) blend_kernel = atoi(e) ? 1u : 0u;
+		blend_ctas = uint32_t(sms) * uint32_t(rdp_kernels_blend_ctas_per_sm(int(blend_kernel)));
 		tuner.active = shade_variant_choice(device) < 0;
 		num_queues = uint32_t(sms);
 		if (const char *e = getenv("RDP_SHADE_PERM_MIN_PRIMS")) perm_min_prims = uint32_t(strtoul(e, nullptr, 10));
@@ -945,6 +948,7 @@ struct Executor
 		L.shade_variant = uint32_t(variant);
 		L.shade_ctas = shade_ctas_v[variant];
 		L.blend_ctas = blend_ctas;
+		L.blend_kernel = blend_kernel;
 		L.pair_log = sample ? d_pair_log : nullptr;
 		L.log_slot = sample ? uint32_t(tuner.samples_taken++ % 256) : 0u;
 		if (!sample && !cap && launch_log && tile_base && launch_log_pending.size() < kLaunchLogSlots)

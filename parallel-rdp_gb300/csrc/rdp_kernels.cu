@@ -3316,11 +3316,12 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 // The per-pair inputs come through shared memory: a ring of BLEND_STAGES stages, each holding up
 // to BLEND_CHUNK consecutive pairs of the tile -- their shaded records (a tile's pairs are
 // consecutive in the scratch, so one 1-D bulk copy moves them all) and each pair's primitive
-// state (one 128-byte bulk copy per pair).  Thread 0 issues the copies a stage ahead; they complete
-// on the stage's mbarrier (transaction bytes).  So no global load sits in a pixel's serial chain of
-// pairs.  Waits are bounded: a wait that gives up sets bit 0 of the launch's error word (ctrl[8])
-// and the CTA stops.
-constexpr int BLEND_STAGES = 2, BLEND_CHUNK = 4;
+// state (one 128-byte bulk copy per pair).  Thread 0 issues the copies up to BLEND_STAGES chunks
+// ahead; they complete on the stage's mbarrier (transaction bytes).  So no global load sits in a
+// pixel's serial chain of pairs.  Waits are bounded: a wait that gives up marks the CTA; at the
+// chunk's barrier the CTA then sets bit 0 of the launch's error word (ctrl[8]), stops issuing,
+// drains its own copies (bounded) and ends.
+constexpr int BLEND_STAGES = 3, BLEND_CHUNK = 4;
 constexpr uint32_t BLEND_WAIT_POLLS = 1u << 20; // mbarrier polls before a wait gives up
 constexpr uint32_t BLEND_ERR_WAIT = 1u;
 
@@ -3385,7 +3386,8 @@ __device__ __forceinline__ bool blend_tile(uint32_t item, const RdpPass *__restr
                                            const uint32_t *__restrict__ offsets, const uint2 *__restrict__ pairs,
                                            const RdpPrimShade *__restrict__ shade, const uint2 *__restrict__ sc,
                                            uint32_t *__restrict__ cycles, BlendStage *stages, uint64_t *bars,
-                                           uint32_t &chunk_seq, uint32_t &issued_seq, uint32_t *__restrict__ err)
+                                           uint32_t &chunk_seq, uint32_t &issued_seq, uint32_t *__restrict__ err,
+                                           volatile uint32_t *fail)
 {
 	const uint32_t p0 = offsets[item], p1 = offsets[item + 1];
 	const int tid = threadIdx.x;
@@ -3438,12 +3440,7 @@ __device__ __forceinline__ bool blend_tile(uint32_t item, const RdpPass *__restr
 	for (uint32_t c = 0; c < nchunks; c++)
 	{
 		const uint32_t sidx = chunk_seq % BLEND_STAGES, parity = (chunk_seq / BLEND_STAGES) & 1u;
-		const bool ok = mbar_wait(&bars[sidx], parity);
-		if (__syncthreads_or(!ok))
-		{
-			if (tid == 0) atomicOr(err, BLEND_ERR_WAIT);
-			return false;
-		}
+		if (!mbar_wait(&bars[sidx], parity)) *fail = 1u; // seen by all at the chunk's barrier
 		const BlendStage &st = stages[sidx];
 		const uint32_t cnt = chunk_count(c);
 		if (inside)
@@ -3476,6 +3473,11 @@ __device__ __forceinline__ bool blend_tile(uint32_t item, const RdpPass *__restr
 				frags += blend_pixel(ps, pc, sh, in, px);
 			}
 		__syncthreads(); // every thread is done with the stage
+		if (*fail)
+		{
+			if (tid == 0) atomicOr(err, BLEND_ERR_WAIT);
+			return false;
+		}
 		if (tid == 0 && c + BLEND_STAGES < nchunks)
 		{
 			const uint32_t n = c + BLEND_STAGES;
@@ -3523,10 +3525,11 @@ __global__ void __launch_bounds__(SHADE_THREADS, 24) k_blend(const RdpPass *__re
 {
 	__shared__ BlendStage s_stage[BLEND_STAGES];
 	__shared__ __align__(8) uint64_t s_bar[BLEND_STAGES];
-	__shared__ uint32_t s_next;
+	__shared__ uint32_t s_next, s_fail;
 	if (ctrl[1]) return;
 	if (threadIdx.x == 0)
 	{
+		s_fail = 0u;
 		for (int i = 0; i < BLEND_STAGES; i++) mbar_init(&s_bar[i], 1);
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 	}
@@ -3542,7 +3545,7 @@ __global__ void __launch_bounds__(SHADE_THREADS, 24) k_blend(const RdpPass *__re
 		if (k >= n) break;
 		const uint32_t item = order ? order[k] : nonempty[k];
 		if (!blend_tile(item, passes, num_passes, offsets, pairs, shade, sc, cycles, s_stage, s_bar, chunk_seq,
-		                issued_seq, ctrl + 8))
+		                issued_seq, ctrl + 8, &s_fail))
 		{
 			// A wait gave up: the copies still in flight (issued, not consumed) finish before the
 			// CTA's shared memory goes away, each wait bounded again.
@@ -3551,6 +3554,167 @@ __global__ void __launch_bounds__(SHADE_THREADS, 24) k_blend(const RdpPass *__re
 					mbar_wait(&s_bar[q % BLEND_STAGES], (q / BLEND_STAGES) & 1u);
 			break;
 		}
+	}
+}
+
+// ---------------------------------------------------------------------------- k_blend, register look-ahead
+// The same blend with the per-pair inputs loaded straight from global memory: each thread keeps
+// the shaded records and primitive indices of the next BLEND_AHEAD pairs in registers and
+// prefetches their primitive state into L1.
+__device__ __forceinline__ void blend_tile_lookahead(uint32_t item, const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                           const uint32_t *__restrict__ offsets, const uint2 *__restrict__ pairs,
+                                           const RdpPrimShade *__restrict__ shade, const uint2 *__restrict__ sc,
+                                           uint32_t *__restrict__ cycles)
+{
+	const uint32_t p0 = offsets[item], p1 = offsets[item + 1];
+	if (p0 == p1)
+	{
+		if (cycles && threadIdx.x == 0) cycles[item] = 0;
+		return;
+	}
+	const long long t_start = clock64();
+	const uint32_t pi = pass_of_item(passes, num_passes, item);
+	const RdpPass &ps = passes[pi];
+	const uint32_t tl = item - ps.tile_item_begin;
+	const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
+	const int tid = threadIdx.x;
+	const int x = tx * 8 + (tid & 7), y = ty * 8 + (tid >> 3);
+	const bool inside = x < int(ps.fb_width) && y < int(ps.fb_height);
+	PassConst pc;
+	switch (ps.fb_fmt)
+	{
+	case FBF_I4: pc.fb_size = 0; pc.dx_mask = 0; pc.dx_shift = 0; break;
+	case FBF_I8: pc.fb_size = 1; pc.dx_mask = ~7; pc.dx_shift = 3; break;
+	case FBF_RGBA5551:
+	case FBF_IA88: pc.fb_size = 2; pc.dx_mask = ~3; pc.dx_shift = 2; break;
+	default: pc.fb_size = 4; pc.dx_mask = ~1; pc.dx_shift = 1; break;
+	}
+	pc.alias = ps.fb_addr == ps.depth_addr;
+	uint32_t addr_index;
+	switch (ps.fb_fmt)
+	{
+	case FBF_I4:
+	case FBF_I8: addr_index = ps.fb_addr; break;
+	case FBF_RGBA5551:
+	case FBF_IA88: addr_index = ps.fb_addr >> 1; break;
+	default: addr_index = ps.fb_addr >> 2; break;
+	}
+	const uint32_t ci = addr_index + ps.fb_width * uint32_t(y) + uint32_t(x);
+	const uint32_t di = (ps.depth_addr >> 1) + ps.fb_width * uint32_t(y) + uint32_t(x);
+	Pix px;
+	uint32_t frags = 0;
+	if (inside)
+	{
+		load_pixel(ps, px, ci, di);
+		// Software pipeline: the shaded record and primitive of pair pr + BLEND_AHEAD are loaded
+		// (and its primitive's shading state prefetched into L1) while pair pr blends.
+		constexpr int BLEND_AHEAD = 2;
+		uint2 q_rec[BLEND_AHEAD];
+		uint32_t q_prim[BLEND_AHEAD];
+#pragma unroll
+		for (int k = 0; k < BLEND_AHEAD; k++)
+		{
+			const uint32_t pr = p0 + uint32_t(k);
+			q_rec[k] = kScratchEmpty;
+			q_prim[k] = 0u;
+			if (pr < p1)
+			{
+				q_rec[k] = sc[size_t(pr) * SHADE_THREADS + tid];
+				q_prim[k] = pairs[pr].x;
+				asm volatile("prefetch.global.L1 [%0];" ::"l"(shade + q_prim[k]));
+			}
+		}
+		for (uint32_t pr = p0; pr < p1; pr++)
+		{
+			const uint2 rec = q_rec[0];
+			const uint32_t prim = q_prim[0];
+#pragma unroll
+			for (int k = 0; k + 1 < BLEND_AHEAD; k++)
+			{
+				q_rec[k] = q_rec[k + 1];
+				q_prim[k] = q_prim[k + 1];
+			}
+			const uint32_t nx = pr + BLEND_AHEAD;
+			if (nx < p1)
+			{
+				q_rec[BLEND_AHEAD - 1] = sc[size_t(nx) * SHADE_THREADS + tid];
+				q_prim[BLEND_AHEAD - 1] = pairs[nx].x;
+				asm volatile("prefetch.global.L1 [%0];" ::"l"(shade + q_prim[BLEND_AHEAD - 1]));
+			}
+			const uint32_t code = (rec.y >> 18) & 15u;
+			if (code == SC_NONE) continue;
+			const RdpPrimShade &sh = shade[prim];
+			Shaded in;
+			in.combined = rec.x;
+			in.shade_alpha = 0;
+			if (code == SC_FILL)
+			{
+				in.coverage = 0x40;
+				in.z_dith = 0;
+			}
+			else if (code == SC_COPY)
+			{
+				in.coverage = 0x20;
+				in.z_dith = int(rec.y & 0xffffu);
+			}
+			else
+			{
+				in.coverage = int(code);
+				in.shade_alpha = int(rec.y >> 22);
+				const uint32_t noise = (sh.static_flags & RS_NEED_NOISE) ? reseed_noise(uint32_t(x), uint32_t(y), sh.prim_index) : 0u;
+				in.z_dith = int((rec.y & 0x3ffffu) << 9) | rgb_dither_value(sh.static_flags, sh.dither, x, y, noise);
+			}
+			frags += blend_pixel(ps, pc, sh, in, px);
+		}
+		store_pixel(ps, px, ci, di, pc.alias);
+	}
+	if (ps.wmask) mark_pixel(ps, px, ci, di, pc.alias, inside);
+	unsigned long long *counters = ps.counters;
+	if (counters)
+	{
+		unsigned long long total = frags;
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+		if ((tid & 31) == 0 && total) atomicAdd(counters, total);
+		if (tid == 0)
+		{
+			atomicAdd(counters + 1, 1ull);
+			atomicAdd(counters + 2, (unsigned long long)(p1 - p0));
+		}
+	}
+	if (cycles)
+	{
+		// Per-tile cost sample for the learned tile-order model: the slower warp's cycles.
+		__syncthreads();
+		if (tid == 0) cycles[item] = uint32_t(min(clock64() - t_start, 0xffffffffll));
+	}
+}
+
+// Persistent CTAs take non-empty tiles from a shared counter, in the order of `order`
+// (longest predicted first) when given, else in tile order.  Each pixel's pairs form a serial
+// dependency chain, so residency matters more than the few spills of a 40-register budget
+// (24 CTAs per SM measured 8 % faster than 16 with 64 registers, 32 CTAs slower).
+__global__ void __launch_bounds__(SHADE_THREADS, 24) k_blend_lookahead(const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                                        const uint32_t *__restrict__ offsets,
+                                                        const uint2 *__restrict__ pairs, uint32_t *__restrict__ ctrl,
+                                                        const uint32_t *__restrict__ nonempty,
+                                                        const RdpPrimShade *__restrict__ shade,
+                                                        const uint2 *__restrict__ sc,
+                                                        const uint32_t *__restrict__ order,
+                                                        uint32_t *__restrict__ cycles)
+{
+	__shared__ uint32_t s_next;
+	if (ctrl[1]) return;
+	const uint32_t n = ctrl[3];
+	for (;;)
+	{
+		if (threadIdx.x == 0) s_next = atomicAdd(&ctrl[4], 1u);
+		__syncthreads();
+		const uint32_t k = s_next;
+		__syncthreads();
+		if (k >= n) break;
+		const uint32_t item = order ? order[k] : nonempty[k];
+		blend_tile_lookahead(item, passes, num_passes, offsets, pairs, shade, sc, cycles);
 	}
 }
 
@@ -3717,10 +3881,12 @@ const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = {
 };
 } // namespace
 
-extern "C" int rdp_kernels_blend_ctas_per_sm(void)
+extern "C" int rdp_kernels_blend_ctas_per_sm(int kernel)
 {
 	int n = 0;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, rdp::k_blend, rdp::SHADE_THREADS, 0) != cudaSuccess) n = 8;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel ? rdp::k_blend : rdp::k_blend_lookahead,
+	                                                  rdp::SHADE_THREADS, 0) != cudaSuccess)
+		n = 8;
 	return n > 0 ? n : 1;
 }
 
@@ -3846,9 +4012,14 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 			if (L->sched->order_enabled) order = L->sched->order;
 		}
 		if (L->blend_events[0]) cudaEventRecordWithFlags(L->blend_events[0], stream, ev_flags);
-		rdp::k_blend<<<tile_ctas, rdp::SHADE_THREADS, 0, stream>>>(
-			L->passes, L->num_passes, L->pair_offsets, L->pairs, L->ctrl, L->nonempty_tiles, L->shade, L->scratch,
-			order, L->tile_cycles);
+		if (L->blend_kernel)
+			rdp::k_blend<<<tile_ctas, rdp::SHADE_THREADS, 0, stream>>>(
+				L->passes, L->num_passes, L->pair_offsets, L->pairs, L->ctrl, L->nonempty_tiles, L->shade, L->scratch,
+				order, L->tile_cycles);
+		else
+			rdp::k_blend_lookahead<<<tile_ctas, rdp::SHADE_THREADS, 0, stream>>>(
+				L->passes, L->num_passes, L->pair_offsets, L->pairs, L->ctrl, L->nonempty_tiles, L->shade, L->scratch,
+				order, L->tile_cycles);
 		if (L->blend_events[1]) cudaEventRecordWithFlags(L->blend_events[1], stream, ev_flags);
 		if (L->sched && L->sched->train_enabled && L->tile_cycles)
 		{

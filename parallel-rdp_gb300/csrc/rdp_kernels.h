@@ -62,6 +62,8 @@ typedef struct RdpLaunch
 	uint32_t *prim_scan_blocks;     /* [2 * ceil(num_prims / 1024)] (with shade_list) */
 	uint32_t shade_variant;         /* which compiled k_shade (register budget), < RDP_SHADE_VARIANTS */
 	uint32_t blend_ctas;            /* persistent CTAs of k_blend / k_raster */
+	uint32_t blend_kernel;          /* 0: k_blend_lookahead (inputs through registers), 1: k_blend (shared-memory
+	                                   ring filled by bulk copies) */
 	uint32_t *pair_log;             /* optional: k_scan writes the launch's pair count to pair_log[log_slot] */
 	uint32_t log_slot;
 	const struct RdpSchedDev *sched; /* optional learned tile order / online training (sched.h) */
@@ -79,7 +81,7 @@ cudaError_t rdp_kernels_init_luts(const uint8_t *blender_lut);
 cudaError_t rdp_kernels_launch(const RdpLaunch *launch, cudaStream_t stream);
 uint32_t rdp_kernels_count(const RdpLaunch *launch);
 int rdp_kernels_shade_ctas_per_sm(int variant);
-int rdp_kernels_blend_ctas_per_sm(void);
+int rdp_kernels_blend_ctas_per_sm(int kernel);
 #ifdef __cplusplus
 }
 #endif

@@ -124,3 +124,28 @@ def test_shade_orders_bit_exact(restore_order, restore_tuning, monkeypatch, vari
 def test_shade_order_rejects_unknown():
     with pytest.raises(Exception):
         set_shade_order(3)
+
+
+@pytest.mark.parametrize("kernel", ["0", "1"], ids=["lookahead", "staged"])
+def test_blend_kernels_bit_exact(monkeypatch, kernel):
+    """Both blend kernels -- per-pair inputs through registers with L1 prefetch, or staged in a
+    shared-memory ring by bulk copies on mbarriers -- give the oracle's bytes, on a stand-alone
+    processor (mixed primitives) and on a batch."""
+    monkeypatch.setenv("RDP_BLEND_KERNEL", kernel)
+    m = cmdgen.default_params(cmdgen.CONFIG_MIXED, seed=61, num_prims=4000, num_frames=1)
+    words, rdram, _ = cmdgen.generate_stream(m)
+    assert_parity(words, rdram)
+    streams = []
+    for i in range(6):
+        q = cmdgen.batched_instance_params(i, min_prims=500, max_prims=3000, seed_base=90)
+        w, rd, _ = cmdgen.generate_stream(q)
+        streams.append((w, rd))
+    with Batch() as b:
+        insts = [b.add_instance(rd.copy()) for _, rd in streams]
+        for cp, (w, _) in zip(insts, streams):
+            cp.enqueue_command(w)
+        b.idle()
+        for cp, (w, rd) in zip(insts, streams):
+            single = run_gpu(w, rd)
+            assert np.array_equal(cp.begin_read_rdram(), single[0])
+            assert np.array_equal(cp.begin_read_hidden_rdram(), single[1])

@@ -665,6 +665,7 @@ def run_ours_batched(args):
 
     # ---------------- plain: one processor + graph per instance, one after another
     plain_ms = 0.0
+    per_instance_ms = []
     for st in streams:
         cp = CommandProcessor(st[1].copy(), device=local)
         g = cp.capture(st[0])
@@ -676,10 +677,20 @@ def run_ours_batched(args):
             flush()
             ms += g.replay(1)
         plain_ms += ms
+        per_instance_ms.append(ms / args.steps)
         g.close()
         cp.close()
     t_plain = _max_over_ranks(dist, plain_ms / 1e3)
     plain_value = total_passes / t_plain
+    # Where the plain path's time goes: the smallest instances' graph time is mostly the fixed cost
+    # of a kernel chain; the rest grows with the work.
+    order = sorted(range(len(streams)), key=lambda i: streams[i][2])
+    small = [per_instance_ms[i] for i in order[:8]]
+    plain_breakdown = {"instance_ms_min": min(per_instance_ms), "instance_ms_median": statistics.median(per_instance_ms),
+                       "instance_ms_max": max(per_instance_ms),
+                       "fixed_ms_per_instance_estimate": statistics.median(small),
+                       "largest_instance_ms": per_instance_ms[order[-1]],
+                       "largest_instance_primitives": int(streams[order[-1]][2])}
 
     # ---------------- serving: 256 instances, Poisson arrivals, continuous batching
     serving = None
@@ -714,7 +725,7 @@ def run_ours_batched(args):
         "mpix_per_s": total_frags / t_value / 1e6,
         "frames_per_s": world * args.steps * args.instances / t_value,
         "plain": {"value": plain_value, "unit": UNIT, "ms_per_step": t_plain * 1e3 / args.steps,
-                  "mpix_per_s": total_frags / t_plain / 1e6},
+                  "mpix_per_s": total_frags / t_plain / 1e6, "breakdown": plain_breakdown},
         "batched_over_plain": value / plain_value,
         "tile_order": {"learned": {"ms_per_step": t_value * 1e3 / args.steps,
                                    "blend_ms_per_step": statistics.mean(rl["blend_ms"])},

@@ -85,7 +85,25 @@ enum
 	 * called while the thread decodes.  Calls that read or write processor state directly (RDRAM
 	 * and TMEM access, scanout, statistics) first wait until the ring is drained.  Not for batch
 	 * instances or sync-point captures. */
-	RDP_CREATE_COMMAND_THREAD = 1u << 0
+	RDP_CREATE_COMMAND_THREAD = 1u << 0,
+	/* Internal upscaling by 2, 4 or 8 (the reference's COMMAND_PROCESSOR_FLAG_UPSCALING_*_BIT,
+	 * rdp_device.hpp:43-52, rdp_device.cpp:189-205; the largest factor given wins).  Every render
+	 * pass into a 16/32-bit image at least 256 pixels wide is rendered a second time at the scaled
+	 * resolution into a multisampled copy of RDRAM (factor^2 slices; pixel (x, y) of the scaled
+	 * image is slice (y % f) * f + x % f at the address of native pixel (x / f, y / f)); RDRAM
+	 * itself still receives the 1x rendering.  The multisampled copy follows CPU writes and other
+	 * passes' output through the reference's "pre" / "post" updates, and scanout reads it: images
+	 * are f times larger (ScanoutOptions.downscale_steps halves them).  hidden_rdram_size must be
+	 * rdram_size / 2.  Not for batch instances or sync-point captures. */
+	RDP_CREATE_UPSCALING_2X = 1u << 2,
+	RDP_CREATE_UPSCALING_4X = 1u << 3,
+	RDP_CREATE_UPSCALING_8X = 1u << 4,
+	/* Super-sampled readback (COMMAND_PROCESSOR_FLAG_SUPER_SAMPLED_READ_BACK_BIT): every pass
+	 * renders only at the scaled resolution and each native pixel a sample wrote is resolved into
+	 * RDRAM (mean of the samples for colour, the first sample for depth); needs an upscaling flag. */
+	RDP_CREATE_SUPER_SAMPLED_READ_BACK = 1u << 5,
+	/* With super-sampled readback: RGBA5551 means are ordered-dithered (4x4 Bayer). */
+	RDP_CREATE_SUPER_SAMPLED_DITHER = 1u << 6
 };
 
 /* CommandProcessor::CommandProcessor (rdp_device.cpp:44-162). */
@@ -132,10 +150,20 @@ size_t rdp_cp_get_rdram_size(rdp_cp *cp);
 size_t rdp_cp_get_hidden_rdram_size(rdp_cp *cp);
 int rdp_cp_get_tmem(rdp_cp *cp, uint16_t *out_2048_words);
 
+/* Renderer::get_scaling_factor (rdp_renderer.cpp:2694-2697): 1, 2, 4 or 8. */
+uint32_t rdp_cp_get_scaling_factor(rdp_cp *cp);
+/* The multisampled copies of an upscaling processor (Renderer::get_upscaled_rdram_buffer /
+ * get_upscaled_hidden_rdram_buffer, rdp_renderer.cpp:2699-2707): idles, then copies `size` bytes
+ * from byte `offset` of the factor^2 slices of RDRAM (of hidden RDRAM).  RDP_ERR_INVALID without
+ * upscaling or past the end. */
+int rdp_cp_read_upscaled_rdram(rdp_cp *cp, void *dst, uint64_t offset, uint64_t size);
+int rdp_cp_read_upscaled_hidden_rdram(rdp_cp *cp, void *dst, uint64_t offset, uint64_t size);
+
 /* CommandProcessor::set_vi_register (rdp_device.cpp:970-975); reg is VIRegister (rdp_common.hpp:286-302). */
 int rdp_cp_set_vi_register(rdp_cp *cp, uint32_t reg, uint32_t value);
 
-/* ScanoutOptions (video_interface.hpp:31-81) at 1x scale. */
+/* ScanoutOptions (video_interface.hpp:31-81).  Crop pixels are native pixels (scaled with the
+ * image on an upscaling processor). */
 typedef struct rdp_scanout_options
 {
 	uint32_t crop_overscan_pixels;
@@ -144,8 +172,9 @@ typedef struct rdp_scanout_options
 	uint32_t blend_previous_frame;
 	uint32_t upscale_deinterlacing; /* 1 (default): serrate is not woven at 1x; 0: weave the fields */
 	uint32_t vi_aa, vi_scale, vi_serrate, vi_dither_filter, vi_divot_filter, vi_gamma_dither;
-	/* Halvings of an upscaled image before output (video_interface.hpp:51); the scanout here is at
-	 * 1x scale, where the reference skips them too (video_interface.cpp:1009, 1354). */
+	/* Halvings of an upscaled image before output (video_interface.hpp:51; at most 8, and none past
+	 * 1x; video_interface.cpp:1000-1064, 1354).  Each halving averages 2x2 pixels, rounded half up
+	 * (the reference's 2:1 linear blit). */
 	uint32_t downscale_steps;
 } rdp_scanout_options;
 /* Fills the reference's defaults (every VI filter on, upscale deinterlacing on). */
@@ -154,8 +183,8 @@ void rdp_scanout_options_default(rdp_scanout_options *opts);
 /* CommandProcessor::scanout_sync (rdp_device.cpp:1130-1182): renders everything
  * queued, runs the VI filters on the device and writes the RGBA8 image
  * (r | g << 8 | b << 16 | a << 24 per pixel) into `rgba_out`, which must hold
- * 640 x 576 pixels.  A width/height of 0 means no image (blank or invalid VI
- * state).  opts may be NULL for the defaults. */
+ * 640 x 576 pixels times the square of the scaling factor.  A width/height of 0 means
+ * no image (blank or invalid VI state).  opts may be NULL for the defaults. */
 int rdp_cp_scanout_sync(rdp_cp *cp, const rdp_scanout_options *opts, uint32_t *rgba_out, uint32_t *width,
                         uint32_t *height);
 /* A scanned-out image in device memory: width x height RGBA8 pixels (r | g << 8 | b << 16 | a << 24),

@@ -9,8 +9,9 @@
  * Same method names, argument meanings and error behaviour: no exceptions; an unusable device or an
  * unsupported configuration makes device_is_supported() return false and the other methods do
  * nothing.  Differences follow from the device API: scanout() returns the image in device memory
- * (ScanoutImage) instead of a Vulkan image, scanout_async_buffer() fills a VIScanoutBuffer whose
- * fence is a CUDA event, and the upscaling / super-sampling flags are not supported.
+ * (ScanoutImage) instead of a Vulkan image and scanout_async_buffer() fills a VIScanoutBuffer whose
+ * fence is a CUDA event.  Upscaling and super-sampled readback follow the reference's flags (an
+ * upscaling processor needs hidden_rdram_size == rdram_size / 2).
  */
 #ifndef RDP_CUDA_HPP
 #define RDP_CUDA_HPP
@@ -160,18 +161,17 @@ public:
 	CommandProcessor(int device, void *rdram_ptr, size_t rdram_offset, size_t rdram_size, size_t hidden_rdram_size,
 	                 CommandProcessorFlags flags)
 	{
-		const CommandProcessorFlags unsupported = COMMAND_PROCESSOR_FLAG_UPSCALING_2X_BIT |
-		                                          COMMAND_PROCESSOR_FLAG_UPSCALING_4X_BIT |
-		                                          COMMAND_PROCESSOR_FLAG_UPSCALING_8X_BIT |
-		                                          COMMAND_PROCESSOR_FLAG_SUPER_SAMPLED_READ_BACK_BIT |
-		                                          COMMAND_PROCESSOR_FLAG_SUPER_SAMPLED_DITHER_BIT;
-		if (flags & unsupported) return;
 		rdp_create_info info = {};
 		info.rdram = rdram_ptr;
 		info.rdram_offset = rdram_offset;
 		info.rdram_size = rdram_size;
 		info.hidden_rdram_size = hidden_rdram_size;
 		info.flags = (flags & COMMAND_PROCESSOR_FLAG_COMMAND_THREAD_BIT) ? RDP_CREATE_COMMAND_THREAD : 0u;
+		if (flags & COMMAND_PROCESSOR_FLAG_UPSCALING_2X_BIT) info.flags |= RDP_CREATE_UPSCALING_2X;
+		if (flags & COMMAND_PROCESSOR_FLAG_UPSCALING_4X_BIT) info.flags |= RDP_CREATE_UPSCALING_4X;
+		if (flags & COMMAND_PROCESSOR_FLAG_UPSCALING_8X_BIT) info.flags |= RDP_CREATE_UPSCALING_8X;
+		if (flags & COMMAND_PROCESSOR_FLAG_SUPER_SAMPLED_READ_BACK_BIT) info.flags |= RDP_CREATE_SUPER_SAMPLED_READ_BACK;
+		if (flags & COMMAND_PROCESSOR_FLAG_SUPER_SAMPLED_DITHER_BIT) info.flags |= RDP_CREATE_SUPER_SAMPLED_DITHER;
 		info.device = device;
 		if (rdp_cp_create(&info, &cp) != RDP_OK) cp = nullptr;
 	}
@@ -212,6 +212,8 @@ public:
 	void end_write_hidden_rdram() { if (cp) rdp_cp_end_write_hidden_rdram(cp); }
 	size_t get_rdram_size() const { return cp ? rdp_cp_get_rdram_size(cp) : 0; }
 	size_t get_hidden_rdram_size() const { return cp ? rdp_cp_get_hidden_rdram_size(cp) : 0; }
+	// The internal upscaling factor (Renderer::get_scaling_factor, rdp_renderer.cpp:2694-2697).
+	unsigned get_scaling_factor() const { return cp ? rdp_cp_get_scaling_factor(cp) : 1u; }
 	// TMEM as 2048 16-bit words (a host copy, current when the call returns).
 	void *get_tmem()
 	{

@@ -57,6 +57,13 @@ def _load():
         L.oracle_vi_latch_scanline.argtypes = [vp, u32]
         L.oracle_vi_end_per_scanline.argtypes = [vp]
         L.oracle_scanout.argtypes = [vp, vp, vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+        L.oracle_set_upscaling.argtypes = [vp, u32, u32, u32]
+        L.oracle_set_upscaling.restype = ctypes.c_int
+        L.oracle_upscaling_factor.argtypes = [vp]
+        L.oracle_upscaling_factor.restype = u32
+        for n in ("oracle_read_upscaled_rdram", "oracle_read_upscaled_hidden"):
+            getattr(L, n).argtypes = [vp, vp, ctypes.c_uint64, ctypes.c_uint64]
+        L.oracle_upscale_pre_external.argtypes = [vp, u32, u32, u32]
         L.oracle_noise.argtypes = [u32, u32, u32]
         L.oracle_noise.restype = ctypes.c_int
         _lib = L
@@ -133,10 +140,34 @@ class Oracle:
     def end_vi_register_per_scanline(self):
         self.L.oracle_vi_end_per_scanline(self.h)
 
+    def set_upscaling(self, factor, super_sampled=False, dither=False):
+        """Internal upscaling by 1, 2, 4 or 8, optionally with super-sampled readback; before any command."""
+        if self.L.oracle_set_upscaling(self.h, factor, int(super_sampled), int(dither)) != 0:
+            raise ValueError("unsupported upscaling")
+
+    def upscaling_factor(self):
+        return self.L.oracle_upscaling_factor(self.h)
+
+    def upscaled_rdram(self):
+        """The multisampled RDRAM: factor^2 slices of RDRAM, slice (y % f) * f + x % f."""
+        f = self.upscaling_factor()
+        out = np.zeros(self.rdram_size * f * f, dtype=np.uint8)
+        self.L.oracle_read_upscaled_rdram(self.h, out.ctypes.data, 0, out.size)
+        return out
+
+    def upscaled_hidden(self):
+        f = self.upscaling_factor()
+        out = np.zeros(self.hidden_size * f * f, dtype=np.uint8)
+        self.L.oracle_read_upscaled_hidden(self.h, out.ctypes.data, 0, out.size)
+        return out
+
     def scanout(self, option_words):
-        """option_words: the 15 ScanoutOptions fields in C-ABI order.  Returns uint32[h, w] or None."""
-        opts = np.array(option_words, dtype=np.uint32)
-        buf = np.zeros(640 * 576, dtype=np.uint32)
+        """option_words: the ScanoutOptions fields in C-ABI order (15, or 16 with downscale_steps).
+        Returns uint32[h, w] or None."""
+        words = list(option_words) + [0] * (16 - len(option_words))
+        opts = np.array(words[:16], dtype=np.uint32)
+        f = self.upscaling_factor()
+        buf = np.zeros(640 * 576 * f * f, dtype=np.uint32)
         w, h = ctypes.c_uint32(), ctypes.c_uint32()
         self.L.oracle_scanout(self.h, opts.ctypes.data, buf.ctypes.data, ctypes.byref(w), ctypes.byref(h))
         return buf[:w.value * h.value].reshape(h.value, w.value) if w.value else None

@@ -40,6 +40,7 @@
 #include <stdlib.h>
 #include <vector>
 #include <algorithm>
+#include <memory>
 
 #include "../parallel-rdp_gb300/csrc/blender_divider_runs.inc"
 
@@ -276,6 +277,7 @@ struct Oracle
 	std::vector<uint32_t> touched;
 	uint32_t pass_prims = 0, pass_uploads = 0, deduced_height = 0;
 	bool color_pending = false, depth_pending = false;
+	uint32_t pass_span_prims = 0;   // primitives of the pass with span rows (the reference's span jobs)
 	uint32_t primitive_counter = 0; // running count == base_primitive_index + index in pass
 	uint64_t fragments = 0;         // depth_blend/fill/copy executions
 
@@ -284,35 +286,38 @@ struct Oracle
 
 	// ------------------------------------------------------------------ RDRAM access
 	uint32_t mask8() const { return rdram_size - 1; }
-	uint8_t vram8(uint32_t i) const { return rdram[i & (rdram_size - 1)]; }
-	void w_vram8(uint32_t i, uint8_t v) { rdram[i & (rdram_size - 1)] = v; }
+	// The memory the pixel accessors address: RDRAM and hidden RDRAM, or one sample slice of their
+	// multisampled copies while a pass renders upscaled.
+	uint8_t *mem_rd = nullptr, *mem_hd = nullptr;
+	uint8_t vram8(uint32_t i) const { return mem_rd[i & (rdram_size - 1)]; }
+	void w_vram8(uint32_t i, uint8_t v) { mem_rd[i & (rdram_size - 1)] = v; }
 	uint16_t vram16(uint32_t i) const
 	{
 		uint32_t b = (i * 2) & (rdram_size - 1);
-		return uint16_t(rdram[b] | (rdram[b + 1] << 8));
+		return uint16_t(mem_rd[b] | (mem_rd[b + 1] << 8));
 	}
 	void w_vram16(uint32_t i, uint16_t v)
 	{
 		uint32_t b = (i * 2) & (rdram_size - 1);
-		rdram[b] = uint8_t(v);
-		rdram[b + 1] = uint8_t(v >> 8);
+		mem_rd[b] = uint8_t(v);
+		mem_rd[b + 1] = uint8_t(v >> 8);
 	}
 	uint32_t vram32(uint32_t i) const
 	{
 		uint32_t b = (i * 4) & (rdram_size - 1);
-		return uint32_t(rdram[b]) | (uint32_t(rdram[b + 1]) << 8) | (uint32_t(rdram[b + 2]) << 16) |
-		       (uint32_t(rdram[b + 3]) << 24);
+		return uint32_t(mem_rd[b]) | (uint32_t(mem_rd[b + 1]) << 8) | (uint32_t(mem_rd[b + 2]) << 16) |
+		       (uint32_t(mem_rd[b + 3]) << 24);
 	}
 	void w_vram32(uint32_t i, uint32_t v)
 	{
 		uint32_t b = (i * 4) & (rdram_size - 1);
-		rdram[b] = uint8_t(v);
-		rdram[b + 1] = uint8_t(v >> 8);
-		rdram[b + 2] = uint8_t(v >> 16);
-		rdram[b + 3] = uint8_t(v >> 24);
+		mem_rd[b] = uint8_t(v);
+		mem_rd[b + 1] = uint8_t(v >> 8);
+		mem_rd[b + 2] = uint8_t(v >> 16);
+		mem_rd[b + 3] = uint8_t(v >> 24);
 	}
-	uint8_t hid(uint32_t i) const { return hidden[i & (hidden_size - 1)]; }
-	void w_hid(uint32_t i, uint8_t v) { hidden[i & (hidden_size - 1)] = v; }
+	uint8_t hid(uint32_t i) const { return mem_hd[i & (hidden_size - 1)]; }
+	void w_hid(uint32_t i, uint8_t v) { mem_hd[i & (hidden_size - 1)] = v; }
 
 	// TMEM byte view of the 16-bit words (tmem8 aliases tmem16 on a little-endian buffer).
 	static uint8_t tm8(const uint16_t *t, uint32_t i) { return uint8_t(t[(i >> 1) & 2047] >> ((i & 1) * 8)); }
@@ -620,15 +625,23 @@ struct Oracle
 	}
 
 	// ======================================================================= span setup
-	// parallel-rdp/shaders/span_setup.comp:59-227, scaling factor 1.
+	// parallel-rdp/shaders/span_setup.comp:59-227; L is log2 of the upscaling factor (0 at 1x).
 	static int quantize_x(int x)
 	{
 		int sticky = (x & 0xfff) != 0 ? 1 : 0;
 		return (x >> 12) | sticky;
 	}
 
-	static Span span_setup(const TriSetup &s, const Attr &a, const Scissor &sc, int y)
+	// interpolate_snapped (span_setup.comp:80-85): whole pixels step by the full derivative,
+	// sub-pixels of an upscaled pixel by the derivative divided by the factor.
+	static int interpolate_snapped(int d, int dy, int L)
 	{
+		return (dy >> L) * d + (dy & ((1 << L) - 1)) * (d >> L);
+	}
+
+	static Span span_setup(const TriSetup &s, const Attr &a, const Scissor &sc, int y, int L = 0)
+	{
+		const int S = 1 << L;
 		Span sp = {};
 		bool flip = (s.flags & TRI_FLIP) != 0;
 		bool interlace_en = (s.flags & TRI_INTERLACE_FIELD) != 0;
@@ -636,13 +649,13 @@ struct Oracle
 		{
 			bool do_offset = (s.flags & TRI_DO_OFFSET) != 0;
 			bool skip_xfrac = (s.flags & TRI_SKIP_XFRAC) != 0;
-			int y_base = s.yh >> 2;
+			int y_base = (s.yh >> 2) * S;
 			int dy = y - y_base;
-			int xh = s.xh + dy * (s.dxhdy << 2);
+			int xh = s.xh * S + dy * (s.dxhdy << 2);
 			int drgba_diff[4] = {}, dstzw_diff[4] = {};
 			if (do_offset)
 			{
-				xh += 3 * s.dxhdy;
+				xh += (S * 3) * s.dxhdy;
 				for (int c = 0; c < 4; c++)
 				{
 					int deh = a.drgba_de[c] & ~0x1ff, dyh = a.drgba_dy[c] & ~0x1ff;
@@ -656,37 +669,37 @@ struct Oracle
 			int xfrac = skip_xfrac ? 0 : ((xh >> 7) & 0xff);
 			for (int c = 0; c < 4; c++)
 			{
-				int v = a.rgba[c] + dy * a.drgba_de[c];
-				sp.rgba[c] = ((v & ~0x1ff) + drgba_diff[c] - xfrac * ((a.drgba_dx[c] >> 8) & ~1)) & ~0x3ff;
-				v = a.stzw[c] + dy * a.dstzw_de[c];
-				sp.stzw[c] = ((v & ~0x1ff) + dstzw_diff[c] - xfrac * ((a.dstzw_dx[c] >> 8) & ~1)) & ~0x3ff;
+				int v = a.rgba[c] + interpolate_snapped(a.drgba_de[c], dy, L);
+				sp.rgba[c] = ((v & ~0x1ff) + drgba_diff[c] - interpolate_snapped((a.drgba_dx[c] >> 8) & ~1, xfrac, L)) & ~0x3ff;
+				v = a.stzw[c] + interpolate_snapped(a.dstzw_de[c], dy, L);
+				sp.stzw[c] = ((v & ~0x1ff) + dstzw_diff[c] - interpolate_snapped((a.dstzw_dx[c] >> 8) & ~1, xfrac, L)) & ~0x3ff;
 			}
 			sp.base_x = base_x;
 		}
 
-		int yh_base = s.yh & ~3;
-		int ym_base = s.ym;
-		int ylo = std::max(s.yh, sc.ylo);
-		int yhi = std::min(s.yl, sc.yhi);
+		int yh_base = (s.yh & ~3) * S;
+		int ym_base = s.ym * S;
+		int ylo = std::max(s.yh, sc.ylo) * S;
+		int yhi = std::min(s.yl, sc.yhi) * S;
 		int xl4[4], xr4[4];
 		bool invalid[4];
 		for (int i = 0; i < 4; i++)
 		{
 			int ys = y * 4 + i;
 			bool clip_y = ys < ylo || ys >= yhi;
-			int xh = s.xh + (ys - yh_base) * s.dxhdy;
-			int xm = s.xm + (ys - yh_base) * s.dxmdy;
-			int xl = s.xl + (ys - ym_base) * s.dxldy;
-			if (ys < s.ym) xl = xm;
-			xl = bfe_s(xl, 27);
-			xh = bfe_s(xh, 27);
+			int xh = s.xh * S + (ys - yh_base) * s.dxhdy;
+			int xm = s.xm * S + (ys - yh_base) * s.dxmdy;
+			int xl = s.xl * S + (ys - ym_base) * s.dxldy;
+			if (ys < S * s.ym) xl = xm;
+			xl = bfe_s(xl, 27 + L);
+			xh = bfe_s(xh, 27 + L);
 			int xhs = quantize_x(xh), xls = quantize_x(xl);
 			xl4[i] = flip ? xhs : xls;
 			xr4[i] = flip ? xls : xhs;
 			invalid[i] = (xl4[i] >> 1) > (xr4[i] >> 1);
 			invalid[i] = invalid[i] || clip_y;
 		}
-		int lo_sc = sc.xlo << 1, hi_sc = sc.xhi << 1;
+		int lo_sc = S * (sc.xlo << 1), hi_sc = S * (sc.xhi << 1);
 		bool all_over = true, all_under = true;
 		for (int i = 0; i < 4; i++)
 		{
@@ -708,7 +721,7 @@ struct Oracle
 		sp.start_x = mn >> 3;
 		sp.end_x = mx >> 3;
 		sp.valid = !all_invalid && !all_over && !all_under;
-		if (interlace_en && ((y & 1) != int(keep_odd)))
+		if (interlace_en && (((y >> L) & 1) != int(keep_odd)))
 			sp.valid = false;
 		// lodlength is stored as int16 in the span record.
 		sp.lodlength = int16_t(flip ? (sp.end_x - sp.base_x) : (sp.base_x - sp.start_x));
@@ -722,18 +735,18 @@ struct Oracle
 	}
 
 	// ======================================================================= binning
-	// parallel-rdp/shaders/binning.h:58-144, scaling 1.
-	static void interpolate_xs(const TriSetup &s, const int ys[4], bool flip, int &rmin, int &rmax)
+	// parallel-rdp/shaders/binning.h:58-144; S is the upscaling factor (1 at 1x).
+	static void interpolate_xs(const TriSetup &s, const int ys[4], bool flip, int &rmin, int &rmax, int S = 1)
 	{
-		int64_t yh_base = s.yh & ~3;
-		int64_t ym_base = s.ym;
+		int64_t yh_base = int64_t(s.yh & ~3) * S;
+		int64_t ym_base = int64_t(s.ym) * S;
 		int xls[4], xrs[4];
 		for (int i = 0; i < 4; i++)
 		{
-			int64_t xh = int64_t(s.xh) + int64_t(ys[i] - yh_base) * s.dxhdy;
-			int64_t xm = int64_t(s.xm) + int64_t(ys[i] - yh_base) * s.dxmdy;
-			int64_t xl = int64_t(s.xl) + int64_t(ys[i] - ym_base) * s.dxldy;
-			if (ys[i] < s.ym) xl = xm;
+			int64_t xh = int64_t(S * s.xh) + int64_t(ys[i] - yh_base) * s.dxhdy;
+			int64_t xm = int64_t(S * s.xm) + int64_t(ys[i] - yh_base) * s.dxmdy;
+			int64_t xl = int64_t(S * s.xl) + int64_t(ys[i] - ym_base) * s.dxldy;
+			if (ys[i] < S * s.ym) xl = xm;
 			auto sat = [](int64_t v) -> int {
 				if (v > INT32_MAX) return INT32_MAX;
 				if (v < INT32_MIN) return INT32_MIN;
@@ -748,7 +761,7 @@ struct Oracle
 		int max_range = 0;
 		for (int i = 0; i < 4; i++)
 			max_range = std::max(max_range, std::max(std::abs(xls[i]), std::abs(xrs[i])));
-		if (max_range <= 2047)
+		if (max_range <= 2047 * S)
 		{
 			rmin = std::min(std::min(xls[0], xls[1]), std::min(xls[2], xls[3]));
 			rmax = std::max(std::max(xrs[0], xrs[1]), std::max(xrs[2], xrs[3]));
@@ -760,21 +773,21 @@ struct Oracle
 		}
 	}
 
-	static bool bin_primitive(const TriSetup &s, int lox, int loy, int hix, int hiy, const Scissor &sc)
+	static bool bin_primitive(const TriSetup &s, int lox, int loy, int hix, int hiy, const Scissor &sc, int S = 1)
 	{
-		loy = std::max(loy, sc.ylo >> 2);
-		hiy = std::min(hiy, ((sc.yhi + 3) >> 2) - 1);
+		loy = std::max(loy, S * (sc.ylo >> 2));
+		hiy = std::min(hiy, S * ((sc.yhi + 3) >> 2) - 1);
 		int start_y = loy * 4;
 		int end_y = hiy * 4 + 3;
-		start_y = std::max(start_y, s.yh);
-		end_y = std::min(end_y, s.yl - 1);
+		start_y = std::max(start_y, S * s.yh);
+		end_y = std::min(end_y, S * s.yl - 1);
 		if (end_y < start_y) return false;
 		bool flip = (s.flags & TRI_FLIP) != 0;
-		int ys[4] = { start_y, end_y, clampi(s.ym - 1, start_y, end_y), clampi(s.ym, start_y, end_y) };
+		int ys[4] = { start_y, end_y, clampi(S * s.ym - 1, start_y, end_y), clampi(S * s.ym, start_y, end_y) };
 		int rx0, rx1;
-		interpolate_xs(s, ys, flip, rx0, rx1);
+		interpolate_xs(s, ys, flip, rx0, rx1, S);
 		int x_bias = (s.flags & TRI_FILL_COPY_RASTER) ? 4 : 3;
-		int sx0 = sc.xlo >> 2, sx1 = ((sc.xhi + x_bias) >> 2) - 1;
+		int sx0 = S * (sc.xlo >> 2), sx1 = S * ((sc.xhi + x_bias) >> 2) - 1;
 		rx0 = clampi(rx0, sx0, sx1);
 		rx1 = clampi(rx1, sx0, sx1);
 		rx0 = std::max(rx0, lox);
@@ -839,18 +852,20 @@ struct Oracle
 		return clampi(z, 0, 0x3ffff);
 	}
 
-	static void interpolate_rgba(const int rgba_in[4], const int ddx[4], const int ddy[4], int dx, int coverage, int out[4])
+	// interpolation.h:29-53.  The 16-bit snapped value of the shader keeps every bit this reads.
+	static void interpolate_rgba(const int rgba_in[4], const int ddx[4], const int ddy[4], int dx, int coverage, int out[4],
+	                             int L = 0)
 	{
 		int first = find_lsb(uint32_t(coverage));
 		int yoff = first >> 1;
 		int xoff = ((first & 1) << 1) + (yoff & 1);
 		for (int c = 0; c < 4; c++)
 		{
-			int v = rgba_in[c] + (ddx[c] & ~0x1f) * dx;
+			int v = rgba_in[c] + ((ddx[c] & ~0x1f) >> L) * dx;
 			int sn = v >> 14;
-			sn <<= 2;
+			sn <<= 2 + L;
 			sn += xoff * (ddx[c] >> 14) + yoff * (ddy[c] >> 14);
-			sn >>= 4;
+			sn >>= 4 + L;
 			out[c] = clamp_9bit_notrunc(sn);
 		}
 	}
@@ -907,9 +922,11 @@ struct Oracle
 	}
 
 	void interpolate_st_copy(const Span &sp, const int dstzw_dx[4], int x, bool perspective, bool flip,
-	                         int dx_mask, int dx_shift, int st[2], int &s_offset) const
+	                         int dx_mask, int dx_shift, int st[2], int &s_offset, int L = 0) const
 	{
 		int dx = flip ? (x - sp.start_x) : (sp.end_x - x);
+		// Upscaled copies repeat pixels (interpolation.h:60-61).
+		dx >>= L;
 		int snapped = dx & dx_mask;
 		s_offset = dx - snapped;
 		int lerp_dx = (dx >> dx_shift) * (flip ? 1 : -1);
@@ -920,32 +937,36 @@ struct Oracle
 		st_divide(stw, perspective, st, ov);
 	}
 
-	static void interpolate_st_single(const int stzw[4], const int dstzw_dx[4], int dx, bool perspective, int st[2])
+	static void interpolate_st_single(const int stzw[4], const int dstzw_dx[4], int dx, bool perspective, int st[2],
+	                                  int L = 0)
 	{
-		int stw[3] = { (stzw[0] + (dstzw_dx[0] & ~0x1f) * dx) >> 16, (stzw[1] + (dstzw_dx[1] & ~0x1f) * dx) >> 16,
-		               (stzw[3] + (dstzw_dx[3] & ~0x1f) * dx) >> 16 };
+		int stw[3] = { (stzw[0] + ((dstzw_dx[0] & ~0x1f) >> L) * dx) >> 16,
+		               (stzw[1] + ((dstzw_dx[1] & ~0x1f) >> L) * dx) >> 16,
+		               (stzw[3] + ((dstzw_dx[3] & ~0x1f) >> L) * dx) >> 16 };
 		bool ov = false;
 		st_divide(stw, perspective, st, ov);
 	}
 
+	// interpolation.h:93-141.
 	static void interpolate_stz(const int stzw[4], const int ddx[4], const int ddy[4], int dx, int coverage,
 	                            bool perspective, bool uses_lod, int flip_dir, int st[2], int st_dx[2], int st_dy[2],
-	                            int &z, bool &overflow)
+	                            int &z, bool &overflow, int L = 0)
 	{
+		const int S = 1 << L;
 		int idx[3] = { 0, 1, 3 };
 		int stw[3], stw_dx[3], stw_dy[3];
 		for (int i = 0; i < 3; i++)
 		{
 			int c = idx[i];
-			stw[i] = stzw[c] + (ddx[c] & ~0x1f) * dx;
+			stw[i] = stzw[c] + ((ddx[c] & ~0x1f) >> L) * dx;
 		}
 		if (uses_lod)
 		{
 			for (int i = 0; i < 3; i++)
 			{
 				int c = idx[i];
-				stw_dx[i] = stw[i] + flip_dir * (ddx[c] & ~0x1f);
-				stw_dy[i] = stw[i] + (ddy[c] & ~0x7fff);
+				stw_dx[i] = stw[i] + flip_dir * ((ddx[c] & ~0x1f) >> L);
+				stw_dy[i] = stw[i] + (S > 1 ? std::abs(flip_dir) : 1) * ((ddy[c] & ~0x7fff) >> L);
 			}
 		}
 		int s0[3] = { stw[0] >> 16, stw[1] >> 16, stw[2] >> 16 };
@@ -957,14 +978,14 @@ struct Oracle
 			st_divide(s1, perspective, st_dx, overflow);
 			st_divide(s2, perspective, st_dy, overflow);
 		}
-		z = stzw[2] + ddx[2] * dx;
+		z = stzw[2] + ddx[2] * (dx >> L) + (ddx[2] >> L) * (dx & (S - 1));
 		int sz = z >> 10;
 		int first = find_lsb(uint32_t(coverage));
 		int yoff = first >> 1;
 		int xoff = ((first & 1) << 1) + (yoff & 1);
-		sz <<= 2;
+		sz <<= 2 + L;
 		sz += xoff * (ddx[2] >> 10) + yoff * (ddy[2] >> 10);
-		sz >>= 5;
+		sz >>= 5 + L;
 		z = clamp_z(sz);
 	}
 
@@ -1811,11 +1832,22 @@ struct Oracle
 		return span_rows[i];
 	}
 
-	// shading.h:38-359, scaling 1.
-	bool shade_pixel(const Prim &p, int x, int y, Shaded &out, int fb_size, int dx_mask, int dx_shift)
+	// Scaled span rows of the primitive being rendered upscaled: row r is scanline S * span_ylo + r
+	// (the last one is the pipelined texel1 peek at the next line).
+	const Span *up_rows = nullptr;
+	const Span &scaled_row(const Prim &p, int y, int L) const { return up_rows[y - (p.span_ylo << L)]; }
+
+	// shading.h:38-359; L is log2 of the upscaling factor (0 at 1x), x and y are scaled coordinates.
+	bool shade_pixel(const Prim &p, int x, int y, Shaded &out, int fb_size, int dx_mask, int dx_shift, int L = 0)
 	{
-		if (y < p.span_ylo || y > p.span_yhi) return false;
-		const Span &sp = span_row(p, y);
+		const int S = 1 << L;
+		if (y < S * p.span_ylo || y > p.span_yhi * S + (S - 1)) return false;
+		if (S > 1 && (p.setup.flags & TRI_DISABLE_UPSCALING))
+		{
+			x &= ~(S - 1);
+			y &= ~(S - 1);
+		}
+		const Span &sp = L ? scaled_row(p, y, L) : span_row(p, y);
 		if (!sp.valid) return false;
 		const StaticState &st = p.st;
 		uint32_t f = st.flags;
@@ -1837,7 +1869,7 @@ struct Oracle
 		{
 			if (!(x >= sp.start_x && x <= sp.end_x)) return false;
 			int st2[2], s_offset;
-			interpolate_st_copy(sp, p.attr.dstzw_dx, x, perspective, flip, dx_mask, dx_shift, st2, s_offset);
+			interpolate_st_copy(sp, p.attr.dstzw_dx, x, perspective, flip, dx_mask, dx_shift, st2, s_offset, L);
 			uint32_t tile0 = p.setup.tile & 7u;
 			int texel0 = sample_texture_copy(p.tmem, p.tiles[tile0], st2[0], st2[1], s_offset, tlut, fb_size);
 			out.z_dith = texel0;
@@ -1860,12 +1892,14 @@ struct Oracle
 		int dx = x - sp.base_x;
 		int interp_dir = flip ? 1 : -1;
 		int shade[4];
-		interpolate_rgba(sp.rgba, p.attr.drgba_dx, p.attr.drgba_dy, dx, coverage, shade);
+		interpolate_rgba(sp.rgba, p.attr.drgba_dx, p.attr.drgba_dy, dx, coverage, shade, L);
 
 		int st2[2] = {}, st_dx[2] = {}, st_dy[2] = {}, z = 0;
 		bool persp_overflow = false;
-		interpolate_stz(sp.stzw, p.attr.dstzw_dx, p.attr.dstzw_dy, dx, coverage, perspective, uses_lod, interp_dir,
-		                st2, st_dx, st_dy, z, persp_overflow);
+		int tex_dir = interp_dir;
+		if (S > 1 && uses_lod && (p.setup.flags & TRI_NATIVE_LOD)) tex_dir *= S;
+		interpolate_stz(sp.stzw, p.attr.dstzw_dx, p.attr.dstzw_dy, dx, coverage, perspective, uses_lod, tex_dir,
+		                st2, st_dx, st_dy, z, persp_overflow, L);
 
 		uint32_t tile0 = p.setup.tile & 7u;
 		uint32_t tile1 = (tile0 + 1) & 7u;
@@ -1882,7 +1916,7 @@ struct Oracle
 
 		if (uses_pipelined_texel1)
 		{
-			const Span &next = span_row(p, y + 1);
+			const Span &next = L ? scaled_row(p, y + 1, L) : span_row(p, y + 1);
 			bool valid_line = next.valid;
 			bool long_span = sp.lodlength >= 8;
 			bool end_span = x == (flip ? sp.end_x : sp.start_x);
@@ -1893,7 +1927,7 @@ struct Oracle
 				st_divide(stw, perspective, st2, ov);
 			}
 			else
-				interpolate_st_single(sp.stzw, p.attr.dstzw_dx, dx + interp_dir, perspective, st2);
+				interpolate_st_single(sp.stzw, p.attr.dstzw_dx, dx + interp_dir * S, perspective, st2, L);
 			tile1 = tile0;
 			uses_texel1 = true;
 		}
@@ -2500,26 +2534,56 @@ struct Oracle
 		deduced_height = std::max<uint32_t>(deduced_height, uint32_t(std::max((max_sub >> 2) + 1, 0)));
 		color_pending = true;
 		if (depth_blend.flags & DB_DEPTH_UPDATE) depth_pending = true;
+		if (yhi >= ylo) pass_span_prims++;
+		if (up_log2 && yhi >= ylo)
+		{
+			// The upscaled pass renders after the pass ends: keep the primitive with its TMEM.
+			if (!tmem_snap) tmem_snap = std::make_shared<std::vector<uint16_t>>(tmem, tmem + 2048);
+			pass_list.push_back({ p, tmem_snap });
+			pass_list.back().p.tmem = tmem_snap->data();
+		}
 		if (fb.width != 0 && yhi >= ylo) render_primitive(p);
 		if (++pass_prims >= 256) end_pass();
 	}
 
-	// Ends the current render pass: stores every pixel touched in it (finish_tile).
+	// Ends the current render pass: stores every pixel touched in it (finish_tile).  With upscaling
+	// the pass is also rendered at the scaled resolution (Renderer::flush_queues,
+	// rdp_renderer.cpp:2953-2986): the 1x pass is bracketed by the "pre" and "post" updates of the
+	// upscaled domain (submit_render_pass, 2223-2285) and followed by the upscaled pass
+	// (submit_render_pass_upscaled, 2287-2342); with super-sampled readback only the upscaled pass
+	// runs and is resolved into RDRAM.
 	void end_pass()
 	{
+		const bool need_render_pass = fb.width != 0 && deduced_height != 0 && pass_span_prims != 0;
+		if (up_log2 && !ssaa && need_render_pass) update_upscaled_domain(false);
 		if (!touched.empty())
 		{
 			bool alias = fb.addr == fb.depth_addr;
 			uint32_t depth_index = fb.depth_addr >> 1;
-			for (uint32_t slot : touched)
-			{
-				const PixelState &ps = pixel_cache[slot];
-				uint32_t x = slot & 1023u, y = slot >> 10;
-				store_color(ps, ps.color_index);
-				store_depth(ps, depth_index + fb.width * y + x, alias);
-			}
+			if (!ssaa)
+				for (uint32_t slot : touched)
+				{
+					const PixelState &ps = pixel_cache[slot];
+					uint32_t x = slot & 1023u, y = slot >> 10;
+					store_color(ps, ps.color_index);
+					store_depth(ps, depth_index + fb.width * y + x, alias);
+				}
 			touched.clear();
 		}
+		if (up_log2 && (ssaa || (need_render_pass && render_upscaled_format())))
+		{
+			if (ssaa)
+			{
+				update_upscaled_domain(false);
+				clear_ssaa_mask();
+			}
+			else
+				update_upscaled_domain(true);
+			render_upscaled();
+			if (ssaa) ssaa_resolve();
+		}
+		pass_list.clear();
+		pass_span_prims = 0;
 		pass_stamp++;
 		pass_prims = pass_uploads = 0;
 		deduced_height = 0;
@@ -2607,6 +2671,290 @@ struct Oracle
 				}
 			}
 		}
+	}
+
+	// ======================================================================= upscaling
+	// Internal upscaling by S = 2, 4 or 8 (Renderer::init_internal_upscaling_factor,
+	// rdp_renderer.cpp:545-601).  The multisampled copy of RDRAM holds S * S slices of RDRAM (and of
+	// hidden RDRAM, initialised to 3): pixel (x, y) of the scaled image lives in slice
+	// (y % S) * S + x % S, at the address of native pixel (x / S, y / S) (memory_interfacing.h:
+	// 286-362).  A reference copy of RDRAM (initially zero) records what the multisampled copy
+	// already reflects.
+	int up_log2 = 0;
+	bool ssaa = false, ssaa_dither = false;
+	std::vector<uint8_t> ms_rdram, ms_hidden, up_reference;
+	std::vector<uint32_t> ssaa_mask; // 2 bits (colour, depth written) per native pixel, 4x4 pixels a word
+	struct PassPrim
+	{
+		Prim p;
+		std::shared_ptr<std::vector<uint16_t>> tmem;
+	};
+	std::vector<PassPrim> pass_list;                  // the pass's primitives with span rows
+	std::shared_ptr<std::vector<uint16_t>> tmem_snap; // TMEM as drawn primitives see it since the last upload
+
+	bool set_upscaling(int factor, bool super_sampled, bool dither)
+	{
+		int l = factor == 2 ? 1 : factor == 4 ? 2 : factor == 8 ? 3 : factor == 1 ? 0 : -1;
+		if (l < 0 || hidden_size != rdram_size / 2) return false;
+		end_pass();
+		up_log2 = l;
+		ssaa = l && super_sampled;
+		ssaa_dither = ssaa && dither;
+		const size_t n = size_t(1) << (2 * l);
+		ms_rdram.assign(l ? n * rdram_size : 0, 0);
+		ms_hidden.assign(l ? n * hidden_size : 0, 0x03);
+		up_reference.assign(l ? rdram_size : 0, 0);
+		ssaa_mask.assign(ssaa ? (1024 / 4) * (1024 / 4) : 0, 0);
+		return true;
+	}
+
+	// Renderer::should_render_upscaled (rdp_renderer.cpp:2997-3009): 16/32-bit images at least
+	// 256 pixels wide.
+	bool render_upscaled_format() const
+	{
+		return (fb.fmt == FB_RGBA5551 || fb.fmt == FB_RGBA8888) && fb.width >= 256;
+	}
+	static int pixel_size_log2(int fmt)
+	{
+		return fmt == FB_RGBA8888 ? 2 : (fmt == FB_RGBA5551 || fmt == FB_IA88) ? 1 : 0;
+	}
+
+	// One element of update_upscaled_domain_pre.comp (post = false: RDRAM bytes that differ from the
+	// reference copy are written to every sample, with their hidden bits, and recorded) or of
+	// update_upscaled_domain_post.comp (post = true: the reference copy takes RDRAM).
+	void upscale_element(uint32_t index, int psl2, bool post)
+	{
+		const uint32_t n = 1u << (2 * up_log2), hs = rdram_size >> 1;
+		index &= (rdram_size >> psl2) - 1;
+		const uint32_t b = index << psl2, bytes = 1u << psl2;
+		if (post)
+		{
+			memcpy(&up_reference[b], &rdram[b], bytes);
+			return;
+		}
+		if (!memcmp(&up_reference[b], &rdram[b], bytes)) return;
+		for (uint32_t i = 0; i < n; i++)
+		{
+			memcpy(&ms_rdram[b + size_t(i) * rdram_size], &rdram[b], bytes);
+			uint8_t *mh = &ms_hidden[size_t(i) * hs];
+			if (psl2 == 0)
+			{
+				uint32_t m = index ^ 3u;
+				if (m & 1u) mh[m >> 1] = hidden[(m >> 1) & (hidden_size - 1)];
+			}
+			else if (psl2 == 1)
+			{
+				uint32_t m = index ^ 1u;
+				mh[m] = hidden[m & (hidden_size - 1)];
+			}
+			else
+			{
+				mh[2 * index] = hidden[(2 * index) & (hidden_size - 1)];
+				mh[2 * index + 1] = hidden[(2 * index + 1) & (hidden_size - 1)];
+			}
+		}
+		memcpy(&up_reference[b], &rdram[b], bytes);
+	}
+
+	// Renderer::submit_update_upscaled_domain (rdp_renderer.cpp:1943-2035): `pixels` elements of the
+	// image at `addr` (word aligned, whole words) and of the depth image at `depth_addr` unless the
+	// two coincide.
+	void upscale_range(uint32_t addr, uint32_t depth_addr, uint32_t pixels, int psl2, bool post)
+	{
+		addr &= ~3u;
+		depth_addr &= ~3u;
+		const uint32_t align = 4u >> psl2;
+		pixels = (pixels + align - 1) & ~(align - 1);
+		const bool alias = addr == depth_addr;
+		for (uint32_t i = 0; i < pixels; i++)
+		{
+			upscale_element((addr >> psl2) + i, psl2, post);
+			if (!alias) upscale_element((depth_addr >> 1) + i, 1, post);
+		}
+	}
+	void update_upscaled_domain(bool post)
+	{
+		upscale_range(fb.addr, fb.depth_addr, fb.width * deduced_height, pixel_size_log2(fb.fmt), post);
+	}
+
+	// clear_super_sampled_write_mask.comp over the image's 4x4 blocks (rdp_renderer.cpp:2037-2060).
+	void clear_ssaa_mask()
+	{
+		const uint32_t words = ((fb.width + 3) / 4) * ((deduced_height + 3) / 4);
+		std::fill(ssaa_mask.begin(), ssaa_mask.begin() + std::min<size_t>(words, ssaa_mask.size()), 0u);
+	}
+
+	// The pass at the scaled resolution: depth_blend.comp per 8x8 tile of the scaled image, over the
+	// pass's primitives in order, with the scaled span rows (span_setup.comp), binning
+	// (binning.h) and shading (shading.h).
+	void render_upscaled()
+	{
+		if (!fb.width || !deduced_height || pass_list.empty()) return;
+		const int L = up_log2, S = 1 << L;
+		int fb_size, dx_mask, dx_shift;
+		uint32_t addr_index;
+		switch (fb.fmt)
+		{
+		case FB_I4: fb_size = 0; dx_mask = 0; dx_shift = 0; addr_index = fb.addr; break;
+		case FB_I8: fb_size = 1; dx_mask = ~7; dx_shift = 3; addr_index = fb.addr; break;
+		case FB_RGBA5551:
+		case FB_IA88: fb_size = 2; dx_mask = ~3; dx_shift = 2; addr_index = fb.addr >> 1; break;
+		default: fb_size = 4; dx_mask = ~1; dx_shift = 1; addr_index = fb.addr >> 2; break;
+		}
+		const uint32_t depth_index = fb.depth_addr >> 1;
+		const bool alias = fb.addr == fb.depth_addr;
+		const int width = int(fb.width), ws = width * S, hs = int(deduced_height) * S;
+
+		std::vector<std::vector<Span>> rows(pass_list.size());
+		for (size_t k = 0; k < pass_list.size(); k++)
+		{
+			const Prim &p = pass_list[k].p;
+			const int n = (p.span_yhi - p.span_ylo + 1) * S + 1;
+			rows[k].resize(size_t(n));
+			for (int r = 0; r < n; r++) rows[k][size_t(r)] = span_setup(p.setup, p.attr, p.scissor, S * p.span_ylo + r, L);
+		}
+
+		uint8_t *const native_rd = mem_rd, *const native_hd = mem_hd;
+		auto select_slice = [&](int x, int y) {
+			const uint32_t slice = uint32_t(((y & (S - 1)) << L) + (x & (S - 1)));
+			mem_rd = ms_rdram.data() + size_t(slice) * rdram_size;
+			mem_hd = ms_hidden.data() + size_t(slice) * (rdram_size >> 1);
+		};
+		const int tiles_x = (ws + 7) / 8, tiles_y = (hs + 7) / 8;
+		PixelState px[64];
+		for (int ty = 0; ty < tiles_y; ty++)
+			for (int tx = 0; tx < tiles_x; tx++)
+			{
+				const int lox = tx * 8, loy = ty * 8, hix = std::min(lox + 7, ws - 1), hiy = std::min(loy + 7, hs - 1);
+				for (int y = loy; y <= hiy; y++)
+					for (int x = lox; x <= hix; x++)
+					{
+						PixelState &ps = px[(y - loy) * 8 + (x - lox)];
+						ps = {};
+						const uint32_t off = uint32_t(width) * uint32_t(y >> L) + uint32_t(x >> L);
+						ps.color_index = addr_index + off; // the fill colour's half / byte follows it
+						select_slice(x, y);
+						load_color(ps, addr_index + off);
+						load_depth(ps, depth_index + off);
+					}
+				for (size_t k = 0; k < pass_list.size(); k++)
+				{
+					const Prim &p = pass_list[k].p;
+					if (!bin_primitive(p.setup, lox, loy, hix, hiy, p.scissor, S)) continue;
+					up_rows = rows[k].data();
+					for (int y = loy; y <= hiy; y++)
+						for (int x = lox; x <= hix; x++)
+						{
+							Shaded sh = {};
+							if (!shade_pixel(p, x, y, sh, fb_size, dx_mask, dx_shift, L)) continue;
+							PixelState &ps = px[(y - loy) * 8 + (x - lox)];
+							if (sh.coverage_count & 0x40) fill_color_op(ps, p.derived.fill_color, alias);
+							else if (sh.coverage_count & 0x20) copy_pipeline(ps, uint32_t(sh.z_dith), alias);
+							else depth_blend_op(ps, p, sh, alias);
+						}
+				}
+				up_rows = nullptr;
+				for (int y = loy; y <= hiy; y++)
+					for (int x = lox; x <= hix; x++)
+					{
+						const PixelState &ps = px[(y - loy) * 8 + (x - lox)];
+						const uint32_t xn = uint32_t(x >> L), yn = uint32_t(y >> L);
+						const uint32_t off = uint32_t(width) * yn + xn;
+						select_slice(x, y);
+						store_color(ps, addr_index + off);
+						store_depth(ps, depth_index + off, alias);
+						if (ssaa)
+						{
+							// emit_scaled_write_masks (memory_interfacing.h:305-337).
+							const uint32_t block = (yn >> 2) * ((uint32_t(width) + 3) >> 2) + (xn >> 2);
+							const uint32_t word = (uint32_t(ps.color_dirty) + 2u * uint32_t(ps.depth_dirty))
+							                      << (2 * ((xn & 3) + (yn & 3) * 4));
+							if (block < ssaa_mask.size()) ssaa_mask[block] |= word;
+						}
+					}
+			}
+		mem_rd = native_rd;
+		mem_hd = native_hd;
+	}
+
+	// update_upscaled_domain_resolve.comp: every native pixel of the image that a sample wrote takes
+	// the average of its samples (colour; RGBA5551 with an optional ordered dither) or its first
+	// sample (depth), in RDRAM and in the reference copy.  Hidden RDRAM is not written.
+	void ssaa_resolve()
+	{
+		static const uint32_t bayer[16] = { 0, 4, 1, 5, 4, 0, 5, 1, 3, 7, 2, 6, 7, 3, 6, 2 };
+		const uint32_t n = 1u << (2 * up_log2), w = fb.width, h = deduced_height;
+		const int psl2 = pixel_size_log2(fb.fmt);
+		const uint32_t color_base = fb.addr >> psl2, depth_base = fb.depth_addr >> 1;
+		const bool alias = fb.addr == fb.depth_addr;
+		auto rd16 = [](const uint8_t *m, uint32_t i) { return uint32_t(m[2 * i]) | (uint32_t(m[2 * i + 1]) << 8); };
+		auto wr16 = [](uint8_t *m, uint32_t i, uint32_t v) { m[2 * i] = uint8_t(v); m[2 * i + 1] = uint8_t(v >> 8); };
+		auto rd32 = [](const uint8_t *m, uint32_t i) {
+			return uint32_t(m[4 * i]) | (uint32_t(m[4 * i + 1]) << 8) | (uint32_t(m[4 * i + 2]) << 16) |
+			       (uint32_t(m[4 * i + 3]) << 24);
+		};
+		auto wr32 = [](uint8_t *m, uint32_t i, uint32_t v) {
+			for (int k = 0; k < 4; k++) m[4 * i + k] = uint8_t(v >> (8 * k));
+		};
+		for (uint32_t y = 0; y < h; y++)
+			for (uint32_t x = 0; x < w; x++)
+			{
+				const uint32_t index = y * w + x;
+				const uint32_t block = (x >> 2) + (y >> 2) * ((w + 3) >> 2);
+				const uint32_t wm = block < ssaa_mask.size() ? ssaa_mask[block] >> (2 * ((x & 3) + 4 * (y & 3))) : 0u;
+				if (wm & 1u)
+				{
+					uint32_t ci = color_base + index;
+					if (psl2 == 0)
+					{
+						// The shader sums the first sample NUM_SAMPLES times: the result is that sample.
+						ci = (ci & (rdram_size - 1)) ^ 3u;
+						rdram[ci] = up_reference[ci] = ms_rdram[ci];
+					}
+					else if (psl2 == 1)
+					{
+						ci = (ci & ((rdram_size >> 1) - 1)) ^ 1u;
+						uint32_t sum[4] = { 0, 0, 0, 0 };
+						for (uint32_t i = 0; i < n; i++)
+						{
+							uint32_t v = rd16(ms_rdram.data() + size_t(i) * rdram_size, ci);
+							sum[0] += (v >> 11) & 0x1f;
+							sum[1] += (v >> 6) & 0x1f;
+							sum[2] += (v >> 1) & 0x1f;
+							sum[3] += v & 1;
+						}
+						for (int c = 0; c < 4; c++)
+						{
+							if (ssaa_dither) sum[c] = (8 * sum[c] + bayer[(y & 3) * 4 + (x & 3)] * n) / (8 * n);
+							else sum[c] = (sum[c] + (n >> 1)) / n;
+						}
+						uint32_t enc = (sum[0] << 11) | (sum[1] << 6) | (sum[2] << 1) | sum[3];
+						wr16(rdram.data(), ci, enc & 0xffff);
+						wr16(up_reference.data(), ci, enc & 0xffff);
+					}
+					else
+					{
+						ci &= (rdram_size >> 2) - 1;
+						uint32_t sum[4] = { 0, 0, 0, 0 };
+						for (uint32_t i = 0; i < n; i++)
+						{
+							uint32_t v = rd32(ms_rdram.data() + size_t(i) * rdram_size, ci);
+							for (int c = 0; c < 4; c++) sum[c] += (v >> (24 - 8 * c)) & 0xff;
+						}
+						uint32_t enc = 0;
+						for (int c = 0; c < 4; c++) enc |= (((sum[c] + (n >> 1)) / n) & 0xffu) << (24 - 8 * c);
+						wr32(rdram.data(), ci, enc);
+						wr32(up_reference.data(), ci, enc);
+					}
+				}
+				if (!alias && (wm & 2u))
+				{
+					const uint32_t di = ((depth_base + index) & ((rdram_size >> 1) - 1)) ^ 1u;
+					const uint32_t v = rd16(ms_rdram.data(), di);
+					wr16(rdram.data(), di, v);
+					wr16(up_reference.data(), di, v);
+				}
+			}
 	}
 
 	// ======================================================================= TMEM upload (tmem_update.comp)
@@ -2924,6 +3272,7 @@ struct Oracle
 			next[gid] = uint16_t(value);
 		}
 		memcpy(tmem, next, sizeof(tmem));
+		tmem_snap.reset();
 	}
 
 	// rdp_renderer.cpp:3099-3220 / 3222-3486.
@@ -3400,6 +3749,8 @@ void *oracle_create(uint32_t rdram_size, uint32_t hidden_size)
 	o->rdram.assign(rdram_size, 0);
 	o->pixel_cache.assign(1024 * 1024, PixelStateSlot{});
 	o->hidden.assign(hidden_size, 0x03);
+	o->mem_rd = o->rdram.data();
+	o->mem_hd = o->hidden.data();
 	o->init_luts();
 	return o;
 }
@@ -3433,6 +3784,37 @@ void oracle_read_hidden(void *h, uint8_t *data, uint32_t offset, uint32_t size)
 	o->end_pass();
 	memcpy(data, o->hidden.data() + offset, size);
 }
+// Internal upscaling (factor 1, 2, 4 or 8) with optional super-sampled readback and its dither;
+// set before the first command.  Returns 0, or -1 for an unsupported factor or a hidden RDRAM
+// that is not half of RDRAM.
+int oracle_set_upscaling(void *h, uint32_t factor, uint32_t super_sampled, uint32_t dither)
+{
+	Oracle *o = static_cast<Oracle *>(h);
+	return o->set_upscaling(int(factor), super_sampled != 0, dither != 0) ? 0 : -1;
+}
+uint32_t oracle_upscaling_factor(void *h) { return 1u << static_cast<Oracle *>(h)->up_log2; }
+// The multisampled copies (factor^2 slices of RDRAM / hidden RDRAM); byte offsets.
+void oracle_read_upscaled_rdram(void *h, uint8_t *data, uint64_t offset, uint64_t size)
+{
+	Oracle *o = static_cast<Oracle *>(h);
+	o->end_pass();
+	memcpy(data, o->ms_rdram.data() + offset, size_t(size));
+}
+void oracle_read_upscaled_hidden(void *h, uint8_t *data, uint64_t offset, uint64_t size)
+{
+	Oracle *o = static_cast<Oracle *>(h);
+	o->end_pass();
+	memcpy(data, o->ms_hidden.data() + offset, size_t(size));
+}
+// The "pre" update of the upscaled domain over a scanout range (VideoInterface::vram_fetch_stage,
+// video_interface.cpp:412-420): `length` elements of 2^psl2 bytes from `offset`.
+void oracle_upscale_pre_external(void *h, uint32_t offset, uint32_t length, uint32_t psl2)
+{
+	Oracle *o = static_cast<Oracle *>(h);
+	o->end_pass();
+	if (o->up_log2) o->upscale_range(offset, offset, length, int(psl2), false);
+}
+
 void oracle_write_hidden(void *h, const uint8_t *data, uint32_t offset, uint32_t size)
 {
 	Oracle *o = static_cast<Oracle *>(h);

@@ -19,6 +19,7 @@
 #include <math.h>
 #include <algorithm>
 #include <vector>
+#include <functional>
 
 namespace {
 
@@ -185,15 +186,44 @@ struct ViOracle
 		uint32_t crop_overscan_pixels, crop_rect_enable, crop_left, crop_right, crop_top, crop_bottom;
 		uint32_t persist_frame_on_invalid_input, blend_previous_frame, upscale_deinterlacing;
 		uint32_t vi_aa, vi_scale, vi_serrate, vi_dither_filter, vi_divot_filter, vi_gamma_dither;
+		uint32_t downscale_steps;
 	};
 
-	// Returns true and fills `out` when an image is produced.
-	bool scanout(const Options &o, const uint8_t *rdram, uint32_t rdram_size, const uint8_t *hidden, Img &out)
+	// VideoInterface::scanout_memory_range (video_interface.cpp:369-396): the bytes the fetch reads,
+	// from the registers as they are after the per-scanline state is cleared.
+	void memory_range(uint32_t &offset, uint32_t &length)
+	{
+		const bool ended = ps_ended;
+		ps_ended = false;
+		Regs r = decode(nullptr);
+		ps_ended = ended;
+		bool divot = (r.status & VI_DIVOT) != 0;
+		int aw = r.max_x + 2 + 4 + int(divot) * 2, ah = r.max_y + 1 + 4;
+		if (r.vi_offset == 0 || r.h_res <= 0 || r.h_start >= SCANOUT_WIDTH)
+		{
+			offset = length = 0;
+			return;
+		}
+		int pixel_size = ((r.status & VI_TYPE_MASK) | VI_TYPE_5551) == VI_TYPE_8888 ? 4 : 2;
+		int off = r.vi_offset & ~(pixel_size - 1);
+		off += ((divot ? -3 : -2) + -2 * r.vi_width) * pixel_size;
+		offset = uint32_t(off);
+		length = uint32_t((ah * r.vi_width + aw) * pixel_size);
+	}
+
+	// Returns true and fills `out` when an image is produced.  With an upscaling factor S > 1 the
+	// sources are the multisampled copies (S * S slices of rdram_size / hidden bytes) and the image
+	// is S times larger (video_interface.cpp:1299-1318), then halved downscale_steps times.
+	// `sources` is called when the framebuffer is fetched (not for frames without an image) and
+	// returns the RDRAM and hidden RDRAM to fetch from.
+	bool scanout(const Options &o, const std::function<std::pair<const uint8_t *, const uint8_t *>()> &sources,
+	             uint32_t rdram_size, Img &out, int S = 1)
 	{
 		Line lines[MAX_OUTPUT_SCANLINES];
 		Regs r = decode(lines);
 		ps_flags = 0;
 		ps_ended = false;
+		const int L = S == 8 ? 3 : S == 4 ? 2 : S == 2 ? 1 : 0;
 		if (r.vi_offset == 0)
 		{
 			have_prev = false;
@@ -234,7 +264,28 @@ struct ViOracle
 		}
 		last_valid_frame_count = frame_count;
 		bool degenerate = r.h_res <= 0 || r.v_res <= 0;
-		bool fetch_bug = r.init_y_add < 1024;
+		if (S > 1)
+		{
+			r.h_start *= S;
+			r.h_start_clamp *= S;
+			r.v_start *= S;
+			r.h_res *= S;
+			r.h_res_clamp *= S;
+			r.v_res *= S;
+			r.max_x = r.max_x * S + (S - 1);
+			r.max_y = r.max_y * S + (S - 1);
+			for (Line &li : lines)
+			{
+				li.h_start *= S;
+				li.h_start_clamp *= S;
+				li.h_end_clamp *= S;
+				li.x_start *= S;
+				li.y_start *= S;
+				li.y_base *= S;
+			}
+		}
+		// need_fetch_bug_emulation (video_interface.cpp:398-403).
+		bool fetch_bug = r.init_y_add < 1024 && S == 1;
 		bool is_8888 = (r.status & VI_TYPE_MASK) == VI_TYPE_8888;
 		bool fetch_aa = (r.status & VI_META_AA) != 0;
 		bool dither_filter = (r.status & VI_DITHER_FILTER) != 0;
@@ -242,6 +293,8 @@ struct ViOracle
 		Img vram, aa, dv;
 		if (!degenerate)
 		{
+			const auto src = sources();
+			const uint8_t *rdram = src.first, *hidden = src.second;
 			// extract_vram.comp
 			int ew = r.max_x + 2 + 4 + int(divot) * 2, eh = r.max_y + 1 + 4;
 			vram.init(ew, eh, 1);
@@ -251,11 +304,16 @@ struct ViOracle
 				for (int x = 0; x < ew; x++)
 				{
 					int cx = x + xo, cy = y + yo;
+					// extract_vram.comp:58-67: the sample slice of an upscaled pixel.
+					const int slice = ((cy & (S - 1)) << L) + (cx & (S - 1));
+					cx >>= L;
+					cy >>= L;
 					uint32_t c[4];
 					int lin = cy * r.vi_width + cx + fb_offset;
 					if (is_8888)
 					{
 						lin &= int((rdram_size >> 2) - 1);
+						lin += slice * int(rdram_size >> 2);
 						const uint8_t *p = rdram + size_t(lin) * 4;
 						uint32_t w = uint32_t(p[0]) | (uint32_t(p[1]) << 8) | (uint32_t(p[2]) << 16) | (uint32_t(p[3]) << 24);
 						c[0] = (w >> 24) & 0xff; c[1] = (w >> 16) & 0xff; c[2] = (w >> 8) & 0xff; c[3] = (w >> 5) & 7;
@@ -263,9 +321,10 @@ struct ViOracle
 					else
 					{
 						lin &= int((rdram_size >> 1) - 1);
+						lin += slice * int(rdram_size >> 1);
 						const uint8_t *p = rdram + size_t(lin ^ 1) * 2;
 						uint32_t w = uint32_t(p[0]) | (uint32_t(p[1]) << 8);
-						uint32_t hw = hidden[lin & int((rdram_size >> 1) - 1)];
+						uint32_t hw = hidden[lin];
 						c[0] = (w >> 8) & 0xf8; c[1] = (w >> 3) & 0xf8; c[2] = (w << 2) & 0xf8; c[3] = ((w & 1) << 2) | hw;
 					}
 					if (!fetch_aa) c[3] = 7;
@@ -404,7 +463,7 @@ struct ViOracle
 
 		// vi_scale.frag + blend of the previous frame (video_interface.cpp:719-988).
 		bool serrate = (r.status & VI_SERRATE) != 0 && !o.upscale_deinterlacing;
-		int width = SCANOUT_WIDTH, height = (r.is_pal ? V_RES_PAL : V_RES_NTSC) >> int(!serrate);
+		int width = SCANOUT_WIDTH * S, height = ((r.is_pal ? V_RES_PAL : V_RES_NTSC) >> int(!serrate)) * S;
 		unsigned cl = 0, cr = 0, ct = 0, cb = 0;
 		if (o.crop_rect_enable)
 		{
@@ -418,6 +477,10 @@ struct ViOracle
 			cl = cr = cx;
 			ct = cb = cy;
 		}
+		cl *= unsigned(S);
+		cr *= unsigned(S);
+		ct *= unsigned(S);
+		cb *= unsigned(S);
 		if (cl + cr < unsigned(width) && ct + cb < unsigned(height))
 		{
 			width -= int(cl + cr);
@@ -426,7 +489,7 @@ struct ViOracle
 		out.init(width, height, 1);
 
 		int v_start = r.v_start, v_res = r.v_res;
-		int serrate_shift = 0, serrate_mask = 0, serrate_select = 0, info_y_shift = 0;
+		int serrate_shift = 0, serrate_mask = 0, serrate_select = 0, info_y_shift = L;
 		if (serrate)
 		{
 			v_start *= 2;
@@ -434,7 +497,7 @@ struct ViOracle
 			serrate_shift = 1;
 			serrate_mask = 1;
 			serrate_select = int(r.v_current_line == 0);
-			info_y_shift = 1;
+			info_y_shift++;
 		}
 		bool scale_aa = (r.status & VI_META_SCALE) != 0;
 		bool gamma_en = (r.status & VI_GAMMA) != 0, gamma_dither = (r.status & VI_GAMMA_DITHER) != 0;
@@ -544,6 +607,25 @@ struct ViOracle
 				if (r.h_res > 0 && prev.h > v_start + v_res) blend(r.h_start, v_start + v_res, r.h_res, prev.h - (v_start + v_res));
 			}
 		}
+		// downscale_stage (video_interface.cpp:1000-1064): each step halves the image; the
+		// reference's linear blit of exactly 2:1 is the mean of each 2x2 block, rounded half up.
+		for (int steps = int(std::min(8u, o.downscale_steps)), f = S; f > 1 && steps > 0; f >>= 1, steps--)
+		{
+			Img half;
+			half.init(out.w / 2, out.h / 2, 1);
+			for (int y = 0; y < half.h; y++)
+				for (int x = 0; x < half.w; x++)
+				{
+					uint32_t a[4], b[4], c[4], d[4];
+					out.get(2 * x, 2 * y, 0, a);
+					out.get(2 * x + 1, 2 * y, 0, b);
+					out.get(2 * x, 2 * y + 1, 0, c);
+					out.get(2 * x + 1, 2 * y + 1, 0, d);
+					uint8_t *q = half.at(x, y, 0);
+					for (int i = 0; i < 4; i++) q[i] = uint8_t((a[i] + b[i] + c[i] + d[i] + 2) >> 2);
+				}
+			out = half;
+		}
 		prev = out;
 		have_prev = true;
 		frame_count++;
@@ -601,6 +683,10 @@ extern "C" uint32_t oracle_rdram_size(void *h);
 extern "C" uint32_t oracle_hidden_size(void *h);
 extern "C" void *oracle_vi_state(void *h);
 extern "C" void oracle_set_vi_state(void *h, void *vi);
+extern "C" uint32_t oracle_upscaling_factor(void *h);
+extern "C" void oracle_read_upscaled_rdram(void *h, uint8_t *data, uint64_t offset, uint64_t size);
+extern "C" void oracle_read_upscaled_hidden(void *h, uint8_t *data, uint64_t offset, uint64_t size);
+extern "C" void oracle_upscale_pre_external(void *h, uint32_t offset, uint32_t length, uint32_t psl2);
 
 static ViOracle *vi_of(void *h)
 {
@@ -626,18 +712,42 @@ void oracle_vi_set_for_scanline(void *h, uint32_t reg, uint32_t value) { vi_of(h
 void oracle_vi_latch_scanline(void *h, uint32_t line) { vi_of(h)->latch_scanline(line); }
 void oracle_vi_end_per_scanline(void *h) { vi_of(h)->end_per_scanline(); }
 
-// opts: 15 uint32 in ViOracle::Options order.  out: capacity 640 x 576 RGBA8 words.
+// opts: 16 uint32 in ViOracle::Options order.  out: capacity (640 x 576) x factor^2 RGBA8 words.
 int oracle_scanout(void *h, const uint32_t *opts, uint32_t *out, uint32_t *width, uint32_t *height)
 {
 	ViOracle *v = vi_of(h);
 	ViOracle::Options o;
 	memcpy(&o, opts, sizeof(o));
 	uint32_t rs = oracle_rdram_size(h), hs = oracle_hidden_size(h);
-	std::vector<uint8_t> rd(rs), hid(hs);
-	oracle_read_rdram(h, rd.data(), 0, rs);
-	oracle_read_hidden(h, hid.data(), 0, hs);
+	const uint32_t factor = oracle_upscaling_factor(h);
+	const uint32_t raw_status = v->regs[0];
+	std::vector<uint8_t> rd, hid;
+	auto sources = [&]() -> std::pair<const uint8_t *, const uint8_t *> {
+		if (factor > 1)
+		{
+			// The fetch first brings the scanned range of the upscaled domain up to date with RDRAM
+			// (VideoInterface::vram_fetch_stage, video_interface.cpp:410-420); the pixel size follows
+			// the status with the RGBA5551 bit forced (video_interface.cpp:1256).
+			uint32_t offset, length;
+			v->memory_range(offset, length);
+			uint32_t psl2 = ((raw_status & VI_TYPE_MASK) | VI_TYPE_5551) == VI_TYPE_8888 ? 2 : 1;
+			oracle_upscale_pre_external(h, offset, length, psl2);
+			rd.resize(size_t(rs) * factor * factor);
+			hid.resize(size_t(hs) * factor * factor);
+			oracle_read_upscaled_rdram(h, rd.data(), 0, rd.size());
+			oracle_read_upscaled_hidden(h, hid.data(), 0, hid.size());
+		}
+		else
+		{
+			rd.resize(rs);
+			hid.resize(hs);
+			oracle_read_rdram(h, rd.data(), 0, rs);
+			oracle_read_hidden(h, hid.data(), 0, hs);
+		}
+		return { rd.data(), hid.data() };
+	};
 	Img img;
-	if (!v->scanout(o, rd.data(), rs, hid.data(), img))
+	if (!v->scanout(o, sources, rs, img, int(factor)))
 	{
 		*width = *height = 0;
 		return 0;

@@ -19,8 +19,8 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I" + INCLUDE]
 
-CUDA_SOURCES = ["rdp_kernels.cu", "rdp_cp.cpp", "vi.cu", "sched.cu", "rdp_dump.cpp", "coherency.cu"]
-HEADERS = ["rdp_types.h", "rdp_kernels.h", "blender_divider_runs.inc", "vi.h", "sched.h", "rdp_exec.h", "rdp_coherency.h"]
+CUDA_SOURCES = ["rdp_kernels.cu", "rdp_cp.cpp", "vi.cu", "sched.cu", "rdp_dump.cpp", "coherency.cu", "upscale.cu"]
+HEADERS = ["rdp_types.h", "rdp_kernels.h", "blender_divider_runs.inc", "vi.h", "sched.h", "rdp_exec.h", "rdp_coherency.h", "rdp_upscale.h"]
 
 
 def _newer(src_paths, target):

@@ -40,6 +40,7 @@
 #include <cuda_fp16.h>
 #include "vi.h"
 #include "rdp_coherency.h"
+#include "rdp_upscale.h"
 #include "blender_divider_runs.inc"
 
 namespace {
@@ -314,6 +315,30 @@ struct rdp_cp
 	std::deque<rdpx::PassPacket> deferred;   // batched: passes waiting for the batch's next launch
 	std::vector<uint64_t> unsubmitted;       // batched: timeline values signalled before that launch
 
+	// ---------------------------------------------------------------- internal upscaling
+	// RDP_CREATE_UPSCALING_* (Renderer::init_internal_upscaling_factor, rdp_renderer.cpp:545-601):
+	// the multisampled copy of RDRAM and hidden RDRAM (factor^2 slices each, then the super-sampled
+	// write mask) and the reference copy of what it reflects of RDRAM.
+	uint32_t up_log2 = 0;
+	bool ssaa = false, ssaa_dither = false;
+	uint8_t *d_ms_rdram = nullptr, *d_ms_hidden = nullptr, *d_up_reference = nullptr;
+	static constexpr size_t kSsaaMaskBytes = 2 * 1024 * 1024 / 8; // 2 bits per pixel of a 1024 x 1024 image
+	RdpUpscaleDomain up_domain() const
+	{
+		RdpUpscaleDomain d = {};
+		d.rdram = d_rdram;
+		d.hidden = d_hidden;
+		d.reference = d_up_reference;
+		d.ms_rdram = d_ms_rdram;
+		d.ms_hidden = d_ms_hidden;
+		d.ssaa_mask = ssaa ? reinterpret_cast<uint32_t *>(d_ms_rdram + (size_t(rdram_size) << (2 * up_log2))) : nullptr;
+		d.wmask = coherent ? d_wmask : nullptr;
+		d.rdram_size = rdram_size;
+		d.hidden_size = hidden_size;
+		d.samples = 1u << (2 * up_log2);
+		return d;
+	}
+
 	// ---------------------------------------------------------------- pass being recorded
 	std::vector<RdpPrimIn> prims;
 	std::vector<RdpPrimIn> grouped; // prims regrouped by target at flush
@@ -344,6 +369,7 @@ struct rdp_cp
 	struct Target
 	{
 		uint32_t addr = 0, width = 0, fmt = 0, depth_addr = 0, deduced_height = 0;
+		uint32_t span_prims = 0;        // primitives with span rows (the reference's span jobs)
 		bool color_pending = false, depth_pending = false, depth_used = false;
 		std::vector<uint32_t> prim_ids; // indices into `prims`
 	};
@@ -364,7 +390,9 @@ struct rdp_cp
 	{
 		return fmt == FBF_I8 || addr == depth_addr;
 	}
-	bool pass_boundaries_visible() const { return boundaries_visible(fb.fmt, fb.addr, fb.depth_addr); }
+	// With upscaling every pass is the reference's pass: its pre / post updates of the upscaled
+	// domain follow the reference's pass boundaries.
+	bool pass_boundaries_visible() const { return up_log2 || boundaries_visible(fb.fmt, fb.addr, fb.depth_addr); }
 	// The reference's pass ends: with visible boundaries this processor's pass ends too.
 	void rv_end()
 	{
@@ -424,6 +452,8 @@ struct rdp_cp
 		int prev_w = 0, prev_h = 0;
 		// Device images.
 		uint32_t *d_aa = nullptr, *d_dv = nullptr, *d_out[2] = { nullptr, nullptr };
+		uint32_t *d_half = nullptr; // downscale step output
+		size_t half_cap = 0;
 		size_t aa_cap = 0, dv_cap = 0;
 		int cur = 0;
 		RdpViLine *d_lines = nullptr, *h_lines = nullptr;
@@ -551,6 +581,23 @@ struct rdp_cp
 		}
 		if (check(cudaMemsetAsync(d_hidden, 0x03, hidden_size, stream))) return RDP_ERR_DEVICE;
 		if (check(cudaMemsetAsync(d_tmem, 0, 4096, stream))) return RDP_ERR_DEVICE;
+		const uint32_t up = info->flags & (RDP_CREATE_UPSCALING_2X | RDP_CREATE_UPSCALING_4X | RDP_CREATE_UPSCALING_8X);
+		if (up)
+		{
+			// The largest factor asked for wins (rdp_device.cpp:189-196).
+			up_log2 = (up & RDP_CREATE_UPSCALING_8X) ? 3 : (up & RDP_CREATE_UPSCALING_4X) ? 2 : 1;
+			ssaa = (info->flags & RDP_CREATE_SUPER_SAMPLED_READ_BACK) != 0;
+			ssaa_dither = ssaa && (info->flags & RDP_CREATE_SUPER_SAMPLED_DITHER) != 0;
+			const size_t n = size_t(1) << (2 * up_log2);
+			const size_t ms_bytes = n * rdram_size + (ssaa ? kSsaaMaskBytes : 0);
+			if (cudaMalloc(&d_ms_rdram, ms_bytes) != cudaSuccess) return RDP_ERR_OOM;
+			if (cudaMalloc(&d_ms_hidden, n * hidden_size) != cudaSuccess) return RDP_ERR_OOM;
+			if (cudaMalloc(&d_up_reference, rdram_size) != cudaSuccess) return RDP_ERR_OOM;
+			if (check(cudaMemsetAsync(d_ms_rdram, 0, ms_bytes, stream)) ||
+			    check(cudaMemsetAsync(d_ms_hidden, 0x03, n * hidden_size, stream)) ||
+			    check(cudaMemsetAsync(d_up_reference, 0, rdram_size, stream)))
+				return RDP_ERR_DEVICE;
+		}
 		if (check(cudaMemsetAsync(d_fragments, 0, 4 * sizeof(unsigned long long), stream))) return RDP_ERR_DEVICE;
 		if (check(cudaMemcpyAsync(d_rdram, host_rdram, rdram_size, cudaMemcpyHostToDevice, stream))) return RDP_ERR_DEVICE;
 		if (check(cudaStreamSynchronize(stream))) return RDP_ERR_DEVICE;
@@ -580,10 +627,14 @@ struct rdp_cp
 		cudaFree(d_snapshots);
 		cudaFree(d_fragments);
 		cudaFree(d_wmask);
+		cudaFree(d_ms_rdram);
+		cudaFree(d_ms_hidden);
+		cudaFree(d_up_reference);
 		cudaFree(vi.d_aa);
 		cudaFree(vi.d_dv);
 		cudaFree(vi.d_out[0]);
 		cudaFree(vi.d_out[1]);
+		cudaFree(vi.d_half);
 		cudaFree(vi.d_lines);
 		if (vi.h_lines) cudaFreeHost(vi.h_lines);
 		if (vi.lines_copied) cudaEventDestroy(vi.lines_copied);
@@ -835,6 +886,13 @@ struct rdp_cp
 			if (coherent && !in_capture()) pk.read_pages = read_pages;
 			deferred.push_back(std::move(pk));
 		}
+		else if (up_log2)
+		{
+			if (coherent && refresh_pages(read_pages) != RDP_OK) return sticky_error;
+			uint64_t before = exec->kernel_launches;
+			if (launch_upscaled(v) != RDP_OK) return sticky_error;
+			stats.kernel_launches += exec->kernel_launches - before;
+		}
 		else
 		{
 			// A capture records the GPU work only: its replays render against the device copy.
@@ -849,6 +907,74 @@ struct rdp_cp
 		stats.tmem_uploads += num_recorded_uploads;
 		base_prim_index += num_recorded_prims;
 		reset_pass();
+		return sticky_error;
+	}
+
+	static uint32_t pixel_size_log2(uint32_t fmt)
+	{
+		return fmt == FBF_RGBA8888 ? 2u : (fmt == FBF_RGBA5551 || fmt == FBF_IA88) ? 1u : 0u;
+	}
+	// A recorded pass of an upscaling processor (Renderer::flush_queues, rdp_renderer.cpp:2953-2986).
+	// Without super-sampled readback: the "pre" update of the upscaled domain over the image, the
+	// 1x pass, and -- for 16/32-bit images at least 256 wide (should_render_upscaled, 2997-3009) --
+	// the "post" update and the pass again at the scaled resolution (submit_render_pass 2223-2285,
+	// submit_render_pass_upscaled 2287-2342).  With it: only the upscaled pass, between the "pre"
+	// update plus a cleared write mask and the resolve into RDRAM.  Passes have one target here.
+	int launch_upscaled(const rdpx::PassView &v)
+	{
+		const Target *tg = targets.empty() ? nullptr : &targets[0];
+		const bool need_render_pass = tg && tg->width && tg->deduced_height && tg->span_prims;
+		const uint32_t psl2 = tg ? pixel_size_log2(tg->fmt) : 0;
+		const uint32_t pixels = tg ? tg->width * tg->deduced_height : 0;
+		const RdpUpscaleDomain dom = up_domain();
+		if (!ssaa)
+		{
+			if (need_render_pass && check(rdp_upscale_sync(&dom, tg->addr, tg->depth_addr, pixels, psl2, 0, stream)))
+				return sticky_error;
+			if (!exec->launch(&v, 1, nullptr)) return check(cudaErrorUnknown);
+			if (!need_render_pass || !((tg->fmt == FBF_RGBA5551 || tg->fmt == FBF_RGBA8888) && tg->width >= 256))
+				return sticky_error;
+			if (check(rdp_upscale_sync(&dom, tg->addr, tg->depth_addr, pixels, psl2, 1, stream))) return sticky_error;
+		}
+		else
+		{
+			if (tg && (check(rdp_upscale_sync(&dom, tg->addr, tg->depth_addr, pixels, psl2, 0, stream)) ||
+			           check(rdp_ssaa_clear_mask(&dom, tg->width, tg->deduced_height, stream))))
+				return sticky_error;
+			if (v.num_uploads)
+			{
+				// The pass's TMEM uploads (they read RDRAM itself), without its primitives.
+				rdpx::PassView uv = v;
+				for (uint32_t t = 0; t < uv.num_targets; t++)
+				{
+					uv.target_prims[t] = 0;
+					uv.target[t].tiles_x = uv.target[t].tiles_y = 0;
+				}
+				uv.num_prims = 0;
+				if (!exec->launch(&uv, 1, nullptr)) return check(cudaErrorUnknown);
+			}
+		}
+		// The 1x launch applied the uploads; the upscaled pass samples the same TMEM snapshots.
+		rdpx::PassView sv = v;
+		sv.uploads = nullptr;
+		sv.num_uploads = 0;
+		for (uint32_t t = 0; t < sv.num_targets; t++)
+		{
+			RdpPass &d = sv.target[t];
+			d.rdram = d_ms_rdram;
+			d.hidden = d_ms_hidden;
+			d.wmask = nullptr;
+			d.counters = nullptr;
+			d.fb_width <<= up_log2;
+			d.fb_height <<= up_log2;
+			d.tiles_x = sv.target_prims[t] ? (d.fb_width + 7) / 8 : 0;
+			d.tiles_y = sv.target_prims[t] ? (d.fb_height + 7) / 8 : 0;
+			d.scale = up_log2 | (ssaa ? 0x100u : 0u);
+		}
+		if (!exec->launch(&sv, 1, nullptr, true)) return check(cudaErrorUnknown);
+		if (ssaa && tg &&
+		    check(rdp_ssaa_resolve(&dom, tg->addr, tg->depth_addr, tg->width, tg->deduced_height, psl2, ssaa_dither, stream)))
+			return sticky_error;
 		return sticky_error;
 	}
 
@@ -970,6 +1096,7 @@ struct rdp_cp
 		rv.color_pending = true;
 		rv.depth_pending |= writes_depth;
 		int min_line = std::max(yh, scissor_ylo) >> 2;
+		if ((max_sub >> 2) >= min_line) tg.span_prims++;
 		ref_note_prim((max_sub >> 2) - min_line + 1);
 
 		if (validation_cb)
@@ -1423,6 +1550,27 @@ struct rdp_cp
 		return r;
 	}
 
+	// VideoInterface::scanout_memory_range (video_interface.cpp:369-396): the bytes the fetch reads,
+	// from the registers with the per-scanline state cleared (as scanout leaves it).
+	void vi_memory_range(uint32_t &off, uint32_t &len)
+	{
+		RdpViLine tmp[RDP_VI_MAX_LINES];
+		const bool ended = vi.ended;
+		vi.ended = false;
+		const ViRegs m = vi_decode(tmp);
+		vi.ended = ended;
+		const bool dv = (m.status & (1u << 4)) != 0;
+		const int aw = m.max_x + 2 + 4 + int(dv) * 2, ah = m.max_y + 1 + 4;
+		if (m.vi_offset == 0 || m.h_res <= 0 || m.h_start >= 640)
+		{
+			off = len = 0;
+			return;
+		}
+		const int ps = (((m.status & 3u) | 2u) == 3u) ? 4 : 2;
+		off = uint32_t((m.vi_offset & ~(ps - 1)) + ((dv ? -3 : -2) - 2 * m.vi_width) * ps);
+		len = uint32_t((ah * m.vi_width + aw) * ps);
+	}
+
 	int vi_ensure(uint32_t **buf, size_t *cap, size_t words)
 	{
 		if (*cap >= words) return RDP_OK;
@@ -1459,7 +1607,7 @@ struct rdp_cp
 			if (check(rdp_vi_init_tables())) return sticky_error;
 			if (check(cudaMalloc(&vi.d_lines, sizeof(RdpViLine) * RDP_VI_MAX_LINES))) return RDP_ERR_OOM;
 			for (auto &b : vi.d_out)
-				if (check(cudaMalloc(&b, size_t(640) * 576 * 4))) return RDP_ERR_OOM;
+				if (check(cudaMalloc(&b, (size_t(640) * 576 * 4) << (2 * up_log2)))) return RDP_ERR_OOM;
 			vi.tables = true;
 		}
 		RdpViLine lines[RDP_VI_MAX_LINES];
@@ -1507,18 +1655,42 @@ struct rdp_cp
 		vi.last_valid_frame_count = vi.frame_count;
 		bool degenerate = r.h_res <= 0 || r.v_res <= 0;
 		bool is_8888 = (r.status & 3u) == 3u;
+		const int native_max_y = r.max_y;
+		// Upscaled scanout works in scaled pixels (video_interface.cpp:1299-1318).
+		const int S = 1 << up_log2;
+		if (up_log2)
+		{
+			r.h_start *= S;
+			r.h_start_clamp *= S;
+			r.v_start *= S;
+			r.h_res *= S;
+			r.h_res_clamp *= S;
+			r.v_res *= S;
+			r.max_x = r.max_x * S + (S - 1);
+			r.max_y = r.max_y * S + (S - 1);
+			for (RdpViLine &li : lines)
+			{
+				li.h_start *= S;
+				li.h_start_clamp *= S;
+				li.h_end_clamp *= S;
+				li.x_start *= S;
+				li.y_start *= S;
+				li.y_base *= S;
+			}
+		}
 
 		RdpViParams p = {};
-		p.rdram = d_rdram;
-		p.hidden = d_hidden;
+		p.rdram = up_log2 ? d_ms_rdram : d_rdram;
+		p.hidden = up_log2 ? d_ms_hidden : d_hidden;
 		p.rdram_size = rdram_size;
+		p.scale_log2 = int(up_log2);
 		p.fb_offset = is_8888 ? (r.vi_offset >> 2) : (r.vi_offset >> 1);
 		p.fb_width = r.vi_width;
 		p.is_8888 = is_8888;
 		p.fetch_aa = (r.status & (1u << 17)) != 0;
 		p.dither_filter = (r.status & (1u << 16)) != 0;
 		p.divot = divot;
-		p.fetch_bug = r.init_y_add < 1024;
+		p.fetch_bug = r.init_y_add < 1024 && !up_log2; // need_fetch_bug_emulation (video_interface.cpp:398-403)
 		p.degenerate = degenerate;
 		if (!degenerate)
 		{
@@ -1542,7 +1714,7 @@ struct rdp_cp
 		}
 
 		bool serrate = (r.status & (1u << 6)) != 0 && !o->upscale_deinterlacing;
-		int w = 640, h = (r.is_pal ? 576 : 480) >> int(!serrate);
+		int w = 640 * S, h = ((r.is_pal ? 576 : 480) >> int(!serrate)) * S;
 		unsigned cl, cr, ct, cb;
 		if (o->crop_rect_enable)
 		{
@@ -1556,6 +1728,10 @@ struct rdp_cp
 			cl = cr = cx;
 			ct = cb = cy;
 		}
+		cl *= unsigned(S);
+		cr *= unsigned(S);
+		ct *= unsigned(S);
+		cb *= unsigned(S);
 		if (cl + cr < unsigned(w) && ct + cb < unsigned(h))
 		{
 			w -= int(cl + cr);
@@ -1572,6 +1748,7 @@ struct rdp_cp
 		p.crop_top = int(ct);
 		p.v_start = r.v_start;
 		p.v_res = r.v_res;
+		p.info_y_shift = int(up_log2);
 		if (serrate)
 		{
 			p.v_start *= 2;
@@ -1579,7 +1756,7 @@ struct rdp_cp
 			p.serrate_shift = 1;
 			p.serrate_mask = 1;
 			p.serrate_select = int(r.v_current_line == 0);
-			p.info_y_shift = 1;
+			p.info_y_shift++;
 		}
 		p.h_start = r.h_start;
 		p.h_res = r.h_res;
@@ -1597,7 +1774,7 @@ struct rdp_cp
 			// The VI reads the framebuffer lines it scans: those pages come from the caller's RDRAM
 			// first (resolve_coherency_external, rdp_device.cpp:1103).
 			begin_page_list();
-			mark_read_range(r.vi_offset, uint64_t(std::max(r.vi_width, 1)) * uint64_t(std::max(r.max_y, 0) + 3) *
+			mark_read_range(r.vi_offset, uint64_t(std::max(r.vi_width, 1)) * uint64_t(std::max(native_max_y, 0) + 3) *
 			                                 (is_8888 ? 4u : 2u));
 			if (refresh_all) mark_read_range(0, rdram_size);
 			refresh_all = false;
@@ -1614,7 +1791,26 @@ struct rdp_cp
 		memcpy(vi.h_lines, lines, sizeof(lines));
 		if (check(cudaMemcpyAsync(vi.d_lines, vi.h_lines, sizeof(lines), cudaMemcpyHostToDevice, stream))) return sticky_error;
 		if (check(cudaEventRecord(vi.lines_copied, stream))) return sticky_error;
+		if (up_log2 && !degenerate)
+		{
+			// The fetch first brings the scanned range of the upscaled domain up to date with RDRAM
+			// (VideoInterface::vram_fetch_stage, video_interface.cpp:410-420).
+			uint32_t off, len;
+			vi_memory_range(off, len);
+			const RdpUpscaleDomain dom = up_domain();
+			if (check(rdp_upscale_sync(&dom, off, off, len, is_8888 ? 2u : 1u, 0, stream))) return sticky_error;
+		}
 		if (check(rdp_vi_launch(&p, stream))) return sticky_error;
+		// downscale_stage (video_interface.cpp:1000-1064): halve while the factor allows.
+		for (uint32_t steps = std::min(8u, o->downscale_steps), f = uint32_t(S); f > 1 && steps; f >>= 1, steps--)
+		{
+			if (vi_ensure(&vi.d_half, &vi.half_cap, size_t(w / 2) * size_t(h / 2)) != RDP_OK) return RDP_ERR_OOM;
+			if (check(rdp_vi_downscale(p.out, w, h, vi.d_half, stream))) return sticky_error;
+			w /= 2;
+			h /= 2;
+			if (check(cudaMemcpyAsync(p.out, vi.d_half, size_t(w) * h * 4, cudaMemcpyDeviceToDevice, stream)))
+				return sticky_error;
+		}
 		*img = p.out;
 		*width = uint32_t(w);
 		*height = uint32_t(h);
@@ -2052,7 +2248,11 @@ int rdp_cp_create(const rdp_create_info *info, rdp_cp **out)
 	if (!info || !out) return RDP_ERR_INVALID;
 	*out = nullptr;
 	size_t rs = info->rdram_size, hs = info->hidden_rdram_size;
-	if (!rs || (rs & (rs - 1)) || !hs || (hs & (hs - 1)) || rs > (64u << 20) || (info->flags & ~uint32_t(RDP_CREATE_COMMAND_THREAD)))
+	const uint32_t known = RDP_CREATE_COMMAND_THREAD | RDP_CREATE_UPSCALING_2X | RDP_CREATE_UPSCALING_4X |
+	                       RDP_CREATE_UPSCALING_8X | RDP_CREATE_SUPER_SAMPLED_READ_BACK | RDP_CREATE_SUPER_SAMPLED_DITHER;
+	const bool upscaling = (info->flags & (RDP_CREATE_UPSCALING_2X | RDP_CREATE_UPSCALING_4X | RDP_CREATE_UPSCALING_8X)) != 0;
+	if (!rs || (rs & (rs - 1)) || !hs || (hs & (hs - 1)) || rs > (64u << 20) || (info->flags & ~known) ||
+	    (upscaling && hs != rs / 2) || (!upscaling && (info->flags & RDP_CREATE_SUPER_SAMPLED_READ_BACK)))
 		return RDP_ERR_INVALID;
 	if (!rdp_device_is_supported(info->device)) return RDP_ERR_UNSUPPORTED;
 	rdp_cp *cp = new (std::nothrow) rdp_cp();
@@ -2203,6 +2403,28 @@ int rdp_cp_get_tmem(rdp_cp *cp, uint16_t *out)
 	int r = cp->idle();
 	if (r != RDP_OK) return r;
 	return cp->check(cudaMemcpy(out, cp->d_tmem, 4096, cudaMemcpyDeviceToHost));
+}
+
+uint32_t rdp_cp_get_scaling_factor(rdp_cp *cp) { return cp ? 1u << cp->up_log2 : 1u; }
+
+static int read_upscaled(rdp_cp *cp, const uint8_t *src, uint64_t total, void *dst, uint64_t offset, uint64_t size)
+{
+	if (!cp || !dst || !cp->up_log2 || offset > total || size > total - offset) return RDP_ERR_INVALID;
+	cudaSetDevice(cp->device);
+	cp->sync_ring();
+	int r = cp->idle();
+	if (r != RDP_OK) return r;
+	return cp->check(cudaMemcpy(dst, src + offset, size_t(size), cudaMemcpyDeviceToHost));
+}
+int rdp_cp_read_upscaled_rdram(rdp_cp *cp, void *dst, uint64_t offset, uint64_t size)
+{
+	return read_upscaled(cp, cp ? cp->d_ms_rdram : nullptr, cp ? uint64_t(cp->rdram_size) << (2 * cp->up_log2) : 0,
+	                     dst, offset, size);
+}
+int rdp_cp_read_upscaled_hidden_rdram(rdp_cp *cp, void *dst, uint64_t offset, uint64_t size)
+{
+	return read_upscaled(cp, cp ? cp->d_ms_hidden : nullptr, cp ? uint64_t(cp->hidden_size) << (2 * cp->up_log2) : 0,
+	                     dst, offset, size);
 }
 
 int rdp_cp_set_vi_register(rdp_cp *cp, uint32_t reg, uint32_t value)
@@ -2421,7 +2643,7 @@ static int build_graph(rdpx::Executor *exec, rdpx::CaptureSink &sink, rdp_stats 
 
 int rdp_cp_capture_begin(rdp_cp *cp)
 {
-	if (!cp || cp->capturing || cp->batch || cp->ring) return RDP_ERR_INVALID;
+	if (!cp || cp->capturing || cp->batch || cp->ring || cp->up_log2) return RDP_ERR_INVALID;
 	cudaSetDevice(cp->device);
 	int r = cp->hard_flush();
 	if (r != RDP_OK) return r;

@@ -783,7 +783,8 @@ struct Executor
 
 	// Launches the kernel chain once for the passes v[0..n) (distinct instances).
 	// With `cap`, the launch is recorded with device-resident inputs instead.
-	bool launch(const PassView *v, uint32_t n, CaptureSink *cap)
+	// `upscaled`: the views are upscaled passes (RdpPass.scale), rendered by k_raster_upscaled.
+	bool launch(const PassView *v, uint32_t n, CaptureSink *cap, bool upscaled = false)
 	{
 		if (!n || failed) return !failed;
 		ExecCaps need = caps;
@@ -936,9 +937,10 @@ struct Executor
 		L.prim_pairs = d_prim_pairs;
 		L.prim_offsets = d_prim_offsets;
 		L.prim_scan_blocks = d_prim_blocks;
+		L.upscaled = upscaled ? 1u : 0u;
 		int variant = current_variant();
 		bool sample = false;
-		if (tuner.active && shade_variant_choice(device) < 0 && !cap && tile_base &&
+		if (!upscaled && tuner.active && shade_variant_choice(device) < 0 && !cap && tile_base &&
 		    tuner.in_epoch < ShadeTuner::kMaxSamplesPerEpoch)
 		{
 			variant = int((tuner.in_epoch + uint32_t(tuner.epoch)) % RDP_SHADE_VARIANTS);
@@ -951,7 +953,7 @@ struct Executor
 		L.blend_kernel = blend_kernel;
 		L.pair_log = sample ? d_pair_log : nullptr;
 		L.log_slot = sample ? uint32_t(tuner.samples_taken++ % 256) : 0u;
-		if (!sample && !cap && launch_log && tile_base && launch_log_pending.size() < kLaunchLogSlots)
+		if (!upscaled && !sample && !cap && launch_log && tile_base && launch_log_pending.size() < kLaunchLogSlots)
 		{
 			L.pair_log = d_launch_pairs;
 			L.log_slot = uint32_t(launch_log_pending.size());
@@ -965,7 +967,7 @@ struct Executor
 		L.num_tile_items = tile_base;
 		L.tile_cycles = record_cycles ? d_tile_cycles : nullptr;
 		L.tile_order = nullptr;
-		if (sched_ready && (sched.order_enabled || sched.train_enabled))
+		if (!upscaled && sched_ready && (sched.order_enabled || sched.train_enabled))
 		{
 			sched.order = d_tile_order;
 			L.sched = &sched;

@@ -105,14 +105,15 @@ __device__ void put_rgb(uint8_t *o, uint32_t c)
 	o[2] = uint8_t(c >> 8);
 }
 
-// Conservative x range over one y sample (rdp_renderer.cpp:962-992).
-__device__ void interp_x64(const RdpPrimGeom &g, int y, bool flip, long long &xl, long long &xr)
+// Conservative x range over one y sample (rdp_renderer.cpp:962-992); y is a sub-scanline of the
+// image scaled by 2^sl.
+__device__ void interp_x64(const RdpPrimGeom &g, int y, bool flip, long long &xl, long long &xr, int sl = 0)
 {
-	long long yh_base = g.yh & ~3;
-	long long xh = (long long)g.xh + (long long)(y - yh_base) * g.dxhdy;
-	long long xm = (long long)g.xm + (long long)(y - yh_base) * g.dxmdy;
-	long long xlv = (long long)g.xl + (long long)(y - (long long)g.ym) * g.dxldy;
-	if (y < g.ym) xlv = xm;
+	long long yh_base = (long long)(g.yh & ~3) << sl, ym = (long long)g.ym << sl;
+	long long xh = ((long long)g.xh << sl) + (long long)(y - yh_base) * g.dxhdy;
+	long long xm = ((long long)g.xm << sl) + (long long)(y - yh_base) * g.dxmdy;
+	long long xlv = ((long long)g.xl << sl) + (long long)(y - ym) * g.dxldy;
+	if (y < ym) xlv = xm;
 	long long hs = xh >> 15, ls = xlv >> 15;
 	xl = flip ? hs : ls;
 	xr = flip ? ls : hs;
@@ -497,7 +498,11 @@ __global__ void k_prim_setup(const RdpPrimIn *__restrict__ in, uint32_t num_prim
 	g.span_ylo = ylo;
 	g.span_yhi = yhi;
 
-	// ---- conservative tile bounding box (rdp_renderer.cpp:994-1060)
+	// ---- conservative tile bounding box (rdp_renderer.cpp:994-1060), in the pass's pixels: for an
+	// upscaled pass the edges are evaluated at scaled sub-scanlines over every scaled row the
+	// primitive's lines cover (the binning test reaches S * yl - 1), with one scaled pixel of
+	// margin for the rounding of the scaled edge positions.
+	const int sl = int(pass.scale & 3u);
 	g.bbox[0] = 1; g.bbox[1] = 0; g.bbox[2] = 0; g.bbox[3] = 0;
 	if (g.yl > g.yh && yhi >= ylo)
 	{
@@ -508,23 +513,25 @@ __global__ void k_prim_setup(const RdpPrimIn *__restrict__ in, uint32_t num_prim
 		if (end_y >= start_y)
 		{
 			bool flip = (tflags & TRI_FLIP) != 0;
+			const int sy0 = start_y << sl, sy1 = ((end_y + 1) << sl) - 1, ym = g.ym << sl;
 			long long l0, r0, l1, r1, l2, r2, l3, r3;
-			interp_x64(g, start_y, flip, l0, r0);
-			interp_x64(g, end_y, flip, l1, r1);
+			interp_x64(g, sy0, flip, l0, r0, sl);
+			interp_x64(g, sy1, flip, l1, r1, sl);
 			l2 = l3 = l0; r2 = r3 = r0;
-			if (g.ym > start_y && g.ym < end_y)
+			if (ym > sy0 && ym < sy1)
 			{
-				interp_x64(g, g.ym, flip, l2, r2);
-				interp_x64(g, g.ym - 1, flip, l3, r3);
+				interp_x64(g, ym, flip, l2, r2, sl);
+				interp_x64(g, ym - 1, flip, l3, r3, sl);
 			}
 			long long sx = min(min(l0, l1), min(l2, l3));
 			long long ex = max(max(r0, r1), max(r2, r3));
 			long long mr = max(sx < 0 ? -sx : sx, ex < 0 ? -ex : ex);
-			if (mr > 2047) { sx = 0; ex = 0x7fffffff; }
-			sx = max(sx, (long long)(g.scissor[0] >> 2));
-			ex = min(ex, (long long)(((g.scissor[2] + 4) >> 2) - 1) + 1);
+			if (mr > (2047ll << sl)) { sx = 0; ex = 0x7fffffff; }
+			else if (sl) { sx -= 1; ex += 1; }
+			sx = max(sx, (long long)((g.scissor[0] >> 2) << sl));
+			ex = min(ex, (long long)(((g.scissor[2] + 4) >> 2) << sl));
 			ex = min(ex, (long long)pass.fb_width - 1);
-			int ty0 = start_y / 32, ty1 = min(end_y / 32, int(pass.tiles_y) - 1);
+			int ty0 = sy0 / 32, ty1 = min(sy1 / 32, int(pass.tiles_y) - 1);
 			if (ex >= sx && ty1 >= ty0)
 			{
 				g.bbox[0] = uint16_t(sx / 8);
@@ -556,17 +563,24 @@ struct __align__(16) SpanRow
 };
 static_assert(sizeof(SpanRow) == RDP_SPAN_ROW_BYTES, "span row layout");
 
-// Attribute half of span_setup.comp:99-150.
-__device__ void span_attr(const RdpPrimGeom &g, const RdpPrimAttr &a, int y, SpanRow &out)
+// interpolate_snapped (span_setup.comp:80-85): whole pixels step by the full derivative, the
+// sub-pixels of an upscaled pixel by the derivative over the factor (sl = log2 of the factor).
+__device__ __forceinline__ int interp_snapped(int d, int dy, int sl)
+{
+	return mulw(dy >> sl, d) + mulw(dy & ((1 << sl) - 1), d >> sl);
+}
+
+// Attribute half of span_setup.comp:99-150; y is a scanline of the image scaled by 2^sl.
+__device__ void span_attr(const RdpPrimGeom &g, const RdpPrimAttr &a, int y, SpanRow &out, int sl = 0)
 {
 	bool do_offset = (g.flags & TRI_DO_OFFSET) != 0;
 	bool skip_xfrac = (g.flags & TRI_SKIP_XFRAC) != 0;
-	int dy = y - (g.yh >> 2);
-	int xh = g.xh + mulw(dy, shlw(g.dxhdy, 2));
+	int dy = y - ((g.yh >> 2) << sl);
+	int xh = shlw(g.xh, sl) + mulw(dy, shlw(g.dxhdy, 2));
 	int drd[4] = { 0, 0, 0, 0 }, dsd[4] = { 0, 0, 0, 0 };
 	if (do_offset)
 	{
-		xh += mulw(3, g.dxhdy);
+		xh += mulw(3 << sl, g.dxhdy);
 #pragma unroll
 		for (int c = 0; c < 4; c++)
 		{
@@ -581,24 +595,25 @@ __device__ void span_attr(const RdpPrimGeom &g, const RdpPrimAttr &a, int y, Spa
 #pragma unroll
 	for (int c = 0; c < 4; c++)
 	{
-		int v = a.rgba[c] + mulw(dy, a.drgba_de[c]);
-		out.rgba[c] = ((v & ~0x1ff) + drd[c] - mulw(xfrac, (a.drgba_dx[c] >> 8) & ~1)) & ~0x3ff;
-		v = a.stzw[c] + mulw(dy, a.dstzw_de[c]);
-		out.stzw[c] = ((v & ~0x1ff) + dsd[c] - mulw(xfrac, (a.dstzw_dx[c] >> 8) & ~1)) & ~0x3ff;
+		int v = a.rgba[c] + interp_snapped(a.drgba_de[c], dy, sl);
+		out.rgba[c] = ((v & ~0x1ff) + drd[c] - interp_snapped((a.drgba_dx[c] >> 8) & ~1, xfrac, sl)) & ~0x3ff;
+		v = a.stzw[c] + interp_snapped(a.dstzw_de[c], dy, sl);
+		out.stzw[c] = ((v & ~0x1ff) + dsd[c] - interp_snapped((a.dstzw_dx[c] >> 8) & ~1, xfrac, sl)) & ~0x3ff;
 	}
 	out.base_x = xh >> 15;
 }
 
 __device__ __forceinline__ int quantize_x(int x) { return (x >> 12) | ((x & 0xfff) != 0 ? 1 : 0); }
 
-// Coverage half of span_setup.comp:152-225.
-__device__ void span_x(const RdpPrimGeom &g, int y, SpanRow &out)
+// Coverage half of span_setup.comp:152-225; y is a scanline of the image scaled by 2^sl.
+__device__ void span_x(const RdpPrimGeom &g, int y, SpanRow &out, int sl = 0)
 {
 	bool flip = (g.flags & TRI_FLIP) != 0;
-	int yh_base = g.yh & ~3;
-	int ylo = max(g.yh, g.scissor[1]);
-	int yhi = min(g.yl, g.scissor[3]);
-	int lo_sc = g.scissor[0] << 1, hi_sc = g.scissor[2] << 1;
+	int yh_base = (g.yh & ~3) << sl;
+	int ym_base = g.ym << sl;
+	int ylo = max(g.yh, g.scissor[1]) << sl;
+	int yhi = min(g.yl, g.scissor[3]) << sl;
+	int lo_sc = (g.scissor[0] << 1) << sl, hi_sc = (g.scissor[2] << 1) << sl;
 	bool all_over = true, all_under = true, all_invalid = true;
 	int mn = 0x7fffffff, mx = -0x7fffffff - 1;
 #pragma unroll
@@ -606,12 +621,12 @@ __device__ void span_x(const RdpPrimGeom &g, int y, SpanRow &out)
 	{
 		int ys = y * 4 + k;
 		bool clip_y = ys < ylo || ys >= yhi;
-		int xh = g.xh + mulw(ys - yh_base, g.dxhdy);
-		int xm = g.xm + mulw(ys - yh_base, g.dxmdy);
-		int xl = g.xl + mulw(ys - g.ym, g.dxldy);
-		if (ys < g.ym) xl = xm;
-		xl = bfe_s(xl, 27);
-		xh = bfe_s(xh, 27);
+		int xh = shlw(g.xh, sl) + mulw(ys - yh_base, g.dxhdy);
+		int xm = shlw(g.xm, sl) + mulw(ys - yh_base, g.dxmdy);
+		int xl = shlw(g.xl, sl) + mulw(ys - ym_base, g.dxldy);
+		if (ys < ym_base) xl = xm;
+		xl = bfe_s(xl, 27 + sl);
+		xh = bfe_s(xh, 27 + sl);
 		int hs = quantize_x(xh), ls = quantize_x(xl);
 		int l = flip ? hs : ls, r = flip ? ls : hs;
 		bool invalid = ((l >> 1) > (r >> 1)) || clip_y;
@@ -629,30 +644,31 @@ __device__ void span_x(const RdpPrimGeom &g, int y, SpanRow &out)
 	out.start_x = mn >> 3;
 	out.end_x = mx >> 3;
 	bool valid = !all_invalid && !all_over && !all_under;
-	if ((g.flags & TRI_INTERLACE_FIELD) && ((y & 1) != int((g.flags & TRI_INTERLACE_KEEP_ODD) != 0))) valid = false;
+	if ((g.flags & TRI_INTERLACE_FIELD) && (((y >> sl) & 1) != int((g.flags & TRI_INTERLACE_KEEP_ODD) != 0))) valid = false;
 	out.valid = valid ? 1 : 0;
 }
 
 // ============================================================================ k_bin
-// binning.h:58-144 at scaling 1.
-__device__ bool bin_primitive(const RdpPrimGeom &g, int lox, int loy, int hix, int hiy)
+// binning.h:58-144; lo/hi are pixels of the image scaled by 2^sl.
+__device__ bool bin_primitive(const RdpPrimGeom &g, int lox, int loy, int hix, int hiy, int sl = 0)
 {
-	loy = max(loy, g.scissor[1] >> 2);
-	hiy = min(hiy, ((g.scissor[3] + 3) >> 2) - 1);
-	int start_y = max(loy * 4, g.yh);
-	int end_y = min(hiy * 4 + 3, g.yl - 1);
+	loy = max(loy, (g.scissor[1] >> 2) << sl);
+	hiy = min(hiy, (((g.scissor[3] + 3) >> 2) << sl) - 1);
+	int start_y = max(loy * 4, g.yh << sl);
+	int end_y = min(hiy * 4 + 3, (g.yl << sl) - 1);
 	if (end_y < start_y) return false;
 	bool flip = (g.flags & TRI_FLIP) != 0;
-	int ys[4] = { start_y, end_y, clampi(g.ym - 1, start_y, end_y), clampi(g.ym, start_y, end_y) };
-	int yh_base = g.yh & ~3;
+	const int ym = g.ym << sl;
+	int ys[4] = { start_y, end_y, clampi(ym - 1, start_y, end_y), clampi(ym, start_y, end_y) };
+	const long long yh_base = (long long)((g.yh & ~3) << sl), ym_base = ym;
 	int xmin = 0x7fffffff, xmax = -0x7fffffff - 1, mr = 0;
 #pragma unroll
 	for (int k = 0; k < 4; k++)
 	{
-		long long xh = (long long)g.xh + (long long)(ys[k] - yh_base) * g.dxhdy;
-		long long xm = (long long)g.xm + (long long)(ys[k] - yh_base) * g.dxmdy;
-		long long xl = (long long)g.xl + (long long)(ys[k] - g.ym) * g.dxldy;
-		if (ys[k] < g.ym) xl = xm;
+		long long xh = (long long)shlw(g.xh, sl) + (long long)(ys[k] - yh_base) * g.dxhdy;
+		long long xm = (long long)shlw(g.xm, sl) + (long long)(ys[k] - yh_base) * g.dxmdy;
+		long long xl = (long long)shlw(g.xl, sl) + (long long)(ys[k] - ym_base) * g.dxldy;
+		if (ys[k] < ym) xl = xm;
 		xh = min(max(xh, -2147483648LL), 2147483647LL);
 		xl = min(max(xl, -2147483648LL), 2147483647LL);
 		int hs = int(xh) >> 15, ls = int(xl) >> 15;
@@ -662,10 +678,10 @@ __device__ bool bin_primitive(const RdpPrimGeom &g, int lox, int loy, int hix, i
 		mr = max(mr, max(abs(l), abs(r)));
 	}
 	int rx0, rx1;
-	if (mr <= 2047) { rx0 = xmin; rx1 = xmax; }
+	if (mr <= (2047 << sl)) { rx0 = xmin; rx1 = xmax; }
 	else { rx0 = 0; rx1 = 0x7fffffff; }
 	int x_bias = (g.flags & TRI_FILL_COPY_RASTER) ? 4 : 3;
-	int sx0 = g.scissor[0] >> 2, sx1 = ((g.scissor[2] + x_bias) >> 2) - 1;
+	int sx0 = (g.scissor[0] >> 2) << sl, sx1 = (((g.scissor[2] + x_bias) >> 2) << sl) - 1;
 	rx0 = clampi(rx0, sx0, sx1);
 	rx1 = clampi(rx1, sx0, sx1);
 	rx0 = max(rx0, lox);
@@ -694,6 +710,7 @@ __global__ void k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom, 
 	int tw = g.bbox[2] - g.bbox[0] + 1, th = g.bbox[3] - g.bbox[1] + 1;
 	int count = tw * th;
 	int fbw = int(pass.fb_width), fbh = int(pass.fb_height);
+	const int sl = int(pass.scale & 3u);
 	uint32_t binned = 0;
 	for (int t0 = 0; t0 < count; t0 += 32)
 	{
@@ -704,12 +721,13 @@ __global__ void k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom, 
 			int tx = g.bbox[0] + t % tw, ty = g.bbox[1] + t / tw;
 			int lox = tx * 8, loy = ty * 8;
 			int hix = min(lox + 7, fbw - 1), hiy = min(loy + 7, fbh - 1);
-			hit = bin_primitive(g, lox, loy, hix, hiy);
+			hit = bin_primitive(g, lox, loy, hix, hiy, sl);
 			if (hit)
 			{
 				uint32_t tl = uint32_t(ty) * pass.tiles_x + uint32_t(tx);
 				atomicOr(&pass.masks[size_t(tl) * RDP_MASK_WORDS_PER_TILE + word], bit);
-				atomicAdd(&tile_counts[pass.tile_item_begin + tl], 1u);
+				// Upscaled passes render from the bitmasks alone (no pair list).
+				if (!sl) atomicAdd(&tile_counts[pass.tile_item_begin + tl], 1u);
 			}
 		}
 		binned += __popc(__ballot_sync(0xffffffffu, hit));
@@ -2085,6 +2103,7 @@ struct PassConst
 {
 	int fb_size, dx_mask, dx_shift;
 	bool alias;
+	int sl = 0; // log2 of the upscaling factor: 0 for every pass but an upscaled one
 };
 
 // Output of the shading stage for one pixel and primitive (the reference's ShadedData,
@@ -2120,6 +2139,7 @@ __device__ __forceinline__ bool shade_pixel_v(const PassConst &pc, const RdpPrim
 	{
 		if (!(x >= sp.start_x && x <= sp.end_x)) return false;
 		int dxp = flip ? (x - sp.start_x) : (sp.end_x - x);
+		dxp >>= pc.sl; // upscaled copies repeat pixels (interpolation.h:60-61)
 		int s_offset = dxp - (dxp & pc.dx_mask);
 		int lerp_dx = (dxp >> pc.dx_shift) * (flip ? 1 : -1);
 		int s = (sp.stzw[0] + mulw(a.dstzw_dx[0] & ~0x1f, lerp_dx)) >> 16;
@@ -2177,14 +2197,15 @@ __device__ __forceinline__ bool shade_pixel_v(const PassConst &pc, const RdpPrim
 	int xoff = ((first & 1) << 1) + (yoff & 1);
 
 	// ---- interpolate_rgba (interpolation.h:30-51)
+	const int sl = pc.sl;
 	int shade[4];
 #pragma unroll
 	for (int c = 0; c < 4; c++)
 	{
-		int v = sp.rgba[c] + mulw(a.drgba_dx[c] & ~0x1f, dx);
-		int sn = shlw(v >> 14, 2);
+		int v = sp.rgba[c] + mulw((a.drgba_dx[c] & ~0x1f) >> sl, dx);
+		int sn = shlw(v >> 14, 2 + sl);
 		sn += xoff * (a.drgba_dx[c] >> 14) + yoff * (a.drgba_dy[c] >> 14);
-		sn >>= 4;
+		sn >>= 4 + sl;
 		shade[c] = clamp_9bit(sn);
 	}
 
@@ -2195,27 +2216,31 @@ __device__ __forceinline__ bool shade_pixel_v(const PassConst &pc, const RdpPrim
 	{
 		int sw[3], idx3[3] = { 0, 1, 3 };
 #pragma unroll
-		for (int k = 0; k < 3; k++) sw[k] = sp.stzw[idx3[k]] + mulw(a.dstzw_dx[idx3[k]] & ~0x1f, dx);
+		for (int k = 0; k < 3; k++) sw[k] = sp.stzw[idx3[k]] + mulw((a.dstzw_dx[idx3[k]] & ~0x1f) >> sl, dx);
 		if (F(RS_USES_TEXEL0) || F(RS_USES_TEXEL1) || F(RS_USES_PIPELINED_TEXEL1) || F(RS_USES_LOD))
 		{
 			st_div(sw[0] >> 16, sw[1] >> 16, sw[2] >> 16, perspective, s0, t0v, povf);
 			if (uses_lod)
 			{
+				// Upscaled: the LOD step in x covers one native pixel with native_texture_lod, and
+				// the y step scales the same way (interpolation.h:100-108, shading.h:193-196).
+				const int tdir = (sl && (g.flags & TRI_NATIVE_LOD)) ? (idir << sl) : idir;
+				const int ymul = sl ? abs(tdir) : 1;
 				int wx[3], wy[3];
 #pragma unroll
 				for (int k = 0; k < 3; k++)
 				{
-					wx[k] = sw[k] + mulw(idir, a.dstzw_dx[idx3[k]] & ~0x1f);
-					wy[k] = sw[k] + (a.dstzw_dy[idx3[k]] & ~0x7fff);
+					wx[k] = sw[k] + mulw(tdir, (a.dstzw_dx[idx3[k]] & ~0x1f) >> sl);
+					wy[k] = sw[k] + mulw(ymul, (a.dstzw_dy[idx3[k]] & ~0x7fff) >> sl);
 				}
 				st_div(wx[0] >> 16, wx[1] >> 16, wx[2] >> 16, perspective, sdx, tdx, povf);
 				st_div(wy[0] >> 16, wy[1] >> 16, wy[2] >> 16, perspective, sdy, tdy, povf);
 			}
 		}
-		z = sp.stzw[2] + mulw(a.dstzw_dx[2], dx);
-		int sz = shlw(z >> 10, 2);
+		z = sp.stzw[2] + mulw(a.dstzw_dx[2], dx >> sl) + mulw(a.dstzw_dx[2] >> sl, dx & ((1 << sl) - 1));
+		int sz = shlw(z >> 10, 2 + sl);
 		sz += xoff * (a.dstzw_dx[2] >> 10) + yoff * (a.dstzw_dy[2] >> 10);
-		sz >>= 5;
+		sz >>= 5 + sl;
 		z = clamp_z(sz);
 	}
 
@@ -2297,10 +2322,10 @@ __device__ __forceinline__ bool shade_pixel_v(const PassConst &pc, const RdpPrim
 		}
 		else
 		{
-			int ndx = dx + idir;
-			int ss = (sp.stzw[0] + mulw(a.dstzw_dx[0] & ~0x1f, ndx)) >> 16;
-			int tt = (sp.stzw[1] + mulw(a.dstzw_dx[1] & ~0x1f, ndx)) >> 16;
-			int ww = (sp.stzw[3] + mulw(a.dstzw_dx[3] & ~0x1f, ndx)) >> 16;
+			int ndx = dx + (idir << sl);
+			int ss = (sp.stzw[0] + mulw((a.dstzw_dx[0] & ~0x1f) >> sl, ndx)) >> 16;
+			int tt = (sp.stzw[1] + mulw((a.dstzw_dx[1] & ~0x1f) >> sl, ndx)) >> 16;
+			int ww = (sp.stzw[3] + mulw((a.dstzw_dx[3] & ~0x1f) >> sl, ndx)) >> 16;
 			bool dummy = false;
 			st_div(ss, tt, ww, perspective, s0, t0v, dummy);
 		}
@@ -3862,6 +3887,147 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const RdpPass *__rest
 	}
 }
 
+// ============================================================================ k_raster_upscaled
+// The upscaled pass (depth_blend.comp with SCALING_LOG2 > 0, rdp_renderer.cpp:2287-2342): one 8x8
+// tile of the scaled image per CTA, its binned primitives walked in order, shading and blending
+// fused as in k_raster.  Scanline y of the scaled image has its own span row (span_setup.comp
+// with the factor), computed per primitive for the warp's rows.  Pixel (x, y) reads and writes
+// sample slice (y % S) * S + x % S of the multisampled RDRAM at native pixel (x / S, y / S)
+// (memory_interfacing.h:286-362).  Primitives drawn at native resolution
+// (TRIANGLE_SETUP_DISABLE_UPSCALING_BIT) shade every pixel at the top-left sample of its native
+// pixel (shading.h:45-52).  With super-sampled readback each written pixel sets its native
+// pixel's colour / depth bits in the write mask (emit_scaled_write_masks, memory_interfacing.h:
+// 305-337), which the resolve reads.
+__device__ __forceinline__ void raster_tile_upscaled(uint32_t item, const RdpPass *__restrict__ passes,
+                                                     uint32_t num_passes, const RdpPrimGeom *__restrict__ geom,
+                                                     const RdpPrimAttr *__restrict__ attr,
+                                                     const RdpPrimShade *__restrict__ shade,
+                                                     const RdpTile *__restrict__ tilesets)
+{
+	__shared__ SpanRow s_sp[2][5];
+	const int wib = threadIdx.x >> 5;
+	const int lane = threadIdx.x & 31;
+
+	const uint32_t pi = pass_of_item(passes, num_passes, item);
+	const RdpPass &ps = passes[pi];
+	const uint32_t tile_linear = item - ps.tile_item_begin;
+	const int tx = int(tile_linear % ps.tiles_x), ty = int(tile_linear / ps.tiles_x);
+	uint32_t *masks = ps.masks + size_t(tile_linear) * RDP_MASK_WORDS_PER_TILE;
+	const uint32_t nwords = (ps.prim_count + 31) / 32;
+	const int sl = int(ps.scale & 3u), S = 1 << sl;
+
+	PassConst pc;
+	switch (ps.fb_fmt)
+	{
+	case FBF_I4: pc.fb_size = 0; pc.dx_mask = 0; pc.dx_shift = 0; break;
+	case FBF_I8: pc.fb_size = 1; pc.dx_mask = ~7; pc.dx_shift = 3; break;
+	case FBF_RGBA5551:
+	case FBF_IA88: pc.fb_size = 2; pc.dx_mask = ~3; pc.dx_shift = 2; break;
+	default: pc.fb_size = 4; pc.dx_mask = ~1; pc.dx_shift = 1; break;
+	}
+	pc.alias = ps.fb_addr == ps.depth_addr;
+	pc.sl = sl;
+	uint32_t addr_index;
+	switch (ps.fb_fmt)
+	{
+	case FBF_I4:
+	case FBF_I8: addr_index = ps.fb_addr; break;
+	case FBF_RGBA5551:
+	case FBF_IA88: addr_index = ps.fb_addr >> 1; break;
+	default: addr_index = ps.fb_addr >> 2; break;
+	}
+	const uint32_t depth_index = ps.depth_addr >> 1;
+
+	const int row0 = ty * 8 + wib * 4;
+	const int px_x = tx * 8 + (lane & 7);
+	const int px_y = row0 + (lane >> 3);
+	const bool inside = px_x < int(ps.fb_width) && px_y < int(ps.fb_height);
+	const uint32_t native_w = ps.fb_width >> sl;
+	const uint32_t xn = uint32_t(px_x) >> sl, yn = uint32_t(px_y) >> sl;
+	const uint32_t slice = ((uint32_t(px_y) & uint32_t(S - 1)) << sl) + (uint32_t(px_x) & uint32_t(S - 1));
+	const uint32_t ci = addr_index + native_w * yn + xn;
+	const uint32_t di = depth_index + native_w * yn + xn;
+	// This pixel's sample slice of the multisampled copies.
+	RdpPass sp = ps;
+	sp.rdram = ps.rdram + size_t(slice) * ps.rdram_size;
+	sp.hidden = ps.hidden + size_t(slice) * (ps.rdram_size >> 1);
+	sp.wmask = nullptr;
+
+	Pix px;
+	bool loaded = false;
+	for (uint32_t base = 0; base < nwords; base += 32)
+	{
+		uint32_t wi = base + lane;
+		uint32_t wv = wi < nwords ? masks[wi] : 0u;
+		unsigned nz = __ballot_sync(0xffffffffu, wv != 0);
+		while (nz)
+		{
+			int src = __ffs(nz) - 1;
+			nz &= nz - 1;
+			uint32_t bits = __shfl_sync(0xffffffffu, wv, src);
+			if (!loaded)
+			{
+				if (inside) load_pixel(sp, px, ci, di);
+				loaded = true;
+			}
+			while (bits)
+			{
+				int b = __ffs(bits) - 1;
+				bits &= bits - 1;
+				uint32_t prim = ps.prim_begin + (base + src) * 32 + b;
+				const RdpPrimGeom &g = geom[prim];
+				const int ylo = g.span_ylo << sl, yhi = (g.span_yhi << sl) + S - 1;
+				if (yhi < row0 || ylo > row0 + 3) continue; // no row of this warp is covered
+				const bool native_res = (g.flags & TRI_DISABLE_UPSCALING) != 0;
+				// Rows rb .. rb + 4 hold every (masked) row of the warp and the next row.
+				const int rb = native_res ? (row0 & ~(S - 1)) : row0;
+				if (lane < 5)
+					span_attr(g, attr[prim], rb + lane, s_sp[wib][lane], sl);
+				else if (lane >= 16 && lane < 21)
+					span_x(g, rb + (lane - 16), s_sp[wib][lane - 16], sl);
+				__syncwarp();
+				if (inside && px_y >= ylo && px_y <= yhi)
+				{
+					const int xs = native_res ? (px_x & ~(S - 1)) : px_x;
+					const int ys = native_res ? (px_y & ~(S - 1)) : px_y;
+					const RdpPrimShade &sh = shade[prim];
+					shade_and_blend(ps, pc, g, attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
+					                ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, s_sp[wib][ys - rb],
+					                s_sp[wib][ys - rb + 1], xs, ys, px);
+				}
+				__syncwarp();
+			}
+		}
+	}
+	if (loaded && inside)
+	{
+		store_pixel(sp, px, ci, di, pc.alias);
+		if (ps.scale & 0x100u)
+		{
+			const uint32_t word = (uint32_t(px.cdirty) + 2u * uint32_t(px.ddirty)) << (2 * ((xn & 3) + (yn & 3) * 4));
+			uint32_t *wm = reinterpret_cast<uint32_t *>(ps.rdram + (size_t(ps.rdram_size) << (2 * sl)));
+			if (word) atomicOr(wm + (yn >> 2) * ((native_w + 3) >> 2) + (xn >> 2), word);
+		}
+	}
+	// Clear the bitmask words this tile consumed for the next pass using the slot.
+	__syncthreads();
+	for (uint32_t wi = threadIdx.x; wi < nwords; wi += RASTER_THREADS) masks[wi] = 0u;
+}
+
+__global__ void __launch_bounds__(RASTER_THREADS) k_raster_upscaled(const RdpPass *__restrict__ passes,
+                                                                   uint32_t num_passes, uint32_t num_items,
+                                                                   const RdpPrimGeom *__restrict__ geom,
+                                                                   const RdpPrimAttr *__restrict__ attr,
+                                                                   const RdpPrimShade *__restrict__ shade,
+                                                                   const RdpTile *__restrict__ tilesets)
+{
+	for (uint32_t item = blockIdx.x; item < num_items; item += gridDim.x)
+	{
+		raster_tile_upscaled(item, passes, num_passes, geom, attr, shade, tilesets);
+		__syncthreads();
+	}
+}
+
 } // namespace rdp
 
 // ============================================================================ host launchers
@@ -3910,6 +4076,8 @@ static bool multi_cta_scan(const RdpLaunch *L)
 extern "C" uint32_t rdp_kernels_count(const RdpLaunch *L)
 {
 	uint32_t n = 0;
+	if (L->upscaled)
+		return (L->num_prims ? 2u : 0u) + (L->num_tmem_passes ? 2u : 0u) + (L->num_prims && L->num_tile_items ? 1u : 0u);
 	if (L->num_prims) n += 2;
 	if (L->num_prims && L->num_tile_items && L->spans) n += 1;
 	if (L->num_tmem_passes) n += 2;
@@ -3928,6 +4096,32 @@ extern "C" uint32_t rdp_kernels_count(const RdpLaunch *L)
 
 extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t stream)
 {
+	if (L->upscaled)
+	{
+		// Upscaled passes: set-up, binning at the scaled resolution, TMEM (super-sampled readback
+		// applies the pass's uploads here) and the fused per-tile kernel.
+		if (L->num_prims)
+		{
+			rdp::k_prim_setup<<<(L->num_prims + 127) / 128, 128, 0, stream>>>(L->prims_in, L->num_prims, L->words,
+			                                                                   L->state_blocks, L->passes,
+			                                                                   L->num_passes, L->geom, L->attr,
+			                                                                   L->shade, nullptr);
+			rdp::k_bin<<<(L->num_prims * 32 + 255) / 256, 256, 0, stream>>>(L->num_prims, L->geom, L->shade,
+			                                                                 L->passes, L->tile_counts, nullptr);
+		}
+		if (L->num_tmem_passes)
+		{
+			rdp::k_tmem_apply<<<dim3(L->max_uploads, L->num_tmem_passes), 256, 0, stream>>>(
+				L->passes, L->tmem_pass_list, L->uploads, L->tmem_keep);
+			rdp::k_tmem_carry<<<dim3(2048 / 32, L->num_tmem_passes), rdp::TMEM_CARRY_WARPS * 32, 0, stream>>>(
+				L->passes, L->tmem_pass_list, L->tmem_keep);
+		}
+		if (L->num_prims && L->num_tile_items)
+			rdp::k_raster_upscaled<<<std::min<uint32_t>(L->num_tile_items, L->blend_ctas), rdp::RASTER_THREADS, 0,
+			                         stream>>>(L->passes, L->num_passes, L->num_tile_items, L->geom, L->attr,
+			                                   L->shade, L->tilesets);
+		return cudaGetLastError();
+	}
 	const bool raster = L->num_prims && L->num_tile_items;
 	if (L->num_prims)
 	{

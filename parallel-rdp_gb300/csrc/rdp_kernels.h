@@ -72,6 +72,8 @@ typedef struct RdpLaunch
 	uint32_t *prim_rows;            /* [num_prims] first span row of each primitive */
 	uint32_t num_sms;               /* the device's SM count (sizes k_span's CTAs) */
 	uint2 *scratch;                 /* [pair_capacity * 64] shaded records, 8 bytes per pixel */
+	uint32_t upscaled;              /* the passes are upscaled passes (RdpPass.scale): set-up, binning, TMEM and
+	                                   k_raster_upscaled only */
 } RdpLaunch;
 
 #ifdef __cplusplus

@@ -212,7 +212,12 @@ typedef struct __attribute__((aligned(16))) RdpPass
 	uint32_t base_prim_index; /* primitives drawn by this instance before the pass (noise seed base) */
 	/* Offsets of the pass's command words, state blocks and tile sets in the launch's buffers
 	   (a primitive's word_offset / state_block / tileset are relative to its pass). */
-	uint32_t word_base, sb_base, ts_base, pad0;
+	uint32_t word_base, sb_base, ts_base;
+	/* Upscaled pass (the reference's render_pass_upscaled): bits 0-1 are log2 of the factor (0 for
+	   a 1x pass); rdram / hidden are then the multisampled copies (factor^2 slices of rdram_size /
+	   hidden_size bytes), fb_width / fb_height the scaled image.  Bit 8: record the super-sampled
+	   write mask (2 bits per native pixel, after the slices). */
+	uint32_t scale;
 	unsigned long long *counters; /* the instance's [0] fragments, [1] touched tiles, [2] tile instances */
 	uint32_t *wmask;              /* the instance's RDRAM write mask (1 bit per byte), or null */
 } RdpPass;

@@ -29,20 +29,27 @@ __device__ __forceinline__ uint32_t pack(uint32_t r, uint32_t g, uint32_t b, uin
 }
 __device__ __forceinline__ uint32_t ch(uint32_t c, int i) { return (c >> (8 * i)) & 0xff; }
 
-// extract_vram.comp: one framebuffer pixel with its 3-bit coverage.
+// extract_vram.comp: one framebuffer pixel with its 3-bit coverage; an upscaled pixel reads its
+// sample slice (extract_vram.comp:58-67).
 __device__ uint32_t fetch_vram(const RdpViParams &p, int cx, int cy)
 {
+	const int sl = p.scale_log2, m = (1 << sl) - 1;
+	const int slice = ((cy & m) << sl) + (cx & m);
+	cx >>= sl;
+	cy >>= sl;
 	int lin = cy * p.fb_width + cx + p.fb_offset;
 	uint32_t r, g, b, a;
 	if (p.is_8888)
 	{
 		lin &= int((p.rdram_size >> 2) - 1);
+		lin += slice * int(p.rdram_size >> 2);
 		uint32_t w = *reinterpret_cast<const uint32_t *>(p.rdram + size_t(lin) * 4);
 		r = (w >> 24) & 0xff; g = (w >> 16) & 0xff; b = (w >> 8) & 0xff; a = (w >> 5) & 7;
 	}
 	else
 	{
 		lin &= int((p.rdram_size >> 1) - 1);
+		lin += slice * int(p.rdram_size >> 1);
 		uint32_t w = *reinterpret_cast<const uint16_t *>(p.rdram + size_t(lin ^ 1) * 2);
 		uint32_t hw = p.hidden[lin];
 		r = (w >> 8) & 0xf8; g = (w >> 3) & 0xf8; b = (w << 2) & 0xf8; a = ((w & 1) << 2) | hw;
@@ -314,6 +321,28 @@ extern "C" cudaError_t rdp_vi_init_tables(void)
 	for (int i = 0; i < 256; i++) g[i] = uint8_t(isq(i * 256) & ~1);
 	for (int i = 0; i < 256 * 64; i++) g[256 + i] = uint8_t(isq(i * 4) & ~1);
 	return cudaMemcpyToSymbol(rdpvi::g_gamma, g, sizeof(g));
+}
+
+namespace rdpvi {
+__global__ void k_vi_half(const uint32_t *__restrict__ src, int w, uint32_t *__restrict__ dst, int hw, int hh)
+{
+	const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+	if (x >= hw || y >= hh) return;
+	const uint32_t a = src[size_t(2 * y) * w + 2 * x], b = src[size_t(2 * y) * w + 2 * x + 1];
+	const uint32_t c = src[size_t(2 * y + 1) * w + 2 * x], d = src[size_t(2 * y + 1) * w + 2 * x + 1];
+	uint32_t o = 0;
+#pragma unroll
+	for (int i = 0; i < 4; i++) o |= ((ch(a, i) + ch(b, i) + ch(c, i) + ch(d, i) + 2) >> 2) << (8 * i);
+	dst[size_t(y) * hw + x] = o;
+}
+} // namespace rdpvi
+
+extern "C" cudaError_t rdp_vi_downscale(const uint32_t *src, int32_t w, int32_t h, uint32_t *dst, cudaStream_t stream)
+{
+	const int hw = w / 2, hh = h / 2;
+	if (hw <= 0 || hh <= 0) return cudaSuccess;
+	rdpvi::k_vi_half<<<dim3((hw + 15) / 16, (hh + 7) / 8), dim3(16, 8), 0, stream>>>(src, w, dst, hw, hh);
+	return cudaGetLastError();
 }
 
 extern "C" cudaError_t rdp_vi_launch(const RdpViParams *p, cudaStream_t stream)

@@ -50,6 +50,9 @@ typedef struct RdpViParams
 	uint32_t frame_count;
 	int32_t scale_aa, gamma, gamma_dither;
 	int32_t blend_prev;
+	// Upscaling: log2 of the factor.  rdram / hidden are then the multisampled copies (factor^2
+	// slices of rdram_size / rdram_size / 2 bytes) and the images are in scaled pixels.
+	int32_t scale_log2;
 } RdpViParams;
 
 #ifdef __cplusplus
@@ -57,6 +60,9 @@ extern "C" {
 #endif
 cudaError_t rdp_vi_init_tables(void);
 cudaError_t rdp_vi_launch(const RdpViParams *p, cudaStream_t stream);
+/* One step of downscale_stage (video_interface.cpp:1000-1064): dst (w / 2 x h / 2) = the 2x2 means
+ * of src (w x h), rounded half up. */
+cudaError_t rdp_vi_downscale(const uint32_t *src, int32_t w, int32_t h, uint32_t *dst, cudaStream_t stream);
 #ifdef __cplusplus
 }
 #endif

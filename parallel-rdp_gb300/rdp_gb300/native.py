@@ -98,6 +98,7 @@ EXPORTED_SYMBOLS = [
     "rdp_serve_run", "rdp_batch_enqueue_many", "rdp_dump_writer_open", "rdp_dump_writer_flush_rdram",
     "rdp_dump_writer_flush_hidden_rdram", "rdp_dump_writer_command", "rdp_dump_writer_set_vi_register",
     "rdp_dump_writer_end_frame", "rdp_dump_writer_signal_complete", "rdp_dump_writer_close", "rdp_dump_replay",
+    "rdp_cp_get_scaling_factor", "rdp_cp_read_upscaled_rdram", "rdp_cp_read_upscaled_hidden_rdram",
 ]
 
 
@@ -130,6 +131,12 @@ class _BatchStats(ctypes.Structure):
 
 
 CREATE_COMMAND_THREAD = 1 << 0
+CREATE_UPSCALING_2X = 1 << 2
+CREATE_UPSCALING_4X = 1 << 3
+CREATE_UPSCALING_8X = 1 << 4
+CREATE_SUPER_SAMPLED_READ_BACK = 1 << 5
+CREATE_SUPER_SAMPLED_DITHER = 1 << 6
+_UPSCALING_FLAGS = {1: 0, 2: CREATE_UPSCALING_2X, 4: CREATE_UPSCALING_4X, 8: CREATE_UPSCALING_8X}
 BATCH_TILE_ORDER_LEARNED = 1 << 0
 BATCH_RECORD_TILE_CYCLES = 1 << 1
 
@@ -172,6 +179,10 @@ def lib():
     L.rdp_cp_get_hidden_rdram_size.argtypes = [vp]
     L.rdp_cp_get_hidden_rdram_size.restype = sz
     L.rdp_cp_get_tmem.argtypes = [vp, vp]
+    L.rdp_cp_get_scaling_factor.argtypes = [vp]
+    L.rdp_cp_get_scaling_factor.restype = u32
+    for n in ("rdp_cp_read_upscaled_rdram", "rdp_cp_read_upscaled_hidden_rdram"):
+        getattr(L, n).argtypes = [vp, vp, u64, u64]
     L.rdp_cp_set_vi_register.argtypes = [vp, u32, u32]
     L.rdp_cp_scanout_sync.argtypes = [vp, ctypes.POINTER(ScanoutOptions), vp, ctypes.POINTER(u32),
                                       ctypes.POINTER(u32)]
@@ -290,7 +301,9 @@ class CommandProcessor:
     """
 
     def __init__(self, rdram=None, rdram_size=8 << 20, hidden_rdram_size=None, device=0, batch=None,
-                 command_thread=False):
+                 command_thread=False, upscaling=1, super_sampled_readback=False, super_sampled_dither=False):
+        """upscaling: internal upscaling factor 1, 2, 4 or 8 (COMMAND_PROCESSOR_FLAG_UPSCALING_*_BIT);
+        super_sampled_readback / super_sampled_dither: resolve the scaled rendering into RDRAM."""
         if hidden_rdram_size is None:
             hidden_rdram_size = rdram_size // 2
         if rdram is None:
@@ -298,8 +311,12 @@ class CommandProcessor:
         assert rdram.dtype == np.uint8 and rdram.flags["C_CONTIGUOUS"] and rdram.size >= rdram_size
         self._rdram = rdram
         self._batch = batch
-        info = _CreateInfo(rdram.ctypes.data, 0, rdram_size, hidden_rdram_size,
-                           CREATE_COMMAND_THREAD if command_thread else 0, device)
+        if upscaling not in _UPSCALING_FLAGS:
+            raise ValueError("upscaling must be 1, 2, 4 or 8")
+        flags = (CREATE_COMMAND_THREAD if command_thread else 0) | _UPSCALING_FLAGS[upscaling]
+        flags |= (CREATE_SUPER_SAMPLED_READ_BACK if super_sampled_readback else 0)
+        flags |= (CREATE_SUPER_SAMPLED_DITHER if super_sampled_dither else 0)
+        info = _CreateInfo(rdram.ctypes.data, 0, rdram_size, hidden_rdram_size, flags, device)
         h = ctypes.c_void_p()
         if batch is None:
             _check(lib().rdp_cp_create(ctypes.byref(info), ctypes.byref(h)), "rdp_cp_create")
@@ -381,6 +398,24 @@ class CommandProcessor:
         _check(lib().rdp_cp_get_tmem(self._h, out.ctypes.data), "get_tmem")
         return out
 
+    # -- internal upscaling -------------------------------------------------
+    def get_scaling_factor(self):
+        return lib().rdp_cp_get_scaling_factor(self._h)
+
+    def upscaled_rdram(self):
+        """The multisampled RDRAM: factor^2 slices of RDRAM, slice (y % f) * f + x % f."""
+        f = self.get_scaling_factor()
+        out = np.zeros(self.rdram_size * f * f, dtype=np.uint8)
+        _check(lib().rdp_cp_read_upscaled_rdram(self._h, out.ctypes.data, 0, out.size), "read_upscaled_rdram")
+        return out
+
+    def upscaled_hidden_rdram(self):
+        f = self.get_scaling_factor()
+        out = np.zeros(self.hidden_rdram_size * f * f, dtype=np.uint8)
+        _check(lib().rdp_cp_read_upscaled_hidden_rdram(self._h, out.ctypes.data, 0, out.size),
+               "read_upscaled_hidden_rdram")
+        return out
+
     # -- video interface ----------------------------------------------------
     def set_vi_register(self, reg, value):
         _check(lib().rdp_cp_set_vi_register(self._h, int(reg), value & 0xffffffff), "set_vi_register")
@@ -388,7 +423,8 @@ class CommandProcessor:
     def scanout_sync(self, options=None, **kw):
         """Returns the RGBA8 scanout as uint32[h, w] (r | g << 8 | b << 16 | a << 24), or None."""
         opts = options if options is not None else ScanoutOptions(**kw)
-        buf = np.zeros(640 * 576, dtype=np.uint32)
+        f = self.get_scaling_factor()
+        buf = np.zeros(640 * 576 * f * f, dtype=np.uint32)
         w, h = ctypes.c_uint32(), ctypes.c_uint32()
         _check(lib().rdp_cp_scanout_sync(self._h, ctypes.byref(opts), buf.ctypes.data, ctypes.byref(w),
                                          ctypes.byref(h)), "scanout_sync")

@@ -186,8 +186,9 @@ int main(int argc, char **argv)
 	// --------------------------------------------------------------------- unsupported configuration
 	{
 		std::vector<uint8_t> rdram(1 << 20);
+		// Super-sampled readback without an upscaling factor (Renderer::init_renderer refuses it).
 		RDP::CommandProcessor cp(0, rdram.data(), 0, rdram.size(), rdram.size() / 2,
-		                         RDP::COMMAND_PROCESSOR_FLAG_UPSCALING_2X_BIT);
+		                         RDP::COMMAND_PROCESSOR_FLAG_SUPER_SAMPLED_READ_BACK_BIT);
 		CHECK(!cp.device_is_supported());
 		cp.enqueue_command(1, words); // no effect, no crash
 		CHECK(cp.signal_timeline() == 0 && cp.begin_read_rdram() == nullptr);

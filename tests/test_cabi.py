@@ -72,3 +72,20 @@ def test_cpp_facade_header_compiles():
     subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
                     "-I", os.path.join(cuda, "include"), os.path.join(ROOT, "tests", "cpp", "facade_test.cpp")],
                    check=True)
+
+
+def test_create_rejects_inconsistent_upscaling_flags():
+    """rdp_cp_create checks its flags before touching a device: super-sampled readback needs an
+    upscaling factor (Renderer::init_renderer, rdp_renderer.cpp:59-60), and upscaling needs hidden
+    RDRAM of half the RDRAM size (the multisampled slices are addressed that way)."""
+    lib = native.lib()
+    rd = (ctypes.c_uint8 * (1 << 20))()
+    cases = [(native.CREATE_SUPER_SAMPLED_READ_BACK, 1 << 19),
+             (native.CREATE_UPSCALING_2X, 1 << 18),
+             (native.CREATE_UPSCALING_4X | native.CREATE_SUPER_SAMPLED_READ_BACK, 1 << 20),
+             (1 << 9, 1 << 19)]
+    for flags, hidden in cases:
+        info = native._CreateInfo(ctypes.addressof(rd), 0, 1 << 20, hidden, flags, 0)
+        h = ctypes.c_void_p()
+        assert lib.rdp_cp_create(ctypes.byref(info), ctypes.byref(h)) == native.RDP_ERR_INVALID, hex(flags)
+        assert not h.value

@@ -47,7 +47,7 @@ namespace {
 
 constexpr uint32_t kMaxWordsPerPass = RDP_MAX_PRIMS_PER_PASS * 44;
 constexpr uint32_t kMaxStateBlocks = RDP_MAX_PRIMS_PER_PASS;
-constexpr uint32_t kMaxTilesets = 4096;
+constexpr uint32_t kMaxTilesets = 32768;
 constexpr uint32_t kMaxTiles = RDP_MAX_TILES_X * RDP_MAX_TILES_Y;
 
 
@@ -568,6 +568,7 @@ struct rdp_cp
 			rdpx::ExecCaps c;
 			c.passes = 1;
 			c.prims = RDP_MAX_PRIMS_PER_PASS;
+			c.uploads = RDP_MAX_UPLOADS_PER_PASS;
 			c.tile_items = kMaxTiles;
 			c.staging = rdpx::align16(sizeof(RdpPass)) + rdpx::align16(sizeof(RdpPrimIn) * RDP_MAX_PRIMS_PER_PASS) +
 			            rdpx::align16(sizeof(uint32_t) * kMaxWordsPerPass) +
@@ -2214,17 +2215,19 @@ bool rdp_batch::reserve_for_capture()
 	for (size_t r = 0; r < depth; r++)
 	{
 		views.clear();
-		uint32_t prims = 0, tiles = 0;
+		uint32_t prims = 0, tiles = 0, uploads = 0;
 		for (rdp_cp *cp : instances)
 			if (r < cp->deferred.size())
 			{
 				views.push_back(cp->deferred[r].view());
 				prims += views.back().num_prims;
+				uploads += views.back().num_uploads;
 				for (uint32_t t = 0; t < views.back().num_targets; t++)
 					tiles += views.back().target[t].tiles_x * views.back().target[t].tiles_y;
 			}
 		need.passes = std::max(need.passes, uint32_t(views.size()));
 		need.prims = std::max(need.prims, prims);
+		need.uploads = std::max(need.uploads, uploads);
 		need.tile_items = std::max(need.tile_items, tiles);
 		need.staging = std::max(need.staging, rdpx::Executor::staging_bytes_for(views.data(), uint32_t(views.size())));
 	}

@@ -180,7 +180,7 @@ struct PassPacket
 
 struct ExecCaps
 {
-	uint32_t passes = 0, descs = 0, prims = 0, tile_items = 0, pairs = 0, span_rows = 0;
+	uint32_t passes = 0, descs = 0, prims = 0, tile_items = 0, pairs = 0, span_rows = 0, uploads = 0;
 	size_t staging = 0;
 };
 
@@ -276,6 +276,7 @@ struct Executor
 	// Pair-scratch and span-row capacities a new executor starts with (RDP_PAIR_CAPACITY and
 	// RDP_SPAN_ROW_CAPACITY override them; launches beyond them take the fused fallback).
 	uint32_t initial_pairs = 1u << 20, initial_span_rows = kInitialSpanRows;
+	bool fused_only = false; // RDP_RASTER_PATH=fused: the pair scratch never grows
 	uint32_t *d_queues = nullptr, num_queues = 0; // per-SM work queues of k_shade + used-up bitmask
 	size_t queue_bytes() const { return (size_t(num_queues) + (num_queues + 31) / 32) * 4; }
 
@@ -466,6 +467,15 @@ struct Executor
 		if (const char *e = getenv("RDP_PAIR_CAPACITY")) initial_pairs = std::max(1u, uint32_t(strtoul(e, nullptr, 10)));
 		if (const char *e = getenv("RDP_SPAN_ROW_CAPACITY"))
 			initial_span_rows = std::max(1u, uint32_t(strtoul(e, nullptr, 10)));
+		// RDP_RASTER_PATH=fused: every launch takes the fused per-tile kernel (k_raster: shading and
+		// blending in one CTA per tile) instead of the pair path, for comparing the two designs.
+		if (const char *e = getenv("RDP_RASTER_PATH"))
+			if (!strcmp(e, "fused"))
+			{
+				fused_only = true;
+				initial_pairs = 1;
+				initial_span_rows = 1;
+			}
 		if (const char *e = getenv("RDP_LAUNCH_LOG"))
 		{
 			launch_log = fopen(e, "a");
@@ -647,7 +657,9 @@ struct Executor
 		bool grow_prims = need.prims > caps.prims, grow_tiles = need.tile_items > caps.tile_items;
 		bool grow_passes = need.passes > caps.passes, grow_pairs = need.pairs > caps.pairs;
 		bool grow_staging = need.staging > caps.staging, grow_spans = need.span_rows > caps.span_rows;
-		if (!(grow_prims || grow_tiles || grow_passes || grow_pairs || grow_staging || grow_spans)) return true;
+		bool grow_uploads = need.uploads > caps.uploads;
+		if (!(grow_prims || grow_tiles || grow_passes || grow_pairs || grow_staging || grow_spans || grow_uploads))
+			return true;
 		if (check(cudaStreamSynchronize(stream)) || (copy_stream && check(cudaStreamSynchronize(copy_stream))))
 			return false;
 		for (auto &st : staging) st.in_flight = false;
@@ -698,13 +710,14 @@ struct Executor
 			caps.tile_items = n;
 			if (!sched_buffers(n)) return false;
 		}
-		if (grow_passes)
+		if (grow_passes) caps.passes = std::max(need.passes, caps.passes * 2);
+		if (grow_uploads)
 		{
-			uint32_t n = std::max(need.passes, caps.passes * 2);
+			uint32_t n = std::max(need.uploads, caps.uploads + caps.uploads / 2);
 			cudaFree(d_tmem_keep);
 			d_tmem_keep = nullptr;
-			if (check(cudaMalloc(&d_tmem_keep, size_t(n) * RDP_MAX_UPLOADS_PER_PASS * 64 * 4))) return false;
-			caps.passes = n;
+			if (check(cudaMalloc(&d_tmem_keep, size_t(n) * 64 * 4))) return false;
+			caps.uploads = n;
 		}
 		if (grow_pairs)
 		{
@@ -754,6 +767,7 @@ struct Executor
 	// launch has needed, so that later launches take the pair path instead of the fused fallback.
 	bool adapt_pairs()
 	{
+		if (fused_only) return true;
 		uint32_t seen[6] = { 0, 0, 0, 0, 0, 0 };
 		if (check(cudaMemcpy(seen, d_ctrl, sizeof(seen), cudaMemcpyDeviceToHost))) return false;
 		if (seen[2] <= caps.pairs && seen[5] <= caps.span_rows) return true;
@@ -788,16 +802,18 @@ struct Executor
 	{
 		if (!n || failed) return !failed;
 		ExecCaps need = caps;
-		uint32_t prims = 0, tiles = 0, descs = 0;
+		uint32_t prims = 0, tiles = 0, descs = 0, uploads = 0;
 		for (uint32_t i = 0; i < n; i++)
 		{
 			prims += v[i].num_prims;
+			uploads += v[i].num_uploads;
 			descs += v[i].num_targets;
 			for (uint32_t t = 0; t < v[i].num_targets; t++) tiles += v[i].target[t].tiles_x * v[i].target[t].tiles_y;
 		}
 		need.passes = std::max(need.passes, n);
 		need.descs = std::max(need.descs, descs);
 		need.prims = std::max(need.prims, std::max(prims, 1u));
+		need.uploads = std::max(need.uploads, std::max(uploads, 1u));
 		need.tile_items = std::max(need.tile_items, std::max(tiles, 1u));
 		need.pairs = std::max(need.pairs, initial_pairs);
 		need.span_rows = std::max(need.span_rows, initial_span_rows);
@@ -917,6 +933,7 @@ struct Executor
 		L.num_tmem_passes = num_tmem;
 		L.uploads = reinterpret_cast<const RdpUpload *>(dst + o_up);
 		L.max_uploads = max_uploads;
+		L.num_uploads = up_base;
 		L.tmem_keep = d_tmem_keep;
 		L.tile_counts = d_tile_counts;
 		L.nonempty_tiles = d_nonempty;

@@ -1103,16 +1103,27 @@ __device__ bool tmem_lut(const RdpPass &ps, const RdpUpload &info, int tmem16_in
 }
 
 // Phase 1: every (upload, TMEM word) pair independently -- does upload u write word w, and with
-// what value?  Written values land in snapshot u+1; unwritten words are marked in a bitmask.
+// what value?  Written values land in snapshot u+1; unwritten words are marked in a bitmask.  One
+// CTA per upload of the launch (the launch's uploads are the TMEM passes' uploads, concatenated in
+// pass order); the CTA finds its pass by binary search over their first uploads.
 __global__ void k_tmem_apply(const RdpPass *__restrict__ passes, const uint32_t *__restrict__ pass_list,
-                             const RdpUpload *__restrict__ uploads, uint32_t *__restrict__ keep_bits)
+                             uint32_t num_tmem_passes, const RdpUpload *__restrict__ uploads,
+                             uint32_t *__restrict__ keep_bits)
 {
-	const RdpPass &ps = passes[pass_list[blockIdx.y]];
-	uint32_t u = blockIdx.x;
-	if (u >= ps.upload_count) return;
-	RdpUpload info = uploads[ps.upload_begin + u];
+	const uint32_t g = blockIdx.x;
+	uint32_t lo = 0, hi = num_tmem_passes;
+	while (hi - lo > 1)
+	{
+		const uint32_t mid = (lo + hi) >> 1;
+		if (passes[pass_list[mid]].upload_begin <= g) lo = mid;
+		else hi = mid;
+	}
+	const RdpPass &ps = passes[pass_list[lo]];
+	const uint32_t u = g - ps.upload_begin;
+	if (g < ps.upload_begin || u >= ps.upload_count) return;
+	RdpUpload info = uploads[g];
 	uint16_t *dst = ps.tmem_snapshots + size_t(u + 1) * 2048;
-	uint32_t *keep = keep_bits + (size_t(blockIdx.y) * RDP_MAX_UPLOADS_PER_PASS + u) * 64;
+	uint32_t *keep = keep_bits + size_t(g) * 64;
 	for (int gid = threadIdx.x; gid < 2048; gid += blockDim.x)
 	{
 		int idx = gid ^ 1;
@@ -1153,7 +1164,7 @@ __global__ void __launch_bounds__(TMEM_CARRY_WARPS * 32) k_tmem_carry(const RdpP
 	const uint32_t chunk = (n + TMEM_CARRY_WARPS - 1) / TMEM_CARRY_WARPS;
 	const uint32_t u0 = min(n, uint32_t(warp) * chunk), u1 = min(n, u0 + chunk);
 	uint16_t *snap = ps.tmem_snapshots;
-	const uint32_t *keep = keep_bits + size_t(blockIdx.y) * RDP_MAX_UPLOADS_PER_PASS * 64 + (gid >> 5);
+	const uint32_t *keep = keep_bits + size_t(ps.upload_begin) * 64 + (gid >> 5);
 	const uint32_t bit = 1u << (gid & 31);
 
 	uint16_t last = 0;
@@ -4111,8 +4122,8 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		}
 		if (L->num_tmem_passes)
 		{
-			rdp::k_tmem_apply<<<dim3(L->max_uploads, L->num_tmem_passes), 256, 0, stream>>>(
-				L->passes, L->tmem_pass_list, L->uploads, L->tmem_keep);
+			rdp::k_tmem_apply<<<L->num_uploads, 256, 0, stream>>>(L->passes, L->tmem_pass_list, L->num_tmem_passes,
+			                                                      L->uploads, L->tmem_keep);
 			rdp::k_tmem_carry<<<dim3(2048 / 32, L->num_tmem_passes), rdp::TMEM_CARRY_WARPS * 32, 0, stream>>>(
 				L->passes, L->tmem_pass_list, L->tmem_keep);
 		}
@@ -4148,8 +4159,8 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 	}
 	if (L->num_tmem_passes)
 	{
-		rdp::k_tmem_apply<<<dim3(L->max_uploads, L->num_tmem_passes), 256, 0, stream>>>(L->passes, L->tmem_pass_list,
-		                                                                                 L->uploads, L->tmem_keep);
+		rdp::k_tmem_apply<<<L->num_uploads, 256, 0, stream>>>(L->passes, L->tmem_pass_list, L->num_tmem_passes,
+		                                                      L->uploads, L->tmem_keep);
 		rdp::k_tmem_carry<<<dim3(2048 / 32, L->num_tmem_passes), rdp::TMEM_CARRY_WARPS * 32, 0, stream>>>(
 			L->passes, L->tmem_pass_list, L->tmem_keep);
 	}

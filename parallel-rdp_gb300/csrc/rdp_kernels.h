@@ -35,7 +35,8 @@ typedef struct RdpLaunch
 	uint32_t num_tmem_passes;
 	const RdpUpload *uploads;
 	uint32_t max_uploads;     /* largest upload count of the TMEM passes */
-	uint32_t *tmem_keep;      /* [num_tmem_passes][RDP_MAX_UPLOADS_PER_PASS][64] scratch bitmask */
+	uint32_t num_uploads;     /* uploads of the launch (all TMEM passes' uploads, concatenated) */
+	uint32_t *tmem_keep;      /* [num_uploads][64] scratch bitmask */
 	uint32_t num_tile_items;
 	cudaEvent_t shade_events[2];    /* optional: recorded around the k_shade launch */
 	cudaEvent_t blend_events[2];    /* optional: recorded around the k_blend launch */

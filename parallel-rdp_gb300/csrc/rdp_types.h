@@ -22,10 +22,10 @@
 
 #define RDP_TILE_W 8
 #define RDP_TILE_H 8
-#define RDP_MAX_PRIMS_PER_PASS 16384
+#define RDP_MAX_PRIMS_PER_PASS 65536
 #define RDP_MASK_WORDS_PER_TILE (RDP_MAX_PRIMS_PER_PASS / 32)
 #define RDP_COARSE_WORDS_PER_TILE (RDP_MAX_PRIMS_PER_PASS / 1024)
-#define RDP_MAX_UPLOADS_PER_PASS 4096
+#define RDP_MAX_UPLOADS_PER_PASS 16384
 #define RDP_MAX_TILES_X 128
 #define RDP_MAX_TILES_Y 128
 #define RDP_STATE_BLOCK_WORDS 32

@@ -181,6 +181,7 @@ struct PassPacket
 struct ExecCaps
 {
 	uint32_t passes = 0, descs = 0, prims = 0, tile_items = 0, pairs = 0, span_rows = 0, uploads = 0;
+	size_t mask_words = 0; // tiles x each pass's bitmask words, summed over a launch
 	size_t staging = 0;
 };
 
@@ -657,8 +658,9 @@ struct Executor
 		bool grow_prims = need.prims > caps.prims, grow_tiles = need.tile_items > caps.tile_items;
 		bool grow_passes = need.passes > caps.passes, grow_pairs = need.pairs > caps.pairs;
 		bool grow_staging = need.staging > caps.staging, grow_spans = need.span_rows > caps.span_rows;
-		bool grow_uploads = need.uploads > caps.uploads;
-		if (!(grow_prims || grow_tiles || grow_passes || grow_pairs || grow_staging || grow_spans || grow_uploads))
+		bool grow_uploads = need.uploads > caps.uploads, grow_masks = need.mask_words > caps.mask_words;
+		if (!(grow_prims || grow_tiles || grow_passes || grow_pairs || grow_staging || grow_spans || grow_uploads ||
+		      grow_masks))
 			return true;
 		if (check(cudaStreamSynchronize(stream)) || (copy_stream && check(cudaStreamSynchronize(copy_stream))))
 			return false;
@@ -689,26 +691,32 @@ struct Executor
 		if (grow_tiles)
 		{
 			uint32_t n = std::max(need.tile_items, caps.tile_items + caps.tile_items / 2);
-			cudaFree(d_masks);
 			cudaFree(d_tile_counts);
 			cudaFree(d_pair_offsets);
 			cudaFree(d_tile_order);
 			cudaFree(d_tile_cycles);
 			cudaFree(d_nonempty);
 			cudaFree(d_scan_blocks);
-			d_masks = d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = d_nonempty = d_scan_blocks = nullptr;
-			if (check(cudaMalloc(&d_masks, size_t(n) * RDP_MASK_WORDS_PER_TILE * 4)) ||
-			    check(cudaMalloc(&d_tile_counts, size_t(n + 1) * 4)) || check(cudaMalloc(&d_pair_offsets, size_t(n + 1) * 4)) ||
+			d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = d_nonempty = d_scan_blocks = nullptr;
+			if (check(cudaMalloc(&d_tile_counts, size_t(n + 1) * 4)) || check(cudaMalloc(&d_pair_offsets, size_t(n + 1) * 4)) ||
 			    check(cudaMalloc(&d_tile_order, size_t(n) * 4)) || check(cudaMalloc(&d_tile_cycles, size_t(n) * 4)) ||
 			    check(cudaMalloc(&d_nonempty, size_t(n) * 4)) ||
 			    check(cudaMalloc(&d_scan_blocks, (size_t(n) / 1024 + 2) * 8)))
 				return false;
-			// Bitmasks and counts are self-clearing between launches; they start at zero.
-			if (check(cudaMemsetAsync(d_masks, 0, size_t(n) * RDP_MASK_WORDS_PER_TILE * 4, stream)) ||
-			    check(cudaMemsetAsync(d_tile_counts, 0, size_t(n + 1) * 4, stream)))
-				return false;
+			// Counts are self-clearing between launches; they start at zero.
+			if (check(cudaMemsetAsync(d_tile_counts, 0, size_t(n + 1) * 4, stream))) return false;
 			caps.tile_items = n;
 			if (!sched_buffers(n)) return false;
+		}
+		if (grow_masks)
+		{
+			// The tiles' primitive bitmasks, laid out per launch (each pass's tiles with its own word
+			// count); self-clearing between launches, so they start at zero.
+			size_t n = std::max(need.mask_words, caps.mask_words + caps.mask_words / 2);
+			cudaFree(d_masks);
+			d_masks = nullptr;
+			if (check(cudaMalloc(&d_masks, n * 4)) || check(cudaMemsetAsync(d_masks, 0, n * 4, stream))) return false;
+			caps.mask_words = n;
 		}
 		if (grow_passes) caps.passes = std::max(need.passes, caps.passes * 2);
 		if (grow_uploads)
@@ -803,17 +811,24 @@ struct Executor
 		if (!n || failed) return !failed;
 		ExecCaps need = caps;
 		uint32_t prims = 0, tiles = 0, descs = 0, uploads = 0;
+		size_t mask_words = 0;
 		for (uint32_t i = 0; i < n; i++)
 		{
 			prims += v[i].num_prims;
 			uploads += v[i].num_uploads;
 			descs += v[i].num_targets;
-			for (uint32_t t = 0; t < v[i].num_targets; t++) tiles += v[i].target[t].tiles_x * v[i].target[t].tiles_y;
+			for (uint32_t t = 0; t < v[i].num_targets; t++)
+			{
+				const uint32_t tt = v[i].target[t].tiles_x * v[i].target[t].tiles_y;
+				tiles += tt;
+				mask_words += size_t(tt) * ((v[i].target_prims[t] + 31) / 32);
+			}
 		}
 		need.passes = std::max(need.passes, n);
 		need.descs = std::max(need.descs, descs);
 		need.prims = std::max(need.prims, std::max(prims, 1u));
 		need.uploads = std::max(need.uploads, std::max(uploads, 1u));
+		need.mask_words = std::max(need.mask_words, std::max<size_t>(mask_words, 1));
 		need.tile_items = std::max(need.tile_items, std::max(tiles, 1u));
 		need.pairs = std::max(need.pairs, initial_pairs);
 		need.span_rows = std::max(need.span_rows, initial_span_rows);
@@ -836,8 +851,9 @@ struct Executor
 		size_t o_list = reserve(4 * n);
 		RdpPass *passes = reinterpret_cast<RdpPass *>(h + o_pass);
 		uint32_t *tmem_list = reinterpret_cast<uint32_t *>(h + o_list);
-		uint32_t num_tmem = 0, max_uploads = 0;
+		uint32_t num_tmem = 0;
 		uint32_t prim_base = 0, word_base = 0, sb_base = 0, ts_base = 0, up_base = 0, tile_base = 0;
+		size_t mask_base = 0;
 		// Sections: all prims, then all words, state blocks, tile sets, uploads; each view's
 		// share of a section is contiguous.  The views are copied in parallel.
 		std::vector<size_t> at(size_t(n) * 5);
@@ -882,15 +898,13 @@ struct Executor
 				p.upload_begin = up_base;
 				p.upload_count = t == 0 ? v[i].num_uploads : 0;
 				p.tile_item_begin = tile_base;
-				p.masks = d_masks + size_t(tile_base) * RDP_MASK_WORDS_PER_TILE;
+				p.mask_words = (p.prim_count + 31) / 32;
+				p.masks = d_masks + mask_base;
 				passes[d] = p;
-				if (t == 0 && v[i].num_uploads)
-				{
-					tmem_list[num_tmem++] = d;
-					max_uploads = std::max(max_uploads, v[i].num_uploads);
-				}
+				if (t == 0 && v[i].num_uploads) tmem_list[num_tmem++] = d;
 				prim_base += p.prim_count;
 				tile_base += p.tiles_x * p.tiles_y;
+				mask_base += size_t(p.tiles_x) * p.tiles_y * p.mask_words;
 			}
 			word_base += v[i].num_words;
 			sb_base += v[i].num_state_blocks;
@@ -932,7 +946,6 @@ struct Executor
 		L.tmem_pass_list = reinterpret_cast<const uint32_t *>(dst + o_list);
 		L.num_tmem_passes = num_tmem;
 		L.uploads = reinterpret_cast<const RdpUpload *>(dst + o_up);
-		L.max_uploads = max_uploads;
 		L.num_uploads = up_base;
 		L.tmem_keep = d_tmem_keep;
 		L.tile_counts = d_tile_counts;

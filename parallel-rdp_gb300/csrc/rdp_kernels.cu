@@ -725,7 +725,7 @@ __global__ void k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom, 
 			if (hit)
 			{
 				uint32_t tl = uint32_t(ty) * pass.tiles_x + uint32_t(tx);
-				atomicOr(&pass.masks[size_t(tl) * RDP_MASK_WORDS_PER_TILE + word], bit);
+				atomicOr(&pass.masks[size_t(tl) * pass.mask_words + word], bit);
 				// Upscaled passes render from the bitmasks alone (no pair list).
 				if (!sl) atomicAdd(&tile_counts[pass.tile_item_begin + tl], 1u);
 			}
@@ -3001,7 +3001,7 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 	const uint32_t pi = pass_of_item(passes, num_passes, item);
 	const RdpPass &ps = passes[pi];
 	uint32_t tl = item - ps.tile_item_begin;
-	uint32_t *masks = ps.masks + size_t(tl) * RDP_MASK_WORDS_PER_TILE;
+	uint32_t *masks = ps.masks + size_t(tl) * ps.mask_words;
 	uint32_t nwords = (ps.prim_count + 31) / 32;
 	uint32_t out = offsets[item];
 	const uint32_t npairs = offsets[item + 1] - out;
@@ -3773,7 +3773,7 @@ __device__ __forceinline__ void raster_tile(uint32_t item, const RdpPass *__rest
 	const RdpPass &ps = passes[pi];
 	const uint32_t tile_linear = item - ps.tile_item_begin;
 	const int tx = int(tile_linear % ps.tiles_x), ty = int(tile_linear / ps.tiles_x);
-	uint32_t *masks = ps.masks + size_t(tile_linear) * RDP_MASK_WORDS_PER_TILE;
+	uint32_t *masks = ps.masks + size_t(tile_linear) * ps.mask_words;
 	const uint32_t nwords = (ps.prim_count + 31) / 32;
 
 	PassConst pc;
@@ -3923,7 +3923,7 @@ __device__ __forceinline__ void raster_tile_upscaled(uint32_t item, const RdpPas
 	const RdpPass &ps = passes[pi];
 	const uint32_t tile_linear = item - ps.tile_item_begin;
 	const int tx = int(tile_linear % ps.tiles_x), ty = int(tile_linear / ps.tiles_x);
-	uint32_t *masks = ps.masks + size_t(tile_linear) * RDP_MASK_WORDS_PER_TILE;
+	uint32_t *masks = ps.masks + size_t(tile_linear) * ps.mask_words;
 	const uint32_t nwords = (ps.prim_count + 31) / 32;
 	const int sl = int(ps.scale & 3u), S = 1 << sl;
 

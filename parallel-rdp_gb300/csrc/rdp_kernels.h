@@ -34,7 +34,6 @@ typedef struct RdpLaunch
 	const uint32_t *tmem_pass_list;
 	uint32_t num_tmem_passes;
 	const RdpUpload *uploads;
-	uint32_t max_uploads;     /* largest upload count of the TMEM passes */
 	uint32_t num_uploads;     /* uploads of the launch (all TMEM passes' uploads, concatenated) */
 	uint32_t *tmem_keep;      /* [num_uploads][64] scratch bitmask */
 	uint32_t num_tile_items;

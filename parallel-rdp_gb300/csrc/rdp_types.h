@@ -23,8 +23,6 @@
 #define RDP_TILE_W 8
 #define RDP_TILE_H 8
 #define RDP_MAX_PRIMS_PER_PASS 65536
-#define RDP_MASK_WORDS_PER_TILE (RDP_MAX_PRIMS_PER_PASS / 32)
-#define RDP_COARSE_WORDS_PER_TILE (RDP_MAX_PRIMS_PER_PASS / 1024)
 #define RDP_MAX_UPLOADS_PER_PASS 16384
 #define RDP_MAX_TILES_X 128
 #define RDP_MAX_TILES_Y 128
@@ -198,8 +196,7 @@ typedef struct __attribute__((aligned(16))) RdpPass
 {
 	uint8_t *rdram;
 	uint8_t *hidden;
-	uint32_t *masks;    /* [tiles][RDP_MASK_WORDS_PER_TILE] */
-	uint32_t *coarse;   /* [tiles][RDP_COARSE_WORDS_PER_TILE] */
+	uint32_t *masks;    /* [tiles][mask_words]: bit p of a tile's words = primitive p of the pass binned there */
 	uint16_t *tmem_snapshots; /* [uploads + 1][2048] */
 	uint16_t *tmem_state;     /* the instance's persistent TMEM */
 	uint32_t rdram_size, hidden_size;
@@ -218,6 +215,7 @@ typedef struct __attribute__((aligned(16))) RdpPass
 	   hidden_size bytes), fb_width / fb_height the scaled image.  Bit 8: record the super-sampled
 	   write mask (2 bits per native pixel, after the slices). */
 	uint32_t scale;
+	uint32_t mask_words; /* 32-bit words of a tile's primitive bitmask: ceil(prim_count / 32) */
 	unsigned long long *counters; /* the instance's [0] fragments, [1] touched tiles, [2] tile instances */
 	uint32_t *wmask;              /* the instance's RDRAM write mask (1 bit per byte), or null */
 } RdpPass;

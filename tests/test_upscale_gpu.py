@@ -162,3 +162,39 @@ def test_upscaled_scanout(factor, downscale):
             assert img is not None and ref is not None
             assert img.shape == ref.shape == (480 * factor >> downscale, 640 * factor >> downscale)
             assert np.array_equal(img, ref), "frame %d: %d pixels differ" % (frame, np.count_nonzero(img != ref))
+
+
+def test_upscaling_limits():
+    # An upscaling processor cannot record sync-point captures, and batch instances cannot upscale
+    # (rdp_cp_capture_begin / rdp_batch_add_instance return RDP_ERR_INVALID).
+    import ctypes
+    from rdp_gb300 import native
+    with CommandProcessor(rdram_size=RDRAM, upscaling=2) as cp:
+        assert native.lib().rdp_cp_capture_begin(cp._h) == native.RDP_ERR_INVALID
+        # Still usable afterwards.
+        cp.enqueue_command(np.array([0x29000000, 0], dtype=np.uint32))
+        cp.wait_for_timeline(cp.signal_timeline())
+    b = native.Batch()
+    try:
+        rd = np.zeros(RDRAM, dtype=np.uint8)
+        info = native._CreateInfo(rd.ctypes.data, 0, RDRAM, RDRAM // 2, native.CREATE_UPSCALING_2X, 0)
+        h = ctypes.c_void_p()
+        assert native.lib().rdp_batch_add_instance(b._h, ctypes.byref(info), ctypes.byref(h)) == native.RDP_ERR_INVALID
+    finally:
+        b.close()
+
+
+def test_upscaling_with_command_thread():
+    # Decoding on the processor's command thread drives the same upscaled passes.
+    from oracle import Oracle
+    words, rdram = _stream(cmdgen.CONFIG_TEXTURED, seed=5, num_prims=400)
+    o = Oracle(RDRAM)
+    o.set_upscaling(2)
+    o.write_rdram(rdram)
+    o.enqueue(words)
+    rd = np.array(rdram, dtype=np.uint8, copy=True)
+    with CommandProcessor(rd, rdram_size=RDRAM, upscaling=2, command_thread=True) as cp:
+        for chunk in np.array_split(words, 5):
+            cp.enqueue_command(chunk)
+        cp.wait_for_timeline(cp.signal_timeline())
+        _compare(cp, o)

@@ -48,6 +48,8 @@ namespace {
 constexpr uint32_t kMaxWordsPerPass = RDP_MAX_PRIMS_PER_PASS * 44;
 constexpr uint32_t kMaxStateBlocks = RDP_MAX_PRIMS_PER_PASS;
 constexpr uint32_t kMaxTilesets = 32768;
+// Primitives after which (and every as many after) a stand-alone processor's pass goes to an idle GPU.
+constexpr size_t kEagerFlushPrims = 4096;
 constexpr uint32_t kMaxTiles = RDP_MAX_TILES_X * RDP_MAX_TILES_Y;
 
 
@@ -1041,6 +1043,13 @@ struct rdp_cp
 
 	void record_prim(const uint32_t *w, uint32_t len, uint32_t op)
 	{
+		// A stand-alone processor hands a long pass to the GPU early when the GPU has nothing left to
+		// do (the reference submits whenever no submission is active, maintain_queues,
+		// rdp_renderer.cpp:2353-2371), so that the host parses on while it renders; only where the
+		// pass boundary is not observable, and never while recording a capture.
+		if (!batch && !capturing && !up_log2 && prims.size() >= kEagerFlushPrims &&
+		    prims.size() % kEagerFlushPrims == 0 && !pass_boundaries_visible() && cudaStreamQuery(stream) == cudaSuccess)
+			flush();
 		if (prims.size() >= RDP_MAX_PRIMS_PER_PASS || words.size() + len > kMaxWordsPerPass ||
 		    (sb_dirty && state_blocks.size() / RDP_STATE_BLOCK_WORDS >= kMaxStateBlocks) ||
 		    (tiles_dirty && tilesets.size() / 8 >= kMaxTilesets))
@@ -2216,18 +2225,25 @@ bool rdp_batch::reserve_for_capture()
 	{
 		views.clear();
 		uint32_t prims = 0, tiles = 0, uploads = 0;
+		size_t mask_words = 0;
 		for (rdp_cp *cp : instances)
 			if (r < cp->deferred.size())
 			{
 				views.push_back(cp->deferred[r].view());
-				prims += views.back().num_prims;
-				uploads += views.back().num_uploads;
-				for (uint32_t t = 0; t < views.back().num_targets; t++)
-					tiles += views.back().target[t].tiles_x * views.back().target[t].tiles_y;
+				const rdpx::PassView &pv = views.back();
+				prims += pv.num_prims;
+				uploads += pv.num_uploads;
+				for (uint32_t t = 0; t < pv.num_targets; t++)
+				{
+					const uint32_t tt = pv.target[t].tiles_x * pv.target[t].tiles_y;
+					tiles += tt;
+					mask_words += size_t(tt) * ((pv.target_prims[t] + 31) / 32);
+				}
 			}
 		need.passes = std::max(need.passes, uint32_t(views.size()));
 		need.prims = std::max(need.prims, prims);
 		need.uploads = std::max(need.uploads, uploads);
+		need.mask_words = std::max(need.mask_words, mask_words);
 		need.tile_items = std::max(need.tile_items, tiles);
 		need.staging = std::max(need.staging, rdpx::Executor::staging_bytes_for(views.data(), uint32_t(views.size())));
 	}

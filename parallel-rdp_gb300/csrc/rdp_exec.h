@@ -293,12 +293,15 @@ struct Executor
 	uint4 *d_shade_list = nullptr; // primitive-major shading records
 	uint2 *d_pairs = nullptr;
 	uint2 *d_scratch = nullptr; // shaded records, 64 per pair
-	uint8_t *d_staging = nullptr; // two slots of caps.staging bytes
-	// Launch inputs are copied on copy_stream into alternating device slots, so that the copy of
-	// the next launch overlaps this launch's kernels.  slot_copied[s] orders the kernels after the
-	// copy; slot_free[s] (recorded after the kernels that read slot s) orders the next copy into it.
+	// Launch inputs are copied on copy_stream into a ring of kStagingSlots device slots, so that the
+	// copies of the next launches overlap this launch's kernels (a sync point's large round follows
+	// small ones: its copy starts while the previous sync point still renders).  slot_copied[s]
+	// orders the kernels after the copy; slot_free[s] (recorded after the kernels that read slot s)
+	// orders the next copy into it.
+	static constexpr int kStagingSlots = 4;
+	uint8_t *d_staging = nullptr; // kStagingSlots slots of caps.staging bytes
 	cudaStream_t copy_stream = nullptr;
-	cudaEvent_t slot_copied[2] = {}, slot_free[2] = {};
+	cudaEvent_t slot_copied[kStagingSlots] = {}, slot_free[kStagingSlots] = {};
 	int staging_slot = 0;
 
 	// Pinned host staging buffers, used round-robin; a buffer is reused once the H2D copy
@@ -486,7 +489,7 @@ struct Executor
 		    check(cudaMalloc(&d_queues, queue_bytes())) ||
 		    check(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking)))
 			return false;
-		for (int k = 0; k < 2; k++)
+		for (int k = 0; k < kStagingSlots; k++)
 			if (check(cudaEventCreateWithFlags(&slot_copied[k], cudaEventDisableTiming)) ||
 			    check(cudaEventCreateWithFlags(&slot_free[k], cudaEventDisableTiming)))
 				return false;
@@ -635,7 +638,7 @@ struct Executor
 		d_ctrl = nullptr;
 		d_pair_log = nullptr;
 		d_queues = nullptr;
-		for (int k = 0; k < 2; k++)
+		for (int k = 0; k < kStagingSlots; k++)
 		{
 			if (slot_copied[k]) cudaEventDestroy(slot_copied[k]);
 			if (slot_free[k]) cudaEventDestroy(slot_free[k]);
@@ -754,7 +757,7 @@ struct Executor
 			size_t n = std::max(need.staging, caps.staging + caps.staging / 2);
 			cudaFree(d_staging);
 			d_staging = nullptr;
-			if (check(cudaMalloc(&d_staging, 2 * n))) return false;
+			if (check(cudaMalloc(&d_staging, kStagingSlots * n))) return false;
 			caps.staging = n;
 		}
 		return !check(cudaStreamSynchronize(stream));
@@ -922,7 +925,7 @@ struct Executor
 		}
 		else
 		{
-			staging_slot ^= 1;
+			staging_slot = (staging_slot + 1) % kStagingSlots;
 			if (check(cudaStreamWaitEvent(copy_stream, slot_free[slot], 0)) ||
 			    check(cudaMemcpyAsync(dst, h, off, cudaMemcpyHostToDevice, copy_stream)) ||
 			    check(cudaEventRecord(st.done, copy_stream)) || check(cudaEventRecord(slot_copied[slot], copy_stream)) ||

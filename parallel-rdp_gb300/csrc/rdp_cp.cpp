@@ -376,6 +376,7 @@ struct rdp_cp
 		std::vector<uint32_t> prim_ids; // indices into `prims`
 	};
 	std::vector<Target> targets;
+	bool pass_fill_only = true; // every primitive of the pass is drawn by the fill pipe (cycle type 3)
 
 	// The reference's own pass (it ends after 256 primitives, before the 256th TMEM upload,
 	// at image changes, load hazards and SyncFull; rdp_renderer.cpp:1564-1590, 3051-3097,
@@ -871,6 +872,7 @@ struct rdp_cp
 		v.num_tilesets = uint32_t(tilesets.size() / 8);
 		v.uploads = uploads.data();
 		v.num_uploads = uint32_t(uploads.size());
+		v.fill_only = pass_fill_only;
 
 		if (batch)
 		{
@@ -887,6 +889,7 @@ struct rdp_cp
 			pk.tilesets = std::move(tilesets);
 			pk.uploads = std::move(uploads);
 			if (coherent && !in_capture()) pk.read_pages = read_pages;
+			pk.fill_only = v.fill_only;
 			deferred.push_back(std::move(pk));
 		}
 		else if (up_log2)
@@ -989,6 +992,7 @@ struct rdp_cp
 		tilesets.clear();
 		uploads.clear();
 		targets.clear();
+		pass_fill_only = true;
 		sb_dirty = true;
 		tiles_dirty = true;
 	}
@@ -1087,6 +1091,7 @@ struct rdp_cp
 			tilesets.insert(tilesets.end(), tiles, tiles + 8);
 			tiles_dirty = false;
 		}
+		if (cycle_type() != 3) pass_fill_only = false;
 		RdpPrimIn pi;
 		pi.word_offset = uint32_t(words.size());
 		pi.state_block = uint32_t(state_blocks.size() / RDP_STATE_BLOCK_WORDS - 1);

@@ -142,6 +142,7 @@ struct PassView
 	uint32_t num_tilesets;
 	const RdpUpload *uploads;
 	uint32_t num_uploads;
+	bool fill_only; // every primitive is drawn by the fill pipe (cycle type 3)
 };
 
 // An owned copy of a recorded pass (batched instances defer their passes).
@@ -154,6 +155,7 @@ struct PassPacket
 	std::vector<RdpTile> tilesets;
 	std::vector<RdpUpload> uploads;
 	std::vector<uint32_t> read_pages; // RDRAM pages refreshed from the caller's memory before the pass
+	bool fill_only = false;
 
 	PassView view() const
 	{
@@ -174,6 +176,7 @@ struct PassPacket
 		v.num_tilesets = uint32_t(tilesets.size() / 8);
 		v.uploads = uploads.data();
 		v.num_uploads = uint32_t(uploads.size());
+		v.fill_only = fill_only;
 		return v;
 	}
 };
@@ -971,9 +974,13 @@ struct Executor
 		L.prim_offsets = d_prim_offsets;
 		L.prim_scan_blocks = d_prim_blocks;
 		L.upscaled = upscaled ? 1u : 0u;
+		// Launches whose passes only fill rectangles (a frame's clears) take the per-tile fill kernel.
+		bool fill_only = !upscaled && tile_base != 0;
+		for (uint32_t i = 0; i < n && fill_only; i++) fill_only = v[i].fill_only;
+		L.fill_only = fill_only ? 1u : 0u;
 		int variant = current_variant();
 		bool sample = false;
-		if (!upscaled && tuner.active && shade_variant_choice(device) < 0 && !cap && tile_base &&
+		if (!upscaled && !fill_only && tuner.active && shade_variant_choice(device) < 0 && !cap && tile_base &&
 		    tuner.in_epoch < ShadeTuner::kMaxSamplesPerEpoch)
 		{
 			variant = int((tuner.in_epoch + uint32_t(tuner.epoch)) % RDP_SHADE_VARIANTS);
@@ -986,7 +993,7 @@ struct Executor
 		L.blend_kernel = blend_kernel;
 		L.pair_log = sample ? d_pair_log : nullptr;
 		L.log_slot = sample ? uint32_t(tuner.samples_taken++ % 256) : 0u;
-		if (!upscaled && !sample && !cap && launch_log && tile_base && launch_log_pending.size() < kLaunchLogSlots)
+		if (!upscaled && !fill_only && !sample && !cap && launch_log && tile_base && launch_log_pending.size() < kLaunchLogSlots)
 		{
 			L.pair_log = d_launch_pairs;
 			L.log_slot = uint32_t(launch_log_pending.size());
@@ -1000,7 +1007,7 @@ struct Executor
 		L.num_tile_items = tile_base;
 		L.tile_cycles = record_cycles ? d_tile_cycles : nullptr;
 		L.tile_order = nullptr;
-		if (!upscaled && sched_ready && (sched.order_enabled || sched.train_enabled))
+		if (!upscaled && !fill_only && sched_ready && (sched.order_enabled || sched.train_enabled))
 		{
 			sched.order = d_tile_order;
 			L.sched = &sched;

@@ -726,8 +726,8 @@ __global__ void k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom, 
 			{
 				uint32_t tl = uint32_t(ty) * pass.tiles_x + uint32_t(tx);
 				atomicOr(&pass.masks[size_t(tl) * pass.mask_words + word], bit);
-				// Upscaled passes render from the bitmasks alone (no pair list).
-				if (!sl) atomicAdd(&tile_counts[pass.tile_item_begin + tl], 1u);
+				// Upscaled and fill-only launches render from the bitmasks alone (no pair list).
+				if (tile_counts) atomicAdd(&tile_counts[pass.tile_item_begin + tl], 1u);
 			}
 		}
 		binned += __popc(__ballot_sync(0xffffffffu, hit));
@@ -3792,8 +3792,14 @@ __global__ void __launch_bounds__(SHADE_THREADS, 24) k_blend_lookahead(const Rdp
 // One CTA of 64 threads per 8x8 tile, one pixel per thread; warp w owns rows 4w..4w+3.
 // Both warps walk the tile's primitive bitmask in primitive order; pixel state stays in
 // registers for the whole pass (init_tile/finish_tile, memory_interfacing.h:286-362).
+//
+// FILL: every primitive of the launch is drawn by the fill pipe (cycle type 3: a frame's
+// clears).  Its pixels take the fill colour wherever x lies in the row's span
+// (shading.h:55-62 with the fill branch of memory_interfacing.h:381-571), so only the x extent
+// of each row is set up and no shading record is built.
 constexpr int RASTER_THREADS = 64;
 
+template <bool FILL = false>
 __device__ __forceinline__ void raster_tile(uint32_t item, const RdpPass *__restrict__ passes, uint32_t num_passes,
                                             const RdpPrimGeom *__restrict__ geom, const RdpPrimAttr *__restrict__ attr,
                                             const RdpPrimShade *__restrict__ shade, const RdpTile *__restrict__ tilesets)
@@ -3866,6 +3872,23 @@ __device__ __forceinline__ void raster_tile(uint32_t item, const RdpPass *__rest
 				const RdpPrimGeom &g = geom[prim];
 				const int ylo = g.span_ylo, yhi = g.span_yhi;
 				if (yhi < row0 || ylo > row0 + 3) continue; // no row of this warp is covered
+				if (FILL)
+				{
+					if (lane < 4) span_x(g, row0 + lane, s_sp[wib][lane]);
+					__syncwarp();
+					const SpanRow &sp = s_sp[wib][r];
+					if (inside && px_y >= ylo && px_y <= yhi && sp.valid && px_x >= sp.start_x && px_x <= sp.end_x)
+					{
+						Shaded in;
+						in.combined = 0u;
+						in.z_dith = 0;
+						in.coverage = 0x40;
+						in.shade_alpha = 0;
+						frags += blend_pixel(ps, pc, shade[prim], in, px);
+					}
+					__syncwarp();
+					continue;
+				}
 				// Spans for the warp's 4 rows plus the next row (pipelined texel1 peek).
 				if (lane < 5)
 					span_attr(g, attr[prim], row0 + lane, s_sp[wib][lane]);
@@ -3928,6 +3951,18 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const RdpPass *__rest
 	for (uint32_t item = blockIdx.x; item < num_items; item += gridDim.x)
 	{
 		raster_tile(item, passes, num_passes, geom, attr, shade, tilesets);
+		__syncthreads();
+	}
+}
+
+// Launches whose primitives all fill (RdpLaunch.fill_only): persistent CTAs over every tile.
+__global__ void __launch_bounds__(RASTER_THREADS) k_fill(const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                                        uint32_t num_items, const RdpPrimGeom *__restrict__ geom,
+                                                        const RdpPrimShade *__restrict__ shade)
+{
+	for (uint32_t item = blockIdx.x; item < num_items; item += gridDim.x)
+	{
+		raster_tile<true>(item, passes, num_passes, geom, nullptr, shade, nullptr);
 		__syncthreads();
 	}
 }
@@ -4121,7 +4156,7 @@ static bool multi_cta_scan(const RdpLaunch *L)
 extern "C" uint32_t rdp_kernels_count(const RdpLaunch *L)
 {
 	uint32_t n = 0;
-	if (L->upscaled)
+	if (L->upscaled || L->fill_only)
 		return (L->num_prims ? 2u : 0u) + (L->num_tmem_passes ? 2u : 0u) + (L->num_prims && L->num_tile_items ? 1u : 0u);
 	if (L->num_prims) n += 2;
 	if (L->num_prims && L->num_tile_items && L->spans) n += 1;
@@ -4152,7 +4187,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 			                                                                   L->num_passes, L->geom, L->attr,
 			                                                                   L->shade, nullptr);
 			rdp::k_bin<<<(L->num_prims * 32 + 255) / 256, 256, 0, stream>>>(L->num_prims, L->geom, L->shade,
-			                                                                 L->passes, L->tile_counts, nullptr);
+			                                                                 L->passes, nullptr, nullptr);
 		}
 		if (L->num_tmem_passes)
 		{
@@ -4165,6 +4200,31 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 			rdp::k_raster_upscaled<<<std::min<uint32_t>(L->num_tile_items, L->blend_ctas), rdp::RASTER_THREADS, 0,
 			                         stream>>>(L->passes, L->num_passes, L->num_tile_items, L->geom, L->attr,
 			                                   L->shade, L->tilesets);
+		return cudaGetLastError();
+	}
+	if (L->fill_only)
+	{
+		// Fill-only passes: set-up, binning, TMEM, and one per-tile kernel (no pair list).
+		if (L->num_prims)
+		{
+			rdp::k_prim_setup<<<(L->num_prims + 127) / 128, 128, 0, stream>>>(L->prims_in, L->num_prims, L->words,
+			                                                                   L->state_blocks, L->passes,
+			                                                                   L->num_passes, L->geom, L->attr,
+			                                                                   L->shade, nullptr);
+			rdp::k_bin<<<(L->num_prims * 32 + 255) / 256, 256, 0, stream>>>(L->num_prims, L->geom, L->shade,
+			                                                                 L->passes, nullptr, nullptr);
+		}
+		if (L->num_tmem_passes)
+		{
+			rdp::k_tmem_apply<<<L->num_uploads, 256, 0, stream>>>(L->passes, L->tmem_pass_list, L->num_tmem_passes,
+			                                                      L->uploads, L->tmem_keep);
+			rdp::k_tmem_carry<<<dim3(2048 / 32, L->num_tmem_passes), rdp::TMEM_CARRY_WARPS * 32, 0, stream>>>(
+				L->passes, L->tmem_pass_list, L->tmem_keep);
+		}
+		if (L->num_prims && L->num_tile_items)
+			rdp::k_fill<<<std::min<uint32_t>(L->num_tile_items, std::max<uint32_t>(L->num_sms, 1u) * 32u),
+			              rdp::RASTER_THREADS, 0, stream>>>(L->passes, L->num_passes, L->num_tile_items, L->geom,
+			                                                L->shade);
 		return cudaGetLastError();
 	}
 	const bool raster = L->num_prims && L->num_tile_items;

@@ -74,6 +74,7 @@ typedef struct RdpLaunch
 	uint2 *scratch;                 /* [pair_capacity * 64] shaded records, 8 bytes per pixel */
 	uint32_t upscaled;              /* the passes are upscaled passes (RdpPass.scale): set-up, binning, TMEM and
 	                                   k_raster_upscaled only */
+	uint32_t fill_only;             /* every primitive fills a rectangle: set-up, binning, TMEM and k_fill only */
 } RdpLaunch;
 
 #ifdef __cplusplus

@@ -147,6 +147,25 @@ __device__ __forceinline__ uint32_t pass_of_item(const RdpPass *__restrict__ pas
 	return lo;
 }
 
+// The same with a warp's 32 lanes probing 32 evenly spaced passes per step (a 32-ary search): two
+// dependent loads for up to 1,024 passes instead of ten.  Called by all lanes of a warp.
+__device__ __forceinline__ uint32_t pass_of_item_warp(const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                                      uint32_t item, int lane)
+{
+	// passes[lo].tile_item_begin <= item, and the last such pass lies in [lo, lo + n).
+	uint32_t lo = 0, n = num_passes;
+	while (n > 1)
+	{
+		const uint32_t step = (n + 31) / 32;
+		const uint32_t cand = lo + uint32_t(lane) * step;
+		const bool le = cand < lo + n && passes[cand].tile_item_begin <= item;
+		const uint32_t k = 31u - uint32_t(__clz(int(__ballot_sync(0xffffffffu, le))));
+		lo += k * step;
+		n = min(step, n - k * step);
+	}
+	return lo;
+}
+
 __global__ void k_prim_setup(const RdpPrimIn *__restrict__ in, uint32_t num_prims, const uint32_t *__restrict__ words,
                              const uint32_t *__restrict__ state_blocks, const RdpPass *__restrict__ passes,
                              uint32_t num_passes, RdpPrimGeom *__restrict__ geom_out, RdpPrimAttr *__restrict__ attr_out,
@@ -689,7 +708,10 @@ __device__ bool bin_primitive(const RdpPrimGeom &g, int lox, int loy, int hix, i
 	return rx0 <= rx1;
 }
 
-// With `prim_pairs`, also writes each primitive's number of binned tiles (its pairs).
+// With `prim_pairs`, also writes each primitive's number of binned tiles (its pairs).  Without it
+// the grid's y dimension may split a primitive's tiles over several warps (launches of a few large
+// primitives, such as a frame's clears): warp k of a primitive takes its tiles k*32 .. k*32+31,
+// then every 32*gridDim.y-th further.
 __global__ void k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom, const RdpPrimShade *__restrict__ shade,
                       const RdpPass *__restrict__ passes, uint32_t *__restrict__ tile_counts,
                       uint32_t *__restrict__ prim_pairs)
@@ -712,7 +734,7 @@ __global__ void k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom, 
 	int fbw = int(pass.fb_width), fbh = int(pass.fb_height);
 	const int sl = int(pass.scale & 3u);
 	uint32_t binned = 0;
-	for (int t0 = 0; t0 < count; t0 += 32)
+	for (int t0 = int(blockIdx.y) * 32; t0 < count; t0 += 32 * int(gridDim.y))
 	{
 		const int t = t0 + int(lane);
 		bool hit = false;
@@ -2544,40 +2566,43 @@ __device__ __forceinline__ uint2 pack_shaded(const Shaded &o)
 	return make_uint2(o.combined, y);
 }
 
+// The fill pipe (memory_interfacing.h:381-571, fill branch): the pixel takes the fill colour,
+// the 16-bit formats the half of the 32-bit fill word at the pixel's address.
+__device__ __forceinline__ bool fill_pixel(const RdpPass &ps, const PassConst &pc, uint32_t col, Pix &px)
+{
+	switch (ps.fb_fmt)
+	{
+	case FBF_RGBA8888:
+		write_color(ps.fb_fmt, px, int((col >> 24) & 0xff), int((col >> 16) & 0xff), int((col >> 8) & 0xff), int(col & 0xff));
+		break;
+	case FBF_RGBA5551:
+		col >>= ((px.cidx & 1u) ^ 1u) * 16u;
+		write_color(ps.fb_fmt, px, int((col >> 8) & 0xf8u), int((col >> 3) & 0xf8u), int((col << 2) & 0xf8u),
+		            int((col & 1u) * 0xe0u));
+		break;
+	case FBF_IA88:
+	{
+		col >>= ((px.cidx & 1u) ^ 1u) * 16u;
+		int r = int((col >> 8) & 0xff);
+		write_color(ps.fb_fmt, px, r, r, r, int(col & 0xff));
+		break;
+	}
+	case FBF_I8:
+	{
+		col >>= ((px.cidx & 3u) ^ 3u) * 8u;
+		int v = int(col & 0xff);
+		write_color(ps.fb_fmt, px, v, v, v, v);
+		break;
+	}
+	default: break;
+	}
+	if (pc.alias) alias_c2d(ps.fb_fmt, px);
+	return ps.fb_fmt != FBF_I4;
+}
+
 __device__ bool blend_pixel(const RdpPass &ps, const PassConst &pc, const RdpPrimShade &sh, const Shaded &in, Pix &px)
 {
-	if (in.coverage & 0x40)
-	{
-		uint32_t col = sh.fill_color;
-		switch (ps.fb_fmt)
-		{
-		case FBF_RGBA8888:
-			write_color(ps.fb_fmt, px, int((col >> 24) & 0xff), int((col >> 16) & 0xff), int((col >> 8) & 0xff), int(col & 0xff));
-			break;
-		case FBF_RGBA5551:
-			col >>= ((px.cidx & 1u) ^ 1u) * 16u;
-			write_color(ps.fb_fmt, px, int((col >> 8) & 0xf8u), int((col >> 3) & 0xf8u), int((col << 2) & 0xf8u),
-			            int((col & 1u) * 0xe0u));
-			break;
-		case FBF_IA88:
-		{
-			col >>= ((px.cidx & 1u) ^ 1u) * 16u;
-			int r = int((col >> 8) & 0xff);
-			write_color(ps.fb_fmt, px, r, r, r, int(col & 0xff));
-			break;
-		}
-		case FBF_I8:
-		{
-			col >>= ((px.cidx & 3u) ^ 3u) * 8u;
-			int v = int(col & 0xff);
-			write_color(ps.fb_fmt, px, v, v, v, v);
-			break;
-		}
-		default: break;
-		}
-		if (pc.alias) alias_c2d(ps.fb_fmt, px);
-		return ps.fb_fmt != FBF_I4;
-	}
+	if (in.coverage & 0x40) return fill_pixel(ps, pc, sh.fill_color, px);
 	if (in.coverage & 0x20)
 	{
 		uint32_t word = uint32_t(in.z_dith);
@@ -3792,14 +3817,8 @@ __global__ void __launch_bounds__(SHADE_THREADS, 24) k_blend_lookahead(const Rdp
 // One CTA of 64 threads per 8x8 tile, one pixel per thread; warp w owns rows 4w..4w+3.
 // Both warps walk the tile's primitive bitmask in primitive order; pixel state stays in
 // registers for the whole pass (init_tile/finish_tile, memory_interfacing.h:286-362).
-//
-// FILL: every primitive of the launch is drawn by the fill pipe (cycle type 3: a frame's
-// clears).  Its pixels take the fill colour wherever x lies in the row's span
-// (shading.h:55-62 with the fill branch of memory_interfacing.h:381-571), so only the x extent
-// of each row is set up and no shading record is built.
 constexpr int RASTER_THREADS = 64;
 
-template <bool FILL = false>
 __device__ __forceinline__ void raster_tile(uint32_t item, const RdpPass *__restrict__ passes, uint32_t num_passes,
                                             const RdpPrimGeom *__restrict__ geom, const RdpPrimAttr *__restrict__ attr,
                                             const RdpPrimShade *__restrict__ shade, const RdpTile *__restrict__ tilesets)
@@ -3872,23 +3891,6 @@ __device__ __forceinline__ void raster_tile(uint32_t item, const RdpPass *__rest
 				const RdpPrimGeom &g = geom[prim];
 				const int ylo = g.span_ylo, yhi = g.span_yhi;
 				if (yhi < row0 || ylo > row0 + 3) continue; // no row of this warp is covered
-				if (FILL)
-				{
-					if (lane < 4) span_x(g, row0 + lane, s_sp[wib][lane]);
-					__syncwarp();
-					const SpanRow &sp = s_sp[wib][r];
-					if (inside && px_y >= ylo && px_y <= yhi && sp.valid && px_x >= sp.start_x && px_x <= sp.end_x)
-					{
-						Shaded in;
-						in.combined = 0u;
-						in.z_dith = 0;
-						in.coverage = 0x40;
-						in.shade_alpha = 0;
-						frags += blend_pixel(ps, pc, shade[prim], in, px);
-					}
-					__syncwarp();
-					continue;
-				}
 				// Spans for the warp's 4 rows plus the next row (pipelined texel1 peek).
 				if (lane < 5)
 					span_attr(g, attr[prim], row0 + lane, s_sp[wib][lane]);
@@ -3955,15 +3957,124 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const RdpPass *__rest
 	}
 }
 
-// Launches whose primitives all fill (RdpLaunch.fill_only): persistent CTAs over every tile.
-__global__ void __launch_bounds__(RASTER_THREADS) k_fill(const RdpPass *__restrict__ passes, uint32_t num_passes,
-                                                        uint32_t num_items, const RdpPrimGeom *__restrict__ geom,
-                                                        const RdpPrimShade *__restrict__ shade)
+// ============================================================================ k_fill
+// Launches whose primitives all take the fill pipe (cycle type 3: a frame's clears;
+// RdpLaunch.fill_only).  A pixel takes the fill colour wherever x lies in its row's span
+// (shading.h:55-62 with the fill branch of memory_interfacing.h:381-571), so only the x extent of
+// each row is set up and no shading record is built.  One warp per 8x8 tile, independent of the
+// CTA's other warps: lane l owns pixels (l % 8, l / 8) and (l % 8, l / 8 + 4) of the tile, both
+// loaded as the tile's bitmask is read (a pixel without fills stores nothing), and the warp alone
+// clears the bitmask words it consumed.
+constexpr int FILL_THREADS = 256;
+
+__global__ void __launch_bounds__(FILL_THREADS) k_fill(const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                                      uint32_t num_items, const RdpPrimGeom *__restrict__ geom,
+                                                      const RdpPrimShade *__restrict__ shade)
 {
-	for (uint32_t item = blockIdx.x; item < num_items; item += gridDim.x)
+	__shared__ SpanRow s_sp[FILL_THREADS / 32][8];
+	const int wib = threadIdx.x >> 5;
+	const int lane = threadIdx.x & 31;
+	const uint32_t item = blockIdx.x * (FILL_THREADS / 32) + uint32_t(wib);
+	if (item >= num_items) return; // the whole warp
+
+	const uint32_t pi = pass_of_item_warp(passes, num_passes, item, lane);
+	const RdpPass &ps = passes[pi];
+	const uint32_t tile_linear = item - ps.tile_item_begin;
+	const int tx = int(tile_linear % ps.tiles_x), ty = int(tile_linear / ps.tiles_x);
+	uint32_t *masks = ps.masks + size_t(tile_linear) * ps.mask_words;
+	const uint32_t nwords = (ps.prim_count + 31) / 32;
+
+	PassConst pc;
+	pc.fb_size = pc.dx_mask = pc.dx_shift = 0; // the fill pipe reads neither
+	pc.alias = ps.fb_addr == ps.depth_addr;
+	uint32_t addr_index;
+	switch (ps.fb_fmt)
 	{
-		raster_tile<true>(item, passes, num_passes, geom, nullptr, shade, nullptr);
-		__syncthreads();
+	case FBF_I4:
+	case FBF_I8: addr_index = ps.fb_addr; break;
+	case FBF_RGBA5551:
+	case FBF_IA88: addr_index = ps.fb_addr >> 1; break;
+	default: addr_index = ps.fb_addr >> 2; break;
+	}
+	const uint32_t depth_index = ps.depth_addr >> 1;
+
+	const int row0 = ty * 8;
+	const int px_x = tx * 8 + (lane & 7);
+	const int y0 = row0 + (lane >> 3), y1 = y0 + 4;
+	const bool in0 = px_x < int(ps.fb_width) && y0 < int(ps.fb_height);
+	const bool in1 = px_x < int(ps.fb_width) && y1 < int(ps.fb_height);
+	const uint32_t ci0 = addr_index + ps.fb_width * uint32_t(y0) + uint32_t(px_x);
+	const uint32_t di0 = depth_index + ps.fb_width * uint32_t(y0) + uint32_t(px_x);
+	const uint32_t ci1 = ci0 + 4u * ps.fb_width, di1 = di0 + 4u * ps.fb_width;
+
+	Pix p0, p1;
+	p0.cdirty = p0.ddirty = p1.cdirty = p1.ddirty = false;
+	if (in0) load_pixel(ps, p0, ci0, di0);
+	if (in1) load_pixel(ps, p1, ci1, di1);
+	uint32_t frags = 0;
+	bool any = false;
+	for (uint32_t base = 0; base < nwords; base += 32)
+	{
+		const uint32_t wi = base + lane;
+		const uint32_t wv = wi < nwords ? masks[wi] : 0u;
+		unsigned nz = __ballot_sync(0xffffffffu, wv != 0);
+		any = any || nz != 0;
+		while (nz)
+		{
+			const int src = __ffs(nz) - 1;
+			nz &= nz - 1;
+			uint32_t bits = __shfl_sync(0xffffffffu, wv, src);
+			while (bits)
+			{
+				const int b = __ffs(bits) - 1;
+				bits &= bits - 1;
+				const uint32_t prim = ps.prim_begin + (base + src) * 32 + b;
+				const RdpPrimGeom &g = geom[prim];
+				const uint32_t col = shade[prim].fill_color;
+				const int ylo = g.span_ylo, yhi = g.span_yhi;
+				if (yhi < row0 || ylo > row0 + 7) continue; // no row of the tile is covered
+				if (lane < 8) span_x(g, row0 + lane, s_sp[wib][lane]);
+				__syncwarp();
+				const SpanRow &a = s_sp[wib][lane >> 3], &c = s_sp[wib][(lane >> 3) + 4];
+				if (in0 && y0 >= ylo && y0 <= yhi && a.valid && px_x >= a.start_x && px_x <= a.end_x)
+					frags += fill_pixel(ps, pc, col, p0);
+				if (in1 && y1 >= ylo && y1 <= yhi && c.valid && px_x >= c.start_x && px_x <= c.end_x)
+					frags += fill_pixel(ps, pc, col, p1);
+				__syncwarp();
+			}
+		}
+	}
+	if (!any) return; // no primitive binned here: nothing stored, marked or counted
+	if (in0) store_pixel(ps, p0, ci0, di0, pc.alias);
+	if (in1) store_pixel(ps, p1, ci1, di1, pc.alias);
+	if (ps.wmask)
+	{
+		mark_pixel(ps, p0, ci0, di0, pc.alias, in0);
+		mark_pixel(ps, p1, ci1, di1, pc.alias, in1);
+	}
+	// The warp has consumed the bitmask: clear it for the next pass using this slot.
+	unsigned long long pairs_here = 0;
+	for (uint32_t wi = lane; wi < nwords; wi += 32)
+	{
+		pairs_here += __popc(masks[wi]);
+		masks[wi] = 0u;
+	}
+	unsigned long long *counters = ps.counters;
+	if (counters)
+	{
+		unsigned long long total = frags;
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1)
+		{
+			total += __shfl_xor_sync(0xffffffffu, total, o);
+			pairs_here += __shfl_xor_sync(0xffffffffu, pairs_here, o);
+		}
+		if (lane == 0)
+		{
+			if (total) atomicAdd(counters, total);
+			atomicAdd(counters + 1, 1ull);
+			atomicAdd(counters + 2, pairs_here);
+		}
 	}
 }
 
@@ -4153,6 +4264,14 @@ static bool multi_cta_scan(const RdpLaunch *L)
 	                          (L->shade_list && L->prim_scan_blocks && L->num_prims > RDP_SCAN_SINGLE_CTA_MAX));
 }
 
+// Warps per primitive in k_bin (its grid's y dimension) when no per-primitive count is taken: a
+// launch of few primitives still fills the GPU.
+static uint32_t bin_split(const RdpLaunch *L)
+{
+	const uint32_t target = std::max<uint32_t>(L->num_sms, 1u) * 32u;
+	return std::min<uint32_t>(std::max<uint32_t>(target / std::max<uint32_t>(L->num_prims, 1u), 1u), 64u);
+}
+
 extern "C" uint32_t rdp_kernels_count(const RdpLaunch *L)
 {
 	uint32_t n = 0;
@@ -4186,8 +4305,8 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 			                                                                   L->state_blocks, L->passes,
 			                                                                   L->num_passes, L->geom, L->attr,
 			                                                                   L->shade, nullptr);
-			rdp::k_bin<<<(L->num_prims * 32 + 255) / 256, 256, 0, stream>>>(L->num_prims, L->geom, L->shade,
-			                                                                 L->passes, nullptr, nullptr);
+			rdp::k_bin<<<dim3((L->num_prims * 32 + 255) / 256, bin_split(L)), 256, 0, stream>>>(
+				L->num_prims, L->geom, L->shade, L->passes, nullptr, nullptr);
 		}
 		if (L->num_tmem_passes)
 		{
@@ -4211,8 +4330,8 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 			                                                                   L->state_blocks, L->passes,
 			                                                                   L->num_passes, L->geom, L->attr,
 			                                                                   L->shade, nullptr);
-			rdp::k_bin<<<(L->num_prims * 32 + 255) / 256, 256, 0, stream>>>(L->num_prims, L->geom, L->shade,
-			                                                                 L->passes, nullptr, nullptr);
+			rdp::k_bin<<<dim3((L->num_prims * 32 + 255) / 256, bin_split(L)), 256, 0, stream>>>(
+				L->num_prims, L->geom, L->shade, L->passes, nullptr, nullptr);
 		}
 		if (L->num_tmem_passes)
 		{
@@ -4222,9 +4341,9 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 				L->passes, L->tmem_pass_list, L->tmem_keep);
 		}
 		if (L->num_prims && L->num_tile_items)
-			rdp::k_fill<<<std::min<uint32_t>(L->num_tile_items, std::max<uint32_t>(L->num_sms, 1u) * 32u),
-			              rdp::RASTER_THREADS, 0, stream>>>(L->passes, L->num_passes, L->num_tile_items, L->geom,
-			                                                L->shade);
+			rdp::k_fill<<<(L->num_tile_items + rdp::FILL_THREADS / 32 - 1) / (rdp::FILL_THREADS / 32),
+			              rdp::FILL_THREADS, 0, stream>>>(L->passes, L->num_passes, L->num_tile_items, L->geom,
+			                                              L->shade);
 		return cudaGetLastError();
 	}
 	const bool raster = L->num_prims && L->num_tile_items;
@@ -4237,10 +4356,9 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		                                                                                L->sched->train_enabled)
 		                                                                       ? L->sched->featbits
 		                                                                       : nullptr);
-		rdp::k_bin<<<(L->num_prims * 32 + 255) / 256, 256, 0, stream>>>(L->num_prims, L->geom, L->shade, L->passes,
-		                                                                 L->tile_counts,
-		                                                                 L->shade_list && L->num_tile_items ? L->prim_pairs
-		                                                                                                   : nullptr);
+		uint32_t *prim_pairs = L->shade_list && L->num_tile_items ? L->prim_pairs : nullptr;
+		rdp::k_bin<<<dim3((L->num_prims * 32 + 255) / 256, prim_pairs ? 1u : bin_split(L)), 256, 0, stream>>>(
+			L->num_prims, L->geom, L->shade, L->passes, L->tile_counts, prim_pairs);
 		// Span rows only when the pair path follows (k_scan resets their counter).
 		if (L->num_tile_items && L->spans)
 		{

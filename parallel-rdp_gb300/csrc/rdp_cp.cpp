@@ -2242,7 +2242,7 @@ bool rdp_batch::reserve_for_capture()
 				{
 					const uint32_t tt = pv.target[t].tiles_x * pv.target[t].tiles_y;
 					tiles += tt;
-					mask_words += size_t(tt) * ((pv.target_prims[t] + 31) / 32);
+					mask_words += size_t(tt) * RDP_MASK_WORDS(pv.target_prims[t]);
 				}
 			}
 		need.passes = std::max(need.passes, uint32_t(views.size()));

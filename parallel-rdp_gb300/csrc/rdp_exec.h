@@ -398,11 +398,22 @@ struct Executor
 		return sched_buffers(caps.tile_items) && sched_prim_buffers(caps.prims);
 	}
 
+	// While a capture is being recorded, buffers that growth replaces stay allocated: the launches
+	// recorded before the growth point into them.  The graph takes them and frees them when it is
+	// destroyed.
+	std::vector<void *> *retired = nullptr;
+	void release(void *p)
+	{
+		if (!p) return;
+		if (retired) retired->push_back(p);
+		else cudaFree(p);
+	}
+
 	uint32_t sched_prim_capacity = 0;
 	bool sched_prim_buffers(uint32_t n)
 	{
 		if (!sched_ready || n <= sched_prim_capacity) return true;
-		cudaFree(sched.featbits);
+		release(sched.featbits);
 		sched.featbits = nullptr;
 		if (check(cudaMalloc(&sched.featbits, sizeof(uint16_t) * size_t(n)))) return false;
 		sched_prim_capacity = n;
@@ -413,9 +424,9 @@ struct Executor
 	bool sched_buffers(uint32_t n)
 	{
 		if (!sched_ready || n <= sched_capacity) return true;
-		cudaFree(sched.features);
-		cudaFree(sched.pred);
-		cudaFree(sched.bucket);
+		release(sched.features);
+		release(sched.pred);
+		release(sched.bucket);
 		sched.features = nullptr;
 		sched.pred = nullptr;
 		sched.bucket = nullptr;
@@ -675,13 +686,13 @@ struct Executor
 		if (grow_prims)
 		{
 			uint32_t n = std::max(need.prims, caps.prims * 2);
-			cudaFree(d_geom);
-			cudaFree(d_attr);
-			cudaFree(d_shade);
-			cudaFree(d_prim_pairs);
-			cudaFree(d_prim_offsets);
-			cudaFree(d_prim_blocks);
-			cudaFree(d_prim_rows);
+			release(d_geom);
+			release(d_attr);
+			release(d_shade);
+			release(d_prim_pairs);
+			release(d_prim_offsets);
+			release(d_prim_blocks);
+			release(d_prim_rows);
 			d_geom = nullptr;
 			d_attr = nullptr;
 			d_shade = nullptr;
@@ -697,12 +708,12 @@ struct Executor
 		if (grow_tiles)
 		{
 			uint32_t n = std::max(need.tile_items, caps.tile_items + caps.tile_items / 2);
-			cudaFree(d_tile_counts);
-			cudaFree(d_pair_offsets);
-			cudaFree(d_tile_order);
-			cudaFree(d_tile_cycles);
-			cudaFree(d_nonempty);
-			cudaFree(d_scan_blocks);
+			release(d_tile_counts);
+			release(d_pair_offsets);
+			release(d_tile_order);
+			release(d_tile_cycles);
+			release(d_nonempty);
+			release(d_scan_blocks);
 			d_tile_counts = d_pair_offsets = d_tile_order = d_tile_cycles = d_nonempty = d_scan_blocks = nullptr;
 			if (check(cudaMalloc(&d_tile_counts, size_t(n + 1) * 4)) || check(cudaMalloc(&d_pair_offsets, size_t(n + 1) * 4)) ||
 			    check(cudaMalloc(&d_tile_order, size_t(n) * 4)) || check(cudaMalloc(&d_tile_cycles, size_t(n) * 4)) ||
@@ -719,7 +730,7 @@ struct Executor
 			// The tiles' primitive bitmasks, laid out per launch (each pass's tiles with its own word
 			// count); self-clearing between launches, so they start at zero.
 			size_t n = std::max(need.mask_words, caps.mask_words + caps.mask_words / 2);
-			cudaFree(d_masks);
+			release(d_masks);
 			d_masks = nullptr;
 			if (check(cudaMalloc(&d_masks, n * 4)) || check(cudaMemsetAsync(d_masks, 0, n * 4, stream))) return false;
 			caps.mask_words = n;
@@ -728,7 +739,7 @@ struct Executor
 		if (grow_uploads)
 		{
 			uint32_t n = std::max(need.uploads, caps.uploads + caps.uploads / 2);
-			cudaFree(d_tmem_keep);
+			release(d_tmem_keep);
 			d_tmem_keep = nullptr;
 			if (check(cudaMalloc(&d_tmem_keep, size_t(n) * 64 * 4))) return false;
 			caps.uploads = n;
@@ -736,9 +747,9 @@ struct Executor
 		if (grow_pairs)
 		{
 			uint32_t n = std::max(need.pairs, caps.pairs * 2);
-			cudaFree(d_pairs);
-			cudaFree(d_shade_list);
-			cudaFree(d_scratch);
+			release(d_pairs);
+			release(d_shade_list);
+			release(d_scratch);
 			d_pairs = nullptr;
 			d_shade_list = nullptr;
 			d_scratch = nullptr;
@@ -750,7 +761,7 @@ struct Executor
 		if (grow_spans)
 		{
 			uint32_t n = std::max(need.span_rows, caps.span_rows + caps.span_rows / 2);
-			cudaFree(d_spans);
+			release(d_spans);
 			d_spans = nullptr;
 			if (check(cudaMalloc(&d_spans, size_t(n) * RDP_SPAN_ROW_BYTES))) return false;
 			caps.span_rows = n;
@@ -758,7 +769,7 @@ struct Executor
 		if (grow_staging)
 		{
 			size_t n = std::max(need.staging, caps.staging + caps.staging / 2);
-			cudaFree(d_staging);
+			release(d_staging);
 			d_staging = nullptr;
 			if (check(cudaMalloc(&d_staging, kStagingSlots * n))) return false;
 			caps.staging = n;
@@ -827,7 +838,7 @@ struct Executor
 			{
 				const uint32_t tt = v[i].target[t].tiles_x * v[i].target[t].tiles_y;
 				tiles += tt;
-				mask_words += size_t(tt) * ((v[i].target_prims[t] + 31) / 32);
+				mask_words += size_t(tt) * RDP_MASK_WORDS(v[i].target_prims[t]);
 			}
 		}
 		need.passes = std::max(need.passes, n);
@@ -839,7 +850,10 @@ struct Executor
 		need.pairs = std::max(need.pairs, initial_pairs);
 		need.span_rows = std::max(need.span_rows, initial_span_rows);
 		need.staging = std::max(need.staging, staging_bytes_for(v, n));
-		if (!ensure(need)) return false;
+		retired = cap ? &cap->buffers : nullptr;
+		const bool grown = ensure(need);
+		retired = nullptr;
+		if (!grown) return false;
 
 		Staging *stp = take_staging(staging_bytes_for(v, n));
 		if (!stp) return false;
@@ -904,7 +918,7 @@ struct Executor
 				p.upload_begin = up_base;
 				p.upload_count = t == 0 ? v[i].num_uploads : 0;
 				p.tile_item_begin = tile_base;
-				p.mask_words = (p.prim_count + 31) / 32;
+				p.mask_words = RDP_MASK_WORDS(p.prim_count);
 				p.masks = d_masks + mask_base;
 				passes[d] = p;
 				if (t == 0 && v[i].num_uploads) tmem_list[num_tmem++] = d;

@@ -3048,7 +3048,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(uint32_t num_items, 
 // With `list`, also places each pair in primitive-major order: list[prim_offsets[prim] + n] =
 // {primitive, tx | ty << 16, pair index, pass}, n counted by prim_cursor (zeroed by k_scan_down);
 // the order of one primitive's tiles is arbitrary, which changes no result.
-__global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes, uint32_t num_items,
+// A warp step covers 128 bitmask words: each lane loads one 16-byte group.
+__global__ void __launch_bounds__(256) k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes, uint32_t num_items,
                          const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ ctrl, uint2 *__restrict__ pairs,
                          const uint16_t *__restrict__ featbits, float *__restrict__ features, bool train,
                          const uint32_t *__restrict__ prim_offsets, uint32_t *__restrict__ prim_cursor,
@@ -3057,11 +3058,11 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 	uint32_t item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
 	int lane = threadIdx.x & 31;
 	if (item >= num_items || ctrl[1]) return;
-	const uint32_t pi = pass_of_item(passes, num_passes, item);
+	const uint32_t pi = pass_of_item_warp(passes, num_passes, item, lane);
 	const RdpPass &ps = passes[pi];
 	uint32_t tl = item - ps.tile_item_begin;
-	uint32_t *masks = ps.masks + size_t(tl) * ps.mask_words;
-	uint32_t nwords = (ps.prim_count + 31) / 32;
+	uint4 *masks = reinterpret_cast<uint4 *>(ps.masks + size_t(tl) * ps.mask_words);
+	const uint32_t ngroups = (ps.prim_count + 127) / 128; // 16-byte groups holding bits
 	uint32_t out = offsets[item];
 	const uint32_t npairs = offsets[item + 1] - out;
 	if (!npairs) return;
@@ -3071,11 +3072,11 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 	for (int i = 0; i < RDP_FEAT_COUNT; i++) fc[i] = 0;
 	// Without training, only tiles the model evaluates need features.
 	if (featbits && !train && npairs < RDP_SCHED_MIN_PAIRS) featbits = nullptr;
-	for (uint32_t base = 0; base < nwords; base += 32)
+	for (uint32_t base = 0; base < ngroups; base += 32)
 	{
-		uint32_t wi = base + lane;
-		uint32_t wv = wi < nwords ? masks[wi] : 0u;
-		uint32_t c = __popc(wv);
+		const uint32_t gi = base + uint32_t(lane);
+		const uint4 g = gi < ngroups ? masks[gi] : make_uint4(0u, 0u, 0u, 0u);
+		const uint32_t c = __popc(g.x) + __popc(g.y) + __popc(g.z) + __popc(g.w);
 		uint32_t x = c;
 #pragma unroll
 		for (int o = 1; o < 32; o <<= 1)
@@ -3084,14 +3085,17 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 			if (lane >= o) x += y;
 		}
 		uint32_t pos = out + x - c;
-		if (wv)
+		out += __shfl_sync(0xffffffffu, x, 31);
+		if (!c) continue;
+		masks[gi] = make_uint4(0u, 0u, 0u, 0u);
+		for (int k = 0; k < 4; k++)
 		{
-			masks[wi] = 0u;
+			uint32_t wv = k == 0 ? g.x : k == 1 ? g.y : k == 2 ? g.z : g.w;
 			while (wv)
 			{
-				int b = __ffs(wv) - 1;
+				const int b = __ffs(wv) - 1;
 				wv &= wv - 1;
-				const uint32_t prim = ps.prim_begin + wi * 32 + uint32_t(b);
+				const uint32_t prim = ps.prim_begin + (gi * 4 + uint32_t(k)) * 32 + uint32_t(b);
 				if (list) list[prim_offsets[prim] + atomicAdd(&prim_cursor[prim], 1u)] = make_uint4(prim, tile_xy, pos, pi);
 				pairs[pos++] = make_uint2(prim, item);
 				if (featbits)
@@ -3102,7 +3106,6 @@ __global__ void k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes
 				}
 			}
 		}
-		out += __shfl_sync(0xffffffffu, x, 31);
 	}
 	if (featbits)
 	{

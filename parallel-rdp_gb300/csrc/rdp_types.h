@@ -24,6 +24,9 @@
 #define RDP_TILE_H 8
 #define RDP_MAX_PRIMS_PER_PASS 65536
 #define RDP_MAX_UPLOADS_PER_PASS 16384
+/* 32-bit words of one tile's primitive bitmask for a pass of `prims` primitives: one bit per
+ * primitive, padded to whole 16-byte groups (k_expand reads a bitmask four words at a time). */
+#define RDP_MASK_WORDS(prims) ((((prims) + 127u) >> 7) << 2)
 #define RDP_MAX_TILES_X 128
 #define RDP_MAX_TILES_Y 128
 #define RDP_STATE_BLOCK_WORDS 32
@@ -215,7 +218,7 @@ typedef struct __attribute__((aligned(16))) RdpPass
 	   hidden_size bytes), fb_width / fb_height the scaled image.  Bit 8: record the super-sampled
 	   write mask (2 bits per native pixel, after the slices). */
 	uint32_t scale;
-	uint32_t mask_words; /* 32-bit words of a tile's primitive bitmask: ceil(prim_count / 32) */
+	uint32_t mask_words; /* 32-bit words of a tile's primitive bitmask: RDP_MASK_WORDS(prim_count) */
 	unsigned long long *counters; /* the instance's [0] fragments, [1] touched tiles, [2] tile instances */
 	uint32_t *wmask;              /* the instance's RDRAM write mask (1 bit per byte), or null */
 } RdpPass;

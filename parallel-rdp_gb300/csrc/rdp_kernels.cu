@@ -3048,7 +3048,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(uint32_t num_items, 
 // With `list`, also places each pair in primitive-major order: list[prim_offsets[prim] + n] =
 // {primitive, tx | ty << 16, pair index, pass}, n counted by prim_cursor (zeroed by k_scan_down);
 // the order of one primitive's tiles is arbitrary, which changes no result.
-// A warp step covers 128 bitmask words: each lane loads one 16-byte group.
+// A warp step covers 128 bitmask words: each lane holds one 16-byte group and loads the next
+// step's ahead.  The primitive-major slots (an atomic each) and the features are taken in a
+// second loop over the tile's pairs just written, lanes in parallel, so no atomic waits in the
+// bitmask walk.
 __global__ void __launch_bounds__(256) k_expand(const RdpPass *__restrict__ passes, uint32_t num_passes, uint32_t num_items,
                          const uint32_t *__restrict__ offsets, const uint32_t *__restrict__ ctrl, uint2 *__restrict__ pairs,
                          const uint16_t *__restrict__ featbits, float *__restrict__ features, bool train,
@@ -3063,19 +3066,17 @@ __global__ void __launch_bounds__(256) k_expand(const RdpPass *__restrict__ pass
 	uint32_t tl = item - ps.tile_item_begin;
 	uint4 *masks = reinterpret_cast<uint4 *>(ps.masks + size_t(tl) * ps.mask_words);
 	const uint32_t ngroups = (ps.prim_count + 127) / 128; // 16-byte groups holding bits
-	uint32_t out = offsets[item];
-	const uint32_t npairs = offsets[item + 1] - out;
+	const uint32_t first = offsets[item];
+	const uint32_t npairs = offsets[item + 1] - first;
 	if (!npairs) return;
 	const uint32_t tile_xy = (tl % ps.tiles_x) | ((tl / ps.tiles_x) << 16); // tx | ty << 16
-	uint32_t fc[RDP_FEAT_COUNT];
-#pragma unroll
-	for (int i = 0; i < RDP_FEAT_COUNT; i++) fc[i] = 0;
-	// Without training, only tiles the model evaluates need features.
-	if (featbits && !train && npairs < RDP_SCHED_MIN_PAIRS) featbits = nullptr;
+	const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+	uint32_t out = first;
+	uint4 g = uint32_t(lane) < ngroups ? masks[lane] : zero;
 	for (uint32_t base = 0; base < ngroups; base += 32)
 	{
 		const uint32_t gi = base + uint32_t(lane);
-		const uint4 g = gi < ngroups ? masks[gi] : make_uint4(0u, 0u, 0u, 0u);
+		const uint4 gn = gi + 32 < ngroups ? masks[gi + 32] : zero;
 		const uint32_t c = __popc(g.x) + __popc(g.y) + __popc(g.z) + __popc(g.w);
 		uint32_t x = c;
 #pragma unroll
@@ -3086,25 +3087,38 @@ __global__ void __launch_bounds__(256) k_expand(const RdpPass *__restrict__ pass
 		}
 		uint32_t pos = out + x - c;
 		out += __shfl_sync(0xffffffffu, x, 31);
-		if (!c) continue;
-		masks[gi] = make_uint4(0u, 0u, 0u, 0u);
-		for (int k = 0; k < 4; k++)
+		if (c)
 		{
-			uint32_t wv = k == 0 ? g.x : k == 1 ? g.y : k == 2 ? g.z : g.w;
-			while (wv)
+			masks[gi] = zero;
+			for (int k = 0; k < 4; k++)
 			{
-				const int b = __ffs(wv) - 1;
-				wv &= wv - 1;
-				const uint32_t prim = ps.prim_begin + (gi * 4 + uint32_t(k)) * 32 + uint32_t(b);
-				if (list) list[prim_offsets[prim] + atomicAdd(&prim_cursor[prim], 1u)] = make_uint4(prim, tile_xy, pos, pi);
-				pairs[pos++] = make_uint2(prim, item);
-				if (featbits)
+				uint32_t wv = k == 0 ? g.x : k == 1 ? g.y : k == 2 ? g.z : g.w;
+				while (wv)
 				{
-					const uint32_t fb = featbits[prim];
-#pragma unroll
-					for (int i = 0; i < RDP_FEAT_COUNT; i++) fc[i] += (fb >> i) & 1u;
+					const int b = __ffs(wv) - 1;
+					wv &= wv - 1;
+					pairs[pos++] = make_uint2(ps.prim_begin + (gi * 4 + uint32_t(k)) * 32 + uint32_t(b), item);
 				}
 			}
+		}
+		g = gn;
+	}
+	// Without training, only tiles the model evaluates need features.
+	if (featbits && !train && npairs < RDP_SCHED_MIN_PAIRS) featbits = nullptr;
+	if (!list && !featbits) return;
+	__syncwarp(); // the lanes' pair entries are visible to the whole warp
+	uint32_t fc[RDP_FEAT_COUNT];
+#pragma unroll
+	for (int i = 0; i < RDP_FEAT_COUNT; i++) fc[i] = 0;
+	for (uint32_t p = first + uint32_t(lane); p < first + npairs; p += 32)
+	{
+		const uint32_t prim = pairs[p].x;
+		if (list) list[prim_offsets[prim] + atomicAdd(&prim_cursor[prim], 1u)] = make_uint4(prim, tile_xy, p, pi);
+		if (featbits)
+		{
+			const uint32_t fb = featbits[prim];
+#pragma unroll
+			for (int i = 0; i < RDP_FEAT_COUNT; i++) fc[i] += (fb >> i) & 1u;
 		}
 	}
 	if (featbits)

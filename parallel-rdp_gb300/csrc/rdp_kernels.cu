@@ -708,53 +708,75 @@ __device__ bool bin_primitive(const RdpPrimGeom &g, int lox, int loy, int hix, i
 	return rx0 <= rx1;
 }
 
-// With `prim_pairs`, also writes each primitive's number of binned tiles (its pairs).  Without it
-// the grid's y dimension may split a primitive's tiles over several warps (launches of a few large
-// primitives, such as a frame's clears): warp k of a primitive takes its tiles k*32 .. k*32+31,
-// then every 32*gridDim.y-th further.
-__global__ void k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom, const RdpPrimShade *__restrict__ shade,
-                      const RdpPass *__restrict__ passes, uint32_t *__restrict__ tile_counts,
-                      uint32_t *__restrict__ prim_pairs)
+// Bins one primitive into the tiles t = t_begin, t_begin + t_step, ... of its tile box: sets its
+// bit in each covered tile's bitmask and counts the tile's pairs.  Returns the tiles binned.
+__device__ __forceinline__ uint32_t bin_tiles(const RdpPrimGeom &g, const RdpPass &pass, uint32_t prim,
+                                              uint32_t *__restrict__ tile_counts, int t_begin, int t_step)
 {
-	uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	uint32_t lane = threadIdx.x & 31;
-	if (warp >= num_prims) return;
-	const RdpPrimGeom g = geom[warp];
-	if (g.bbox[2] < g.bbox[0] || g.bbox[3] < g.bbox[1])
-	{
-		if (prim_pairs && lane == 0) prim_pairs[warp] = 0u;
-		return;
-	}
-	const RdpPass &pass = passes[shade[warp].pass];
-	uint32_t local = warp - pass.prim_begin;
-	uint32_t bit = 1u << (local & 31);
-	uint32_t word = local >> 5;
-	int tw = g.bbox[2] - g.bbox[0] + 1, th = g.bbox[3] - g.bbox[1] + 1;
-	int count = tw * th;
-	int fbw = int(pass.fb_width), fbh = int(pass.fb_height);
+	const uint32_t local = prim - pass.prim_begin;
+	const uint32_t bit = 1u << (local & 31);
+	const uint32_t word = local >> 5;
+	const int tw = g.bbox[2] - g.bbox[0] + 1, count = tw * (g.bbox[3] - g.bbox[1] + 1);
+	const int fbw = int(pass.fb_width), fbh = int(pass.fb_height);
 	const int sl = int(pass.scale & 3u);
 	uint32_t binned = 0;
-	for (int t0 = int(blockIdx.y) * 32; t0 < count; t0 += 32 * int(gridDim.y))
+	for (int t = t_begin; t < count; t += t_step)
 	{
-		const int t = t0 + int(lane);
-		bool hit = false;
-		if (t < count)
+		const int tx = g.bbox[0] + t % tw, ty = g.bbox[1] + t / tw;
+		const int lox = tx * 8, loy = ty * 8;
+		const int hix = min(lox + 7, fbw - 1), hiy = min(loy + 7, fbh - 1);
+		if (bin_primitive(g, lox, loy, hix, hiy, sl))
 		{
-			int tx = g.bbox[0] + t % tw, ty = g.bbox[1] + t / tw;
-			int lox = tx * 8, loy = ty * 8;
-			int hix = min(lox + 7, fbw - 1), hiy = min(loy + 7, fbh - 1);
-			hit = bin_primitive(g, lox, loy, hix, hiy, sl);
-			if (hit)
-			{
-				uint32_t tl = uint32_t(ty) * pass.tiles_x + uint32_t(tx);
-				atomicOr(&pass.masks[size_t(tl) * pass.mask_words + word], bit);
-				// Upscaled and fill-only launches render from the bitmasks alone (no pair list).
-				if (tile_counts) atomicAdd(&tile_counts[pass.tile_item_begin + tl], 1u);
-			}
+			const uint32_t tl = uint32_t(ty) * pass.tiles_x + uint32_t(tx);
+			atomicOr(&pass.masks[size_t(tl) * pass.mask_words + word], bit);
+			// Upscaled and fill-only launches render from the bitmasks alone (no pair list).
+			if (tile_counts) atomicAdd(&tile_counts[pass.tile_item_begin + tl], 1u);
+			binned++;
 		}
-		binned += __popc(__ballot_sync(0xffffffffu, hit));
 	}
-	if (prim_pairs && lane == 0) prim_pairs[warp] = binned;
+	return binned;
+}
+
+// One thread per primitive: a primitive whose tile box holds at most BIN_LANE_TILES tiles is
+// binned by its own lane; larger ones are binned afterwards by the whole warp, one after another,
+// the lanes striding over the box.  With `prim_pairs`, also writes each primitive's number of
+// binned tiles (its pairs).  Without it the grid's y dimension may split a large primitive's box
+// over several warps (launches of a few large primitives, such as a frame's clears): warp k takes
+// tiles k*32 + lane, then every 32*gridDim.y-th further.
+constexpr int BIN_LANE_TILES = 16;
+
+__global__ void __launch_bounds__(256) k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom,
+                                            const RdpPrimShade *__restrict__ shade, const RdpPass *__restrict__ passes,
+                                            uint32_t *__restrict__ tile_counts, uint32_t *__restrict__ prim_pairs)
+{
+	const uint32_t prim = blockIdx.x * blockDim.x + threadIdx.x;
+	const int lane = int(threadIdx.x & 31);
+	const uint32_t warp_first = prim - uint32_t(lane);
+	if (warp_first >= num_prims) return; // the whole warp
+	int count = 0;
+	uint32_t binned = 0;
+	if (prim < num_prims)
+	{
+		const RdpPrimGeom g = geom[prim];
+		if (g.bbox[2] >= g.bbox[0] && g.bbox[3] >= g.bbox[1])
+			count = (g.bbox[2] - g.bbox[0] + 1) * (g.bbox[3] - g.bbox[1] + 1);
+		if (count > 0 && count <= BIN_LANE_TILES && blockIdx.y == 0)
+			binned = bin_tiles(g, passes[shade[prim].pass], prim, tile_counts, 0, 1);
+	}
+	unsigned big = __ballot_sync(0xffffffffu, count > BIN_LANE_TILES);
+	while (big)
+	{
+		const int src = __ffs(big) - 1;
+		big &= big - 1;
+		const uint32_t bp = warp_first + uint32_t(src);
+		const RdpPrimGeom g = geom[bp];
+		uint32_t n = bin_tiles(g, passes[shade[bp].pass], bp, tile_counts, int(blockIdx.y) * 32 + lane,
+		                       32 * int(gridDim.y));
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+		if (lane == src) binned = n;
+	}
+	if (prim_pairs && prim < num_prims) prim_pairs[prim] = binned;
 }
 
 // ============================================================================ k_span
@@ -4281,12 +4303,13 @@ static bool multi_cta_scan(const RdpLaunch *L)
 	                          (L->shade_list && L->prim_scan_blocks && L->num_prims > RDP_SCAN_SINGLE_CTA_MAX));
 }
 
-// Warps per primitive in k_bin (its grid's y dimension) when no per-primitive count is taken: a
-// launch of few primitives still fills the GPU.
+// Warps that share each large primitive's tile box in k_bin (its grid's y dimension) when no
+// per-primitive count is taken: a launch of few primitives still fills the GPU.
 static uint32_t bin_split(const RdpLaunch *L)
 {
 	const uint32_t target = std::max<uint32_t>(L->num_sms, 1u) * 32u;
-	return std::min<uint32_t>(std::max<uint32_t>(target / std::max<uint32_t>(L->num_prims, 1u), 1u), 64u);
+	const uint32_t warps = std::max<uint32_t>((L->num_prims + 31) / 32, 1u);
+	return std::min<uint32_t>(std::max<uint32_t>(target / warps, 1u), 1024u);
 }
 
 extern "C" uint32_t rdp_kernels_count(const RdpLaunch *L)
@@ -4322,7 +4345,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 			                                                                   L->state_blocks, L->passes,
 			                                                                   L->num_passes, L->geom, L->attr,
 			                                                                   L->shade, nullptr);
-			rdp::k_bin<<<dim3((L->num_prims * 32 + 255) / 256, bin_split(L)), 256, 0, stream>>>(
+			rdp::k_bin<<<dim3((L->num_prims + 255) / 256, bin_split(L)), 256, 0, stream>>>(
 				L->num_prims, L->geom, L->shade, L->passes, nullptr, nullptr);
 		}
 		if (L->num_tmem_passes)
@@ -4347,7 +4370,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 			                                                                   L->state_blocks, L->passes,
 			                                                                   L->num_passes, L->geom, L->attr,
 			                                                                   L->shade, nullptr);
-			rdp::k_bin<<<dim3((L->num_prims * 32 + 255) / 256, bin_split(L)), 256, 0, stream>>>(
+			rdp::k_bin<<<dim3((L->num_prims + 255) / 256, bin_split(L)), 256, 0, stream>>>(
 				L->num_prims, L->geom, L->shade, L->passes, nullptr, nullptr);
 		}
 		if (L->num_tmem_passes)
@@ -4374,7 +4397,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		                                                                       ? L->sched->featbits
 		                                                                       : nullptr);
 		uint32_t *prim_pairs = L->shade_list && L->num_tile_items ? L->prim_pairs : nullptr;
-		rdp::k_bin<<<dim3((L->num_prims * 32 + 255) / 256, prim_pairs ? 1u : bin_split(L)), 256, 0, stream>>>(
+		rdp::k_bin<<<dim3((L->num_prims + 255) / 256, prim_pairs ? 1u : bin_split(L)), 256, 0, stream>>>(
 			L->num_prims, L->geom, L->shade, L->passes, L->tile_counts, prim_pairs);
 		// Span rows only when the pair path follows (k_scan resets their counter).
 		if (L->num_tile_items && L->spans)

@@ -11,7 +11,9 @@
  *                the reference's masked copy);
  *   k_coh_out -- when a timeline value is signalled: the bytes the GPU wrote go to the host, the
  *                others are left alone (the reference's masked read-back), and the mask is cleared.
- * One CTA per page, one thread per 32 bytes (one mask word).
+ * One CTA per page; thread t moves bytes 16t .. 16t+15 of each 2 KiB half of the page, so that one
+ * warp instruction covers 512 contiguous bytes of the link (whole 32-byte sectors, each read or
+ * written once).
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -21,9 +23,11 @@
 
 namespace {
 
-constexpr int kThreads = RDP_RDRAM_PAGE_BYTES / 32;
+constexpr int kThreads = 128;
+constexpr uint32_t kHalf = kThreads * 16; // bytes of a page one CTA instruction covers
+static_assert(RDP_RDRAM_PAGE_BYTES == 2 * kHalf, "two 16-byte pieces per thread and page");
 
-// Byte mask (0xff per selected byte) of the 4 bytes of word k of a 32-byte line from its mask bits.
+// Byte mask (0xff per selected byte) of the 4 bytes of word k of a 16-byte piece from its mask bits.
 __device__ __forceinline__ uint32_t byte_mask(uint32_t m, int k)
 {
 	const uint32_t b = (m >> (4 * k)) & 15u;
@@ -31,79 +35,96 @@ __device__ __forceinline__ uint32_t byte_mask(uint32_t m, int k)
 	       ((b & 8u) ? 0xff000000u : 0u);
 }
 
-__device__ __forceinline__ void locate(const RdpCohList &L, uint32_t &inst, size_t &off)
+// Instance slot and byte offset of this CTA's page.
+__device__ __forceinline__ void locate(const RdpCohList &L, uint32_t &inst, size_t &page)
 {
 	const uint32_t e = L.entry[blockIdx.x];
 	inst = e >> 24;
-	off = size_t(e & 0xffffffu) * RDP_RDRAM_PAGE_BYTES + threadIdx.x * 32u;
+	page = size_t(e & 0xffffffu) * RDP_RDRAM_PAGE_BYTES;
+}
+
+// The 16 mask bits of the piece at byte offset `off` (a multiple of 16).
+__device__ __forceinline__ uint32_t piece_mask(const uint32_t *wmask, size_t off)
+{
+	return (wmask[off >> 5] >> (off & 16u)) & 0xffffu;
 }
 
 __global__ void __launch_bounds__(kThreads) k_coh_in(const RdpCohList L)
 {
 	uint32_t inst;
-	size_t off;
-	locate(L, inst, off);
-	const uint32_t m = L.wmask[inst][off >> 5];
-	if (m == 0xffffffffu) return; // every byte of the line is the GPU's
-	const uint8_t *h = L.host[inst] + off;
-	uint8_t *d = L.dev[inst] + off;
-	if ((L.host_aligned >> inst) & 1u)
-	{
-		// Host bytes: fetched again on every access (__ldcv), never from a cached line.
-		uint4 hv[2] = { __ldcv(reinterpret_cast<const uint4 *>(h)), __ldcv(reinterpret_cast<const uint4 *>(h + 16)) };
-		if (m)
-		{
-			const uint4 *dv = reinterpret_cast<const uint4 *>(d);
-			uint4 cur[2] = { dv[0], dv[1] };
-			uint32_t *hw = reinterpret_cast<uint32_t *>(hv);
-			const uint32_t *cw = reinterpret_cast<const uint32_t *>(cur);
+	size_t page;
+	locate(L, inst, page);
+	const bool aligned = (L.host_aligned >> inst) & 1u;
 #pragma unroll
-			for (int k = 0; k < 8; k++)
-			{
-				const uint32_t bm = byte_mask(m, k);
-				hw[k] = (cw[k] & bm) | (hw[k] & ~bm);
-			}
-		}
-		reinterpret_cast<uint4 *>(d)[0] = hv[0];
-		reinterpret_cast<uint4 *>(d)[1] = hv[1];
-	}
-	else
+	for (int half = 0; half < 2; half++)
 	{
-		for (int b = 0; b < 32; b++)
-			if (!((m >> b) & 1u)) d[b] = __ldcv(reinterpret_cast<const unsigned char *>(h) + b);
+		const size_t off = page + half * kHalf + threadIdx.x * 16u;
+		const uint32_t m = piece_mask(L.wmask[inst], off);
+		if (m == 0xffffu) continue; // every byte of the piece is the GPU's
+		const uint8_t *h = L.host[inst] + off;
+		uint8_t *d = L.dev[inst] + off;
+		if (aligned)
+		{
+			// Host bytes: fetched again on every access (__ldcv), never from a cached line.
+			uint4 hv = __ldcv(reinterpret_cast<const uint4 *>(h));
+			if (m)
+			{
+				const uint4 cur = *reinterpret_cast<const uint4 *>(d);
+				hv.x = (cur.x & byte_mask(m, 0)) | (hv.x & ~byte_mask(m, 0));
+				hv.y = (cur.y & byte_mask(m, 1)) | (hv.y & ~byte_mask(m, 1));
+				hv.z = (cur.z & byte_mask(m, 2)) | (hv.z & ~byte_mask(m, 2));
+				hv.w = (cur.w & byte_mask(m, 3)) | (hv.w & ~byte_mask(m, 3));
+			}
+			*reinterpret_cast<uint4 *>(d) = hv;
+		}
+		else
+		{
+			for (int b = 0; b < 16; b++)
+				if (!((m >> b) & 1u)) d[b] = __ldcv(reinterpret_cast<const unsigned char *>(h) + b);
+		}
 	}
 }
 
 __global__ void __launch_bounds__(kThreads) k_coh_out(const RdpCohList L)
 {
 	uint32_t inst;
-	size_t off;
-	locate(L, inst, off);
-	uint32_t *mw = L.wmask[inst] + (off >> 5);
-	const uint32_t m = *mw;
-	if (!m) return;
-	const uint8_t *d = L.dev[inst] + off;
-	uint8_t *h = L.host[inst] + off;
-	if (m == 0xffffffffu && ((L.host_aligned >> inst) & 1u))
+	size_t page;
+	locate(L, inst, page);
+	const bool aligned = (L.host_aligned >> inst) & 1u;
+	uint32_t *wmask = L.wmask[inst];
+#pragma unroll
+	for (int half = 0; half < 2; half++)
 	{
-		// Host bytes: written through to the caller's memory (__stwt).
-		__stwt(reinterpret_cast<uint4 *>(h), reinterpret_cast<const uint4 *>(d)[0]);
-		__stwt(reinterpret_cast<uint4 *>(h) + 1, reinterpret_cast<const uint4 *>(d)[1]);
-	}
-	else
-	{
-		const uint32_t *dw = reinterpret_cast<const uint32_t *>(d);
-		for (int k = 0; k < 8; k++)
+		const size_t off = page + half * kHalf + threadIdx.x * 16u;
+		const uint32_t m = piece_mask(wmask, off);
+		if (m)
 		{
-			const uint32_t nib = (m >> (4 * k)) & 15u;
-			if (nib == 15u && ((L.host_aligned >> inst) & 1u))
-				__stwt(reinterpret_cast<unsigned int *>(h) + k, dw[k]);
+			const uint8_t *d = L.dev[inst] + off;
+			uint8_t *h = L.host[inst] + off;
+			if (m == 0xffffu && aligned)
+			{
+				// Host bytes: written through to the caller's memory (__stwt).
+				__stwt(reinterpret_cast<uint4 *>(h), *reinterpret_cast<const uint4 *>(d));
+			}
 			else
-				for (int b = 0; b < 4; b++)
-					if ((nib >> b) & 1u) __stwt(reinterpret_cast<unsigned char *>(h) + 4 * k + b, d[4 * k + b]);
+			{
+				const uint32_t *dw = reinterpret_cast<const uint32_t *>(d);
+				for (int k = 0; k < 4; k++)
+				{
+					const uint32_t nib = (m >> (4 * k)) & 15u;
+					if (nib == 15u && aligned)
+						__stwt(reinterpret_cast<unsigned int *>(h) + k, dw[k]);
+					else
+						for (int b = 0; b < 4; b++)
+							if ((nib >> b) & 1u) __stwt(reinterpret_cast<unsigned char *>(h) + 4 * k + b, d[4 * k + b]);
+				}
+			}
 		}
+		// The mask word covers this piece and its neighbour's (thread t ^ 1, same warp): both have
+		// read it before the even thread clears it.
+		const uint32_t pair = m | __shfl_xor_sync(0xffffffffu, m, 1);
+		if (!(threadIdx.x & 1u) && pair) wmask[off >> 5] = 0u;
 	}
-	*mw = 0u;
 }
 
 } // namespace

@@ -4001,9 +4001,8 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const RdpPass *__rest
 // RdpLaunch.fill_only).  A pixel takes the fill colour wherever x lies in its row's span
 // (shading.h:55-62 with the fill branch of memory_interfacing.h:381-571), so only the x extent of
 // each row is set up and no shading record is built.  One warp per 8x8 tile, independent of the
-// CTA's other warps: lane l owns pixels (l % 8, l / 8) and (l % 8, l / 8 + 4) of the tile, both
-// loaded as the tile's bitmask is read (a pixel without fills stores nothing), and the warp alone
-// clears the bitmask words it consumed.
+// CTA's other warps: lane l owns pixels (l % 8, l / 8) and (l % 8, l / 8 + 4) of the tile, and the
+// warp alone clears the bitmask words it consumed.
 constexpr int FILL_THREADS = 256;
 
 __global__ void __launch_bounds__(FILL_THREADS) k_fill(const RdpPass *__restrict__ passes, uint32_t num_passes,
@@ -4046,10 +4045,15 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill(const RdpPass *__restrict
 	const uint32_t di0 = depth_index + ps.fb_width * uint32_t(y0) + uint32_t(px_x);
 	const uint32_t ci1 = ci0 + 4u * ps.fb_width, di1 = di0 + 4u * ps.fb_width;
 
+	// The fill pipe sets every stored field of a pixel from the fill colour alone (colour, coverage
+	// bits, the aliased depth) and a pixel no fill covers is not stored, so nothing is loaded.
 	Pix p0, p1;
+	p0.cidx = ci0;
+	p1.cidx = ci1;
 	p0.cdirty = p0.ddirty = p1.cdirty = p1.ddirty = false;
-	if (in0) load_pixel(ps, p0, ci0, di0);
-	if (in1) load_pixel(ps, p1, ci1, di1);
+	p0.depth = p0.dz = p1.depth = p1.dz = 0;
+#pragma unroll
+	for (int c = 0; c < 4; c++) p0.col[c] = p1.col[c] = 0;
 	uint32_t frags = 0;
 	bool any = false;
 	for (uint32_t base = 0; base < nwords; base += 32)

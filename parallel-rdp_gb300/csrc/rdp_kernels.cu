@@ -1189,27 +1189,13 @@ __global__ void k_tmem_apply(const RdpPass *__restrict__ passes, const uint32_t 
 
 // Phase 2: carry the previous snapshot's value through uploads that did not write a word
 // (tmem_update.comp:546-576: instance i+1 = instance i with upload i applied).  One CTA per
-// (pass, 32 TMEM words); its TMEM_CARRY_WARPS warps split the uploads into chunks: each
-// warp finds the last value its chunk writes, the chunks' carry-ins are chained in shared
-// memory, then every warp fills its chunk.  A warp takes 32 uploads at a time: lane j loads upload
-// j's keep word, 32 ballots transpose them into each word's mask of writing uploads, and the
-// snapshot values of a block are loaded a few at a time ahead of the stores that carry them on.
+// (pass, 32 TMEM words), lane = word; its TMEM_CARRY_WARPS warps split the uploads into chunks:
+// each warp finds the last value its chunk writes, the chunks' carry-ins are chained in shared
+// memory, then every warp fills its chunk.  A warp reads each upload's keep word of its 32 words
+// (one broadcast load) and tests its lane's bit; TMEM_CARRY_AHEAD uploads' keep words and written
+// snapshot values are loaded together ahead of the stores that carry them on.
 constexpr int TMEM_CARRY_WARPS = 32; // 8: +0.19 ms per batched sync point, 16: +0.05 ms
-constexpr int TMEM_CARRY_AHEAD = 4;  // snapshot values loaded ahead of the stores
-
-// Bit j of the result (for the calling lane's word): upload ub + j wrote it.  `kw` is lane j's
-// keep word of upload ub + j (all ones past the chunk).
-__device__ __forceinline__ uint32_t tmem_written_mask(uint32_t kw, int lane)
-{
-	uint32_t wm = 0;
-#pragma unroll
-	for (int i = 0; i < 32; i++)
-	{
-		const uint32_t m = __ballot_sync(0xffffffffu, ((kw >> i) & 1u) == 0u);
-		if (lane == i) wm = m;
-	}
-	return wm;
-}
+constexpr int TMEM_CARRY_AHEAD = 8;  // uploads whose loads are issued together
 
 __global__ void __launch_bounds__(TMEM_CARRY_WARPS * 32, 2) k_tmem_carry(const RdpPass *__restrict__ passes,
                                                                        const uint32_t *__restrict__ pass_list,
@@ -1224,24 +1210,29 @@ __global__ void __launch_bounds__(TMEM_CARRY_WARPS * 32, 2) k_tmem_carry(const R
 	const uint32_t n = ps.upload_count;
 	const uint32_t chunk = (n + TMEM_CARRY_WARPS - 1) / TMEM_CARRY_WARPS;
 	const uint32_t u0 = min(n, uint32_t(warp) * chunk), u1 = min(n, u0 + chunk);
-	uint16_t *snap = ps.tmem_snapshots;
-	// This CTA's keep word of upload u: keep_words[u * 64].
+	// Word gid of snapshot s (the state after s uploads): col[s * 2048].
+	uint16_t *col = ps.tmem_snapshots + gid;
+	// This CTA's keep word of upload u: keep_words[u * 64] (bit = lane: the upload left the word alone).
 	const uint32_t *keep_words = keep_bits + size_t(ps.upload_begin) * 64 + blockIdx.x;
 
 	int last_u = -1;
-	for (uint32_t ub = u0; ub < u1; ub += 32)
+	for (uint32_t ub = u0; ub < u1; ub += TMEM_CARRY_AHEAD)
 	{
-		const uint32_t u = ub + uint32_t(lane);
-		const uint32_t wm = tmem_written_mask(u < u1 ? keep_words[size_t(u) * 64] : 0xffffffffu, lane);
-		if (wm) last_u = int(ub) + 31 - __clz(wm);
+		uint32_t kw[TMEM_CARRY_AHEAD];
+#pragma unroll
+		for (int k = 0; k < TMEM_CARRY_AHEAD; k++)
+			kw[k] = ub + uint32_t(k) < u1 ? keep_words[size_t(ub + uint32_t(k)) * 64] : 0xffffffffu;
+#pragma unroll
+		for (int k = 0; k < TMEM_CARRY_AHEAD; k++)
+			if (!((kw[k] >> lane) & 1u)) last_u = int(ub) + k;
 	}
-	s_last[warp][lane] = last_u >= 0 ? snap[size_t(last_u + 1) * 2048 + gid] : uint16_t(0);
+	s_last[warp][lane] = last_u >= 0 ? col[size_t(last_u + 1) * 2048] : uint16_t(0);
 	s_has[warp][lane] = last_u >= 0;
 	__syncthreads();
 	if (warp == 0)
 	{
 		uint16_t v = ps.tmem_state[gid];
-		snap[gid] = v;
+		col[0] = v;
 		for (int w = 0; w < TMEM_CARRY_WARPS; w++)
 		{
 			s_in[w][lane] = v;
@@ -1251,28 +1242,24 @@ __global__ void __launch_bounds__(TMEM_CARRY_WARPS * 32, 2) k_tmem_carry(const R
 	}
 	__syncthreads();
 	uint16_t value = s_in[warp][lane];
-	for (uint32_t ub = u0; ub < u1; ub += 32)
+	for (uint32_t ub = u0; ub < u1; ub += TMEM_CARRY_AHEAD)
 	{
-		const uint32_t u = ub + uint32_t(lane);
-		const uint32_t wm = tmem_written_mask(u < u1 ? keep_words[size_t(u) * 64] : 0xffffffffu, lane);
-		const uint32_t cnt = min(32u, u1 - ub);
-		for (uint32_t j0 = 0; j0 < cnt; j0 += TMEM_CARRY_AHEAD)
+		bool wrote[TMEM_CARRY_AHEAD];
+		uint16_t got[TMEM_CARRY_AHEAD];
+#pragma unroll
+		for (int k = 0; k < TMEM_CARRY_AHEAD; k++)
 		{
-			uint16_t got[TMEM_CARRY_AHEAD];
+			const uint32_t u = ub + uint32_t(k);
+			wrote[k] = u < u1 && !((keep_words[size_t(u) * 64] >> lane) & 1u);
+			got[k] = wrote[k] ? col[size_t(u + 1) * 2048] : uint16_t(0);
+		}
 #pragma unroll
-			for (int k = 0; k < TMEM_CARRY_AHEAD; k++)
-			{
-				const uint32_t j = j0 + uint32_t(k);
-				got[k] = (j < cnt && ((wm >> j) & 1u)) ? snap[size_t(ub + j + 1) * 2048 + gid] : uint16_t(0);
-			}
-#pragma unroll
-			for (int k = 0; k < TMEM_CARRY_AHEAD; k++)
-			{
-				const uint32_t j = j0 + uint32_t(k);
-				if (j >= cnt) break;
-				if ((wm >> j) & 1u) value = got[k];
-				else snap[size_t(ub + j + 1) * 2048 + gid] = value;
-			}
+		for (int k = 0; k < TMEM_CARRY_AHEAD; k++)
+		{
+			const uint32_t u = ub + uint32_t(k);
+			if (u >= u1) break;
+			if (wrote[k]) value = got[k];
+			else col[size_t(u + 1) * 2048] = value;
 		}
 	}
 }

@@ -745,7 +745,7 @@ __device__ __forceinline__ uint32_t bin_tiles(const RdpPrimGeom &g, const RdpPas
 // tiles k*32 + lane, then every 32*gridDim.y-th further.
 constexpr int BIN_LANE_TILES = 16;
 
-__global__ void __launch_bounds__(256) k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom,
+__global__ void __launch_bounds__(256, 3) k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom,
                                             const RdpPrimShade *__restrict__ shade, const RdpPass *__restrict__ passes,
                                             uint32_t *__restrict__ tile_counts, uint32_t *__restrict__ prim_pairs)
 {
@@ -764,17 +764,37 @@ __global__ void __launch_bounds__(256) k_bin(uint32_t num_prims, const RdpPrimGe
 			binned = bin_tiles(g, passes[shade[prim].pass], prim, tile_counts, 0, 1);
 	}
 	unsigned big = __ballot_sync(0xffffffffu, count > BIN_LANE_TILES);
-	while (big)
+	if (big)
 	{
-		const int src = __ffs(big) - 1;
-		big &= big - 1;
-		const uint32_t bp = warp_first + uint32_t(src);
-		const RdpPrimGeom g = geom[bp];
-		uint32_t n = bin_tiles(g, passes[shade[bp].pass], bp, tile_counts, int(blockIdx.y) * 32 + lane,
-		                       32 * int(gridDim.y));
+		// The large primitives' records are loaded by their own lanes at once, then shuffled to the
+		// warp one primitive at a time.
+		static_assert(sizeof(RdpPrimGeom) == 80, "five 16-byte words");
+		uint4 gq[5] = {};
+		uint32_t my_pass = 0;
+		if ((big >> lane) & 1u)
+		{
+			const uint4 *src = reinterpret_cast<const uint4 *>(geom + prim);
 #pragma unroll
-		for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
-		if (lane == src) binned = n;
+			for (int i = 0; i < 5; i++) gq[i] = src[i];
+			my_pass = shade[prim].pass;
+		}
+		while (big)
+		{
+			const int src = __ffs(big) - 1;
+			big &= big - 1;
+			RdpPrimGeom g;
+			uint4 *dst = reinterpret_cast<uint4 *>(&g);
+#pragma unroll
+			for (int i = 0; i < 5; i++)
+				dst[i] = make_uint4(__shfl_sync(0xffffffffu, gq[i].x, src), __shfl_sync(0xffffffffu, gq[i].y, src),
+				                    __shfl_sync(0xffffffffu, gq[i].z, src), __shfl_sync(0xffffffffu, gq[i].w, src));
+			const uint32_t bp = warp_first + uint32_t(src);
+			uint32_t n = bin_tiles(g, passes[__shfl_sync(0xffffffffu, my_pass, src)], bp, tile_counts,
+			                       int(blockIdx.y) * 32 + lane, 32 * int(gridDim.y));
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+			if (lane == src) binned = n;
+		}
 	}
 	if (prim_pairs && prim < num_prims) prim_pairs[prim] = binned;
 }

@@ -708,95 +708,79 @@ __device__ bool bin_primitive(const RdpPrimGeom &g, int lox, int loy, int hix, i
 	return rx0 <= rx1;
 }
 
-// Bins one primitive into the tiles t = t_begin, t_begin + t_step, ... of its tile box: sets its
-// bit in each covered tile's bitmask and counts the tile's pairs.  Returns the tiles binned.
-__device__ __forceinline__ uint32_t bin_tiles(const RdpPrimGeom &g, const RdpPass &pass, uint32_t prim,
-                                              uint32_t *__restrict__ tile_counts, int t_begin, int t_step)
-{
-	const uint32_t local = prim - pass.prim_begin;
-	const uint32_t bit = 1u << (local & 31);
-	const uint32_t word = local >> 5;
-	const int tw = g.bbox[2] - g.bbox[0] + 1, count = tw * (g.bbox[3] - g.bbox[1] + 1);
-	const int fbw = int(pass.fb_width), fbh = int(pass.fb_height);
-	const int sl = int(pass.scale & 3u);
-	uint32_t binned = 0;
-	for (int t = t_begin; t < count; t += t_step)
-	{
-		const int tx = g.bbox[0] + t % tw, ty = g.bbox[1] + t / tw;
-		const int lox = tx * 8, loy = ty * 8;
-		const int hix = min(lox + 7, fbw - 1), hiy = min(loy + 7, fbh - 1);
-		if (bin_primitive(g, lox, loy, hix, hiy, sl))
-		{
-			const uint32_t tl = uint32_t(ty) * pass.tiles_x + uint32_t(tx);
-			atomicOr(&pass.masks[size_t(tl) * pass.mask_words + word], bit);
-			// Upscaled and fill-only launches render from the bitmasks alone (no pair list).
-			if (tile_counts) atomicAdd(&tile_counts[pass.tile_item_begin + tl], 1u);
-			binned++;
-		}
-	}
-	return binned;
-}
-
-// One thread per primitive: a primitive whose tile box holds at most BIN_LANE_TILES tiles is
-// binned by its own lane; larger ones are binned afterwards by the whole warp, one after another,
-// the lanes striding over the box.  With `prim_pairs`, also writes each primitive's number of
-// binned tiles (its pairs).  Without it the grid's y dimension may split a large primitive's box
-// over several warps (launches of a few large primitives, such as a frame's clears): warp k takes
-// tiles k*32 + lane, then every 32*gridDim.y-th further.
-constexpr int BIN_LANE_TILES = 16;
-
-__global__ void __launch_bounds__(256, 3) k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom,
+// A warp takes 32 consecutive primitives and tests their (primitive, tile) pairs flattened: the
+// exclusive prefix of the primitives' tile-box sizes numbers the warp's tests, lane l takes tests
+// l, l + 32, ... and finds its primitive by binary search of the prefix, so the lanes stay busy
+// whatever the mix of box sizes.  With `prim_pairs`, also writes each primitive's number of binned
+// tiles (its pairs), counted in shared memory.  Without it the grid's y dimension may split a
+// warp's tests over several warps (launches of a few large primitives, such as a frame's clears):
+// warp k takes tests k*32 + lane, then every 32*gridDim.y-th further.
+__global__ void __launch_bounds__(256) k_bin(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom,
                                             const RdpPrimShade *__restrict__ shade, const RdpPass *__restrict__ passes,
                                             uint32_t *__restrict__ tile_counts, uint32_t *__restrict__ prim_pairs)
 {
+	__shared__ uint32_t s_binned[8][32];
 	const uint32_t prim = blockIdx.x * blockDim.x + threadIdx.x;
-	const int lane = int(threadIdx.x & 31);
+	const int lane = int(threadIdx.x & 31), wib = int(threadIdx.x >> 5);
 	const uint32_t warp_first = prim - uint32_t(lane);
 	if (warp_first >= num_prims) return; // the whole warp
-	int count = 0;
-	uint32_t binned = 0;
+	uint32_t count = 0;
 	if (prim < num_prims)
 	{
-		const RdpPrimGeom g = geom[prim];
+		const RdpPrimGeom &g = geom[prim];
 		if (g.bbox[2] >= g.bbox[0] && g.bbox[3] >= g.bbox[1])
-			count = (g.bbox[2] - g.bbox[0] + 1) * (g.bbox[3] - g.bbox[1] + 1);
-		if (count > 0 && count <= BIN_LANE_TILES && blockIdx.y == 0)
-			binned = bin_tiles(g, passes[shade[prim].pass], prim, tile_counts, 0, 1);
+			count = uint32_t(g.bbox[2] - g.bbox[0] + 1) * uint32_t(g.bbox[3] - g.bbox[1] + 1);
 	}
-	unsigned big = __ballot_sync(0xffffffffu, count > BIN_LANE_TILES);
-	if (big)
+	uint32_t incl = count;
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1)
 	{
-		// The large primitives' records are loaded by their own lanes at once, then shuffled to the
-		// warp one primitive at a time.
-		static_assert(sizeof(RdpPrimGeom) == 80, "five 16-byte words");
-		uint4 gq[5] = {};
-		uint32_t my_pass = 0;
-		if ((big >> lane) & 1u)
-		{
-			const uint4 *src = reinterpret_cast<const uint4 *>(geom + prim);
+		const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+		if (lane >= o) incl += y;
+	}
+	const uint32_t first = incl - count, total = __shfl_sync(0xffffffffu, incl, 31);
+	if (prim_pairs) s_binned[wib][lane] = 0u;
+	__syncwarp();
+	for (uint32_t f0 = blockIdx.y * 32u; f0 < total; f0 += 32u * gridDim.y)
+	{
+		const uint32_t f = f0 + uint32_t(lane);
+		// The primitive holding test f: the largest j with first_j <= f (first_0 = 0).
+		int j = 0;
+		uint32_t fj = 0;
 #pragma unroll
-			for (int i = 0; i < 5; i++) gq[i] = src[i];
-			my_pass = shade[prim].pass;
+		for (int step = 16; step > 0; step >>= 1)
+		{
+			const uint32_t c = __shfl_sync(0xffffffffu, first, j + step);
+			if (c <= f)
+			{
+				j += step;
+				fj = c;
+			}
 		}
-		while (big)
+		if (f >= total) continue;
+		const uint32_t p = warp_first + uint32_t(j);
+		const RdpPrimGeom &g = geom[p];
+		const RdpPass &pass = passes[shade[p].pass];
+		const int t = int(f - fj);
+		const int tw = g.bbox[2] - g.bbox[0] + 1;
+		const int tx = g.bbox[0] + t % tw, ty = g.bbox[1] + t / tw;
+		const int lox = tx * 8, loy = ty * 8;
+		const int hix = min(lox + 7, int(pass.fb_width) - 1), hiy = min(loy + 7, int(pass.fb_height) - 1);
+		if (bin_primitive(g, lox, loy, hix, hiy, int(pass.scale & 3u)))
 		{
-			const int src = __ffs(big) - 1;
-			big &= big - 1;
-			RdpPrimGeom g;
-			uint4 *dst = reinterpret_cast<uint4 *>(&g);
-#pragma unroll
-			for (int i = 0; i < 5; i++)
-				dst[i] = make_uint4(__shfl_sync(0xffffffffu, gq[i].x, src), __shfl_sync(0xffffffffu, gq[i].y, src),
-				                    __shfl_sync(0xffffffffu, gq[i].z, src), __shfl_sync(0xffffffffu, gq[i].w, src));
-			const uint32_t bp = warp_first + uint32_t(src);
-			uint32_t n = bin_tiles(g, passes[__shfl_sync(0xffffffffu, my_pass, src)], bp, tile_counts,
-			                       int(blockIdx.y) * 32 + lane, 32 * int(gridDim.y));
-#pragma unroll
-			for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
-			if (lane == src) binned = n;
+			const uint32_t local = p - pass.prim_begin;
+			const uint32_t tl = uint32_t(ty) * pass.tiles_x + uint32_t(tx);
+			atomicOr(&pass.masks[size_t(tl) * pass.mask_words + (local >> 5)], 1u << (local & 31));
+			// Upscaled and fill-only launches render from the bitmasks alone (no pair list).
+			if (tile_counts) atomicAdd(&tile_counts[pass.tile_item_begin + tl], 1u);
+			if (prim_pairs) atomicAdd(&s_binned[wib][j], 1u);
 		}
 	}
-	if (prim_pairs && prim < num_prims) prim_pairs[prim] = binned;
+	if (prim_pairs)
+	{
+		__syncwarp();
+		if (prim < num_prims) prim_pairs[prim] = s_binned[wib][lane];
+	}
 }
 
 // ============================================================================ k_span
@@ -4314,7 +4298,7 @@ static bool multi_cta_scan(const RdpLaunch *L)
 	                          (L->shade_list && L->prim_scan_blocks && L->num_prims > RDP_SCAN_SINGLE_CTA_MAX));
 }
 
-// Warps that share each large primitive's tile box in k_bin (its grid's y dimension) when no
+// Warps that share each warp's (primitive, tile) tests in k_bin (its grid's y dimension) when no
 // per-primitive count is taken: a launch of few primitives still fills the GPU.
 static uint32_t bin_split(const RdpLaunch *L)
 {

@@ -3994,22 +3994,46 @@ __global__ void __launch_bounds__(RASTER_THREADS) k_raster(const RdpPass *__rest
 // each row is set up and no shading record is built.  One warp per 8x8 tile, independent of the
 // CTA's other warps: lane l owns pixels (l % 8, l / 8) and (l % 8, l / 8 + 4) of the tile, and the
 // warp alone clears the bitmask words it consumed.
-constexpr int FILL_THREADS = 256;
+constexpr int FILL_THREADS = 256, FILL_TILES = 4; // tiles per warp, consecutive items
 
-__global__ void __launch_bounds__(FILL_THREADS) k_fill(const RdpPass *__restrict__ passes, uint32_t num_passes,
-                                                      uint32_t num_items, const RdpPrimGeom *__restrict__ geom,
-                                                      const RdpPrimShade *__restrict__ shade)
+// Marks the colour bytes of a fill's stored pixels (px.cdirty) in the write mask.  The 8 pixels
+// of a tile row (lanes 8r .. 8r+7) hold at most 32 contiguous bytes -- at most two mask words,
+// also where the address wraps -- so each row's lanes merge their bits with three reductions and
+// one lane issues at most two atomics.
+__device__ __forceinline__ void mark_fill_row(const RdpPass &p, const Pix &px, uint32_t ci, int lane)
 {
-	__shared__ SpanRow s_sp[FILL_THREADS / 32][8];
-	const int wib = threadIdx.x >> 5;
-	const int lane = threadIdx.x & 31;
-	const uint32_t item = blockIdx.x * (FILL_THREADS / 32) + uint32_t(wib);
-	if (item >= num_items) return; // the whole warp
+	uint32_t ca, cn;
+	switch (p.fb_fmt)
+	{
+	case FBF_I4:
+	case FBF_I8: ca = (ci & (p.rdram_size - 1)) ^ 3u; cn = 1; break;
+	case FBF_RGBA5551:
+	case FBF_IA88: ca = ((ci & ((p.rdram_size >> 1) - 1)) ^ 1u) * 2u; cn = 2; break;
+	default: ca = (ci & ((p.rdram_size >> 2) - 1)) * 4u; cn = 4; break;
+	}
+	const bool c = px.cdirty;
+	const uint32_t word = ca >> 5, bits = c ? ((1u << cn) - 1u) << (ca & 31u) : 0u;
+	const unsigned row = 0xffu << (lane & 24);
+	const uint32_t lo = __reduce_min_sync(row, c ? word : 0xffffffffu);
+	const uint32_t hi = __reduce_max_sync(row, c ? word : 0u);
+	const uint32_t blo = __reduce_or_sync(row, word == lo ? bits : 0u);
+	const uint32_t bhi = __reduce_or_sync(row, word != lo ? bits : 0u);
+	if ((lane & 7) == 0)
+	{
+		if (blo) atomicOr(p.wmask + lo, blo);
+		if (bhi) atomicOr(p.wmask + hi, bhi);
+	}
+}
 
-	const uint32_t pi = pass_of_item_warp(passes, num_passes, item, lane);
-	const RdpPass &ps = passes[pi];
-	const uint32_t tile_linear = item - ps.tile_item_begin;
-	const int tx = int(tile_linear % ps.tiles_x), ty = int(tile_linear / ps.tiles_x);
+// One 8x8 tile of a fill-only launch (k_fill).  Returns whether any primitive was binned there;
+// adds the fragments and binned primitives to frags / pairs.
+// The x extents in s_sp belong to primitive *sp_prim at tile row *sp_row0 (shared by the tiles of
+// one row of the image, so consecutive tiles reuse them).
+__device__ __forceinline__ bool fill_tile(const RdpPass &ps, uint32_t tile_linear, int tx, int ty,
+                                          const RdpPrimGeom *__restrict__ geom,
+                                          const RdpPrimShade *__restrict__ shade, SpanRow *s_sp, uint32_t &sp_prim,
+                                          int &sp_row0, int lane, uint32_t &frags, uint32_t &pairs)
+{
 	uint32_t *masks = ps.masks + size_t(tile_linear) * ps.mask_words;
 	const uint32_t nwords = (ps.prim_count + 31) / 32;
 
@@ -4037,7 +4061,8 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill(const RdpPass *__restrict
 	const uint32_t ci1 = ci0 + 4u * ps.fb_width, di1 = di0 + 4u * ps.fb_width;
 
 	// The fill pipe sets every stored field of a pixel from the fill colour alone (colour, coverage
-	// bits, the aliased depth) and a pixel no fill covers is not stored, so nothing is loaded.
+	// bits, the aliased depth; never the depth image) and a pixel no fill covers is not stored, so
+	// nothing is loaded.
 	Pix p0, p1;
 	p0.cidx = ci0;
 	p1.cidx = ci1;
@@ -4045,7 +4070,6 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill(const RdpPass *__restrict
 	p0.depth = p0.dz = p1.depth = p1.dz = 0;
 #pragma unroll
 	for (int c = 0; c < 4; c++) p0.col[c] = p1.col[c] = 0;
-	uint32_t frags = 0;
 	bool any = false;
 	for (uint32_t base = 0; base < nwords; base += 32)
 	{
@@ -4067,49 +4091,98 @@ __global__ void __launch_bounds__(FILL_THREADS) k_fill(const RdpPass *__restrict
 				const uint32_t col = shade[prim].fill_color;
 				const int ylo = g.span_ylo, yhi = g.span_yhi;
 				if (yhi < row0 || ylo > row0 + 7) continue; // no row of the tile is covered
-				if (lane < 8) span_x(g, row0 + lane, s_sp[wib][lane]);
-				__syncwarp();
-				const SpanRow &a = s_sp[wib][lane >> 3], &c = s_sp[wib][(lane >> 3) + 4];
+				if (prim != sp_prim || row0 != sp_row0)
+				{
+					__syncwarp();
+					if (lane < 8) span_x(g, row0 + lane, s_sp[lane]);
+					sp_prim = prim;
+					sp_row0 = row0;
+					__syncwarp();
+				}
+				const SpanRow &a = s_sp[lane >> 3], &c = s_sp[(lane >> 3) + 4];
 				if (in0 && y0 >= ylo && y0 <= yhi && a.valid && px_x >= a.start_x && px_x <= a.end_x)
 					frags += fill_pixel(ps, pc, col, p0);
 				if (in1 && y1 >= ylo && y1 <= yhi && c.valid && px_x >= c.start_x && px_x <= c.end_x)
 					frags += fill_pixel(ps, pc, col, p1);
-				__syncwarp();
 			}
 		}
 	}
-	if (!any) return; // no primitive binned here: nothing stored, marked or counted
+	if (!any) return false; // no primitive binned here: nothing stored, marked or counted
 	if (in0) store_pixel(ps, p0, ci0, di0, pc.alias);
 	if (in1) store_pixel(ps, p1, ci1, di1, pc.alias);
 	if (ps.wmask)
 	{
-		mark_pixel(ps, p0, ci0, di0, pc.alias, in0);
-		mark_pixel(ps, p1, ci1, di1, pc.alias, in1);
+		mark_fill_row(ps, p0, ci0, lane);
+		mark_fill_row(ps, p1, ci1, lane);
 	}
 	// The warp has consumed the bitmask: clear it for the next pass using this slot.
-	unsigned long long pairs_here = 0;
 	for (uint32_t wi = lane; wi < nwords; wi += 32)
 	{
-		pairs_here += __popc(masks[wi]);
+		pairs += __popc(masks[wi]);
 		masks[wi] = 0u;
 	}
-	unsigned long long *counters = ps.counters;
-	if (counters)
-	{
-		unsigned long long total = frags;
+	return true;
+}
+
+// One warp per FILL_TILES consecutive tiles (mostly of one pass: the pass is looked up again only
+// when a tile leaves the current one), independent of the CTA's other warps: lane l owns pixels
+// (l % 8, l / 8) and (l % 8, l / 8 + 4) of each tile, and the warp alone clears the bitmask
+// words it consumed.  A pass's counters take one update per warp.
+__global__ void __launch_bounds__(FILL_THREADS) k_fill(const RdpPass *__restrict__ passes, uint32_t num_passes,
+                                                      uint32_t num_items, const RdpPrimGeom *__restrict__ geom,
+                                                      const RdpPrimShade *__restrict__ shade)
+{
+	__shared__ SpanRow s_sp[FILL_THREADS / 32][8];
+	const int wib = threadIdx.x >> 5;
+	const int lane = threadIdx.x & 31;
+	const uint32_t first = (blockIdx.x * (FILL_THREADS / 32) + uint32_t(wib)) * FILL_TILES;
+	uint32_t pi = 0, begin = 1, end = 0; // the current pass and its tile items [begin, end)
+	uint32_t frags = 0, pairs = 0, tiles = 0;
+	int tx = 0, ty = 0; // of the next tile of the current pass
+	uint32_t sp_prim = 0xffffffffu;
+	int sp_row0 = -1;
+	auto flush = [&]() {
+		unsigned long long *counters = passes[pi].counters;
+		if (!counters || !tiles) return;
+		unsigned long long f = frags, pr = pairs;
 #pragma unroll
 		for (int o = 16; o > 0; o >>= 1)
 		{
-			total += __shfl_xor_sync(0xffffffffu, total, o);
-			pairs_here += __shfl_xor_sync(0xffffffffu, pairs_here, o);
+			f += __shfl_xor_sync(0xffffffffu, f, o);
+			pr += __shfl_xor_sync(0xffffffffu, pr, o);
 		}
 		if (lane == 0)
 		{
-			if (total) atomicAdd(counters, total);
-			atomicAdd(counters + 1, 1ull);
-			atomicAdd(counters + 2, pairs_here);
+			if (f) atomicAdd(counters, f);
+			atomicAdd(counters + 1, (unsigned long long)tiles);
+			atomicAdd(counters + 2, pr);
+		}
+	};
+	for (uint32_t k = 0; k < uint32_t(FILL_TILES); k++)
+	{
+		const uint32_t item = first + k;
+		if (item >= num_items) break; // the whole warp
+		if (item < begin || item >= end)
+		{
+			if (begin < end) flush();
+			frags = pairs = tiles = 0;
+			pi = pass_of_item_warp(passes, num_passes, item, lane);
+			begin = passes[pi].tile_item_begin;
+			end = begin + passes[pi].tiles_x * passes[pi].tiles_y;
+			tx = int((item - begin) % passes[pi].tiles_x);
+			ty = int((item - begin) / passes[pi].tiles_x);
+			sp_prim = 0xffffffffu; // primitive indices are per launch, so a new pass keeps none
+		}
+		if (fill_tile(passes[pi], item - begin, tx, ty, geom, shade, s_sp[wib], sp_prim, sp_row0, lane, frags,
+		              pairs))
+			tiles++;
+		if (++tx == int(passes[pi].tiles_x))
+		{
+			tx = 0;
+			ty++;
 		}
 	}
+	if (begin < end) flush();
 }
 
 // ============================================================================ k_raster_upscaled
@@ -4376,9 +4449,11 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 				L->passes, L->tmem_pass_list, L->tmem_keep);
 		}
 		if (L->num_prims && L->num_tile_items)
-			rdp::k_fill<<<(L->num_tile_items + rdp::FILL_THREADS / 32 - 1) / (rdp::FILL_THREADS / 32),
-			              rdp::FILL_THREADS, 0, stream>>>(L->passes, L->num_passes, L->num_tile_items, L->geom,
-			                                              L->shade);
+		{
+			constexpr uint32_t per_cta = rdp::FILL_THREADS / 32 * rdp::FILL_TILES;
+			rdp::k_fill<<<(L->num_tile_items + per_cta - 1) / per_cta, rdp::FILL_THREADS, 0, stream>>>(
+				L->passes, L->num_passes, L->num_tile_items, L->geom, L->shade);
+		}
 		return cudaGetLastError();
 	}
 	const bool raster = L->num_prims && L->num_tile_items;

@@ -304,6 +304,10 @@ struct Executor
 	static constexpr int kStagingSlots = 4;
 	uint8_t *d_staging = nullptr; // kStagingSlots slots of caps.staging bytes
 	cudaStream_t copy_stream = nullptr;
+	// The TMEM kernels of a rasterising launch run on side_stream, overlapping set-up, binning,
+	// span rows, scans and pair expansion (none of which reads TMEM); shading waits for them.
+	cudaStream_t side_stream = nullptr;
+	cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
 	cudaEvent_t slot_copied[kStagingSlots] = {}, slot_free[kStagingSlots] = {};
 	int staging_slot = 0;
 
@@ -501,7 +505,10 @@ struct Executor
 		}
 		if (check(cudaMalloc(&d_ctrl, 64)) || check(cudaMalloc(&d_pair_log, 256 * 4)) ||
 		    check(cudaMalloc(&d_queues, queue_bytes())) ||
-		    check(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking)))
+		    check(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking)) ||
+		    check(cudaStreamCreateWithFlags(&side_stream, cudaStreamNonBlocking)) ||
+		    check(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming)) ||
+		    check(cudaEventCreateWithFlags(&join_ev, cudaEventDisableTiming)))
 			return false;
 		for (int k = 0; k < kStagingSlots; k++)
 			if (check(cudaEventCreateWithFlags(&slot_copied[k], cudaEventDisableTiming)) ||
@@ -660,6 +667,15 @@ struct Executor
 		}
 		if (copy_stream) cudaStreamDestroy(copy_stream);
 		copy_stream = nullptr;
+		if (side_stream)
+		{
+			cudaStreamSynchronize(side_stream);
+			cudaStreamDestroy(side_stream);
+		}
+		side_stream = nullptr;
+		if (fork_ev) cudaEventDestroy(fork_ev);
+		if (join_ev) cudaEventDestroy(join_ev);
+		fork_ev = join_ev = nullptr;
 		tuner.destroy();
 		for (auto &st : staging)
 		{
@@ -992,6 +1008,9 @@ struct Executor
 		bool fill_only = !upscaled && tile_base != 0;
 		for (uint32_t i = 0; i < n && fill_only; i++) fill_only = v[i].fill_only;
 		L.fill_only = fill_only ? 1u : 0u;
+		L.side_stream = side_stream;
+		L.fork_event = fork_ev;
+		L.join_event = join_ev;
 		int variant = current_variant();
 		bool sample = false;
 		if (!upscaled && !fill_only && tuner.active && shade_variant_choice(device) < 0 && !cap && tile_base &&

@@ -4457,6 +4457,20 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		return cudaGetLastError();
 	}
 	const bool raster = L->num_prims && L->num_tile_items;
+	// TMEM on the side stream: the kernels up to pair expansion read no TMEM snapshot.
+	const bool side = raster && L->num_tmem_passes && L->side_stream && L->fork_event && L->join_event;
+	if (side)
+	{
+		cudaError_t e = cudaEventRecord(L->fork_event, stream);
+		if (e == cudaSuccess) e = cudaStreamWaitEvent(L->side_stream, L->fork_event, 0);
+		if (e != cudaSuccess) return e;
+		rdp::k_tmem_apply<<<L->num_uploads, 256, 0, L->side_stream>>>(L->passes, L->tmem_pass_list, L->num_tmem_passes,
+		                                                               L->uploads, L->tmem_keep);
+		rdp::k_tmem_carry<<<dim3(2048 / 32, L->num_tmem_passes), rdp::TMEM_CARRY_WARPS * 32, 0, L->side_stream>>>(
+			L->passes, L->tmem_pass_list, L->tmem_keep);
+		e = cudaEventRecord(L->join_event, L->side_stream);
+		if (e != cudaSuccess) return e;
+	}
 	if (L->num_prims)
 	{
 		rdp::k_prim_setup<<<(L->num_prims + 127) / 128, 128, 0, stream>>>(L->prims_in, L->num_prims, L->words,
@@ -4479,7 +4493,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 				L->span_capacity, L->prim_rows, reinterpret_cast<unsigned long long *>(L->ctrl + 6), chunk);
 		}
 	}
-	if (L->num_tmem_passes)
+	if (L->num_tmem_passes && !side)
 	{
 		rdp::k_tmem_apply<<<L->num_uploads, 256, 0, stream>>>(L->passes, L->tmem_pass_list, L->num_tmem_passes,
 		                                                      L->uploads, L->tmem_keep);
@@ -4515,6 +4529,11 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 			L->passes, L->num_passes, L->num_tile_items, L->pair_offsets, L->ctrl, L->pairs,
 			sched ? L->sched->featbits : nullptr, sched ? L->sched->features : nullptr,
 			sched && L->sched->train_enabled && L->tile_cycles, L->prim_offsets, L->prim_pairs, L->shade_list);
+		if (side)
+		{
+			const cudaError_t e = cudaStreamWaitEvent(stream, L->join_event, 0);
+			if (e != cudaSuccess) return e;
+		}
 		// Inside a stream capture the events become record nodes of the graph.
 		cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
 		if ((L->shade_events[0] || L->blend_events[0]) && cudaStreamIsCapturing(stream, &capture) != cudaSuccess)

@@ -75,6 +75,9 @@ typedef struct RdpLaunch
 	uint32_t upscaled;              /* the passes are upscaled passes (RdpPass.scale): set-up, binning, TMEM and
 	                                   k_raster_upscaled only */
 	uint32_t fill_only;             /* every primitive fills a rectangle: set-up, binning, TMEM and k_fill only */
+	cudaStream_t side_stream;       /* optional: the TMEM kernels of a rasterising launch run here, forked
+	                                   after fork_event and joined (join_event) before shading */
+	cudaEvent_t fork_event, join_event;
 } RdpLaunch;
 
 #ifdef __cplusplus

@@ -408,9 +408,10 @@ int rdp_dump_replay(rdp_cp *cp, const char *path, rdp_dump_frame_cb on_frame, vo
 /* Kernel specialisation.  The reference compiles its shading shaders per normalised static render
  * state with specialisation constants (rdp_renderer.cpp:1294-1331, 1790-1822).  Here the shading
  * kernel is compiled for RDP_SHADE_VARIANTS variants: 0-3 run one general shader for every
- * primitive, 4-7 dispatch each primitive to separately compiled code for its render-state class
- * (fill, copy, untextured, one texel, one texel through a TLUT, two texels, LOD; others take the
- * general shader), each at register budgets for 16, 18, 20 and 24 resident CTAs per SM.  By default
+ * primitive (2, 3, 4 and 4 (primitive, tile) pairs per warp step, at register budgets for 18, 16, 16
+ * and 18 resident CTAs per SM), 4-7 dispatch each primitive to separately compiled code for its
+ * render-state class (fill, copy, untextured, one texel, one texel through a TLUT, two texels, LOD;
+ * others take the general shader; 2 pairs per step at budgets for 16, 18, 20 and 24 CTAs).  By default
  * an autotuner times them on the first launches of a device and keeps the fastest per shaded
  * (primitive, tile) pair.  All variants give identical results.  rdp_set_shade_variant forces one
  * (0..7) or restarts tuning (-1); rdp_get_shade_variant returns the device's choice, -1 while tuning. */

@@ -4339,8 +4339,8 @@ typedef void (*ShadeKernel)(const RdpPass *, uint32_t, const uint2 *, const uint
                             const RdpPrimAttr *, const RdpPrimShade *, const RdpTile *, uint2 *, const uint4 *,
                             uint32_t *, uint32_t, uint32_t, const rdp::SpanRow *, const uint32_t *);
 const ShadeKernel kShadeVariants[RDP_SHADE_VARIANTS] = {
-	rdp::k_shade_packedn<2, 16, false>, rdp::k_shade_packedn<2, 18, false>, rdp::k_shade_packedn<2, 20, false>,
-	rdp::k_shade_packedn<2, 24, false>, rdp::k_shade_packedn<2, 16, true>,  rdp::k_shade_packedn<2, 18, true>,
+	rdp::k_shade_packedn<2, 18, false>, rdp::k_shade_packedn<3, 16, false>, rdp::k_shade_packedn<4, 16, false>,
+	rdp::k_shade_packedn<4, 18, false>, rdp::k_shade_packedn<2, 16, true>,  rdp::k_shade_packedn<2, 18, true>,
 	rdp::k_shade_packedn<2, 20, true>,  rdp::k_shade_packedn<2, 24, true>
 };
 } // namespace

@@ -5,10 +5,11 @@
 #include <cuda_runtime.h>
 #include "rdp_types.h"
 
-/* Shading kernel variants (the autotuner chooses among them): k_shade_packedn with two pairs per
- * warp step (candidate pixels of both pairs packed together), with the general shading code
- * (variants 0-3) or with separate code per render-state class (variants 4-7), each for minimum
- * residencies of 16, 18, 20 and 24 64-thread CTAs per SM. */
+/* Shading kernel variants (the autotuner chooses among them): k_shade_packedn<NP, R, SPEC> takes NP
+ * (primitive, tile) pairs per warp step (their candidate pixels packed together) at a register
+ * budget for R resident 64-thread CTAs per SM: the general shading code as <2, 18>, <3, 16>,
+ * <4, 16>, <4, 18> (variants 0-3), separate code per render-state class as <2, 16 / 18 / 20 / 24>
+ * (variants 4-7). */
 /* Bytes of one span row (one scanline of one primitive, computed by k_bin). */
 #define RDP_SPAN_ROW_BYTES 64
 /* Launches with more tiles (or, in primitive-major order, primitives) than this scan their

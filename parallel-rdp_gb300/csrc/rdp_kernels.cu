@@ -123,7 +123,7 @@ __device__ void interp_x64(const RdpPrimGeom &g, int y, bool flip, long long &xl
 	if (xr < -2147483648LL) xr = -2147483648LL;
 }
 
-// Pass of a launch that holds primitive i / tile item `item` (passes are sorted by both).
+// Pass of a launch that holds primitive i (passes are sorted by their first primitive).
 __device__ __forceinline__ uint32_t pass_of_prim(const RdpPass *__restrict__ passes, uint32_t num_passes, uint32_t i)
 {
 	uint32_t lo = 0, hi = num_passes - 1;
@@ -135,20 +135,10 @@ __device__ __forceinline__ uint32_t pass_of_prim(const RdpPass *__restrict__ pas
 	}
 	return lo;
 }
-__device__ __forceinline__ uint32_t pass_of_item(const RdpPass *__restrict__ passes, uint32_t num_passes, uint32_t item)
-{
-	uint32_t lo = 0, hi = num_passes - 1;
-	while (lo < hi)
-	{
-		uint32_t mid = (lo + hi + 1) >> 1;
-		if (passes[mid].tile_item_begin <= item) lo = mid;
-		else hi = mid - 1;
-	}
-	return lo;
-}
 
-// The same with a warp's 32 lanes probing 32 evenly spaced passes per step (a 32-ary search): two
-// dependent loads for up to 1,024 passes instead of ten.  Called by all lanes of a warp.
+// The pass holding tile item `item`, the last with tile_item_begin <= item: a warp's 32 lanes probe
+// 32 evenly spaced passes per step (a 32-ary search), two dependent loads for up to 1,024 passes
+// where a binary search takes ten.  Called by all lanes of a warp.
 __device__ __forceinline__ uint32_t pass_of_item_warp(const RdpPass *__restrict__ passes, uint32_t num_passes,
                                                       uint32_t item, int lane)
 {
@@ -3532,7 +3522,7 @@ __device__ __forceinline__ bool blend_tile(uint32_t item, const RdpPass *__restr
 			blend_issue(stages[sidx], &bars[sidx], p0 + c * BLEND_CHUNK, chunk_count(c), pairs, shade, sc);
 			issued_seq++;
 		}
-	const uint32_t pi = pass_of_item(passes, num_passes, item);
+	const uint32_t pi = pass_of_item_warp(passes, num_passes, item, int(threadIdx.x & 31));
 	const RdpPass &ps = passes[pi];
 	const uint32_t tl = item - ps.tile_item_begin;
 	const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
@@ -3698,7 +3688,7 @@ __device__ __forceinline__ void blend_tile_lookahead(uint32_t item, const RdpPas
 		return;
 	}
 	const long long t_start = clock64();
-	const uint32_t pi = pass_of_item(passes, num_passes, item);
+	const uint32_t pi = pass_of_item_warp(passes, num_passes, item, int(threadIdx.x & 31));
 	const RdpPass &ps = passes[pi];
 	const uint32_t tl = item - ps.tile_item_begin;
 	const int tx = int(tl % ps.tiles_x), ty = int(tl / ps.tiles_x);
@@ -3858,7 +3848,7 @@ __device__ __forceinline__ void raster_tile(uint32_t item, const RdpPass *__rest
 	const int wib = threadIdx.x >> 5;
 	const int lane = threadIdx.x & 31;
 
-	const uint32_t pi = pass_of_item(passes, num_passes, item);
+	const uint32_t pi = pass_of_item_warp(passes, num_passes, item, int(threadIdx.x & 31));
 	const RdpPass &ps = passes[pi];
 	const uint32_t tile_linear = item - ps.tile_item_begin;
 	const int tx = int(tile_linear % ps.tiles_x), ty = int(tile_linear / ps.tiles_x);
@@ -4206,7 +4196,7 @@ __device__ __forceinline__ void raster_tile_upscaled(uint32_t item, const RdpPas
 	const int wib = threadIdx.x >> 5;
 	const int lane = threadIdx.x & 31;
 
-	const uint32_t pi = pass_of_item(passes, num_passes, item);
+	const uint32_t pi = pass_of_item_warp(passes, num_passes, item, int(threadIdx.x & 31));
 	const RdpPass &ps = passes[pi];
 	const uint32_t tile_linear = item - ps.tile_item_begin;
 	const int tx = int(tile_linear % ps.tiles_x), ty = int(tile_linear / ps.tiles_x);

@@ -92,38 +92,43 @@ __global__ void __launch_bounds__(kThreads) k_coh_out(const RdpCohList L)
 	locate(L, inst, page);
 	const bool aligned = (L.host_aligned >> inst) & 1u;
 	uint32_t *wmask = L.wmask[inst];
+	// Both pieces' masks and device bytes are loaded before any is written out.
+	size_t off[2];
+	uint32_t m[2];
+	uint4 v[2];
 #pragma unroll
 	for (int half = 0; half < 2; half++)
 	{
-		const size_t off = page + half * kHalf + threadIdx.x * 16u;
-		const uint32_t m = piece_mask(wmask, off);
-		if (m)
+		off[half] = page + half * kHalf + threadIdx.x * 16u;
+		m[half] = piece_mask(wmask, off[half]);
+		v[half] = *reinterpret_cast<const uint4 *>(L.dev[inst] + off[half]);
+	}
+#pragma unroll
+	for (int half = 0; half < 2; half++)
+	{
+		uint8_t *h = L.host[inst] + off[half];
+		if (m[half] == 0xffffu && aligned)
 		{
-			const uint8_t *d = L.dev[inst] + off;
-			uint8_t *h = L.host[inst] + off;
-			if (m == 0xffffu && aligned)
+			// Host bytes: written through to the caller's memory (__stwt).
+			__stwt(reinterpret_cast<uint4 *>(h), v[half]);
+		}
+		else if (m[half])
+		{
+			const uint32_t dw[4] = { v[half].x, v[half].y, v[half].z, v[half].w };
+			for (int k = 0; k < 4; k++)
 			{
-				// Host bytes: written through to the caller's memory (__stwt).
-				__stwt(reinterpret_cast<uint4 *>(h), *reinterpret_cast<const uint4 *>(d));
-			}
-			else
-			{
-				const uint32_t *dw = reinterpret_cast<const uint32_t *>(d);
-				for (int k = 0; k < 4; k++)
-				{
-					const uint32_t nib = (m >> (4 * k)) & 15u;
-					if (nib == 15u && aligned)
-						__stwt(reinterpret_cast<unsigned int *>(h) + k, dw[k]);
-					else
-						for (int b = 0; b < 4; b++)
-							if ((nib >> b) & 1u) __stwt(reinterpret_cast<unsigned char *>(h) + 4 * k + b, d[4 * k + b]);
-				}
+				const uint32_t nib = (m[half] >> (4 * k)) & 15u;
+				if (nib == 15u && aligned)
+					__stwt(reinterpret_cast<unsigned int *>(h) + k, dw[k]);
+				else
+					for (int b = 0; b < 4; b++)
+						if ((nib >> b) & 1u) __stwt(h + 4 * k + b, uint8_t(dw[k] >> (8 * b)));
 			}
 		}
 		// The mask word covers this piece and its neighbour's (thread t ^ 1, same warp): both have
 		// read it before the even thread clears it.
-		const uint32_t pair = m | __shfl_xor_sync(0xffffffffu, m, 1);
-		if (!(threadIdx.x & 1u) && pair) wmask[off >> 5] = 0u;
+		const uint32_t pair = m[half] | __shfl_xor_sync(0xffffffffu, m[half], 1);
+		if (!(threadIdx.x & 1u) && pair) wmask[off[half] >> 5] = 0u;
 	}
 }
 

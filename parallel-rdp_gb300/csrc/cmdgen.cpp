@@ -529,7 +529,8 @@ struct Gen
 		}
 		if (!two_cycle)
 		{
-			// LOD fraction is only defined in 2-cycle mode (README.md:204): keep it out of 1-cycle combiners.
+			// LOD fraction is only defined in 2-cycle mode (the reference project's README lists reading it in
+			// 1-cycle mode as unsupported): keep it out of 1-cycle combiners.
 			if (c.rgb[1][2] == 13) c.rgb[1][2] = 4;
 			if (c.alpha[1][2] == 0) c.alpha[1][2] = 4;
 		}

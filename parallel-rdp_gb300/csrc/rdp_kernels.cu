@@ -3388,8 +3388,8 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 			count += n0 + __popc(m1);
 			const uint32_t pr = list ? rec.z : pos;
 			const size_t base = size_t(pr) * SHADE_THREADS;
-			if (!c0) sc[base + lane] = kScratchEmpty;
-			if (!c1) sc[base + 32 + lane] = kScratchEmpty;
+			if (!c0) __stcs(sc + base + lane, kScratchEmpty);
+			if (!c1) __stcs(sc + base + 32 + lane, kScratchEmpty);
 			if (lane == 0) s_slot[s] = Slot{ prim, pi, pr, tx, ty, ylo, rows };
 		}
 		__syncwarp();
@@ -3416,7 +3416,7 @@ __global__ void __launch_bounds__(SHADE_THREADS, MIN_CTAS)
 			const bool ok = shade_pixel_any<SPEC>(pc, geom[prim], attr[prim], sh, tilesets + size_t(sh.tileset) * 8,
 			                                      ps.tmem_snapshots + size_t(sh.tmem_index) * 2048, sp[0], sp[1],
 			                                      sl.tx * 8 + (px & 7), y, out);
-			sc[size_t(sl.pr) * SHADE_THREADS + px] = ok ? pack_shaded(out) : kScratchEmpty;
+			__stcs(sc + size_t(sl.pr) * SHADE_THREADS + px, ok ? pack_shaded(out) : kScratchEmpty);
 		}
 		if (lane == 0) cp_async_wait_all();
 		__syncwarp();
@@ -3734,7 +3734,7 @@ __device__ __forceinline__ void blend_tile_lookahead(uint32_t item, const RdpPas
 			q_prim[k] = 0u;
 			if (pr < p1)
 			{
-				q_rec[k] = sc[size_t(pr) * SHADE_THREADS + tid];
+				q_rec[k] = __ldcs(sc + size_t(pr) * SHADE_THREADS + tid);
 				q_prim[k] = pairs[pr].x;
 				asm volatile("prefetch.global.L1 [%0];" ::"l"(shade + q_prim[k]));
 			}
@@ -3752,7 +3752,7 @@ __device__ __forceinline__ void blend_tile_lookahead(uint32_t item, const RdpPas
 			const uint32_t nx = pr + BLEND_AHEAD;
 			if (nx < p1)
 			{
-				q_rec[BLEND_AHEAD - 1] = sc[size_t(nx) * SHADE_THREADS + tid];
+				q_rec[BLEND_AHEAD - 1] = __ldcs(sc + size_t(nx) * SHADE_THREADS + tid);
 				q_prim[BLEND_AHEAD - 1] = pairs[nx].x;
 				asm volatile("prefetch.global.L1 [%0];" ::"l"(shade + q_prim[BLEND_AHEAD - 1]));
 			}

@@ -4118,7 +4118,7 @@ __device__ __forceinline__ bool fill_tile(const RdpPass &ps, uint32_t tile_linea
 // when a tile leaves the current one), independent of the CTA's other warps: lane l owns pixels
 // (l % 8, l / 8) and (l % 8, l / 8 + 4) of each tile, and the warp alone clears the bitmask
 // words it consumed.  A pass's counters take one update per warp.
-__global__ void __launch_bounds__(FILL_THREADS) k_fill(const RdpPass *__restrict__ passes, uint32_t num_passes,
+__global__ void __launch_bounds__(FILL_THREADS, 4) k_fill(const RdpPass *__restrict__ passes, uint32_t num_passes,
                                                       uint32_t num_items, const RdpPrimGeom *__restrict__ geom,
                                                       const RdpPrimShade *__restrict__ shade)
 {

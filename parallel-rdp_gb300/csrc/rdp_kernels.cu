@@ -786,7 +786,7 @@ __global__ void __launch_bounds__(256) k_bin(uint32_t num_prims, const RdpPrimGe
 // grows the buffer to the count seen.
 constexpr int SPAN_THREADS = 256;
 
-__global__ void __launch_bounds__(SPAN_THREADS) k_span(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom,
+__global__ void __launch_bounds__(SPAN_THREADS, 6) k_span(uint32_t num_prims, const RdpPrimGeom *__restrict__ geom,
                                                       const RdpPrimAttr *__restrict__ attr,
                                                       const RdpPrimShade *__restrict__ shade,
                                                       const RdpPass *__restrict__ passes, SpanRow *__restrict__ spans,
@@ -1144,7 +1144,7 @@ __device__ bool tmem_lut(const RdpPass &ps, const RdpUpload &info, int tmem16_in
 // what value?  Written values land in snapshot u+1; unwritten words are marked in a bitmask.  One
 // CTA per upload of the launch (the launch's uploads are the TMEM passes' uploads, concatenated in
 // pass order); the CTA finds its pass by binary search over their first uploads.
-__global__ void k_tmem_apply(const RdpPass *__restrict__ passes, const uint32_t *__restrict__ pass_list,
+__global__ void __launch_bounds__(256, 8) k_tmem_apply(const RdpPass *__restrict__ passes, const uint32_t *__restrict__ pass_list,
                              uint32_t num_tmem_passes, const RdpUpload *__restrict__ uploads,
                              uint32_t *__restrict__ keep_bits)
 {

@@ -884,7 +884,7 @@ struct Executor
 		uint32_t num_descs = 0;
 		for (uint32_t i = 0; i < n; i++) num_descs += v[i].num_targets;
 		size_t o_pass = reserve(sizeof(RdpPass) * num_descs);
-		size_t o_list = reserve(4 * n);
+		size_t o_list = reserve(8 * n); // TMEM passes in launch order, then largest first
 		RdpPass *passes = reinterpret_cast<RdpPass *>(h + o_pass);
 		uint32_t *tmem_list = reinterpret_cast<uint32_t *>(h + o_list);
 		uint32_t num_tmem = 0;
@@ -948,6 +948,12 @@ struct Executor
 			up_base += v[i].num_uploads;
 		}
 
+		// The carry kernel takes the TMEM passes with the most uploads first (their CTAs run longest).
+		uint32_t *carry_list = tmem_list + n;
+		std::copy(tmem_list, tmem_list + num_tmem, carry_list);
+		std::stable_sort(carry_list, carry_list + num_tmem, [&](uint32_t a, uint32_t b) {
+			return passes[a].upload_count > passes[b].upload_count;
+		});
 		const int slot = staging_slot;
 		uint8_t *dst = d_staging + size_t(slot) * caps.staging;
 		if (cap)
@@ -980,6 +986,7 @@ struct Executor
 		L.shade = d_shade;
 		L.tilesets = reinterpret_cast<const RdpTile *>(dst + o_ts);
 		L.tmem_pass_list = reinterpret_cast<const uint32_t *>(dst + o_list);
+		L.tmem_carry_list = L.tmem_pass_list + n;
 		L.num_tmem_passes = num_tmem;
 		L.uploads = reinterpret_cast<const RdpUpload *>(dst + o_up);
 		L.num_uploads = up_base;

@@ -4411,7 +4411,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 			rdp::k_tmem_apply<<<L->num_uploads, 256, 0, stream>>>(L->passes, L->tmem_pass_list, L->num_tmem_passes,
 			                                                      L->uploads, L->tmem_keep);
 			rdp::k_tmem_carry<<<dim3(2048 / 32, L->num_tmem_passes), rdp::TMEM_CARRY_WARPS * 32, 0, stream>>>(
-				L->passes, L->tmem_pass_list, L->tmem_keep);
+				L->passes, L->tmem_carry_list, L->tmem_keep);
 		}
 		if (L->num_prims && L->num_tile_items)
 			rdp::k_raster_upscaled<<<std::min<uint32_t>(L->num_tile_items, L->blend_ctas), rdp::RASTER_THREADS, 0,
@@ -4436,7 +4436,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 			rdp::k_tmem_apply<<<L->num_uploads, 256, 0, stream>>>(L->passes, L->tmem_pass_list, L->num_tmem_passes,
 			                                                      L->uploads, L->tmem_keep);
 			rdp::k_tmem_carry<<<dim3(2048 / 32, L->num_tmem_passes), rdp::TMEM_CARRY_WARPS * 32, 0, stream>>>(
-				L->passes, L->tmem_pass_list, L->tmem_keep);
+				L->passes, L->tmem_carry_list, L->tmem_keep);
 		}
 		if (L->num_prims && L->num_tile_items)
 		{
@@ -4457,7 +4457,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		rdp::k_tmem_apply<<<L->num_uploads, 256, 0, L->side_stream>>>(L->passes, L->tmem_pass_list, L->num_tmem_passes,
 		                                                               L->uploads, L->tmem_keep);
 		rdp::k_tmem_carry<<<dim3(2048 / 32, L->num_tmem_passes), rdp::TMEM_CARRY_WARPS * 32, 0, L->side_stream>>>(
-			L->passes, L->tmem_pass_list, L->tmem_keep);
+			L->passes, L->tmem_carry_list, L->tmem_keep);
 		e = cudaEventRecord(L->join_event, L->side_stream);
 		if (e != cudaSuccess) return e;
 	}
@@ -4488,7 +4488,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		rdp::k_tmem_apply<<<L->num_uploads, 256, 0, stream>>>(L->passes, L->tmem_pass_list, L->num_tmem_passes,
 		                                                      L->uploads, L->tmem_keep);
 		rdp::k_tmem_carry<<<dim3(2048 / 32, L->num_tmem_passes), rdp::TMEM_CARRY_WARPS * 32, 0, stream>>>(
-			L->passes, L->tmem_pass_list, L->tmem_keep);
+			L->passes, L->tmem_carry_list, L->tmem_keep);
 	}
 	if (raster)
 	{

@@ -32,7 +32,8 @@ typedef struct RdpLaunch
 	RdpPrimAttr *attr;
 	RdpPrimShade *shade;
 	const RdpTile *tilesets;
-	const uint32_t *tmem_pass_list;
+	const uint32_t *tmem_pass_list;  /* descriptors of the passes with uploads, in launch order */
+	const uint32_t *tmem_carry_list; /* the same, most uploads first (k_tmem_carry's grid order) */
 	uint32_t num_tmem_passes;
 	const RdpUpload *uploads;
 	uint32_t num_uploads;     /* uploads of the launch (all TMEM passes' uploads, concatenated) */

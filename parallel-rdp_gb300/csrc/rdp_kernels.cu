@@ -4477,7 +4477,7 @@ extern "C" cudaError_t rdp_kernels_launch(const RdpLaunch *L, cudaStream_t strea
 		if (L->num_tile_items && L->spans)
 		{
 			const uint32_t chunk = std::min<uint32_t>(
-				std::max<uint32_t>(L->num_prims / (4u * std::max<uint32_t>(L->num_sms, 1u)), 1u), rdp::SPAN_THREADS);
+				std::max<uint32_t>(L->num_prims / (4u * std::max<uint32_t>(L->num_sms, 1u)), 1u), rdp::SPAN_THREADS / 2);
 			rdp::k_span<<<(L->num_prims + chunk - 1) / chunk, rdp::SPAN_THREADS, 0, stream>>>(
 				L->num_prims, L->geom, L->attr, L->shade, L->passes, static_cast<rdp::SpanRow *>(L->spans),
 				L->span_capacity, L->prim_rows, reinterpret_cast<unsigned long long *>(L->ctrl + 6), chunk);
